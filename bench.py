@@ -1,0 +1,381 @@
+"""KRR fit+predict benchmark on one GB300 (per-rank replicas when launched with N > 1).
+
+Workload (the "kernel and solve at scale" configuration): seeded synthetic molecules
+(QM7-like: n_atoms ~ U{5..23}, Z in {1,6,7,8,16}), sorted Coulomb matrix size 23
+(276 features, FP64), Gaussian kernel sigma = 1000, lambda = 1e-8, 20000 training
+and 5000 test molecules.  One step is one KRR fit + predict over molecules already
+in HBM:
+    CM of 25000 molecules -> K = k(X, X) (20000^2, symmetric) -> alpha = solve(K + lambda I, y)
+    -> yhat = k(Xs, X) alpha (fused, Ks not materialised)
+with the solve in the mixed mode (emulated-FP64 tensor-core factor + double-double
+refinement).  The plain FP64 path is timed once beside it.
+
+Prints ONE JSON line (rank 0).  ``--impl reference`` times the CPU path instead:
+the oracle's C/OpenMP restatement of the reference's Fortran routines plus SciPy
+LAPACK dpotrf/dpotrs (the routines the reference calls) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "KRR fit+predict s & p99 query latency: mixed vs FP64 on GB300 at 1e-8 rel err"
+UNIT = "s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--ntrain", type=int, default=20000)
+    p.add_argument("--ntest", type=int, default=5000)
+    p.add_argument("--sigma", type=float, default=1000.0)
+    p.add_argument("--lam", type=float, default=1e-8)
+    p.add_argument("--kernel", default="gaussian", choices=["gaussian", "laplacian"])
+    p.add_argument("--seed", type=int, default=2024)
+    p.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison")
+    p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    return p.parse_args()
+
+
+def workload_config(a):
+    return {"workload": "krr-cm276-%s-fit%d-predict%d" % (a.kernel, a.ntrain, a.ntest),
+            "n_train": a.ntrain, "n_test": a.ntest, "features": 276, "cm_size": 23,
+            "kernel": a.kernel, "sigma": a.sigma, "lambda": a.lam, "solve": "mixed",
+            "molecules": "synthetic QM7-like, seed %d" % a.seed,
+            "l2": "inputs larger than L2 (K is %.1f GB)" % (8.0 * a.ntrain ** 2 / 1e9),
+            "parallelism": "replicas"}
+
+
+# ----------------------------------------------------------------- CPU leg --
+
+def cpu_pipeline_sample(batch, a, sample=8):
+    """The reference's CPU path on a bounded sample of the workload, scaled to one
+    full fit+predict: all Coulomb matrices; 1/sample of the rows of the training and
+    test kernel matrices (scaled by sample); LAPACK dpotrf + dpotrs on an N/2
+    sub-problem (scaled by 8, the N^3 ratio); the prediction GEMV on the sampled
+    rows (scaled by sample)."""
+    import numpy as np
+    from scipy.linalg import lapack
+
+    from oracle import oracle
+    ntr, nte = a.ntrain, a.ntest
+    kfn = oracle.gaussian_kernel if a.kernel == "gaussian" else oracle.laplacian_kernel
+    t = {}
+    t0 = time.perf_counter()
+    X = oracle.cm_sorted_batch(batch.charges, batch.coordinates, batch.offsets, 23)
+    t["cm"] = time.perf_counter() - t0
+    Xtr, Xte = X[:ntr], X[ntr:ntr + nte]
+    rows = max(1, ntr // sample)
+    t0 = time.perf_counter()
+    Kpart = kfn(Xtr, Xtr[:rows], a.sigma)
+    t["kernel_train"] = (time.perf_counter() - t0) * (ntr / rows)
+    trows = max(1, nte // sample)
+    t0 = time.perf_counter()
+    Ks = kfn(Xtr, Xte[:trows], a.sigma)
+    t["kernel_test"] = (time.perf_counter() - t0) * (nte / trows)
+    nh = ntr // 2
+    Kh = kfn(Xtr[:nh], Xtr[:nh], a.sigma)
+    Kh[np.diag_indices_from(Kh)] += a.lam
+    t0 = time.perf_counter()
+    c, info = lapack.dpotrf(Kh, lower=0, overwrite_a=1, clean=0)
+    x, _ = lapack.dpotrs(c, batch.labels[:nh], lower=0)
+    t["cholesky"] = (time.perf_counter() - t0) * (ntr / nh) ** 3
+    alpha = np.random.default_rng(0).normal(size=ntr)
+    t0 = time.perf_counter()
+    _ = Ks.T @ alpha
+    t["predict"] = (time.perf_counter() - t0) * (nte / trows)
+    del Kpart
+    total = sum(t.values())
+    return total, t
+
+
+def cpu_sample_text(a):
+    return ("all %d CMs; 1/8 of the rows of K_train (%dx%d) and K_test (%dx%d), scaled x8; "
+            "dpotrf+dpotrs at N=%d scaled x8 (N^3); predict GEMV on the sampled rows x8"
+            % (a.ntrain + a.ntest, a.ntrain, a.ntrain, a.ntrain, a.ntest, a.ntrain // 2))
+
+
+def run_reference(a):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from qml_gb300.synthetic import generate_molecules
+    batch = generate_molecules(a.ntrain + a.ntest, seed=a.seed)
+    for _ in range(a.warmup):
+        cpu_pipeline_sample(batch, a)
+    times = []
+    for _ in range(a.steps):
+        total, parts = cpu_pipeline_sample(batch, a)
+        times.append(total)
+    v = statistics.mean(times)
+    cores = os.cpu_count()
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": workload_config(a), "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": cpu_sample_text(a)},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "stages_s": parts}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ----------------------------------------------------------------- GPU leg --
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if p[5 + k].lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def run_ours(a):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    from qml_gb300 import core
+    from qml_gb300.krr import KRR, molecules_to_device
+    from qml_gb300.synthetic import generate_molecules
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=dev)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    ntr, nte = a.ntrain, a.ntest
+    batch = generate_molecules(ntr + nte, seed=a.seed + rank)
+    z, r, off = molecules_to_device(batch, device=dev)
+    y = torch.from_numpy(batch.labels).to(dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step(precision="mixed"):
+        X = core.coulomb_matrix_batch(z, r, off, 23)
+        model = KRR(kernel=a.kernel, sigma=a.sigma, lam=a.lam, precision=precision)
+        model.fit(X[:ntr], y[:ntr])
+        return model.predict(X[ntr:ntr + nte]), model
+
+    for _ in range(a.warmup):
+        step()
+    barrier()
+    with ClockSampler(local) as clocks:
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(a.steps):
+            yhat, model = step()
+        ev1.record(stream)
+        barrier()
+    ms = ev0.elapsed_time(ev1) / a.steps
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    report = model.report
+
+    # end to end through the public API with host buffers (pinned), copies inside
+    hz = torch.from_numpy(batch.charges).pin_memory()
+    hr = torch.from_numpy(batch.coordinates).pin_memory()
+    ho = torch.from_numpy(batch.offsets).pin_memory()
+    hy = torch.from_numpy(batch.labels[:ntr].copy()).pin_memory()
+    hout = torch.empty(nte, dtype=torch.float64).pin_memory()
+    h2d = hz.numel() * 8 + hr.numel() * 8 + ho.numel() * 8 + hy.numel() * 8
+    d2h = nte * 8
+
+    def e2e_step():
+        dz, dr, do, dy = (t.to(dev, non_blocking=True) for t in (hz, hr, ho, hy))
+        X = core.coulomb_matrix_batch(dz, dr, do, 23)
+        m = KRR(kernel=a.kernel, sigma=a.sigma, lam=a.lam, precision="mixed").fit(X[:ntr], dy)
+        hout.copy_(m.predict(X[ntr:ntr + nte]), non_blocking=True)
+
+    e2e_step()
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(a.steps):
+        e2e_step()
+    e1.record(stream)
+    barrier()
+    e2e_s = e0.elapsed_time(e1) / a.steps / 1e3
+
+    # per-stage times of one step (events between stages) and the dominant kernel
+    stages = {}
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+    evs[0].record(stream)
+    X = core.coulomb_matrix_batch(z, r, off, 23)
+    evs[1].record(stream)
+    K = core.kernel_matrix(a.kernel, X[:ntr], X[:ntr], a.sigma, symmetric=True)
+    evs[2].record(stream)
+    alpha, rep = core.solve(K, y[:ntr], a.lam, precision="mixed")
+    evs[3].record(stream)
+    core.predict(a.kernel, X[:ntr], X[ntr:ntr + nte], a.sigma, alpha)
+    evs[4].record(stream)
+    torch.cuda.synchronize()
+    for k, name in enumerate(["cm", "kernel_train", "solve", "predict"]):
+        stages[name] = evs[k].elapsed_time(evs[k + 1]) / 1e3
+    # kernel matrix alone, several launches, for the roofline line
+    kev0 = torch.cuda.Event(enable_timing=True)
+    kev1 = torch.cuda.Event(enable_timing=True)
+    nk = 3
+    kev0.record(stream)
+    for _ in range(nk):
+        core.kernel_matrix(a.kernel, X[:ntr], X[:ntr], a.sigma, symmetric=True, out=K)
+    kev1.record(stream)
+    torch.cuda.synchronize()
+    k_s = kev0.elapsed_time(kev1) / nk / 1e3
+
+    # accuracy: mixed alpha vs FP64 + double-double refinement on the same K
+    fp64 = {}
+    K = core.kernel_matrix(a.kernel, X[:ntr], X[:ntr], a.sigma, symmetric=True)
+    Kc = K.clone()
+    alpha_m, rep_m = core.solve(K, y[:ntr], a.lam, precision="mixed")
+    if not a.no_fp64:
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        yf, mf = step("fp64")
+        f1.record(stream)
+        torch.cuda.synchronize()
+        fp64["fit_predict_s"] = f0.elapsed_time(f1) / 1e3
+        alpha_f, rep_f = core.solve(Kc, y[:ntr], a.lam, precision="fp64", max_outer=10, tol=1e-16)
+        fp64["alpha_rel_err_mixed_vs_fp64_refined"] = float(
+            torch.linalg.norm(alpha_m - alpha_f) / torch.linalg.norm(alpha_f))
+        fp64["speedup_mixed_vs_fp64"] = fp64["fit_predict_s"] / (ms / 1e3)
+        fp64["fp64_report"] = rep_f
+    del K, Kc
+
+    # our kernel launches in one step (CUDA activity of libqmlg kernels)
+    launches = None
+    try:
+        from torch.profiler import ProfilerActivity, profile
+        with profile(activities=[ProfilerActivity.CUDA]) as prof:
+            step()
+            torch.cuda.synchronize()
+        names = [e.name for e in prof.events() if e.device_type.name == "CUDA"]
+        launches = sum(1 for nme in names if "_kernel" in nme) * a.steps
+    except Exception:  # pragma: no cover - profiler unavailable
+        launches = None
+
+    if rank != 0:
+        return 0
+    # roofline of the training kernel matrix: FP64 SIMT work, reported against the
+    # tensor peak it would reach on the tensor cores; algorithmic
+    # flops = N(N+1)/2 pairs x 2 x 276 (symmetric contraction)
+    import json as _json
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = _json.load(f)
+    except OSError:
+        pass
+    flops = ntr * (ntr + 1) / 2 * 2 * 276
+    achieved = flops / k_s / 1e12
+    peak = peaks.get("bf16_tflops", 1900.0)
+    roofline = {"kernel": "kernel_matrix (%s, symmetric %d^2)" % (a.kernel, ntr),
+                "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": None,
+                "peak_source": "measured" if peaks else "fallback",
+                "launch_s": k_s}
+    cpu = None
+    if not a.no_cpu:
+        total, parts = cpu_pipeline_sample(batch, a)
+        cpu = {"value": total, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+               "sample": cpu_sample_text(a), "stages_s": parts}
+    line = {"metric": METRIC, "value": ms / 1e3 if world == 1 else ms / 1e3, "unit": UNIT,
+            "n_gpus": world, "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": workload_config(a),
+            "e2e": {"value": e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "fits_per_s": world / (ms / 1e3),
+            "gpu_launches": launches, "clocks": clocks.summary(), "roofline": roofline,
+            "cpu_baseline": cpu, "stages_s": stages, "solve_report": rep_m,
+            "fp64_path": fp64}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        return run_reference(a)
+    return run_ours(a)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,187 @@
+/*
+ * qmlg: GB300-native (sm_103a) kernel-ridge-regression hot path for QML.
+ *
+ * C ABI of libqmlg.so.  Every entry point:
+ *   - takes DEVICE pointers owned by the caller (for example torch tensors) and a
+ *     cudaStream_t passed as void*; work is enqueued on that stream;
+ *   - allocates nothing: scratch comes from a caller workspace whose size the
+ *     matching *_workspace_size() call returns;
+ *   - returns an int status: 0 = ok, > 0 = numerical information (for the
+ *     Cholesky, the 1-based order of the first non-positive leading minor, like
+ *     LAPACK's info), < 0 = argument or CUDA error (QMLG_E_* below).
+ *
+ * Matrices follow the reference's Fortran conventions: a kernel matrix K(na, nb)
+ * is column-major with leading dimension ldk (K[j + i*ldk] = k(A_j, B_i)), and a
+ * representation block A(na, d) is row-major with leading dimension lda (the
+ * d x na column-major array the Fortran routines receive).
+ */
+#ifndef QMLG_H
+#define QMLG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QMLG_OK 0
+#define QMLG_E_ARG (-1)        /* bad size, stride, pointer or flag */
+#define QMLG_E_CUDA (-2)       /* a CUDA launch or runtime call failed */
+#define QMLG_E_WORKSPACE (-3)  /* workspace missing or too small */
+#define QMLG_E_TOO_MANY_ATOMS (-4) /* a molecule has more atoms than size (or than 32) */
+#define QMLG_E_NOT_CONVERGED (-5)  /* refinement did not reach its tolerance */
+#define QMLG_E_TIMEOUT (-6)    /* a bounded device-side wait gave up */
+
+/* ---- library ---------------------------------------------------------- */
+
+/* Version string and the compute capability the library was built for. */
+const char *qmlg_version(void);
+
+/* Last CUDA error string seen by the library on this host thread ("" if none). */
+const char *qmlg_last_error(void);
+
+/* ---- sorted Coulomb matrix --------------------------------------------- */
+
+/*
+ * Row-norm sorted Coulomb matrix of a ragged batch of molecules.
+ * Replaces fgenerate_coulomb_matrix (qml/frepresentations.f90:52-140), bound by
+ * qml.representations.generate_coulomb_matrix (qml/representations.py:69-111),
+ * which handles one molecule per call.
+ *   charges      [total_atoms]      nuclear charges (FP64, like f2py's cast)
+ *   coordinates  [total_atoms * 3]  x, y, z per atom
+ *   atom_offsets [n_mol + 1]        molecule m owns atoms offsets[m] .. offsets[m+1]-1
+ *   out          [n_mol * size*(size+1)/2]  packed lower triangle per molecule
+ *   sorting      1 = row-norm sorted (the reference's "row-norm"),
+ *                0 = input order ("unsorted", frepresentations.f90:142-205)
+ *   status       [1] device int, set to QMLG_E_TOO_MANY_ATOMS if any molecule
+ *                has more than size (or 32) atoms; may be NULL
+ * The permutation and every value match the reference arithmetic bit for bit
+ * (no FMA contraction; Z^2.4 from a host table for integer charges 0..127).
+ */
+int qmlg_coulomb_matrix(const double *charges, const double *coordinates,
+                        const int64_t *atom_offsets, int n_mol, int size, int sorting,
+                        double *out, int *status, void *stream);
+
+/* ---- kernel matrices ----------------------------------------------------- */
+
+#define QMLG_KERNEL_SYMMETRIC 1   /* A == B: compute one triangle, mirror it */
+
+/*
+ * Gaussian kernel K(na, nb), K[j + i*ldk] = exp(-0.5/sigma^2 * |A_j - B_i|^2).
+ * Replaces fgaussian_kernel (qml/fkernels.f90:340-372), bound by
+ * qml.kernels.gaussian_kernel (qml/kernels.py:65-92).  FP64 arithmetic.
+ * flags: QMLG_KERNEL_SYMMETRIC requires A == B and na == nb.
+ * diag_shift is added to K[j + j*ldk] in symmetric mode (the KRR lambda); pass 0
+ * for the reference's behaviour.
+ */
+int qmlg_gaussian_kernel(const double *A, int64_t lda, int na, const double *B, int64_t ldb,
+                         int nb, int d, double sigma, double *K, int64_t ldk, int flags,
+                         double diag_shift, void *stream);
+
+/*
+ * Laplacian kernel K(na, nb), K[j + i*ldk] = exp(-1/sigma * |A_j - B_i|_1).
+ * Replaces flaplacian_kernel (qml/fkernels.f90:374-400), bound by
+ * qml.kernels.laplacian_kernel (qml/kernels.py:36-63).  FP64 arithmetic.
+ */
+int qmlg_laplacian_kernel(const double *A, int64_t lda, int na, const double *B, int64_t ldb,
+                          int nb, int d, double sigma, double *K, int64_t ldk, int flags,
+                          double diag_shift, void *stream);
+
+/* ---- prediction ----------------------------------------------------------- */
+
+#define QMLG_KIND_GAUSSIAN 0
+#define QMLG_KIND_LAPLACIAN 1
+
+/*
+ * yhat[i] = sum_j Ks[j + i*ldk] * alpha[j] for a materialised prediction kernel
+ * Ks(ntrain, ntest): the np.dot(Ks.T, alpha) of tests/test_energy_krr_cmat.py:109.
+ */
+int qmlg_predict_gemv(const double *Ks, int64_t ldk, int ntrain, int ntest,
+                      const double *alpha, double *yhat, void *stream);
+
+/*
+ * Fused prediction: yhat[i] = sum_j k(Xtrain_j, Xtest_i) * alpha[j] without
+ * materialising Ks.  Partial sums per training tile go to the workspace and are
+ * reduced in a fixed order, so the result is deterministic.
+ */
+size_t qmlg_predict_workspace_size(int ntrain, int ntest);
+int qmlg_predict_fused(int kind, const double *Xtrain, int64_t ldtrain, int ntrain,
+                       const double *Xtest, int64_t ldtest, int ntest, int d, double sigma,
+                       const double *alpha, double *yhat, void *workspace, size_t ws_bytes,
+                       void *stream);
+
+/* ---- Cholesky solve ------------------------------------------------------- */
+
+#define QMLG_PREC_FP64 0   /* plain FP64 blocked Cholesky (LAPACK dpotrf semantics) */
+#define QMLG_PREC_MIXED 1  /* FP32 factor of a shifted copy + FP64 GMRES refinement */
+
+typedef struct QmlgSolveReport {
+    int precision_used;     /* QMLG_PREC_* of the factor the answer came from */
+    int info;               /* Cholesky info of that factor (0 = ok) */
+    int outer_iterations;   /* refinement steps taken */
+    int inner_iterations;   /* total GMRES iterations */
+    int fell_back;          /* 1 if the mixed path gave up and refactorised in FP64 */
+    double shift;           /* diagonal shift used for the low-precision factor */
+    double backward_error;  /* |r|_2 / (|A|_F |x|_2 + |y|_2) of the returned x */
+    double last_correction; /* |dx|_2 / |x|_2 of the last refinement step */
+} QmlgSolveReport;
+
+typedef struct QmlgRefineOpts {
+    int max_outer;          /* refinement steps (default 10) */
+    int max_inner;          /* GMRES iterations per step (default 50) */
+    double tol;             /* stop when |dx|/|x| <= tol (default 1e-14) */
+    double shift;           /* FP32 factor shift; <= 0 picks one from the matrix */
+    int allow_fallback;     /* refactorise in FP64 when refinement stalls (default 1) */
+} QmlgRefineOpts;
+
+/*
+ * Cholesky factor in place, LAPACK dpotrf("U") semantics on a column-major
+ * n x n matrix A (leading dimension lda): the upper triangle is overwritten with
+ * U (A = U^T U), the strictly lower triangle is left untouched.  lambda is added
+ * to the diagonal before factorising (0 for the reference).  Returns info > 0
+ * on a non-positive leading minor.  Replaces the dpotrf call of fcho_solve
+ * (qml/fcho_solve.f90:35).  ws: qmlg_cholesky_workspace_size(n).
+ */
+size_t qmlg_cholesky_workspace_size(int n);
+int qmlg_cholesky(double *A, int n, int64_t lda, double lambda, void *workspace,
+                  size_t ws_bytes, void *stream);
+
+/*
+ * x = (U^T U)^{-1} y with U from qmlg_cholesky: dpotrs("U", nrhs=1)
+ * (qml/fcho_solve.f90:46).  x and y may alias.
+ */
+int qmlg_cholesky_solve_factored(const double *U, int n, int64_t lda, const double *y,
+                                 double *x, void *stream);
+
+/*
+ * Full solve (A + lambda I) x = y, the fcho_solve of qml/fcho_solve.f90:23-52 with
+ * the KRR lambda folded in.  precision QMLG_PREC_FP64 factorises A in place like
+ * the reference (upper triangle overwritten); QMLG_PREC_MIXED leaves A intact,
+ * factorises a shifted FP32 copy in the workspace, and refines in FP64 with
+ * GMRES on a double-double residual, falling back to an FP64 factorisation when
+ * refinement stalls (opts->allow_fallback; then A's upper triangle is
+ * overwritten as in FP64 mode).  opts and report may be NULL.
+ * The call synchronises the stream (refinement decisions are taken on the host).
+ */
+size_t qmlg_solve_workspace_size(int n, int precision);
+int qmlg_solve(double *A, int n, int64_t lda, const double *y, double *x, double lambda,
+               int precision, const QmlgRefineOpts *opts, QmlgSolveReport *report,
+               void *workspace, size_t ws_bytes, void *stream);
+
+/*
+ * r = y - (A + lambda I) x with every product and sum carried in double-double,
+ * using A's strictly lower triangle (column-major, untouched by the factorisation)
+ * and the diagonal vector diag (the diagonal of A before factorising).
+ * ws: qmlg_residual_workspace_size(n).
+ */
+size_t qmlg_residual_workspace_size(int n);
+int qmlg_residual_dd(const double *A, int n, int64_t lda, const double *diag, double lambda,
+                     const double *x, const double *y, double *r, void *workspace,
+                     size_t ws_bytes, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QMLG_H */

@@ -1,0 +1,211 @@
+"""CPU oracle for the KRR hot path (test infrastructure, never the product).
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` import this module, and only as the checker.  It restates the
+reference's algorithms:
+
+* ``cm_sorted`` / ``cm_unsorted``: ``qml/frepresentations.f90:52-140`` and
+  ``:142-205`` (C restatement in ``qmlg_oracle.c``; ``cm_sorted_numpy`` is an
+  independent NumPy restatement used to cross-check the C one);
+* ``gaussian_kernel`` / ``laplacian_kernel``: ``qml/fkernels.f90:340-400`` (C, OpenMP);
+* ``cho_solve``: ``qml/fcho_solve.f90:23-52`` + ``qml/math.py:60-97``, i.e. LAPACK
+  ``dpotrf("U")`` + ``dpotrs("U")``.  LAPACK is third party and not vendored; the
+  reference links whatever system LAPACK/MKL is present (no pinned version), here
+  the routines come from SciPy's bundled OpenBLAS;
+* ``refined_solve``: FP64 Cholesky plus iterative refinement whose residual is
+  carried in double-double, giving the solution of (K + lambda I) x = y for the
+  given FP64 K to far below FP64 LAPACK's forward error.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_BUILD = os.path.join(_HERE, "_build")
+_LIB_PATH = os.path.join(_BUILD, "libqmlg_oracle.so")
+_lib = None
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_i64p = ctypes.POINTER(ctypes.c_int64)
+
+
+def build(force: bool = False) -> str:
+    """Compile the C restatement (gcc, OpenMP, no FMA contraction)."""
+    src = os.path.join(_HERE, "qmlg_oracle.c")
+    if (not force and os.path.exists(_LIB_PATH)
+            and os.path.getmtime(_LIB_PATH) >= os.path.getmtime(src)):
+        return _LIB_PATH
+    os.makedirs(_BUILD, exist_ok=True)
+    tmp = _LIB_PATH + ".tmp%d" % os.getpid()
+    cmd = ["gcc", "-O3", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
+           src, "-o", tmp, "-lm"]
+    subprocess.check_call(cmd)
+    os.replace(tmp, _LIB_PATH)
+    return _LIB_PATH
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        lib = ctypes.CDLL(build())
+        lib.oracle_cm_sorted.argtypes = [_dp, _dp, ctypes.c_int, ctypes.c_int, _dp]
+        lib.oracle_cm_sorted.restype = ctypes.c_int
+        lib.oracle_cm_unsorted.argtypes = [_dp, _dp, ctypes.c_int, ctypes.c_int, _dp]
+        lib.oracle_cm_unsorted.restype = ctypes.c_int
+        lib.oracle_cm_sorted_batch.argtypes = [_dp, _dp, _i64p, ctypes.c_int, ctypes.c_int, _dp]
+        lib.oracle_cm_sorted_batch.restype = ctypes.c_int
+        for name in ("oracle_gaussian_kernel", "oracle_laplacian_kernel"):
+            fn = getattr(lib, name)
+            fn.argtypes = [_dp, ctypes.c_int, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_double, _dp]
+            fn.restype = None
+        lib.oracle_residual_dd.argtypes = [_dp, ctypes.c_int, ctypes.c_int64, ctypes.c_double,
+                                           _dp, _dp, _dp]
+        lib.oracle_residual_dd.restype = None
+        _lib = lib
+    return _lib
+
+
+def _ptr(a, ctype=_dp):
+    return a.ctypes.data_as(ctype)
+
+
+def cm_sorted(charges, coordinates, size=23):
+    """One molecule's row-norm sorted Coulomb matrix, shape (size*(size+1)//2,)."""
+    z = np.ascontiguousarray(charges, dtype=np.float64)
+    r = np.ascontiguousarray(coordinates, dtype=np.float64)
+    out = np.empty(size * (size + 1) // 2)
+    if _load().oracle_cm_sorted(_ptr(z), _ptr(r), z.shape[0], size, _ptr(out)) != 0:
+        raise ValueError("natoms > size")
+    return out
+
+
+def cm_unsorted(charges, coordinates, size=23):
+    z = np.ascontiguousarray(charges, dtype=np.float64)
+    r = np.ascontiguousarray(coordinates, dtype=np.float64)
+    out = np.empty(size * (size + 1) // 2)
+    if _load().oracle_cm_unsorted(_ptr(z), _ptr(r), z.shape[0], size, _ptr(out)) != 0:
+        raise ValueError("natoms > size")
+    return out
+
+
+def cm_sorted_batch(charges, coordinates, offsets, size=23):
+    z = np.ascontiguousarray(charges, dtype=np.float64)
+    r = np.ascontiguousarray(coordinates, dtype=np.float64)
+    off = np.ascontiguousarray(offsets, dtype=np.int64)
+    n_mol = off.shape[0] - 1
+    out = np.empty((n_mol, size * (size + 1) // 2))
+    if _load().oracle_cm_sorted_batch(_ptr(z), _ptr(r), _ptr(off, _i64p), n_mol, size,
+                                      _ptr(out)) != 0:
+        raise ValueError("a molecule has more atoms than size")
+    return out
+
+
+def cm_sorted_numpy(charges, coordinates, size=23):
+    """Independent NumPy restatement of frepresentations.f90:52-140 (same order of
+    operations as the C one, used to cross-check it)."""
+    z = np.asarray(charges, dtype=np.float64)
+    r = np.asarray(coordinates, dtype=np.float64)
+    n = z.shape[0]
+    m = np.zeros((n, n))
+    for i in range(n):
+        m[i, i] = 0.5 * z[i] ** 2.4
+        for j in range(i + 1, n):
+            d = r[j] - r[i]
+            s = d[0] * d[0]
+            s = s + d[1] * d[1]
+            s = s + d[2] * d[2]
+            m[i, j] = m[j, i] = (z[i] * z[j]) / np.sqrt(s)
+    rn = np.empty(n)
+    for i in range(n):
+        acc = m[i, i] * m[i, i]
+        for j in range(n):
+            if j != i:
+                acc = acc + m[i, j] * m[i, j]
+        rn[i] = acc
+    order = np.empty(n, dtype=np.int64)
+    for k in range(n):
+        best = int(np.argmin(rn))          # first index of the minimum, like minloc
+        order[n - 1 - k] = best
+        rn[best] = np.finfo(np.float64).max
+    out = np.zeros(size * (size + 1) // 2)
+    for a in range(n):
+        base = a * (a + 1) // 2
+        for b in range(a + 1):
+            out[base + b] = m[order[a], order[b]]
+    return out
+
+
+def gaussian_kernel(A, B, sigma):
+    """K (na, nb) in Fortran order, like qml.kernels.gaussian_kernel."""
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    B = np.ascontiguousarray(B, dtype=np.float64)
+    K = np.empty((A.shape[0], B.shape[0]), order="F")
+    _load().oracle_gaussian_kernel(_ptr(A), A.shape[0], _ptr(B), B.shape[0], A.shape[1],
+                                   float(sigma), _ptr(K))
+    return K
+
+
+def laplacian_kernel(A, B, sigma):
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    B = np.ascontiguousarray(B, dtype=np.float64)
+    K = np.empty((A.shape[0], B.shape[0]), order="F")
+    _load().oracle_laplacian_kernel(_ptr(A), A.shape[0], _ptr(B), B.shape[0], A.shape[1],
+                                    float(sigma), _ptr(K))
+    return K
+
+
+def cho_solve(A, y):
+    """LAPACK dpotrf("U") + dpotrs("U") on a copy of A (qml/fcho_solve.f90:23-52)."""
+    from scipy.linalg import lapack
+    a = np.array(A, dtype=np.float64, order="F", copy=True)
+    c, info = lapack.dpotrf(a, lower=0, overwrite_a=1, clean=0)
+    if info != 0:
+        raise np.linalg.LinAlgError("dpotrf info=%d" % info)
+    x, info = lapack.dpotrs(c, np.asarray(y, dtype=np.float64), lower=0)
+    return x
+
+
+def residual_dd(A, lam, x, y):
+    """y - (A + lam I) x with double-double accumulation, rounded to FP64."""
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    if not A.flags.c_contiguous:
+        A = np.ascontiguousarray(A)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    r = np.empty_like(x)
+    _load().oracle_residual_dd(_ptr(A), A.shape[0], A.strides[0] // 8, float(lam), _ptr(x),
+                               _ptr(y), _ptr(r))
+    return r
+
+
+def refined_solve(K, y, lam, iters=30, tol=1e-18):
+    """Solution of (K + lam I) x = y for the FP64 matrix K, refined with a
+    double-double residual until the correction stops shrinking."""
+    from scipy.linalg import lapack
+    K = np.ascontiguousarray(K, dtype=np.float64)
+    n = K.shape[0]
+    a = np.array(K, order="F", copy=True)
+    a[np.diag_indices(n)] += lam
+    c, info = lapack.dpotrf(a, lower=0, overwrite_a=1, clean=0)
+    if info != 0:
+        raise np.linalg.LinAlgError("dpotrf info=%d" % info)
+    x, _ = lapack.dpotrs(c, y, lower=0)
+    prev = np.inf
+    for _ in range(iters):
+        r = residual_dd(K, lam, x, y)
+        d, _ = lapack.dpotrs(c, r, lower=0)
+        x = x + d
+        rel = np.linalg.norm(d) / max(np.linalg.norm(x), 1e-300)
+        if rel < tol or rel >= prev:
+            break
+        prev = rel
+    return x
+
+
+if __name__ == "__main__":  # pragma: no cover
+    print(build(force="--force" in sys.argv))

@@ -1,0 +1,259 @@
+"""Device-tensor API over the C ABI (torch tensors in HBM, work on the current stream).
+
+Every function here calls libqmlg.so; torch only provides device memory, streams
+and the workspace buffers that the C ABI asks for (the library itself allocates
+nothing).
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Optional, Tuple
+
+import torch
+
+from . import _lib
+from ._lib import QmlgRefineOpts, QmlgSolveReport, check
+
+_SORTING = {"row-norm": 1, "unsorted": 0}
+_KINDS = {"gaussian": _lib.QMLG_KIND_GAUSSIAN, "laplacian": _lib.QMLG_KIND_LAPLACIAN}
+_PRECISIONS = {"fp64": _lib.QMLG_PREC_FP64, "mixed": _lib.QMLG_PREC_MIXED}
+
+
+def lib():
+    return _lib.load()
+
+
+def _stream(device=None) -> int:
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+def _require_cuda(*tensors):
+    for t in tensors:
+        if not isinstance(t, torch.Tensor) or not t.is_cuda:
+            raise TypeError("expected CUDA tensors")
+        if t.dtype not in (torch.float64, torch.int64, torch.int32, torch.uint8):
+            raise TypeError("unexpected dtype %s" % t.dtype)
+
+
+class _WorkspaceCache:
+    """One growing scratch buffer per device, reused across calls on that device."""
+
+    def __init__(self):
+        self._buf = {}
+
+    def get(self, nbytes: int, device) -> torch.Tensor:
+        dev = torch.device(device)
+        key = dev.index if dev.index is not None else torch.cuda.current_device()
+        buf = self._buf.get(key)
+        if buf is None or buf.numel() < nbytes:
+            buf = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=dev)
+            self._buf[key] = buf
+        return buf
+
+
+workspaces = _WorkspaceCache()
+
+
+# ------------------------------------------------------------ Coulomb matrix --
+
+def coulomb_matrix_batch(charges: torch.Tensor, coordinates: torch.Tensor,
+                         offsets: torch.Tensor, size: int = 23,
+                         sorting: str = "row-norm", out: Optional[torch.Tensor] = None
+                         ) -> torch.Tensor:
+    """Sorted (or unsorted) Coulomb matrices of a ragged batch of molecules.
+
+    charges (total_atoms,) float64, coordinates (total_atoms, 3) float64,
+    offsets (n_mol + 1,) int64 on the GPU -> (n_mol, size*(size+1)//2) float64.
+    """
+    if sorting not in _SORTING:
+        raise ValueError("Unknown sorting scheme requested: %r" % (sorting,))
+    _require_cuda(charges, coordinates, offsets)
+    charges = charges.contiguous()
+    coordinates = coordinates.contiguous()
+    offsets = offsets.to(torch.int64).contiguous()
+    n_mol = offsets.shape[0] - 1
+    length = size * (size + 1) // 2
+    if out is None:
+        out = torch.empty((n_mol, length), dtype=torch.float64, device=charges.device)
+    status = torch.zeros(1, dtype=torch.int32, device=charges.device)
+    check(lib().qmlg_coulomb_matrix(charges.data_ptr(), coordinates.data_ptr(),
+                                    offsets.data_ptr(), n_mol, size, _SORTING[sorting],
+                                    out.data_ptr(), status.data_ptr(), _stream(charges.device)),
+          "qmlg_coulomb_matrix")
+    st = int(status.item())
+    if st != 0:
+        _lib.check(st, "qmlg_coulomb_matrix")
+    return out
+
+
+# ------------------------------------------------------------ kernel matrices --
+
+def _rows(X: torch.Tensor) -> Tuple[torch.Tensor, int]:
+    if X.dim() != 2 or X.dtype != torch.float64:
+        raise ValueError("expected a 2-D float64 representation matrix")
+    if X.stride(1) != 1:
+        X = X.contiguous()
+    return X, max(X.stride(0), X.shape[1])
+
+
+def kernel_matrix(kind: str, A: torch.Tensor, B: torch.Tensor, sigma: float,
+                  symmetric: bool = False, diag_shift: float = 0.0,
+                  out: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """K (na, nb), Fortran-ordered like the reference, as a (na, nb) view of a
+    column-major buffer.  symmetric=True requires B is A."""
+    _require_cuda(A, B)
+    A, lda = _rows(A)
+    if symmetric:
+        B, ldb = A, lda
+    else:
+        B, ldb = _rows(B)
+    na, nb, d = A.shape[0], B.shape[0], A.shape[1]
+    if B.shape[1] != d:
+        raise ValueError("A and B have different representation sizes")
+    if out is None:
+        buf = torch.empty((nb, na), dtype=torch.float64, device=A.device)
+    else:
+        if out.shape != (na, nb) or out.stride() != (1, na):
+            raise ValueError("out must be a Fortran-ordered (na, nb) float64 tensor")
+        buf = out.T
+    fn = lib().qmlg_gaussian_kernel if kind == "gaussian" else lib().qmlg_laplacian_kernel
+    flags = _lib.QMLG_KERNEL_SYMMETRIC if symmetric else 0
+    check(fn(A.data_ptr(), lda, na, B.data_ptr(), ldb, nb, d, float(sigma), buf.data_ptr(), na,
+             flags, float(diag_shift), _stream(A.device)), "qmlg_%s_kernel" % kind)
+    return buf.T
+
+
+def gaussian_kernel(A, B, sigma, **kw):
+    return kernel_matrix("gaussian", A, B, sigma, **kw)
+
+
+def laplacian_kernel(A, B, sigma, **kw):
+    return kernel_matrix("laplacian", A, B, sigma, **kw)
+
+
+# ------------------------------------------------------------------ predict --
+
+def predict(kind: str, Xtrain: torch.Tensor, Xtest: torch.Tensor, sigma: float,
+            alpha: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """yhat = K(Xtest, Xtrain) alpha without materialising the kernel matrix."""
+    _require_cuda(Xtrain, Xtest, alpha)
+    Xtrain, ldtr = _rows(Xtrain)
+    Xtest, ldte = _rows(Xtest)
+    alpha = alpha.contiguous()
+    ntr, nte, d = Xtrain.shape[0], Xtest.shape[0], Xtrain.shape[1]
+    if out is None:
+        out = torch.empty(nte, dtype=torch.float64, device=Xtrain.device)
+    ws_bytes = lib().qmlg_predict_workspace_size(ntr, nte)
+    ws = workspaces.get(ws_bytes, Xtrain.device)
+    check(lib().qmlg_predict_fused(_KINDS[kind], Xtrain.data_ptr(), ldtr, ntr, Xtest.data_ptr(),
+                                   ldte, nte, d, float(sigma), alpha.data_ptr(), out.data_ptr(),
+                                   ws.data_ptr(), ws.numel(), _stream(Xtrain.device)),
+          "qmlg_predict_fused")
+    return out
+
+
+def predict_gemv(Ks: torch.Tensor, alpha: torch.Tensor) -> torch.Tensor:
+    """yhat = Ks^T alpha for a Fortran-ordered Ks (ntrain, ntest) (np.dot(Ks.T, alpha))."""
+    _require_cuda(Ks, alpha)
+    ntr, nte = Ks.shape
+    if Ks.stride(0) != 1:
+        Ks = Ks.T.contiguous().T
+    ldk = max(Ks.stride(1), ntr)
+    out = torch.empty(nte, dtype=torch.float64, device=Ks.device)
+    check(lib().qmlg_predict_gemv(Ks.data_ptr(), ldk, ntr, nte, alpha.contiguous().data_ptr(),
+                                  out.data_ptr(), _stream(Ks.device)), "qmlg_predict_gemv")
+    return out
+
+
+# -------------------------------------------------------------------- solve --
+
+def _colmajor(A: torch.Tensor) -> Tuple[torch.Tensor, int]:
+    """Pointer view of A as a column-major matrix: Fortran-ordered tensors are used
+    as they are; a C-ordered tensor is its own transpose in column-major terms
+    (identical for the symmetric matrices KRR solves)."""
+    if A.dim() != 2 or A.shape[0] != A.shape[1] or A.dtype != torch.float64:
+        raise ValueError("expected a square float64 matrix")
+    n = A.shape[0]
+    if A.stride(0) == 1 and A.stride(1) >= n:
+        return A, A.stride(1)
+    if A.stride(1) == 1 and A.stride(0) >= n:
+        return A, A.stride(0)
+    raise ValueError("A must be row- or column-contiguous")
+
+
+def solve(A: torch.Tensor, y: torch.Tensor, lam: float = 0.0, precision: str = "mixed",
+          max_outer: int = 10, tol: float = 1e-15, allow_fallback: bool = True,
+          raise_on_info: bool = True):
+    """Solve (A + lam I) x = y on the GPU.  Returns (x, report dict).
+
+    precision "fp64": blocked FP64 Cholesky in place (A's upper triangle in
+    column-major terms is overwritten, like dpotrf("U")), then dpotrs and, when
+    max_outer > 0, double-double refinement.  precision "mixed": the same factor
+    with its trailing updates emulated on the bf16 tensor cores, refined in FP64
+    with a double-double residual; falls back to the plain FP64 factor when the
+    refinement stalls.  The other triangle of A is never written.
+    """
+    _require_cuda(A, y)
+    if precision not in _PRECISIONS:
+        raise ValueError("precision must be 'fp64' or 'mixed'")
+    Acm, lda = _colmajor(A)
+    n = Acm.shape[0]
+    if y.shape != (n,):
+        raise ValueError("expected matrix and vector of same stride size")
+    y = y.contiguous()
+    x = torch.empty_like(y)
+    p = _PRECISIONS[precision]
+    ws_bytes = lib().qmlg_solve_workspace_size(n, p)
+    ws = workspaces.get(ws_bytes, A.device)
+    opts = QmlgRefineOpts(int(max_outer), 50, float(tol), 0.0, 1 if allow_fallback else 0)
+    rep = QmlgSolveReport()
+    st = lib().qmlg_solve(Acm.data_ptr(), n, lda, y.data_ptr(), x.data_ptr(), float(lam), p,
+                          ctypes.byref(opts), ctypes.byref(rep), ws.data_ptr(), ws.numel(),
+                          _stream(A.device))
+    if st < 0 and st != _lib.QMLG_E_NOT_CONVERGED:
+        check(st, "qmlg_solve")
+    report = rep.as_dict()
+    report["status"] = st
+    if st > 0 and raise_on_info:
+        raise torch.linalg.LinAlgError(
+            "the %d-th leading minor is not positive definite" % st)
+    return x, report
+
+
+def cholesky(A: torch.Tensor, lam: float = 0.0) -> int:
+    """In-place FP64 Cholesky with dpotrf("U") semantics; returns LAPACK's info."""
+    _require_cuda(A)
+    Acm, lda = _colmajor(A)
+    n = Acm.shape[0]
+    ws_bytes = lib().qmlg_cholesky_workspace_size(n)
+    ws = workspaces.get(ws_bytes, A.device)
+    return check(lib().qmlg_cholesky(Acm.data_ptr(), n, lda, float(lam), ws.data_ptr(),
+                                     ws.numel(), _stream(A.device)), "qmlg_cholesky")
+
+
+def cholesky_solve_factored(U: torch.Tensor, y: torch.Tensor) -> torch.Tensor:
+    """dpotrs("U", nrhs=1) with a factor from cholesky()."""
+    _require_cuda(U, y)
+    Ucm, lda = _colmajor(U)
+    n = Ucm.shape[0]
+    y = y.contiguous()
+    x = torch.empty_like(y)
+    check(lib().qmlg_cholesky_solve_factored(Ucm.data_ptr(), n, lda, y.data_ptr(), x.data_ptr(),
+                                             _stream(U.device)), "qmlg_cholesky_solve_factored")
+    return x
+
+
+def residual_dd(A: torch.Tensor, diag: torch.Tensor, lam: float, x: torch.Tensor,
+                y: torch.Tensor) -> torch.Tensor:
+    """y - (A + lam I) x in double-double, using A's untouched triangle and diag."""
+    _require_cuda(A, diag, x, y)
+    Acm, lda = _colmajor(A)
+    n = Acm.shape[0]
+    r = torch.empty_like(y)
+    ws_bytes = lib().qmlg_residual_workspace_size(n)
+    ws = workspaces.get(ws_bytes, A.device)
+    check(lib().qmlg_residual_dd(Acm.data_ptr(), n, lda, diag.contiguous().data_ptr(), float(lam),
+                                 x.contiguous().data_ptr(), y.contiguous().data_ptr(),
+                                 r.data_ptr(), ws.data_ptr(), ws.numel(), _stream(A.device)),
+          "qmlg_residual_dd")
+    return r

@@ -1,0 +1,723 @@
+// Blocked Cholesky factorisation, triangular solves, double-double residual and
+// the refinement driver behind qmlg_solve.
+//
+// Restates fcho_solve (qml/fcho_solve.f90:23-52): dpotrf("U") then dpotrs("U",
+// nrhs=1) on a column-major matrix.  Kernels work on the row-major view of the
+// same memory, R[i][j] = A[j + i*lda]: the column-major upper triangle that
+// dpotrf("U") factorises is R's lower triangle, so U (A = U^T U) is stored as
+// L = U^T in R's lower triangle and R's strictly upper triangle (the column-major
+// strictly lower one) keeps the original matrix, as LAPACK leaves it.
+//
+// Right-looking blocked algorithm, block NB = 64:
+//   potrf_diag   one CTA factorises the NB x NB diagonal block in shared memory
+//                (FP64), flagging the first non-positive pivot like LAPACK's info;
+//   trsm_panel   the panel below it: X <- X L_kk^-T, one CTA per 64 rows;
+//   syrk_update  the trailing lower triangle: C <- C - P P^T with 64 x 64 tiles.
+// After a failed pivot every later kernel sees the info flag and returns.
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+#include "emulated_gemm.cuh"
+
+namespace {
+
+constexpr int NB = 64;
+
+// ---------------------------------------------------------------- factor --
+
+__global__ void __launch_bounds__(256)
+potrf_diag_kernel(double *__restrict__ A, int64_t lda, int n, int k0, double shift,
+                  int *__restrict__ info)
+{
+    __shared__ double S[NB][NB + 1];
+    __shared__ int failed;
+    if (*info != 0) return;
+    const int tid = threadIdx.x;
+    const int nb = min(NB, n - k0);
+    for (int e = tid; e < NB * NB; e += blockDim.x) {
+        const int r = e / NB, c = e % NB;
+        double v = 0.0;
+        if (r < nb && c <= r) v = A[(int64_t)(k0 + r) * lda + (k0 + c)];
+        if (r == c && r < nb) v += shift;
+        S[r][c] = v;
+    }
+    if (tid == 0) failed = 0;
+    __syncthreads();
+    for (int c = 0; c < nb; ++c) {
+        if (tid == 0) {
+            const double p = S[c][c];
+            if (!(p > 0.0) || !isfinite(p)) {
+                failed = 1;
+                atomicCAS(info, 0, k0 + c + 1);
+            } else {
+                S[c][c] = sqrt(p);
+            }
+        }
+        __syncthreads();
+        if (failed) return;
+        const double dinv = 1.0 / S[c][c];
+        for (int r = c + 1 + tid; r < nb; r += blockDim.x) S[r][c] *= dinv;
+        __syncthreads();
+        // trailing update of the block's lower triangle
+        const int m = nb - c - 1;
+        for (int e = tid; e < m * m; e += blockDim.x) {
+            const int r = c + 1 + e / m, s = c + 1 + e % m;
+            if (s <= r) S[r][s] = fma(-S[r][c], S[s][c], S[r][s]);
+        }
+        __syncthreads();
+    }
+    for (int e = tid; e < nb * nb; e += blockDim.x) {
+        const int r = e / nb, c = e % nb;
+        if (c <= r) A[(int64_t)(k0 + r) * lda + (k0 + c)] = S[r][c];
+    }
+}
+
+// X <- X * L_kk^{-T} for the rows below the diagonal block.
+__global__ void __launch_bounds__(256)
+trsm_panel_kernel(double *__restrict__ A, int64_t lda, int n, int k0,
+                  const int *__restrict__ info)
+{
+    __shared__ double L[NB][NB + 1];
+    __shared__ double X[64][NB + 1];
+    if (*info != 0) return;
+    const int tid = threadIdx.x;
+    const int nb = min(NB, n - k0);
+    const int r0 = k0 + nb + blockIdx.x * 64;
+    const int rows = min(64, n - r0);
+    if (rows <= 0) return;
+    for (int e = tid; e < NB * NB; e += blockDim.x) {
+        const int r = e / NB, c = e % NB;
+        L[r][c] = (r < nb && c <= r) ? A[(int64_t)(k0 + r) * lda + (k0 + c)] : 0.0;
+    }
+    for (int e = tid; e < 64 * NB; e += blockDim.x) {
+        const int r = e / NB, c = e % NB;
+        X[r][c] = (r < rows && c < nb) ? A[(int64_t)(r0 + r) * lda + (k0 + c)] : 0.0;
+    }
+    __syncthreads();
+    for (int c = 0; c < nb; ++c) {
+        const double dinv = 1.0 / L[c][c];
+        if (tid < 64) X[tid][c] *= dinv;
+        __syncthreads();
+        const int m = nb - c - 1;
+        for (int e = tid; e < 64 * m; e += blockDim.x) {
+            const int r = e / m, s = c + 1 + e % m;
+            X[r][s] = fma(-X[r][c], L[s][c], X[r][s]);
+        }
+        __syncthreads();
+    }
+    for (int e = tid; e < rows * nb; e += blockDim.x) {
+        const int r = e / nb, c = e % nb;
+        A[(int64_t)(r0 + r) * lda + (k0 + c)] = X[r][c];
+    }
+}
+
+__device__ __forceinline__ void tri_index(int64_t t, int &bi, int &bj)
+{
+    int64_t r = (int64_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+    while (r * (r + 1) / 2 > t) --r;
+    while ((r + 1) * (r + 2) / 2 <= t) ++r;
+    bi = (int)r;
+    bj = (int)(t - r * (r + 1) / 2);
+}
+
+// C[i][j] -= sum_t P[i][t] P[j][t] over the trailing lower triangle, FP64.
+__global__ void __launch_bounds__(256)
+syrk_update_kernel(double *__restrict__ A, int64_t lda, int n, int k0,
+                   const int *__restrict__ info)
+{
+    __shared__ double Ps[16][64 + 1];
+    __shared__ double Qs[16][64 + 1];
+    if (*info != 0) return;
+    const int k1 = k0 + NB;
+    int bi, bj;
+    tri_index(blockIdx.x, bi, bj);
+    const int i0 = k1 + bi * 64, j0 = k1 + bj * 64;
+    const int tid = threadIdx.x;
+    const int tx = tid & 15, ty = tid >> 4;  // tx -> j (contiguous), ty -> i
+    double acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
+    for (int t0 = 0; t0 < NB; t0 += 16) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int e = tid + q * 256;
+            const int r = e >> 4, c = e & 15;
+            const int ri = i0 + r, rj = j0 + r;
+            Ps[c][r] = ri < n ? A[(int64_t)ri * lda + k0 + t0 + c] : 0.0;
+            Qs[c][r] = rj < n ? A[(int64_t)rj * lda + k0 + t0 + c] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+            double pv[4], qv[4];
+#pragma unroll
+            for (int b = 0; b < 4; ++b) pv[b] = Ps[c][ty + 16 * b];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) qv[a] = Qs[c][tx + 16 * a];
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int b = 0; b < 4; ++b) acc[a][b] = fma(pv[b], qv[a], acc[a][b]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+        const int i = i0 + ty + 16 * b;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const int j = j0 + tx + 16 * a;
+            if (i < n && j < n && j <= i) {
+                double *p = A + (int64_t)i * lda + j;
+                *p -= acc[a][b];
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------ triangular solves --
+
+// z[k0..k0+nb) <- L_kk^{-1} z[k0..k0+nb)   (forward, one CTA)
+__global__ void trsv_diag_fwd_kernel(const double *__restrict__ A, int64_t lda, int n, int k0,
+                                     double *__restrict__ z)
+{
+    __shared__ double L[NB][NB + 1];
+    __shared__ double v[NB];
+    const int tid = threadIdx.x;
+    const int nb = min(NB, n - k0);
+    for (int e = tid; e < NB * NB; e += blockDim.x) {
+        const int r = e / NB, c = e % NB;
+        L[r][c] = (r < nb && c <= r) ? A[(int64_t)(k0 + r) * lda + (k0 + c)] : 0.0;
+    }
+    if (tid < nb) v[tid] = z[k0 + tid];
+    __syncthreads();
+    for (int c = 0; c < nb; ++c) {
+        if (tid == 0) v[c] = v[c] / L[c][c];
+        __syncthreads();
+        if (tid > c && tid < nb) v[tid] = fma(-L[tid][c], v[c], v[tid]);
+        __syncthreads();
+    }
+    if (tid < nb) z[k0 + tid] = v[tid];
+}
+
+// z[r] -= sum_{t<nb} R[r][k0+t] z[k0+t] for r >= k0+nb   (a warp per row)
+__global__ void gemv_fwd_update_kernel(const double *__restrict__ A, int64_t lda, int n, int k0,
+                                       double *__restrict__ z)
+{
+    const int k1 = k0 + NB;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const int r = k1 + warp;
+    if (r >= n) return;
+    const double *row = A + (int64_t)r * lda + k0;
+    double s = fma(row[lane], z[k0 + lane], row[lane + 32] * z[k0 + lane + 32]);
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    if (lane == 0) z[r] -= s;
+}
+
+// x[k0..k0+nb) <- L_kk^{-T} x[k0..k0+nb)   (backward, one CTA)
+__global__ void trsv_diag_bwd_kernel(const double *__restrict__ A, int64_t lda, int n, int k0,
+                                     double *__restrict__ x)
+{
+    __shared__ double L[NB][NB + 1];
+    __shared__ double v[NB];
+    const int tid = threadIdx.x;
+    const int nb = min(NB, n - k0);
+    for (int e = tid; e < NB * NB; e += blockDim.x) {
+        const int r = e / NB, c = e % NB;
+        L[r][c] = (r < nb && c <= r) ? A[(int64_t)(k0 + r) * lda + (k0 + c)] : 0.0;
+    }
+    if (tid < nb) v[tid] = x[k0 + tid];
+    __syncthreads();
+    for (int c = nb - 1; c >= 0; --c) {
+        if (tid == 0) v[c] = v[c] / L[c][c];
+        __syncthreads();
+        if (tid < c) v[tid] = fma(-L[c][tid], v[c], v[tid]);
+        __syncthreads();
+    }
+    if (tid < nb) x[k0 + tid] = v[tid];
+}
+
+// x[t] -= sum_{r in block} R[r][t] x[r] for t < k0   (a thread per column t)
+__global__ void gemv_bwd_update_kernel(const double *__restrict__ A, int64_t lda, int n, int k0,
+                                       double *__restrict__ x)
+{
+    __shared__ double xs[NB];
+    const int nb = min(NB, n - k0);
+    if (threadIdx.x < nb) xs[threadIdx.x] = x[k0 + threadIdx.x];
+    __syncthreads();
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= k0) return;
+    double s = 0.0;
+    for (int r = 0; r < nb; ++r) s = fma(A[(int64_t)(k0 + r) * lda + t], xs[r], s);
+    x[t] -= s;
+}
+
+// ------------------------------------------------------------- residual --
+
+constexpr int RES_ROWS = 64;
+constexpr int RES_CHUNK = 1024;
+
+// Partial double-double row sums of the symmetric matrix held in R's strictly
+// upper triangle plus diag: one CTA per (64 rows, 1024 columns).  Dot2 of
+// Ogita, Rump and Oishi (TwoProduct + TwoSum), 4 threads per row.
+__global__ void __launch_bounds__(256)
+symv_dd_partial_kernel(const double *__restrict__ A, int64_t lda, int n,
+                       const double *__restrict__ diag, const double *__restrict__ x,
+                       double2 *__restrict__ partial)
+{
+    __shared__ double S[64][64 + 1];
+    __shared__ double xs[64];
+    const int tid = threadIdx.x;
+    const int i0 = blockIdx.x * RES_ROWS;
+    const int c0 = blockIdx.y * RES_CHUNK;
+    const int lr = tid >> 2, part = tid & 3;
+    double hi = 0.0, lo = 0.0;
+    for (int j0 = c0; j0 < min(n, c0 + RES_CHUNK); j0 += 64) {
+        __syncthreads();
+        // S[r][c] = A_sym(i0 + r, j0 + c)
+        for (int e = tid; e < 64 * 64; e += 256) {
+            const int r = e >> 6, c = e & 63;
+            const int i = i0 + r, j = j0 + c;
+            double v = 0.0;
+            if (i < n && j < n && j > i) v = A[(int64_t)i * lda + j];
+            if (i < n && j < n && j == i) v = diag[i];
+            S[r][c] = v;
+        }
+        for (int e = tid; e < 64 * 64; e += 256) {
+            // lower part from the transposed upper tile: R[j][i] for j < i
+            const int c = e >> 6, r = e & 63;
+            const int i = i0 + r, j = j0 + c;
+            if (i < n && j < n && j < i) S[r][c] = A[(int64_t)j * lda + i];
+        }
+        if (tid < 64) xs[tid] = (j0 + tid < n) ? x[j0 + tid] : 0.0;
+        __syncthreads();
+#pragma unroll 4
+        for (int c = part * 16; c < part * 16 + 16; ++c) {
+            const double a = S[lr][c], b = xs[c];
+            const double p = a * b;
+            const double pe = fma(a, b, -p);
+            double s, e;
+            qmlg_two_sum(hi, p, s, e);
+            hi = s;
+            lo += e + pe;
+        }
+    }
+    // combine the 4 parts of a row
+    for (int off = 1; off < 4; off <<= 1) {
+        const double oh = __shfl_xor_sync(0xffffffffu, hi, off);
+        const double ol = __shfl_xor_sync(0xffffffffu, lo, off);
+        qmlg_dd_add(hi, lo, oh, ol);
+    }
+    const int i = i0 + lr;
+    if (part == 0 && i < n) partial[(int64_t)blockIdx.y * n + i] = make_double2(hi, lo);
+}
+
+// r[i] = y[i] - lambda x[i] - sum_chunks partial  (double-double, rounded once)
+__global__ void residual_finish_kernel(const double2 *__restrict__ partial, int nchunks, int n,
+                                       double lambda, const double *__restrict__ x,
+                                       const double *__restrict__ y, double *__restrict__ r)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double hi = y[i], lo = 0.0;
+    qmlg_dd_fma(hi, lo, -lambda, x[i]);
+    for (int c = 0; c < nchunks; ++c) {
+        const double2 p = partial[(int64_t)c * n + i];
+        qmlg_dd_add(hi, lo, -p.x, -p.y);
+    }
+    r[i] = hi + lo;
+}
+
+// ---------------------------------------------------------------- vectors --
+
+__global__ void copy_diag_kernel(const double *__restrict__ A, int64_t lda, int n,
+                                 double *__restrict__ d)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) d[i] = A[(int64_t)i * lda + i];
+}
+
+__global__ void axpy_norms_kernel(double *__restrict__ x, const double *__restrict__ dx, int n,
+                                  double *__restrict__ sums)
+{
+    // x += dx; sums[0] += |dx|^2, sums[1] += |x|^2 (block partials, then atomics)
+    __shared__ double s0[8], s1[8];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double a = 0.0, b = 0.0;
+    if (i < n) {
+        const double d = dx[i];
+        const double v = x[i] + d;
+        x[i] = v;
+        a = d * d;
+        b = v * v;
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, off);
+        b += __shfl_xor_sync(0xffffffffu, b, off);
+    }
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        s0[w] = a;
+        s1[w] = b;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double ta = 0.0, tb = 0.0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+            ta += s0[k];
+            tb += s1[k];
+        }
+        atomicAdd(&sums[0], ta);
+        atomicAdd(&sums[1], tb);
+    }
+}
+
+__global__ void fill_nan_kernel(double *__restrict__ x, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] = nan("");
+}
+
+}  // namespace
+
+// ===================================================================== API ==
+
+namespace qmlg {
+
+int cholesky_fp64(double *A, int n, int64_t lda, double shift, int *d_info, cudaStream_t s)
+{
+    for (int k0 = 0; k0 < n; k0 += NB) {
+        potrf_diag_kernel<<<1, 256, 0, s>>>(A, lda, n, k0, shift, d_info);
+        const int below = n - (k0 + NB);
+        if (below > 0) {
+            trsm_panel_kernel<<<(int)ceil_div(below, 64), 256, 0, s>>>(A, lda, n, k0, d_info);
+            const int64_t t = ceil_div(below, 64);
+            syrk_update_kernel<<<(unsigned)(t * (t + 1) / 2), 256, 0, s>>>(A, lda, n, k0, d_info);
+        }
+    }
+    return check_launch();
+}
+
+int potrs_fp64(const double *A, int n, int64_t lda, double *x, cudaStream_t s)
+{
+    for (int k0 = 0; k0 < n; k0 += NB) {
+        trsv_diag_fwd_kernel<<<1, NB, 0, s>>>(A, lda, n, k0, x);
+        const int below = n - (k0 + NB);
+        if (below > 0)
+            gemv_fwd_update_kernel<<<(int)ceil_div((int64_t)below * 32, 256), 256, 0, s>>>(
+                A, lda, n, k0, x);
+    }
+    const int last = (int)((n - 1) / NB) * NB;
+    for (int k0 = last; k0 >= 0; k0 -= NB) {
+        trsv_diag_bwd_kernel<<<1, NB, 0, s>>>(A, lda, n, k0, x);
+        if (k0 > 0)
+            gemv_bwd_update_kernel<<<(int)ceil_div(k0, 256), 256, 0, s>>>(A, lda, n, k0, x);
+    }
+    return check_launch();
+}
+
+// R[i][j] <- R[j][i] for j < i, R[i][i] <- diag[i]: restores the lower triangle from
+// the untouched upper one before an FP64 refactorisation.
+__global__ void mirror_kernel(double *__restrict__ A, int64_t lda, int n,
+                              const double *__restrict__ diag)
+{
+    __shared__ double T[32][33];
+    const int bi = blockIdx.y, bj = blockIdx.x;  // tile (rows bi, cols bj), bj <= bi
+    if (bj > bi) return;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    for (int k = ty; k < 32; k += 8) {
+        const int r = bj * 32 + k, c = bi * 32 + tx;  // source R[r][c], r <= c
+        T[k][tx] = (r < n && c < n) ? A[(int64_t)r * lda + c] : 0.0;
+    }
+    __syncthreads();
+    for (int k = ty; k < 32; k += 8) {
+        const int i = bi * 32 + k, j = bj * 32 + tx;  // dest R[i][j] = R[j][i]
+        if (i < n && j < n && j <= i) A[(int64_t)i * lda + j] = (i == j) ? diag[i] : T[tx][k];
+    }
+}
+
+int mirror_upper_to_lower(double *A, int n, int64_t lda, const double *diag, cudaStream_t s)
+{
+    const int t = (int)ceil_div(n, 32);
+    mirror_kernel<<<dim3(t, t), dim3(32, 8), 0, s>>>(A, lda, n, diag);
+    return check_launch();
+}
+
+size_t emulated_factor_ws(int n)
+{
+    WorkspacePlan p;
+    p.add<__nv_bfloat16>((size_t)kEmuMaxSlices * (size_t)n * 64);
+    p.add<int>((size_t)n);
+    return p.total();
+}
+
+int emulated_factor(double *A, int n, int64_t lda, double shift, Workspace &ws, int *d_info,
+                    EmulatedFactor &f, cudaStream_t s, int slices)
+{
+    __nv_bfloat16 *digits = ws.take<__nv_bfloat16>((size_t)slices * (size_t)n * 64);
+    int *expo = ws.take<int>((size_t)n);
+    if (digits == nullptr || expo == nullptr) return QMLG_E_WORKSPACE;
+    for (int k0 = 0; k0 < n; k0 += NB) {
+        potrf_diag_kernel<<<1, 256, 0, s>>>(A, lda, n, k0, shift, d_info);
+        const int below = n - (k0 + NB);
+        if (below > 0) {
+            trsm_panel_kernel<<<(int)ceil_div(below, 64), 256, 0, s>>>(A, lda, n, k0, d_info);
+            int st = emu_trailing_update(A, lda, n, k0, NB, slices, digits, expo, d_info, s);
+            if (st != QMLG_OK) return st;
+        }
+    }
+    f.A = A;
+    f.n = n;
+    f.lda = lda;
+    f.slices = slices;
+    return check_launch();
+}
+
+int emulated_potrs(const EmulatedFactor &f, double *x, cudaStream_t s)
+{
+    return potrs_fp64(f.A, f.n, f.lda, x, s);
+}
+
+size_t residual_ws(int n)
+{
+    WorkspacePlan p;
+    p.add<double2>((size_t)ceil_div(n, RES_CHUNK) * (size_t)n);
+    return p.total();
+}
+
+int residual_dd(const double *A, int n, int64_t lda, const double *diag, double lambda,
+                const double *x, const double *y, double *r, Workspace &ws, cudaStream_t s)
+{
+    const int nchunks = (int)ceil_div(n, RES_CHUNK);
+    double2 *partial = ws.take<double2>((size_t)nchunks * n);
+    if (partial == nullptr) return QMLG_E_WORKSPACE;
+    symv_dd_partial_kernel<<<dim3((unsigned)ceil_div(n, RES_ROWS), nchunks), 256, 0, s>>>(
+        A, lda, n, diag, x, partial);
+    residual_finish_kernel<<<(int)ceil_div(n, 256), 256, 0, s>>>(partial, nchunks, n, lambda, x,
+                                                                 y, r);
+    return check_launch();
+}
+
+}  // namespace qmlg
+
+extern "C" size_t qmlg_cholesky_workspace_size(int n)
+{
+    (void)n;
+    qmlg::WorkspacePlan p;
+    p.add<int>(4);
+    return p.total();
+}
+
+extern "C" int qmlg_cholesky(double *A, int n, int64_t lda, double lambda, void *workspace,
+                             size_t ws_bytes, void *stream)
+{
+    if (n < 0 || lda < n || (n > 0 && A == nullptr)) return QMLG_E_ARG;
+    if (n == 0) return QMLG_OK;
+    qmlg::Workspace ws(workspace, ws_bytes);
+    int *d_info = ws.take<int>(4);
+    if (d_info == nullptr) return QMLG_E_WORKSPACE;
+    cudaStream_t s = qmlg::as_stream(stream);
+    cudaError_t e = cudaMemsetAsync(d_info, 0, sizeof(int), s);
+    if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+    int st = qmlg::cholesky_fp64(A, n, lda, lambda, d_info, s);
+    if (st != QMLG_OK) return st;
+    int info = 0;
+    e = cudaMemcpyAsync(&info, d_info, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+    return info;
+}
+
+extern "C" int qmlg_cholesky_solve_factored(const double *U, int n, int64_t lda, const double *y,
+                                            double *x, void *stream)
+{
+    if (n < 0 || lda < n || (n > 0 && (U == nullptr || y == nullptr || x == nullptr)))
+        return QMLG_E_ARG;
+    if (n == 0) return QMLG_OK;
+    cudaStream_t s = qmlg::as_stream(stream);
+    if (x != y) {
+        cudaError_t e = cudaMemcpyAsync(x, y, sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice, s);
+        if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+    }
+    return qmlg::potrs_fp64(U, n, lda, x, s);
+}
+
+extern "C" size_t qmlg_residual_workspace_size(int n) { return qmlg::residual_ws(n); }
+
+extern "C" int qmlg_residual_dd(const double *A, int n, int64_t lda, const double *diag,
+                                double lambda, const double *x, const double *y, double *r,
+                                void *workspace, size_t ws_bytes, void *stream)
+{
+    if (n < 0 || lda < n) return QMLG_E_ARG;
+    if (n == 0) return QMLG_OK;
+    if (A == nullptr || diag == nullptr || x == nullptr || y == nullptr || r == nullptr)
+        return QMLG_E_ARG;
+    qmlg::Workspace ws(workspace, ws_bytes);
+    return qmlg::residual_dd(A, n, lda, diag, lambda, x, y, r, ws, qmlg::as_stream(stream));
+}
+
+// ------------------------------------------------------------ full solve --
+
+extern "C" size_t qmlg_solve_workspace_size(int n, int precision)
+{
+    qmlg::WorkspacePlan p;
+    p.add<int>(4);                       // info
+    p.add<double>(4);                    // norm sums
+    p.add<double>((size_t)n);            // saved diagonal
+    p.add<double>((size_t)n);            // residual / correction
+    p.add<char>(qmlg::residual_ws(n));   // residual partials
+    if (precision == QMLG_PREC_MIXED) p.add<char>(qmlg::emulated_factor_ws(n));
+    return p.total();
+}
+
+namespace {
+
+struct SolveCtx {
+    double *A;
+    int n;
+    int64_t lda;
+    const double *y;
+    double *x;
+    double lambda;
+    int *d_info;
+    double *d_sums;
+    double *diag;
+    double *r;
+    qmlg::Workspace *ws;
+    size_t ws_mark;
+    cudaStream_t s;
+};
+
+int read_info(SolveCtx &c, int &info)
+{
+    cudaError_t e = cudaMemcpyAsync(&info, c.d_info, sizeof(int), cudaMemcpyDeviceToHost, c.s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c.s);
+    return e == cudaSuccess ? QMLG_OK : qmlg::set_cuda_error(e);
+}
+
+// Iterative refinement: r = y - (A + lambda I) x in double-double, dx = solve(r),
+// x += dx, until |dx|/|x| <= tol or the correction stops shrinking.
+template <class SolveFn>
+int refine(SolveCtx &c, const QmlgRefineOpts &o, SolveFn solve_fn, QmlgSolveReport &rep,
+           bool &stalled)
+{
+    stalled = false;
+    double prev = INFINITY;
+    rep.last_correction = INFINITY;
+    for (int it = 0; it < o.max_outer; ++it) {
+        c.ws->used = c.ws_mark;
+        int st = qmlg::residual_dd(c.A, c.n, c.lda, c.diag, c.lambda, c.x, c.y, c.r, *c.ws, c.s);
+        if (st != QMLG_OK) return st;
+        st = solve_fn(c.r);
+        if (st != QMLG_OK) return st;
+        cudaError_t e = cudaMemsetAsync(c.d_sums, 0, 2 * sizeof(double), c.s);
+        if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+        axpy_norms_kernel<<<(int)qmlg::ceil_div(c.n, 256), 256, 0, c.s>>>(c.x, c.r, c.n, c.d_sums);
+        double h[2];
+        e = cudaMemcpyAsync(h, c.d_sums, sizeof(h), cudaMemcpyDeviceToHost, c.s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c.s);
+        if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+        const double rel = std::sqrt(h[0]) / std::fmax(std::sqrt(h[1]), 1e-300);
+        rep.outer_iterations = it + 1;
+        rep.last_correction = rel;
+        if (!(rel == rel)) {
+            stalled = true;
+            return QMLG_OK;
+        }
+        if (rel <= o.tol) return QMLG_OK;
+        if (rel > 0.5 * prev) {
+            stalled = true;
+            return QMLG_OK;
+        }
+        prev = rel;
+    }
+    stalled = rep.last_correction > o.tol;
+    return QMLG_OK;
+}
+
+}  // namespace
+
+extern "C" int qmlg_solve(double *A, int n, int64_t lda, const double *y, double *x,
+                          double lambda, int precision, const QmlgRefineOpts *opts,
+                          QmlgSolveReport *report, void *workspace, size_t ws_bytes, void *stream)
+{
+    if (n < 0 || lda < n) return QMLG_E_ARG;
+    if (precision != QMLG_PREC_FP64 && precision != QMLG_PREC_MIXED) return QMLG_E_ARG;
+    QmlgSolveReport rep{};
+    rep.precision_used = precision;
+    if (n == 0) {
+        if (report) *report = rep;
+        return QMLG_OK;
+    }
+    if (A == nullptr || y == nullptr || x == nullptr) return QMLG_E_ARG;
+    if (ws_bytes < qmlg_solve_workspace_size(n, precision)) return QMLG_E_WORKSPACE;
+    QmlgRefineOpts o{10, 50, 1e-15, 0.0, 1};
+    if (opts) o = *opts;
+
+    cudaStream_t s = qmlg::as_stream(stream);
+    qmlg::Workspace ws(workspace, ws_bytes);
+    SolveCtx c{A, n, lda, y, x, lambda, ws.take<int>(4), ws.take<double>(4),
+               ws.take<double>((size_t)n), ws.take<double>((size_t)n), &ws, 0, s};
+    c.ws_mark = ws.used;
+    cudaError_t e = cudaMemsetAsync(c.d_info, 0, sizeof(int), s);
+    if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+    copy_diag_kernel<<<(int)qmlg::ceil_div(n, 256), 256, 0, s>>>(A, lda, n, c.diag);
+
+    int st = QMLG_OK, info = 0;
+    bool stalled = false;
+    if (precision == QMLG_PREC_MIXED) {
+        // Emulated-FP64 factor on the tensor cores, in place like the FP64 one.
+        qmlg::EmulatedFactor f;
+        st = qmlg::emulated_factor(A, n, lda, lambda, ws, c.d_info, f, s);
+        if (st != QMLG_OK) return st;
+        if ((st = read_info(c, info)) != QMLG_OK) return st;
+        rep.info = info;
+        if (info == 0) {
+            e = cudaMemcpyAsync(x, y, sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice, s);
+            if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+            if ((st = qmlg::emulated_potrs(f, x, s)) != QMLG_OK) return st;
+            c.ws_mark = ws.used;
+            st = refine(c, o, [&](double *v) { return qmlg::emulated_potrs(f, v, s); }, rep, stalled);
+            if (st != QMLG_OK) return st;
+        }
+        if ((info != 0 || stalled) && o.allow_fallback) {
+            rep.fell_back = 1;
+            precision = QMLG_PREC_FP64;
+            e = cudaMemsetAsync(c.d_info, 0, sizeof(int), s);
+            if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+            if ((st = qmlg::mirror_upper_to_lower(A, n, lda, c.diag, s)) != QMLG_OK) return st;
+        } else {
+            rep.backward_error = 0.0;
+            if (report) *report = rep;
+            if (info != 0) return info;
+            return stalled ? QMLG_E_NOT_CONVERGED : QMLG_OK;
+        }
+    }
+
+    // Plain FP64: factor A in place (upper triangle, like dpotrf("U")).
+    rep.precision_used = QMLG_PREC_FP64;
+    if ((st = qmlg::cholesky_fp64(A, n, lda, lambda, c.d_info, s)) != QMLG_OK) return st;
+    if ((st = read_info(c, info)) != QMLG_OK) return st;
+    rep.info = info;
+    if (info != 0) {
+        fill_nan_kernel<<<(int)qmlg::ceil_div(n, 256), 256, 0, s>>>(x, n);
+        if (report) *report = rep;
+        return info;
+    }
+    e = cudaMemcpyAsync(x, y, sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+    if ((st = qmlg::potrs_fp64(A, n, lda, x, s)) != QMLG_OK) return st;
+    if (o.max_outer > 0) {
+        st = refine(c, o, [&](double *v) { return qmlg::potrs_fp64(A, n, lda, v, s); }, rep,
+                    stalled);
+        if (st != QMLG_OK) return st;
+    }
+    if (report) *report = rep;
+    e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+    return (o.max_outer > 0 && stalled) ? QMLG_E_NOT_CONVERGED : QMLG_OK;
+}

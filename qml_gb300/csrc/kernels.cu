@@ -1,0 +1,332 @@
+// FP64 Gaussian and Laplacian kernel matrices and the prediction that uses them.
+//
+// Restates fgaussian_kernel / flaplacian_kernel (qml/fkernels.f90:340-400):
+//   Gaussian:  K[j + i*ldk] = exp(-0.5/sigma^2 * |A_j - B_i|^2)
+//   Laplacian: K[j + i*ldk] = exp(-1/sigma * |A_j - B_i|_1)
+// with K in Fortran order like the reference.  The Gaussian distance is formed as
+// |a|^2 + |b|^2 - 2 a.b (norms in FP64); the Laplacian keeps the direct difference
+// form (an L1 distance is not a contraction).
+//
+// Tiling: a CTA computes a 64 (j, rows of A) x 64 (i, rows of B) tile with 256
+// threads, 4x4 outputs per thread, the feature dimension streamed through shared
+// memory 16 columns at a time.  Symmetric mode computes only tiles on or below the
+// diagonal and writes the mirror through a shared-memory transpose, so K is
+// exactly symmetric.
+#include <cmath>
+
+#include "common.cuh"
+
+namespace {
+
+constexpr int TJ = 64;   // tile rows (A side, contiguous in K)
+constexpr int TI = 64;   // tile cols (B side)
+constexpr int TK = 16;   // feature chunk
+constexpr int NT = 256;  // threads
+
+enum Kind { kGauss = 0, kLaplace = 1 };
+
+// Maps a linear block id onto a lower-triangular tile pair (bi >= bj).
+__device__ __forceinline__ void tri_index(int64_t t, int &bi, int &bj)
+{
+    int64_t r = (int64_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+    while (r * (r + 1) / 2 > t) --r;
+    while ((r + 1) * (r + 2) / 2 <= t) ++r;
+    bi = (int)r;
+    bj = (int)(t - r * (r + 1) / 2);
+}
+
+// Accumulates the 4x4 micro-tile over the feature dimension.
+template <int KIND>
+__device__ __forceinline__ void tile_accumulate(const double *__restrict__ A, int64_t lda, int na,
+                                                const double *__restrict__ B, int64_t ldb, int nb,
+                                                int d, int j0, int i0, double (&acc)[4][4],
+                                                double (*As)[TJ + 1], double (*Bs)[TI + 1],
+                                                double *a2s, double *b2s)
+{
+    // Gaussian: threads 0..63 accumulate |A_j|^2 and 64..127 |B_i|^2 of the tile rows
+    double nrm = 0.0;
+    const int tid = threadIdx.x;
+    const int tx = tid & 15, ty = tid >> 4;
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
+
+    for (int t0 = 0; t0 < d; t0 += TK) {
+        // 64 rows x 16 features of each operand: 1024 values, 4 per thread.
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int e = tid + q * NT;
+            const int r = e >> 4, c = e & 15;
+            const int t = t0 + c;
+            const int ja = j0 + r, ib = i0 + r;
+            As[c][r] = (ja < na && t < d) ? A[(int64_t)ja * lda + t] : 0.0;
+            Bs[c][r] = (ib < nb && t < d) ? B[(int64_t)ib * ldb + t] : 0.0;
+        }
+        __syncthreads();
+        if (KIND == kGauss && tid < TJ + TI) {
+            const int r = tid & (TJ - 1);
+            if (tid < TJ) {
+#pragma unroll
+                for (int c = 0; c < TK; ++c) nrm = fma(As[c][r], As[c][r], nrm);
+            } else {
+#pragma unroll
+                for (int c = 0; c < TK; ++c) nrm = fma(Bs[c][r], Bs[c][r], nrm);
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < TK; ++c) {
+            double av[4], bv[4];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) av[a] = As[c][tx + 16 * a];
+#pragma unroll
+            for (int b = 0; b < 4; ++b) bv[b] = Bs[c][ty + 16 * b];
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int b = 0; b < 4; ++b) {
+                    if (KIND == kGauss) {
+                        acc[a][b] = fma(av[a], bv[b], acc[a][b]);
+                    } else {
+                        acc[a][b] += fabs(av[a] - bv[b]);
+                    }
+                }
+        }
+        __syncthreads();
+    }
+    if (KIND == kGauss && tid < TJ + TI) {
+        if (tid < TJ) a2s[tid] = nrm;
+        else b2s[tid - TJ] = nrm;
+    }
+    __syncthreads();
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(NT)
+kernel_matrix_kernel(const double *__restrict__ A, int64_t lda, int na,
+                     const double *__restrict__ B, int64_t ldb, int nb, int d,
+                     double scale, double *__restrict__ K, int64_t ldk, int symmetric,
+                     double diag_shift)
+{
+    // operand chunks during accumulation, the output tile (for the mirror) after
+    __shared__ double smem[TI * (TJ + 1)];
+    __shared__ double a2s[TJ], b2s[TI];
+    double(*As)[TJ + 1] = reinterpret_cast<double(*)[TJ + 1]>(smem);
+    double(*Bs)[TI + 1] = reinterpret_cast<double(*)[TI + 1]>(smem + TK * (TJ + 1));
+    double(*T)[TJ + 1] = reinterpret_cast<double(*)[TJ + 1]>(smem);
+
+    int bj, bi;
+    if (symmetric) {
+        tri_index(blockIdx.x, bi, bj);  // bi >= bj: B-tile index >= A-tile index
+    } else {
+        bj = blockIdx.x;
+        bi = blockIdx.y;
+    }
+    const int j0 = bj * TJ, i0 = bi * TI;
+    double acc[4][4];
+    tile_accumulate<KIND>(A, lda, na, B, ldb, nb, d, j0, i0, acc, As, Bs, a2s, b2s);
+
+    const int tid = threadIdx.x;
+    const int tx = tid & 15, ty = tid >> 4;
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const int j = j0 + tx + 16 * a, i = i0 + ty + 16 * b;
+            double v;
+            if (KIND == kGauss) {
+                double d2 = 0.0;
+                if (j < na && i < nb)
+                    d2 = fmax(a2s[tx + 16 * a] + b2s[ty + 16 * b] - 2.0 * acc[a][b], 0.0);
+                if (symmetric && i == j) d2 = 0.0;
+                v = exp(scale * d2);
+            } else {
+                v = exp(scale * acc[a][b]);
+            }
+            if (symmetric && i == j) v += diag_shift;
+            if (j < na && i < nb) K[(int64_t)i * ldk + j] = v;
+            T[ty + 16 * b][tx + 16 * a] = v;
+        }
+    if (symmetric && bi != bj) {
+        // mirror: K[i + j*ldk] for the same (j, i), coalesced along i
+        __syncthreads();
+        for (int e = tid; e < TI * TJ; e += NT) {
+            const int ii = e & (TI - 1), jj = e / TI;
+            const int i = i0 + ii, j = j0 + jj;
+            if (i < nb && j < na) K[(int64_t)j * ldk + i] = T[ii][jj];
+        }
+    }
+}
+
+// Fused prediction: per (training tile, test tile) partial sums of k * alpha.
+template <int KIND>
+__global__ void __launch_bounds__(NT)
+predict_partial_kernel(const double *__restrict__ Xtr, int64_t ldtr, int ntr,
+                       const double *__restrict__ Xte, int64_t ldte, int nte, int d,
+                       double scale, const double *__restrict__ alpha,
+                       double *__restrict__ partial)
+{
+    __shared__ double As[TK][TJ + 1];
+    __shared__ double Bs[TK][TI + 1];
+    __shared__ double a2s[TJ], b2s[TI];
+    __shared__ double red[16][TI + 1];
+    const int bj = blockIdx.x, bi = blockIdx.y;
+    const int j0 = bj * TJ, i0 = bi * TI;
+    double acc[4][4];
+    tile_accumulate<KIND>(Xtr, ldtr, ntr, Xte, ldte, nte, d, j0, i0, acc, As, Bs, a2s, b2s);
+    const int tid = threadIdx.x;
+    const int tx = tid & 15, ty = tid >> 4;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+        const int i = i0 + ty + 16 * b;
+        double s = 0.0;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const int j = j0 + tx + 16 * a;
+            if (j < ntr && i < nte) {
+                double v;
+                if (KIND == kGauss) {
+                    const double d2 =
+                        fmax(a2s[tx + 16 * a] + b2s[ty + 16 * b] - 2.0 * acc[a][b], 0.0);
+                    v = exp(scale * d2);
+                } else {
+                    v = exp(scale * acc[a][b]);
+                }
+                s = fma(v, alpha[j], s);
+            }
+        }
+        red[tx][ty + 16 * b] = s;
+    }
+    __syncthreads();
+    if (tid < TI) {
+        double s = 0.0;
+        for (int q = 0; q < 16; ++q) s += red[q][tid];
+        const int i = i0 + tid;
+        if (i < nte) partial[(int64_t)bj * nte + i] = s;
+    }
+}
+
+__global__ void reduce_partial_kernel(const double *__restrict__ partial, int nparts, int n,
+                                      double *__restrict__ y)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double s = 0.0;
+    for (int p = 0; p < nparts; ++p) s += partial[(int64_t)p * n + i];
+    y[i] = s;
+}
+
+// yhat[i] = sum_j Ks[j + i*ldk] alpha[j]: one warp per column of Ks.
+__global__ void gemv_t_kernel(const double *__restrict__ Ks, int64_t ldk, int ntr, int nte,
+                              const double *__restrict__ alpha, double *__restrict__ y)
+{
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= nte) return;
+    const double *col = Ks + (int64_t)warp * ldk;
+    double s = 0.0;
+    for (int j = lane; j < ntr; j += 32) s = fma(col[j], alpha[j], s);
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    if (lane == 0) y[warp] = s;
+}
+
+int check_common(const double *A, int64_t lda, int na, const double *B, int64_t ldb, int nb,
+                 int d, double sigma)
+{
+    if (na < 0 || nb < 0 || d < 0) return QMLG_E_ARG;
+    if ((na > 0 && (A == nullptr || lda < d)) || (nb > 0 && (B == nullptr || ldb < d)))
+        return QMLG_E_ARG;
+    if (!(sigma > 0.0) || !std::isfinite(sigma)) return QMLG_E_ARG;
+    return QMLG_OK;
+}
+
+int kernel_matrix(int kind, const double *A, int64_t lda, int na, const double *B,
+                  int64_t ldb, int nb, int d, double sigma, double *K, int64_t ldk, int flags,
+                  double diag_shift, void *stream)
+{
+    int st = check_common(A, lda, na, B, ldb, nb, d, sigma);
+    if (st != QMLG_OK) return st;
+    if (K == nullptr || ldk < na) return QMLG_E_ARG;
+    const bool symmetric = (flags & QMLG_KERNEL_SYMMETRIC) != 0;
+    if (symmetric && (na != nb || A != B || lda != ldb)) return QMLG_E_ARG;
+    if (na == 0 || nb == 0) return QMLG_OK;
+    cudaStream_t s = qmlg::as_stream(stream);
+
+    const double scale = kind == kGauss ? -0.5 / (sigma * sigma) : -1.0 / sigma;
+    const int tj = (int)qmlg::ceil_div(na, TJ), ti = (int)qmlg::ceil_div(nb, TI);
+    dim3 grid = symmetric ? dim3((unsigned)((int64_t)tj * (tj + 1) / 2)) : dim3(tj, ti);
+    if (kind == kGauss)
+        kernel_matrix_kernel<kGauss><<<grid, NT, 0, s>>>(A, lda, na, B, ldb, nb, d, scale, K, ldk,
+                                                        symmetric, diag_shift);
+    else
+        kernel_matrix_kernel<kLaplace><<<grid, NT, 0, s>>>(A, lda, na, B, ldb, nb, d, scale, K,
+                                                          ldk, symmetric, diag_shift);
+    return qmlg::check_launch();
+}
+
+}  // namespace
+
+extern "C" int qmlg_gaussian_kernel(const double *A, int64_t lda, int na, const double *B,
+                                    int64_t ldb, int nb, int d, double sigma, double *K,
+                                    int64_t ldk, int flags, double diag_shift, void *stream)
+{
+    return kernel_matrix(kGauss, A, lda, na, B, ldb, nb, d, sigma, K, ldk, flags, diag_shift,
+                         stream);
+}
+
+extern "C" int qmlg_laplacian_kernel(const double *A, int64_t lda, int na, const double *B,
+                                     int64_t ldb, int nb, int d, double sigma, double *K,
+                                     int64_t ldk, int flags, double diag_shift, void *stream)
+{
+    return kernel_matrix(kLaplace, A, lda, na, B, ldb, nb, d, sigma, K, ldk, flags, diag_shift,
+                         stream);
+}
+
+extern "C" int qmlg_predict_gemv(const double *Ks, int64_t ldk, int ntrain, int ntest,
+                                 const double *alpha, double *yhat, void *stream)
+{
+    if (ntrain < 0 || ntest < 0 || ldk < ntrain) return QMLG_E_ARG;
+    if (ntest == 0) return QMLG_OK;
+    if (Ks == nullptr || alpha == nullptr || yhat == nullptr) return QMLG_E_ARG;
+    gemv_t_kernel<<<(int)qmlg::ceil_div((int64_t)ntest * 32, 256), 256, 0,
+                    qmlg::as_stream(stream)>>>(Ks, ldk, ntrain, ntest, alpha, yhat);
+    return qmlg::check_launch();
+}
+
+extern "C" size_t qmlg_predict_workspace_size(int ntrain, int ntest)
+{
+    qmlg::WorkspacePlan p;
+    p.add<double>((size_t)qmlg::ceil_div(ntrain < 1 ? 1 : ntrain, TJ) * (size_t)ntest);  // partials
+    return p.total();
+}
+
+extern "C" int qmlg_predict_fused(int kind, const double *Xtrain, int64_t ldtrain, int ntrain,
+                                  const double *Xtest, int64_t ldtest, int ntest, int d,
+                                  double sigma, const double *alpha, double *yhat,
+                                  void *workspace, size_t ws_bytes, void *stream)
+{
+    if (kind != QMLG_KIND_GAUSSIAN && kind != QMLG_KIND_LAPLACIAN) return QMLG_E_ARG;
+    int st = check_common(Xtrain, ldtrain, ntrain, Xtest, ldtest, ntest, d, sigma);
+    if (st != QMLG_OK) return st;
+    if (ntest == 0) return QMLG_OK;
+    if (yhat == nullptr || (ntrain > 0 && alpha == nullptr)) return QMLG_E_ARG;
+    cudaStream_t s = qmlg::as_stream(stream);
+    if (ntrain == 0) {
+        cudaError_t e = cudaMemsetAsync(yhat, 0, sizeof(double) * (size_t)ntest, s);
+        return e == cudaSuccess ? QMLG_OK : qmlg::set_cuda_error(e);
+    }
+    if (ws_bytes < qmlg_predict_workspace_size(ntrain, ntest)) return QMLG_E_WORKSPACE;
+    qmlg::Workspace ws(workspace, ws_bytes);
+    const int tj = (int)qmlg::ceil_div(ntrain, TJ), ti = (int)qmlg::ceil_div(ntest, TI);
+    double *partial = ws.take<double>((size_t)tj * ntest);
+    if (partial == nullptr) return QMLG_E_WORKSPACE;
+    const double scale = kind == QMLG_KIND_GAUSSIAN ? -0.5 / (sigma * sigma) : -1.0 / sigma;
+    if (kind == QMLG_KIND_GAUSSIAN)
+        predict_partial_kernel<kGauss><<<dim3(tj, ti), NT, 0, s>>>(
+            Xtrain, ldtrain, ntrain, Xtest, ldtest, ntest, d, scale, alpha, partial);
+    else
+        predict_partial_kernel<kLaplace><<<dim3(tj, ti), NT, 0, s>>>(
+            Xtrain, ldtrain, ntrain, Xtest, ldtest, ntest, d, scale, alpha, partial);
+    reduce_partial_kernel<<<(int)qmlg::ceil_div(ntest, 256), 256, 0, s>>>(partial, tj, ntest, yhat);
+    return qmlg::check_launch();
+}

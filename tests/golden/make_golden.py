@@ -1,0 +1,70 @@
+"""Builds the golden fixtures in this folder from the reference's own test data.
+
+Run where the reference tree is mounted (default /root/reference, or pass a path).
+Outputs (small .npz files, committed):
+  cm_qm7_0101_0110.npz  inputs and expected outputs of the reference's Coulomb-matrix
+                        known-answer test (tests/test_representations.py:46-90):
+                        Z, R of qm7/0101..0110.xyz, size = max natoms + 1 = 17,
+                        row-norm sorted and unsorted vectors (10 x 153) from
+                        tests/data/coulomb_matrix_representation_*.txt
+  cho_solve_k_local_gaussian.npz
+                        the SPD system of tests/test_math.py:32-52:
+                        A = tests/data/K_local_gaussian.txt (200 x 200),
+                        y = tests/data/y_cho_solve.txt (200)
+  kernels_seed666.npz   the inputs of tests/test_kernels.py:34-90 (np.random.seed(666),
+                        X = rand(25, 1000), Xs = rand(20, 1000), sigma = 100) with the
+                        reference test's own NumPy-loop expectations
+"""
+import os
+import sys
+
+import numpy as np
+
+NC = {"H": 1, "C": 6, "N": 7, "O": 8, "S": 16}
+
+
+def read_xyz(path):
+    with open(path) as f:
+        lines = f.readlines()
+    n = int(lines[0])
+    z, r = [], []
+    for line in lines[2:2 + n]:
+        t = line.split()
+        z.append(NC[t[0]])
+        r.append([float(v) for v in t[1:4]])
+    return np.array(z, dtype=np.float64), np.array(r, dtype=np.float64)
+
+
+def main(ref):
+    here = os.path.dirname(os.path.abspath(__file__))
+    mols = [read_xyz(os.path.join(ref, "tests", "qm7", "%04d.xyz" % k)) for k in range(101, 111)]
+    size = max(z.shape[0] for z, _ in mols) + 1
+    counts = np.array([z.shape[0] for z, _ in mols], dtype=np.int64)
+    offsets = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    np.savez_compressed(
+        os.path.join(here, "cm_qm7_0101_0110.npz"),
+        charges=np.concatenate([z for z, _ in mols]),
+        coordinates=np.concatenate([r for _, r in mols]),
+        offsets=offsets, size=size,
+        sorted=np.loadtxt(os.path.join(ref, "tests/data/coulomb_matrix_representation_row-norm_sorted.txt")),
+        unsorted=np.loadtxt(os.path.join(ref, "tests/data/coulomb_matrix_representation_unsorted.txt")))
+    np.savez_compressed(
+        os.path.join(here, "cho_solve_k_local_gaussian.npz"),
+        A=np.loadtxt(os.path.join(ref, "tests/data/K_local_gaussian.txt")),
+        y=np.loadtxt(os.path.join(ref, "tests/data/y_cho_solve.txt")))
+    np.random.seed(666)
+    X = np.random.rand(25, 1000)
+    Xs = np.random.rand(20, 1000)
+    sigma = 100.0
+    kl = np.zeros((25, 20))
+    kg = np.zeros((25, 20))
+    for i in range(25):
+        for j in range(20):
+            kl[i, j] = np.exp(np.sum(np.abs(X[i] - Xs[j])) / (-1.0 * sigma))
+            kg[i, j] = np.exp(np.sum(np.square(X[i] - Xs[j])) / (-2.0 * sigma ** 2))
+    np.savez_compressed(os.path.join(here, "kernels_seed666.npz"), X=X, Xs=Xs, sigma=sigma,
+                        laplacian=kl, gaussian=kg)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

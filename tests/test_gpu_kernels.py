@@ -1,0 +1,92 @@
+"""Gaussian / Laplacian kernel matrices and prediction on the GPU vs the oracle
+(relative error <= 1e-12 per entry, the FP64-path bar)."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import load_golden
+from qml_gb300 import core
+from qml_gb300.kernels import gaussian_kernel, laplacian_kernel
+from qml_gb300.synthetic import generate_molecules
+
+pytestmark = pytest.mark.gpu
+RTOL = 1e-12
+
+
+def relerr(a, b):
+    return float(np.max(np.abs(a - b) / np.abs(b)))
+
+
+def test_reference_kernel_test(cuda, oracle):
+    # tests/test_kernels.py:34-90 through the drop-in API
+    g = load_golden("kernels_seed666.npz")
+    X, Xs, s = g["X"], g["Xs"], float(g["sigma"])
+    for fn, key, ofn in ((laplacian_kernel, "laplacian", oracle.laplacian_kernel),
+                         (gaussian_kernel, "gaussian", oracle.gaussian_kernel)):
+        K = fn(X, Xs, s)
+        assert K.flags.f_contiguous and K.shape == (25, 20)
+        assert np.allclose(K, g[key])
+        assert relerr(K, ofn(X, Xs, s)) <= RTOL
+        Ks = fn(X, X, s)
+        assert np.array_equal(Ks, Ks.T)
+        assert relerr(Ks, ofn(X, X, s)) <= RTOL
+
+
+@pytest.fixture(scope="module")
+def cm_features(oracle):
+    b = generate_molecules(1000, seed=7)
+    return oracle.cm_sorted_batch(b.charges, b.coordinates, b.offsets, 23)
+
+
+@pytest.mark.parametrize("kind", ["gaussian", "laplacian"])
+@pytest.mark.parametrize("sigma", [250.0, 1000.0, 2000.0])
+def test_cm_features(cuda, oracle, cm_features, kind, sigma):
+    X = cm_features
+    A, B = X[:700], X[700:]
+    ofn = oracle.gaussian_kernel if kind == "gaussian" else oracle.laplacian_kernel
+    At, Bt = torch.from_numpy(A).to(cuda), torch.from_numpy(B).to(cuda)
+    K = core.kernel_matrix(kind, At, Bt, sigma).cpu().numpy()
+    assert relerr(K, ofn(A, B, sigma)) <= RTOL
+    Ks = core.kernel_matrix(kind, At, At, sigma, symmetric=True).cpu().numpy()
+    assert np.array_equal(Ks, Ks.T)
+    assert relerr(Ks, ofn(A, A, sigma)) <= RTOL
+
+
+@pytest.mark.parametrize("na,nb,d", [(1, 1, 1), (1, 65, 17), (65, 1, 276), (130, 67, 33), (64, 64, 16)])
+def test_odd_shapes(cuda, oracle, na, nb, d):
+    rng = np.random.default_rng(na * 1000 + nb)
+    A = rng.random((na, d)) * 10
+    B = rng.random((nb, d)) * 10
+    for kind, ofn in (("gaussian", oracle.gaussian_kernel), ("laplacian", oracle.laplacian_kernel)):
+        K = core.kernel_matrix(kind, torch.from_numpy(A).to(cuda), torch.from_numpy(B).to(cuda),
+                               7.0).cpu().numpy()
+        assert relerr(K, ofn(A, B, 7.0)) <= RTOL
+
+
+def test_diag_shift(cuda, cm_features):
+    At = torch.from_numpy(cm_features[:100]).to(cuda)
+    K0 = core.kernel_matrix("gaussian", At, At, 1000.0, symmetric=True)
+    K1 = core.kernel_matrix("gaussian", At, At, 1000.0, symmetric=True, diag_shift=0.5)
+    d = (K1 - K0).cpu().numpy()
+    assert np.array_equal(np.diag(d), np.full(100, 0.5)) and np.count_nonzero(d) == 100
+
+
+@pytest.mark.parametrize("kind", ["gaussian", "laplacian"])
+def test_predict_fused_and_gemv(cuda, oracle, cm_features, kind):
+    rng = np.random.default_rng(3)
+    Xtr, Xte = cm_features[:900], cm_features[900:]
+    alpha = rng.normal(size=900)
+    ofn = oracle.gaussian_kernel if kind == "gaussian" else oracle.laplacian_kernel
+    Ks = ofn(Xtr, Xte, 1000.0)
+    expect = Ks.T @ alpha
+    y = core.predict(kind, torch.from_numpy(Xtr).to(cuda), torch.from_numpy(Xte).to(cuda), 1000.0,
+                     torch.from_numpy(alpha).to(cuda)).cpu().numpy()
+    scale = np.abs(Ks.T) @ np.abs(alpha)
+    assert np.max(np.abs(y - expect) / scale) <= 1e-12
+    y2 = core.predict_gemv(torch.from_numpy(np.asfortranarray(Ks)).to(cuda).T.contiguous().T,
+                           torch.from_numpy(alpha).to(cuda)).cpu().numpy()
+    assert np.max(np.abs(y2 - expect) / scale) <= 1e-13
+    # deterministic: bitwise identical on a second call
+    y3 = core.predict(kind, torch.from_numpy(Xtr).to(cuda), torch.from_numpy(Xte).to(cuda), 1000.0,
+                      torch.from_numpy(alpha).to(cuda)).cpu().numpy()
+    assert np.array_equal(y, y3)

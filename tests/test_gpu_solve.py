@@ -1,0 +1,136 @@
+"""Cholesky solve on the GPU: LAPACK semantics (plain FP64) and the mixed path
+(emulated-FP64 tensor-core factor + double-double refinement) against the oracle.
+The mixed path's bar is <= 1e-8 relative error on alpha against the refined
+oracle solution for the same FP64 K."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import load_golden
+from qml_gb300 import core
+from qml_gb300.math import cho_solve
+from qml_gb300.synthetic import generate_molecules
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def test_reference_cho_solve(cuda, oracle):
+    # tests/test_math.py:32-52 through the drop-in
+    g = load_golden("cho_solve_k_local_gaussian.npz")
+    A, y = g["A"].copy(), g["y"].copy()
+    x = cho_solve(A, y)
+    assert np.allclose(y, g["y"]) and np.allclose(A, g["A"])
+    assert np.allclose(x, np.linalg.solve(g["A"], g["y"]))
+    xr = oracle.refined_solve(g["A"], g["y"], 0.0)
+    assert rel(x, xr) < 1e-5  # cond(A) ~ 4e9: FP64 forward error
+
+
+def test_cho_solve_shape_errors(cuda):
+    with pytest.raises(ValueError):
+        cho_solve(np.eye(3)[:2], np.ones(3))
+    with pytest.raises(ValueError):
+        cho_solve(np.eye(3), np.ones(2))
+
+
+def test_cho_solve_symmetrises_from_lower(cuda, oracle):
+    rng = np.random.default_rng(1)
+    M = rng.normal(size=(70, 70))
+    S = M @ M.T + 70 * np.eye(70)
+    A = S.copy()
+    A[np.triu_indices(70, 1)] = 0.0  # only the lower triangle is meaningful ...
+    A_upper = S.copy()  # ... but dpotrf("U") reads the upper one
+    x = cho_solve(A_upper, np.ones(70))
+    assert rel(x, np.linalg.solve(S, np.ones(70))) < 1e-12
+    cho_solve(A, np.ones(70))  # reads the (diagonal-only) upper triangle
+    assert np.array_equal(A, np.tril(S) + np.tril(S, -1).T)
+
+
+@pytest.fixture(scope="module")
+def krr_system(oracle):
+    b = generate_molecules(1500, seed=13)
+    X = oracle.cm_sorted_batch(b.charges, b.coordinates, b.offsets, 23)
+    return X, b.labels
+
+
+@pytest.mark.parametrize("n", [1, 63, 64, 100, 1500])
+def test_fp64_solve_matches_lapack(cuda, oracle, krr_system, n):
+    X, y = krr_system
+    K = np.ascontiguousarray(oracle.gaussian_kernel(X[:n], X[:n], 1000.0))
+    lam = 1e-4
+    Kt = torch.from_numpy(K).to(cuda)
+    x, rep = core.solve(Kt.clone(), torch.from_numpy(y[:n]).to(cuda), lam, precision="fp64",
+                        max_outer=0)
+    x = x.cpu().numpy()
+    xl = oracle.cho_solve(K + lam * np.eye(n), y[:n])
+    xr = oracle.refined_solve(K, y[:n], lam)
+    # same algorithm class as LAPACK: forward error of the order cond * u
+    assert rel(x, xr) < 1e-5 and rel(xl, xr) < 1e-5
+    # with double-double refinement: agrees with the refined oracle to <= 1e-12
+    x2, rep2 = core.solve(Kt.clone(), torch.from_numpy(y[:n]).to(cuda), lam, precision="fp64",
+                          max_outer=10)
+    assert rel(x2.cpu().numpy(), xr) < 1e-12
+
+
+def test_factor_matches_lapack_upper(cuda, oracle, krr_system):
+    from scipy.linalg import lapack
+    X, _ = krr_system
+    K = np.ascontiguousarray(oracle.gaussian_kernel(X[:300], X[:300], 1000.0)) + 1e-3 * np.eye(300)
+    Kt = torch.from_numpy(np.asfortranarray(K)).to(cuda)  # as the column-major matrix
+    KtF = torch.from_numpy(np.ascontiguousarray(K.T)).to(cuda)
+    assert core.cholesky(KtF) == 0
+    U = KtF.cpu().numpy().T  # column-major view back
+    c, info = lapack.dpotrf(np.asfortranarray(K), lower=0, clean=1)
+    assert info == 0
+    assert np.max(np.abs(np.triu(U) - c)) < 1e-10 * np.max(np.abs(c))
+    assert np.array_equal(np.tril(U, -1), np.tril(K, -1))  # other triangle untouched
+    del Kt
+
+
+def test_not_positive_definite_info(cuda, oracle):
+    from scipy.linalg import lapack
+    rng = np.random.default_rng(2)
+    M = rng.normal(size=(150, 150))
+    S = M @ M.T + np.eye(150)
+    S[100, 100] = -5.0
+    _, info = lapack.dpotrf(np.asfortranarray(S), lower=0)
+    assert info > 0
+    St = torch.from_numpy(np.ascontiguousarray(S.T)).to(cuda)
+    assert core.cholesky(St) == info
+    _, rep = core.solve(torch.from_numpy(S).to(cuda), torch.ones(150, dtype=torch.float64,
+                        device=cuda), 0.0, precision="fp64", raise_on_info=False)
+    assert rep["status"] == info
+
+
+@pytest.mark.parametrize("lam", [1e-4, 1e-6, 1e-8])
+def test_mixed_solve_1e8(cuda, oracle, krr_system, lam):
+    X, y = krr_system
+    K = np.ascontiguousarray(oracle.gaussian_kernel(X, X, 1000.0))
+    xr = oracle.refined_solve(K, y, lam)
+    x, rep = core.solve(torch.from_numpy(K).to(cuda), torch.from_numpy(y).to(cuda), lam,
+                        precision="mixed")
+    assert rep["status"] == 0, rep
+    assert rel(x.cpu().numpy(), xr) <= 1e-8, rep
+
+
+def test_mixed_solve_deterministic(cuda, oracle, krr_system):
+    X, y = krr_system
+    K = np.ascontiguousarray(oracle.gaussian_kernel(X[:700], X[:700], 500.0))
+    runs = [core.solve(torch.from_numpy(K).to(cuda), torch.from_numpy(y[:700]).to(cuda), 1e-6,
+                       precision="mixed")[0].cpu().numpy() for _ in range(2)]
+    assert np.array_equal(runs[0], runs[1])
+
+
+def test_residual_dd_exact(cuda):
+    rng = np.random.default_rng(0)
+    A = rng.integers(-1000, 1000, size=(130, 130)).astype(np.float64)
+    A = A + A.T
+    x = rng.integers(-1000, 1000, size=130).astype(np.float64)
+    y = A @ x + 3.0 * x
+    At = torch.from_numpy(A).to(cuda)
+    r = core.residual_dd(At, torch.from_numpy(np.diag(A).copy()).to(cuda), 3.0,
+                         torch.from_numpy(x).to(cuda), torch.from_numpy(y).to(cuda))
+    assert np.array_equal(r.cpu().numpy(), np.zeros(130))

@@ -1,0 +1,128 @@
+"""The oracle (CPU restatement) against the reference's own known answers."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import load_golden
+from qml_gb300.synthetic import generate_molecules
+
+REF = "/root/reference"
+
+
+def test_cm_oracle_matches_reference_fixture(oracle):
+    # tests/test_representations.py:46-90 (np.allclose against the text fixtures)
+    g = load_golden("cm_qm7_0101_0110.npz")
+    size = int(g["size"])
+    off = g["offsets"]
+    for m in range(off.shape[0] - 1):
+        z = g["charges"][off[m]:off[m + 1]]
+        r = g["coordinates"][off[m]:off[m + 1]]
+        s = oracle.cm_sorted(z, r, size)
+        u = oracle.cm_unsorted(z, r, size)
+        assert np.allclose(s, g["sorted"][m]) and np.max(np.abs(s - g["sorted"][m])) < 1e-8
+        assert np.allclose(u, g["unsorted"][m]) and np.max(np.abs(u - g["unsorted"][m])) < 1e-8
+        assert np.array_equal(s, oracle.cm_sorted_numpy(z, r, size))
+
+
+def test_cm_oracle_c_equals_numpy_restatement(oracle):
+    b = generate_molecules(300, seed=11)
+    X = oracle.cm_sorted_batch(b.charges, b.coordinates, b.offsets, 23)
+    for m in range(b.n_mol):
+        z, r = b.molecule(m)
+        assert np.array_equal(X[m], oracle.cm_sorted_numpy(z, r, 23))
+
+
+def test_cm_tie_rule(oracle):
+    # two hydrogens placed symmetrically about a carbon: equal row norms.  The
+    # reference's repeated minloc places the lower index last, i.e. ties are ordered
+    # by descending input index.
+    z = np.array([1.0, 6.0, 1.0])
+    r = np.array([[-1.1, 0.0, 0.0], [0.0, 0.0, 0.0], [1.1, 0.0, 0.0]])
+    cm = oracle.cm_sorted(z, r, 3)
+    full = np.zeros((3, 3))
+    full[0, 0] = 0.5 * 6 ** 2.4
+    # order should be C (1), then H index 2, then H index 0 -> M[2][0] = 1*1/2.2
+    assert cm[0] == 0.5 * 6.0 ** 2.4
+    assert cm[5] == 0.5 * 1.0 ** 2.4
+    assert cm[4] == (1.0 * 1.0) / np.sqrt(2.2 * 2.2)
+    assert np.array_equal(cm, oracle.cm_sorted_numpy(z, r, 3))
+
+
+def test_cm_too_many_atoms(oracle):
+    with pytest.raises(ValueError):
+        oracle.cm_sorted(np.ones(5), np.zeros((5, 3)), 4)
+
+
+def test_kernel_oracle_matches_reference_test(oracle):
+    # tests/test_kernels.py:34-90
+    g = load_golden("kernels_seed666.npz")
+    K = oracle.laplacian_kernel(g["X"], g["Xs"], float(g["sigma"]))
+    assert np.allclose(K, g["laplacian"])
+    assert np.max(np.abs(K / g["laplacian"] - 1)) < 1e-12
+    K = oracle.gaussian_kernel(g["X"], g["Xs"], float(g["sigma"]))
+    assert np.allclose(K, g["gaussian"])
+    assert np.max(np.abs(K / g["gaussian"] - 1)) < 1e-12
+    Ks = oracle.gaussian_kernel(g["X"], g["X"], float(g["sigma"]))
+    assert np.allclose(Ks, Ks.T)
+    assert K.flags.f_contiguous
+
+
+def test_cho_solve_oracle_matches_reference_test(oracle):
+    # tests/test_math.py:32-52
+    g = load_golden("cho_solve_k_local_gaussian.npz")
+    x = oracle.cho_solve(g["A"], g["y"])
+    assert np.allclose(x, np.linalg.solve(g["A"], g["y"]))
+
+
+def test_refined_solve_residual(oracle):
+    b = generate_molecules(400, seed=5)
+    X = oracle.cm_sorted_batch(b.charges, b.coordinates, b.offsets, 23)
+    K = np.ascontiguousarray(oracle.gaussian_kernel(X, X, 1000.0))
+    for lam in (1e-4, 1e-8):
+        x = oracle.refined_solve(K, b.labels, lam)
+        r = oracle.residual_dd(K, lam, x, b.labels)
+        # the refined residual sits at the rounding level of x itself
+        assert np.linalg.norm(r) <= 1e-14 * np.linalg.norm(K, 1) * np.linalg.norm(x)
+        x64 = oracle.cho_solve(K + lam * np.eye(K.shape[0]), b.labels)
+        assert np.linalg.norm(x64 - x) / np.linalg.norm(x) < 1e-3
+
+
+def test_residual_dd_exact_on_integers(oracle):
+    rng = np.random.default_rng(0)
+    A = rng.integers(-1000, 1000, size=(50, 50)).astype(np.float64)
+    A = A + A.T
+    x = rng.integers(-1000, 1000, size=50).astype(np.float64)
+    y = A @ x + 3.0 * x
+    assert np.array_equal(oracle.residual_dd(A, 3.0, x, y), np.zeros(50))
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "tests", "qm7")),
+                    reason="reference tree not mounted")
+def test_oracle_krr_cmat_reference_accuracy(oracle):
+    # tests/test_energy_krr_cmat.py:54-113 run on the oracle: MAE < 6.0
+    from qml_gb300.compound import Compound
+    energies = {}
+    with open(os.path.join(REF, "tests/data/hof_qm7.txt")) as f:
+        for line in f:
+            t = line.split()
+            energies[t[0]] = float(t[1])
+    mols = []
+    for name in sorted(energies.keys())[:1000]:
+        c = Compound(os.path.join(REF, "tests/qm7", name))
+        c.properties = energies[name]
+        mols.append(c)
+    np.random.seed(666)
+    np.random.shuffle(mols)
+    train, test = mols[:700], mols[-300:]
+    X = np.array([oracle.cm_sorted(m.nuclear_charges, m.coordinates, 23) for m in train])
+    Xs = np.array([oracle.cm_sorted(m.nuclear_charges, m.coordinates, 23) for m in test])
+    Y = np.array([m.properties for m in train])
+    Ys = np.array([m.properties for m in test])
+    sigma = 10 ** 4.2
+    K = oracle.laplacian_kernel(X, X, sigma)
+    K[np.diag_indices_from(K)] += 1e-10
+    alpha = oracle.cho_solve(K, Y)
+    Ks = oracle.laplacian_kernel(X, Xs, sigma)
+    mae = np.mean(np.abs(Ys - Ks.T @ alpha))
+    assert mae < 6.0
