@@ -317,17 +317,13 @@ def run_ours(a):
         fp64["fp64_report"] = rep_f
     del K, Kc
 
-    # our kernel launches in one step (CUDA activity of libqmlg kernels)
-    launches = None
-    try:
-        from torch.profiler import ProfilerActivity, profile
-        with profile(activities=[ProfilerActivity.CUDA]) as prof:
-            step()
-            torch.cuda.synchronize()
-        names = [e.name for e in prof.events() if e.device_type.name == "CUDA"]
-        launches = sum(1 for nme in names if "_kernel" in nme) * a.steps
-    except Exception:  # pragma: no cover - profiler unavailable
-        launches = None
+    # our kernel launches per step, counted by the library itself
+    lib = core.lib()
+    torch.cuda.synchronize()
+    c0 = lib.qmlg_launch_count()
+    step()
+    torch.cuda.synchronize()
+    launches = int(lib.qmlg_launch_count() - c0) * a.steps
 
     if rank != 0:
         return 0

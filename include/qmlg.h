@@ -41,6 +41,9 @@ const char *qmlg_version(void);
 /* Last CUDA error string seen by the library on this host thread ("" if none). */
 const char *qmlg_last_error(void);
 
+/* Number of CUDA kernels this library has launched in this process so far. */
+uint64_t qmlg_launch_count(void);
+
 /* ---- sorted Coulomb matrix --------------------------------------------- */
 
 /*

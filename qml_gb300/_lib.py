@@ -71,6 +71,7 @@ _SZ = ctypes.c_size_t
 SIGNATURES = {
     "qmlg_version": (ctypes.c_char_p, []),
     "qmlg_last_error": (ctypes.c_char_p, []),
+    "qmlg_launch_count": (ctypes.c_uint64, []),
     "qmlg_coulomb_matrix": (_I, [_P, _P, _P, _I, _I, _I, _P, _P, _P]),
     "qmlg_gaussian_kernel": (_I, [_P, _I64, _I, _P, _I64, _I, _I, _D, _P, _I64, _I, _D, _P]),
     "qmlg_laplacian_kernel": (_I, [_P, _I64, _I, _P, _I64, _I, _I, _D, _P, _I64, _I, _D, _P]),

@@ -279,12 +279,15 @@ symv_dd_partial_kernel(const double *__restrict__ A, int64_t lda, int n,
     for (int j0 = c0; j0 < min(n, c0 + RES_CHUNK); j0 += 64) {
         __syncthreads();
         // S[r][c] = A_sym(i0 + r, j0 + c)
+        // the two loops write disjoint elements: (j >= i or outside) / (j < i inside)
         for (int e = tid; e < 64 * 64; e += 256) {
             const int r = e >> 6, c = e & 63;
             const int i = i0 + r, j = j0 + c;
+            const bool inside = i < n && j < n;
+            if (inside && j < i) continue;
             double v = 0.0;
-            if (i < n && j < n && j > i) v = A[(int64_t)i * lda + j];
-            if (i < n && j < n && j == i) v = diag[i];
+            if (inside && j > i) v = A[(int64_t)i * lda + j];
+            if (inside && j == i) v = diag[i];
             S[r][c] = v;
         }
         for (int e = tid; e < 64 * 64; e += 256) {
@@ -391,12 +394,12 @@ namespace qmlg {
 int cholesky_fp64(double *A, int n, int64_t lda, double shift, int *d_info, cudaStream_t s)
 {
     for (int k0 = 0; k0 < n; k0 += NB) {
-        potrf_diag_kernel<<<1, 256, 0, s>>>(A, lda, n, k0, shift, d_info);
+        { potrf_diag_kernel<<<1, 256, 0, s>>>(A, lda, n, k0, shift, d_info); qmlg::count_launches(1); }
         const int below = n - (k0 + NB);
         if (below > 0) {
-            trsm_panel_kernel<<<(int)ceil_div(below, 64), 256, 0, s>>>(A, lda, n, k0, d_info);
+            { trsm_panel_kernel<<<(int)ceil_div(below, 64), 256, 0, s>>>(A, lda, n, k0, d_info); qmlg::count_launches(1); }
             const int64_t t = ceil_div(below, 64);
-            syrk_update_kernel<<<(unsigned)(t * (t + 1) / 2), 256, 0, s>>>(A, lda, n, k0, d_info);
+            { syrk_update_kernel<<<(unsigned)(t * (t + 1) / 2), 256, 0, s>>>(A, lda, n, k0, d_info); qmlg::count_launches(1); }
         }
     }
     return check_launch();
@@ -405,17 +408,17 @@ int cholesky_fp64(double *A, int n, int64_t lda, double shift, int *d_info, cuda
 int potrs_fp64(const double *A, int n, int64_t lda, double *x, cudaStream_t s)
 {
     for (int k0 = 0; k0 < n; k0 += NB) {
-        trsv_diag_fwd_kernel<<<1, NB, 0, s>>>(A, lda, n, k0, x);
+        { trsv_diag_fwd_kernel<<<1, NB, 0, s>>>(A, lda, n, k0, x); qmlg::count_launches(1); }
         const int below = n - (k0 + NB);
         if (below > 0)
-            gemv_fwd_update_kernel<<<(int)ceil_div((int64_t)below * 32, 256), 256, 0, s>>>(
-                A, lda, n, k0, x);
+            { gemv_fwd_update_kernel<<<(int)ceil_div((int64_t)below * 32, 256), 256, 0, s>>>(
+                A, lda, n, k0, x); qmlg::count_launches(1); }
     }
     const int last = (int)((n - 1) / NB) * NB;
     for (int k0 = last; k0 >= 0; k0 -= NB) {
-        trsv_diag_bwd_kernel<<<1, NB, 0, s>>>(A, lda, n, k0, x);
+        { trsv_diag_bwd_kernel<<<1, NB, 0, s>>>(A, lda, n, k0, x); qmlg::count_launches(1); }
         if (k0 > 0)
-            gemv_bwd_update_kernel<<<(int)ceil_div(k0, 256), 256, 0, s>>>(A, lda, n, k0, x);
+            { gemv_bwd_update_kernel<<<(int)ceil_div(k0, 256), 256, 0, s>>>(A, lda, n, k0, x); qmlg::count_launches(1); }
     }
     return check_launch();
 }
@@ -443,7 +446,7 @@ __global__ void mirror_kernel(double *__restrict__ A, int64_t lda, int n,
 int mirror_upper_to_lower(double *A, int n, int64_t lda, const double *diag, cudaStream_t s)
 {
     const int t = (int)ceil_div(n, 32);
-    mirror_kernel<<<dim3(t, t), dim3(32, 8), 0, s>>>(A, lda, n, diag);
+    { mirror_kernel<<<dim3(t, t), dim3(32, 8), 0, s>>>(A, lda, n, diag); qmlg::count_launches(1); }
     return check_launch();
 }
 
@@ -462,10 +465,10 @@ int emulated_factor(double *A, int n, int64_t lda, double shift, Workspace &ws, 
     int *expo = ws.take<int>((size_t)n);
     if (digits == nullptr || expo == nullptr) return QMLG_E_WORKSPACE;
     for (int k0 = 0; k0 < n; k0 += NB) {
-        potrf_diag_kernel<<<1, 256, 0, s>>>(A, lda, n, k0, shift, d_info);
+        { potrf_diag_kernel<<<1, 256, 0, s>>>(A, lda, n, k0, shift, d_info); qmlg::count_launches(1); }
         const int below = n - (k0 + NB);
         if (below > 0) {
-            trsm_panel_kernel<<<(int)ceil_div(below, 64), 256, 0, s>>>(A, lda, n, k0, d_info);
+            { trsm_panel_kernel<<<(int)ceil_div(below, 64), 256, 0, s>>>(A, lda, n, k0, d_info); qmlg::count_launches(1); }
             int st = emu_trailing_update(A, lda, n, k0, NB, slices, digits, expo, d_info, s);
             if (st != QMLG_OK) return st;
         }
@@ -495,10 +498,10 @@ int residual_dd(const double *A, int n, int64_t lda, const double *diag, double 
     const int nchunks = (int)ceil_div(n, RES_CHUNK);
     double2 *partial = ws.take<double2>((size_t)nchunks * n);
     if (partial == nullptr) return QMLG_E_WORKSPACE;
-    symv_dd_partial_kernel<<<dim3((unsigned)ceil_div(n, RES_ROWS), nchunks), 256, 0, s>>>(
-        A, lda, n, diag, x, partial);
-    residual_finish_kernel<<<(int)ceil_div(n, 256), 256, 0, s>>>(partial, nchunks, n, lambda, x,
-                                                                 y, r);
+    { symv_dd_partial_kernel<<<dim3((unsigned)ceil_div(n, RES_ROWS), nchunks), 256, 0, s>>>(
+        A, lda, n, diag, x, partial); qmlg::count_launches(1); }
+    { residual_finish_kernel<<<(int)ceil_div(n, 256), 256, 0, s>>>(partial, nchunks, n, lambda, x,
+                                                                 y, r); qmlg::count_launches(1); }
     return check_launch();
 }
 
@@ -616,7 +619,7 @@ int refine(SolveCtx &c, const QmlgRefineOpts &o, SolveFn solve_fn, QmlgSolveRepo
         if (st != QMLG_OK) return st;
         cudaError_t e = cudaMemsetAsync(c.d_sums, 0, 2 * sizeof(double), c.s);
         if (e != cudaSuccess) return qmlg::set_cuda_error(e);
-        axpy_norms_kernel<<<(int)qmlg::ceil_div(c.n, 256), 256, 0, c.s>>>(c.x, c.r, c.n, c.d_sums);
+        { axpy_norms_kernel<<<(int)qmlg::ceil_div(c.n, 256), 256, 0, c.s>>>(c.x, c.r, c.n, c.d_sums); qmlg::count_launches(1); }
         double h[2];
         e = cudaMemcpyAsync(h, c.d_sums, sizeof(h), cudaMemcpyDeviceToHost, c.s);
         if (e == cudaSuccess) e = cudaStreamSynchronize(c.s);
@@ -665,7 +668,7 @@ extern "C" int qmlg_solve(double *A, int n, int64_t lda, const double *y, double
     c.ws_mark = ws.used;
     cudaError_t e = cudaMemsetAsync(c.d_info, 0, sizeof(int), s);
     if (e != cudaSuccess) return qmlg::set_cuda_error(e);
-    copy_diag_kernel<<<(int)qmlg::ceil_div(n, 256), 256, 0, s>>>(A, lda, n, c.diag);
+    { copy_diag_kernel<<<(int)qmlg::ceil_div(n, 256), 256, 0, s>>>(A, lda, n, c.diag); qmlg::count_launches(1); }
 
     int st = QMLG_OK, info = 0;
     bool stalled = false;
@@ -704,7 +707,7 @@ extern "C" int qmlg_solve(double *A, int n, int64_t lda, const double *y, double
     if ((st = read_info(c, info)) != QMLG_OK) return st;
     rep.info = info;
     if (info != 0) {
-        fill_nan_kernel<<<(int)qmlg::ceil_div(n, 256), 256, 0, s>>>(x, n);
+        { fill_nan_kernel<<<(int)qmlg::ceil_div(n, 256), 256, 0, s>>>(x, n); qmlg::count_launches(1); }
         if (report) *report = rep;
         return info;
     }

@@ -11,6 +11,9 @@ namespace qmlg {
 // Records the CUDA error for qmlg_last_error() and maps it to a status code.
 int set_cuda_error(cudaError_t e);
 
+// Adds to the process-wide count of kernels this library has launched.
+void count_launches(unsigned n);
+
 inline int check_launch()
 {
     cudaError_t e = cudaGetLastError();

@@ -150,12 +150,13 @@ extern "C" int qmlg_coulomb_matrix(const double *charges, const double *coordina
                                    const int64_t *atom_offsets, int n_mol, int size,
                                    int sorting, double *out, int *status, void *stream)
 {
-    if (n_mol < 0 || size < 1 || atom_offsets == nullptr || out == nullptr) return QMLG_E_ARG;
+    if (n_mol < 0 || size < 1) return QMLG_E_ARG;
     if (n_mol == 0) return QMLG_OK;
+    if (atom_offsets == nullptr || out == nullptr) return QMLG_E_ARG;
     int st = upload_table();
     if (st != QMLG_OK) return st;
     const int blocks = (int)qmlg::ceil_div(n_mol, kWarpsPerBlock);
-    coulomb_kernel<<<blocks, kWarpsPerBlock * 32, 0, qmlg::as_stream(stream)>>>(
-        charges, coordinates, atom_offsets, n_mol, size, sorting ? 1 : 0, out, status);
+    { coulomb_kernel<<<blocks, kWarpsPerBlock * 32, 0, qmlg::as_stream(stream)>>>(
+        charges, coordinates, atom_offsets, n_mol, size, sorting ? 1 : 0, out, status); qmlg::count_launches(1); }
     return qmlg::check_launch();
 }

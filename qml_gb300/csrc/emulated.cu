@@ -194,8 +194,8 @@ int emu_trailing_update(double *A, int64_t lda, int n, int k0, int nb, int slice
     const int k1 = k0 + nb;
     const int rows = n - k1;
     if (rows <= 0) return QMLG_OK;
-    slice_panel_kernel<<<(int)ceil_div((int64_t)rows * 32, 256), 256, 0, s>>>(
-        A, lda, n, k0, nb, k1, slices, digits, expo, d_info);
+    { slice_panel_kernel<<<(int)ceil_div((int64_t)rows * 32, 256), 256, 0, s>>>(
+        A, lda, n, k0, nb, k1, slices, digits, expo, d_info); qmlg::count_launches(1); }
     const int64_t t = ceil_div(rows, TILE);
     const size_t smem = (size_t)2 * slices * TILE * KS * sizeof(__nv_bfloat16);
     static bool attr_set = false;
@@ -204,8 +204,8 @@ int emu_trailing_update(double *A, int64_t lda, int n, int k0, int nb, int slice
                              (int)((size_t)2 * kEmuMaxSlices * TILE * KS * sizeof(__nv_bfloat16)));
         attr_set = true;
     }
-    emu_syrk_kernel<<<(unsigned)(t * (t + 1) / 2), 256, smem, s>>>(A, lda, n, k1, slices, digits,
-                                                                   expo, d_info);
+    { emu_syrk_kernel<<<(unsigned)(t * (t + 1) / 2), 256, smem, s>>>(A, lda, n, k1, slices, digits,
+                                                                   expo, d_info); qmlg::count_launches(1); }
     return check_launch();
 }
 

@@ -256,11 +256,11 @@ int kernel_matrix(int kind, const double *A, int64_t lda, int na, const double *
     const int tj = (int)qmlg::ceil_div(na, TJ), ti = (int)qmlg::ceil_div(nb, TI);
     dim3 grid = symmetric ? dim3((unsigned)((int64_t)tj * (tj + 1) / 2)) : dim3(tj, ti);
     if (kind == kGauss)
-        kernel_matrix_kernel<kGauss><<<grid, NT, 0, s>>>(A, lda, na, B, ldb, nb, d, scale, K, ldk,
-                                                        symmetric, diag_shift);
+        { kernel_matrix_kernel<kGauss><<<grid, NT, 0, s>>>(A, lda, na, B, ldb, nb, d, scale, K, ldk,
+                                                        symmetric, diag_shift); qmlg::count_launches(1); }
     else
-        kernel_matrix_kernel<kLaplace><<<grid, NT, 0, s>>>(A, lda, na, B, ldb, nb, d, scale, K,
-                                                          ldk, symmetric, diag_shift);
+        { kernel_matrix_kernel<kLaplace><<<grid, NT, 0, s>>>(A, lda, na, B, ldb, nb, d, scale, K,
+                                                          ldk, symmetric, diag_shift); qmlg::count_launches(1); }
     return qmlg::check_launch();
 }
 
@@ -288,8 +288,8 @@ extern "C" int qmlg_predict_gemv(const double *Ks, int64_t ldk, int ntrain, int 
     if (ntrain < 0 || ntest < 0 || ldk < ntrain) return QMLG_E_ARG;
     if (ntest == 0) return QMLG_OK;
     if (Ks == nullptr || alpha == nullptr || yhat == nullptr) return QMLG_E_ARG;
-    gemv_t_kernel<<<(int)qmlg::ceil_div((int64_t)ntest * 32, 256), 256, 0,
-                    qmlg::as_stream(stream)>>>(Ks, ldk, ntrain, ntest, alpha, yhat);
+    { gemv_t_kernel<<<(int)qmlg::ceil_div((int64_t)ntest * 32, 256), 256, 0,
+                    qmlg::as_stream(stream)>>>(Ks, ldk, ntrain, ntest, alpha, yhat); qmlg::count_launches(1); }
     return qmlg::check_launch();
 }
 
@@ -322,11 +322,11 @@ extern "C" int qmlg_predict_fused(int kind, const double *Xtrain, int64_t ldtrai
     if (partial == nullptr) return QMLG_E_WORKSPACE;
     const double scale = kind == QMLG_KIND_GAUSSIAN ? -0.5 / (sigma * sigma) : -1.0 / sigma;
     if (kind == QMLG_KIND_GAUSSIAN)
-        predict_partial_kernel<kGauss><<<dim3(tj, ti), NT, 0, s>>>(
-            Xtrain, ldtrain, ntrain, Xtest, ldtest, ntest, d, scale, alpha, partial);
+        { predict_partial_kernel<kGauss><<<dim3(tj, ti), NT, 0, s>>>(
+            Xtrain, ldtrain, ntrain, Xtest, ldtest, ntest, d, scale, alpha, partial); qmlg::count_launches(1); }
     else
-        predict_partial_kernel<kLaplace><<<dim3(tj, ti), NT, 0, s>>>(
-            Xtrain, ldtrain, ntrain, Xtest, ldtest, ntest, d, scale, alpha, partial);
-    reduce_partial_kernel<<<(int)qmlg::ceil_div(ntest, 256), 256, 0, s>>>(partial, tj, ntest, yhat);
+        { predict_partial_kernel<kLaplace><<<dim3(tj, ti), NT, 0, s>>>(
+            Xtrain, ldtrain, ntrain, Xtest, ldtest, ntest, d, scale, alpha, partial); qmlg::count_launches(1); }
+    { reduce_partial_kernel<<<(int)qmlg::ceil_div(ntest, 256), 256, 0, s>>>(partial, tj, ntest, yhat); qmlg::count_launches(1); }
     return qmlg::check_launch();
 }
