@@ -32,6 +32,7 @@ extern "C" {
 #define QMLG_E_TOO_MANY_ATOMS (-4) /* a molecule has more atoms than size (or than 32) */
 #define QMLG_E_NOT_CONVERGED (-5)  /* refinement did not reach its tolerance */
 #define QMLG_E_TIMEOUT (-6)    /* a bounded device-side wait gave up */
+#define QMLG_E_TOO_LARGE (-7)  /* problem exceeds a fixed-size internal buffer */
 
 /* ---- library ---------------------------------------------------------- */
 
@@ -113,6 +114,24 @@ int qmlg_predict_fused(int kind, const double *Xtrain, int64_t ldtrain, int ntra
                        const double *Xtest, int64_t ldtest, int ntest, int d, double sigma,
                        const double *alpha, double *yhat, void *workspace, size_t ws_bytes,
                        void *stream);
+
+/*
+ * qmlg_predict_fused without a workspace, for callers that cannot allocate device
+ * memory (for example a serving process whose memory manager reserves all of its
+ * HBM at start-up and forbids later cudaMalloc calls, which synchronise the device
+ * and can fail under fragmentation).  No counterpart in the reference: the
+ * reference has no device memory at all.
+ * Scratch lives in a fixed 32 MiB array inside the library (reserved on every GPU
+ * that loads it, until exit); the call needs ceil(ntrain/64) * ntest <= 4194304
+ * and returns QMLG_E_TOO_LARGE beyond that.  It allocates nothing.  The first call
+ * on a device looks up the array's device address (cudaGetSymbolAddress) with that
+ * device current, so make that first call before any stream capture; the stream
+ * must belong to the current device.  All calls share the array: calls whose work
+ * overlaps on the GPU race and must be serialised by the caller.
+ */
+int qmlg_predict_fused_noalloc(int kind, const double *Xtrain, int64_t ldtrain, int ntrain,
+                               const double *Xtest, int64_t ldtest, int ntest, int d,
+                               double sigma, const double *alpha, double *yhat, void *stream);
 
 /* ---- Cholesky solve ------------------------------------------------------- */
 

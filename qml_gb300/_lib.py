@@ -20,6 +20,7 @@ QMLG_E_WORKSPACE = -3
 QMLG_E_TOO_MANY_ATOMS = -4
 QMLG_E_NOT_CONVERGED = -5
 QMLG_E_TIMEOUT = -6
+QMLG_E_TOO_LARGE = -7
 
 QMLG_KERNEL_SYMMETRIC = 1
 QMLG_KIND_GAUSSIAN = 0
@@ -34,6 +35,7 @@ _ERRORS = {
     QMLG_E_TOO_MANY_ATOMS: "a molecule has more atoms than size (or than 32)",
     QMLG_E_NOT_CONVERGED: "refinement did not converge",
     QMLG_E_TIMEOUT: "a bounded device wait gave up",
+    QMLG_E_TOO_LARGE: "problem exceeds a fixed-size internal buffer",
 }
 
 
@@ -78,6 +80,7 @@ SIGNATURES = {
     "qmlg_predict_gemv": (_I, [_P, _I64, _I, _I, _P, _P, _P]),
     "qmlg_predict_workspace_size": (_SZ, [_I, _I]),
     "qmlg_predict_fused": (_I, [_I, _P, _I64, _I, _P, _I64, _I, _I, _D, _P, _P, _P, _SZ, _P]),
+    "qmlg_predict_fused_noalloc": (_I, [_I, _P, _I64, _I, _P, _I64, _I, _I, _D, _P, _P, _P]),
     "qmlg_cholesky_workspace_size": (_SZ, [_I]),
     "qmlg_cholesky": (_I, [_P, _I, _I64, _D, _P, _SZ, _P]),
     "qmlg_cholesky_solve_factored": (_I, [_P, _I, _I64, _P, _P, _P]),

@@ -13,6 +13,7 @@
 // diagonal and writes the mirror through a shared-memory transpose, so K is
 // exactly symmetric.
 #include <cmath>
+#include <mutex>
 
 #include "common.cuh"
 
@@ -328,5 +329,90 @@ extern "C" int qmlg_predict_fused(int kind, const double *Xtrain, int64_t ldtrai
         { predict_partial_kernel<kLaplace><<<dim3(tj, ti), NT, 0, s>>>(
             Xtrain, ldtrain, ntrain, Xtest, ldtest, ntest, d, scale, alpha, partial); qmlg::count_launches(1); }
     { reduce_partial_kernel<<<(int)qmlg::ceil_div(ntest, 256), 256, 0, s>>>(partial, tj, ntest, yhat); qmlg::count_launches(1); }
+    return qmlg::check_launch();
+}
+
+// ---------------------------------------------------------------------------
+// Fused prediction for callers that cannot allocate device memory.
+//
+// Some callers cannot call cudaMalloc at all.  An example is a serving process
+// whose memory manager reserves its whole HBM budget at start-up and forbids later
+// allocations, because cudaMalloc synchronises the device and can fail mid-request
+// once memory is fragmented.  Such a caller may also be unable to size and hand
+// over a workspace.  This variant keeps its scratch (the per-training-tile partial
+// sums) in a fixed array compiled into the library, so the call allocates nothing.
+//
+// The array holds kNoAllocPartials doubles (32 MiB).  Every GPU that loads the
+// library keeps it reserved until the process exits.  A call needs
+// ceil(ntrain / 64) * ntest partial sums and is rejected with QMLG_E_TOO_LARGE
+// beyond that.  Every partial sum is written before it is read, so nothing has
+// to be cleared between calls.  All calls share the one array, so calls whose
+// work overlaps on the GPU (different streams, or different host threads) race
+// on it and must be serialised by the caller.
+// ---------------------------------------------------------------------------
+
+namespace {
+
+constexpr size_t kNoAllocPartials = (size_t)4 << 20;  // doubles: 32 MiB
+constexpr int kNoAllocMaxDevices = 64;
+
+__device__ __align__(256) double g_noalloc_partials[kNoAllocPartials];
+
+std::mutex g_noalloc_mutex;
+double *g_noalloc_address[kNoAllocMaxDevices] = {};
+
+// Device address of the array on the current device.  The host-side symbol is
+// only a stand-in, so the address is looked up once per device (with that device
+// current) and cached.
+int noalloc_scratch(double **out)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return QMLG_E_ARG;
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (g_noalloc_address[dev] == nullptr) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+        if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+        g_noalloc_address[dev] = static_cast<double *>(p);
+    }
+    *out = g_noalloc_address[dev];
+    return QMLG_OK;
+}
+
+}  // namespace
+
+extern "C" int qmlg_predict_fused_noalloc(int kind, const double *Xtrain, int64_t ldtrain,
+                                          int ntrain, const double *Xtest, int64_t ldtest,
+                                          int ntest, int d, double sigma, const double *alpha,
+                                          double *yhat, void *stream)
+{
+    if (kind != QMLG_KIND_GAUSSIAN && kind != QMLG_KIND_LAPLACIAN) return QMLG_E_ARG;
+    int st = check_common(Xtrain, ldtrain, ntrain, Xtest, ldtest, ntest, d, sigma);
+    if (st != QMLG_OK) return st;
+    if (ntest == 0) return QMLG_OK;
+    if (yhat == nullptr || (ntrain > 0 && alpha == nullptr)) return QMLG_E_ARG;
+    cudaStream_t s = qmlg::as_stream(stream);
+    if (ntrain == 0) {
+        cudaError_t e = cudaMemsetAsync(yhat, 0, sizeof(double) * (size_t)ntest, s);
+        return e == cudaSuccess ? QMLG_OK : qmlg::set_cuda_error(e);
+    }
+    const int tj = (int)qmlg::ceil_div(ntrain, TJ), ti = (int)qmlg::ceil_div(ntest, TI);
+    if ((size_t)tj * (size_t)ntest > kNoAllocPartials) return QMLG_E_TOO_LARGE;
+    double *partial = nullptr;
+    st = noalloc_scratch(&partial);
+    if (st != QMLG_OK) return st;
+    const double scale = kind == QMLG_KIND_GAUSSIAN ? -0.5 / (sigma * sigma) : -1.0 / sigma;
+    if (kind == QMLG_KIND_GAUSSIAN) {
+        predict_partial_kernel<kGauss><<<dim3(tj, ti), NT, 0, s>>>(
+            Xtrain, ldtrain, ntrain, Xtest, ldtest, ntest, d, scale, alpha, partial);
+    } else {
+        predict_partial_kernel<kLaplace><<<dim3(tj, ti), NT, 0, s>>>(
+            Xtrain, ldtrain, ntrain, Xtest, ldtest, ntest, d, scale, alpha, partial);
+    }
+    qmlg::count_launches(1);
+    reduce_partial_kernel<<<(int)qmlg::ceil_div(ntest, 256), 256, 0, s>>>(partial, tj, ntest, yhat);
+    qmlg::count_launches(1);
     return qmlg::check_launch();
 }
