@@ -136,7 +136,7 @@ int qmlg_predict_fused_noalloc(int kind, const double *Xtrain, int64_t ldtrain, 
 /* ---- Cholesky solve ------------------------------------------------------- */
 
 #define QMLG_PREC_FP64 0   /* plain FP64 blocked Cholesky (LAPACK dpotrf semantics) */
-#define QMLG_PREC_MIXED 1  /* FP32 factor of a shifted copy + FP64 GMRES refinement */
+#define QMLG_PREC_MIXED 1  /* emulated-FP64 tensor-core factor + double-double refinement */
 
 typedef struct QmlgSolveReport {
     int precision_used;     /* QMLG_PREC_* of the factor the answer came from */
@@ -170,6 +170,19 @@ int qmlg_cholesky(double *A, int n, int64_t lda, double lambda, void *workspace,
                   size_t ws_bytes, void *stream);
 
 /*
+ * The same factorisation with the O(n^3) trailing updates emulated to FP64 accuracy
+ * on the bf16 tensor cores (tcgen05): every panel row is scaled by a power of two
+ * and cut into 8 base-128 digits; the digit-plane products are summed exactly in
+ * FP32 tensor memory and merged into FP64 once per element.  Diagonal blocks and
+ * panel solves stay in FP64.  Same storage, same info as qmlg_cholesky; the factor
+ * agrees with it to FP64 rounding level (not bit for bit).  Returns
+ * QMLG_E_TIMEOUT if a bounded device-side wait gave up.
+ */
+size_t qmlg_cholesky_mixed_workspace_size(int n);
+int qmlg_cholesky_mixed(double *A, int n, int64_t lda, double lambda, void *workspace,
+                        size_t ws_bytes, void *stream);
+
+/*
  * x = (U^T U)^{-1} y with U from qmlg_cholesky: dpotrs("U", nrhs=1)
  * (qml/fcho_solve.f90:46).  x and y may alias.
  */
@@ -179,11 +192,12 @@ int qmlg_cholesky_solve_factored(const double *U, int n, int64_t lda, const doub
 /*
  * Full solve (A + lambda I) x = y, the fcho_solve of qml/fcho_solve.f90:23-52 with
  * the KRR lambda folded in.  precision QMLG_PREC_FP64 factorises A in place like
- * the reference (upper triangle overwritten); QMLG_PREC_MIXED leaves A intact,
- * factorises a shifted FP32 copy in the workspace, and refines in FP64 with
- * GMRES on a double-double residual, falling back to an FP64 factorisation when
- * refinement stalls (opts->allow_fallback; then A's upper triangle is
- * overwritten as in FP64 mode).  opts and report may be NULL.
+ * the reference (upper triangle overwritten); QMLG_PREC_MIXED factorises in place
+ * the same way with qmlg_cholesky_mixed, then refines with a double-double
+ * residual read from the untouched triangle, and falls back to a plain FP64
+ * refactorisation when refinement stalls (opts->allow_fallback).  In both modes
+ * the column-major strictly lower triangle of A is never written.  opts and
+ * report may be NULL.
  * The call synchronises the stream (refinement decisions are taken on the host).
  */
 size_t qmlg_solve_workspace_size(int n, int precision);

@@ -83,6 +83,8 @@ SIGNATURES = {
     "qmlg_predict_fused_noalloc": (_I, [_I, _P, _I64, _I, _P, _I64, _I, _I, _D, _P, _P, _P]),
     "qmlg_cholesky_workspace_size": (_SZ, [_I]),
     "qmlg_cholesky": (_I, [_P, _I, _I64, _D, _P, _SZ, _P]),
+    "qmlg_cholesky_mixed_workspace_size": (_SZ, [_I]),
+    "qmlg_cholesky_mixed": (_I, [_P, _I, _I64, _D, _P, _SZ, _P]),
     "qmlg_cholesky_solve_factored": (_I, [_P, _I, _I64, _P, _P, _P]),
     "qmlg_solve_workspace_size": (_SZ, [_I, _I]),
     "qmlg_solve": (_I, [_P, _I, _I64, _P, _P, _D, _I, ctypes.POINTER(QmlgRefineOpts),

@@ -220,15 +220,22 @@ def solve(A: torch.Tensor, y: torch.Tensor, lam: float = 0.0, precision: str = "
     return x, report
 
 
-def cholesky(A: torch.Tensor, lam: float = 0.0) -> int:
-    """In-place FP64 Cholesky with dpotrf("U") semantics; returns LAPACK's info."""
+def cholesky(A: torch.Tensor, lam: float = 0.0, precision: str = "fp64") -> int:
+    """In-place Cholesky with dpotrf("U") semantics; returns LAPACK's info.
+    precision "mixed" emulates the trailing updates on the bf16 tensor cores."""
     _require_cuda(A)
     Acm, lda = _colmajor(A)
     n = Acm.shape[0]
-    ws_bytes = lib().qmlg_cholesky_workspace_size(n)
+    if precision == "mixed":
+        size_fn, fn, name = (lib().qmlg_cholesky_mixed_workspace_size, lib().qmlg_cholesky_mixed,
+                             "qmlg_cholesky_mixed")
+    else:
+        size_fn, fn, name = (lib().qmlg_cholesky_workspace_size, lib().qmlg_cholesky,
+                             "qmlg_cholesky")
+    ws_bytes = size_fn(n)
     ws = workspaces.get(ws_bytes, A.device)
-    return check(lib().qmlg_cholesky(Acm.data_ptr(), n, lda, float(lam), ws.data_ptr(),
-                                     ws.numel(), _stream(A.device)), "qmlg_cholesky")
+    return check(fn(Acm.data_ptr(), n, lda, float(lam), ws.data_ptr(), ws.numel(),
+                    _stream(A.device)), name)
 
 
 def cholesky_solve_factored(U: torch.Tensor, y: torch.Tensor) -> torch.Tensor:

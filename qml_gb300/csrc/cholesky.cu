@@ -450,34 +450,81 @@ int mirror_upper_to_lower(double *A, int n, int64_t lda, const double *diag, cud
     return check_launch();
 }
 
+// Two-level emulated-FP64 factorisation.  Outer panels of NBO = 512 columns: inside
+// a panel, 64-column steps (FP64 diagonal block and TRSM, emulated update of the
+// panel's remaining columns with K = 64); after the panel, one emulated rank-512
+// update of the whole trailing matrix (K = 512, exact levels, one FP64 epilogue per
+// element).
+constexpr int NBO = 512;
+
 size_t emulated_factor_ws(int n)
 {
+    const size_t rpad = (size_t)ceil_div(n < 1 ? 1 : n, 128) * 128;
     WorkspacePlan p;
-    p.add<__nv_bfloat16>((size_t)kEmuMaxSlices * (size_t)n * 64);
-    p.add<int>((size_t)n);
+    p.add<__nv_bfloat16>((size_t)kEmuMaxSlices * rpad * NBO);  // outer panel digits
+    p.add<int>(rpad);
+    p.add<__nv_bfloat16>((size_t)kEmuMaxSlices * rpad * NB);   // inner block digits
+    p.add<int>(rpad);
+    p.add<int>(4);                                             // device error flag
     return p.total();
 }
 
 int emulated_factor(double *A, int n, int64_t lda, double shift, Workspace &ws, int *d_info,
                     EmulatedFactor &f, cudaStream_t s, int slices)
 {
-    __nv_bfloat16 *digits = ws.take<__nv_bfloat16>((size_t)slices * (size_t)n * 64);
-    int *expo = ws.take<int>((size_t)n);
-    if (digits == nullptr || expo == nullptr) return QMLG_E_WORKSPACE;
-    for (int k0 = 0; k0 < n; k0 += NB) {
-        { potrf_diag_kernel<<<1, 256, 0, s>>>(A, lda, n, k0, shift, d_info); qmlg::count_launches(1); }
-        const int below = n - (k0 + NB);
-        if (below > 0) {
-            { trsm_panel_kernel<<<(int)ceil_div(below, 64), 256, 0, s>>>(A, lda, n, k0, d_info); qmlg::count_launches(1); }
-            int st = emu_trailing_update(A, lda, n, k0, NB, slices, digits, expo, d_info, s);
-            if (st != QMLG_OK) return st;
+    const int rpad = (int)ceil_div(n, 128) * 128;
+    __nv_bfloat16 *dig_out = ws.take<__nv_bfloat16>((size_t)kEmuMaxSlices * rpad * NBO);
+    int *exp_out = ws.take<int>((size_t)rpad);
+    __nv_bfloat16 *dig_in = ws.take<__nv_bfloat16>((size_t)kEmuMaxSlices * rpad * NB);
+    int *exp_in = ws.take<int>((size_t)rpad);
+    int *d_err = ws.take<int>(4);
+    if (dig_out == nullptr || exp_out == nullptr || dig_in == nullptr || exp_in == nullptr ||
+        d_err == nullptr)
+        return QMLG_E_WORKSPACE;
+    cudaError_t e = cudaMemsetAsync(d_err, 0, sizeof(int), s);
+    if (e != cudaSuccess) return set_cuda_error(e);
+    int st = QMLG_OK;
+    for (int K0 = 0; K0 < n && st == QMLG_OK; K0 += NBO) {
+        const int K1 = min(K0 + NBO, n);
+        for (int k0 = K0; k0 < K1; k0 += NB) {
+            { potrf_diag_kernel<<<1, 256, 0, s>>>(A, lda, n, k0, shift, d_info); count_launches(1); }
+            const int r1 = k0 + NB;
+            if (r1 >= n) break;
+            { trsm_panel_kernel<<<(int)ceil_div(n - r1, 64), 256, 0, s>>>(A, lda, n, k0, d_info); count_launches(1); }
+            if (r1 < K1) {
+                st = slice_rows(A, lda, r1, n - r1, k0, NB, NB, rpad, slices, dig_in, exp_in, d_info, s);
+                if (st == QMLG_OK)
+                    st = emu_tc_update(A, lda, r1, K1, r1, n, dig_in, exp_in, NB, rpad, slices, 0, 0, 1,
+                                       d_err, s);
+                if (st != QMLG_OK) break;
+            }
+        }
+        if (st == QMLG_OK && K1 < n) {
+            const int kw = K1 - K0;
+            const int kp = (int)ceil_div(kw, 64) * 64;
+            st = slice_rows(A, lda, K1, n - K1, K0, kw, kp, rpad, slices, dig_out, exp_out, d_info, s);
+            if (st == QMLG_OK)
+                st = emu_tc_update(A, lda, K1, n, K1, n, dig_out, exp_out, kp, rpad, slices, 0, 0, 1,
+                                   d_err, s);
         }
     }
+    if (st != QMLG_OK) return st;
     f.A = A;
     f.n = n;
     f.lda = lda;
     f.slices = slices;
+    f.d_err = d_err;
     return check_launch();
+}
+
+// QMLG_E_TIMEOUT if a bounded tensor-core wait gave up (the flag is set on device).
+int read_device_flag(const int *d_flag, cudaStream_t s)
+{
+    int h = 0;
+    cudaError_t e = cudaMemcpyAsync(&h, d_flag, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return set_cuda_error(e);
+    return h != 0 ? QMLG_E_TIMEOUT : QMLG_OK;
 }
 
 int emulated_potrs(const EmulatedFactor &f, double *x, cudaStream_t s)
@@ -528,6 +575,36 @@ extern "C" int qmlg_cholesky(double *A, int n, int64_t lda, double lambda, void 
     if (e != cudaSuccess) return qmlg::set_cuda_error(e);
     int st = qmlg::cholesky_fp64(A, n, lda, lambda, d_info, s);
     if (st != QMLG_OK) return st;
+    int info = 0;
+    e = cudaMemcpyAsync(&info, d_info, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+    return info;
+}
+
+extern "C" size_t qmlg_cholesky_mixed_workspace_size(int n)
+{
+    qmlg::WorkspacePlan p;
+    p.add<int>(4);
+    p.add<char>(qmlg::emulated_factor_ws(n));
+    return p.total();
+}
+
+extern "C" int qmlg_cholesky_mixed(double *A, int n, int64_t lda, double lambda, void *workspace,
+                                   size_t ws_bytes, void *stream)
+{
+    if (n < 0 || lda < n || (n > 0 && A == nullptr)) return QMLG_E_ARG;
+    if (n == 0) return QMLG_OK;
+    if (ws_bytes < qmlg_cholesky_mixed_workspace_size(n)) return QMLG_E_WORKSPACE;
+    qmlg::Workspace ws(workspace, ws_bytes);
+    int *d_info = ws.take<int>(4);
+    cudaStream_t s = qmlg::as_stream(stream);
+    cudaError_t e = cudaMemsetAsync(d_info, 0, sizeof(int), s);
+    if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+    qmlg::EmulatedFactor f;
+    int st = qmlg::emulated_factor(A, n, lda, lambda, ws, d_info, f, s);
+    if (st != QMLG_OK) return st;
+    if ((st = qmlg::read_device_flag(f.d_err, s)) != QMLG_OK) return st;
     int info = 0;
     e = cudaMemcpyAsync(&info, d_info, sizeof(int), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -678,6 +755,7 @@ extern "C" int qmlg_solve(double *A, int n, int64_t lda, const double *y, double
         st = qmlg::emulated_factor(A, n, lda, lambda, ws, c.d_info, f, s);
         if (st != QMLG_OK) return st;
         if ((st = read_info(c, info)) != QMLG_OK) return st;
+        if ((st = qmlg::read_device_flag(f.d_err, s)) != QMLG_OK) return st;
         rep.info = info;
         if (info == 0) {
             e = cudaMemcpyAsync(x, y, sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice, s);

@@ -1,4 +1,5 @@
-// Emulated-FP64 products on the bf16 tensor cores (declarations).
+// Emulated-FP64 products on the bf16 tensor cores (declarations; kernels in
+// emulated_tc.cu, the factorisation driver in cholesky.cu).
 //
 // GB300 runs FP64 at about 1.2 TFLOP/s, so FP64-accurate contractions are formed
 // from exact integer products on the bf16 tensor cores instead (the splitting idea
@@ -21,11 +22,17 @@ namespace qmlg {
 
 constexpr int kEmuMaxSlices = 8;
 
-// Trailing update C <- C - P P^T of the blocked Cholesky (rows/cols k0+nb .. n of the
-// row-major lower triangle, P = the nb-wide panel at column k0), with P cut into
-// `slices` digit planes.  digits: [slices][n][64] bf16, expo: [n] int (workspace).
-int emu_trailing_update(double *A, int64_t lda, int n, int k0, int nb, int slices,
-                        __nv_bfloat16 *digits, int *expo, const int *d_info, cudaStream_t s);
+// tcgen05 path (emulated_tc.cu).
+// Digit planes of rows r0 .. r0+nrows-1, columns c0 .. c0+kw-1 of a row-major matrix:
+// digits [slices][rpad][kp] bf16 (kp a multiple of 64, zero-padded), expo [rpad].
+int slice_rows(const double *A, int64_t lda, int r0, int nrows, int c0, int kw, int kp, int rpad,
+               int slices, __nv_bfloat16 *digits, int *expo, const int *d_info, cudaStream_t s);
+// C[i][j] -= sum_k P[i][k] P[j][k] for j in [jbase, jend), i in [ibase, iend) (j <= i
+// when lower), P rows taken from the digit planes (digit row = a_row0 + j - jbase for
+// the j side, b_row0 + i - ibase for the i side), K = kp <= 512.
+int emu_tc_update(double *C, int64_t ldc, int jbase, int jend, int ibase, int iend,
+                  const __nv_bfloat16 *digits, const int *expo, int kp, int rpad, int slices,
+                  int a_row0, int b_row0, int lower, int *d_err, cudaStream_t s);
 
 // In-place factor with emulated trailing updates; storage as the FP64 factor.
 struct EmulatedFactor {
@@ -33,12 +40,14 @@ struct EmulatedFactor {
     int n = 0;
     int64_t lda = 0;
     int slices = 0;
+    int *d_err = nullptr;  // device flag: a bounded tensor-core wait gave up
 };
 
 size_t emulated_factor_ws(int n);
 int emulated_factor(double *A, int n, int64_t lda, double shift, Workspace &ws, int *d_info,
                     EmulatedFactor &f, cudaStream_t s, int slices = 8);
 int emulated_potrs(const EmulatedFactor &f, double *x, cudaStream_t s);
+int read_device_flag(const int *d_flag, cudaStream_t s);
 
 // Shared with the FP64 path (cholesky.cu).
 int cholesky_fp64(double *A, int n, int64_t lda, double shift, int *d_info, cudaStream_t s);

@@ -134,3 +134,31 @@ def test_residual_dd_exact(cuda):
     r = core.residual_dd(At, torch.from_numpy(np.diag(A).copy()).to(cuda), 3.0,
                          torch.from_numpy(x).to(cuda), torch.from_numpy(y).to(cuda))
     assert np.array_equal(r.cpu().numpy(), np.zeros(130))
+
+
+@pytest.mark.parametrize("n", [65, 700, 1100, 1500])
+def test_mixed_factor_matches_fp64_factor(cuda, oracle, krr_system, n):
+    # the tensor-core factor (emulated FP64 trailing updates) against the plain FP64 one
+    X, _ = krr_system
+    K = np.ascontiguousarray(oracle.gaussian_kernel(X[:n], X[:n], 500.0))
+    lam = 1e-4
+    Fm = torch.from_numpy(K).to(cuda)
+    Fd = torch.from_numpy(K).to(cuda)
+    assert core.cholesky(Fm, lam, precision="mixed") == 0
+    assert core.cholesky(Fd, lam, precision="fp64") == 0
+    Lm = np.tril(Fm.cpu().numpy())
+    Ld = np.tril(Fd.cpu().numpy())
+    assert np.max(np.abs(Lm - Ld)) <= 1e-11 * np.max(np.abs(Ld))
+    # the other triangle is never written
+    assert np.array_equal(np.triu(Fm.cpu().numpy(), 1), np.triu(K, 1))
+
+
+def test_mixed_factor_info(cuda):
+    from scipy.linalg import lapack
+    rng = np.random.default_rng(2)
+    M = rng.normal(size=(700, 700))
+    S = M @ M.T + np.eye(700)
+    S[600, 600] = -5.0
+    _, info = lapack.dpotrf(np.asfortranarray(S), lower=0)
+    St = torch.from_numpy(np.ascontiguousarray(S.T)).to(cuda)
+    assert core.cholesky(St, precision="mixed") == info
