@@ -92,6 +92,23 @@ int qmlg_laplacian_kernel(const double *A, int64_t lda, int na, const double *B,
                           int nb, int d, double sigma, double *K, int64_t ldk, int flags,
                           double diag_shift, void *stream);
 
+/*
+ * Gaussian kernel with the contraction a.b emulated to FP64 accuracy on the bf16
+ * tensor cores (tcgen05): rows are scaled by powers of two and cut into base-128
+ * digit planes; the digit products are summed exactly in tensor memory and
+ * merged, |a|^2 + |b|^2 - 2 a.b and exp are evaluated in FP64 in the epilogue.
+ * The number of digit planes is chosen from a worst-case bound so that every
+ * entry stays within 1e-12 relative of the FP64 kernel; when no plane count up to
+ * 8 reaches it (very small sigma) the FP64 kernel above runs instead.  Same
+ * layout, flags and diag_shift as qmlg_gaussian_kernel.  Synchronises the stream
+ * once (the bound needs max |x| on the host).  ws: the size call below.
+ */
+size_t qmlg_gaussian_kernel_emulated_workspace_size(int na, int nb, int d, int flags);
+int qmlg_gaussian_kernel_emulated(const double *A, int64_t lda, int na, const double *B,
+                                  int64_t ldb, int nb, int d, double sigma, double *K,
+                                  int64_t ldk, int flags, double diag_shift, void *workspace,
+                                  size_t ws_bytes, void *stream);
+
 /* ---- prediction ----------------------------------------------------------- */
 
 #define QMLG_KIND_GAUSSIAN 0
@@ -132,6 +149,17 @@ int qmlg_predict_fused(int kind, const double *Xtrain, int64_t ldtrain, int ntra
 int qmlg_predict_fused_noalloc(int kind, const double *Xtrain, int64_t ldtrain, int ntrain,
                                const double *Xtest, int64_t ldtest, int ntest, int d,
                                double sigma, const double *alpha, double *yhat, void *stream);
+
+/*
+ * Gaussian prediction yhat[i] = sum_j k(Xtrain_j, Xtest_i) alpha[j] with the kernel
+ * formed on the tensor cores as in qmlg_gaussian_kernel_emulated and reduced in
+ * the epilogue (Ks is never written); deterministic fixed-order reduction.
+ */
+size_t qmlg_predict_emulated_workspace_size(int ntrain, int ntest, int d);
+int qmlg_predict_emulated(const double *Xtrain, int64_t ldtrain, int ntrain,
+                          const double *Xtest, int64_t ldtest, int ntest, int d, double sigma,
+                          const double *alpha, double *yhat, void *workspace, size_t ws_bytes,
+                          void *stream);
 
 /* ---- Cholesky solve ------------------------------------------------------- */
 
@@ -181,6 +209,17 @@ int qmlg_cholesky(double *A, int n, int64_t lda, double lambda, void *workspace,
 size_t qmlg_cholesky_mixed_workspace_size(int n);
 int qmlg_cholesky_mixed(double *A, int n, int64_t lda, double lambda, void *workspace,
                         size_t ws_bytes, void *stream);
+
+/*
+ * The trailing update of qmlg_cholesky_mixed on its own: C <- C - P P^T on the
+ * lower triangle of the row-major n x n matrix C (the column-major upper one),
+ * P row-major n x k (k <= 512), the products emulated to FP64 accuracy with 8
+ * digit planes on the tensor cores.  Exposed for timing and for callers that
+ * assemble their own blocked factorisations.
+ */
+size_t qmlg_syrk_emulated_workspace_size(int n, int k);
+int qmlg_syrk_emulated(double *C, int64_t ldc, int n, const double *P, int64_t ldp, int k,
+                       void *workspace, size_t ws_bytes, void *stream);
 
 /*
  * x = (U^T U)^{-1} y with U from qmlg_cholesky: dpotrs("U", nrhs=1)

@@ -77,6 +77,11 @@ SIGNATURES = {
     "qmlg_coulomb_matrix": (_I, [_P, _P, _P, _I, _I, _I, _P, _P, _P]),
     "qmlg_gaussian_kernel": (_I, [_P, _I64, _I, _P, _I64, _I, _I, _D, _P, _I64, _I, _D, _P]),
     "qmlg_laplacian_kernel": (_I, [_P, _I64, _I, _P, _I64, _I, _I, _D, _P, _I64, _I, _D, _P]),
+    "qmlg_gaussian_kernel_emulated_workspace_size": (_SZ, [_I, _I, _I, _I]),
+    "qmlg_gaussian_kernel_emulated": (_I, [_P, _I64, _I, _P, _I64, _I, _I, _D, _P, _I64, _I, _D,
+                                           _P, _SZ, _P]),
+    "qmlg_predict_emulated_workspace_size": (_SZ, [_I, _I, _I]),
+    "qmlg_predict_emulated": (_I, [_P, _I64, _I, _P, _I64, _I, _I, _D, _P, _P, _P, _SZ, _P]),
     "qmlg_predict_gemv": (_I, [_P, _I64, _I, _I, _P, _P, _P]),
     "qmlg_predict_workspace_size": (_SZ, [_I, _I]),
     "qmlg_predict_fused": (_I, [_I, _P, _I64, _I, _P, _I64, _I, _I, _D, _P, _P, _P, _SZ, _P]),
@@ -85,6 +90,8 @@ SIGNATURES = {
     "qmlg_cholesky": (_I, [_P, _I, _I64, _D, _P, _SZ, _P]),
     "qmlg_cholesky_mixed_workspace_size": (_SZ, [_I]),
     "qmlg_cholesky_mixed": (_I, [_P, _I, _I64, _D, _P, _SZ, _P]),
+    "qmlg_syrk_emulated_workspace_size": (_SZ, [_I, _I]),
+    "qmlg_syrk_emulated": (_I, [_P, _I64, _I, _P, _I64, _I, _P, _SZ, _P]),
     "qmlg_cholesky_solve_factored": (_I, [_P, _I, _I64, _P, _P, _P]),
     "qmlg_solve_workspace_size": (_SZ, [_I, _I]),
     "qmlg_solve": (_I, [_P, _I, _I64, _P, _P, _D, _I, ctypes.POINTER(QmlgRefineOpts),

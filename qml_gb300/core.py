@@ -98,9 +98,11 @@ def _rows(X: torch.Tensor) -> Tuple[torch.Tensor, int]:
 
 def kernel_matrix(kind: str, A: torch.Tensor, B: torch.Tensor, sigma: float,
                   symmetric: bool = False, diag_shift: float = 0.0,
-                  out: Optional[torch.Tensor] = None) -> torch.Tensor:
+                  out: Optional[torch.Tensor] = None, emulated: bool = False) -> torch.Tensor:
     """K (na, nb), Fortran-ordered like the reference, as a (na, nb) view of a
-    column-major buffer.  symmetric=True requires B is A."""
+    column-major buffer.  symmetric=True requires B is A.  emulated=True (Gaussian
+    only) forms the contraction on the tensor cores (qmlg_gaussian_kernel_emulated,
+    within 1e-12 of the FP64 kernel)."""
     _require_cuda(A, B)
     A, lda = _rows(A)
     if symmetric:
@@ -116,8 +118,17 @@ def kernel_matrix(kind: str, A: torch.Tensor, B: torch.Tensor, sigma: float,
         if out.shape != (na, nb) or out.stride() != (1, na):
             raise ValueError("out must be a Fortran-ordered (na, nb) float64 tensor")
         buf = out.T
-    fn = lib().qmlg_gaussian_kernel if kind == "gaussian" else lib().qmlg_laplacian_kernel
     flags = _lib.QMLG_KERNEL_SYMMETRIC if symmetric else 0
+    if emulated and kind == "gaussian":
+        ws_bytes = lib().qmlg_gaussian_kernel_emulated_workspace_size(na, nb, d, flags)
+        ws = workspaces.get(ws_bytes, A.device)
+        check(lib().qmlg_gaussian_kernel_emulated(A.data_ptr(), lda, na, B.data_ptr(), ldb, nb, d,
+                                                  float(sigma), buf.data_ptr(), na, flags,
+                                                  float(diag_shift), ws.data_ptr(), ws.numel(),
+                                                  _stream(A.device)),
+              "qmlg_gaussian_kernel_emulated")
+        return buf.T
+    fn = lib().qmlg_gaussian_kernel if kind == "gaussian" else lib().qmlg_laplacian_kernel
     check(fn(A.data_ptr(), lda, na, B.data_ptr(), ldb, nb, d, float(sigma), buf.data_ptr(), na,
              flags, float(diag_shift), _stream(A.device)), "qmlg_%s_kernel" % kind)
     return buf.T
@@ -134,8 +145,10 @@ def laplacian_kernel(A, B, sigma, **kw):
 # ------------------------------------------------------------------ predict --
 
 def predict(kind: str, Xtrain: torch.Tensor, Xtest: torch.Tensor, sigma: float,
-            alpha: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
-    """yhat = K(Xtest, Xtrain) alpha without materialising the kernel matrix."""
+            alpha: torch.Tensor, out: Optional[torch.Tensor] = None,
+            emulated: bool = False) -> torch.Tensor:
+    """yhat = K(Xtest, Xtrain) alpha without materialising the kernel matrix.
+    emulated=True (Gaussian only) uses the tensor-core contraction."""
     _require_cuda(Xtrain, Xtest, alpha)
     Xtrain, ldtr = _rows(Xtrain)
     Xtest, ldte = _rows(Xtest)
@@ -143,6 +156,14 @@ def predict(kind: str, Xtrain: torch.Tensor, Xtest: torch.Tensor, sigma: float,
     ntr, nte, d = Xtrain.shape[0], Xtest.shape[0], Xtrain.shape[1]
     if out is None:
         out = torch.empty(nte, dtype=torch.float64, device=Xtrain.device)
+    if emulated and kind == "gaussian":
+        ws_bytes = lib().qmlg_predict_emulated_workspace_size(ntr, nte, d)
+        ws = workspaces.get(ws_bytes, Xtrain.device)
+        check(lib().qmlg_predict_emulated(Xtrain.data_ptr(), ldtr, ntr, Xtest.data_ptr(), ldte, nte,
+                                          d, float(sigma), alpha.data_ptr(), out.data_ptr(),
+                                          ws.data_ptr(), ws.numel(), _stream(Xtrain.device)),
+              "qmlg_predict_emulated")
+        return out
     ws_bytes = lib().qmlg_predict_workspace_size(ntr, nte)
     ws = workspaces.get(ws_bytes, Xtrain.device)
     check(lib().qmlg_predict_fused(_KINDS[kind], Xtrain.data_ptr(), ldtr, ntr, Xtest.data_ptr(),
@@ -236,6 +257,21 @@ def cholesky(A: torch.Tensor, lam: float = 0.0, precision: str = "fp64") -> int:
     ws = workspaces.get(ws_bytes, A.device)
     return check(fn(Acm.data_ptr(), n, lda, float(lam), ws.data_ptr(), ws.numel(),
                     _stream(A.device)), name)
+
+
+def syrk_emulated(C: torch.Tensor, P: torch.Tensor) -> None:
+    """C <- C - P P^T on C's row-major lower triangle, emulated FP64 on the tensor
+    cores (the trailing update of the mixed factorisation).  C (n, n) row-major,
+    P (n, k) row-major, k <= 512."""
+    _require_cuda(C, P)
+    n, k = P.shape
+    if C.shape != (n, n) or C.stride(1) != 1 or P.stride(1) != 1:
+        raise ValueError("C (n, n) and P (n, k) must be row-major")
+    ws_bytes = lib().qmlg_syrk_emulated_workspace_size(n, k)
+    ws = workspaces.get(ws_bytes, C.device)
+    check(lib().qmlg_syrk_emulated(C.data_ptr(), C.stride(0), n, P.data_ptr(), P.stride(0), k,
+                                   ws.data_ptr(), ws.numel(), _stream(C.device)),
+          "qmlg_syrk_emulated")
 
 
 def cholesky_solve_factored(U: torch.Tensor, y: torch.Tensor) -> torch.Tensor:

@@ -14,11 +14,17 @@
 //   trsm_panel   the panel below it: X <- X L_kk^-T, one CTA per 64 rows;
 //   syrk_update  the trailing lower triangle: C <- C - P P^T with 64 x 64 tiles.
 // After a failed pivot every later kernel sees the info flag and returns.
+#include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <vector>
+
+#include <cooperative_groups.h>
 
 #include "common.cuh"
 #include "emulated_gemm.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace {
 
@@ -30,46 +36,61 @@ __global__ void __launch_bounds__(256)
 potrf_diag_kernel(double *__restrict__ A, int64_t lda, int n, int k0, double shift,
                   int *__restrict__ info)
 {
+    // Thread t owns row r = t / 4 and the columns s = t % 4 (mod 4) of that row.
+    // Per column c: (A) the owners of column c scale it by 1/L_cc; (B) rank-1 update
+    // of the trailing triangle, after which the owner of (c+1, c+1) takes its pivot.
     __shared__ double S[NB][NB + 1];
+    __shared__ double dinv[NB];
     __shared__ int failed;
     if (*info != 0) return;
     const int tid = threadIdx.x;
     const int nb = min(NB, n - k0);
     for (int e = tid; e < NB * NB; e += blockDim.x) {
-        const int r = e / NB, c = e % NB;
+        const int r = e >> 6, c = e & 63;
         double v = 0.0;
         if (r < nb && c <= r) v = A[(int64_t)(k0 + r) * lda + (k0 + c)];
         if (r == c && r < nb) v += shift;
         S[r][c] = v;
     }
-    if (tid == 0) failed = 0;
+    __syncthreads();
+    const int r = tid >> 2, s0 = tid & 3;
+    if (tid == 0) {
+        failed = 0;
+        const double p = S[0][0];
+        if (!(p > 0.0) || !isfinite(p)) {
+            failed = 1;
+            atomicCAS(info, 0, k0 + 1);
+        } else {
+            const double d = sqrt(p);
+            S[0][0] = d;
+            dinv[0] = 1.0 / d;
+        }
+    }
     __syncthreads();
     for (int c = 0; c < nb; ++c) {
-        if (tid == 0) {
-            const double p = S[c][c];
-            if (!(p > 0.0) || !isfinite(p)) {
-                failed = 1;
-                atomicCAS(info, 0, k0 + c + 1);
-            } else {
-                S[c][c] = sqrt(p);
+        if (failed) return;
+        if (r > c && r < nb && s0 == (c & 3)) S[r][c] *= dinv[c];
+        __syncthreads();
+        if (r > c && r < nb) {
+            const double lrc = S[r][c];
+            for (int s = c + 1 + ((s0 - c - 1) & 3); s <= r; s += 4) S[r][s] = fma(-lrc, S[s][c], S[r][s]);
+            if (r == c + 1 && s0 == (r & 3)) {
+                const double p = S[r][r];
+                if (!(p > 0.0) || !isfinite(p)) {
+                    failed = 1;
+                    atomicCAS(info, 0, k0 + r + 1);
+                } else {
+                    const double d = sqrt(p);
+                    S[r][r] = d;
+                    dinv[r] = 1.0 / d;
+                }
             }
         }
         __syncthreads();
-        if (failed) return;
-        const double dinv = 1.0 / S[c][c];
-        for (int r = c + 1 + tid; r < nb; r += blockDim.x) S[r][c] *= dinv;
-        __syncthreads();
-        // trailing update of the block's lower triangle
-        const int m = nb - c - 1;
-        for (int e = tid; e < m * m; e += blockDim.x) {
-            const int r = c + 1 + e / m, s = c + 1 + e % m;
-            if (s <= r) S[r][s] = fma(-S[r][c], S[s][c], S[r][s]);
-        }
-        __syncthreads();
     }
-    for (int e = tid; e < nb * nb; e += blockDim.x) {
-        const int r = e / nb, c = e % nb;
-        if (c <= r) A[(int64_t)(k0 + r) * lda + (k0 + c)] = S[r][c];
+    for (int e = tid; e < nb * NB; e += blockDim.x) {
+        const int rr = e >> 6, cc = e & 63;
+        if (cc <= rr) A[(int64_t)(k0 + rr) * lda + (k0 + cc)] = S[rr][cc];
     }
 }
 
@@ -178,83 +199,6 @@ syrk_update_kernel(double *__restrict__ A, int64_t lda, int n, int k0,
     }
 }
 
-// ------------------------------------------------------ triangular solves --
-
-// z[k0..k0+nb) <- L_kk^{-1} z[k0..k0+nb)   (forward, one CTA)
-__global__ void trsv_diag_fwd_kernel(const double *__restrict__ A, int64_t lda, int n, int k0,
-                                     double *__restrict__ z)
-{
-    __shared__ double L[NB][NB + 1];
-    __shared__ double v[NB];
-    const int tid = threadIdx.x;
-    const int nb = min(NB, n - k0);
-    for (int e = tid; e < NB * NB; e += blockDim.x) {
-        const int r = e / NB, c = e % NB;
-        L[r][c] = (r < nb && c <= r) ? A[(int64_t)(k0 + r) * lda + (k0 + c)] : 0.0;
-    }
-    if (tid < nb) v[tid] = z[k0 + tid];
-    __syncthreads();
-    for (int c = 0; c < nb; ++c) {
-        if (tid == 0) v[c] = v[c] / L[c][c];
-        __syncthreads();
-        if (tid > c && tid < nb) v[tid] = fma(-L[tid][c], v[c], v[tid]);
-        __syncthreads();
-    }
-    if (tid < nb) z[k0 + tid] = v[tid];
-}
-
-// z[r] -= sum_{t<nb} R[r][k0+t] z[k0+t] for r >= k0+nb   (a warp per row)
-__global__ void gemv_fwd_update_kernel(const double *__restrict__ A, int64_t lda, int n, int k0,
-                                       double *__restrict__ z)
-{
-    const int k1 = k0 + NB;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    const int r = k1 + warp;
-    if (r >= n) return;
-    const double *row = A + (int64_t)r * lda + k0;
-    double s = fma(row[lane], z[k0 + lane], row[lane + 32] * z[k0 + lane + 32]);
-    for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
-    if (lane == 0) z[r] -= s;
-}
-
-// x[k0..k0+nb) <- L_kk^{-T} x[k0..k0+nb)   (backward, one CTA)
-__global__ void trsv_diag_bwd_kernel(const double *__restrict__ A, int64_t lda, int n, int k0,
-                                     double *__restrict__ x)
-{
-    __shared__ double L[NB][NB + 1];
-    __shared__ double v[NB];
-    const int tid = threadIdx.x;
-    const int nb = min(NB, n - k0);
-    for (int e = tid; e < NB * NB; e += blockDim.x) {
-        const int r = e / NB, c = e % NB;
-        L[r][c] = (r < nb && c <= r) ? A[(int64_t)(k0 + r) * lda + (k0 + c)] : 0.0;
-    }
-    if (tid < nb) v[tid] = x[k0 + tid];
-    __syncthreads();
-    for (int c = nb - 1; c >= 0; --c) {
-        if (tid == 0) v[c] = v[c] / L[c][c];
-        __syncthreads();
-        if (tid < c) v[tid] = fma(-L[c][tid], v[c], v[tid]);
-        __syncthreads();
-    }
-    if (tid < nb) x[k0 + tid] = v[tid];
-}
-
-// x[t] -= sum_{r in block} R[r][t] x[r] for t < k0   (a thread per column t)
-__global__ void gemv_bwd_update_kernel(const double *__restrict__ A, int64_t lda, int n, int k0,
-                                       double *__restrict__ x)
-{
-    __shared__ double xs[NB];
-    const int nb = min(NB, n - k0);
-    if (threadIdx.x < nb) xs[threadIdx.x] = x[k0 + threadIdx.x];
-    __syncthreads();
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= k0) return;
-    double s = 0.0;
-    for (int r = 0; r < nb; ++r) s = fma(A[(int64_t)(k0 + r) * lda + t], xs[r], s);
-    x[t] -= s;
-}
 
 // ------------------------------------------------------------- residual --
 
@@ -379,6 +323,162 @@ __global__ void axpy_norms_kernel(double *__restrict__ x, const double *__restri
     }
 }
 
+// ------------------------------------------- cooperative triangular solves --
+//
+// One cooperative launch per triangular solve; grid-wide barriers separate the
+// 64-row block steps.  Step kb: CTA 0 applies block kb-1's solution to the rows of
+// block kb and solves the diagonal block with one warp (reciprocal pivots), while
+// the other CTAs apply block kb-1's solution to every row below block kb.
+
+constexpr int TRSV_THREADS = 256;
+
+__device__ __forceinline__ void load_diag_block(const double *__restrict__ A, int64_t lda, int k0,
+                                                int nb, double (*L)[NB + 1], double *dinv)
+{
+    for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) {
+        const int r = e >> 6, c = e & 63;
+        L[r][c] = (r < nb && c <= r) ? A[(int64_t)(k0 + r) * lda + (k0 + c)] : 0.0;
+    }
+    __syncthreads();
+    if (threadIdx.x < NB) dinv[threadIdx.x] = threadIdx.x < nb ? 1.0 / L[threadIdx.x][threadIdx.x] : 0.0;
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(TRSV_THREADS)
+trsv_fwd_coop_kernel(const double *__restrict__ A, int64_t lda, int n, double *__restrict__ x)
+{
+    cg::grid_group grid = cg::this_grid();
+    __shared__ double L[NB][NB + 1];
+    __shared__ double dinv[NB];
+    __shared__ double zp[NB];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    constexpr int nw = TRSV_THREADS / 32;
+    const int nblk = (n + NB - 1) / NB;
+    for (int kb = 0; kb < nblk; ++kb) {
+        const int k0 = kb * NB, nb = min(NB, n - k0), kp = k0 - NB;
+        if (kb > 0) {
+            if (tid < NB) zp[tid] = x[kp + tid];
+            __syncthreads();
+        }
+        if (blockIdx.x == 0) {
+            if (kb > 0) {
+                for (int r = warp; r < nb; r += nw) {
+                    const double *row = A + (int64_t)(k0 + r) * lda + kp;
+                    double sum = fma(row[lane], zp[lane], row[lane + 32] * zp[lane + 32]);
+                    for (int off = 16; off > 0; off >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, off);
+                    if (lane == 0) x[k0 + r] -= sum;
+                }
+            }
+            load_diag_block(A, lda, k0, nb, L, dinv);
+            if (warp == 0) {
+                double v0 = lane < nb ? x[k0 + lane] : 0.0;
+                double v1 = lane + 32 < nb ? x[k0 + lane + 32] : 0.0;
+                for (int c = 0; c < nb; ++c) {
+                    const double own = __shfl_sync(0xffffffffu, c < 32 ? v0 : v1, c & 31);
+                    const double zc = own * dinv[c];
+                    if (c < 32) {
+                        if (lane == c) v0 = zc;
+                    } else if (lane == c - 32) {
+                        v1 = zc;
+                    }
+                    if (lane > c) v0 = fma(-L[lane][c], zc, v0);
+                    if (lane + 32 > c) v1 = fma(-L[lane + 32][c], zc, v1);
+                }
+                if (lane < nb) x[k0 + lane] = v0;
+                if (lane + 32 < nb) x[k0 + lane + 32] = v1;
+            }
+        } else if (kb > 0) {
+            const int tw = (gridDim.x - 1) * nw;
+            for (int r = k0 + NB + (blockIdx.x - 1) * nw + warp; r < n; r += tw) {
+                const double *row = A + (int64_t)r * lda + kp;
+                double sum = fma(row[lane], zp[lane], row[lane + 32] * zp[lane + 32]);
+                for (int off = 16; off > 0; off >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, off);
+                if (lane == 0) x[r] -= sum;
+            }
+        }
+        grid.sync();
+    }
+}
+
+__global__ void __launch_bounds__(TRSV_THREADS)
+trsv_bwd_coop_kernel(const double *__restrict__ A, int64_t lda, int n, double *__restrict__ x)
+{
+    cg::grid_group grid = cg::this_grid();
+    __shared__ double L[NB][NB + 1];
+    __shared__ double dinv[NB];
+    __shared__ double zp[NB];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int nblk = (n + NB - 1) / NB;
+    for (int kb = nblk - 1; kb >= 0; --kb) {
+        const int k0 = kb * NB, nb = min(NB, n - k0), kn = k0 + NB;
+        const int nbn = kb < nblk - 1 ? min(NB, n - kn) : 0;
+        if (nbn > 0) {
+            if (tid < NB) zp[tid] = tid < nbn ? x[kn + tid] : 0.0;
+            __syncthreads();
+        }
+        if (blockIdx.x == 0) {
+            if (nbn > 0 && tid < nb) {
+                double sum = 0.0;
+                for (int r = 0; r < nbn; ++r) sum = fma(A[(int64_t)(kn + r) * lda + k0 + tid], zp[r], sum);
+                x[k0 + tid] -= sum;
+            }
+            load_diag_block(A, lda, k0, nb, L, dinv);
+            if (warp == 0) {
+                double v0 = lane < nb ? x[k0 + lane] : 0.0;
+                double v1 = lane + 32 < nb ? x[k0 + lane + 32] : 0.0;
+                for (int c = nb - 1; c >= 0; --c) {
+                    const double own = __shfl_sync(0xffffffffu, c < 32 ? v0 : v1, c & 31);
+                    const double xc = own * dinv[c];
+                    if (c < 32) {
+                        if (lane == c) v0 = xc;
+                    } else if (lane == c - 32) {
+                        v1 = xc;
+                    }
+                    if (lane < c) v0 = fma(-L[c][lane], xc, v0);
+                    if (lane + 32 < c) v1 = fma(-L[c][lane + 32], xc, v1);
+                }
+                if (lane < nb) x[k0 + lane] = v0;
+                if (lane + 32 < nb) x[k0 + lane + 32] = v1;
+            }
+        } else if (nbn > 0) {
+            const int tt = (gridDim.x - 1) * TRSV_THREADS;
+            for (int t = (blockIdx.x - 1) * TRSV_THREADS + tid; t < k0; t += tt) {
+                double sum = 0.0;
+                for (int r = 0; r < nbn; ++r) sum = fma(A[(int64_t)(kn + r) * lda + t], zp[r], sum);
+                x[t] -= sum;
+            }
+        }
+        grid.sync();
+    }
+}
+
+int trsv_grid(int &grid)
+{
+    static int cached = 0;
+    static std::once_flag once;
+    static int status = QMLG_OK;
+    std::call_once(once, [] {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trsv_fwd_coop_kernel,
+                                                              TRSV_THREADS, 0);
+        int per_sm2 = 0;
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, trsv_bwd_coop_kernel,
+                                                              TRSV_THREADS, 0);
+        if (e != cudaSuccess) {
+            status = qmlg::set_cuda_error(e);
+            return;
+        }
+        cached = sms * std::max(1, std::min(per_sm, per_sm2));
+        if (cached < 2) status = QMLG_E_CUDA;
+    });
+    grid = cached;
+    return status;
+}
+
 __global__ void fill_nan_kernel(double *__restrict__ x, int n)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -407,20 +507,18 @@ int cholesky_fp64(double *A, int n, int64_t lda, double shift, int *d_info, cuda
 
 int potrs_fp64(const double *A, int n, int64_t lda, double *x, cudaStream_t s)
 {
-    for (int k0 = 0; k0 < n; k0 += NB) {
-        { trsv_diag_fwd_kernel<<<1, NB, 0, s>>>(A, lda, n, k0, x); qmlg::count_launches(1); }
-        const int below = n - (k0 + NB);
-        if (below > 0)
-            { gemv_fwd_update_kernel<<<(int)ceil_div((int64_t)below * 32, 256), 256, 0, s>>>(
-                A, lda, n, k0, x); qmlg::count_launches(1); }
-    }
-    const int last = (int)((n - 1) / NB) * NB;
-    for (int k0 = last; k0 >= 0; k0 -= NB) {
-        { trsv_diag_bwd_kernel<<<1, NB, 0, s>>>(A, lda, n, k0, x); qmlg::count_launches(1); }
-        if (k0 > 0)
-            { gemv_bwd_update_kernel<<<(int)ceil_div(k0, 256), 256, 0, s>>>(A, lda, n, k0, x); qmlg::count_launches(1); }
-    }
-    return check_launch();
+    int grid = 0;
+    int st = trsv_grid(grid);
+    if (st != QMLG_OK) return st;
+    void *args[] = {(void *)&A, (void *)&lda, (void *)&n, (void *)&x};
+    cudaError_t e = cudaLaunchCooperativeKernel((const void *)trsv_fwd_coop_kernel, dim3(grid),
+                                                dim3(TRSV_THREADS), args, 0, s);
+    count_launches(1);
+    if (e == cudaSuccess)
+        e = cudaLaunchCooperativeKernel((const void *)trsv_bwd_coop_kernel, dim3(grid),
+                                        dim3(TRSV_THREADS), args, 0, s);
+    count_launches(1);
+    return e == cudaSuccess ? QMLG_OK : set_cuda_error(e);
 }
 
 // R[i][j] <- R[j][i] for j < i, R[i][i] <- diag[i]: restores the lower triangle from

@@ -25,8 +25,10 @@ constexpr int kEmuMaxSlices = 8;
 // tcgen05 path (emulated_tc.cu).
 // Digit planes of rows r0 .. r0+nrows-1, columns c0 .. c0+kw-1 of a row-major matrix:
 // digits [slices][rpad][kp] bf16 (kp a multiple of 64, zero-padded), expo [rpad].
+// norms (optional, [rpad]) receives the FP64 sum of squares of each row.
 int slice_rows(const double *A, int64_t lda, int r0, int nrows, int c0, int kw, int kp, int rpad,
-               int slices, __nv_bfloat16 *digits, int *expo, const int *d_info, cudaStream_t s);
+               int slices, __nv_bfloat16 *digits, int *expo, const int *d_info, cudaStream_t s,
+               double *norms = nullptr);
 // C[i][j] -= sum_k P[i][k] P[j][k] for j in [jbase, jend), i in [ibase, iend) (j <= i
 // when lower), P rows taken from the digit planes (digit row = a_row0 + j - jbase for
 // the j side, b_row0 + i - ibase for the i side), K = kp <= 512.

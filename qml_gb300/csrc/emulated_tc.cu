@@ -20,7 +20,9 @@
 // 2^(e_i + e_j) and subtracted from C.  Waits are bounded; a timeout sets *err.
 #include <cuda.h>
 
+#include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <mutex>
 
 #include "common.cuh"
@@ -38,21 +40,32 @@ constexpr int S_MAX = 8;
 constexpr int A_STAGES = 3;
 constexpr int A_BYTES = TM * KC * 2;  // 16 KB
 constexpr int B_BYTES = TN * KC * 2;  // 8 KB
-constexpr int SMEM_BYTES = 2 * S_MAX * B_BYTES + A_STAGES * A_BYTES + 1024 /*align*/ + 256;
+constexpr int RED_BYTES = 4 * TN * 8;  // predict: per-warp column sums
+constexpr int SMEM_BYTES =
+    2 * S_MAX * B_BYTES + A_STAGES * A_BYTES + 1024 /*align*/ + 256 /*barriers*/ + RED_BYTES;
+
+enum Mode { kSyrk = 0, kKernelMatrix = 1, kPredict = 2 };
 
 struct TileArgs {
-    double *C;
+    double *C;         // kSyrk: row-major C; kKernelMatrix: column-major K
     int64_t ldc;
-    int jbase, jend;   // lanes: C column index range
-    int ibase, iend;   // TMEM columns: C row index range
+    int jbase, jend;   // lanes: contiguous index range of C / K
+    int ibase, iend;   // TMEM columns
     int a_row0;        // digit row of j = jbase
     int b_row0;        // digit row of i = ibase
     int kchunks;
     int slices;
     const int *expA;   // per digit row
     const int *expB;
-    int lower;         // update only j <= i
+    int lower;         // kSyrk: update only j <= i; kKernelMatrix: symmetric (A is B)
     int *err;
+    // Gaussian epilogues
+    const double *normA;  // |x|^2 per digit row
+    const double *normB;
+    double scale;         // -0.5 / sigma^2
+    double diag_shift;
+    const double *alpha;  // kPredict: weights of the j rows
+    double *partial;      // kPredict: [gridDim.x][iend - ibase] partial sums
 };
 
 __device__ __forceinline__ double pow2i(int e)
@@ -61,6 +74,7 @@ __device__ __forceinline__ double pow2i(int e)
     return ldexp(1.0, e);
 }
 
+template <int MODE>
 __global__ void __launch_bounds__(192, 1)
 emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
               TileArgs p)
@@ -74,6 +88,7 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
     uint64_t *bFull = bars, *bEmpty = bars + 2, *aFull = bars + 4, *aEmpty = bars + 7,
              *done = bars + 10;
     uint32_t *tmem_holder = (uint32_t *)(bars + 12);
+    double(*red)[TN] = (double(*)[TN])(bars + 32);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int j0 = p.jbase + blockIdx.x * TM;
@@ -178,6 +193,11 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
         if (!ok && lane == 0) atomicOr(p.err, 4);
         fence_after_sync();
         const int ej = (j < p.jend) ? p.expA[arow + jl] : 0;
+        double aj = 0.0, aw = 0.0;
+        if (MODE != kSyrk && j < p.jend) {
+            aj = p.scale * p.normA[arow + jl];
+            if (MODE == kPredict) aw = p.alpha[j];
+        }
         const int H = (S + 1) / 2;
         const int lo_levels = S - H;
         const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
@@ -204,13 +224,44 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
                 // `shift` bits of lo (far below FP64 resolution of the value)
                 const int shift = lo_levels >= 2 ? 12 : 0;
                 const long long v64 = (hi << (7 * lo_levels - shift)) + (lo >> shift);
-                if (j < p.jend && i < p.iend && (!p.lower || j <= i)) {
-                    const int ei = p.expB[brow + il];
-                    const double scale = pow2i(ei + ej + shift - 7 * (S + 1));
-                    double *cp = p.C + (int64_t)i * p.ldc + j;
-                    *cp = fma(-(double)v64, scale, *cp);
+                const bool valid = j < p.jend && i < p.iend;
+                if (MODE == kSyrk) {
+                    if (valid && (!p.lower || j <= i)) {
+                        const int ei = p.expB[brow + il];
+                        const double scale = pow2i(ei + ej + shift - 7 * (S + 1));
+                        double *cp = p.C + (int64_t)i * p.ldc + j;
+                        *cp = fma(-(double)v64, scale, *cp);
+                    }
+                } else {
+                    double kv = 0.0;
+                    if (valid) {
+                        // x = scale * (|a|^2 + |b|^2 - 2 a.b), clamped at 0 from above
+                        const int ei = p.expB[brow + il];
+                        const double w = -2.0 * p.scale * pow2i(ei + ej + shift - 7 * (S + 1));
+                        const double x = fmin(fma((double)v64, w, aj + p.scale * p.normB[brow + il]), 0.0);
+                        kv = exp(x);
+                        if (MODE == kKernelMatrix && p.lower && i == j) kv = 1.0 + p.diag_shift;
+                    }
+                    if (MODE == kKernelMatrix) {
+                        if (valid && (!p.lower || j <= i)) {
+                            p.C[(int64_t)i * p.ldc + j] = kv;
+                            if (p.lower && j < i) p.C[(int64_t)j * p.ldc + i] = kv;
+                        }
+                    } else {
+                        double c = valid ? kv * aw : 0.0;
+                        for (int off = 16; off > 0; off >>= 1) c += __shfl_xor_sync(0xffffffffu, c, off);
+                        if (lane == 0) red[q][il] = c;
+                    }
                 }
             }
+        }
+        if (MODE == kPredict) {
+            // the four epilogue warps add their column sums in a fixed order
+            asm volatile("bar.sync 1, 128;" ::: "memory");
+            const int t = threadIdx.x - 64;
+            if (ok && t < TN && i0 + t < p.iend)
+                p.partial[(int64_t)blockIdx.x * (p.iend - p.ibase) + (i0 - p.ibase) + t] =
+                    ((red[0][t] + red[1][t]) + red[2][t]) + red[3][t];
         }
     }
     fence_before_sync();
@@ -221,10 +272,14 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
 // One warp per row: power-of-two row scale over the K-range and S digit planes.
 // src rows r0 .. r0+nrows-1, columns c0 .. c0+kw-1 of the row-major matrix;
 // digits [S][rpad][kp] bf16 (zero beyond kw and beyond nrows), expo [rpad].
+// Each value is rounded once to the fixed-point integer q = round(x * 2^(7S-e))
+// (|q| <= 2^(7S-1)), then split into balanced base-128 digits with integer shifts,
+// least significant first: d = ((q + 64) mod 128) - 64, q <- (q - d) / 128; the most
+// significant digit takes what is left, which is at most 64 in magnitude.
 __global__ void slice_rows_kernel(const double *__restrict__ A, int64_t lda, int r0, int nrows,
                                   int c0, int kw, int kp, int rpad, int slices,
                                   __nv_bfloat16 *__restrict__ digits, int *__restrict__ expo,
-                                  const int *__restrict__ info)
+                                  double *__restrict__ norms, const int *__restrict__ info)
 {
     if (info != nullptr && *info != 0) return;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -232,24 +287,43 @@ __global__ void slice_rows_kernel(const double *__restrict__ A, int64_t lda, int
     if (warp >= rpad) return;
     const bool live = warp < nrows;
     const double *row = A + (int64_t)(r0 + warp) * lda + c0;
-    double m = 0.0;
+    double m = 0.0, sq = 0.0;
     if (live)
-        for (int k = lane; k < kw; k += 32) m = fmax(m, fabs(row[k]));
-    for (int off = 16; off > 0; off >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, off));
+        for (int k = lane; k < kw; k += 32) {
+            m = fmax(m, fabs(row[k]));
+            sq = fma(row[k], row[k], sq);
+        }
+    for (int off = 16; off > 0; off >>= 1) {
+        m = fmax(m, __shfl_xor_sync(0xffffffffu, m, off));
+        sq += __shfl_xor_sync(0xffffffffu, sq, off);
+    }
+    if (norms != nullptr && lane == 0) norms[warp] = sq;
     int e = 0;
     if (m > 0.0 && isfinite(m)) {
         frexp(m, &e);
         e += 1;  // |x| * 2^-e < 1/2
     }
+    const double scale = pow2i(7 * slices - e);
     const int64_t plane = (int64_t)rpad * kp;
     __nv_bfloat16 *dst = digits + (int64_t)warp * kp;
-    for (int k = lane; k < kp; k += 32) {
-        double v = (live && k < kw) ? ldexp(row[k], -e) : 0.0;
-        for (int s = 0; s < slices; ++s) {
-            v *= 128.0;
-            const double d = rint(v);
-            v -= d;
-            dst[(int64_t)s * plane + k] = __double2bfloat16(d);
+    for (int k0 = lane * 8; k0 < kp; k0 += 256) {
+        long long q[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int k = k0 + u;
+            q[u] = (live && k < kw) ? __double2ll_rn(row[k] * scale) : 0;
+        }
+        for (int s = slices - 1; s >= 0; --s) {
+            __align__(16) __nv_bfloat16 b[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                // the most significant digit keeps the remainder (|q| <= 64 there)
+                const long long d = s > 0 ? ((q[u] + 64) & 127) - 64 : q[u];
+                q[u] = (q[u] - d) >> 7;
+                b[u] = __int2bfloat16_rn((int)d);
+            }
+            *reinterpret_cast<uint4 *>(dst + (int64_t)s * plane + k0) =
+                *reinterpret_cast<const uint4 *>(b);
         }
     }
     if (lane == 0) expo[warp] = e;
@@ -290,16 +364,102 @@ int make_plane_map(CUtensorMap *map, const __nv_bfloat16 *digits, int kp, int rp
     return r == CUDA_SUCCESS ? QMLG_OK : QMLG_E_CUDA;
 }
 
+
+// Largest |x| over a row-major block (bit pattern of a non-negative double, so the
+// integer maximum is the floating-point maximum).
+__global__ void max_abs_kernel(const double *__restrict__ X, int64_t ldx, int rows, int cols,
+                               unsigned long long *__restrict__ out)
+{
+    unsigned long long m = 0;
+    const int64_t total = (int64_t)rows * cols;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const double v = fabs(X[(e / cols) * ldx + e % cols]);
+        const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+        if (b > m) m = b;
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        const unsigned long long o = __shfl_xor_sync(0xffffffffu, m, off);
+        if (o > m) m = o;
+    }
+    if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+__global__ void reduce_partial_rows_kernel(const double *__restrict__ partial, int nparts, int n,
+                                           double *__restrict__ y)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double s = 0.0;
+    for (int p = 0; p < nparts; ++p) s += partial[(int64_t)p * n + i];
+    y[i] = s;
+}
+
+void set_smem_attrs()
+{
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaFuncSetAttribute(emu_tc_kernel<kSyrk>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             SMEM_BYTES);
+        cudaFuncSetAttribute(emu_tc_kernel<kKernelMatrix>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+        cudaFuncSetAttribute(emu_tc_kernel<kPredict>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    });
+}
+
+// Gaussian path: feature width padded to a multiple of the 64-element chunk.
+int feature_pad(int d) { return (int)qmlg::ceil_div(d < 1 ? 1 : d, KC) * KC; }
+int rows_pad(int n) { return (int)qmlg::ceil_div(n < 1 ? 1 : n, TM) * TM; }
+
+// Smallest S whose worst-case error bound on K keeps the relative error below
+// 0.5e-12: |dot error| <= 2^(eA + eB - 7S) * kp * (S + 1) / 4 (truncated digit
+// levels plus the rounding of the fixed-point values), and the relative error of
+// K = exp(-d^2 / (2 sigma^2)) is that error / sigma^2.  0 if no S <= 8 reaches it.
+int choose_slices(double maxA, double maxB, int kp, double sigma)
+{
+    int ea = 0, eb = 0;
+    if (maxA > 0.0) std::frexp(maxA, &ea);
+    if (maxB > 0.0) std::frexp(maxB, &eb);
+    ea += 1;
+    eb += 1;
+    for (int S = 4; S <= S_MAX; ++S) {
+        const double bound = std::ldexp(1.0, ea + eb - 7 * S) * kp * (S + 1) / 4.0;
+        if (bound / (sigma * sigma) <= 0.5e-12) return S;
+    }
+    return 0;
+}
+
+int read_max(const double *X, int64_t ldx, int rows, int cols, unsigned long long *dbuf,
+             double &out, cudaStream_t s)
+{
+    out = 0.0;
+    if (rows == 0 || cols == 0) return QMLG_OK;
+    cudaError_t e = cudaMemsetAsync(dbuf, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+    const int64_t total = (int64_t)rows * cols;
+    const int blocks = (int)std::min<int64_t>(qmlg::ceil_div(total, 256), 1216);
+    max_abs_kernel<<<blocks, 256, 0, s>>>(X, ldx, rows, cols, dbuf);
+    qmlg::count_launches(1);
+    unsigned long long h = 0;
+    e = cudaMemcpyAsync(&h, dbuf, sizeof(h), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+    std::memcpy(&out, &h, sizeof(out));
+    return QMLG_OK;
+}
+
 }  // namespace
 
 namespace qmlg {
 
 int slice_rows(const double *A, int64_t lda, int r0, int nrows, int c0, int kw, int kp, int rpad,
-               int slices, __nv_bfloat16 *digits, int *expo, const int *d_info, cudaStream_t s)
+               int slices, __nv_bfloat16 *digits, int *expo, const int *d_info, cudaStream_t s,
+               double *norms)
 {
     if (slices < 1 || slices > S_MAX || kp % KC != 0 || kw > kp || nrows > rpad) return QMLG_E_ARG;
     slice_rows_kernel<<<(unsigned)ceil_div((int64_t)rpad * 32, 256), 256, 0, s>>>(
-        A, lda, r0, nrows, c0, kw, kp, rpad, slices, digits, expo, d_info);
+        A, lda, r0, nrows, c0, kw, kp, rpad, slices, digits, expo, norms, d_info);
     count_launches(1);
     return check_launch();
 }
@@ -314,17 +474,262 @@ int emu_tc_update(double *C, int64_t ldc, int jbase, int jend, int ibase, int ie
     int st = make_plane_map(&mA, digits, kp, rpad, slices, TM);
     if (st == QMLG_OK) st = make_plane_map(&mB, digits, kp, rpad, slices, TN);
     if (st != QMLG_OK) return st;
-    static std::once_flag attr_once;
-    std::call_once(attr_once, [] {
-        cudaFuncSetAttribute(emu_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             SMEM_BYTES);
-    });
-    TileArgs a{C, ldc, jbase, jend, ibase, iend, a_row0, b_row0, kp / KC, slices,
-               expo, expo, lower, d_err};
+    set_smem_attrs();
+    TileArgs a{};
+    a.C = C;
+    a.ldc = ldc;
+    a.jbase = jbase;
+    a.jend = jend;
+    a.ibase = ibase;
+    a.iend = iend;
+    a.a_row0 = a_row0;
+    a.b_row0 = b_row0;
+    a.kchunks = kp / KC;
+    a.slices = slices;
+    a.expA = expo;
+    a.expB = expo;
+    a.lower = lower;
+    a.err = d_err;
     dim3 grid((unsigned)ceil_div(jend - jbase, TM), (unsigned)ceil_div(iend - ibase, TN));
-    emu_tc_kernel<<<grid, 192, SMEM_BYTES, s>>>(mA, mB, a);
+    emu_tc_kernel<kSyrk><<<grid, 192, SMEM_BYTES, s>>>(mA, mB, a);
     count_launches(1);
     return check_launch();
 }
 
 }  // namespace qmlg
+
+// ------------------------------------------------------------------ C ABI --
+
+namespace {
+
+struct GaussPlan {
+    int kp, rpa, rpb;
+};
+
+void plan_gauss(qmlg::WorkspacePlan &p, int na, int nb, int d, bool share_b, bool predict)
+{
+    const int kp = feature_pad(d), rpa = rows_pad(na), rpb = rows_pad(nb);
+    p.add<__nv_bfloat16>((size_t)S_MAX * rpa * kp);
+    p.add<int>((size_t)rpa);
+    p.add<double>((size_t)rpa);
+    if (!share_b) {
+        p.add<__nv_bfloat16>((size_t)S_MAX * rpb * kp);
+        p.add<int>((size_t)rpb);
+        p.add<double>((size_t)rpb);
+    }
+    if (predict) p.add<double>((size_t)qmlg::ceil_div(na < 1 ? 1 : na, TM) * (size_t)nb);
+    p.add<unsigned long long>(2);
+    p.add<int>(4);
+}
+
+struct GaussBufs {
+    __nv_bfloat16 *dA = nullptr, *dB = nullptr;
+    int *eA = nullptr, *eB = nullptr;
+    double *nA = nullptr, *nB = nullptr, *partial = nullptr;
+    unsigned long long *maxbuf = nullptr;
+    int *err = nullptr;
+};
+
+bool take_gauss(qmlg::Workspace &ws, int na, int nb, int d, bool share_b, bool predict,
+                GaussBufs &b)
+{
+    const int kp = feature_pad(d), rpa = rows_pad(na), rpb = rows_pad(nb);
+    b.dA = ws.take<__nv_bfloat16>((size_t)S_MAX * rpa * kp);
+    b.eA = ws.take<int>((size_t)rpa);
+    b.nA = ws.take<double>((size_t)rpa);
+    if (share_b) {
+        b.dB = b.dA;
+        b.eB = b.eA;
+        b.nB = b.nA;
+    } else {
+        b.dB = ws.take<__nv_bfloat16>((size_t)S_MAX * rpb * kp);
+        b.eB = ws.take<int>((size_t)rpb);
+        b.nB = ws.take<double>((size_t)rpb);
+    }
+    if (predict) b.partial = ws.take<double>((size_t)qmlg::ceil_div(na, TM) * (size_t)nb);
+    b.maxbuf = ws.take<unsigned long long>(2);
+    b.err = ws.take<int>(4);
+    return b.dA && b.eA && b.nA && b.dB && b.eB && b.nB && b.maxbuf && b.err &&
+           (!predict || b.partial);
+}
+
+// Slices A (and B), picks S; returns S, 0 when the bound cannot be met.
+int prepare_gauss(const double *A, int64_t lda, int na, const double *B, int64_t ldb, int nb,
+                  int d, double sigma, bool share_b, GaussBufs &b, int &S, cudaStream_t s)
+{
+    const int kp = feature_pad(d), rpa = rows_pad(na), rpb = rows_pad(nb);
+    double ma = 0.0, mb = 0.0;
+    int st = read_max(A, lda, na, d, b.maxbuf, ma, s);
+    if (st == QMLG_OK && !share_b) st = read_max(B, ldb, nb, d, b.maxbuf, mb, s);
+    if (st != QMLG_OK) return st;
+    if (share_b) mb = ma;
+    if (!std::isfinite(ma) || !std::isfinite(mb)) {
+        S = 0;
+        return QMLG_OK;
+    }
+    S = choose_slices(ma, mb, kp, sigma);
+    if (S == 0) return QMLG_OK;
+    cudaError_t e = cudaMemsetAsync(b.err, 0, sizeof(int), s);
+    if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+    st = qmlg::slice_rows(A, lda, 0, na, 0, d, kp, rpa, S, b.dA, b.eA, nullptr, s, b.nA);
+    if (st == QMLG_OK && !share_b)
+        st = qmlg::slice_rows(B, ldb, 0, nb, 0, d, kp, rpb, S, b.dB, b.eB, nullptr, s, b.nB);
+    return st;
+}
+
+int launch_gauss(int mode, const GaussBufs &b, int na, int nb, int d, int S, double sigma,
+                 double *K, int64_t ldk, bool sym, double diag_shift, const double *alpha,
+                 double *yhat, cudaStream_t s)
+{
+    const int kp = feature_pad(d), rpa = rows_pad(na), rpb = rows_pad(nb);
+    CUtensorMap mA, mB;
+    int st = make_plane_map(&mA, b.dA, kp, rpa, S, TM);
+    if (st == QMLG_OK) st = make_plane_map(&mB, b.dB, kp, rpb, S, TN);
+    if (st != QMLG_OK) return st;
+    set_smem_attrs();
+    TileArgs a{};
+    a.C = K;
+    a.ldc = ldk;
+    a.jbase = 0;
+    a.jend = na;
+    a.ibase = 0;
+    a.iend = nb;
+    a.kchunks = kp / KC;
+    a.slices = S;
+    a.expA = b.eA;
+    a.expB = b.eB;
+    a.lower = sym ? 1 : 0;
+    a.err = b.err;
+    a.normA = b.nA;
+    a.normB = b.nB;
+    a.scale = -0.5 / (sigma * sigma);
+    a.diag_shift = diag_shift;
+    a.alpha = alpha;
+    a.partial = b.partial;
+    dim3 grid((unsigned)qmlg::ceil_div(na, TM), (unsigned)qmlg::ceil_div(nb, TN));
+    if (mode == kKernelMatrix)
+        emu_tc_kernel<kKernelMatrix><<<grid, 192, SMEM_BYTES, s>>>(mA, mB, a);
+    else
+        emu_tc_kernel<kPredict><<<grid, 192, SMEM_BYTES, s>>>(mA, mB, a);
+    qmlg::count_launches(1);
+    st = qmlg::check_launch();
+    if (st == QMLG_OK && mode == kPredict) {
+        reduce_partial_rows_kernel<<<(int)qmlg::ceil_div(nb, 256), 256, 0, s>>>(
+            b.partial, (int)qmlg::ceil_div(na, TM), nb, yhat);
+        qmlg::count_launches(1);
+        st = qmlg::check_launch();
+    }
+    if (st == QMLG_OK) st = qmlg::read_device_flag(b.err, s);
+    return st;
+}
+
+}  // namespace
+
+extern "C" size_t qmlg_gaussian_kernel_emulated_workspace_size(int na, int nb, int d, int flags)
+{
+    qmlg::WorkspacePlan p;
+    plan_gauss(p, na, nb, d, (flags & QMLG_KERNEL_SYMMETRIC) != 0, false);
+    return p.total();
+}
+
+extern "C" int qmlg_gaussian_kernel_emulated(const double *A, int64_t lda, int na, const double *B,
+                                             int64_t ldb, int nb, int d, double sigma, double *K,
+                                             int64_t ldk, int flags, double diag_shift,
+                                             void *workspace, size_t ws_bytes, void *stream)
+{
+    const bool sym = (flags & QMLG_KERNEL_SYMMETRIC) != 0;
+    if (na < 0 || nb < 0 || d < 0 || !(sigma > 0.0) || !std::isfinite(sigma)) return QMLG_E_ARG;
+    if ((na > 0 && (A == nullptr || lda < d)) || (nb > 0 && (B == nullptr || ldb < d)))
+        return QMLG_E_ARG;
+    if (K == nullptr || ldk < na) return QMLG_E_ARG;
+    if (sym && (na != nb || A != B || lda != ldb)) return QMLG_E_ARG;
+    if (na == 0 || nb == 0) return QMLG_OK;
+    if (ws_bytes < qmlg_gaussian_kernel_emulated_workspace_size(na, nb, d, flags))
+        return QMLG_E_WORKSPACE;
+    cudaStream_t s = qmlg::as_stream(stream);
+    qmlg::Workspace ws(workspace, ws_bytes);
+    GaussBufs b;
+    if (!take_gauss(ws, na, nb, d, sym, false, b)) return QMLG_E_WORKSPACE;
+    int S = 0;
+    int st = prepare_gauss(A, lda, na, B, ldb, nb, d, sigma, sym, b, S, s);
+    if (st != QMLG_OK) return st;
+    if (S == 0)  // sigma too small for the digit bound: the FP64 kernel
+        return qmlg_gaussian_kernel(A, lda, na, B, ldb, nb, d, sigma, K, ldk, flags, diag_shift,
+                                    stream);
+    return launch_gauss(kKernelMatrix, b, na, nb, d, S, sigma, K, ldk, sym, diag_shift, nullptr,
+                        nullptr, s);
+}
+
+extern "C" size_t qmlg_predict_emulated_workspace_size(int ntrain, int ntest, int d)
+{
+    qmlg::WorkspacePlan p;
+    plan_gauss(p, ntrain, ntest, d, false, true);
+    p.add<char>(qmlg_predict_workspace_size(ntrain, ntest));  // FP64 fallback
+    return p.total();
+}
+
+extern "C" int qmlg_predict_emulated(const double *Xtrain, int64_t ldtrain, int ntrain,
+                                     const double *Xtest, int64_t ldtest, int ntest, int d,
+                                     double sigma, const double *alpha, double *yhat,
+                                     void *workspace, size_t ws_bytes, void *stream)
+{
+    if (ntrain < 0 || ntest < 0 || d < 0 || !(sigma > 0.0) || !std::isfinite(sigma))
+        return QMLG_E_ARG;
+    if ((ntrain > 0 && (Xtrain == nullptr || ldtrain < d || alpha == nullptr)) ||
+        (ntest > 0 && (Xtest == nullptr || ldtest < d || yhat == nullptr)))
+        return QMLG_E_ARG;
+    if (ntest == 0) return QMLG_OK;
+    cudaStream_t s = qmlg::as_stream(stream);
+    if (ntrain == 0) {
+        cudaError_t e = cudaMemsetAsync(yhat, 0, sizeof(double) * (size_t)ntest, s);
+        return e == cudaSuccess ? QMLG_OK : qmlg::set_cuda_error(e);
+    }
+    if (ws_bytes < qmlg_predict_emulated_workspace_size(ntrain, ntest, d)) return QMLG_E_WORKSPACE;
+    qmlg::Workspace ws(workspace, ws_bytes);
+    GaussBufs b;
+    if (!take_gauss(ws, ntrain, ntest, d, false, true, b)) return QMLG_E_WORKSPACE;
+    int S = 0;
+    int st = prepare_gauss(Xtrain, ldtrain, ntrain, Xtest, ldtest, ntest, d, sigma, false, b, S, s);
+    if (st != QMLG_OK) return st;
+    if (S == 0) {
+        const size_t fb = qmlg_predict_workspace_size(ntrain, ntest);
+        char *p = ws.take<char>(fb);
+        if (p == nullptr) return QMLG_E_WORKSPACE;
+        return qmlg_predict_fused(QMLG_KIND_GAUSSIAN, Xtrain, ldtrain, ntrain, Xtest, ldtest, ntest,
+                                  d, sigma, alpha, yhat, p, fb, stream);
+    }
+    return launch_gauss(kPredict, b, ntrain, ntest, d, S, sigma, nullptr, 0, false, 0.0, alpha,
+                        yhat, s);
+}
+
+extern "C" size_t qmlg_syrk_emulated_workspace_size(int n, int k)
+{
+    qmlg::WorkspacePlan p;
+    const int kp = feature_pad(k), rp = rows_pad(n);
+    p.add<__nv_bfloat16>((size_t)S_MAX * rp * kp);
+    p.add<int>((size_t)rp);
+    p.add<int>(4);
+    return p.total();
+}
+
+extern "C" int qmlg_syrk_emulated(double *C, int64_t ldc, int n, const double *P, int64_t ldp,
+                                  int k, void *workspace, size_t ws_bytes, void *stream)
+{
+    if (n < 0 || k < 0 || k > 512 || ldc < n || ldp < k) return QMLG_E_ARG;
+    if (n == 0 || k == 0) return QMLG_OK;
+    if (C == nullptr || P == nullptr) return QMLG_E_ARG;
+    if (ws_bytes < qmlg_syrk_emulated_workspace_size(n, k)) return QMLG_E_WORKSPACE;
+    cudaStream_t s = qmlg::as_stream(stream);
+    qmlg::Workspace ws(workspace, ws_bytes);
+    const int kp = feature_pad(k), rp = rows_pad(n);
+    __nv_bfloat16 *dig = ws.take<__nv_bfloat16>((size_t)S_MAX * rp * kp);
+    int *ex = ws.take<int>((size_t)rp);
+    int *err = ws.take<int>(4);
+    if (dig == nullptr || ex == nullptr || err == nullptr) return QMLG_E_WORKSPACE;
+    cudaError_t e = cudaMemsetAsync(err, 0, sizeof(int), s);
+    if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+    int st = qmlg::slice_rows(P, ldp, 0, n, 0, k, kp, rp, S_MAX, dig, ex, nullptr, s);
+    if (st == QMLG_OK)
+        st = qmlg::emu_tc_update(C, ldc, 0, n, 0, n, dig, ex, kp, rp, S_MAX, 0, 0, 1, err, s);
+    return st;
+}

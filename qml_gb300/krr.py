@@ -2,9 +2,14 @@
 tests and tutorial (tests/test_energy_krr_cmat.py:66-113, docs/source/tutorial.rst:128-166):
 
     X  = sorted Coulomb matrices        (qmlg_coulomb_matrix)
-    K  = kernel(X, X) + lambda I          (symmetric kernel, lambda fused on the diagonal)
-    alpha = cho_solve(K, y)               (qmlg_solve, "fp64" or "mixed")
-    yhat  = kernel(Xs, X) alpha           (qmlg_predict_fused, Ks never materialised)
+    K  = kernel(X, X)                     (symmetric kernel)
+    alpha = solve(K + lambda I, y)        (qmlg_solve, "fp64" or "mixed")
+    yhat  = kernel(Xs, X) alpha           (fused prediction, Ks never materialised)
+
+precision "fp64" runs the plain FP64 kernels and factorisation; "mixed" forms the
+Gaussian contractions and the Cholesky trailing updates as emulated-FP64 products
+on the bf16 tensor cores (each kernel entry within 1e-12 of FP64) and refines
+alpha with a double-double residual.
 
 All tensors stay in HBM; ``KRR`` keeps the training representations and alpha
 resident so that predictions reuse them.
@@ -34,7 +39,8 @@ class KRR:
 
     def fit(self, X: torch.Tensor, y: torch.Tensor, keep_kernel: bool = False) -> "KRR":
         """X (n, d) float64 CUDA, y (n,) float64 CUDA."""
-        K = core.kernel_matrix(self.kernel, X, X, self.sigma, symmetric=True)
+        emulated = self.precision == "mixed"
+        K = core.kernel_matrix(self.kernel, X, X, self.sigma, symmetric=True, emulated=emulated)
         # lambda goes to the solver (the kernel's own diagonal stays exact)
         alpha, rep = core.solve(K, y, self.lam, precision=self.precision,
                                 max_outer=self.max_outer, tol=self.tol)
@@ -45,7 +51,8 @@ class KRR:
     def predict(self, Xs: torch.Tensor) -> torch.Tensor:
         if self.alpha is None:
             raise RuntimeError("fit() first")
-        return core.predict(self.kernel, self.X, Xs, self.sigma, self.alpha)
+        return core.predict(self.kernel, self.X, Xs, self.sigma, self.alpha,
+                            emulated=self.precision == "mixed")
 
 
 def molecules_to_device(batch, device="cuda", pin=True):

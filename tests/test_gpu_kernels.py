@@ -90,3 +90,51 @@ def test_predict_fused_and_gemv(cuda, oracle, cm_features, kind):
     y3 = core.predict(kind, torch.from_numpy(Xtr).to(cuda), torch.from_numpy(Xte).to(cuda), 1000.0,
                       torch.from_numpy(alpha).to(cuda)).cpu().numpy()
     assert np.array_equal(y, y3)
+
+
+@pytest.mark.parametrize("sigma", [250.0, 1000.0, 2000.0])
+def test_emulated_gaussian_kernel(cuda, oracle, cm_features, sigma):
+    # tensor-core (digit-plane) contraction: every entry within 1e-12 of the oracle
+    X = cm_features
+    A, B = X[:700], X[700:]
+    At, Bt = torch.from_numpy(A).to(cuda), torch.from_numpy(B).to(cuda)
+    K = core.kernel_matrix("gaussian", At, Bt, sigma, emulated=True).cpu().numpy()
+    assert relerr(K, oracle.gaussian_kernel(A, B, sigma)) <= RTOL
+    Ks = core.kernel_matrix("gaussian", At, At, sigma, symmetric=True, emulated=True,
+                            diag_shift=0.25).cpu().numpy()
+    assert np.array_equal(Ks, Ks.T)
+    Ko = oracle.gaussian_kernel(A, A, sigma)
+    Ko[np.diag_indices_from(Ko)] += 0.25
+    assert relerr(Ks, Ko) <= RTOL
+
+
+@pytest.mark.parametrize("na,nb", [(1, 1), (129, 65), (300, 1000)])
+def test_emulated_gaussian_odd_shapes(cuda, oracle, cm_features, na, nb):
+    A, B = cm_features[:na], cm_features[1000 - nb:]
+    K = core.kernel_matrix("gaussian", torch.from_numpy(A).to(cuda), torch.from_numpy(B).to(cuda),
+                           1000.0, emulated=True).cpu().numpy()
+    assert relerr(K, oracle.gaussian_kernel(A, B, 1000.0)) <= RTOL
+
+
+def test_emulated_gaussian_small_sigma_falls_back(cuda, oracle):
+    g = load_golden("kernels_seed666.npz")
+    X, Xs = g["X"], g["Xs"]
+    for s in (0.05, 100.0):
+        K = core.kernel_matrix("gaussian", torch.from_numpy(X).to(cuda), torch.from_numpy(Xs).to(cuda),
+                               s, emulated=True).cpu().numpy()
+        Ko = oracle.gaussian_kernel(X, Xs, s)
+        assert np.allclose(K, Ko, rtol=1e-12, atol=0)
+
+
+def test_emulated_predict(cuda, oracle, cm_features):
+    rng = np.random.default_rng(4)
+    Xtr, Xte = cm_features[:900], cm_features[900:]
+    alpha = rng.normal(size=900)
+    Ks = oracle.gaussian_kernel(Xtr, Xte, 1000.0)
+    expect = Ks.T @ alpha
+    args = (torch.from_numpy(Xtr).to(cuda), torch.from_numpy(Xte).to(cuda), 1000.0,
+            torch.from_numpy(alpha).to(cuda))
+    y = core.predict("gaussian", *args, emulated=True).cpu().numpy()
+    scale = np.abs(Ks.T) @ np.abs(alpha)
+    assert np.max(np.abs(y - expect) / scale) <= 1e-12
+    assert np.array_equal(y, core.predict("gaussian", *args, emulated=True).cpu().numpy())

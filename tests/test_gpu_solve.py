@@ -162,3 +162,18 @@ def test_mixed_factor_info(cuda):
     _, info = lapack.dpotrf(np.asfortranarray(S), lower=0)
     St = torch.from_numpy(np.ascontiguousarray(S.T)).to(cuda)
     assert core.cholesky(St, precision="mixed") == info
+
+
+def test_syrk_emulated(cuda):
+    rng = np.random.default_rng(9)
+    n, k = 300, 200
+    P = rng.normal(size=(n, k)) * np.exp(rng.normal(size=(n, 1)))
+    C = rng.normal(size=(n, n))
+    Ct = torch.from_numpy(C).to(cuda)
+    core.syrk_emulated(Ct, torch.from_numpy(P).to(cuda))
+    out = Ct.cpu().numpy()
+    ref = C - P @ P.T
+    tri = np.tril_indices(n)
+    scale = np.abs(P) @ np.abs(P).T + np.abs(C)
+    assert np.max(np.abs(out[tri] - ref[tri]) / scale[tri]) < 1e-14
+    assert np.array_equal(np.triu(out, 1), np.triu(C, 1))
