@@ -37,7 +37,7 @@ constexpr int TM = 128;         // TMEM lanes per tile (j)
 constexpr int TN = 64;          // columns per level (i)
 constexpr int KC = 64;          // K chunk: one 128-byte swizzled row of bf16
 constexpr int S_MAX = 8;
-constexpr int A_STAGES = 3;
+constexpr int A_STAGES = 5;
 constexpr int A_BYTES = TM * KC * 2;  // 16 KB
 constexpr int B_BYTES = TN * KC * 2;  // 8 KB
 constexpr int RED_BYTES = 4 * TN * 8;  // predict: per-warp column sums
@@ -47,6 +47,8 @@ constexpr int SMEM_BYTES =
 enum Mode { kSyrk = 0, kKernelMatrix = 1, kPredict = 2 };
 
 struct TileArgs {
+    int ntiles;        // tiles in the (lower-triangular or full) tile list
+    int tj;            // tiles along j
     double *C;         // kSyrk: row-major C; kKernelMatrix: column-major K
     int64_t ldc;
     int jbase, jend;   // lanes: contiguous index range of C / K
@@ -65,7 +67,31 @@ struct TileArgs {
     double scale;         // -0.5 / sigma^2
     double diag_shift;
     const double *alpha;  // kPredict: weights of the j rows
-    double *partial;      // kPredict: [gridDim.x][iend - ibase] partial sums
+    double *partial;      // kPredict: [tiles along j][iend - ibase] partial sums
+};
+
+// Walks the tile list in increasing order.  With `lower`, row-block it (64 rows of
+// i) holds the j-blocks jt with jbase + 128 jt <= ibase + 64 it + 63 (the tiles that
+// reach the lower triangle); otherwise every jt.
+struct TileCursor {
+    int it = 0, base = 0;
+    __device__ __forceinline__ int count(const TileArgs &p, int r) const
+    {
+        if (!p.lower) return p.tj;
+        const int lim = p.ibase - p.jbase + 64 * r + 63;
+        return lim < 0 ? 0 : min(p.tj, lim / 128 + 1);
+    }
+    __device__ __forceinline__ void locate(const TileArgs &p, int t, int &jt, int &itl)
+    {
+        int c = count(p, it);
+        while (base + c <= t) {
+            base += c;
+            ++it;
+            c = count(p, it);
+        }
+        jt = t - base;
+        itl = it;
+    }
 };
 
 __device__ __forceinline__ double pow2i(int e)
@@ -85,30 +111,25 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
     unsigned char *Bbuf = base;                               // [2][S_MAX][B_BYTES]
     unsigned char *Aring = base + 2 * S_MAX * B_BYTES;        // [A_STAGES][A_BYTES]
     uint64_t *bars = (uint64_t *)(Aring + A_STAGES * A_BYTES);
-    uint64_t *bFull = bars, *bEmpty = bars + 2, *aFull = bars + 4, *aEmpty = bars + 7,
-             *done = bars + 10;
-    uint32_t *tmem_holder = (uint32_t *)(bars + 12);
+    uint64_t *bFull = bars, *bEmpty = bars + 2, *aFull = bars + 4, *aEmpty = bars + 4 + A_STAGES,
+             *tFull = bars + 4 + 2 * A_STAGES, *tEmpty = tFull + 1;
+    uint32_t *tmem_holder = (uint32_t *)(tEmpty + 1);
     double(*red)[TN] = (double(*)[TN])(bars + 32);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int j0 = p.jbase + blockIdx.x * TM;
-    const int i0 = p.ibase + blockIdx.y * TN;
-    const int ilast = min(i0 + TN, p.iend) - 1;
-    if (p.lower && j0 > ilast) return;  // tile entirely above the diagonal
     const int S = p.slices;
-    const int arow = p.a_row0 + (j0 - p.jbase);
-    const int brow = p.b_row0 + (i0 - p.ibase);
 
     if (threadIdx.x == 0) {
-        mbar_init(&bFull[0], 1);
-        mbar_init(&bFull[1], 1);
-        mbar_init(&bEmpty[0], 1);
-        mbar_init(&bEmpty[1], 1);
+        for (int k = 0; k < 2; ++k) {
+            mbar_init(&bFull[k], 1);
+            mbar_init(&bEmpty[k], 1);
+        }
         for (int k = 0; k < A_STAGES; ++k) {
             mbar_init(&aFull[k], 1);
             mbar_init(&aEmpty[k], 1);
         }
-        mbar_init(done, 1);
+        mbar_init(tFull, 1);
+        mbar_init(tEmpty, 128);
         fence_barrier_init();
     }
     if (warp == 0 && lane == 0) {
@@ -123,26 +144,32 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
 
     if (warp == 0) {
         if (lane == 0) {
-            // ---------------- TMA producer
-            int it = 0;
+            // ---------------- TMA producer: runs ahead across tiles
+            TileCursor cur;
+            int g = 0, it = 0;
             bool ok = true;
-            for (int c = 0; c < p.kchunks && ok; ++c) {
-                const int bb = c & 1;
-                if (c >= 2 && !mbar_wait(&bEmpty[bb], ((c >> 1) - 1) & 1)) {
-                    ok = false;
-                    break;
-                }
-                mbar_expect_tx(&bFull[bb], (uint32_t)(S * B_BYTES));
-                for (int t = 0; t < S; ++t)
-                    tma_load_3d(Bbuf + (bb * S_MAX + t) * B_BYTES, &mapB, &bFull[bb], c * KC, brow, t);
-                for (int s = 0; s < S; ++s, ++it) {
-                    const int st = it % A_STAGES, round = it / A_STAGES;
-                    if (round >= 1 && !mbar_wait(&aEmpty[st], (round - 1) & 1)) {
+            for (int t = blockIdx.x; t < p.ntiles && ok; t += gridDim.x) {
+                int jt, itl;
+                cur.locate(p, t, jt, itl);
+                const int arow = p.a_row0 + jt * TM, brow = p.b_row0 + itl * TN;
+                for (int c = 0; c < p.kchunks && ok; ++c, ++g) {
+                    const int bb = g & 1;
+                    if (g >= 2 && !mbar_wait(&bEmpty[bb], ((g >> 1) - 1) & 1)) {
                         ok = false;
                         break;
                     }
-                    mbar_expect_tx(&aFull[st], (uint32_t)A_BYTES);
-                    tma_load_3d(Aring + st * A_BYTES, &mapA, &aFull[st], c * KC, arow, s);
+                    mbar_expect_tx(&bFull[bb], (uint32_t)(S * B_BYTES));
+                    for (int u = 0; u < S; ++u)
+                        tma_load_3d(Bbuf + (bb * S_MAX + u) * B_BYTES, &mapB, &bFull[bb], c * KC, brow, u);
+                    for (int s = 0; s < S; ++s, ++it) {
+                        const int st = it % A_STAGES, round = it / A_STAGES;
+                        if (round >= 1 && !mbar_wait(&aEmpty[st], (round - 1) & 1)) {
+                            ok = false;
+                            break;
+                        }
+                        mbar_expect_tx(&aFull[st], (uint32_t)A_BYTES);
+                        tma_load_3d(Aring + st * A_BYTES, &mapA, &aFull[st], c * KC, arow, s);
+                    }
                 }
             }
             if (!ok) atomicOr(p.err, 1);
@@ -151,117 +178,157 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
         if (lane == 0) {
             // ---------------- MMA issuer
             const uint32_t idesc = idesc_bf16_f32(TM, TN);
-            int it = 0;
+            int g = 0, it = 0, u = 0;
             bool ok = true;
-            for (int c = 0; c < p.kchunks && ok; ++c) {
-                const int bb = c & 1;
-                if (!mbar_wait(&bFull[bb], (c >> 1) & 1)) {
+            for (int t = blockIdx.x; t < p.ntiles && ok; t += gridDim.x, ++u) {
+                if (u > 0 && !mbar_wait(tEmpty, (u - 1) & 1)) {
                     ok = false;
                     break;
                 }
                 fence_after_sync();
-                for (int s = 0; s < S; ++s, ++it) {
-                    const int st = it % A_STAGES, round = it / A_STAGES;
-                    if (!mbar_wait(&aFull[st], round & 1)) {
+                for (int c = 0; c < p.kchunks && ok; ++c, ++g) {
+                    const int bb = g & 1;
+                    if (!mbar_wait(&bFull[bb], (g >> 1) & 1)) {
                         ok = false;
                         break;
                     }
                     fence_after_sync();
-                    const uint64_t da = desc_sw128(Aring + st * A_BYTES);
-                    for (int t = 0; t + s < S; ++t) {
-                        const uint64_t db = desc_sw128(Bbuf + (bb * S_MAX + t) * B_BYTES);
-                        const uint32_t dst = tmem + (uint32_t)((s + t) * TN);
-#pragma unroll
-                        for (int kk = 0; kk < KC / 16; ++kk) {
-                            const uint32_t acc = (c > 0 || s > 0 || kk > 0) ? 1u : 0u;
-                            mma_bf16(dst, da + (uint64_t)(kk * 2), db + (uint64_t)(kk * 2), idesc, acc);
+                    for (int s = 0; s < S; ++s, ++it) {
+                        const int st = it % A_STAGES, round = it / A_STAGES;
+                        if (!mbar_wait(&aFull[st], round & 1)) {
+                            ok = false;
+                            break;
                         }
+                        fence_after_sync();
+                        const uint64_t da = desc_sw128(Aring + st * A_BYTES);
+                        for (int v = 0; v + s < S; ++v) {
+                            const uint64_t db = desc_sw128(Bbuf + (bb * S_MAX + v) * B_BYTES);
+                            const uint32_t dst = tmem + (uint32_t)((s + v) * TN);
+#pragma unroll
+                            for (int kk = 0; kk < KC / 16; ++kk) {
+                                const uint32_t acc = (c > 0 || s > 0 || kk > 0) ? 1u : 0u;
+                                mma_bf16(dst, da + (uint64_t)(kk * 2), db + (uint64_t)(kk * 2), idesc, acc);
+                            }
+                        }
+                        mma_commit(&aEmpty[st]);
                     }
-                    mma_commit(&aEmpty[st]);
+                    mma_commit(&bEmpty[bb]);
                 }
-                mma_commit(&bEmpty[bb]);
+                mma_commit(tFull);
             }
             if (!ok) atomicOr(p.err, 2);
-            mma_commit(done);
         }
     } else {
         // ---------------- epilogue: warps 2..5 -> TMEM lane quarters 2,3,0,1
         const int q = warp & 3;
         const int jl = q * 32 + lane;
-        const int j = j0 + jl;
-        bool ok = mbar_wait(done, 0);
-        if (!ok && lane == 0) atomicOr(p.err, 4);
-        fence_after_sync();
-        const int ej = (j < p.jend) ? p.expA[arow + jl] : 0;
-        double aj = 0.0, aw = 0.0;
-        if (MODE != kSyrk && j < p.jend) {
-            aj = p.scale * p.normA[arow + jl];
-            if (MODE == kPredict) aw = p.alpha[j];
-        }
         const int H = (S + 1) / 2;
         const int lo_levels = S - H;
+        const int shift = lo_levels >= 2 ? 12 : 0;
         const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
-        for (int g = 0; g < TN / 16; ++g) {
-            uint32_t v[S_MAX][16];
+        TileCursor cur;
+        int u = 0;
+        bool ok = true;
+        for (int t = blockIdx.x; t < p.ntiles; t += gridDim.x, ++u) {
+            int jt, itl;
+            cur.locate(p, t, jt, itl);
+            const int j0 = p.jbase + jt * TM, i0 = p.ibase + itl * TN;
+            const int arow = p.a_row0 + jt * TM, brow = p.b_row0 + itl * TN;
+            const int j = j0 + jl;
+            if (ok && !mbar_wait(tFull, u & 1)) {
+                ok = false;
+                if (lane == 0) atomicOr(p.err, 4);
+            }
+            fence_after_sync();
+            const bool jvalid = j < p.jend;
+            const int ej = jvalid ? p.expA[arow + jl] : 0;
+            double aj = 0.0, aw = 0.0;
+            if (MODE != kSyrk && jvalid) {
+                aj = p.scale * p.normA[arow + jl];
+                if (MODE == kPredict) aw = p.alpha[j];
+            }
+            for (int gq = 0; gq < TN / 16; ++gq) {
+                uint32_t v[S_MAX][16];
 #pragma unroll
-            for (int l = 0; l < S_MAX; ++l)
-                if (l < S) tmem_ld16(lane_base + (uint32_t)(l * TN + g * 16), v[l]);
-            tmem_ld_wait();
-            if (!ok) continue;
-#pragma unroll
-            for (int col = 0; col < 16; ++col) {
-                const int il = g * 16 + col;
-                const int i = i0 + il;
-                long long hi = 0, lo = 0;
-#pragma unroll
-                for (int l = 0; l < S_MAX; ++l) {
-                    if (l >= S) break;
-                    const long long d = (long long)__float2int_rn(__uint_as_float(v[l][col]));
-                    if (l < H) hi = hi * 128 + d;
-                    else lo = lo * 128 + d;
+                for (int l = 0; l < S_MAX; ++l)
+                    if (l < S) tmem_ld16(lane_base + (uint32_t)(l * TN + gq * 16), v[l]);
+                tmem_ld_wait();
+                if (gq == TN / 16 - 1) {
+                    // every level of this tile is in registers: hand TMEM back
+                    fence_before_sync();
+                    mbar_arrive(tEmpty);
                 }
-                // value = hi * 128^lo_levels + lo, kept in 62 bits by dropping the lowest
-                // `shift` bits of lo (far below FP64 resolution of the value)
-                const int shift = lo_levels >= 2 ? 12 : 0;
-                const long long v64 = (hi << (7 * lo_levels - shift)) + (lo >> shift);
-                const bool valid = j < p.jend && i < p.iend;
+                if (!ok) continue;
+                long long v64[16];
+#pragma unroll
+                for (int col = 0; col < 16; ++col) {
+                    long long hi = 0, lo = 0;
+#pragma unroll
+                    for (int l = 0; l < S_MAX; ++l) {
+                        if (l >= S) break;
+                        const long long d = (long long)__float2int_rn(__uint_as_float(v[l][col]));
+                        if (l < H) hi = hi * 128 + d;
+                        else lo = lo * 128 + d;
+                    }
+                    // value = hi * 128^lo_levels + lo, kept in 62 bits by dropping the
+                    // lowest `shift` bits of lo (far below FP64 resolution of the value)
+                    v64[col] = (hi << (7 * lo_levels - shift)) + (lo >> shift);
+                }
                 if (MODE == kSyrk) {
-                    if (valid && (!p.lower || j <= i)) {
-                        const int ei = p.expB[brow + il];
-                        const double scale = pow2i(ei + ej + shift - 7 * (S + 1));
-                        double *cp = p.C + (int64_t)i * p.ldc + j;
-                        *cp = fma(-(double)v64, scale, *cp);
+                    double cv[16];
+#pragma unroll
+                    for (int col = 0; col < 16; ++col) {
+                        const int i = i0 + gq * 16 + col;
+                        cv[col] = (jvalid && i < p.iend && (!p.lower || j <= i))
+                                      ? p.C[(int64_t)i * p.ldc + j] : 0.0;
+                    }
+#pragma unroll
+                    for (int col = 0; col < 16; ++col) {
+                        const int il = gq * 16 + col;
+                        const int i = i0 + il;
+                        if (jvalid && i < p.iend && (!p.lower || j <= i)) {
+                            const double sc = pow2i(p.expB[brow + il] + ej + shift - 7 * (S + 1));
+                            p.C[(int64_t)i * p.ldc + j] = fma(-(double)v64[col], sc, cv[col]);
+                        }
                     }
                 } else {
-                    double kv = 0.0;
-                    if (valid) {
-                        // x = scale * (|a|^2 + |b|^2 - 2 a.b), clamped at 0 from above
-                        const int ei = p.expB[brow + il];
-                        const double w = -2.0 * p.scale * pow2i(ei + ej + shift - 7 * (S + 1));
-                        const double x = fmin(fma((double)v64, w, aj + p.scale * p.normB[brow + il]), 0.0);
-                        kv = exp(x);
-                        if (MODE == kKernelMatrix && p.lower && i == j) kv = 1.0 + p.diag_shift;
-                    }
-                    if (MODE == kKernelMatrix) {
-                        if (valid && (!p.lower || j <= i)) {
-                            p.C[(int64_t)i * p.ldc + j] = kv;
-                            if (p.lower && j < i) p.C[(int64_t)j * p.ldc + i] = kv;
+#pragma unroll
+                    for (int col = 0; col < 16; ++col) {
+                        const int il = gq * 16 + col;
+                        const int i = i0 + il;
+                        const bool valid = jvalid && i < p.iend;
+                        double kv = 0.0;
+                        if (valid) {
+                            // x = scale * (|a|^2 + |b|^2 - 2 a.b), clamped at 0 from above
+                            const double w =
+                                -2.0 * p.scale * pow2i(p.expB[brow + il] + ej + shift - 7 * (S + 1));
+                            const double x =
+                                fmin(fma((double)v64[col], w, aj + p.scale * p.normB[brow + il]), 0.0);
+                            kv = exp(x);
+                            if (MODE == kKernelMatrix && p.lower && i == j) kv = 1.0 + p.diag_shift;
                         }
-                    } else {
-                        double c = valid ? kv * aw : 0.0;
-                        for (int off = 16; off > 0; off >>= 1) c += __shfl_xor_sync(0xffffffffu, c, off);
-                        if (lane == 0) red[q][il] = c;
+                        if (MODE == kKernelMatrix) {
+                            if (valid && (!p.lower || j <= i)) {
+                                p.C[(int64_t)i * p.ldc + j] = kv;
+                                if (p.lower && j < i) p.C[(int64_t)j * p.ldc + i] = kv;
+                            }
+                        } else {
+                            double c = valid ? kv * aw : 0.0;
+                            for (int off = 16; off > 0; off >>= 1) c += __shfl_xor_sync(0xffffffffu, c, off);
+                            if (lane == 0) red[q][il] = c;
+                        }
                     }
                 }
             }
-        }
-        if (MODE == kPredict) {
-            // the four epilogue warps add their column sums in a fixed order
-            asm volatile("bar.sync 1, 128;" ::: "memory");
-            const int t = threadIdx.x - 64;
-            if (ok && t < TN && i0 + t < p.iend)
-                p.partial[(int64_t)blockIdx.x * (p.iend - p.ibase) + (i0 - p.ibase) + t] =
-                    ((red[0][t] + red[1][t]) + red[2][t]) + red[3][t];
+            if (MODE == kPredict) {
+                // the four epilogue warps add their column sums in a fixed order
+                asm volatile("bar.sync 1, 128;" ::: "memory");
+                const int tt = threadIdx.x - 64;
+                if (ok && tt < TN && i0 + tt < p.iend)
+                    p.partial[(int64_t)jt * (p.iend - p.ibase) + (i0 - p.ibase) + tt] =
+                        ((red[0][tt] + red[1][tt]) + red[2][tt]) + red[3][tt];
+                asm volatile("bar.sync 1, 128;" ::: "memory");
+            }
         }
     }
     fence_before_sync();
@@ -395,6 +462,33 @@ __global__ void reduce_partial_rows_kernel(const double *__restrict__ partial, i
     y[i] = s;
 }
 
+int sm_count()
+{
+    static int n = 0;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            n = 148;
+    });
+    return n;
+}
+
+// Same tile list as TileCursor on the device.
+int count_tiles(int jbase, int jend, int ibase, int iend, int lower, int &tj)
+{
+    tj = (int)qmlg::ceil_div(jend - jbase, TM);
+    const int ti = (int)qmlg::ceil_div(iend - ibase, TN);
+    if (!lower) return tj * ti;
+    int total = 0;
+    for (int r = 0; r < ti; ++r) {
+        const int lim = ibase - jbase + 64 * r + 63;
+        total += lim < 0 ? 0 : std::min(tj, lim / 128 + 1);
+    }
+    return total;
+}
+
 void set_smem_attrs()
 {
     static std::once_flag once;
@@ -476,6 +570,8 @@ int emu_tc_update(double *C, int64_t ldc, int jbase, int jend, int ibase, int ie
     if (st != QMLG_OK) return st;
     set_smem_attrs();
     TileArgs a{};
+    a.ntiles = count_tiles(jbase, jend, ibase, iend, lower, a.tj);
+    if (a.ntiles == 0) return QMLG_OK;
     a.C = C;
     a.ldc = ldc;
     a.jbase = jbase;
@@ -490,7 +586,7 @@ int emu_tc_update(double *C, int64_t ldc, int jbase, int jend, int ibase, int ie
     a.expB = expo;
     a.lower = lower;
     a.err = d_err;
-    dim3 grid((unsigned)ceil_div(jend - jbase, TM), (unsigned)ceil_div(iend - ibase, TN));
+    const int grid = std::min(a.ntiles, sm_count());
     emu_tc_kernel<kSyrk><<<grid, 192, SMEM_BYTES, s>>>(mA, mB, a);
     count_launches(1);
     return check_launch();
@@ -588,6 +684,7 @@ int launch_gauss(int mode, const GaussBufs &b, int na, int nb, int d, int S, dou
     if (st != QMLG_OK) return st;
     set_smem_attrs();
     TileArgs a{};
+    a.ntiles = count_tiles(0, na, 0, nb, sym ? 1 : 0, a.tj);
     a.C = K;
     a.ldc = ldk;
     a.jbase = 0;
@@ -606,7 +703,7 @@ int launch_gauss(int mode, const GaussBufs &b, int na, int nb, int d, int S, dou
     a.diag_shift = diag_shift;
     a.alpha = alpha;
     a.partial = b.partial;
-    dim3 grid((unsigned)qmlg::ceil_div(na, TM), (unsigned)qmlg::ceil_div(nb, TN));
+    const int grid = std::min(a.ntiles, sm_count());
     if (mode == kKernelMatrix)
         emu_tc_kernel<kKernelMatrix><<<grid, 192, SMEM_BYTES, s>>>(mA, mB, a);
     else
