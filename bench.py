@@ -47,6 +47,11 @@ def parse():
     p.add_argument("--seed", type=int, default=2024)
     p.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    p.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
+    p.add_argument("--serve-n", type=int, default=50000, help="resident model size")
+    p.add_argument("--serve-rate", type=float, default=100.0, help="query arrivals per second")
+    p.add_argument("--serve-seconds", type=float, default=10.0)
+    p.add_argument("--serve-fit-every", type=int, default=50, help="every k-th arrival is a fit")
     return p.parse_args()
 
 
@@ -193,6 +198,47 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def run_serving(a, dev):
+    """Continuous-batching serving: one resident Gaussian model of serve_n molecules,
+    Poisson query arrivals (1..4096 molecules, log-uniform), fits of N in
+    [1000, 20000] interleaved every serve_fit_every-th arrival."""
+    import torch
+
+    from qml_gb300 import core, serving
+    from qml_gb300.krr import KRR, molecules_to_device
+    from qml_gb300.synthetic import generate_molecules
+
+    pool = generate_molecules(a.serve_n + 30000, seed=a.seed + 7)
+    train = pool.slice(0, a.serve_n)
+    queries = pool.slice(a.serve_n, a.serve_n + 30000)
+    z, r, o = molecules_to_device(train, device=dev)
+    X = core.coulomb_matrix_batch(z, r, o, 23)
+    y = torch.from_numpy(train.labels).to(dev)
+    t0 = time.perf_counter()
+    model = KRR(sigma=a.sigma, lam=a.lam, precision="mixed").fit(X, y)
+    torch.cuda.synchronize()
+    fit_s = time.perf_counter() - t0
+    ex = serving.GpuExecutor(device=dev, n_streams=4)
+    ex.add_model("main", X, model.alpha, a.sigma)
+    # warm the streams (workspaces, pinned buffers) outside the measured run
+    warm = serving.poisson_workload(50.0, 0.2, queries, "main", seed=a.seed + 1, max_query=4096)
+    serving.Server(ex, serving.Scheduler(64 << 30, model_sizes={"main": a.serve_n})).run(warm)
+    reqs = serving.poisson_workload(a.serve_rate, a.serve_seconds, queries, "main",
+                                    fit_every=a.serve_fit_every, fit_sizes=(1000, 20000),
+                                    seed=a.seed + 2, max_query=4096)
+    sched = serving.Scheduler(budget_bytes=64 << 30, max_slots=4,
+                              model_sizes={"main": a.serve_n})
+    done = serving.Server(ex, sched).run(reqs)
+    st = serving.latency_stats(done)
+    st.update({"resident_n": a.serve_n, "resident_fit_s": fit_s, "rate_hz": a.serve_rate,
+               "duration_s": a.serve_seconds, "query_molecules": "log-uniform 1..4096",
+               "fit_sizes": "log-uniform 1000..20000", "hbm_budget_gb": 64,
+               "precision": "mixed"})
+    st["fit_latency_ms"] = {"n": len(st["fit_latency_ms"]),
+                            "max": max(st["fit_latency_ms"]) if st["fit_latency_ms"] else None}
+    return st
+
+
 def run_ours(a):
     import numpy as np
     import torch
@@ -334,6 +380,10 @@ def run_ours(a):
     torch.cuda.synchronize()
     launches = int(lib.qmlg_launch_count() - c0) * a.steps
 
+    serving_stats = None
+    if not a.no_serving:
+        serving_stats = run_serving(a, dev)
+
     if rank != 0:
         return 0
     # roofline of the dominant kernel (the emulated trailing update): its algorithm
@@ -368,6 +418,7 @@ def run_ours(a):
             "e2e": {"value": e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "fits_per_s": world / (ms / 1e3),
+            "serving": serving_stats,
             "gpu_launches": launches, "clocks": clocks.summary(), "roofline": roofline,
             "cpu_baseline": cpu, "stages_s": stages, "solve_report": rep_m,
             "fp64_path": fp64}

@@ -161,6 +161,20 @@ int qmlg_predict_emulated(const double *Xtrain, int64_t ldtrain, int ntrain,
                           const double *alpha, double *yhat, void *workspace, size_t ws_bytes,
                           void *stream);
 
+/*
+ * qmlg_predict_emulated without any host synchronisation, for serving loops that
+ * keep several streams busy: always 8 digit planes; the accuracy bound and any
+ * bounded-wait timeout are checked on the device and reported by OR-ing into the
+ * caller's device int *d_flag (8 = the 1e-12 bound is not met for this sigma and
+ * data, so recompute with qmlg_predict_fused; 1/2/4 = a tensor-core wait gave
+ * up).  Clear *d_flag before the call; read it after the stream has completed.
+ * Same workspace size as qmlg_predict_emulated.
+ */
+int qmlg_predict_emulated_async(const double *Xtrain, int64_t ldtrain, int ntrain,
+                                const double *Xtest, int64_t ldtest, int ntest, int d,
+                                double sigma, const double *alpha, double *yhat, int *d_flag,
+                                void *workspace, size_t ws_bytes, void *stream);
+
 /* ---- Cholesky solve ------------------------------------------------------- */
 
 #define QMLG_PREC_FP64 0   /* plain FP64 blocked Cholesky (LAPACK dpotrf semantics) */

@@ -82,6 +82,8 @@ SIGNATURES = {
                                            _P, _SZ, _P]),
     "qmlg_predict_emulated_workspace_size": (_SZ, [_I, _I, _I]),
     "qmlg_predict_emulated": (_I, [_P, _I64, _I, _P, _I64, _I, _I, _D, _P, _P, _P, _SZ, _P]),
+    "qmlg_predict_emulated_async": (_I, [_P, _I64, _I, _P, _I64, _I, _I, _D, _P, _P, _P, _P,
+                                         _SZ, _P]),
     "qmlg_predict_gemv": (_I, [_P, _I64, _I, _I, _P, _P, _P]),
     "qmlg_predict_workspace_size": (_SZ, [_I, _I]),
     "qmlg_predict_fused": (_I, [_I, _P, _I64, _I, _P, _I64, _I, _I, _D, _P, _P, _P, _SZ, _P]),

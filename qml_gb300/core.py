@@ -36,14 +36,17 @@ def _require_cuda(*tensors):
 
 
 class _WorkspaceCache:
-    """One growing scratch buffer per device, reused across calls on that device."""
+    """One growing scratch buffer per (device, stream), reused across calls."""
 
     def __init__(self):
         self._buf = {}
 
     def get(self, nbytes: int, device) -> torch.Tensor:
+        # one buffer per (device, stream): work queued on different streams never
+        # shares scratch memory
         dev = torch.device(device)
-        key = dev.index if dev.index is not None else torch.cuda.current_device()
+        index = dev.index if dev.index is not None else torch.cuda.current_device()
+        key = (index, torch.cuda.current_stream(index).cuda_stream)
         buf = self._buf.get(key)
         if buf is None or buf.numel() < nbytes:
             buf = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=dev)
@@ -83,6 +86,26 @@ def coulomb_matrix_batch(charges: torch.Tensor, coordinates: torch.Tensor,
     st = int(status.item())
     if st != 0:
         _lib.check(st, "qmlg_coulomb_matrix")
+    return out
+
+
+def coulomb_matrix_batch_async(charges: torch.Tensor, coordinates: torch.Tensor,
+                               offsets: torch.Tensor, size: int = 23, sorting: str = "row-norm",
+                               status: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """coulomb_matrix_batch without reading the device status back (no host
+    synchronisation).  When `status` (a zeroed int32 CUDA tensor) is given, a
+    molecule with too many atoms sets it to QMLG_E_TOO_MANY_ATOMS."""
+    if sorting not in _SORTING:
+        raise ValueError("Unknown sorting scheme requested: %r" % (sorting,))
+    _require_cuda(charges, coordinates, offsets)
+    n_mol = offsets.shape[0] - 1
+    out = torch.empty((n_mol, size * (size + 1) // 2), dtype=torch.float64, device=charges.device)
+    check(lib().qmlg_coulomb_matrix(charges.contiguous().data_ptr(),
+                                    coordinates.contiguous().data_ptr(),
+                                    offsets.to(torch.int64).contiguous().data_ptr(), n_mol, size,
+                                    _SORTING[sorting], out.data_ptr(),
+                                    status.data_ptr() if status is not None else None,
+                                    _stream(charges.device)), "qmlg_coulomb_matrix")
     return out
 
 
@@ -173,6 +196,28 @@ def predict(kind: str, Xtrain: torch.Tensor, Xtest: torch.Tensor, sigma: float,
     return out
 
 
+def predict_async(Xtrain: torch.Tensor, Xtest: torch.Tensor, sigma: float, alpha: torch.Tensor,
+                  flag: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """Gaussian prediction on the tensor cores with no host synchronisation
+    (qmlg_predict_emulated_async).  flag: a zeroed int32 CUDA tensor of one element;
+    nonzero after the stream completes means recompute with predict(...)."""
+    _require_cuda(Xtrain, Xtest, alpha, flag)
+    Xtrain, ldtr = _rows(Xtrain)
+    Xtest, ldte = _rows(Xtest)
+    alpha = alpha.contiguous()
+    ntr, nte, d = Xtrain.shape[0], Xtest.shape[0], Xtrain.shape[1]
+    if out is None:
+        out = torch.empty(nte, dtype=torch.float64, device=Xtrain.device)
+    ws_bytes = lib().qmlg_predict_emulated_workspace_size(ntr, nte, d)
+    ws = workspaces.get(ws_bytes, Xtrain.device)
+    check(lib().qmlg_predict_emulated_async(Xtrain.data_ptr(), ldtr, ntr, Xtest.data_ptr(), ldte,
+                                            nte, d, float(sigma), alpha.data_ptr(), out.data_ptr(),
+                                            flag.data_ptr(), ws.data_ptr(), ws.numel(),
+                                            _stream(Xtrain.device)),
+          "qmlg_predict_emulated_async")
+    return out
+
+
 def predict_gemv(Ks: torch.Tensor, alpha: torch.Tensor) -> torch.Tensor:
     """yhat = Ks^T alpha for a Fortran-ordered Ks (ntrain, ntest) (np.dot(Ks.T, alpha))."""
     _require_cuda(Ks, alpha)
@@ -203,7 +248,7 @@ def _colmajor(A: torch.Tensor) -> Tuple[torch.Tensor, int]:
 
 
 def solve(A: torch.Tensor, y: torch.Tensor, lam: float = 0.0, precision: str = "mixed",
-          max_outer: int = 10, tol: float = 1e-15, allow_fallback: bool = True,
+          max_outer: int = 10, tol: float = 1e-14, allow_fallback: bool = True,
           raise_on_info: bool = True):
     """Solve (A + lam I) x = y on the GPU.  Returns (x, report dict).
 

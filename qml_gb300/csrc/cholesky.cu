@@ -36,54 +36,76 @@ __global__ void __launch_bounds__(256)
 potrf_diag_kernel(double *__restrict__ A, int64_t lda, int n, int k0, double shift,
                   int *__restrict__ info)
 {
-    // Thread t owns row r = t / 4 and the columns s = t % 4 (mod 4) of that row.
-    // Per column c: (A) the owners of column c scale it by 1/L_cc; (B) rank-1 update
-    // of the trailing triangle, after which the owner of (c+1, c+1) takes its pivot.
+    // The 64 x 64 block in shared memory, factorised in four 16-column sub-panels:
+    // warp 0 factors the 16 x 16 diagonal sub-block (warp-synchronous), every thread
+    // then solves the rows below it (one row per thread) and applies the rank-16
+    // update to the trailing sub-matrix.
     __shared__ double S[NB][NB + 1];
-    __shared__ double dinv[NB];
     __shared__ int failed;
     if (*info != 0) return;
     const int tid = threadIdx.x;
     const int nb = min(NB, n - k0);
     for (int e = tid; e < NB * NB; e += blockDim.x) {
         const int r = e >> 6, c = e & 63;
-        double v = 0.0;
-        if (r < nb && c <= r) v = A[(int64_t)(k0 + r) * lda + (k0 + c)];
-        if (r == c && r < nb) v += shift;
+        double v = (r == c) ? 1.0 : 0.0;  // identity padding keeps short blocks regular
+        if (r < nb && c <= r) v = A[(int64_t)(k0 + r) * lda + (k0 + c)] + (r == c ? shift : 0.0);
         S[r][c] = v;
     }
+    if (tid == 0) failed = 0;
     __syncthreads();
-    const int r = tid >> 2, s0 = tid & 3;
-    if (tid == 0) {
-        failed = 0;
-        const double p = S[0][0];
-        if (!(p > 0.0) || !isfinite(p)) {
-            failed = 1;
-            atomicCAS(info, 0, k0 + 1);
-        } else {
-            const double d = sqrt(p);
-            S[0][0] = d;
-            dinv[0] = 1.0 / d;
-        }
-    }
-    __syncthreads();
-    for (int c = 0; c < nb; ++c) {
-        if (failed) return;
-        if (r > c && r < nb && s0 == (c & 3)) S[r][c] *= dinv[c];
-        __syncthreads();
-        if (r > c && r < nb) {
-            const double lrc = S[r][c];
-            for (int s = c + 1 + ((s0 - c - 1) & 3); s <= r; s += 4) S[r][s] = fma(-lrc, S[s][c], S[r][s]);
-            if (r == c + 1 && s0 == (r & 3)) {
-                const double p = S[r][r];
-                if (!(p > 0.0) || !isfinite(p)) {
-                    failed = 1;
-                    atomicCAS(info, 0, k0 + r + 1);
-                } else {
-                    const double d = sqrt(p);
-                    S[r][r] = d;
-                    dinv[r] = 1.0 / d;
+    for (int b0 = 0; b0 < NB; b0 += 16) {
+        if (tid < 32) {
+            const int lane = tid;
+            for (int c = b0; c < b0 + 16; ++c) {
+                if (lane == 0) {
+                    const double p = S[c][c];
+                    if (!(p > 0.0) || !isfinite(p)) {
+                        if (c < nb && !failed) atomicCAS(info, 0, k0 + c + 1);
+                        failed = 1;
+                        S[c][c] = 1.0;
+                    } else {
+                        S[c][c] = sqrt(p);
+                    }
                 }
+                __syncwarp();
+                const double dinv = 1.0 / S[c][c];
+                const int r = c + 1 + lane;
+                if (r < b0 + 16) S[r][c] *= dinv;
+                __syncwarp();
+                for (int e = lane; e < 16 * 16; e += 32) {
+                    const int rr = b0 + (e >> 4), cc = b0 + (e & 15);
+                    if (cc > c && rr >= cc) S[rr][cc] = fma(-S[rr][c], S[cc][c], S[rr][cc]);
+                }
+                __syncwarp();
+            }
+        }
+        __syncthreads();
+        if (failed) return;
+        // rows below the sub-block: X <- X L_bb^-T, one row per thread
+        const int r = b0 + 16 + tid;
+        if (r < NB) {
+            double x[16];
+#pragma unroll
+            for (int c = 0; c < 16; ++c) x[c] = S[r][b0 + c];
+#pragma unroll
+            for (int c = 0; c < 16; ++c) {
+                x[c] = x[c] / S[b0 + c][b0 + c];
+#pragma unroll
+                for (int c2 = c + 1; c2 < 16; ++c2) x[c2] = fma(-x[c], S[b0 + c2][b0 + c], x[c2]);
+            }
+#pragma unroll
+            for (int c = 0; c < 16; ++c) S[r][b0 + c] = x[c];
+        }
+        __syncthreads();
+        // rank-16 update of the trailing lower triangle
+        const int t0 = b0 + 16, m = NB - t0;
+        for (int e = tid; e < m * m; e += blockDim.x) {
+            const int rr = t0 + e / m, cc = t0 + e % m;
+            if (cc <= rr) {
+                double acc = S[rr][cc];
+#pragma unroll
+                for (int c = 0; c < 16; ++c) acc = fma(-S[rr][b0 + c], S[cc][b0 + c], acc);
+                S[rr][cc] = acc;
             }
         }
         __syncthreads();
@@ -452,6 +474,153 @@ trsv_bwd_coop_kernel(const double *__restrict__ A, int64_t lda, int n, double *_
     }
 }
 
+// Inverse of every 64 x 64 diagonal block of the factor (lower triangular), one CTA
+// per block: column c of L_kk^{-1} by forward substitution (thread c).  Blocks of
+// a short last block are padded with the identity.
+__global__ void __launch_bounds__(64)
+invert_diag_blocks_kernel(const double *__restrict__ A, int64_t lda, int n,
+                          double *__restrict__ Linv)
+{
+    __shared__ double L[NB][NB + 1];
+    __shared__ double X[NB][NB + 1];
+    const int kb = blockIdx.x, k0 = kb * NB, nb = min(NB, n - k0);
+    const int tid = threadIdx.x;
+    for (int e = tid; e < NB * NB; e += blockDim.x) {
+        const int r = e >> 6, c = e & 63;
+        double v = (r == c) ? 1.0 : 0.0;
+        if (r < nb && c <= r) v = A[(int64_t)(k0 + r) * lda + (k0 + c)];
+        L[r][c] = v;
+    }
+    __syncthreads();
+    const int c = tid;  // column of the inverse
+    for (int r = 0; r < NB; ++r) {
+        double v = (r == c) ? 1.0 : 0.0;
+        for (int t = c; t < r; ++t) v = fma(-L[r][t], X[t][c], v);
+        X[r][c] = (r >= c) ? v / L[r][r] : 0.0;
+    }
+    __syncthreads();
+    double *dst = Linv + (int64_t)kb * NB * NB;
+    for (int e = tid; e < NB * NB; e += blockDim.x) dst[e] = X[e >> 6][e & 63];
+}
+
+// y[0..64) = M v for a 64 x 64 row-major M (M in global memory, v in shared memory);
+// 256 threads: row r = tid / 4, quarter tid % 4 of the columns, combined by shuffles.
+__device__ __forceinline__ double gemv64_row(const double *__restrict__ M, int64_t ldm,
+                                             const double *v, int tid, int rows)
+{
+    // rows >= `rows` contribute 0 and are not read; every lane runs the shuffles
+    const int r = tid >> 2, qq = tid & 3;
+    double s = 0.0;
+    if (r < rows) {
+        const double *row = M + (int64_t)r * ldm + qq * 16;
+#pragma unroll
+        for (int c = 0; c < 16; ++c) s = fma(row[c], v[qq * 16 + c], s);
+    }
+    s += __shfl_xor_sync(0xffffffffu, s, 1);
+    s += __shfl_xor_sync(0xffffffffu, s, 2);
+    return s;
+}
+
+// y[t] = sum_r M[r][t] v[r] (transposed), same thread layout: t = tid / 4.
+__device__ __forceinline__ double gemv64_col(const double *__restrict__ M, int64_t ldm,
+                                             const double *v, int tid)
+{
+    const int t = tid >> 2, qq = tid & 3;
+    double s = 0.0;
+#pragma unroll
+    for (int r = 0; r < 16; ++r) s = fma(M[(int64_t)(qq * 16 + r) * ldm + t], v[qq * 16 + r], s);
+    s += __shfl_xor_sync(0xffffffffu, s, 1);
+    s += __shfl_xor_sync(0xffffffffu, s, 2);
+    return s;
+}
+
+// Forward solve with the block inverses: step kb, CTA 0 forms
+// b = x_kb - L[kb, kb-1] z_{kb-1} and z_kb = L_kk^{-1} b; the other CTAs apply z_{kb-1}
+// to every row below block kb.
+__global__ void __launch_bounds__(TRSV_THREADS)
+trsv_fwd_inv_kernel(const double *__restrict__ A, int64_t lda, int n,
+                    const double *__restrict__ Linv, double *__restrict__ x)
+{
+    cg::grid_group grid = cg::this_grid();
+    __shared__ double zp[NB];
+    __shared__ double bb[NB];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    constexpr int nw = TRSV_THREADS / 32;
+    const int nblk = (n + NB - 1) / NB;
+    for (int kb = 0; kb < nblk; ++kb) {
+        const int k0 = kb * NB, nb = min(NB, n - k0), kp = k0 - NB;
+        if (kb > 0) {
+            if (tid < NB) zp[tid] = x[kp + tid];
+            __syncthreads();
+        }
+        if (blockIdx.x == 0) {
+            double s = 0.0;
+            if (kb > 0) s = gemv64_row(A + (int64_t)k0 * lda + kp, lda, zp, tid, nb);
+            if ((tid & 3) == 0) {
+                const int r = tid >> 2;
+                bb[r] = r < nb ? x[k0 + r] - s : 0.0;
+            }
+            __syncthreads();
+            const double z = gemv64_row(Linv + (int64_t)kb * NB * NB, NB, bb, tid, NB);
+            if ((tid & 3) == 0 && (tid >> 2) < nb) x[k0 + (tid >> 2)] = z;
+        } else if (kb > 0) {
+            const int tw = (gridDim.x - 1) * nw;
+            for (int r = k0 + NB + (blockIdx.x - 1) * nw + warp; r < n; r += tw) {
+                const double *row = A + (int64_t)r * lda + kp;
+                double sum = fma(row[lane], zp[lane], row[lane + 32] * zp[lane + 32]);
+                for (int off = 16; off > 0; off >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, off);
+                if (lane == 0) x[r] -= sum;
+            }
+        }
+        grid.sync();
+    }
+}
+
+// Backward solve L^T x = z with the block inverses (transposed products).
+__global__ void __launch_bounds__(TRSV_THREADS)
+trsv_bwd_inv_kernel(const double *__restrict__ A, int64_t lda, int n,
+                    const double *__restrict__ Linv, double *__restrict__ x)
+{
+    cg::grid_group grid = cg::this_grid();
+    __shared__ double zp[NB];
+    __shared__ double bb[NB];
+    const int tid = threadIdx.x;
+    const int nblk = (n + NB - 1) / NB;
+    for (int kb = nblk - 1; kb >= 0; --kb) {
+        const int k0 = kb * NB, nb = min(NB, n - k0), kn = k0 + NB;
+        const int nbn = kb < nblk - 1 ? min(NB, n - kn) : 0;
+        if (nbn > 0) {
+            if (tid < NB) zp[tid] = tid < nbn ? x[kn + tid] : 0.0;
+            __syncthreads();
+        }
+        if (blockIdx.x == 0) {
+            double s = 0.0;
+            // a full next block goes through gemv64_col; a short last block (rows
+            // beyond n do not exist) is summed directly by one thread per column
+            if (nbn == NB) s = gemv64_col(A + (int64_t)kn * lda + k0, lda, zp, tid);
+            else if (nbn > 0 && (tid & 3) == 0) {
+                const int t = tid >> 2;
+                for (int r = 0; r < nbn; ++r) s = fma(A[(int64_t)(kn + r) * lda + k0 + t], zp[r], s);
+            }
+            if ((tid & 3) == 0) {
+                const int t = tid >> 2;
+                bb[t] = t < nb ? x[k0 + t] - s : 0.0;
+            }
+            __syncthreads();
+            const double v = gemv64_col(Linv + (int64_t)kb * NB * NB, NB, bb, tid);
+            if ((tid & 3) == 0 && (tid >> 2) < nb) x[k0 + (tid >> 2)] = v;
+        } else if (nbn > 0) {
+            const int tt = (gridDim.x - 1) * TRSV_THREADS;
+            for (int t = (blockIdx.x - 1) * TRSV_THREADS + tid; t < k0; t += tt) {
+                double sum = 0.0;
+                for (int r = 0; r < nbn; ++r) sum = fma(A[(int64_t)(kn + r) * lda + t], zp[r], sum);
+                x[t] -= sum;
+            }
+        }
+        grid.sync();
+    }
+}
+
 int trsv_grid(int &grid)
 {
     static int cached = 0;
@@ -564,6 +733,7 @@ size_t emulated_factor_ws(int n)
     p.add<__nv_bfloat16>((size_t)kEmuMaxSlices * rpad * NB);   // inner block digits
     p.add<int>(rpad);
     p.add<int>(4);                                             // device error flag
+    p.add<double>((size_t)ceil_div(n < 1 ? 1 : n, NB) * NB * NB);  // diagonal-block inverses
     return p.total();
 }
 
@@ -576,8 +746,9 @@ int emulated_factor(double *A, int n, int64_t lda, double shift, Workspace &ws, 
     __nv_bfloat16 *dig_in = ws.take<__nv_bfloat16>((size_t)kEmuMaxSlices * rpad * NB);
     int *exp_in = ws.take<int>((size_t)rpad);
     int *d_err = ws.take<int>(4);
+    double *linv = ws.take<double>((size_t)ceil_div(n, NB) * NB * NB);
     if (dig_out == nullptr || exp_out == nullptr || dig_in == nullptr || exp_in == nullptr ||
-        d_err == nullptr)
+        d_err == nullptr || linv == nullptr)
         return QMLG_E_WORKSPACE;
     cudaError_t e = cudaMemsetAsync(d_err, 0, sizeof(int), s);
     if (e != cudaSuccess) return set_cuda_error(e);
@@ -607,11 +778,13 @@ int emulated_factor(double *A, int n, int64_t lda, double shift, Workspace &ws, 
         }
     }
     if (st != QMLG_OK) return st;
+    { invert_diag_blocks_kernel<<<(unsigned)ceil_div(n, NB), 64, 0, s>>>(A, lda, n, linv); count_launches(1); }
     f.A = A;
     f.n = n;
     f.lda = lda;
     f.slices = slices;
     f.d_err = d_err;
+    f.Linv = linv;
     return check_launch();
 }
 
@@ -627,7 +800,22 @@ int read_device_flag(const int *d_flag, cudaStream_t s)
 
 int emulated_potrs(const EmulatedFactor &f, double *x, cudaStream_t s)
 {
-    return potrs_fp64(f.A, f.n, f.lda, x, s);
+    if (f.Linv == nullptr) return potrs_fp64(f.A, f.n, f.lda, x, s);
+    int grid = 0;
+    int st = trsv_grid(grid);
+    if (st != QMLG_OK) return st;
+    const double *A = f.A, *Linv = f.Linv;
+    int64_t lda = f.lda;
+    int n = f.n;
+    void *args[] = {(void *)&A, (void *)&lda, (void *)&n, (void *)&Linv, (void *)&x};
+    cudaError_t e = cudaLaunchCooperativeKernel((const void *)trsv_fwd_inv_kernel, dim3(grid),
+                                                dim3(TRSV_THREADS), args, 0, s);
+    count_launches(1);
+    if (e == cudaSuccess)
+        e = cudaLaunchCooperativeKernel((const void *)trsv_bwd_inv_kernel, dim3(grid),
+                                        dim3(TRSV_THREADS), args, 0, s);
+    count_launches(1);
+    return e == cudaSuccess ? QMLG_OK : set_cuda_error(e);
 }
 
 size_t residual_ws(int n)
@@ -807,6 +995,8 @@ int refine(SolveCtx &c, const QmlgRefineOpts &o, SolveFn solve_fn, QmlgSolveRepo
             return QMLG_OK;
         }
         if (rel <= o.tol) return QMLG_OK;
+        // linear convergence: the next correction is about rel * (rel / prev)
+        if (prev < INFINITY && rel * (rel / prev) <= 0.1 * o.tol) return QMLG_OK;
         if (rel > 0.5 * prev) {
             stalled = true;
             return QMLG_OK;

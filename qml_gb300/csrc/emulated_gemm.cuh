@@ -43,6 +43,7 @@ struct EmulatedFactor {
     int64_t lda = 0;
     int slices = 0;
     int *d_err = nullptr;  // device flag: a bounded tensor-core wait gave up
+    const double *Linv = nullptr;  // [n/64][64][64] inverses of the diagonal blocks
 };
 
 size_t emulated_factor_ws(int n);

@@ -830,3 +830,91 @@ extern "C" int qmlg_syrk_emulated(double *C, int64_t ldc, int n, const double *P
         st = qmlg::emu_tc_update(C, ldc, 0, n, 0, n, dig, ex, kp, rp, S_MAX, 0, 0, 1, err, s);
     return st;
 }
+
+// ------------------------------------------------ asynchronous prediction --
+
+namespace {
+
+// Sets *flag when 8 digit planes cannot keep the kernel within 1e-12 for the
+// maxima in maxbits[0..1] (the host-side choose_slices bound, evaluated on device).
+__global__ void bound_check_kernel(const unsigned long long *__restrict__ maxbits, int kp,
+                                   double sigma, int *__restrict__ flag)
+{
+    const double ma = __longlong_as_double((long long)maxbits[0]);
+    const double mb = __longlong_as_double((long long)maxbits[1]);
+    if (!isfinite(ma) || !isfinite(mb)) {
+        atomicOr(flag, 8);
+        return;
+    }
+    int ea = 0, eb = 0;
+    if (ma > 0.0) frexp(ma, &ea);
+    if (mb > 0.0) frexp(mb, &eb);
+    const double bound = ldexp(1.0, ea + 1 + eb + 1 - 7 * S_MAX) * kp * (S_MAX + 1) / 4.0;
+    if (bound / (sigma * sigma) > 0.5e-12) atomicOr(flag, 8);
+}
+
+}  // namespace
+
+extern "C" int qmlg_predict_emulated_async(const double *Xtrain, int64_t ldtrain, int ntrain,
+                                           const double *Xtest, int64_t ldtest, int ntest, int d,
+                                           double sigma, const double *alpha, double *yhat,
+                                           int *d_flag, void *workspace, size_t ws_bytes,
+                                           void *stream)
+{
+    if (ntrain < 0 || ntest < 0 || d < 0 || !(sigma > 0.0) || !std::isfinite(sigma))
+        return QMLG_E_ARG;
+    if ((ntrain > 0 && (Xtrain == nullptr || ldtrain < d || alpha == nullptr)) ||
+        (ntest > 0 && (Xtest == nullptr || ldtest < d || yhat == nullptr)) || d_flag == nullptr)
+        return QMLG_E_ARG;
+    if (ntest == 0) return QMLG_OK;
+    cudaStream_t s = qmlg::as_stream(stream);
+    if (ntrain == 0) {
+        cudaError_t e = cudaMemsetAsync(yhat, 0, sizeof(double) * (size_t)ntest, s);
+        return e == cudaSuccess ? QMLG_OK : qmlg::set_cuda_error(e);
+    }
+    if (ws_bytes < qmlg_predict_emulated_workspace_size(ntrain, ntest, d)) return QMLG_E_WORKSPACE;
+    qmlg::Workspace ws(workspace, ws_bytes);
+    GaussBufs b;
+    if (!take_gauss(ws, ntrain, ntest, d, false, true, b)) return QMLG_E_WORKSPACE;
+    b.err = d_flag;  // timeouts and the accuracy bound share the caller's flag
+    const int kp = feature_pad(d), rpa = rows_pad(ntrain), rpb = rows_pad(ntest);
+    cudaError_t e = cudaMemsetAsync(b.maxbuf, 0, 2 * sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+    const int ba = (int)std::min<int64_t>(qmlg::ceil_div((int64_t)ntrain * d, 256), 1216);
+    const int bb = (int)std::min<int64_t>(qmlg::ceil_div((int64_t)ntest * d, 256), 1216);
+    max_abs_kernel<<<ba, 256, 0, s>>>(Xtrain, ldtrain, ntrain, d, b.maxbuf);
+    max_abs_kernel<<<bb, 256, 0, s>>>(Xtest, ldtest, ntest, d, b.maxbuf + 1);
+    bound_check_kernel<<<1, 1, 0, s>>>(b.maxbuf, kp, sigma, d_flag);
+    qmlg::count_launches(3);
+    int st = qmlg::slice_rows(Xtrain, ldtrain, 0, ntrain, 0, d, kp, rpa, S_MAX, b.dA, b.eA, nullptr,
+                              s, b.nA);
+    if (st == QMLG_OK)
+        st = qmlg::slice_rows(Xtest, ldtest, 0, ntest, 0, d, kp, rpb, S_MAX, b.dB, b.eB, nullptr, s,
+                              b.nB);
+    if (st != QMLG_OK) return st;
+    // launch without the trailing flag read (launch_gauss reads it synchronously)
+    CUtensorMap mA, mB;
+    st = make_plane_map(&mA, b.dA, kp, rpa, S_MAX, TM);
+    if (st == QMLG_OK) st = make_plane_map(&mB, b.dB, kp, rpb, S_MAX, TN);
+    if (st != QMLG_OK) return st;
+    set_smem_attrs();
+    TileArgs a{};
+    a.ntiles = count_tiles(0, ntrain, 0, ntest, 0, a.tj);
+    a.jend = ntrain;
+    a.iend = ntest;
+    a.kchunks = kp / KC;
+    a.slices = S_MAX;
+    a.expA = b.eA;
+    a.expB = b.eB;
+    a.err = d_flag;
+    a.normA = b.nA;
+    a.normB = b.nB;
+    a.scale = -0.5 / (sigma * sigma);
+    a.alpha = alpha;
+    a.partial = b.partial;
+    emu_tc_kernel<kPredict><<<std::min(a.ntiles, sm_count()), 192, SMEM_BYTES, s>>>(mA, mB, a);
+    reduce_partial_rows_kernel<<<(int)qmlg::ceil_div(ntest, 256), 256, 0, s>>>(
+        b.partial, (int)qmlg::ceil_div(ntrain, TM), ntest, yhat);
+    qmlg::count_launches(2);
+    return qmlg::check_launch();
+}

@@ -31,7 +31,7 @@ class KRR:
     lam: float = 1e-8
     precision: str = "mixed"
     max_outer: int = 10
-    tol: float = 1e-15
+    tol: float = 1e-14
     X: Optional[torch.Tensor] = None
     alpha: Optional[torch.Tensor] = None
     report: dict = field(default_factory=dict)

@@ -1,0 +1,410 @@
+"""Continuous-batching KRR serving on one GPU.
+
+Resident models are the training Coulomb matrices and their alpha, both kept in HBM.
+Requests arrive over time:
+  * predict: a batch of molecules against a named model;
+  * fit: molecules + labels -> a new resident model.
+
+The scheduler runs one host loop.  On every turn it does three things:
+  * it moves arrived requests into the queue;
+  * it retires finished work (CUDA events polled, never waited on);
+  * it admits queued requests while slots are free and the HBM budget allows.
+
+Admitted predictions of the same model are merged into one launch.  The merged
+launch is one Coulomb-matrix kernel and one fused tensor-core prediction, and the
+results are split back per request.  It runs on one of several CUDA streams, so
+it overlaps with other batches and with fits.  Fits synchronise internally (the
+solve takes refinement decisions on the host), so they run on a worker thread
+with their own stream.  The host loop keeps admitting predictions meanwhile.
+
+Each prediction depends only on its own molecules.  The per-tile partial sums are
+reduced in a fixed order, and every row is scaled independently.  So a request's
+result is the same alone and in a mix, up to the kernel's 1e-12 bound: the
+digit-plane count may differ when a batch's value range changes.
+"""
+from __future__ import annotations
+
+import collections
+import math
+import queue
+import threading
+import time
+from dataclasses import dataclass, field
+from typing import Callable, Dict, List, Optional
+
+import numpy as np
+
+CM_SIZE = 23
+FEATURES = CM_SIZE * (CM_SIZE + 1) // 2
+
+
+@dataclass
+class Request:
+    rid: int
+    kind: str                    # "predict" | "fit"
+    model: str                   # model to query, or name of the model a fit creates
+    charges: np.ndarray
+    coordinates: np.ndarray
+    offsets: np.ndarray
+    arrival: float               # seconds on the server clock
+    labels: Optional[np.ndarray] = None
+    sigma: float = 1000.0
+    lam: float = 1e-8
+    admitted: float = math.nan
+    done: float = math.nan
+    result: Optional[np.ndarray] = None
+    error: Optional[str] = None
+    path: str = ""               # "tensor" or "fp64" (recomputed when the digit bound failed)
+    flag: int = 0
+
+    @property
+    def n_mol(self) -> int:
+        return int(self.offsets.shape[0] - 1)
+
+    @property
+    def latency(self) -> float:
+        return self.done - self.arrival
+
+
+def fit_bytes(n: int) -> int:
+    """HBM a fit holds while it runs: K (8 n^2), the factor workspace (digit planes
+    8 planes x 512 bf16 + 8 x 64 bf16 per row, block inverses) and small vectors."""
+    rp = -(-n // 128) * 128
+    return 8 * n * n + 16 * rp * 576 + 8 * (-(-n // 64)) * 4096 + 64 * n + (64 << 20)
+
+
+def predict_bytes(n_query: int, n_train: int) -> int:
+    """HBM a prediction batch holds: query molecules and CMs, digit planes of
+    both sides (8 planes x 320 bf16 per row), partial sums."""
+    rq = -(-n_query // 128) * 128
+    rt = -(-n_train // 128) * 128
+    return (n_query * (FEATURES * 8 + 23 * 32) + 16 * 320 * (rq + rt)
+            + 8 * n_query * (-(-n_train // 128)) + (8 << 20))
+
+
+class Scheduler:
+    """Host-side admission and batching (no GPU).  `budget_bytes` caps the HBM that
+    admitted work may hold; `max_slots` caps concurrent prediction batches;
+    `max_batch_molecules` caps one merged prediction launch."""
+
+    def __init__(self, budget_bytes: int, max_slots: int = 4, max_batch_molecules: int = 8192,
+                 model_sizes: Optional[Dict[str, int]] = None):
+        self.budget = int(budget_bytes)
+        self.max_slots = max_slots
+        self.max_batch = max_batch_molecules
+        self.queue: "collections.deque[Request]" = collections.deque()
+        self.in_use = 0
+        self.slots = 0
+        self.fit_running = False
+        self.model_sizes: Dict[str, int] = dict(model_sizes or {})
+
+    def submit(self, req: Request):
+        self.queue.append(req)
+
+    def cost(self, req: Request) -> int:
+        if req.kind == "fit":
+            return fit_bytes(req.n_mol)
+        return predict_bytes(req.n_mol, self.model_sizes.get(req.model, 0))
+
+    def next_batch(self) -> Optional[List[Request]]:
+        """The next admissible unit of work, or None.  Fits go one at a time (one
+        worker); predictions of the head request's model are merged in arrival
+        order up to the molecule cap.  A request that does not fit the budget
+        waits; one that can never fit is rejected."""
+        if not self.queue:
+            return None
+        head = self.queue[0]
+        if head.kind == "predict" and head.model not in self.model_sizes:
+            # its model is still being fitted: look for other work behind it
+            for k, r in enumerate(self.queue):
+                if r.kind == "fit" or r.model in self.model_sizes:
+                    self.queue.rotate(-k)
+                    head = self.queue[0]
+                    break
+            else:
+                return None
+        cost = self.cost(head)
+        if cost > self.budget:
+            self.queue.popleft()
+            head.error = "request needs %d bytes, budget is %d" % (cost, self.budget)
+            return [head]
+        if head.kind == "fit":
+            if self.fit_running or self.in_use + cost > self.budget:
+                # let predictions behind it proceed
+                for k, r in enumerate(self.queue):
+                    if r.kind == "predict" and r.model in self.model_sizes:
+                        self.queue.rotate(-k)
+                        return self.next_batch_predict()
+                return None
+            self.queue.popleft()
+            self.in_use += cost
+            self.fit_running = True
+            return [head]
+        return self.next_batch_predict()
+
+    def next_batch_predict(self) -> Optional[List[Request]]:
+        if self.slots >= self.max_slots or not self.queue:
+            return None
+        head = self.queue[0]
+        batch, mols = [], 0
+        rest = collections.deque()
+        while self.queue:
+            r = self.queue.popleft()
+            if (r.kind == "predict" and r.model == head.model
+                    and (not batch or mols + r.n_mol <= self.max_batch)):
+                batch.append(r)
+                mols += r.n_mol
+            else:
+                rest.append(r)
+        self.queue = rest + self.queue
+        cost = predict_bytes(mols, self.model_sizes.get(head.model, 0))
+        if self.in_use + cost > self.budget:
+            for r in reversed(batch):
+                self.queue.appendleft(r)
+            return None
+        self.in_use += cost
+        self.slots += 1
+        return batch
+
+    def release(self, batch: List[Request]):
+        if not batch:
+            return
+        if batch[0].kind == "fit":
+            self.in_use -= fit_bytes(batch[0].n_mol)
+            self.fit_running = False
+            if batch[0].error is None:
+                self.model_sizes[batch[0].model] = batch[0].n_mol
+        else:
+            mols = sum(r.n_mol for r in batch)
+            self.in_use -= predict_bytes(mols, self.model_sizes.get(batch[0].model, 0))
+            self.slots -= 1
+
+
+def merge_molecules(batch: List[Request]):
+    """Concatenate the ragged molecule arrays of a batch; returns flat arrays and
+    the molecule range of each request."""
+    charges = np.concatenate([r.charges for r in batch])
+    coords = np.concatenate([r.coordinates for r in batch])
+    offsets = [np.zeros(1, dtype=np.int64)]
+    ranges, atom_base, mol_base = [], 0, 0
+    for r in batch:
+        offsets.append(r.offsets[1:] + atom_base)
+        atom_base += int(r.offsets[-1])
+        ranges.append((mol_base, mol_base + r.n_mol))
+        mol_base += r.n_mol
+    return charges, coords, np.concatenate(offsets).astype(np.int64), ranges
+
+
+class GpuExecutor:
+    """Runs prediction batches and fits on the GPU through qml_gb300.core."""
+
+    def __init__(self, device="cuda", n_streams: int = 4, precision: str = "mixed"):
+        import torch
+        from . import core
+        self.torch = torch
+        self.core = core
+        self.device = torch.device(device)
+        self.streams = [torch.cuda.Stream(self.device) for _ in range(n_streams)]
+        self.fit_stream = torch.cuda.Stream(self.device)
+        self.next_stream = 0
+        self.precision = precision
+        self.models: Dict[str, tuple] = {}
+        self.lock = threading.Lock()
+
+    def add_model(self, name, X, alpha, sigma):
+        with self.lock:
+            self.models[name] = (X, alpha, sigma)
+
+    def _to_dev(self, a, dtype, stream):
+        t = self.torch.from_numpy(np.ascontiguousarray(a)).to(dtype).pin_memory()
+        with self.torch.cuda.stream(stream):
+            return t.to(self.device, non_blocking=True)
+
+    def launch_predict(self, batch: List[Request]):
+        """Enqueue one merged prediction; returns (event, finish) where finish()
+        copies the results into the requests once the event has completed."""
+        torch = self.torch
+        stream = self.streams[self.next_stream % len(self.streams)]
+        self.next_stream += 1
+        with self.lock:
+            X, alpha, sigma = self.models[batch[0].model]
+        charges, coords, offsets, ranges = merge_molecules(batch)
+        n = offsets.shape[0] - 1
+        out_host = torch.empty(n, dtype=torch.float64).pin_memory()
+        flag_host = torch.zeros(1, dtype=torch.int32).pin_memory()
+        with torch.cuda.stream(stream):
+            z = self._to_dev(charges, torch.float64, stream)
+            r = self._to_dev(coords, torch.float64, stream)
+            o = self._to_dev(offsets, torch.int64, stream)
+            Xq = self.core.coulomb_matrix_batch_async(z, r, o, CM_SIZE)
+            if self.precision == "mixed":
+                flag = torch.zeros(1, dtype=torch.int32, device=self.device)
+                y = self.core.predict_async(X, Xq, sigma, alpha, flag)
+                flag_host.copy_(flag, non_blocking=True)
+            else:
+                y = self.core.predict("gaussian", X, Xq, sigma, alpha)
+            out_host.copy_(y, non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record(stream)
+
+        def finish():
+            vals = out_host.numpy()
+            flag = int(flag_host[0])
+            path = "tensor" if self.precision == "mixed" else "fp64"
+            if flag != 0:
+                # the tensor-core bound was not met (or a bounded wait gave up):
+                # recompute this batch with the FP64 kernel
+                with torch.cuda.stream(stream):
+                    vals = self.core.predict("gaussian", X, Xq, sigma, alpha).cpu().numpy()
+                path = "fp64"
+            for req, (a, b) in zip(batch, ranges):
+                req.result = vals[a:b].copy()
+                req.path, req.flag = path, flag
+        return ev, finish
+
+    def run_fit(self, req: Request):
+        """Blocking fit on the fit stream (called from the worker thread)."""
+        torch = self.torch
+        from .krr import KRR
+        with torch.cuda.stream(self.fit_stream):
+            z = self._to_dev(req.charges, torch.float64, self.fit_stream)
+            r = self._to_dev(req.coordinates, torch.float64, self.fit_stream)
+            o = self._to_dev(req.offsets, torch.int64, self.fit_stream)
+            y = self._to_dev(req.labels, torch.float64, self.fit_stream)
+            X = self.core.coulomb_matrix_batch(z, r, o, CM_SIZE)
+            m = KRR(sigma=req.sigma, lam=req.lam, precision=self.precision).fit(X, y)
+            self.fit_stream.synchronize()
+        self.add_model(req.model, X, m.alpha, req.sigma)
+        req.result = np.array([m.report.get("outer_iterations", 0)], dtype=np.float64)
+
+
+class Server:
+    """The continuous-batching loop.  `clock` returns seconds."""
+
+    def __init__(self, executor, scheduler: Scheduler, clock: Callable[[], float] = time.perf_counter):
+        self.ex = executor
+        self.sched = scheduler
+        self.clock = clock
+        self.inflight = []          # (event, finish, batch)
+        self.fit_q: "queue.Queue" = queue.Queue()
+        self.fit_done: "queue.Queue" = queue.Queue()
+        self.worker = threading.Thread(target=self._fit_worker, daemon=True)
+        self.worker.start()
+        self.completed: List[Request] = []
+
+    def _fit_worker(self):
+        while True:
+            batch = self.fit_q.get()
+            if batch is None:
+                return
+            try:
+                self.ex.run_fit(batch[0])
+            except Exception as e:  # reported on the request, the server keeps going
+                batch[0].error = repr(e)
+            batch[0].done = self.clock()
+            self.fit_done.put(batch)
+
+    def _retire(self):
+        still = []
+        for ev, finish, batch in self.inflight:
+            if ev.query():
+                finish()
+                t = self.clock()
+                for r in batch:
+                    r.done = t
+                self.sched.release(batch)
+                self.completed.extend(batch)
+            else:
+                still.append((ev, finish, batch))
+        self.inflight = still
+        while not self.fit_done.empty():
+            batch = self.fit_done.get()
+            self.sched.release(batch)
+            self.completed.extend(batch)
+
+    def _admit(self):
+        while True:
+            batch = self.sched.next_batch()
+            if batch is None:
+                return
+            t = self.clock()
+            for r in batch:
+                r.admitted = t
+            if batch[0].error is not None:
+                batch[0].done = t
+                self.completed.append(batch[0])
+                continue
+            if batch[0].kind == "fit":
+                self.fit_q.put(batch)
+            else:
+                ev, finish = self.ex.launch_predict(batch)
+                self.inflight.append((ev, finish, batch))
+
+    def run(self, arrivals: List[Request], idle_sleep: float = 50e-6) -> List[Request]:
+        """Serve `arrivals` (sorted by arrival time, relative to start) to completion."""
+        t0 = self.clock()
+        pending = collections.deque(sorted(arrivals, key=lambda r: r.arrival))
+        total = len(pending)
+        for r in pending:
+            r.arrival += t0
+        while len(self.completed) < total:
+            now = self.clock()
+            while pending and pending[0].arrival <= now:
+                self.sched.submit(pending.popleft())
+            self._retire()
+            self._admit()
+            if not self.inflight and self.sched.queue == collections.deque() and pending:
+                time.sleep(max(0.0, min(idle_sleep, pending[0].arrival - self.clock())))
+            elif self.inflight:
+                time.sleep(idle_sleep)
+        self.fit_q.put(None)
+        return self.completed
+
+
+def poisson_workload(rate_hz: float, duration_s: float, pool, model: str,
+                     fit_every: int = 0, fit_sizes=(1000, 20000), seed: int = 0,
+                     max_query: int = 4096) -> List[Request]:
+    """Poisson arrivals of prediction queries (molecule count log-uniform in
+    1..max_query) and, every `fit_every`-th arrival, a fit request with N
+    log-uniform in fit_sizes.  Molecules are consecutive slices of `pool` (a
+    MoleculeBatch with labels) starting at random offsets."""
+    rng = np.random.default_rng(seed)
+    t, rid, out = 0.0, 0, []
+
+    def take(n):
+        n = min(max(1, n), pool.n_mol)
+        start = int(rng.integers(0, pool.n_mol - n + 1))
+        return pool.slice(start, start + n)
+
+    while True:
+        t += rng.exponential(1.0 / rate_hz)
+        if t > duration_s:
+            break
+        if fit_every and rid % fit_every == fit_every - 1:
+            n = int(round(math.exp(rng.uniform(math.log(fit_sizes[0]), math.log(fit_sizes[1])))))
+            b = take(n)
+            out.append(Request(rid, "fit", "fit-%d" % rid, b.charges, b.coordinates, b.offsets, t,
+                               labels=b.labels))
+        else:
+            n = int(round(math.exp(rng.uniform(0.0, math.log(max_query)))))
+            b = take(n)
+            out.append(Request(rid, "predict", model, b.charges, b.coordinates, b.offsets, t))
+        rid += 1
+    return out
+
+
+def latency_stats(done: List[Request]) -> dict:
+    preds = [r for r in done if r.kind == "predict" and r.error is None]
+    fits = [r for r in done if r.kind == "fit" and r.error is None]
+    lat = np.array([r.latency for r in preds]) if preds else np.zeros(0)
+    span = (max(r.done for r in done) - min(r.arrival for r in done)) if done else 0.0
+    mols = sum(r.n_mol for r in preds)
+    return {
+        "queries": len(preds), "fits": len(fits),
+        "rejected": sum(1 for r in done if r.error is not None),
+        "p50_ms": float(np.percentile(lat, 50) * 1e3) if lat.size else None,
+        "p99_ms": float(np.percentile(lat, 99) * 1e3) if lat.size else None,
+        "mean_ms": float(lat.mean() * 1e3) if lat.size else None,
+        "molecules_per_s": mols / span if span > 0 else None,
+        "fit_latency_ms": [float(r.latency * 1e3) for r in fits],
+    }

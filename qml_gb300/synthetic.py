@@ -82,15 +82,19 @@ def generate_molecules(n_mol: int, seed: int = 0, max_atoms: int = MAX_ATOMS,
     charges = z[mask].astype(np.float64)
     coords = pos[mask]
 
-    # labels: 0.01 * sum_{i<j} Z_i Z_j / r_ij + N(0, 1)
-    diff = pos[:, :, None, :] - pos[:, None, :, :]
-    r = np.sqrt(np.sum(diff * diff, axis=3))
-    zz = z[:, :, None].astype(np.float64) * z[:, None, :]
+    # labels: 0.01 * sum_{i<j} Z_i Z_j / r_ij + N(0, 1), in chunks of molecules
     iu = np.triu(np.ones((max_atoms, max_atoms), dtype=bool), 1)
-    pair = mask[:, :, None] & mask[:, None, :] & iu[None]
-    with np.errstate(divide="ignore", invalid="ignore"):
-        e = np.where(pair, zz / np.where(pair, r, 1.0), 0.0)
-    labels = 0.01 * e.sum(axis=(1, 2)) + rng.normal(size=n_mol)
+    energy = np.empty(n_mol)
+    for a in range(0, n_mol, 4096):
+        b = min(n_mol, a + 4096)
+        diff = pos[a:b, :, None, :] - pos[a:b, None, :, :]
+        r = np.sqrt(np.sum(diff * diff, axis=3))
+        zz = z[a:b, :, None].astype(np.float64) * z[a:b, None, :]
+        pair = mask[a:b, :, None] & mask[a:b, None, :] & iu[None]
+        with np.errstate(divide="ignore", invalid="ignore"):
+            e = np.where(pair, zz / np.where(pair, r, 1.0), 0.0)
+        energy[a:b] = e.sum(axis=(1, 2))
+    labels = 0.01 * energy + rng.normal(size=n_mol)
     return MoleculeBatch(charges, coords, offsets, labels)
 
 

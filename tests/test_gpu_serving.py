@@ -1,0 +1,54 @@
+"""Serving on the GPU: a resident model, Poisson queries mixed with a fit; each
+query's result is the same alone and in the mix (within the kernel's 1e-12 bound)
+and matches the oracle prediction."""
+import numpy as np
+import pytest
+import torch
+
+from qml_gb300 import core, serving
+from qml_gb300.krr import KRR, molecules_to_device
+from qml_gb300.synthetic import generate_molecules
+
+pytestmark = pytest.mark.gpu
+
+
+def test_serving_mix_equals_alone(cuda, oracle):
+    ntr = 3000
+    train = generate_molecules(ntr, seed=101)
+    z, r, o = molecules_to_device(train)
+    X = core.coulomb_matrix_batch(z, r, o, 23)
+    y = torch.from_numpy(train.labels).to(cuda)
+    model = KRR(sigma=1000.0, lam=1e-8, precision="mixed").fit(X, y)
+    ex = serving.GpuExecutor(n_streams=3)
+    ex.add_model("main", X, model.alpha, 1000.0)
+    pool = generate_molecules(4000, seed=102)
+    reqs = serving.poisson_workload(400.0, 0.5, pool, "main", fit_every=40, fit_sizes=(500, 1500),
+                                    seed=5, max_query=512)
+    sched = serving.Scheduler(budget_bytes=8 << 30, max_slots=3,
+                              model_sizes={"main": ntr})
+    done = serving.Server(ex, sched).run(reqs)
+    assert len(done) == len(reqs)
+    assert all(r.error is None for r in done)
+    stats = serving.latency_stats(done)
+    assert stats["queries"] > 50 and stats["fits"] >= 1
+    Xo = oracle.cm_sorted_batch(train.charges, train.coordinates, train.offsets, 23)
+    alpha = model.alpha.cpu().numpy()
+    preds = [r for r in done if r.kind == "predict"]
+    assert all(r.path == "tensor" and r.flag == 0 for r in preds), \
+        sorted({(r.path, r.flag) for r in preds})
+    for req in preds[:12]:
+        # alone: the same request as its own batch through the same executor
+        alone = serving.Request(-1, "predict", "main", req.charges, req.coordinates, req.offsets, 0.0)
+        ev, finish = ex.launch_predict([alone])
+        ev.synchronize()
+        finish()
+        # the result depends on the request's own molecules only: bit for bit here
+        assert np.array_equal(alone.result, req.result)
+        # against the oracle: each kernel entry is within 1e-12 relative, so the
+        # prediction is within 1e-12 of sum_j |k_ij alpha_j| (alpha is large and
+        # cancels: |alpha| reaches ~1e8 at lambda = 1e-8)
+        Xq = oracle.cm_sorted_batch(req.charges, req.coordinates, req.offsets, 23)
+        Ks = oracle.gaussian_kernel(Xo, Xq, 1000.0)
+        expect = Ks.T @ alpha
+        scale = np.abs(Ks.T) @ np.abs(alpha)
+        assert np.max(np.abs(req.result - expect) / scale) <= 1e-12
