@@ -218,7 +218,7 @@ def run_serving(a, dev):
     model = KRR(sigma=a.sigma, lam=a.lam, precision="mixed").fit(X, y)
     torch.cuda.synchronize()
     fit_s = time.perf_counter() - t0
-    ex = serving.GpuExecutor(device=dev, n_streams=4)
+    ex = serving.GpuExecutor(device=dev, n_streams=8)
     ex.add_model("main", X, model.alpha, a.sigma)
     # warm the streams (workspaces, pinned buffers) outside the measured run
     warm = serving.poisson_workload(50.0, 0.2, queries, "main", seed=a.seed + 1, max_query=4096)
@@ -226,7 +226,7 @@ def run_serving(a, dev):
     reqs = serving.poisson_workload(a.serve_rate, a.serve_seconds, queries, "main",
                                     fit_every=a.serve_fit_every, fit_sizes=(1000, 20000),
                                     seed=a.seed + 2, max_query=4096)
-    sched = serving.Scheduler(budget_bytes=64 << 30, max_slots=4,
+    sched = serving.Scheduler(budget_bytes=64 << 30, max_slots=8,
                               model_sizes={"main": a.serve_n})
     done = serving.Server(ex, sched).run(reqs)
     st = serving.latency_stats(done)
@@ -334,6 +334,22 @@ def run_ours(a):
         stages[name] = evs[k].elapsed_time(evs[k + 1]) / 1e3
     del K
 
+    # the Laplacian kernel of the same training set: FP64 and fixed-point paths
+    def time_kernel(kind, emulated, reps=2):
+        core.kernel_matrix(kind, X[:ntr], X[:ntr], a.sigma, symmetric=True, emulated=emulated)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            core.kernel_matrix(kind, X[:ntr], X[:ntr], a.sigma, symmetric=True, emulated=emulated)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps / 1e3
+    kernels_s = {"gaussian_fp64": time_kernel("gaussian", False),
+                 "gaussian_tensor": time_kernel("gaussian", True),
+                 "laplacian_fp64": time_kernel("laplacian", False),
+                 "laplacian_fixed": time_kernel("laplacian", True)}
+
     # dominant kernel: the emulated trailing update of the mixed Cholesky
     # (first outer step of this workload: C (n-512)^2 lower, P (n-512) x 512)
     nsy = ntr - 512
@@ -420,7 +436,8 @@ def run_ours(a):
             "fits_per_s": world / (ms / 1e3),
             "serving": serving_stats,
             "gpu_launches": launches, "clocks": clocks.summary(), "roofline": roofline,
-            "cpu_baseline": cpu, "stages_s": stages, "solve_report": rep_m,
+            "cpu_baseline": cpu, "stages_s": stages,
+            "train_kernel_matrix_s": kernels_s, "solve_report": rep_m,
             "fp64_path": fp64}
     print(json.dumps(line), flush=True)
     if world > 1:

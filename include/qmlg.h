@@ -45,6 +45,23 @@ const char *qmlg_last_error(void);
 /* Number of CUDA kernels this library has launched in this process so far. */
 uint64_t qmlg_launch_count(void);
 
+/*
+ * Caps the grid of the persistent and cooperative kernels launched from the
+ * calling host thread at n CTAs (0 = no cap, the default).  A serving process
+ * gives its fit thread a cap so that query kernels on other streams always find
+ * free SMs instead of waiting behind a whole-GPU factorisation.
+ */
+void qmlg_set_thread_sm_limit(int n);
+
+/*
+ * on = 1 (default): tensor-core kernels launched from the calling host thread use
+ * persistent CTAs (one per SM, looping over tiles, loads of the next tile
+ * overlapping the current epilogue).  on = 0: one CTA per tile, so a launch that
+ * shares the GPU with other work spreads over whichever SMs are free; serving
+ * threads use this for query kernels.
+ */
+void qmlg_set_thread_persistent(int on);
+
 /* ---- sorted Coulomb matrix --------------------------------------------- */
 
 /*
@@ -108,6 +125,21 @@ int qmlg_gaussian_kernel_emulated(const double *A, int64_t lda, int na, const do
                                   int64_t ldb, int nb, int d, double sigma, double *K,
                                   int64_t ldk, int flags, double diag_shift, void *workspace,
                                   size_t ws_bytes, void *stream);
+
+/*
+ * Laplacian kernel with the L1 distances summed exactly in 64-bit fixed point on
+ * the integer pipes: features rounded once to multiples of 2^-F (F from max |x|
+ * and d so that sums cannot overflow), |a - b| summed exactly, converted to FP64
+ * once.  Entries stay within 1e-12 relative of the FP64 kernel (bound
+ * d * 2^-F / sigma <= 0.5e-12, else the FP64 kernel runs); K is exactly
+ * symmetric.  Same layout and flags as qmlg_laplacian_kernel.  Synchronises the
+ * stream once (max |x|).
+ */
+size_t qmlg_laplacian_kernel_fixed_workspace_size(int na, int nb, int d, int flags);
+int qmlg_laplacian_kernel_fixed(const double *A, int64_t lda, int na, const double *B,
+                                int64_t ldb, int nb, int d, double sigma, double *K, int64_t ldk,
+                                int flags, double diag_shift, void *workspace, size_t ws_bytes,
+                                void *stream);
 
 /* ---- prediction ----------------------------------------------------------- */
 

@@ -74,6 +74,8 @@ SIGNATURES = {
     "qmlg_version": (ctypes.c_char_p, []),
     "qmlg_last_error": (ctypes.c_char_p, []),
     "qmlg_launch_count": (ctypes.c_uint64, []),
+    "qmlg_set_thread_sm_limit": (None, [_I]),
+    "qmlg_set_thread_persistent": (None, [_I]),
     "qmlg_coulomb_matrix": (_I, [_P, _P, _P, _I, _I, _I, _P, _P, _P]),
     "qmlg_gaussian_kernel": (_I, [_P, _I64, _I, _P, _I64, _I, _I, _D, _P, _I64, _I, _D, _P]),
     "qmlg_laplacian_kernel": (_I, [_P, _I64, _I, _P, _I64, _I, _I, _D, _P, _I64, _I, _D, _P]),
@@ -84,6 +86,9 @@ SIGNATURES = {
     "qmlg_predict_emulated": (_I, [_P, _I64, _I, _P, _I64, _I, _I, _D, _P, _P, _P, _SZ, _P]),
     "qmlg_predict_emulated_async": (_I, [_P, _I64, _I, _P, _I64, _I, _I, _D, _P, _P, _P, _P,
                                          _SZ, _P]),
+    "qmlg_laplacian_kernel_fixed_workspace_size": (_SZ, [_I, _I, _I, _I]),
+    "qmlg_laplacian_kernel_fixed": (_I, [_P, _I64, _I, _P, _I64, _I, _I, _D, _P, _I64, _I, _D,
+                                         _P, _SZ, _P]),
     "qmlg_predict_gemv": (_I, [_P, _I64, _I, _I, _P, _P, _P]),
     "qmlg_predict_workspace_size": (_SZ, [_I, _I]),
     "qmlg_predict_fused": (_I, [_I, _P, _I64, _I, _P, _I64, _I, _I, _D, _P, _P, _P, _SZ, _P]),

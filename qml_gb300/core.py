@@ -83,6 +83,9 @@ def coulomb_matrix_batch(charges: torch.Tensor, coordinates: torch.Tensor,
                                     offsets.data_ptr(), n_mol, size, _SORTING[sorting],
                                     out.data_ptr(), status.data_ptr(), _stream(charges.device)),
           "qmlg_coulomb_matrix")
+    # wait for the stream before reading back (a read queued behind pending work
+    # would hold up other host threads' CUDA calls until that work finishes)
+    torch.cuda.current_stream(charges.device).synchronize()
     st = int(status.item())
     if st != 0:
         _lib.check(st, "qmlg_coulomb_matrix")
@@ -123,9 +126,10 @@ def kernel_matrix(kind: str, A: torch.Tensor, B: torch.Tensor, sigma: float,
                   symmetric: bool = False, diag_shift: float = 0.0,
                   out: Optional[torch.Tensor] = None, emulated: bool = False) -> torch.Tensor:
     """K (na, nb), Fortran-ordered like the reference, as a (na, nb) view of a
-    column-major buffer.  symmetric=True requires B is A.  emulated=True (Gaussian
-    only) forms the contraction on the tensor cores (qmlg_gaussian_kernel_emulated,
-    within 1e-12 of the FP64 kernel)."""
+    column-major buffer.  symmetric=True requires B is A.  emulated=True takes the
+    fast exact-within-1e-12 paths: the Gaussian contraction on the tensor cores
+    (qmlg_gaussian_kernel_emulated), the Laplacian L1 sums in fixed-point integers
+    (qmlg_laplacian_kernel_fixed)."""
     _require_cuda(A, B)
     A, lda = _rows(A)
     if symmetric:
@@ -150,6 +154,15 @@ def kernel_matrix(kind: str, A: torch.Tensor, B: torch.Tensor, sigma: float,
                                                   float(diag_shift), ws.data_ptr(), ws.numel(),
                                                   _stream(A.device)),
               "qmlg_gaussian_kernel_emulated")
+        return buf.T
+    if emulated and kind == "laplacian":
+        ws_bytes = lib().qmlg_laplacian_kernel_fixed_workspace_size(na, nb, d, flags)
+        ws = workspaces.get(ws_bytes, A.device)
+        check(lib().qmlg_laplacian_kernel_fixed(A.data_ptr(), lda, na, B.data_ptr(), ldb, nb, d,
+                                                float(sigma), buf.data_ptr(), na, flags,
+                                                float(diag_shift), ws.data_ptr(), ws.numel(),
+                                                _stream(A.device)),
+              "qmlg_laplacian_kernel_fixed")
         return buf.T
     fn = lib().qmlg_gaussian_kernel if kind == "gaussian" else lib().qmlg_laplacian_kernel
     check(fn(A.data_ptr(), lda, na, B.data_ptr(), ldb, nb, d, float(sigma), buf.data_ptr(), na,

@@ -679,6 +679,7 @@ int potrs_fp64(const double *A, int n, int64_t lda, double *x, cudaStream_t s)
     int grid = 0;
     int st = trsv_grid(grid);
     if (st != QMLG_OK) return st;
+    grid = std::max(2, sm_limit(grid));
     void *args[] = {(void *)&A, (void *)&lda, (void *)&n, (void *)&x};
     cudaError_t e = cudaLaunchCooperativeKernel((const void *)trsv_fwd_coop_kernel, dim3(grid),
                                                 dim3(TRSV_THREADS), args, 0, s);
@@ -792,9 +793,8 @@ int emulated_factor(double *A, int n, int64_t lda, double shift, Workspace &ws, 
 int read_device_flag(const int *d_flag, cudaStream_t s)
 {
     int h = 0;
-    cudaError_t e = cudaMemcpyAsync(&h, d_flag, sizeof(int), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return set_cuda_error(e);
+    const int st = read_back(&h, d_flag, sizeof(int), s);
+    if (st != QMLG_OK) return st;
     return h != 0 ? QMLG_E_TIMEOUT : QMLG_OK;
 }
 
@@ -804,6 +804,7 @@ int emulated_potrs(const EmulatedFactor &f, double *x, cudaStream_t s)
     int grid = 0;
     int st = trsv_grid(grid);
     if (st != QMLG_OK) return st;
+    grid = std::max(2, sm_limit(grid));
     const double *A = f.A, *Linv = f.Linv;
     int64_t lda = f.lda;
     int n = f.n;
@@ -862,10 +863,8 @@ extern "C" int qmlg_cholesky(double *A, int n, int64_t lda, double lambda, void 
     int st = qmlg::cholesky_fp64(A, n, lda, lambda, d_info, s);
     if (st != QMLG_OK) return st;
     int info = 0;
-    e = cudaMemcpyAsync(&info, d_info, sizeof(int), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return qmlg::set_cuda_error(e);
-    return info;
+    st = qmlg::read_back(&info, d_info, sizeof(int), s);
+    return st != QMLG_OK ? st : info;
 }
 
 extern "C" size_t qmlg_cholesky_mixed_workspace_size(int n)
@@ -892,10 +891,8 @@ extern "C" int qmlg_cholesky_mixed(double *A, int n, int64_t lda, double lambda,
     if (st != QMLG_OK) return st;
     if ((st = qmlg::read_device_flag(f.d_err, s)) != QMLG_OK) return st;
     int info = 0;
-    e = cudaMemcpyAsync(&info, d_info, sizeof(int), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return qmlg::set_cuda_error(e);
-    return info;
+    st = qmlg::read_back(&info, d_info, sizeof(int), s);
+    return st != QMLG_OK ? st : info;
 }
 
 extern "C" int qmlg_cholesky_solve_factored(const double *U, int n, int64_t lda, const double *y,
@@ -960,9 +957,7 @@ struct SolveCtx {
 
 int read_info(SolveCtx &c, int &info)
 {
-    cudaError_t e = cudaMemcpyAsync(&info, c.d_info, sizeof(int), cudaMemcpyDeviceToHost, c.s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c.s);
-    return e == cudaSuccess ? QMLG_OK : qmlg::set_cuda_error(e);
+    return qmlg::read_back(&info, c.d_info, sizeof(int), c.s);
 }
 
 // Iterative refinement: r = y - (A + lambda I) x in double-double, dx = solve(r),
@@ -984,9 +979,8 @@ int refine(SolveCtx &c, const QmlgRefineOpts &o, SolveFn solve_fn, QmlgSolveRepo
         if (e != cudaSuccess) return qmlg::set_cuda_error(e);
         { axpy_norms_kernel<<<(int)qmlg::ceil_div(c.n, 256), 256, 0, c.s>>>(c.x, c.r, c.n, c.d_sums); qmlg::count_launches(1); }
         double h[2];
-        e = cudaMemcpyAsync(h, c.d_sums, sizeof(h), cudaMemcpyDeviceToHost, c.s);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(c.s);
-        if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+        st = qmlg::read_back(h, c.d_sums, sizeof(h), c.s);
+        if (st != QMLG_OK) return st;
         const double rel = std::sqrt(h[0]) / std::fmax(std::sqrt(h[1]), 1e-300);
         rep.outer_iterations = it + 1;
         rep.last_correction = rel;

@@ -14,6 +14,20 @@ int set_cuda_error(cudaError_t e);
 // Adds to the process-wide count of kernels this library has launched.
 void count_launches(unsigned n);
 
+// Small device-to-host read of a result the stream is still producing: waits for
+// the stream first, then copies.  A pageable copy issued behind pending work keeps
+// other host threads' CUDA calls waiting until that work finishes; a copy issued
+// on an idle stream returns at once.
+int read_back(void *host, const void *dev, size_t bytes, cudaStream_t s);
+
+// Grid cap for persistent and cooperative kernels launched from this host thread
+// (qmlg_set_thread_sm_limit); returns `full` when no cap is set.
+int sm_limit(int full);
+
+// False when the calling host thread asked for one CTA per tile instead of
+// persistent CTAs (qmlg_set_thread_persistent).
+bool persistent_tiles();
+
 inline int check_launch()
 {
     cudaError_t e = cudaGetLastError();

@@ -472,7 +472,15 @@ int sm_count()
             cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
             n = 148;
     });
-    return n;
+    return qmlg::sm_limit(n);
+}
+
+// Persistent CTAs (one per SM, looping over tiles) or, when the calling thread
+// turned persistence off, one CTA per tile so that the block scheduler spreads
+// the work over whatever SMs are free.
+int tile_grid(int ntiles)
+{
+    return qmlg::persistent_tiles() ? std::min(ntiles, sm_count()) : ntiles;
 }
 
 // Same tile list as TileCursor on the device.
@@ -536,9 +544,8 @@ int read_max(const double *X, int64_t ldx, int rows, int cols, unsigned long lon
     max_abs_kernel<<<blocks, 256, 0, s>>>(X, ldx, rows, cols, dbuf);
     qmlg::count_launches(1);
     unsigned long long h = 0;
-    e = cudaMemcpyAsync(&h, dbuf, sizeof(h), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+    const int st = qmlg::read_back(&h, dbuf, sizeof(h), s);
+    if (st != QMLG_OK) return st;
     std::memcpy(&out, &h, sizeof(out));
     return QMLG_OK;
 }
@@ -586,7 +593,7 @@ int emu_tc_update(double *C, int64_t ldc, int jbase, int jend, int ibase, int ie
     a.expB = expo;
     a.lower = lower;
     a.err = d_err;
-    const int grid = std::min(a.ntiles, sm_count());
+    const int grid = tile_grid(a.ntiles);
     emu_tc_kernel<kSyrk><<<grid, 192, SMEM_BYTES, s>>>(mA, mB, a);
     count_launches(1);
     return check_launch();
@@ -703,7 +710,7 @@ int launch_gauss(int mode, const GaussBufs &b, int na, int nb, int d, int S, dou
     a.diag_shift = diag_shift;
     a.alpha = alpha;
     a.partial = b.partial;
-    const int grid = std::min(a.ntiles, sm_count());
+    const int grid = tile_grid(a.ntiles);
     if (mode == kKernelMatrix)
         emu_tc_kernel<kKernelMatrix><<<grid, 192, SMEM_BYTES, s>>>(mA, mB, a);
     else
@@ -912,7 +919,7 @@ extern "C" int qmlg_predict_emulated_async(const double *Xtrain, int64_t ldtrain
     a.scale = -0.5 / (sigma * sigma);
     a.alpha = alpha;
     a.partial = b.partial;
-    emu_tc_kernel<kPredict><<<std::min(a.ntiles, sm_count()), 192, SMEM_BYTES, s>>>(mA, mB, a);
+    emu_tc_kernel<kPredict><<<tile_grid(a.ntiles), 192, SMEM_BYTES, s>>>(mA, mB, a);
     reduce_partial_rows_kernel<<<(int)qmlg::ceil_div(ntest, 256), 256, 0, s>>>(
         b.partial, (int)qmlg::ceil_div(ntrain, TM), ntest, yhat);
     qmlg::count_launches(2);

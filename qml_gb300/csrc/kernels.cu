@@ -12,7 +12,9 @@
 // memory 16 columns at a time.  Symmetric mode computes only tiles on or below the
 // diagonal and writes the mirror through a shared-memory transpose, so K is
 // exactly symmetric.
+#include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <mutex>
 
 #include "common.cuh"
@@ -413,6 +415,186 @@ extern "C" int qmlg_predict_fused_noalloc(int kind, const double *Xtrain, int64_
     }
     qmlg::count_launches(1);
     reduce_partial_kernel<<<(int)qmlg::ceil_div(ntest, 256), 256, 0, s>>>(partial, tj, ntest, yhat);
+    qmlg::count_launches(1);
+    return qmlg::check_launch();
+}
+
+// ---------------------------------------------------------------------------
+// Laplacian kernel in exact fixed-point integer arithmetic.
+//
+// Every feature is rounded once to q = round(x * 2^F) (int64).  The L1 distance is
+// then an exact integer sum of |q_a - q_b| (no rounding, so the result does not
+// depend on the summation order and K is exactly symmetric), converted to FP64
+// once: L1 = sum * 2^-F.  F is the largest scale with d * 2 * max|x| * 2^F < 2^62
+// (no overflow); the rounding of the inputs moves L1 by at most d * 2^-F, i.e. K
+// by at most d * 2^-F / sigma relative, which must stay below 0.5e-12 or the FP64
+// kernel runs instead.  The sums run on the integer pipes, not the FP64 ones.
+// ---------------------------------------------------------------------------
+
+namespace {
+
+__global__ void max_abs_rows_kernel(const double *__restrict__ X, int64_t ldx, int rows, int cols,
+                                    unsigned long long *__restrict__ out)
+{
+    unsigned long long m = 0;
+    const int64_t total = (int64_t)rows * cols;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const unsigned long long b =
+            (unsigned long long)__double_as_longlong(fabs(X[(e / cols) * ldx + e % cols]));
+        m = b > m ? b : m;
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        const unsigned long long o = __shfl_xor_sync(0xffffffffu, m, off);
+        m = o > m ? o : m;
+    }
+    if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+__global__ void to_fixed_kernel(const double *__restrict__ X, int64_t ldx, int rows, int cols,
+                                double scale, long long *__restrict__ Q)
+{
+    const int64_t total = (int64_t)rows * cols;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = e / cols, c = e % cols;
+        Q[e] = __double2ll_rn(X[r * ldx + c] * scale);
+    }
+}
+
+__device__ __forceinline__ long long iabs64(long long v) { return v < 0 ? -v : v; }
+
+__global__ void __launch_bounds__(NT)
+laplace_fixed_kernel(const long long *__restrict__ A, int na, const long long *__restrict__ B,
+                     int nb, int d, double inv_scale, double neg_inv_sigma,
+                     double *__restrict__ K, int64_t ldk, int symmetric, double diag_shift)
+{
+    // operand chunks during the sums, the output tile (for the mirror) after
+    __shared__ double smem[TI * (TJ + 1)];
+    long long(*As)[TJ + 1] = reinterpret_cast<long long(*)[TJ + 1]>(smem);
+    long long(*Bs)[TI + 1] = reinterpret_cast<long long(*)[TI + 1]>(smem + TK * (TJ + 1));
+    double(*T)[TJ + 1] = reinterpret_cast<double(*)[TJ + 1]>(smem);
+    int bj, bi;
+    if (symmetric) {
+        tri_index(blockIdx.x, bi, bj);
+    } else {
+        bj = blockIdx.x;
+        bi = blockIdx.y;
+    }
+    const int j0 = bj * TJ, i0 = bi * TI;
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    long long acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = 0;
+    for (int t0 = 0; t0 < d; t0 += TK) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int e = tid + q * NT;
+            const int r = e >> 4, c = e & 15;
+            const int t = t0 + c;
+            As[c][r] = (j0 + r < na && t < d) ? A[(int64_t)(j0 + r) * d + t] : 0;
+            Bs[c][r] = (i0 + r < nb && t < d) ? B[(int64_t)(i0 + r) * d + t] : 0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int c = 0; c < TK; ++c) {
+            long long av[4], bv[4];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) av[a] = As[c][tx + 16 * a];
+#pragma unroll
+            for (int b = 0; b < 4; ++b) bv[b] = Bs[c][ty + 16 * b];
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int b = 0; b < 4; ++b) acc[a][b] += iabs64(av[a] - bv[b]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const int j = j0 + tx + 16 * a, i = i0 + ty + 16 * b;
+            double v = exp(neg_inv_sigma * ((double)acc[a][b] * inv_scale));
+            if (symmetric && i == j) v = 1.0 + diag_shift;
+            if (j < na && i < nb) K[(int64_t)i * ldk + j] = v;
+            T[ty + 16 * b][tx + 16 * a] = v;
+        }
+    if (symmetric && bi != bj) {
+        __syncthreads();
+        for (int e = tid; e < TI * TJ; e += NT) {
+            const int ii = e & (TI - 1), jj = e / TI;
+            const int i = i0 + ii, j = j0 + jj;
+            if (i < nb && j < na) K[(int64_t)j * ldk + i] = T[ii][jj];
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" size_t qmlg_laplacian_kernel_fixed_workspace_size(int na, int nb, int d, int flags)
+{
+    qmlg::WorkspacePlan p;
+    p.add<long long>((size_t)na * d);
+    if (!(flags & QMLG_KERNEL_SYMMETRIC)) p.add<long long>((size_t)nb * d);
+    p.add<unsigned long long>(2);
+    return p.total();
+}
+
+extern "C" int qmlg_laplacian_kernel_fixed(const double *A, int64_t lda, int na, const double *B,
+                                           int64_t ldb, int nb, int d, double sigma, double *K,
+                                           int64_t ldk, int flags, double diag_shift,
+                                           void *workspace, size_t ws_bytes, void *stream)
+{
+    int st = check_common(A, lda, na, B, ldb, nb, d, sigma);
+    if (st != QMLG_OK) return st;
+    if (K == nullptr || ldk < na) return QMLG_E_ARG;
+    const bool symmetric = (flags & QMLG_KERNEL_SYMMETRIC) != 0;
+    if (symmetric && (na != nb || A != B || lda != ldb)) return QMLG_E_ARG;
+    if (na == 0 || nb == 0) return QMLG_OK;
+    if (ws_bytes < qmlg_laplacian_kernel_fixed_workspace_size(na, nb, d, flags))
+        return QMLG_E_WORKSPACE;
+    cudaStream_t s = qmlg::as_stream(stream);
+    qmlg::Workspace ws(workspace, ws_bytes);
+    long long *qa = ws.take<long long>((size_t)na * d);
+    long long *qb = symmetric ? qa : ws.take<long long>((size_t)nb * d);
+    unsigned long long *mx = ws.take<unsigned long long>(2);
+    if (qa == nullptr || qb == nullptr || mx == nullptr) return QMLG_E_WORKSPACE;
+    cudaError_t e = cudaMemsetAsync(mx, 0, 2 * sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+    auto blocks = [](int64_t total) { return (int)std::min<int64_t>(qmlg::ceil_div(total, 256), 2432); };
+    max_abs_rows_kernel<<<blocks((int64_t)na * d), 256, 0, s>>>(A, lda, na, d, mx);
+    if (!symmetric) max_abs_rows_kernel<<<blocks((int64_t)nb * d), 256, 0, s>>>(B, ldb, nb, d, mx + 1);
+    qmlg::count_launches(symmetric ? 1 : 2);
+    unsigned long long h[2] = {0, 0};
+    st = qmlg::read_back(h, mx, sizeof(h), s);
+    if (st != QMLG_OK) return st;
+    double ma, mb;
+    std::memcpy(&ma, &h[0], sizeof(double));
+    std::memcpy(&mb, &h[1], sizeof(double));
+    const double m = std::fmax(ma, symmetric ? ma : mb);
+    if (!std::isfinite(m))
+        return qmlg_laplacian_kernel(A, lda, na, B, ldb, nb, d, sigma, K, ldk, flags, diag_shift,
+                                     stream);
+    int em = 0;
+    if (m > 0.0) std::frexp(m, &em);  // m < 2^em
+    int ed = 0;
+    std::frexp((double)(2 * (int64_t)(d < 1 ? 1 : d)), &ed);  // 2d <= 2^ed
+    const int F = std::min(62 - ed - em, 1000);
+    const double bound = std::ldexp((double)d, -F) / sigma;
+    if (bound > 0.5e-12)  // not representable finely enough: the FP64 kernel
+        return qmlg_laplacian_kernel(A, lda, na, B, ldb, nb, d, sigma, K, ldk, flags, diag_shift,
+                                     stream);
+    const double scale = std::ldexp(1.0, F), inv_scale = std::ldexp(1.0, -F);
+    to_fixed_kernel<<<blocks((int64_t)na * d), 256, 0, s>>>(A, lda, na, d, scale, qa);
+    if (!symmetric) to_fixed_kernel<<<blocks((int64_t)nb * d), 256, 0, s>>>(B, ldb, nb, d, scale, qb);
+    qmlg::count_launches(symmetric ? 1 : 2);
+    const int tj = (int)qmlg::ceil_div(na, TJ), ti = (int)qmlg::ceil_div(nb, TI);
+    dim3 grid = symmetric ? dim3((unsigned)((int64_t)tj * (tj + 1) / 2)) : dim3(tj, ti);
+    laplace_fixed_kernel<<<grid, NT, 0, s>>>(qa, na, qb, nb, d, inv_scale, -1.0 / sigma, K, ldk,
+                                             symmetric ? 1 : 0, diag_shift);
     qmlg::count_launches(1);
     return qmlg::check_launch();
 }

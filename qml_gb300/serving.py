@@ -87,7 +87,7 @@ class Scheduler:
     admitted work may hold; `max_slots` caps concurrent prediction batches;
     `max_batch_molecules` caps one merged prediction launch."""
 
-    def __init__(self, budget_bytes: int, max_slots: int = 4, max_batch_molecules: int = 8192,
+    def __init__(self, budget_bytes: int, max_slots: int = 8, max_batch_molecules: int = 8192,
                  model_sizes: Optional[Dict[str, int]] = None):
         self.budget = int(budget_bytes)
         self.max_slots = max_slots
@@ -196,60 +196,89 @@ def merge_molecules(batch: List[Request]):
 
 
 class GpuExecutor:
-    """Runs prediction batches and fits on the GPU through qml_gb300.core."""
+    """Runs prediction batches and fits on the GPU through qml_gb300.core.
 
-    def __init__(self, device="cuda", n_streams: int = 4, precision: str = "mixed"):
+    Every prediction slot owns a CUDA stream and preallocated pinned staging
+    buffers sized for max_batch_molecules.  Query launches therefore never
+    allocate pinned host memory; such allocations can synchronise the whole
+    device, and a query would then wait behind a running fit."""
+
+    def __init__(self, device="cuda", n_streams: int = 8, precision: str = "mixed",
+                 fit_sm_fraction: float = 0.75, max_batch_molecules: int = 8192,
+                 max_atoms: int = 23):
         import torch
         from . import core
         self.torch = torch
         self.core = core
         self.device = torch.device(device)
-        self.streams = [torch.cuda.Stream(self.device) for _ in range(n_streams)]
-        self.fit_stream = torch.cuda.Stream(self.device)
-        self.next_stream = 0
+        # queries on high-priority streams; fits on a low-priority one, with their
+        # persistent kernels capped below the SM count (fit_sm_fraction) so that
+        # query kernels find free SMs while a factorisation runs
+        lo, hi = torch.cuda.Stream.priority_range()
+        self.streams = [torch.cuda.Stream(self.device, priority=hi) for _ in range(n_streams)]
+        self.fit_stream = torch.cuda.Stream(self.device, priority=lo)
+        self.fit_sm_fraction = fit_sm_fraction
         self.precision = precision
         self.models: Dict[str, tuple] = {}
         self.lock = threading.Lock()
+        self.max_mols = max_batch_molecules
+        atoms = max_batch_molecules * max_atoms
+        self.staging = []
+        for _ in range(n_streams):
+            self.staging.append({
+                "charges": torch.empty(atoms, dtype=torch.float64).pin_memory(),
+                "coords": torch.empty(atoms * 3, dtype=torch.float64).pin_memory(),
+                "offsets": torch.empty(max_batch_molecules + 1, dtype=torch.int64).pin_memory(),
+                "out": torch.empty(max_batch_molecules, dtype=torch.float64).pin_memory(),
+                "flag": torch.zeros(1, dtype=torch.int32).pin_memory(),
+                "dflag": torch.zeros(1, dtype=torch.int32, device=self.device),
+            })
+        self.free = list(range(n_streams))
 
     def add_model(self, name, X, alpha, sigma):
         with self.lock:
             self.models[name] = (X, alpha, sigma)
 
-    def _to_dev(self, a, dtype, stream):
-        t = self.torch.from_numpy(np.ascontiguousarray(a)).to(dtype).pin_memory()
-        with self.torch.cuda.stream(stream):
-            return t.to(self.device, non_blocking=True)
+    def set_query_persistence(self, on: bool):
+        """Query kernels are launched from the serving thread: one CTA per tile
+        while serving (they share the GPU with fits), persistent otherwise."""
+        self.core.lib().qmlg_set_thread_persistent(1 if on else 0)
 
     def launch_predict(self, batch: List[Request]):
-        """Enqueue one merged prediction; returns (event, finish) where finish()
-        copies the results into the requests once the event has completed."""
+        """Enqueue one merged prediction on a free slot; returns (event, finish)
+        where finish() copies the results into the requests once the event has
+        completed and frees the slot."""
         torch = self.torch
-        stream = self.streams[self.next_stream % len(self.streams)]
-        self.next_stream += 1
+        slot = self.free.pop()
+        stream, st = self.streams[slot], self.staging[slot]
         with self.lock:
             X, alpha, sigma = self.models[batch[0].model]
         charges, coords, offsets, ranges = merge_molecules(batch)
-        n = offsets.shape[0] - 1
-        out_host = torch.empty(n, dtype=torch.float64).pin_memory()
-        flag_host = torch.zeros(1, dtype=torch.int32).pin_memory()
+        n, na = offsets.shape[0] - 1, charges.shape[0]
+        if n > self.max_mols or na * 3 > st["coords"].numel():
+            self.free.append(slot)
+            raise ValueError("batch larger than the staging buffers")
+        st["charges"].numpy()[:na] = charges
+        st["coords"].numpy()[:3 * na] = coords.reshape(-1)
+        st["offsets"].numpy()[:n + 1] = offsets
         with torch.cuda.stream(stream):
-            z = self._to_dev(charges, torch.float64, stream)
-            r = self._to_dev(coords, torch.float64, stream)
-            o = self._to_dev(offsets, torch.int64, stream)
+            z = st["charges"][:na].to(self.device, non_blocking=True)
+            r = st["coords"][:3 * na].to(self.device, non_blocking=True).view(na, 3)
+            o = st["offsets"][:n + 1].to(self.device, non_blocking=True)
             Xq = self.core.coulomb_matrix_batch_async(z, r, o, CM_SIZE)
             if self.precision == "mixed":
-                flag = torch.zeros(1, dtype=torch.int32, device=self.device)
-                y = self.core.predict_async(X, Xq, sigma, alpha, flag)
-                flag_host.copy_(flag, non_blocking=True)
+                st["dflag"].zero_()
+                y = self.core.predict_async(X, Xq, sigma, alpha, st["dflag"])
+                st["flag"].copy_(st["dflag"], non_blocking=True)
             else:
                 y = self.core.predict("gaussian", X, Xq, sigma, alpha)
-            out_host.copy_(y, non_blocking=True)
+            st["out"][:n].copy_(y, non_blocking=True)
             ev = torch.cuda.Event()
             ev.record(stream)
 
         def finish():
-            vals = out_host.numpy()
-            flag = int(flag_host[0])
+            vals = st["out"].numpy()[:n]
+            flag = int(st["flag"][0]) if self.precision == "mixed" else 0
             path = "tensor" if self.precision == "mixed" else "fp64"
             if flag != 0:
                 # the tensor-core bound was not met (or a bounded wait gave up):
@@ -260,17 +289,22 @@ class GpuExecutor:
             for req, (a, b) in zip(batch, ranges):
                 req.result = vals[a:b].copy()
                 req.path, req.flag = path, flag
+            self.free.append(slot)
         return ev, finish
 
     def run_fit(self, req: Request):
         """Blocking fit on the fit stream (called from the worker thread)."""
         torch = self.torch
         from .krr import KRR
+        if self.fit_sm_fraction < 1.0:  # per host thread: set it on the thread that fits
+            sms = torch.cuda.get_device_properties(self.device).multi_processor_count
+            self.core.lib().qmlg_set_thread_sm_limit(max(2, int(sms * self.fit_sm_fraction)))
         with torch.cuda.stream(self.fit_stream):
-            z = self._to_dev(req.charges, torch.float64, self.fit_stream)
-            r = self._to_dev(req.coordinates, torch.float64, self.fit_stream)
-            o = self._to_dev(req.offsets, torch.int64, self.fit_stream)
-            y = self._to_dev(req.labels, torch.float64, self.fit_stream)
+            # pageable copies: they block this worker thread only
+            z = torch.from_numpy(np.ascontiguousarray(req.charges)).to(self.device)
+            r = torch.from_numpy(np.ascontiguousarray(req.coordinates)).to(self.device)
+            o = torch.from_numpy(np.ascontiguousarray(req.offsets)).to(self.device)
+            y = torch.from_numpy(np.ascontiguousarray(req.labels)).to(self.device)
             X = self.core.coulomb_matrix_batch(z, r, o, CM_SIZE)
             m = KRR(sigma=req.sigma, lam=req.lam, precision=self.precision).fit(X, y)
             self.fit_stream.synchronize()
@@ -342,6 +376,16 @@ class Server:
 
     def run(self, arrivals: List[Request], idle_sleep: float = 50e-6) -> List[Request]:
         """Serve `arrivals` (sorted by arrival time, relative to start) to completion."""
+        set_persistent = getattr(self.ex, "set_query_persistence", None)
+        if set_persistent is not None:
+            set_persistent(False)
+        try:
+            return self._run(arrivals, idle_sleep)
+        finally:
+            if set_persistent is not None:
+                set_persistent(True)
+
+    def _run(self, arrivals: List[Request], idle_sleep: float) -> List[Request]:
         t0 = self.clock()
         pending = collections.deque(sorted(arrivals, key=lambda r: r.arrival))
         total = len(pending)

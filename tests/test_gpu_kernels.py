@@ -138,3 +138,29 @@ def test_emulated_predict(cuda, oracle, cm_features):
     scale = np.abs(Ks.T) @ np.abs(alpha)
     assert np.max(np.abs(y - expect) / scale) <= 1e-12
     assert np.array_equal(y, core.predict("gaussian", *args, emulated=True).cpu().numpy())
+
+
+@pytest.mark.parametrize("sigma", [100.0, 1000.0, 10 ** 4.2])
+def test_fixed_point_laplacian(cuda, oracle, cm_features, sigma):
+    # exact integer L1 sums: within 1e-12 of the oracle, exactly symmetric
+    X = cm_features
+    A, B = X[:700], X[700:]
+    At, Bt = torch.from_numpy(A).to(cuda), torch.from_numpy(B).to(cuda)
+    K = core.kernel_matrix("laplacian", At, Bt, sigma, emulated=True).cpu().numpy()
+    assert relerr(K, oracle.laplacian_kernel(A, B, sigma)) <= RTOL
+    Ks = core.kernel_matrix("laplacian", At, At, sigma, symmetric=True, emulated=True).cpu().numpy()
+    assert np.array_equal(Ks, Ks.T)
+    assert relerr(Ks, oracle.laplacian_kernel(A, A, sigma)) <= RTOL
+
+
+def test_fixed_point_laplacian_reference_test_and_fallback(cuda, oracle):
+    # tests/test_kernels.py:34-63 (sigma = 100, fixed point) and sigma = 1, where the
+    # fixed-point bound d * 2^-F / sigma is not met and the FP64 kernel runs
+    g = load_golden("kernels_seed666.npz")
+    X, Xs = g["X"], g["Xs"]
+    for s in (float(g["sigma"]), 1.0):
+        K = core.kernel_matrix("laplacian", torch.from_numpy(X).to(cuda),
+                               torch.from_numpy(Xs).to(cuda), s, emulated=True).cpu().numpy()
+        assert relerr(K, oracle.laplacian_kernel(X, Xs, s)) <= RTOL
+        if s == float(g["sigma"]):
+            assert np.allclose(K, g["laplacian"])
