@@ -62,6 +62,16 @@ void qmlg_set_thread_sm_limit(int n);
  */
 void qmlg_set_thread_persistent(int on);
 
+/*
+ * on = 1 (default): the triangular solves of the Cholesky solve run as
+ * cooperative grid-synchronised kernels over every SM (one at a time on the
+ * device; the library chains them with an event).  on = 0: single-CTA solves with
+ * the diagonal-block inverses, which any number of concurrent solves may run side
+ * by side; batched work uses this.  Stream capture always takes the single-CTA
+ * path.
+ */
+void qmlg_set_thread_cooperative(int on);
+
 /* ---- sorted Coulomb matrix --------------------------------------------- */
 
 /*
@@ -140,6 +150,18 @@ int qmlg_laplacian_kernel_fixed(const double *A, int64_t lda, int na, const doub
                                 int64_t ldb, int nb, int d, double sigma, double *K, int64_t ldk,
                                 int flags, double diag_shift, void *workspace, size_t ws_bytes,
                                 void *stream);
+
+/*
+ * Capture-safe qmlg_gaussian_kernel_emulated: no host synchronisation (so it can
+ * be recorded into a CUDA graph); always 8 digit planes; the 1e-12 bound is
+ * checked on the device and a failure ORs 8 into the caller's device int
+ * *d_flag (then recompute with qmlg_gaussian_kernel); 1/2/4 = a bounded
+ * tensor-core wait gave up.  Workspace as qmlg_gaussian_kernel_emulated.
+ */
+int qmlg_gaussian_kernel_emulated_async(const double *A, int64_t lda, int na, const double *B,
+                                        int64_t ldb, int nb, int d, double sigma, double *K,
+                                        int64_t ldk, int flags, double diag_shift, int *d_flag,
+                                        void *workspace, size_t ws_bytes, void *stream);
 
 /* ---- prediction ----------------------------------------------------------- */
 
@@ -289,6 +311,20 @@ size_t qmlg_solve_workspace_size(int n, int precision);
 int qmlg_solve(double *A, int n, int64_t lda, const double *y, double *x, double lambda,
                int precision, const QmlgRefineOpts *opts, QmlgSolveReport *report,
                void *workspace, size_t ws_bytes, void *stream);
+
+/*
+ * Capture-safe mixed solve (A + lambda I) x = y for batched, graph-recorded
+ * work: the qmlg_cholesky_mixed factorisation, one solve and exactly
+ * refine_steps double-double refinement steps, with no host synchronisation and
+ * no host decision.  Results stay on the device: d_status[0] = Cholesky info
+ * (0 = ok), d_status[1] = tensor-core wait flags; d_correction (optional, 2
+ * doubles) = |dx|^2 and |x|^2 of the last step.  The column-major upper
+ * triangle of A receives the factor as in qmlg_cholesky.
+ */
+size_t qmlg_solve_async_workspace_size(int n);
+int qmlg_solve_async(double *A, int n, int64_t lda, const double *y, double *x, double lambda,
+                     int refine_steps, int *d_status, double *d_correction, void *workspace,
+                     size_t ws_bytes, void *stream);
 
 /*
  * r = y - (A + lambda I) x with every product and sum carried in double-double,

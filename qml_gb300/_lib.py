@@ -76,6 +76,7 @@ SIGNATURES = {
     "qmlg_launch_count": (ctypes.c_uint64, []),
     "qmlg_set_thread_sm_limit": (None, [_I]),
     "qmlg_set_thread_persistent": (None, [_I]),
+    "qmlg_set_thread_cooperative": (None, [_I]),
     "qmlg_coulomb_matrix": (_I, [_P, _P, _P, _I, _I, _I, _P, _P, _P]),
     "qmlg_gaussian_kernel": (_I, [_P, _I64, _I, _P, _I64, _I, _I, _D, _P, _I64, _I, _D, _P]),
     "qmlg_laplacian_kernel": (_I, [_P, _I64, _I, _P, _I64, _I, _I, _D, _P, _I64, _I, _D, _P]),
@@ -103,6 +104,10 @@ SIGNATURES = {
     "qmlg_solve_workspace_size": (_SZ, [_I, _I]),
     "qmlg_solve": (_I, [_P, _I, _I64, _P, _P, _D, _I, ctypes.POINTER(QmlgRefineOpts),
                         ctypes.POINTER(QmlgSolveReport), _P, _SZ, _P]),
+    "qmlg_gaussian_kernel_emulated_async": (_I, [_P, _I64, _I, _P, _I64, _I, _I, _D, _P, _I64,
+                                                 _I, _D, _P, _P, _SZ, _P]),
+    "qmlg_solve_async_workspace_size": (_SZ, [_I]),
+    "qmlg_solve_async": (_I, [_P, _I, _I64, _P, _P, _D, _I, _P, _P, _P, _SZ, _P]),
     "qmlg_residual_workspace_size": (_SZ, [_I]),
     "qmlg_residual_dd": (_I, [_P, _I, _I64, _P, _D, _P, _P, _P, _P, _SZ, _P]),
 }

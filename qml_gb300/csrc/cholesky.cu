@@ -621,6 +621,97 @@ trsv_bwd_inv_kernel(const double *__restrict__ A, int64_t lda, int n,
     }
 }
 
+// Both triangular solves in one CTA, with the block inverses: no waiting between
+// CTAs, so any number of these may run at once (batched, graph-recorded solves).
+constexpr int TRSV1_THREADS = 512;
+
+__global__ void __launch_bounds__(TRSV1_THREADS)
+trsv_single_cta_kernel(const double *__restrict__ A, int64_t lda, int n,
+                       const double *__restrict__ Linv, double *__restrict__ x)
+{
+    __shared__ double xb[NB];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    constexpr int nw = TRSV1_THREADS / 32;
+    const int nblk = (n + NB - 1) / NB;
+    for (int kb = 0; kb < nblk; ++kb) {  // L z = b
+        const int k0 = kb * NB, nb = min(NB, n - k0);
+        if (tid < NB) xb[tid] = tid < nb ? x[k0 + tid] : 0.0;
+        __syncthreads();
+        if (tid < 256) {
+            const double z = gemv64_row(Linv + (int64_t)kb * NB * NB, NB, xb, tid, NB);
+            if ((tid & 3) == 0 && (tid >> 2) < nb) x[k0 + (tid >> 2)] = z;
+        }
+        __syncthreads();
+        if (tid < NB) xb[tid] = tid < nb ? x[k0 + tid] : 0.0;
+        __syncthreads();
+        if (nb == NB)
+            for (int r = k0 + NB + warp; r < n; r += nw) {
+                const double *row = A + (int64_t)r * lda + k0;
+                double sum = fma(row[lane], xb[lane], row[lane + 32] * xb[lane + 32]);
+                for (int off = 16; off > 0; off >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, off);
+                if (lane == 0) x[r] -= sum;
+            }
+        __syncthreads();
+    }
+    for (int kb = nblk - 1; kb >= 0; --kb) {  // L^T x = z
+        const int k0 = kb * NB, nb = min(NB, n - k0);
+        if (tid < NB) xb[tid] = tid < nb ? x[k0 + tid] : 0.0;
+        __syncthreads();
+        if (tid < 256) {
+            const double v = gemv64_col(Linv + (int64_t)kb * NB * NB, NB, xb, tid);
+            if ((tid & 3) == 0 && (tid >> 2) < nb) x[k0 + (tid >> 2)] = v;
+        }
+        __syncthreads();
+        if (tid < NB) xb[tid] = tid < nb ? x[k0 + tid] : 0.0;
+        __syncthreads();
+        for (int t = tid; t < k0; t += TRSV1_THREADS) {
+            double sum = 0.0;
+            for (int r = 0; r < nb; ++r) sum = fma(A[(int64_t)(k0 + r) * lda + t], xb[r], sum);
+            x[t] -= sum;
+        }
+        __syncthreads();
+    }
+}
+
+// Cooperative kernels of this process run one at a time on the device: each one
+// waits for the previous one (an event chain across streams), so two grids that
+// each need every SM are never resident together.
+int launch_cooperative(const void *fn, int grid, int threads, void **args, cudaStream_t s)
+{
+    static std::mutex mu;
+    static cudaEvent_t last[64] = {};
+    static bool recorded[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+    if (dev < 0 || dev >= 64) return QMLG_E_ARG;
+    std::lock_guard<std::mutex> lock(mu);
+    if (last[dev] == nullptr) {
+        e = cudaEventCreateWithFlags(&last[dev], cudaEventDisableTiming);
+        if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+    }
+    if (recorded[dev]) {
+        e = cudaStreamWaitEvent(s, last[dev], 0);
+        if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+    }
+    e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(threads), args, 0, s);
+    qmlg::count_launches(1);
+    if (e == cudaSuccess) e = cudaEventRecord(last[dev], s);
+    if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+    recorded[dev] = true;
+    return QMLG_OK;
+}
+
+// Cooperative kernels are off while the stream is being captured (an event
+// recorded outside the capture cannot order it) and on threads that turned them
+// off (qmlg_set_thread_cooperative).
+bool cooperative_allowed(cudaStream_t s)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) return false;
+    return cs == cudaStreamCaptureStatusNone && qmlg::cooperative_on();
+}
+
 int trsv_grid(int &grid)
 {
     static int cached = 0;
@@ -646,6 +737,11 @@ int trsv_grid(int &grid)
     });
     grid = cached;
     return status;
+}
+
+__global__ void or_flag_kernel(int *__restrict__ dst, const int *__restrict__ src)
+{
+    if (*src != 0) atomicOr(dst, *src);
 }
 
 __global__ void fill_nan_kernel(double *__restrict__ x, int n)
@@ -680,15 +776,12 @@ int potrs_fp64(const double *A, int n, int64_t lda, double *x, cudaStream_t s)
     int st = trsv_grid(grid);
     if (st != QMLG_OK) return st;
     grid = std::max(2, sm_limit(grid));
+    if (!cooperative_allowed(s)) return QMLG_E_ARG;  // the plain FP64 solve is not capture-safe
     void *args[] = {(void *)&A, (void *)&lda, (void *)&n, (void *)&x};
-    cudaError_t e = cudaLaunchCooperativeKernel((const void *)trsv_fwd_coop_kernel, dim3(grid),
-                                                dim3(TRSV_THREADS), args, 0, s);
-    count_launches(1);
-    if (e == cudaSuccess)
-        e = cudaLaunchCooperativeKernel((const void *)trsv_bwd_coop_kernel, dim3(grid),
-                                        dim3(TRSV_THREADS), args, 0, s);
-    count_launches(1);
-    return e == cudaSuccess ? QMLG_OK : set_cuda_error(e);
+    st = launch_cooperative((const void *)trsv_fwd_coop_kernel, grid, TRSV_THREADS, args, s);
+    if (st == QMLG_OK)
+        st = launch_cooperative((const void *)trsv_bwd_coop_kernel, grid, TRSV_THREADS, args, s);
+    return st;
 }
 
 // R[i][j] <- R[j][i] for j < i, R[i][i] <- diag[i]: restores the lower triangle from
@@ -808,15 +901,15 @@ int emulated_potrs(const EmulatedFactor &f, double *x, cudaStream_t s)
     const double *A = f.A, *Linv = f.Linv;
     int64_t lda = f.lda;
     int n = f.n;
+    if (!cooperative_allowed(s)) {
+        { trsv_single_cta_kernel<<<1, TRSV1_THREADS, 0, s>>>(A, lda, n, Linv, x); count_launches(1); }
+        return check_launch();
+    }
     void *args[] = {(void *)&A, (void *)&lda, (void *)&n, (void *)&Linv, (void *)&x};
-    cudaError_t e = cudaLaunchCooperativeKernel((const void *)trsv_fwd_inv_kernel, dim3(grid),
-                                                dim3(TRSV_THREADS), args, 0, s);
-    count_launches(1);
-    if (e == cudaSuccess)
-        e = cudaLaunchCooperativeKernel((const void *)trsv_bwd_inv_kernel, dim3(grid),
-                                        dim3(TRSV_THREADS), args, 0, s);
-    count_launches(1);
-    return e == cudaSuccess ? QMLG_OK : set_cuda_error(e);
+    st = launch_cooperative((const void *)trsv_fwd_inv_kernel, grid, TRSV_THREADS, args, s);
+    if (st == QMLG_OK)
+        st = launch_cooperative((const void *)trsv_bwd_inv_kernel, grid, TRSV_THREADS, args, s);
+    return st;
 }
 
 size_t residual_ws(int n)
@@ -1083,4 +1176,55 @@ extern "C" int qmlg_solve(double *A, int n, int64_t lda, const double *y, double
     e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return qmlg::set_cuda_error(e);
     return (o.max_outer > 0 && stalled) ? QMLG_E_NOT_CONVERGED : QMLG_OK;
+}
+
+// ------------------------------------------------- capture-safe mixed solve --
+
+extern "C" size_t qmlg_solve_async_workspace_size(int n)
+{
+    return qmlg_solve_workspace_size(n, QMLG_PREC_MIXED);
+}
+
+extern "C" int qmlg_solve_async(double *A, int n, int64_t lda, const double *y, double *x,
+                                double lambda, int refine_steps, int *d_status,
+                                double *d_correction, void *workspace, size_t ws_bytes,
+                                void *stream)
+{
+    if (n < 0 || lda < n || refine_steps < 0 || d_status == nullptr) return QMLG_E_ARG;
+    if (n == 0) return QMLG_OK;
+    if (A == nullptr || y == nullptr || x == nullptr) return QMLG_E_ARG;
+    if (ws_bytes < qmlg_solve_async_workspace_size(n)) return QMLG_E_WORKSPACE;
+    cudaStream_t s = qmlg::as_stream(stream);
+    qmlg::Workspace ws(workspace, ws_bytes);
+    ws.take<int>(4);  // same layout as qmlg_solve; status lives in d_status here
+    double *d_sums = ws.take<double>(4);
+    double *diag = ws.take<double>((size_t)n);
+    double *r = ws.take<double>((size_t)n);
+    if (d_sums == nullptr || diag == nullptr || r == nullptr) return QMLG_E_WORKSPACE;
+    const size_t mark = ws.used;
+    cudaError_t e = cudaMemsetAsync(d_status, 0, 2 * sizeof(int), s);
+    if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+    { copy_diag_kernel<<<(int)qmlg::ceil_div(n, 256), 256, 0, s>>>(A, lda, n, diag); qmlg::count_launches(1); }
+    ws.used = mark + qmlg::residual_ws(n);  // the residual partials come first
+    qmlg::EmulatedFactor f;
+    int st = qmlg::emulated_factor(A, n, lda, lambda, ws, d_status, f, s);
+    if (st != QMLG_OK) return st;
+    { or_flag_kernel<<<1, 1, 0, s>>>(d_status + 1, f.d_err); qmlg::count_launches(1); }
+    e = cudaMemcpyAsync(x, y, sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+    if ((st = qmlg::emulated_potrs(f, x, s)) != QMLG_OK) return st;
+    for (int it = 0; it < refine_steps; ++it) {
+        qmlg::Workspace rws(workspace, ws_bytes);
+        rws.used = mark;
+        if ((st = qmlg::residual_dd(A, n, lda, diag, lambda, x, y, r, rws, s)) != QMLG_OK) return st;
+        if ((st = qmlg::emulated_potrs(f, r, s)) != QMLG_OK) return st;
+        e = cudaMemsetAsync(d_sums, 0, 2 * sizeof(double), s);
+        if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+        { axpy_norms_kernel<<<(int)qmlg::ceil_div(n, 256), 256, 0, s>>>(x, r, n, d_sums); qmlg::count_launches(1); }
+    }
+    if (d_correction != nullptr && refine_steps > 0) {
+        e = cudaMemcpyAsync(d_correction, d_sums, 2 * sizeof(double), cudaMemcpyDeviceToDevice, s);
+        if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+    }
+    return qmlg::check_launch();
 }

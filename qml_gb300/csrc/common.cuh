@@ -28,6 +28,10 @@ int sm_limit(int full);
 // persistent CTAs (qmlg_set_thread_persistent).
 bool persistent_tiles();
 
+// False when the calling host thread turned cooperative (grid-synchronised)
+// kernels off (qmlg_set_thread_cooperative).
+bool cooperative_on();
+
 inline int check_launch()
 {
     cudaError_t e = cudaGetLastError();

@@ -925,3 +925,65 @@ extern "C" int qmlg_predict_emulated_async(const double *Xtrain, int64_t ldtrain
     qmlg::count_launches(2);
     return qmlg::check_launch();
 }
+
+// Capture-safe Gaussian kernel: 8 digit planes always, no host synchronisation;
+// the accuracy bound (and any bounded-wait timeout) is reported in *d_flag.
+extern "C" int qmlg_gaussian_kernel_emulated_async(const double *A, int64_t lda, int na,
+                                                   const double *B, int64_t ldb, int nb, int d,
+                                                   double sigma, double *K, int64_t ldk, int flags,
+                                                   double diag_shift, int *d_flag, void *workspace,
+                                                   size_t ws_bytes, void *stream)
+{
+    const bool sym = (flags & QMLG_KERNEL_SYMMETRIC) != 0;
+    if (na < 0 || nb < 0 || d < 0 || !(sigma > 0.0) || !std::isfinite(sigma) || d_flag == nullptr)
+        return QMLG_E_ARG;
+    if ((na > 0 && (A == nullptr || lda < d)) || (nb > 0 && (B == nullptr || ldb < d)))
+        return QMLG_E_ARG;
+    if (K == nullptr || ldk < na) return QMLG_E_ARG;
+    if (sym && (na != nb || A != B || lda != ldb)) return QMLG_E_ARG;
+    if (na == 0 || nb == 0) return QMLG_OK;
+    if (ws_bytes < qmlg_gaussian_kernel_emulated_workspace_size(na, nb, d, flags))
+        return QMLG_E_WORKSPACE;
+    cudaStream_t s = qmlg::as_stream(stream);
+    qmlg::Workspace ws(workspace, ws_bytes);
+    GaussBufs b;
+    if (!take_gauss(ws, na, nb, d, sym, false, b)) return QMLG_E_WORKSPACE;
+    b.err = d_flag;
+    const int kp = feature_pad(d), rpa = rows_pad(na), rpb = rows_pad(nb);
+    cudaError_t e = cudaMemsetAsync(b.maxbuf, 0, 2 * sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+    const int ba = (int)std::min<int64_t>(qmlg::ceil_div((int64_t)na * d, 256), 1216);
+    const int bb = (int)std::min<int64_t>(qmlg::ceil_div((int64_t)nb * d, 256), 1216);
+    max_abs_kernel<<<ba, 256, 0, s>>>(A, lda, na, d, b.maxbuf);
+    max_abs_kernel<<<bb, 256, 0, s>>>(B, ldb, nb, d, b.maxbuf + 1);
+    bound_check_kernel<<<1, 1, 0, s>>>(b.maxbuf, kp, sigma, d_flag);
+    qmlg::count_launches(3);
+    int st = qmlg::slice_rows(A, lda, 0, na, 0, d, kp, rpa, S_MAX, b.dA, b.eA, nullptr, s, b.nA);
+    if (st == QMLG_OK && !sym)
+        st = qmlg::slice_rows(B, ldb, 0, nb, 0, d, kp, rpb, S_MAX, b.dB, b.eB, nullptr, s, b.nB);
+    if (st != QMLG_OK) return st;
+    CUtensorMap mA, mB;
+    st = make_plane_map(&mA, b.dA, kp, rpa, S_MAX, TM);
+    if (st == QMLG_OK) st = make_plane_map(&mB, b.dB, kp, rpb, S_MAX, TN);
+    if (st != QMLG_OK) return st;
+    set_smem_attrs();
+    TileArgs a{};
+    a.ntiles = count_tiles(0, na, 0, nb, sym ? 1 : 0, a.tj);
+    a.C = K;
+    a.ldc = ldk;
+    a.jend = na;
+    a.iend = nb;
+    a.kchunks = kp / KC;
+    a.slices = S_MAX;
+    a.expA = b.eA;
+    a.expB = b.eB;
+    a.lower = sym ? 1 : 0;
+    a.err = d_flag;
+    a.normA = b.nA;
+    a.normB = b.nB;
+    a.scale = -0.5 / (sigma * sigma);
+    a.diag_shift = diag_shift;
+    emu_tc_kernel<kKernelMatrix><<<tile_grid(a.ntiles), 192, SMEM_BYTES, s>>>(mA, mB, a);
+    qmlg::count_launches(1);
+    return qmlg::check_launch();
+}

@@ -9,6 +9,7 @@ namespace {
 thread_local std::string g_last_error;
 thread_local int t_sm_limit = 0;
 thread_local int t_persistent = 1;
+thread_local int t_cooperative = 1;
 std::atomic<unsigned long long> g_launches{0};
 }
 
@@ -34,6 +35,8 @@ int sm_limit(int full) { return (t_sm_limit > 0 && t_sm_limit < full) ? t_sm_lim
 
 bool persistent_tiles() { return t_persistent != 0; }
 
+bool cooperative_on() { return t_cooperative != 0; }
+
 }  // namespace qmlg
 
 extern "C" uint64_t qmlg_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
@@ -45,3 +48,5 @@ extern "C" const char *qmlg_last_error(void) { return g_last_error.c_str(); }
 extern "C" void qmlg_set_thread_sm_limit(int n) { t_sm_limit = n > 0 ? n : 0; }
 
 extern "C" void qmlg_set_thread_persistent(int on) { t_persistent = on ? 1 : 0; }
+
+extern "C" void qmlg_set_thread_cooperative(int on) { t_cooperative = on ? 1 : 0; }

@@ -1,0 +1,72 @@
+"""Batched fits in one CUDA graph: every fit matches the refined oracle solution of
+its own kernel matrix (<= 1e-8 on alpha), the graph replay reproduces the eager run
+bit for bit, and the autotuned schedule gives the same answers."""
+import numpy as np
+import pytest
+import torch
+
+from qml_gb300 import core
+from qml_gb300.batch import BatchedKRR, Problem
+from qml_gb300.synthetic import generate_molecules
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [100, 300, 700, 1100, 1500, 64, 513]
+SIGMAS = [250.0, 500.0, 1000.0, 2000.0, 1000.0, 500.0, 2000.0]
+LAMS = [1e-4, 1e-6, 1e-8, 1e-8, 1e-6, 1e-4, 1e-8]
+
+
+@pytest.fixture(scope="module")
+def batch_problems(oracle):
+    pool = generate_molecules(2500, seed=404)
+    X = oracle.cm_sorted_batch(pool.charges, pool.coordinates, pool.offsets, 23)
+    probs, host = [], []
+    start = 0
+    for n, s, lam in zip(SIZES, SIGMAS, LAMS):
+        Xi = X[start % 900:start % 900 + n]
+        yi = pool.labels[start % 900:start % 900 + n]
+        start += 137
+        probs.append(Problem(torch.from_numpy(np.ascontiguousarray(Xi)).cuda(),
+                             torch.from_numpy(np.ascontiguousarray(yi)).cuda(), s, lam))
+        host.append((Xi, yi, s, lam))
+    return probs, host
+
+
+def test_batched_fits_match_oracle_and_graph(cuda, oracle, batch_problems):
+    probs, host = batch_problems
+    b = BatchedKRR(probs, refine_steps=3, streams=3)
+    b.run_eager()
+    alphas, reps = b.results()
+    eager = [a.cpu().numpy().copy() for a in alphas]
+    for i, ((Xi, yi, s, lam), a, rep) in enumerate(zip(host, eager, reps)):
+        # the exact kernel matrix the fit solved: the factorisation leaves the
+        # strictly upper triangle of the row-major view untouched and K_ii = 1
+        Kb = b.K[i].cpu().numpy()
+        U = np.triu(Kb, 1)
+        K = U + U.T + np.eye(Kb.shape[0])
+        # that K is the tensor-core kernel: within 1e-12 of the oracle's FP64 one
+        Ko = oracle.gaussian_kernel(Xi, Xi, s)
+        assert np.max(np.abs(K - Ko) / Ko) <= 1e-12
+        ref = oracle.refined_solve(K, yi, lam)
+        assert rep["info"] == 0 and rep["flags"] == 0, rep
+        assert np.linalg.norm(a - ref) / np.linalg.norm(ref) <= 1e-8, rep
+    b.capture()
+    b.replay()
+    alphas, reps = b.results()
+    for a, e in zip(alphas, eager):
+        assert np.array_equal(a.cpu().numpy(), e)
+
+
+def test_autotuned_schedule(cuda, batch_problems):
+    probs, _ = batch_problems
+    b = BatchedKRR(probs, refine_steps=3)
+    best = b.autotune(candidates=[{"streams": 2, "order": "size", "persistent": True},
+                                  {"streams": 4, "order": "rr", "persistent": False}], reps=1)
+    assert best["streams"] in (2, 4)
+    b.replay()
+    alphas, reps = b.results()
+    assert all(r["info"] == 0 and r["flags"] == 0 for r in reps)
+    ref = BatchedKRR(probs, refine_steps=3, streams=1)
+    ref.run_eager()
+    for a, r in zip(alphas, ref.results()[0]):
+        assert np.array_equal(a.cpu().numpy(), r.cpu().numpy())
