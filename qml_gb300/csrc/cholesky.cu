@@ -41,6 +41,7 @@ potrf_diag_kernel(double *__restrict__ A, int64_t lda, int n, int k0, double shi
     // then solves the rows below it (one row per thread) and applies the rank-16
     // update to the trailing sub-matrix.
     __shared__ double S[NB][NB + 1];
+    __shared__ double rdiag[NB];  // 1 / L_cc, one FP64 division per column
     __shared__ int failed;
     if (*info != 0) return;
     const int tid = threadIdx.x;
@@ -63,12 +64,15 @@ potrf_diag_kernel(double *__restrict__ A, int64_t lda, int n, int k0, double shi
                         if (c < nb && !failed) atomicCAS(info, 0, k0 + c + 1);
                         failed = 1;
                         S[c][c] = 1.0;
+                        rdiag[c] = 1.0;
                     } else {
-                        S[c][c] = sqrt(p);
+                        const double dd = sqrt(p);
+                        S[c][c] = dd;
+                        rdiag[c] = 1.0 / dd;
                     }
                 }
                 __syncwarp();
-                const double dinv = 1.0 / S[c][c];
+                const double dinv = rdiag[c];
                 const int r = c + 1 + lane;
                 if (r < b0 + 16) S[r][c] *= dinv;
                 __syncwarp();
@@ -89,7 +93,7 @@ potrf_diag_kernel(double *__restrict__ A, int64_t lda, int n, int k0, double shi
             for (int c = 0; c < 16; ++c) x[c] = S[r][b0 + c];
 #pragma unroll
             for (int c = 0; c < 16; ++c) {
-                x[c] = x[c] / S[b0 + c][b0 + c];
+                x[c] = x[c] * rdiag[b0 + c];
 #pragma unroll
                 for (int c2 = c + 1; c2 < 16; ++c2) x[c2] = fma(-x[c], S[b0 + c2][b0 + c], x[c2]);
             }
@@ -123,6 +127,7 @@ trsm_panel_kernel(double *__restrict__ A, int64_t lda, int n, int k0,
 {
     __shared__ double L[NB][NB + 1];
     __shared__ double X[64][NB + 1];
+    __shared__ double rdiag[NB];
     if (*info != 0) return;
     const int tid = threadIdx.x;
     const int nb = min(NB, n - k0);
@@ -137,9 +142,10 @@ trsm_panel_kernel(double *__restrict__ A, int64_t lda, int n, int k0,
         const int r = e / NB, c = e % NB;
         X[r][c] = (r < rows && c < nb) ? A[(int64_t)(r0 + r) * lda + (k0 + c)] : 0.0;
     }
+    if (tid < NB) rdiag[tid] = tid < nb ? 1.0 / L[tid][tid] : 1.0;
     __syncthreads();
     for (int c = 0; c < nb; ++c) {
-        const double dinv = 1.0 / L[c][c];
+        const double dinv = rdiag[c];
         if (tid < 64) X[tid][c] *= dinv;
         __syncthreads();
         const int m = nb - c - 1;
@@ -732,7 +738,8 @@ int trsv_grid(int &grid)
             status = qmlg::set_cuda_error(e);
             return;
         }
-        cached = sms * std::max(1, std::min(per_sm, per_sm2));
+        // one CTA per SM: enough for the memory-bound updates, cheaper grid barriers
+        cached = std::min(per_sm, per_sm2) >= 1 ? sms : 0;
         if (cached < 2) status = QMLG_E_CUDA;
     });
     grid = cached;

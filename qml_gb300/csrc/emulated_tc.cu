@@ -144,24 +144,49 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
 
     if (warp == 0) {
         if (lane == 0) {
-            // ---------------- TMA producer: runs ahead across tiles
-            TileCursor cur;
+            // ---------------- TMA producer: runs ahead across tiles.  The i-planes of
+            // chunk g+1 are requested halfway through the j-planes of chunk g, so they
+            // are in flight while chunk g's MMAs run.
+            TileCursor cur, nxt;
             int g = 0, it = 0;
             bool ok = true;
+            int b_issued = -1;  // highest chunk index whose i-planes are requested
+            auto issue_b = [&](int gg, int brow_g, int cc) -> bool {
+                const int bb = gg & 1;
+                if (gg >= 2 && !mbar_wait(&bEmpty[bb], ((gg >> 1) - 1) & 1)) return false;
+                mbar_expect_tx(&bFull[bb], (uint32_t)(S * B_BYTES));
+                for (int u = 0; u < S; ++u)
+                    tma_load_3d(Bbuf + (bb * S_MAX + u) * B_BYTES, &mapB, &bFull[bb], cc * KC, brow_g, u);
+                b_issued = gg;
+                return true;
+            };
             for (int t = blockIdx.x; t < p.ntiles && ok; t += gridDim.x) {
                 int jt, itl;
                 cur.locate(p, t, jt, itl);
                 const int arow = p.a_row0 + jt * TM, brow = p.b_row0 + itl * TN;
+                // the chunk after this tile's last one belongs to the next tile
+                int brow_next = -1;
+                if (t + (int)gridDim.x < p.ntiles) {
+                    int jt2, it2;
+                    nxt = cur;
+                    nxt.locate(p, t + gridDim.x, jt2, it2);
+                    brow_next = p.b_row0 + it2 * TN;
+                }
                 for (int c = 0; c < p.kchunks && ok; ++c, ++g) {
-                    const int bb = g & 1;
-                    if (g >= 2 && !mbar_wait(&bEmpty[bb], ((g >> 1) - 1) & 1)) {
+                    if (b_issued < g && !issue_b(g, brow, c)) {
                         ok = false;
                         break;
                     }
-                    mbar_expect_tx(&bFull[bb], (uint32_t)(S * B_BYTES));
-                    for (int u = 0; u < S; ++u)
-                        tma_load_3d(Bbuf + (bb * S_MAX + u) * B_BYTES, &mapB, &bFull[bb], c * KC, brow, u);
                     for (int s = 0; s < S; ++s, ++it) {
+                        if (s == S / 2) {
+                            // next chunk's i-planes (this tile, or the next tile's first)
+                            if (c + 1 < p.kchunks) {
+                                if (!issue_b(g + 1, brow, c + 1)) ok = false;
+                            } else if (brow_next >= 0) {
+                                if (!issue_b(g + 1, brow_next, 0)) ok = false;
+                            }
+                            if (!ok) break;
+                        }
                         const int st = it % A_STAGES, round = it / A_STAGES;
                         if (round >= 1 && !mbar_wait(&aEmpty[st], (round - 1) & 1)) {
                             ok = false;
@@ -177,7 +202,6 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
     } else if (warp == 1) {
         if (lane == 0) {
             // ---------------- MMA issuer
-            const uint32_t idesc = idesc_bf16_f32(TM, TN);
             int g = 0, it = 0, u = 0;
             bool ok = true;
             for (int t = blockIdx.x; t < p.ntiles && ok; t += gridDim.x, ++u) {
@@ -201,14 +225,20 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
                         }
                         fence_after_sync();
                         const uint64_t da = desc_sw128(Aring + st * A_BYTES);
-                        for (int v = 0; v + s < S; ++v) {
+                        // the i-planes v .. v+cnt-1 sit back to back in shared memory, so
+                        // one MMA with N = 64 cnt (<= 256) accumulates levels s+v ..
+                        // s+v+cnt-1, each into its own 64 TMEM columns
+                        for (int v = 0; v + s < S;) {
+                            const int cnt = min(4, S - s - v);
+                            const uint32_t idn = idesc_bf16_f32(TM, TN * cnt);
                             const uint64_t db = desc_sw128(Bbuf + (bb * S_MAX + v) * B_BYTES);
                             const uint32_t dst = tmem + (uint32_t)((s + v) * TN);
 #pragma unroll
                             for (int kk = 0; kk < KC / 16; ++kk) {
                                 const uint32_t acc = (c > 0 || s > 0 || kk > 0) ? 1u : 0u;
-                                mma_bf16(dst, da + (uint64_t)(kk * 2), db + (uint64_t)(kk * 2), idesc, acc);
+                                mma_bf16(dst, da + (uint64_t)(kk * 2), db + (uint64_t)(kk * 2), idn, acc);
                             }
+                            v += cnt;
                         }
                         mma_commit(&aEmpty[st]);
                     }
@@ -235,6 +265,14 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
             const int j0 = p.jbase + jt * TM, i0 = p.ibase + itl * TN;
             const int arow = p.a_row0 + jt * TM, brow = p.b_row0 + itl * TN;
             const int j = j0 + jl;
+            if (MODE == kSyrk && j < p.jend) {
+                // while the MMAs run, pull this thread's column of C into L2 so the
+                // read-modify-write below does not wait on DRAM
+                const int ilim = min(i0 + TN, p.iend);
+                for (int i = i0; i < ilim; ++i)
+                    if (!p.lower || j <= i)
+                        asm volatile("prefetch.global.L2 [%0];" ::"l"(p.C + (int64_t)i * p.ldc + j));
+            }
             if (ok && !mbar_wait(tFull, u & 1)) {
                 ok = false;
                 if (lane == 0) atomicOr(p.err, 4);
