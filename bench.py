@@ -314,9 +314,8 @@ def run_ours(a):
     from qml_gb300.krr import KRR, molecules_to_device
     from qml_gb300.synthetic import generate_molecules
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    from qml_gb300 import replicas
+    world, rank, local = replicas.rank_info()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     if world > 1:
@@ -328,7 +327,7 @@ def run_ours(a):
         torch.cuda.synchronize()
 
     ntr, nte = a.ntrain, a.ntest
-    batch = generate_molecules(ntr + nte, seed=a.seed + rank)
+    batch = generate_molecules(ntr + nte, seed=replicas.replica_seed(a.seed, rank))
     z, r, off = molecules_to_device(batch, device=dev)
     y = torch.from_numpy(batch.labels).to(dev)
     stream = torch.cuda.current_stream(dev)
@@ -350,11 +349,7 @@ def run_ours(a):
             yhat, model = step()
         ev1.record(stream)
         barrier()
-    ms = ev0.elapsed_time(ev1) / a.steps
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = replicas.max_over_ranks(ev0.elapsed_time(ev1) / a.steps, device=dev)
     report = model.report
 
     # end to end through the public API with host buffers (pinned), copies inside
@@ -381,7 +376,7 @@ def run_ours(a):
         e2e_step()
     e1.record(stream)
     barrier()
-    e2e_s = e0.elapsed_time(e1) / a.steps / 1e3
+    e2e_s = replicas.max_over_ranks(e0.elapsed_time(e1) / a.steps / 1e3, device=dev)
 
     # per-stage times of one mixed step (events between stages)
     stages = {}
@@ -487,7 +482,13 @@ def run_ours(a):
     roofline = {"kernel": "emu_tc_kernel<syrk> (C %dx%d lower -= P P^T, k=%d, 8 digit planes)"
                 % (nsy, nsy, ksy),
                 "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak, "traffic": None,
+                "frac": achieved / peak,
+                # DRAM bytes per launch: 1.214e9 read+written by one ncu capture of
+                # the same kernel at n = 8192, k = 512 (profiles/emu_tc_syrk_n8192_k512.md),
+                # scaled by the lower-triangle size
+                "traffic": 1.214e9 * (nsy / 8192.0) ** 2,
+                "traffic_note": "scaled from an ncu capture at n=8192, k=512",
+                "algorithmic_bytes": 8.0 * nsy * (nsy + 1) + 8.0 * nsy * ksy + 16.0 * nsy * ksy,
                 "peak_source": "measured bf16 (MEASURED_PEAKS.json)" if peaks else "fallback",
                 "launch_s": syrk_s,
                 "fp64_equivalent_tflops": nsy * (nsy + 1) * ksy / syrk_s / 1e12}
@@ -502,7 +503,7 @@ def run_ours(a):
             "data": "synthetic", "config": workload_config(a),
             "e2e": {"value": e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "fits_per_s": world / (ms / 1e3),
+            "fits_per_s": replicas.job_throughput(1.0, ms / 1e3, world),
             "serving": serving_stats,
             "batching": batching_stats,
             "gpu_launches": launches, "clocks": clocks.summary(), "roofline": roofline,

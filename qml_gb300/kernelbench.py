@@ -1,0 +1,73 @@
+"""Run one hot-path kernel on seeded data, for timing and profiling.
+
+    python -m qml_gb300.kernelbench syrk  --n 8192 --k 512       # emulated trailing update
+    python -m qml_gb300.kernelbench gauss --n 8192               # tensor-core Gaussian K (symmetric)
+    python -m qml_gb300.kernelbench lapl  --n 8192               # fixed-point Laplacian K
+    python -m qml_gb300.kernelbench predict --n 20000 --m 5000   # tensor-core fused prediction
+    python -m qml_gb300.kernelbench cm    --n 25000              # sorted Coulomb matrices
+
+Each command runs the kernel `--reps` times after one warm-up call and prints the
+mean time per call (CUDA events on the launching stream).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+
+import torch
+
+from . import core
+from .krr import molecules_to_device
+from .synthetic import generate_molecules
+
+
+def _features(n, seed):
+    b = generate_molecules(n, seed=seed)
+    z, r, o = molecules_to_device(b)
+    return core.coulomb_matrix_batch(z, r, o, 23), (z, r, o)
+
+
+def main(argv=None):
+    p = argparse.ArgumentParser()
+    p.add_argument("kernel", choices=["syrk", "gauss", "lapl", "predict", "cm"])
+    p.add_argument("--n", type=int, default=8192)
+    p.add_argument("--m", type=int, default=2048)
+    p.add_argument("--k", type=int, default=512)
+    p.add_argument("--sigma", type=float, default=1000.0)
+    p.add_argument("--reps", type=int, default=2)
+    a = p.parse_args(argv)
+    dev = torch.device("cuda")
+    g = torch.Generator(device=dev).manual_seed(7)
+    if a.kernel == "syrk":
+        C = torch.rand((a.n, a.n), dtype=torch.float64, device=dev, generator=g)
+        P = torch.rand((a.n, a.k), dtype=torch.float64, device=dev, generator=g)
+        run = lambda: core.syrk_emulated(C, P)  # noqa: E731
+    elif a.kernel in ("gauss", "lapl"):
+        X, _ = _features(a.n, 1)
+        kind = "gaussian" if a.kernel == "gauss" else "laplacian"
+        K = torch.empty((a.n, a.n), dtype=torch.float64, device=dev).T
+        run = lambda: core.kernel_matrix(kind, X, X, a.sigma, symmetric=True, emulated=True,  # noqa: E731
+                                         out=K)
+    elif a.kernel == "predict":
+        X, _ = _features(a.n + a.m, 2)
+        alpha = torch.rand(a.n, dtype=torch.float64, device=dev, generator=g)
+        run = lambda: core.predict("gaussian", X[:a.n], X[a.n:], a.sigma, alpha,  # noqa: E731
+                                   emulated=True)
+    else:
+        _, (z, r, o) = _features(a.n, 3)
+        run = lambda: core.coulomb_matrix_batch(z, r, o, 23)  # noqa: E731
+    run()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(a.reps):
+        run()
+    e1.record()
+    torch.cuda.synchronize()
+    print(json.dumps({"kernel": a.kernel, "n": a.n, "m": a.m, "k": a.k,
+                      "ms_per_call": e0.elapsed_time(e1) / a.reps}))
+
+
+if __name__ == "__main__":
+    main()
