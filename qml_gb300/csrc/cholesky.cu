@@ -32,17 +32,52 @@ constexpr int NB = 64;
 
 // ---------------------------------------------------------------- factor --
 
+// 1/sqrt(p) for a positive finite double, without FP64 sqrt or division (each
+// costs ~650 cycles on this GPU against 64 for an FMA): p is scaled by an even
+// power of two into [1, 4), an FP32 rsqrtf gives ~23 bits, and one Halley step
+// (cubic convergence for f(y) = 1/y^2 - p) brings it to full FP64 precision:
+//   e = 1 - p y^2,  y <- y + y e (1/2 + 3/8 e).
+__device__ __forceinline__ double rsqrt_halley(double p)
+{
+    int ex = ilogb(p) & ~1;
+    const double q = scalbn(p, -ex);
+    double y = (double)rsqrtf((float)q);
+    const double e = fma(-q * y, y, 1.0);
+    y = fma(y * e, fma(0.375, e, 0.5), y);
+    return scalbn(y, -ex / 2);
+}
+
+// Pivot of column c: S_cc <- sqrt(S_cc), rd[c] <- 1/sqrt(S_cc) (always > 0).  When
+// S_cc is not positive and finite, rd[c] <- 0 marks the failure and the failing
+// column is recorded in info.
+__device__ __forceinline__ void potrf_pivot(double (*S)[NB + 1], double *rd, int c, int k0,
+                                            int nb, int *info)
+{
+    const double p = S[c][c];
+    if (!(p > 0.0) || !isfinite(p)) {
+        if (c < nb) atomicCAS(info, 0, k0 + c + 1);
+        rd[c] = 0.0;
+        return;
+    }
+    const double y = rsqrt_halley(p);
+    rd[c] = y;
+    S[c][c] = p * y;
+}
+
 __global__ void __launch_bounds__(256)
 potrf_diag_kernel(double *__restrict__ A, int64_t lda, int n, int k0, double shift,
                   int *__restrict__ info)
 {
-    // The 64 x 64 block in shared memory, factorised in four 16-column sub-panels:
-    // warp 0 factors the 16 x 16 diagonal sub-block (warp-synchronous), every thread
-    // then solves the rows below it (one row per thread) and applies the rank-16
-    // update to the trailing sub-matrix.
+    // Right-looking in shared memory with one barrier per column.  Thread t owns
+    // row r = t / 4 and the columns s = t % 4 (mod 4) of that row.  In phase c
+    // every owned element with c < s <= r takes the rank-1 update
+    // S_rs -= S_rc S_sc / S_cc (one FMA: the row factor carries rd[c]^2); the
+    // owner of S_{c+1,c+1} then computes the next pivot at once, so the pivot's
+    // latency overlaps the other rows' updates.  Column c is scaled by rd[c] by
+    // its owners in phase c+1, when nobody reads it any more.  rd[c] is written one
+    // phase before it is read, so rd[c] == 0 is a race-free failure signal.
     __shared__ double S[NB][NB + 1];
-    __shared__ double rdiag[NB];  // 1 / L_cc, one FP64 division per column
-    __shared__ int failed;
+    __shared__ double rd[NB];
     if (*info != 0) return;
     const int tid = threadIdx.x;
     const int nb = min(NB, n - k0);
@@ -52,65 +87,19 @@ potrf_diag_kernel(double *__restrict__ A, int64_t lda, int n, int k0, double shi
         if (r < nb && c <= r) v = A[(int64_t)(k0 + r) * lda + (k0 + c)] + (r == c ? shift : 0.0);
         S[r][c] = v;
     }
-    if (tid == 0) failed = 0;
     __syncthreads();
-    for (int b0 = 0; b0 < NB; b0 += 16) {
-        if (tid < 32) {
-            const int lane = tid;
-            for (int c = b0; c < b0 + 16; ++c) {
-                if (lane == 0) {
-                    const double p = S[c][c];
-                    if (!(p > 0.0) || !isfinite(p)) {
-                        if (c < nb && !failed) atomicCAS(info, 0, k0 + c + 1);
-                        failed = 1;
-                        S[c][c] = 1.0;
-                        rdiag[c] = 1.0;
-                    } else {
-                        const double dd = sqrt(p);
-                        S[c][c] = dd;
-                        rdiag[c] = 1.0 / dd;
-                    }
-                }
-                __syncwarp();
-                const double dinv = rdiag[c];
-                const int r = c + 1 + lane;
-                if (r < b0 + 16) S[r][c] *= dinv;
-                __syncwarp();
-                for (int e = lane; e < 16 * 16; e += 32) {
-                    const int rr = b0 + (e >> 4), cc = b0 + (e & 15);
-                    if (cc > c && rr >= cc) S[rr][cc] = fma(-S[rr][c], S[cc][c], S[rr][cc]);
-                }
-                __syncwarp();
-            }
-        }
-        __syncthreads();
-        if (failed) return;
-        // rows below the sub-block: X <- X L_bb^-T, one row per thread
-        const int r = b0 + 16 + tid;
-        if (r < NB) {
-            double x[16];
-#pragma unroll
-            for (int c = 0; c < 16; ++c) x[c] = S[r][b0 + c];
-#pragma unroll
-            for (int c = 0; c < 16; ++c) {
-                x[c] = x[c] * rdiag[b0 + c];
-#pragma unroll
-                for (int c2 = c + 1; c2 < 16; ++c2) x[c2] = fma(-x[c], S[b0 + c2][b0 + c], x[c2]);
-            }
-#pragma unroll
-            for (int c = 0; c < 16; ++c) S[r][b0 + c] = x[c];
-        }
-        __syncthreads();
-        // rank-16 update of the trailing lower triangle
-        const int t0 = b0 + 16, m = NB - t0;
-        for (int e = tid; e < m * m; e += blockDim.x) {
-            const int rr = t0 + e / m, cc = t0 + e % m;
-            if (cc <= rr) {
-                double acc = S[rr][cc];
-#pragma unroll
-                for (int c = 0; c < 16; ++c) acc = fma(-S[rr][b0 + c], S[cc][b0 + c], acc);
-                S[rr][cc] = acc;
-            }
+    if (tid == 0) potrf_pivot(S, rd, 0, k0, nb, info);
+    __syncthreads();
+    const int r = tid >> 2, s0 = tid & 3;
+    for (int c = 0; c < NB; ++c) {
+        if (rd[c] == 0.0) return;
+        if (c > 0 && r >= c && s0 == ((c - 1) & 3)) S[r][c - 1] *= rd[c - 1];
+        if (r > c) {
+            const double y = rd[c];
+            const double f = -S[r][c] * (y * y);
+            for (int s = c + 1 + ((s0 - c - 1) & 3); s <= r; s += 4)
+                S[r][s] = fma(f, S[s][c], S[r][s]);
+            if (r == c + 1 && s0 == (r & 3)) potrf_pivot(S, rd, r, k0, nb, info);
         }
         __syncthreads();
     }
@@ -838,6 +827,58 @@ size_t emulated_factor_ws(int n)
     return p.total();
 }
 
+// Internal second stream and events of the calling thread on the current device,
+// created on first use (the look-ahead below forks onto it and joins back).
+struct AuxStream {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+};
+
+int aux_stream(AuxStream *&out)
+{
+    thread_local AuxStream pool[16];
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return set_cuda_error(e);
+    if (dev < 0 || dev >= 16) return QMLG_E_ARG;
+    AuxStream &a = pool[dev];
+    if (a.stream == nullptr) {
+        e = cudaStreamCreateWithFlags(&a.stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&a.fork, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&a.join, cudaEventDisableTiming);
+        if (e != cudaSuccess) return set_cuda_error(e);
+    }
+    out = &a;
+    return QMLG_OK;
+}
+
+// The 64-wide steps of one 512-column panel [K0, K1): FP64 diagonal block and
+// TRSM, then the emulated K = 64 update of the panel's remaining columns.
+int factor_panel(double *A, int n, int64_t lda, double shift, int K0, int K1, int rpad,
+                 int slices, __nv_bfloat16 *dig_in, int *exp_in, int *d_info, int *d_err,
+                 cudaStream_t s, int update_ctas)
+{
+    for (int k0 = K0; k0 < K1; k0 += NB) {
+        { potrf_diag_kernel<<<1, 256, 0, s>>>(A, lda, n, k0, shift, d_info); count_launches(1); }
+        const int r1 = k0 + NB;
+        if (r1 >= n) break;
+        { trsm_panel_kernel<<<(int)ceil_div(n - r1, 64), 256, 0, s>>>(A, lda, n, k0, d_info); count_launches(1); }
+        if (r1 < K1) {
+            int st = slice_rows(A, lda, r1, n - r1, k0, NB, NB, rpad, slices, dig_in, exp_in, d_info, s);
+            if (st == QMLG_OK)
+                st = emu_tc_update(A, lda, r1, K1, r1, n, dig_in, exp_in, NB, rpad, slices, 0, 0, 1,
+                                   d_err, s, update_ctas);
+            if (st != QMLG_OK) return st;
+        }
+    }
+    return check_launch();
+}
+
+// Look-ahead schedule.  After panel p is factorised its rank-512 update is split:
+// (1) the next panel's columns [K1, K2) on the caller's stream; then (2) all
+// columns right of K2 on the caller's stream with a grid that leaves a few SMs
+// free, while the next panel's 64-wide FP64 chain runs on the auxiliary stream in
+// those SMs.  The two touch disjoint columns; the next outer step joins them.
 int emulated_factor(double *A, int n, int64_t lda, double shift, Workspace &ws, int *d_info,
                     EmulatedFactor &f, cudaStream_t s, int slices)
 {
@@ -853,29 +894,52 @@ int emulated_factor(double *A, int n, int64_t lda, double shift, Workspace &ws, 
         return QMLG_E_WORKSPACE;
     cudaError_t e = cudaMemsetAsync(d_err, 0, sizeof(int), s);
     if (e != cudaSuccess) return set_cuda_error(e);
-    int st = QMLG_OK;
+    AuxStream *aux = nullptr;
+    int st = aux_stream(aux);
+    if (st != QMLG_OK) return st;
+    const int sms = tc_sm_count();
+    // SMs left to the panel chain.  Threads that run many solves side by side
+    // (cooperative kernels off, e.g. batched fits) keep one stream per solve and
+    // skip the look-ahead, so concurrent solves do not share the auxiliary stream.
+    const int reserve = (sms >= 64 && cooperative_on()) ? 8 : 0;
+    st = factor_panel(A, n, lda, shift, 0, std::min(NBO, n), rpad, slices, dig_in, exp_in, d_info,
+                      d_err, s, 0);
     for (int K0 = 0; K0 < n && st == QMLG_OK; K0 += NBO) {
-        const int K1 = min(K0 + NBO, n);
-        for (int k0 = K0; k0 < K1; k0 += NB) {
-            { potrf_diag_kernel<<<1, 256, 0, s>>>(A, lda, n, k0, shift, d_info); count_launches(1); }
-            const int r1 = k0 + NB;
-            if (r1 >= n) break;
-            { trsm_panel_kernel<<<(int)ceil_div(n - r1, 64), 256, 0, s>>>(A, lda, n, k0, d_info); count_launches(1); }
-            if (r1 < K1) {
-                st = slice_rows(A, lda, r1, n - r1, k0, NB, NB, rpad, slices, dig_in, exp_in, d_info, s);
-                if (st == QMLG_OK)
-                    st = emu_tc_update(A, lda, r1, K1, r1, n, dig_in, exp_in, NB, rpad, slices, 0, 0, 1,
-                                       d_err, s);
-                if (st != QMLG_OK) break;
+        const int K1 = std::min(K0 + NBO, n);
+        if (K1 >= n) break;
+        const int K2 = std::min(K1 + NBO, n);
+        const int kw = K1 - K0;
+        const int kp = (int)ceil_div(kw, 64) * 64;
+        st = slice_rows(A, lda, K1, n - K1, K0, kw, kp, rpad, slices, dig_out, exp_out, d_info, s);
+        if (st != QMLG_OK) break;
+        // (1) the next panel's columns
+        st = emu_tc_update(A, lda, K1, K2, K1, n, dig_out, exp_out, kp, rpad, slices, 0, 0, 1, d_err,
+                           s, 0);
+        if (st != QMLG_OK) break;
+        if (K2 < n && reserve > 0) {
+            // fork: the next panel's chain on the auxiliary stream
+            if ((e = cudaEventRecord(aux->fork, s)) != cudaSuccess ||
+                (e = cudaStreamWaitEvent(aux->stream, aux->fork, 0)) != cudaSuccess) {
+                st = set_cuda_error(e);
+                break;
             }
-        }
-        if (st == QMLG_OK && K1 < n) {
-            const int kw = K1 - K0;
-            const int kp = (int)ceil_div(kw, 64) * 64;
-            st = slice_rows(A, lda, K1, n - K1, K0, kw, kp, rpad, slices, dig_out, exp_out, d_info, s);
+            // (2) the rest of the trailing matrix, leaving `reserve` SMs free
+            st = emu_tc_update(A, lda, K2, n, K2, n, dig_out, exp_out, kp, rpad, slices, K2 - K1,
+                               K2 - K1, 1, d_err, s, sms - reserve);
             if (st == QMLG_OK)
-                st = emu_tc_update(A, lda, K1, n, K1, n, dig_out, exp_out, kp, rpad, slices, 0, 0, 1,
-                                   d_err, s);
+                st = factor_panel(A, n, lda, shift, K1, K2, rpad, slices, dig_in, exp_in, d_info,
+                                  d_err, aux->stream, -1);
+            // join before the next outer step reads the panel (and reuses dig_out)
+            if (st == QMLG_OK && ((e = cudaEventRecord(aux->join, aux->stream)) != cudaSuccess ||
+                                  (e = cudaStreamWaitEvent(s, aux->join, 0)) != cudaSuccess))
+                st = set_cuda_error(e);
+        } else {
+            if (K2 < n)
+                st = emu_tc_update(A, lda, K2, n, K2, n, dig_out, exp_out, kp, rpad, slices, K2 - K1,
+                                   K2 - K1, 1, d_err, s, 0);
+            if (st == QMLG_OK)
+                st = factor_panel(A, n, lda, shift, K1, K2, rpad, slices, dig_in, exp_in, d_info,
+                                  d_err, s, 0);
         }
     }
     if (st != QMLG_OK) return st;

@@ -32,9 +32,13 @@ int slice_rows(const double *A, int64_t lda, int r0, int nrows, int c0, int kw, 
 // C[i][j] -= sum_k P[i][k] P[j][k] for j in [jbase, jend), i in [ibase, iend) (j <= i
 // when lower), P rows taken from the digit planes (digit row = a_row0 + j - jbase for
 // the j side, b_row0 + i - ibase for the i side), K = kp <= 512.
+// max_ctas: 0 = the calling thread's default grid, > 0 = persistent grid of at most
+// that many CTAs, < 0 = one CTA per tile.
 int emu_tc_update(double *C, int64_t ldc, int jbase, int jend, int ibase, int iend,
                   const __nv_bfloat16 *digits, const int *expo, int kp, int rpad, int slices,
-                  int a_row0, int b_row0, int lower, int *d_err, cudaStream_t s);
+                  int a_row0, int b_row0, int lower, int *d_err, cudaStream_t s, int max_ctas = 0);
+// SM count of the current device, after the calling thread's cap.
+int tc_sm_count();
 
 // In-place factor with emulated trailing updates; storage as the FP64 factor.
 struct EmulatedFactor {

@@ -605,7 +605,7 @@ int slice_rows(const double *A, int64_t lda, int r0, int nrows, int c0, int kw, 
 
 int emu_tc_update(double *C, int64_t ldc, int jbase, int jend, int ibase, int iend,
                   const __nv_bfloat16 *digits, const int *expo, int kp, int rpad, int slices,
-                  int a_row0, int b_row0, int lower, int *d_err, cudaStream_t s)
+                  int a_row0, int b_row0, int lower, int *d_err, cudaStream_t s, int max_ctas)
 {
     if (jend <= jbase || iend <= ibase) return QMLG_OK;
     if (slices < 1 || slices > S_MAX || kp % KC != 0 || kp / KC > 8) return QMLG_E_ARG;
@@ -631,11 +631,17 @@ int emu_tc_update(double *C, int64_t ldc, int jbase, int jend, int ibase, int ie
     a.expB = expo;
     a.lower = lower;
     a.err = d_err;
-    const int grid = tile_grid(a.ntiles);
+    // max_ctas > 0: persistent grid of at most that many CTAs (leaves SMs free for
+    // work on another stream); max_ctas < 0: one CTA per tile; 0: the thread default
+    int grid = tile_grid(a.ntiles);
+    if (max_ctas > 0) grid = std::min(a.ntiles, max_ctas);
+    if (max_ctas < 0) grid = a.ntiles;
     emu_tc_kernel<kSyrk><<<grid, 192, SMEM_BYTES, s>>>(mA, mB, a);
     count_launches(1);
     return check_launch();
 }
+
+int tc_sm_count() { return sm_count(); }
 
 }  // namespace qmlg
 
@@ -872,7 +878,7 @@ extern "C" int qmlg_syrk_emulated(double *C, int64_t ldc, int n, const double *P
     if (e != cudaSuccess) return qmlg::set_cuda_error(e);
     int st = qmlg::slice_rows(P, ldp, 0, n, 0, k, kp, rp, S_MAX, dig, ex, nullptr, s);
     if (st == QMLG_OK)
-        st = qmlg::emu_tc_update(C, ldc, 0, n, 0, n, dig, ex, kp, rp, S_MAX, 0, 0, 1, err, s);
+        st = qmlg::emu_tc_update(C, ldc, 0, n, 0, n, dig, ex, kp, rp, S_MAX, 0, 0, 1, err, s, 0);
     return st;
 }
 
