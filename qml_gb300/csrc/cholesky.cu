@@ -33,25 +33,37 @@ constexpr int NB = 64;
 // ---------------------------------------------------------------- factor --
 
 // 1/sqrt(p) for a positive finite double, without FP64 sqrt or division (each
-// costs ~650 cycles on this GPU against 64 for an FMA): p is scaled by an even
-// power of two into [1, 4), an FP32 rsqrtf gives ~23 bits, and one Halley step
-// (cubic convergence for f(y) = 1/y^2 - p) brings it to full FP64 precision:
-//   e = 1 - p y^2,  y <- y + y e (1/2 + 3/8 e).
+// costs ~650 cycles on this GPU against 64 for an FMA): an FP32 rsqrtf gives ~23
+// bits and one Halley step (cubic convergence for f(y) = 1/y^2 - p) brings it to
+// full FP64 precision:  e = 1 - p y^2,  y <- y + y e (1/2 + 3/8 e).  Outside
+// [2^-120, 2^120] p is first scaled by an even power of two into [1, 4).
 __device__ __forceinline__ double rsqrt_halley(double p)
 {
-    int ex = ilogb(p) & ~1;
-    const double q = scalbn(p, -ex);
+    double q = p;
+    int h = 0;
+    if (!(p >= 0x1p-120 && p <= 0x1p120)) {
+        const int ex = ilogb(p) & ~1;
+        q = scalbn(p, -ex);
+        h = -ex / 2;
+    }
     double y = (double)rsqrtf((float)q);
     const double e = fma(-q * y, y, 1.0);
     y = fma(y * e, fma(0.375, e, 0.5), y);
-    return scalbn(y, -ex / 2);
+    return h != 0 ? scalbn(y, h) : y;
 }
 
-// Pivot of column c: S_cc <- sqrt(S_cc), rd[c] <- 1/sqrt(S_cc) (always > 0).  When
-// S_cc is not positive and finite, rd[c] <- 0 marks the failure and the failing
-// column is recorded in info.
-__device__ __forceinline__ void potrf_pivot(double (*S)[NB + 1], double *rd, int c, int k0,
-                                            int nb, int *info)
+// Number of lower-triangle elements (r, s) with c < s <= r < NB.
+__host__ __device__ constexpr int tri_prefix(int c) { return (NB - 1 - c) * (NB - c) / 2; }
+
+constexpr int POTRF_THREADS = 256;
+constexpr int POTRF_WORKERS = 224;  // warps 0-6 update; lane 0 of warp 7 takes the pivots
+constexpr int POTRF_PIVOT = POTRF_WORKERS;
+
+// Pivot of column c: S_cc <- sqrt(S_cc), rd[c] <- 1/sqrt(S_cc) (> 0), rd2[c] <-
+// 1/S_cc.  When S_cc is not positive and finite, rd[c] <- 0 marks the failure and
+// the failing column is recorded in info.
+__device__ __forceinline__ void potrf_pivot(double (*S)[NB + 1], double *rd, double *rd2, int c,
+                                            int k0, int nb, int *info)
 {
     const double p = S[c][c];
     if (!(p > 0.0) || !isfinite(p)) {
@@ -61,23 +73,26 @@ __device__ __forceinline__ void potrf_pivot(double (*S)[NB + 1], double *rd, int
     }
     const double y = rsqrt_halley(p);
     rd[c] = y;
+    rd2[c] = y * y;
     S[c][c] = p * y;
 }
 
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(POTRF_THREADS)
 potrf_diag_kernel(double *__restrict__ A, int64_t lda, int n, int k0, double shift,
                   int *__restrict__ info)
 {
-    // Right-looking in shared memory with one barrier per column.  Thread t owns
-    // row r = t / 4 and the columns s = t % 4 (mod 4) of that row.  In phase c
-    // every owned element with c < s <= r takes the rank-1 update
-    // S_rs -= S_rc S_sc / S_cc (one FMA: the row factor carries rd[c]^2); the
-    // owner of S_{c+1,c+1} then computes the next pivot at once, so the pivot's
-    // latency overlaps the other rows' updates.  Column c is scaled by rd[c] by
-    // its owners in phase c+1, when nobody reads it any more.  rd[c] is written one
-    // phase before it is read, so rd[c] == 0 is a race-free failure signal.
+    // Right-looking in shared memory, one barrier per column.  In phase c every
+    // element with c < s <= r takes S_rs -= S_rc S_sc / S_cc (one FMA; the unscaled
+    // column c and rd2[c] = 1/S_cc).  The elements are listed in `order` by s
+    // descending, r descending, so phase c's are the first tri_prefix(c) entries and
+    // the last of them is the next diagonal S_{c+1,c+1}: the workers share the others
+    // evenly, while the pivot thread updates that diagonal and takes its pivot at
+    // once, so the pivot latency overlaps the updates.  rd[c] is written one phase
+    // before it is read, so rd[c] == 0 is a race-free failure signal.  Columns are
+    // scaled by rd at the end.
     __shared__ double S[NB][NB + 1];
-    __shared__ double rd[NB];
+    __shared__ double rd[NB], rd2[NB];
+    __shared__ unsigned short order[tri_prefix(0)];
     if (*info != 0) return;
     const int tid = threadIdx.x;
     const int nb = min(NB, n - k0);
@@ -87,66 +102,136 @@ potrf_diag_kernel(double *__restrict__ A, int64_t lda, int n, int k0, double shi
         if (r < nb && c <= r) v = A[(int64_t)(k0 + r) * lda + (k0 + c)] + (r == c ? shift : 0.0);
         S[r][c] = v;
     }
+    if (tid >= 1 && tid < NB) {
+        const int sc = tid, base = tri_prefix(sc);
+        for (int t = 0; t < NB - sc; ++t) order[base + t] = (unsigned short)(((NB - 1 - t) << 8) | sc);
+    }
     __syncthreads();
-    if (tid == 0) potrf_pivot(S, rd, 0, k0, nb, info);
+    if (tid == POTRF_PIVOT) potrf_pivot(S, rd, rd2, 0, k0, nb, info);
     __syncthreads();
-    const int r = tid >> 2, s0 = tid & 3;
     for (int c = 0; c < NB; ++c) {
         if (rd[c] == 0.0) return;
-        if (c > 0 && r >= c && s0 == ((c - 1) & 3)) S[r][c - 1] *= rd[c - 1];
-        if (r > c) {
-            const double y = rd[c];
-            const double f = -S[r][c] * (y * y);
-            for (int s = c + 1 + ((s0 - c - 1) & 3); s <= r; s += 4)
-                S[r][s] = fma(f, S[s][c], S[r][s]);
-            if (r == c + 1 && s0 == (r & 3)) potrf_pivot(S, rd, r, k0, nb, info);
+        const double y2 = rd2[c];
+        if (tid == POTRF_PIVOT) {
+            if (c + 1 < NB) {
+                const double v = S[c + 1][c];
+                S[c + 1][c + 1] = fma(-v * y2, v, S[c + 1][c + 1]);
+                potrf_pivot(S, rd, rd2, c + 1, k0, nb, info);
+            }
+        } else if (tid < POTRF_WORKERS) {
+            const int cnt = tri_prefix(c) - 1;
+            for (int e0 = tid; e0 < cnt; e0 += 3 * POTRF_WORKERS) {
+                // loads of three elements first, then their FMAs and stores
+                int rr[3], ss[3];
+                double x[3], u[3], v[3];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const int e = e0 + k * POTRF_WORKERS;
+                    if (e < cnt) {
+                        const unsigned code = order[e];
+                        rr[k] = (int)(code >> 8);
+                        ss[k] = (int)(code & 255u);
+                        x[k] = S[rr[k]][ss[k]];
+                        u[k] = S[rr[k]][c];
+                        v[k] = S[ss[k]][c];
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < 3; ++k)
+                    if (e0 + k * POTRF_WORKERS < cnt) S[rr[k]][ss[k]] = fma(-u[k] * y2, v[k], x[k]);
+            }
         }
         __syncthreads();
     }
     for (int e = tid; e < nb * NB; e += blockDim.x) {
-        const int rr = e >> 6, cc = e & 63;
-        if (cc <= rr) A[(int64_t)(k0 + rr) * lda + (k0 + cc)] = S[rr][cc];
+        const int r = e >> 6, c = e & 63;
+        if (c <= r) A[(int64_t)(k0 + r) * lda + (k0 + c)] = (c < r) ? S[r][c] * rd[c] : S[r][c];
     }
 }
 
-// X <- X * L_kk^{-T} for the rows below the diagonal block.
+constexpr int TRSM_ROWS = 64;
+
+// X <- X L_kk^{-T} for the rows below the diagonal block, one CTA per 64 rows.  A
+// row is held by the four lanes of a quad (lane q owns the columns = q mod 4, in
+// registers); column c is finished by its owner and broadcast with a shuffle, so
+// the substitution needs no block barrier.  With `digits`, the kernel also writes
+// what slice_rows would make of the solved rows (the operand of the emulated K = 64
+// update that follows): per-row exponents and the `slices` balanced base-128 digit
+// planes, digits[s][row][64] with row = global row - (k0 + 64), for the rows below
+// drows (zeros past the matrix).
 __global__ void __launch_bounds__(256)
 trsm_panel_kernel(double *__restrict__ A, int64_t lda, int n, int k0,
-                  const int *__restrict__ info)
+                  const int *__restrict__ info, int slices, int rpad, int drows,
+                  __nv_bfloat16 *__restrict__ digits, int *__restrict__ expo)
 {
     __shared__ double L[NB][NB + 1];
-    __shared__ double X[64][NB + 1];
-    __shared__ double rdiag[NB];
+    __shared__ double rdg[NB];
+    __shared__ __align__(16) __nv_bfloat16 P[TRSM_ROWS][NB + 8];
     if (*info != 0) return;
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31;
     const int nb = min(NB, n - k0);
-    const int r0 = k0 + nb + blockIdx.x * 64;
-    const int rows = min(64, n - r0);
-    if (rows <= 0) return;
+    const int r1 = k0 + nb, nrows = n - r1;
+    const int rbase = blockIdx.x * TRSM_ROWS;
     for (int e = tid; e < NB * NB; e += blockDim.x) {
-        const int r = e / NB, c = e % NB;
-        L[r][c] = (r < nb && c <= r) ? A[(int64_t)(k0 + r) * lda + (k0 + c)] : 0.0;
+        const int r = e >> 6, c = e & 63;
+        L[r][c] = (r < nb && c <= r) ? A[(int64_t)(k0 + r) * lda + (k0 + c)] : (r == c ? 1.0 : 0.0);
     }
-    for (int e = tid; e < 64 * NB; e += blockDim.x) {
-        const int r = e / NB, c = e % NB;
-        X[r][c] = (r < rows && c < nb) ? A[(int64_t)(r0 + r) * lda + (k0 + c)] : 0.0;
-    }
-    if (tid < NB) rdiag[tid] = tid < nb ? 1.0 / L[tid][tid] : 1.0;
     __syncthreads();
-    for (int c = 0; c < nb; ++c) {
-        const double dinv = rdiag[c];
-        if (tid < 64) X[tid][c] *= dinv;
-        __syncthreads();
-        const int m = nb - c - 1;
-        for (int e = tid; e < 64 * m; e += blockDim.x) {
-            const int r = e / m, s = c + 1 + e % m;
-            X[r][s] = fma(-X[r][c], L[s][c], X[r][s]);
+    if (tid < NB) rdg[tid] = 1.0 / L[tid][tid];
+    const int r = tid >> 2, s0 = tid & 3, qbase = lane & ~3;
+    const int grow = rbase + r;
+    const bool live = grow < nrows;
+    double *row = A + (int64_t)(r1 + (live ? grow : 0)) * lda + k0;
+    double x[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) x[j] = live ? row[s0 + 4 * j] : 0.0;
+    __syncthreads();
+#pragma unroll
+    for (int c = 0; c < NB; ++c) {
+        const int jc = c >> 2, oc = c & 3;
+        const double t = x[jc] * rdg[c];
+        const double xc = __shfl_sync(0xffffffffu, t, qbase | oc);
+        if (s0 == oc) x[jc] = xc;
+        if (s0 > oc) x[jc] = fma(-xc, L[s0 + 4 * jc][c], x[jc]);
+#pragma unroll
+        for (int j = jc + 1; j < 16; ++j) x[j] = fma(-xc, L[s0 + 4 * j][c], x[j]);
+    }
+    if (live)
+#pragma unroll
+        for (int j = 0; j < 16; ++j) row[s0 + 4 * j] = x[j];
+    if (digits == nullptr) return;
+    double m = 0.0;
+#pragma unroll
+    for (int j = 0; j < 16; ++j) m = fmax(m, fabs(x[j]));
+    m = fmax(m, __shfl_xor_sync(0xffffffffu, m, 1));
+    m = fmax(m, __shfl_xor_sync(0xffffffffu, m, 2));
+    int e = 0;
+    if (m > 0.0 && isfinite(m)) {
+        frexp(m, &e);
+        e += 1;  // |x| * 2^-e < 1/2
+    }
+    const double scale = scalbn(1.0, 7 * slices - e);
+    long long q[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) q[j] = __double2ll_rn(x[j] * scale);
+    if (s0 == 0 && grow < drows) expo[grow] = e;
+    const int64_t plane = (int64_t)rpad * NB;
+    for (int sl = slices - 1; sl >= 0; --sl) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            // the most significant digit keeps the remainder (|q| <= 64 there)
+            const long long d = sl > 0 ? ((q[j] + 64) & 127) - 64 : q[j];
+            q[j] = (q[j] - d) >> 7;
+            P[r][s0 + 4 * j] = __int2bfloat16_rn((int)d);
         }
         __syncthreads();
-    }
-    for (int e = tid; e < rows * nb; e += blockDim.x) {
-        const int r = e / nb, c = e % nb;
-        A[(int64_t)(r0 + r) * lda + (k0 + c)] = X[r][c];
+        for (int i = tid; i < TRSM_ROWS * (NB / 8); i += blockDim.x) {
+            const int rr = i >> 3, ch = i & 7, g = rbase + rr;
+            if (g < drows)
+                *reinterpret_cast<uint4 *>(digits + sl * plane + (int64_t)g * NB + ch * 8) =
+                    *reinterpret_cast<const uint4 *>(&P[rr][ch * 8]);
+        }
+        __syncthreads();
     }
 }
 
@@ -758,7 +843,7 @@ int cholesky_fp64(double *A, int n, int64_t lda, double shift, int *d_info, cuda
         { potrf_diag_kernel<<<1, 256, 0, s>>>(A, lda, n, k0, shift, d_info); qmlg::count_launches(1); }
         const int below = n - (k0 + NB);
         if (below > 0) {
-            { trsm_panel_kernel<<<(int)ceil_div(below, 64), 256, 0, s>>>(A, lda, n, k0, d_info); qmlg::count_launches(1); }
+            { trsm_panel_kernel<<<(int)ceil_div(below, TRSM_ROWS), 256, 0, s>>>(A, lda, n, k0, d_info, 0, 0, 0, nullptr, nullptr); qmlg::count_launches(1); }
             const int64_t t = ceil_div(below, 64);
             { syrk_update_kernel<<<(unsigned)(t * (t + 1) / 2), 256, 0, s>>>(A, lda, n, k0, d_info); qmlg::count_launches(1); }
         }
@@ -862,12 +947,18 @@ int factor_panel(double *A, int n, int64_t lda, double shift, int K0, int K1, in
         { potrf_diag_kernel<<<1, 256, 0, s>>>(A, lda, n, k0, shift, d_info); count_launches(1); }
         const int r1 = k0 + NB;
         if (r1 >= n) break;
-        { trsm_panel_kernel<<<(int)ceil_div(n - r1, 64), 256, 0, s>>>(A, lda, n, k0, d_info); count_launches(1); }
-        if (r1 < K1) {
-            int st = slice_rows(A, lda, r1, n - r1, k0, NB, NB, rpad, slices, dig_in, exp_in, d_info, s);
-            if (st == QMLG_OK)
-                st = emu_tc_update(A, lda, r1, K1, r1, n, dig_in, exp_in, NB, rpad, slices, 0, 0, 1,
-                                   d_err, s, update_ctas);
+        // the solved rows' digit planes feed the panel's own K = 64 update
+        const bool inner = r1 < K1;
+        const int drows = inner ? std::min(rpad, (int)ceil_div(n - r1, 128) * 128) : 0;
+        {
+            trsm_panel_kernel<<<(int)ceil_div(inner ? drows : n - r1, TRSM_ROWS), 256, 0, s>>>(
+                A, lda, n, k0, d_info, slices, rpad, drows, inner ? dig_in : nullptr,
+                inner ? exp_in : nullptr);
+            count_launches(1);
+        }
+        if (inner) {
+            const int st = emu_tc_update(A, lda, r1, K1, r1, n, dig_in, exp_in, NB, rpad, slices, 0,
+                                         0, 1, d_err, s, update_ctas);
             if (st != QMLG_OK) return st;
         }
     }

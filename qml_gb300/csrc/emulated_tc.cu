@@ -597,7 +597,11 @@ int slice_rows(const double *A, int64_t lda, int r0, int nrows, int c0, int kw, 
                double *norms)
 {
     if (slices < 1 || slices > S_MAX || kp % KC != 0 || kw > kp || nrows > rpad) return QMLG_E_ARG;
-    slice_rows_kernel<<<(unsigned)ceil_div((int64_t)rpad * 32, 256), 256, 0, s>>>(
+    // Tiles read digit rows below ceil128(nrows) only: rows up to there are written
+    // (zeros past nrows), the rest of the buffer is left as it is.
+    const int rows = std::min(rpad, (int)ceil_div(nrows, 128) * 128);
+    if (rows == 0) return QMLG_OK;
+    slice_rows_kernel<<<(unsigned)ceil_div((int64_t)rows * 32, 256), 256, 0, s>>>(
         A, lda, r0, nrows, c0, kw, kp, rpad, slices, digits, expo, norms, d_info);
     count_launches(1);
     return check_launch();
