@@ -317,7 +317,8 @@ int qmlg_solve(double *A, int n, int64_t lda, const double *y, double *x, double
  * work: the qmlg_cholesky_mixed factorisation, one solve and exactly
  * refine_steps double-double refinement steps, with no host synchronisation and
  * no host decision.  Results stay on the device: d_status[0] = Cholesky info
- * (0 = ok), d_status[1] = tensor-core wait flags; d_correction (optional, 2
+ * (0 = ok), d_status[1] = bounded-wait flags (bit 1: a tensor-core pipeline
+ * wait, bit 2: a triangular-solve wait gave up); d_correction (optional, 2
  * doubles) = |dx|^2 and |x|^2 of the last step.  The column-major upper
  * triangle of A receives the factor as in qmlg_cholesky.
  */

@@ -614,90 +614,144 @@ __device__ __forceinline__ double gemv64_col(const double *__restrict__ M, int64
     return s;
 }
 
-// Forward solve with the block inverses: step kb, CTA 0 forms
-// b = x_kb - L[kb, kb-1] z_{kb-1} and z_kb = L_kk^{-1} b; the other CTAs apply z_{kb-1}
-// to every row below block kb.
-__global__ void __launch_bounds__(TRSV_THREADS)
-trsv_fwd_inv_kernel(const double *__restrict__ A, int64_t lda, int n,
-                    const double *__restrict__ Linv, double *__restrict__ x)
+// Flag-driven triangular solves with the block inverses, one cooperative launch per
+// direction and no grid-wide barrier.  CTA b owns row blocks b, b + grid, ... in
+// solve order.  For its block i it applies every finished block k (forward: k < i,
+// L[i][k] z_k; backward: k > i, L[k][i]^T x_k) as soon as k's ready flag is set,
+// then applies the diagonal-block inverse and publishes block i (stores, fence,
+// release flag).  All CTAs are resident (cooperative launch) and each takes its
+// blocks in solve order, so the lowest unfinished block always has its inputs and
+// every wait ends; a wait is still bounded: after kFlagWaitLimit polls the CTA sets
+// bit 2 of *err and returns, and the CTAs that wait on it follow.  Solved values
+// are read with ld.global.cg (L2), never through a possibly stale L1 line.
+
+constexpr int kFlagWaitLimit = 1 << 21;
+
+__device__ __forceinline__ int ld_acquire(const int *p)
 {
-    cg::grid_group grid = cg::this_grid();
-    __shared__ double zp[NB];
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release(int *p, int v)
+{
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ bool wait_flag(const int *p)
+{
+    for (int it = 0; it < kFlagWaitLimit; ++it) {
+        if (ld_acquire(p) != 0) return true;
+        __nanosleep(64);
+    }
+    return false;
+}
+
+// Publishes a solved block: every thread's stores are fenced before the flag.
+__device__ __forceinline__ void publish_block(int *flag)
+{
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) st_release(flag, 1);
+}
+
+__global__ void __launch_bounds__(TRSV_THREADS)
+trsv_fwd_flag_kernel(const double *__restrict__ A, int64_t lda, int n,
+                     const double *__restrict__ Linv, double *x, int *flags, int *err)
+{
     __shared__ double bb[NB];
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    constexpr int nw = TRSV_THREADS / 32;
+    __shared__ int ready;
+    const int tid = threadIdx.x, r = tid >> 2, q = tid & 3;
     const int nblk = (n + NB - 1) / NB;
-    for (int kb = 0; kb < nblk; ++kb) {
-        const int k0 = kb * NB, nb = min(NB, n - k0), kp = k0 - NB;
-        if (kb > 0) {
-            if (tid < NB) zp[tid] = x[kp + tid];
-            __syncthreads();
-        }
-        if (blockIdx.x == 0) {
-            double s = 0.0;
-            if (kb > 0) s = gemv64_row(A + (int64_t)k0 * lda + kp, lda, zp, tid, nb);
-            if ((tid & 3) == 0) {
-                const int r = tid >> 2;
-                bb[r] = r < nb ? x[k0 + r] - s : 0.0;
+    for (int i = blockIdx.x; i < nblk; i += gridDim.x) {
+        const int i0 = i * NB, nb = min(NB, n - i0);
+        const bool live = r < nb;
+        const double *arow = A + (int64_t)(i0 + (live ? r : 0)) * lda + q;
+        double s = 0.0;
+        int k = 0;
+        while (k < i) {
+            if (tid == 0) {
+                int kk = k;
+                if (!wait_flag(flags + kk)) {
+                    atomicOr(err, 2);
+                    kk = -1;
+                } else {
+                    ++kk;
+                    while (kk < i && ld_acquire(flags + kk) != 0) ++kk;
+                }
+                ready = kk;
             }
             __syncthreads();
-            const double z = gemv64_row(Linv + (int64_t)kb * NB * NB, NB, bb, tid, NB);
-            if ((tid & 3) == 0 && (tid >> 2) < nb) x[k0 + (tid >> 2)] = z;
-        } else if (kb > 0) {
-            const int tw = (gridDim.x - 1) * nw;
-            for (int r = k0 + NB + (blockIdx.x - 1) * nw + warp; r < n; r += tw) {
-                const double *row = A + (int64_t)r * lda + kp;
-                double sum = fma(row[lane], zp[lane], row[lane + 32] * zp[lane + 32]);
-                for (int off = 16; off > 0; off >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, off);
-                if (lane == 0) x[r] -= sum;
-            }
+            const int kend = ready;
+            __syncthreads();
+            if (kend < 0) return;
+            if (live)
+                for (; k < kend; ++k) {
+                    const double *lp = arow + k * NB;
+                    const double *zp = x + k * NB + q;
+#pragma unroll
+                    for (int c = 0; c < 16; ++c) s = fma(lp[4 * c], __ldcg(zp + 4 * c), s);
+                }
+            k = kend;
         }
-        grid.sync();
+        s += __shfl_xor_sync(0xffffffffu, s, 1);
+        s += __shfl_xor_sync(0xffffffffu, s, 2);
+        if (q == 0) bb[r] = live ? x[i0 + r] - s : 0.0;
+        __syncthreads();
+        const double z = gemv64_row(Linv + (int64_t)i * NB * NB, NB, bb, tid, NB);
+        if (q == 0 && live) x[i0 + r] = z;
+        publish_block(flags + i);
     }
 }
 
-// Backward solve L^T x = z with the block inverses (transposed products).
 __global__ void __launch_bounds__(TRSV_THREADS)
-trsv_bwd_inv_kernel(const double *__restrict__ A, int64_t lda, int n,
-                    const double *__restrict__ Linv, double *__restrict__ x)
+trsv_bwd_flag_kernel(const double *__restrict__ A, int64_t lda, int n,
+                     const double *__restrict__ Linv, double *x, int *flags, int *err)
 {
-    cg::grid_group grid = cg::this_grid();
-    __shared__ double zp[NB];
     __shared__ double bb[NB];
-    const int tid = threadIdx.x;
+    __shared__ int ready;
+    const int tid = threadIdx.x, t = tid >> 2, q = tid & 3;
     const int nblk = (n + NB - 1) / NB;
-    for (int kb = nblk - 1; kb >= 0; --kb) {
-        const int k0 = kb * NB, nb = min(NB, n - k0), kn = k0 + NB;
-        const int nbn = kb < nblk - 1 ? min(NB, n - kn) : 0;
-        if (nbn > 0) {
-            if (tid < NB) zp[tid] = tid < nbn ? x[kn + tid] : 0.0;
-            __syncthreads();
-        }
-        if (blockIdx.x == 0) {
-            double s = 0.0;
-            // a full next block goes through gemv64_col; a short last block (rows
-            // beyond n do not exist) is summed directly by one thread per column
-            if (nbn == NB) s = gemv64_col(A + (int64_t)kn * lda + k0, lda, zp, tid);
-            else if (nbn > 0 && (tid & 3) == 0) {
-                const int t = tid >> 2;
-                for (int r = 0; r < nbn; ++r) s = fma(A[(int64_t)(kn + r) * lda + k0 + t], zp[r], s);
-            }
-            if ((tid & 3) == 0) {
-                const int t = tid >> 2;
-                bb[t] = t < nb ? x[k0 + t] - s : 0.0;
+    for (int j = blockIdx.x; j < nblk; j += gridDim.x) {
+        const int i = nblk - 1 - j;
+        const int i0 = i * NB, nb = min(NB, n - i0);
+        double s = 0.0;
+        int k = nblk - 1;
+        while (k > i) {
+            if (tid == 0) {
+                int kk = k;
+                if (!wait_flag(flags + kk)) {
+                    atomicOr(err, 2);
+                    kk = -2;
+                } else {
+                    --kk;
+                    while (kk > i && ld_acquire(flags + kk) != 0) --kk;
+                }
+                ready = kk;
             }
             __syncthreads();
-            const double v = gemv64_col(Linv + (int64_t)kb * NB * NB, NB, bb, tid);
-            if ((tid & 3) == 0 && (tid >> 2) < nb) x[k0 + (tid >> 2)] = v;
-        } else if (nbn > 0) {
-            const int tt = (gridDim.x - 1) * TRSV_THREADS;
-            for (int t = (blockIdx.x - 1) * TRSV_THREADS + tid; t < k0; t += tt) {
-                double sum = 0.0;
-                for (int r = 0; r < nbn; ++r) sum = fma(A[(int64_t)(kn + r) * lda + t], zp[r], sum);
-                x[t] -= sum;
+            const int kend = ready;
+            __syncthreads();
+            if (kend == -2) return;
+            // i < nblk - 1 here, so block i is full and columns i0 + t exist
+            for (; k > kend; --k) {
+                const int k0 = k * NB, nbk = min(NB, n - k0);
+#pragma unroll
+                for (int c = 0; c < 16; ++c) {
+                    const int rr = q + 4 * c;
+                    if (rr < nbk)
+                        s = fma(A[(int64_t)(k0 + rr) * lda + i0 + t], __ldcg(x + k0 + rr), s);
+                }
             }
         }
-        grid.sync();
+        s += __shfl_xor_sync(0xffffffffu, s, 1);
+        s += __shfl_xor_sync(0xffffffffu, s, 2);
+        if (q == 0) bb[t] = t < nb ? x[i0 + t] - s : 0.0;
+        __syncthreads();
+        const double v = gemv64_col(Linv + (int64_t)i * NB * NB, NB, bb, tid);
+        if (q == 0 && t < nb) x[i0 + t] = v;
+        publish_block(flags + i);
     }
 }
 
@@ -804,16 +858,22 @@ int trsv_grid(int &grid)
         if (e == cudaSuccess)
             e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trsv_fwd_coop_kernel,
                                                               TRSV_THREADS, 0);
-        int per_sm2 = 0;
+        int per_sm2 = 0, per_sm3 = 0, per_sm4 = 0;
         if (e == cudaSuccess)
             e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, trsv_bwd_coop_kernel,
+                                                              TRSV_THREADS, 0);
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm3, trsv_fwd_flag_kernel,
+                                                              TRSV_THREADS, 0);
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm4, trsv_bwd_flag_kernel,
                                                               TRSV_THREADS, 0);
         if (e != cudaSuccess) {
             status = qmlg::set_cuda_error(e);
             return;
         }
         // one CTA per SM: enough for the memory-bound updates, cheaper grid barriers
-        cached = std::min(per_sm, per_sm2) >= 1 ? sms : 0;
+        cached = std::min(std::min(per_sm, per_sm2), std::min(per_sm3, per_sm4)) >= 1 ? sms : 0;
         if (cached < 2) status = QMLG_E_CUDA;
     });
     grid = cached;
@@ -909,6 +969,7 @@ size_t emulated_factor_ws(int n)
     p.add<int>(rpad);
     p.add<int>(4);                                             // device error flag
     p.add<double>((size_t)ceil_div(n < 1 ? 1 : n, NB) * NB * NB);  // diagonal-block inverses
+    p.add<int>((size_t)2 * ceil_div(n < 1 ? 1 : n, NB));           // triangular-solve flags
     return p.total();
 }
 
@@ -980,8 +1041,9 @@ int emulated_factor(double *A, int n, int64_t lda, double shift, Workspace &ws, 
     int *exp_in = ws.take<int>((size_t)rpad);
     int *d_err = ws.take<int>(4);
     double *linv = ws.take<double>((size_t)ceil_div(n, NB) * NB * NB);
+    int *flags = ws.take<int>((size_t)2 * ceil_div(n, NB));
     if (dig_out == nullptr || exp_out == nullptr || dig_in == nullptr || exp_in == nullptr ||
-        d_err == nullptr || linv == nullptr)
+        d_err == nullptr || linv == nullptr || flags == nullptr)
         return QMLG_E_WORKSPACE;
     cudaError_t e = cudaMemsetAsync(d_err, 0, sizeof(int), s);
     if (e != cudaSuccess) return set_cuda_error(e);
@@ -1041,6 +1103,7 @@ int emulated_factor(double *A, int n, int64_t lda, double shift, Workspace &ws, 
     f.slices = slices;
     f.d_err = d_err;
     f.Linv = linv;
+    f.flags = flags;
     return check_launch();
 }
 
@@ -1067,10 +1130,17 @@ int emulated_potrs(const EmulatedFactor &f, double *x, cudaStream_t s)
         { trsv_single_cta_kernel<<<1, TRSV1_THREADS, 0, s>>>(A, lda, n, Linv, x); count_launches(1); }
         return check_launch();
     }
-    void *args[] = {(void *)&A, (void *)&lda, (void *)&n, (void *)&Linv, (void *)&x};
-    st = launch_cooperative((const void *)trsv_fwd_inv_kernel, grid, TRSV_THREADS, args, s);
+    const int nblk = (int)ceil_div(n, NB);
+    cudaError_t e = cudaMemsetAsync(f.flags, 0, sizeof(int) * 2 * (size_t)nblk, s);
+    if (e != cudaSuccess) return set_cuda_error(e);
+    int *fwd_flags = f.flags, *bwd_flags = f.flags + nblk, *err = f.d_err;
+    void *fa[] = {(void *)&A, (void *)&lda, (void *)&n, (void *)&Linv, (void *)&x,
+                  (void *)&fwd_flags, (void *)&err};
+    void *ba[] = {(void *)&A, (void *)&lda, (void *)&n, (void *)&Linv, (void *)&x,
+                  (void *)&bwd_flags, (void *)&err};
+    st = launch_cooperative((const void *)trsv_fwd_flag_kernel, grid, TRSV_THREADS, fa, s);
     if (st == QMLG_OK)
-        st = launch_cooperative((const void *)trsv_bwd_inv_kernel, grid, TRSV_THREADS, args, s);
+        st = launch_cooperative((const void *)trsv_bwd_flag_kernel, grid, TRSV_THREADS, ba, s);
     return st;
 }
 
@@ -1301,6 +1371,7 @@ extern "C" int qmlg_solve(double *A, int n, int64_t lda, const double *y, double
             c.ws_mark = ws.used;
             st = refine(c, o, [&](double *v) { return qmlg::emulated_potrs(f, v, s); }, rep, stalled);
             if (st != QMLG_OK) return st;
+            if ((st = qmlg::read_device_flag(f.d_err, s)) != QMLG_OK) return st;
         }
         if ((info != 0 || stalled) && o.allow_fallback) {
             rep.fell_back = 1;
@@ -1371,7 +1442,6 @@ extern "C" int qmlg_solve_async(double *A, int n, int64_t lda, const double *y, 
     qmlg::EmulatedFactor f;
     int st = qmlg::emulated_factor(A, n, lda, lambda, ws, d_status, f, s);
     if (st != QMLG_OK) return st;
-    { or_flag_kernel<<<1, 1, 0, s>>>(d_status + 1, f.d_err); qmlg::count_launches(1); }
     e = cudaMemcpyAsync(x, y, sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice, s);
     if (e != cudaSuccess) return qmlg::set_cuda_error(e);
     if ((st = qmlg::emulated_potrs(f, x, s)) != QMLG_OK) return st;
@@ -1384,6 +1454,8 @@ extern "C" int qmlg_solve_async(double *A, int n, int64_t lda, const double *y, 
         if (e != cudaSuccess) return qmlg::set_cuda_error(e);
         { axpy_norms_kernel<<<(int)qmlg::ceil_div(n, 256), 256, 0, s>>>(x, r, n, d_sums); qmlg::count_launches(1); }
     }
+    // tensor-core and triangular-solve waits that gave up
+    { or_flag_kernel<<<1, 1, 0, s>>>(d_status + 1, f.d_err); qmlg::count_launches(1); }
     if (d_correction != nullptr && refine_steps > 0) {
         e = cudaMemcpyAsync(d_correction, d_sums, 2 * sizeof(double), cudaMemcpyDeviceToDevice, s);
         if (e != cudaSuccess) return qmlg::set_cuda_error(e);

@@ -48,6 +48,7 @@ struct EmulatedFactor {
     int slices = 0;
     int *d_err = nullptr;  // device flag: a bounded tensor-core wait gave up
     const double *Linv = nullptr;  // [n/64][64][64] inverses of the diagonal blocks
+    int *flags = nullptr;          // [2][n/64] ready flags of the triangular solves
 };
 
 size_t emulated_factor_ws(int n);
