@@ -14,10 +14,11 @@
 // Exactness: a level sums at most 8 * (64*kchunks) * 4096 products, so kchunks <= 8
 // keeps every partial sum below 2^24.
 //
-// Warp roles (192 threads): warp 0 issues TMA loads, warp 1 owns TMEM and issues
-// the MMAs from one thread, warps 2-5 (one per TMEM lane quarter) run the epilogue:
-// the levels are merged in 64-bit integers, converted once to FP64, scaled by
-// 2^(e_i + e_j) and subtracted from C.  Waits are bounded; a timeout sets *err.
+// Warp roles (320 threads): warp 0 issues TMA loads, warp 1 owns TMEM and issues
+// the MMAs from one thread, warps 2-9 run the epilogue, two per TMEM lane quarter
+// (one per half of the 64 columns, so each scheduler interleaves two epilogue
+// warps): the levels are merged in 64-bit integers, converted once to FP64, scaled
+// by 2^(e_i + e_j) and subtracted from C.  Waits are bounded; a timeout sets *err.
 #include <cuda.h>
 
 #include <algorithm>
@@ -37,6 +38,9 @@ constexpr int TM = 128;         // TMEM lanes per tile (j)
 constexpr int TN = 64;          // columns per level (i)
 constexpr int KC = 64;          // K chunk: one 128-byte swizzled row of bf16
 constexpr int S_MAX = 8;
+constexpr int THREADS = 320;    // 2 producer warps + 8 epilogue warps
+constexpr int EPI_THREADS = 256;
+constexpr int EG = 8;           // columns per epilogue step
 constexpr int A_STAGES = 5;
 constexpr int A_BYTES = TM * KC * 2;  // 16 KB
 constexpr int B_BYTES = TN * KC * 2;  // 8 KB
@@ -101,7 +105,7 @@ __device__ __forceinline__ double pow2i(int e)
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(192, 1)
+__global__ void __launch_bounds__(THREADS, 1)
 emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
               TileArgs p)
 {
@@ -129,7 +133,7 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
             mbar_init(&aEmpty[k], 1);
         }
         mbar_init(tFull, 1);
-        mbar_init(tEmpty, 128);
+        mbar_init(tEmpty, EPI_THREADS);
         fence_barrier_init();
     }
     if (warp == 0 && lane == 0) {
@@ -249,8 +253,9 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
             if (!ok) atomicOr(p.err, 2);
         }
     } else {
-        // ---------------- epilogue: warps 2..5 -> TMEM lane quarters 2,3,0,1
-        const int q = warp & 3;
+        // ---------------- epilogue: warps 2..9 -> TMEM lane quarter q = warp & 3,
+        // columns 32h .. 32h+31 of each level with h = (warp - 2) / 4
+        const int q = warp & 3, h = (warp - 2) >> 2;
         const int jl = q * 32 + lane;
         const int H = (S + 1) / 2;
         const int lo_levels = S - H;
@@ -265,12 +270,15 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
             const int j0 = p.jbase + jt * TM, i0 = p.ibase + itl * TN;
             const int arow = p.a_row0 + jt * TM, brow = p.b_row0 + itl * TN;
             const int j = j0 + jl;
+            // every (j, i) of the tile is inside the updated range
+            const bool interior = j0 + TM <= p.jend && i0 + TN <= p.iend &&
+                                  (!p.lower || j0 + TM - 1 <= i0);
             if (MODE == kSyrk && j < p.jend) {
-                // while the MMAs run, pull this thread's column of C into L2 so the
+                // while the MMAs run, pull this thread's part of C into L2 so the
                 // read-modify-write below does not wait on DRAM
-                const int ilim = min(i0 + TN, p.iend);
-                for (int i = i0; i < ilim; ++i)
-                    if (!p.lower || j <= i)
+                const int ilo = i0 + h * 32, ilim = min(ilo + 32, p.iend);
+                for (int i = ilo; i < ilim; ++i)
+                    if (interior || !p.lower || j <= i)
                         asm volatile("prefetch.global.L2 [%0];" ::"l"(p.C + (int64_t)i * p.ldc + j));
             }
             if (ok && !mbar_wait(tFull, u & 1)) {
@@ -285,54 +293,69 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
                 aj = p.scale * p.normA[arow + jl];
                 if (MODE == kPredict) aw = p.alpha[j];
             }
-            for (int gq = 0; gq < TN / 16; ++gq) {
-                uint32_t v[S_MAX][16];
+            for (int gq = 0; gq < 32 / EG; ++gq) {
+                const int cb = h * 32 + gq * EG;  // first column of this step in the tile
+                uint32_t v[S_MAX][EG];
 #pragma unroll
                 for (int l = 0; l < S_MAX; ++l)
-                    if (l < S) tmem_ld16(lane_base + (uint32_t)(l * TN + gq * 16), v[l]);
+                    if (l < S) tmem_ld8(lane_base + (uint32_t)(l * TN + cb), v[l]);
                 tmem_ld_wait();
-                if (gq == TN / 16 - 1) {
-                    // every level of this tile is in registers: hand TMEM back
+                if (gq == 32 / EG - 1) {
+                    // every level of this warp's columns is in registers: release TMEM
                     fence_before_sync();
                     mbar_arrive(tEmpty);
                 }
                 if (!ok) continue;
-                long long v64[16];
+                long long v64[EG];
+                if (S == 8) {
+                    // K <= 512 bounds level l by (l+1) 2^21, so two adjacent levels
+                    // combine exactly in 32 bits (d6 * 128 + d7 < 1.9e9)
 #pragma unroll
-                for (int col = 0; col < 16; ++col) {
-                    long long hi = 0, lo = 0;
+                    for (int col = 0; col < EG; ++col) {
+                        int d[8];
 #pragma unroll
-                    for (int l = 0; l < S_MAX; ++l) {
-                        if (l >= S) break;
-                        const long long d = (long long)__float2int_rn(__uint_as_float(v[l][col]));
-                        if (l < H) hi = hi * 128 + d;
-                        else lo = lo * 128 + d;
+                        for (int l = 0; l < 8; ++l) d[l] = __float2int_rn(__uint_as_float(v[l][col]));
+                        const long long hi = (long long)(d[0] * 128 + d[1]) * 16384 + (d[2] * 128 + d[3]);
+                        const long long lo = (long long)(d[4] * 128 + d[5]) * 16384 + (d[6] * 128 + d[7]);
+                        v64[col] = (hi << (28 - 12)) + (lo >> 12);
                     }
-                    // value = hi * 128^lo_levels + lo, kept in 62 bits by dropping the
-                    // lowest `shift` bits of lo (far below FP64 resolution of the value)
-                    v64[col] = (hi << (7 * lo_levels - shift)) + (lo >> shift);
+                } else {
+#pragma unroll
+                    for (int col = 0; col < EG; ++col) {
+                        long long hi = 0, lo = 0;
+#pragma unroll
+                        for (int l = 0; l < S_MAX; ++l) {
+                            if (l >= S) break;
+                            const long long d = (long long)__float2int_rn(__uint_as_float(v[l][col]));
+                            if (l < H) hi = hi * 128 + d;
+                            else lo = lo * 128 + d;
+                        }
+                        // value = hi * 128^lo_levels + lo, kept in 62 bits by dropping the
+                        // lowest `shift` bits of lo (far below FP64 resolution of the value)
+                        v64[col] = (hi << (7 * lo_levels - shift)) + (lo >> shift);
+                    }
                 }
                 if (MODE == kSyrk) {
-                    double cv[16];
+                    double cv[EG];
 #pragma unroll
-                    for (int col = 0; col < 16; ++col) {
-                        const int i = i0 + gq * 16 + col;
-                        cv[col] = (jvalid && i < p.iend && (!p.lower || j <= i))
+                    for (int col = 0; col < EG; ++col) {
+                        const int i = i0 + cb + col;
+                        cv[col] = (interior || (jvalid && i < p.iend && (!p.lower || j <= i)))
                                       ? p.C[(int64_t)i * p.ldc + j] : 0.0;
                     }
 #pragma unroll
-                    for (int col = 0; col < 16; ++col) {
-                        const int il = gq * 16 + col;
+                    for (int col = 0; col < EG; ++col) {
+                        const int il = cb + col;
                         const int i = i0 + il;
-                        if (jvalid && i < p.iend && (!p.lower || j <= i)) {
+                        if (interior || (jvalid && i < p.iend && (!p.lower || j <= i))) {
                             const double sc = pow2i(p.expB[brow + il] + ej + shift - 7 * (S + 1));
                             p.C[(int64_t)i * p.ldc + j] = fma(-(double)v64[col], sc, cv[col]);
                         }
                     }
                 } else {
 #pragma unroll
-                    for (int col = 0; col < 16; ++col) {
-                        const int il = gq * 16 + col;
+                    for (int col = 0; col < EG; ++col) {
+                        const int il = cb + col;
                         const int i = i0 + il;
                         const bool valid = jvalid && i < p.iend;
                         double kv = 0.0;
@@ -359,13 +382,13 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
                 }
             }
             if (MODE == kPredict) {
-                // the four epilogue warps add their column sums in a fixed order
-                asm volatile("bar.sync 1, 128;" ::: "memory");
+                // the four quarters' column sums are added in a fixed order
+                asm volatile("bar.sync 1, 256;" ::: "memory");
                 const int tt = threadIdx.x - 64;
                 if (ok && tt < TN && i0 + tt < p.iend)
                     p.partial[(int64_t)jt * (p.iend - p.ibase) + (i0 - p.ibase) + tt] =
                         ((red[0][tt] + red[1][tt]) + red[2][tt]) + red[3][tt];
-                asm volatile("bar.sync 1, 128;" ::: "memory");
+                asm volatile("bar.sync 1, 256;" ::: "memory");
             }
         }
     }
@@ -640,7 +663,7 @@ int emu_tc_update(double *C, int64_t ldc, int jbase, int jend, int ibase, int ie
     int grid = tile_grid(a.ntiles);
     if (max_ctas > 0) grid = std::min(a.ntiles, max_ctas);
     if (max_ctas < 0) grid = a.ntiles;
-    emu_tc_kernel<kSyrk><<<grid, 192, SMEM_BYTES, s>>>(mA, mB, a);
+    emu_tc_kernel<kSyrk><<<grid, THREADS, SMEM_BYTES, s>>>(mA, mB, a);
     count_launches(1);
     return check_launch();
 }
@@ -760,9 +783,9 @@ int launch_gauss(int mode, const GaussBufs &b, int na, int nb, int d, int S, dou
     a.partial = b.partial;
     const int grid = tile_grid(a.ntiles);
     if (mode == kKernelMatrix)
-        emu_tc_kernel<kKernelMatrix><<<grid, 192, SMEM_BYTES, s>>>(mA, mB, a);
+        emu_tc_kernel<kKernelMatrix><<<grid, THREADS, SMEM_BYTES, s>>>(mA, mB, a);
     else
-        emu_tc_kernel<kPredict><<<grid, 192, SMEM_BYTES, s>>>(mA, mB, a);
+        emu_tc_kernel<kPredict><<<grid, THREADS, SMEM_BYTES, s>>>(mA, mB, a);
     qmlg::count_launches(1);
     st = qmlg::check_launch();
     if (st == QMLG_OK && mode == kPredict) {
@@ -967,7 +990,7 @@ extern "C" int qmlg_predict_emulated_async(const double *Xtrain, int64_t ldtrain
     a.scale = -0.5 / (sigma * sigma);
     a.alpha = alpha;
     a.partial = b.partial;
-    emu_tc_kernel<kPredict><<<tile_grid(a.ntiles), 192, SMEM_BYTES, s>>>(mA, mB, a);
+    emu_tc_kernel<kPredict><<<tile_grid(a.ntiles), THREADS, SMEM_BYTES, s>>>(mA, mB, a);
     reduce_partial_rows_kernel<<<(int)qmlg::ceil_div(ntest, 256), 256, 0, s>>>(
         b.partial, (int)qmlg::ceil_div(ntrain, TM), ntest, yhat);
     qmlg::count_launches(2);
@@ -1031,7 +1054,7 @@ extern "C" int qmlg_gaussian_kernel_emulated_async(const double *A, int64_t lda,
     a.normB = b.nB;
     a.scale = -0.5 / (sigma * sigma);
     a.diag_shift = diag_shift;
-    emu_tc_kernel<kKernelMatrix><<<tile_grid(a.ntiles), 192, SMEM_BYTES, s>>>(mA, mB, a);
+    emu_tc_kernel<kKernelMatrix><<<tile_grid(a.ntiles), THREADS, SMEM_BYTES, s>>>(mA, mB, a);
     qmlg::count_launches(1);
     return qmlg::check_launch();
 }
