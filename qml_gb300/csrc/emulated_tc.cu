@@ -293,20 +293,9 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
                 aj = p.scale * p.normA[arow + jl];
                 if (MODE == kPredict) aw = p.alpha[j];
             }
-            for (int gq = 0; gq < 32 / EG; ++gq) {
-                const int cb = h * 32 + gq * EG;  // first column of this step in the tile
-                uint32_t v[S_MAX][EG];
-#pragma unroll
-                for (int l = 0; l < S_MAX; ++l)
-                    if (l < S) tmem_ld8(lane_base + (uint32_t)(l * TN + cb), v[l]);
-                tmem_ld_wait();
-                if (gq == 32 / EG - 1) {
-                    // every level of this warp's columns is in registers: release TMEM
-                    fence_before_sync();
-                    mbar_arrive(tEmpty);
-                }
-                if (!ok) continue;
-                long long v64[EG];
+            // Levels of eight columns -> exact integers (value in units of 2^(shift -
+            // 7(S+1)) relative to the row scales).
+            auto merge8 = [&](const uint32_t (&v)[S_MAX][EG], long long *out) {
                 if (S == 8) {
                     // K <= 512 bounds level l by (l+1) 2^21, so two adjacent levels
                     // combine exactly in 32 bits (d6 * 128 + d7 < 1.9e9)
@@ -317,7 +306,7 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
                         for (int l = 0; l < 8; ++l) d[l] = __float2int_rn(__uint_as_float(v[l][col]));
                         const long long hi = (long long)(d[0] * 128 + d[1]) * 16384 + (d[2] * 128 + d[3]);
                         const long long lo = (long long)(d[4] * 128 + d[5]) * 16384 + (d[6] * 128 + d[7]);
-                        v64[col] = (hi << (28 - 12)) + (lo >> 12);
+                        out[col] = (hi << (28 - 12)) + (lo >> 12);
                     }
                 } else {
 #pragma unroll
@@ -332,27 +321,64 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
                         }
                         // value = hi * 128^lo_levels + lo, kept in 62 bits by dropping the
                         // lowest `shift` bits of lo (far below FP64 resolution of the value)
-                        v64[col] = (hi << (7 * lo_levels - shift)) + (lo >> shift);
+                        out[col] = (hi << (7 * lo_levels - shift)) + (lo >> shift);
                     }
                 }
-                if (MODE == kSyrk) {
-                    double cv[EG];
+            };
+            if (MODE == kSyrk) {
+                // (1) merge all 32 of this warp's columns, then hand TMEM back, so the
+                // next tile's MMAs overlap (2), the read-modify-write of C
+                long long v64[32];
 #pragma unroll
-                    for (int col = 0; col < EG; ++col) {
-                        const int i = i0 + cb + col;
-                        cv[col] = (interior || (jvalid && i < p.iend && (!p.lower || j <= i)))
-                                      ? p.C[(int64_t)i * p.ldc + j] : 0.0;
-                    }
+                for (int gq = 0; gq < 32 / EG; ++gq) {
+                    uint32_t v[S_MAX][EG];
 #pragma unroll
-                    for (int col = 0; col < EG; ++col) {
-                        const int il = cb + col;
-                        const int i = i0 + il;
-                        if (interior || (jvalid && i < p.iend && (!p.lower || j <= i))) {
-                            const double sc = pow2i(p.expB[brow + il] + ej + shift - 7 * (S + 1));
-                            p.C[(int64_t)i * p.ldc + j] = fma(-(double)v64[col], sc, cv[col]);
+                    for (int l = 0; l < S_MAX; ++l)
+                        if (l < S) tmem_ld8(lane_base + (uint32_t)(l * TN + h * 32 + gq * EG), v[l]);
+                    tmem_ld_wait();
+                    merge8(v, v64 + gq * EG);
+                }
+                fence_before_sync();
+                mbar_arrive(tEmpty);
+                if (ok) {
+#pragma unroll
+                    for (int gq = 0; gq < 32 / EG; ++gq) {
+                        const int cb = h * 32 + gq * EG;
+                        double cv[EG];
+#pragma unroll
+                        for (int col = 0; col < EG; ++col) {
+                            const int i = i0 + cb + col;
+                            cv[col] = (interior || (jvalid && i < p.iend && (!p.lower || j <= i)))
+                                          ? p.C[(int64_t)i * p.ldc + j] : 0.0;
+                        }
+#pragma unroll
+                        for (int col = 0; col < EG; ++col) {
+                            const int il = cb + col;
+                            const int i = i0 + il;
+                            if (interior || (jvalid && i < p.iend && (!p.lower || j <= i))) {
+                                const double sc = pow2i(p.expB[brow + il] + ej + shift - 7 * (S + 1));
+                                p.C[(int64_t)i * p.ldc + j] = fma(-(double)v64[gq * EG + col], sc, cv[col]);
+                            }
                         }
                     }
-                } else {
+                }
+            } else {
+                // Gaussian epilogues: the FP64 exp dominates; eight columns at a time,
+                // TMEM released once the last eight are in registers
+                for (int gq = 0; gq < 32 / EG; ++gq) {
+                    const int cb = h * 32 + gq * EG;
+                    uint32_t v[S_MAX][EG];
+#pragma unroll
+                    for (int l = 0; l < S_MAX; ++l)
+                        if (l < S) tmem_ld8(lane_base + (uint32_t)(l * TN + cb), v[l]);
+                    tmem_ld_wait();
+                    if (gq == 32 / EG - 1) {
+                        fence_before_sync();
+                        mbar_arrive(tEmpty);
+                    }
+                    if (!ok) continue;
+                    long long v64[EG];
+                    merge8(v, v64);
 #pragma unroll
                     for (int col = 0; col < EG; ++col) {
                         const int il = cb + col;
