@@ -32,21 +32,30 @@ constexpr int NB = 64;
 
 // ---------------------------------------------------------------- factor --
 
-// 1/sqrt(p) for a positive finite double, without FP64 sqrt or division (each
-// costs ~650 cycles on this GPU against 64 for an FMA): an FP32 rsqrtf gives ~23
-// bits and one Halley step (cubic convergence for f(y) = 1/y^2 - p) brings it to
-// full FP64 precision:  e = 1 - p y^2,  y <- y + y e (1/2 + 3/8 e).  Outside
-// [2^-120, 2^120] p is first scaled by an even power of two into [1, 4).
+// 1/sqrt(p) for a positive finite double, with as few FP64 instructions as possible
+// (on this GPU each costs ~64 cycles of the FP64 pipe; sqrt and division ~650): an
+// FP32 rsqrtf of p's leading bits gives ~23 bits, and one Halley step (cubic
+// convergence for f(y) = 1/y^2 - p) brings it to full FP64 precision:
+//   e = 1 - p y^2,  y <- y + y e (1/2 + 3/8 e).
+// The FP32 <-> FP64 moves are done on the bits.  Outside [2^-120, 2^120] p is first
+// scaled by an even power of two into [1, 4).
 __device__ __forceinline__ double rsqrt_halley(double p)
 {
     double q = p;
     int h = 0;
-    if (!(p >= 0x1p-120 && p <= 0x1p120)) {
+    const int ed = (int)((unsigned long long)__double_as_longlong(p) >> 52);
+    if (ed < 1023 - 120 || ed > 1023 + 120) {
         const int ex = ilogb(p) & ~1;
         q = scalbn(p, -ex);
         h = -ex / 2;
     }
-    double y = (double)rsqrtf((float)q);
+    const unsigned long long qb = (unsigned long long)__double_as_longlong(q);
+    // q truncated to FP32: exponent rebiased from 1023 to 127, top 23 mantissa bits
+    const uint32_t fb = (uint32_t)(((qb >> 52) - 896ull) << 23) | (uint32_t)((qb >> 29) & 0x7fffffull);
+    const uint32_t yb = __float_as_uint(rsqrtf(__uint_as_float(fb)));
+    // the FP32 estimate (a normal positive float) as an exact double
+    double y = __longlong_as_double((long long)((((unsigned long long)(yb >> 23) + 896ull) << 52) |
+                                                ((unsigned long long)(yb & 0x7fffffu) << 29)));
     const double e = fma(-q * y, y, 1.0);
     y = fma(y * e, fma(0.375, e, 0.5), y);
     return h != 0 ? scalbn(y, h) : y;
@@ -56,17 +65,22 @@ __device__ __forceinline__ double rsqrt_halley(double p)
 __host__ __device__ constexpr int tri_prefix(int c) { return (NB - 1 - c) * (NB - c) / 2; }
 
 constexpr int POTRF_THREADS = 256;
-constexpr int POTRF_WORKERS = 224;  // warps 0-6 update; lane 0 of warp 7 takes the pivots
-constexpr int POTRF_PIVOT = POTRF_WORKERS;
+// Warps 0-2 and 4-6 update; lane 0 of warp 3 takes the pivots, alone on its
+// scheduler's FP64 pipe (warp 7 only joins the barriers).
+constexpr int POTRF_WORKERS = 192;
+constexpr int POTRF_PIVOT = 96;
+constexpr int POTRF_BATCH = 3;  // elements whose loads are issued before their FMAs
 
-// Pivot of column c: S_cc <- sqrt(S_cc), rd[c] <- 1/sqrt(S_cc) (> 0), rd2[c] <-
-// 1/S_cc.  When S_cc is not positive and finite, rd[c] <- 0 marks the failure and
-// the failing column is recorded in info.
+// Pivot of column c: rd[c] <- 1/sqrt(S_cc) (> 0), rd2[c] <- 1/S_cc; S_cc keeps the
+// pivot (the factor's diagonal sqrt(S_cc) = S_cc rd[c] is formed at write-back).
+// When S_cc is not positive and finite, rd[c] <- 0 marks the failure and the failing
+// column is recorded in info.  The checks are on the bits (no FP64 compares).
 __device__ __forceinline__ void potrf_pivot(double (*S)[NB + 1], double *rd, double *rd2, int c,
                                             int k0, int nb, int *info)
 {
     const double p = S[c][c];
-    if (!(p > 0.0) || !isfinite(p)) {
+    const long long b = __double_as_longlong(p);
+    if (b <= 0 || ((unsigned long long)b >> 52) >= 0x7ffull) {
         if (c < nb) atomicCAS(info, 0, k0 + c + 1);
         rd[c] = 0.0;
         return;
@@ -74,7 +88,6 @@ __device__ __forceinline__ void potrf_pivot(double (*S)[NB + 1], double *rd, dou
     const double y = rsqrt_halley(p);
     rd[c] = y;
     rd2[c] = y * y;
-    S[c][c] = p * y;
 }
 
 __global__ void __launch_bounds__(POTRF_THREADS)
@@ -82,24 +95,28 @@ potrf_diag_kernel(double *__restrict__ A, int64_t lda, int n, int k0, double shi
                   int *__restrict__ info)
 {
     // Right-looking in shared memory, one barrier per column.  In phase c every
-    // element with c < s <= r takes S_rs -= S_rc S_sc / S_cc (one FMA; the unscaled
-    // column c and rd2[c] = 1/S_cc).  The elements are listed in `order` by s
-    // descending, r descending, so phase c's are the first tri_prefix(c) entries and
-    // the last of them is the next diagonal S_{c+1,c+1}: the workers share the others
-    // evenly, while the pivot thread updates that diagonal and takes its pivot at
-    // once, so the pivot latency overlaps the updates.  rd[c] is written one phase
-    // before it is read, so rd[c] == 0 is a race-free failure signal.  Columns are
-    // scaled by rd at the end.
+    // element with c < s <= r takes S_rs -= S_rc S_sc / S_cc (the unscaled column c
+    // and rd2[c] = 1/S_cc).  The elements are listed in `order` by s descending, r
+    // descending, so phase c's are the first tri_prefix(c) entries and the last of
+    // them is the next diagonal S_{c+1,c+1}: the workers share the others evenly,
+    // while the pivot thread updates that diagonal and takes its pivot at once, so
+    // the pivot latency overlaps the updates.  rd[c] is written one phase before it
+    // is read, so rd[c] == 0 is a race-free failure signal.  Columns are scaled by rd
+    // at write-back.
     __shared__ double S[NB][NB + 1];
     __shared__ double rd[NB], rd2[NB];
     __shared__ unsigned short order[tri_prefix(0)];
     if (*info != 0) return;
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, warp = tid >> 5;
     const int nb = min(NB, n - k0);
-    for (int e = tid; e < NB * NB; e += blockDim.x) {
+#pragma unroll
+    for (int e = tid; e < NB * NB; e += POTRF_THREADS) {  // loads issued back to back
         const int r = e >> 6, c = e & 63;
         double v = (r == c) ? 1.0 : 0.0;  // identity padding keeps short blocks regular
-        if (r < nb && c <= r) v = A[(int64_t)(k0 + r) * lda + (k0 + c)] + (r == c ? shift : 0.0);
+        if (r < nb && c <= r) {
+            v = A[(int64_t)(k0 + r) * lda + (k0 + c)];
+            if (r == c) v += shift;
+        }
         S[r][c] = v;
     }
     if (tid >= 1 && tid < NB) {
@@ -109,8 +126,10 @@ potrf_diag_kernel(double *__restrict__ A, int64_t lda, int n, int k0, double shi
     __syncthreads();
     if (tid == POTRF_PIVOT) potrf_pivot(S, rd, rd2, 0, k0, nb, info);
     __syncthreads();
+    const bool worker = warp != 3 && warp != 7;
+    const int wid = (warp < 3 ? warp : warp - 1) * 32 + (tid & 31);
     for (int c = 0; c < NB; ++c) {
-        if (rd[c] == 0.0) return;
+        if (__double_as_longlong(rd[c]) == 0) return;
         const double y2 = rd2[c];
         if (tid == POTRF_PIVOT) {
             if (c + 1 < NB) {
@@ -118,14 +137,14 @@ potrf_diag_kernel(double *__restrict__ A, int64_t lda, int n, int k0, double shi
                 S[c + 1][c + 1] = fma(-v * y2, v, S[c + 1][c + 1]);
                 potrf_pivot(S, rd, rd2, c + 1, k0, nb, info);
             }
-        } else if (tid < POTRF_WORKERS) {
+        } else if (worker) {
             const int cnt = tri_prefix(c) - 1;
-            for (int e0 = tid; e0 < cnt; e0 += 3 * POTRF_WORKERS) {
-                // loads of three elements first, then their FMAs and stores
-                int rr[3], ss[3];
-                double x[3], u[3], v[3];
+            for (int e0 = wid; e0 < cnt; e0 += POTRF_BATCH * POTRF_WORKERS) {
+                // loads of a batch of elements first, then their FMAs and stores
+                int rr[POTRF_BATCH], ss[POTRF_BATCH];
+                double x[POTRF_BATCH], u[POTRF_BATCH], v[POTRF_BATCH];
 #pragma unroll
-                for (int k = 0; k < 3; ++k) {
+                for (int k = 0; k < POTRF_BATCH; ++k) {
                     const int e = e0 + k * POTRF_WORKERS;
                     if (e < cnt) {
                         const unsigned code = order[e];
@@ -137,7 +156,7 @@ potrf_diag_kernel(double *__restrict__ A, int64_t lda, int n, int k0, double shi
                     }
                 }
 #pragma unroll
-                for (int k = 0; k < 3; ++k)
+                for (int k = 0; k < POTRF_BATCH; ++k)
                     if (e0 + k * POTRF_WORKERS < cnt) S[rr[k]][ss[k]] = fma(-u[k] * y2, v[k], x[k]);
             }
         }
@@ -145,33 +164,48 @@ potrf_diag_kernel(double *__restrict__ A, int64_t lda, int n, int k0, double shi
     }
     for (int e = tid; e < nb * NB; e += blockDim.x) {
         const int r = e >> 6, c = e & 63;
-        if (c <= r) A[(int64_t)(k0 + r) * lda + (k0 + c)] = (c < r) ? S[r][c] * rd[c] : S[r][c];
+        if (c <= r) A[(int64_t)(k0 + r) * lda + (k0 + c)] = S[r][c] * rd[c];
     }
 }
 
-constexpr int TRSM_ROWS = 64;
+constexpr int TRSM_MAX_ROWS = 128;  // rows per CTA: 4 threads per row
 
-// X <- X L_kk^{-T} for the rows below the diagonal block, one CTA per 64 rows.  A
-// row is held by the four lanes of a quad (lane q owns the columns = q mod 4, in
+// Rows per TRSM CTA for `rows` rows on `sms` SMs: a multiple of 8 up to 128, chosen
+// so the CTAs spread evenly (every SM gets the same number, up to rounding).
+inline int trsm_rows_per_cta(int rows, int sms)
+{
+    sms = std::max(1, sms);
+    const int k = (int)qmlg::ceil_div(rows, sms * TRSM_MAX_ROWS);  // CTAs per SM
+    const int r = (int)qmlg::ceil_div(qmlg::ceil_div(rows, std::max(1, k * sms)), 8) * 8;
+    return std::min(TRSM_MAX_ROWS, std::max(32, r));
+}
+
+inline size_t trsm_smem(int rpc) { return (size_t)rpc * (NB + 8) * sizeof(__nv_bfloat16); }
+
+// X <- X L_kk^{-T} for the rows below the diagonal block, blockDim / 4 rows per CTA.
+// A row is held by the four lanes of a quad (lane q owns the columns = q mod 4, in
 // registers); column c is finished by its owner and broadcast with a shuffle, so
 // the substitution needs no block barrier.  With `digits`, the kernel also writes
 // what slice_rows would make of the solved rows (the operand of the emulated K = 64
 // update that follows): per-row exponents and the `slices` balanced base-128 digit
 // planes, digits[s][row][64] with row = global row - (k0 + 64), for the rows below
 // drows (zeros past the matrix).
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(4 * TRSM_MAX_ROWS)
 trsm_panel_kernel(double *__restrict__ A, int64_t lda, int n, int k0,
                   const int *__restrict__ info, int slices, int rpad, int drows,
                   __nv_bfloat16 *__restrict__ digits, int *__restrict__ expo)
 {
     __shared__ double L[NB][NB + 1];
     __shared__ double rdg[NB];
-    __shared__ __align__(16) __nv_bfloat16 P[TRSM_ROWS][NB + 8];
+    extern __shared__ __align__(16) unsigned char trsm_dyn[];
+    __nv_bfloat16(*P)[NB + 8] = reinterpret_cast<__nv_bfloat16(*)[NB + 8]>(trsm_dyn);
     if (*info != 0) return;
     const int tid = threadIdx.x, lane = tid & 31;
+    const int rpc = blockDim.x >> 2;
     const int nb = min(NB, n - k0);
     const int r1 = k0 + nb, nrows = n - r1;
-    const int rbase = blockIdx.x * TRSM_ROWS;
+    const int rbase = blockIdx.x * rpc;
+#pragma unroll 8
     for (int e = tid; e < NB * NB; e += blockDim.x) {
         const int r = e >> 6, c = e & 63;
         L[r][c] = (r < nb && c <= r) ? A[(int64_t)(k0 + r) * lda + (k0 + c)] : (r == c ? 1.0 : 0.0);
@@ -225,7 +259,7 @@ trsm_panel_kernel(double *__restrict__ A, int64_t lda, int n, int k0,
             P[r][s0 + 4 * j] = __int2bfloat16_rn((int)d);
         }
         __syncthreads();
-        for (int i = tid; i < TRSM_ROWS * (NB / 8); i += blockDim.x) {
+        for (int i = tid; i < rpc * (NB / 8); i += blockDim.x) {
             const int rr = i >> 3, ch = i & 7, g = rbase + rr;
             if (g < drows)
                 *reinterpret_cast<uint4 *>(digits + sl * plane + (int64_t)g * NB + ch * 8) =
@@ -233,6 +267,27 @@ trsm_panel_kernel(double *__restrict__ A, int64_t lda, int n, int k0,
         }
         __syncthreads();
     }
+}
+
+// Launches the TRSM of the rows below diagonal block k0 (with `digits`: the digit
+// planes of the rows below drows as well).
+int launch_trsm(double *A, int64_t lda, int n, int k0, const int *d_info, int slices, int rpad,
+                int drows, __nv_bfloat16 *digits, int *expo, cudaStream_t s)
+{
+    static std::once_flag once;
+    static cudaError_t attr = cudaSuccess;
+    std::call_once(once, [] {
+        attr = cudaFuncSetAttribute(trsm_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)trsm_smem(TRSM_MAX_ROWS));
+    });
+    if (attr != cudaSuccess) return qmlg::set_cuda_error(attr);
+    const int rows = digits != nullptr ? drows : n - (k0 + NB);
+    if (rows <= 0) return QMLG_OK;
+    const int rpc = trsm_rows_per_cta(rows, qmlg::tc_sm_count());
+    trsm_panel_kernel<<<(unsigned)qmlg::ceil_div(rows, rpc), 4 * rpc, trsm_smem(rpc), s>>>(
+        A, lda, n, k0, d_info, slices, rpad, drows, digits, expo);
+    qmlg::count_launches(1);
+    return QMLG_OK;
 }
 
 __device__ __forceinline__ void tri_index(int64_t t, int &bi, int &bj)
@@ -903,7 +958,8 @@ int cholesky_fp64(double *A, int n, int64_t lda, double shift, int *d_info, cuda
         { potrf_diag_kernel<<<1, 256, 0, s>>>(A, lda, n, k0, shift, d_info); qmlg::count_launches(1); }
         const int below = n - (k0 + NB);
         if (below > 0) {
-            { trsm_panel_kernel<<<(int)ceil_div(below, TRSM_ROWS), 256, 0, s>>>(A, lda, n, k0, d_info, 0, 0, 0, nullptr, nullptr); qmlg::count_launches(1); }
+            const int st = launch_trsm(A, lda, n, k0, d_info, 0, 0, 0, nullptr, nullptr, s);
+            if (st != QMLG_OK) return st;
             const int64_t t = ceil_div(below, 64);
             { syrk_update_kernel<<<(unsigned)(t * (t + 1) / 2), 256, 0, s>>>(A, lda, n, k0, d_info); qmlg::count_launches(1); }
         }
@@ -1011,15 +1067,12 @@ int factor_panel(double *A, int n, int64_t lda, double shift, int K0, int K1, in
         // the solved rows' digit planes feed the panel's own K = 64 update
         const bool inner = r1 < K1;
         const int drows = inner ? std::min(rpad, (int)ceil_div(n - r1, 128) * 128) : 0;
-        {
-            trsm_panel_kernel<<<(int)ceil_div(inner ? drows : n - r1, TRSM_ROWS), 256, 0, s>>>(
-                A, lda, n, k0, d_info, slices, rpad, drows, inner ? dig_in : nullptr,
-                inner ? exp_in : nullptr);
-            count_launches(1);
-        }
+        int st = launch_trsm(A, lda, n, k0, d_info, slices, rpad, drows, inner ? dig_in : nullptr,
+                             inner ? exp_in : nullptr, s);
+        if (st != QMLG_OK) return st;
         if (inner) {
-            const int st = emu_tc_update(A, lda, r1, K1, r1, n, dig_in, exp_in, NB, rpad, slices, 0,
-                                         0, 1, d_err, s, update_ctas);
+            st = emu_tc_update(A, lda, r1, K1, r1, n, dig_in, exp_in, NB, rpad, slices, 0, 0, 1,
+                               d_err, s, update_ctas);
             if (st != QMLG_OK) return st;
         }
     }
