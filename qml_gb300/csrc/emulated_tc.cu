@@ -29,6 +29,7 @@
 #include "common.cuh"
 #include "emulated_gemm.cuh"
 #include "tc_ptx.cuh"
+#include "exp2_table.cuh"
 
 namespace {
 
@@ -102,6 +103,35 @@ __device__ __forceinline__ double pow2i(int e)
 {
     if (e >= -1022 && e <= 1023) return __longlong_as_double((long long)(e + 1023) << 52);
     return ldexp(1.0, e);
+}
+
+// exp(x) for the Gaussian epilogues, x <= 0 after clamping, by table-driven reduction
+// (P. T. P. Tang, "Table-driven implementation of the exponential function in IEEE
+// floating-point arithmetic", ACM TOMS 15(2), 1989):
+//   x = (128 m + j) ln2/128 + r,  |r| <= ln2/256,  exp(x) = 2^m 2^(j/128) e^r,
+// 2^(j/128) from a (lead, trail) table, e^r - 1 by its Taylor polynomial to degree 5
+// (the next term is below 6e-19), 2^m applied to the exponent bits.  11 FP64
+// instructions; the range checks are integer compares on the bits.  x > 0 (and +NaN)
+// is clamped to 0, as the distance formula can round slightly above it; x <= -700 and
+// -NaN go to the library exp.
+__device__ __forceinline__ double exp_nonpos(double x)
+{
+    const long long xs = __double_as_longlong(x);
+    if (xs > 0) return 1.0;
+    if ((unsigned long long)xs >= 0xC085E00000000000ull) return exp(x);  // bits of -700.0
+    const double t = fma(x, k128OverLn2, 0x1.8p52);  // 1.5 * 2^52 + round(x * 128 / ln2)
+    const int n = (int)(__double_as_longlong(t) - 0x4338000000000000ll);
+    const double nd = t - 0x1.8p52;
+    double r = fma(-nd, kLn2Over128Hi, x);
+    r = fma(-nd, kLn2Over128Lo, r);
+    double q = fma(r, 1.0 / 120.0, 1.0 / 24.0);
+    q = fma(q, r, 1.0 / 6.0);
+    q = fma(q, r, 0.5);
+    q = fma(q, r, 1.0);
+    q *= r;  // e^r - 1
+    const double2 T = kExp2Tab128[n & 127];
+    const double v = T.x + fma(T.x, q, T.y);
+    return __longlong_as_double(__double_as_longlong(v) + ((long long)(n >> 7) << 52));
 }
 
 template <int MODE>
@@ -364,7 +394,16 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
                 }
             } else {
                 // Gaussian epilogues: the FP64 exp dominates; eight columns at a time,
-                // TMEM released once the last eight are in registers
+                // TMEM released once the last eight are in registers.  The per-column
+                // terms (scale |b|^2, b's exponent) are loaded once per tile by the lane
+                // of that column and broadcast; -2 scale 2^e is formed on the bits.
+                const int ibl = i0 + h * 32 + lane;
+                const bool ilv = ibl < p.iend;
+                const double sBl = ilv ? p.scale * p.normB[brow + h * 32 + lane] : 0.0;
+                const int eBl = ilv ? p.expB[brow + h * 32 + lane] : 0;
+                const double m2s = -2.0 * p.scale;
+                const long long m2s_bits = __double_as_longlong(m2s);
+                const int m2s_exp = (int)((m2s_bits >> 52) & 0x7ff);
                 for (int gq = 0; gq < 32 / EG; ++gq) {
                     const int cb = h * 32 + gq * EG;
                     uint32_t v[S_MAX][EG];
@@ -383,15 +422,18 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
                     for (int col = 0; col < EG; ++col) {
                         const int il = cb + col;
                         const int i = i0 + il;
+                        const double sb = __shfl_sync(0xffffffffu, sBl, gq * EG + col);
+                        const int eb = __shfl_sync(0xffffffffu, eBl, gq * EG + col);
                         const bool valid = jvalid && i < p.iend;
                         double kv = 0.0;
                         if (valid) {
-                            // x = scale * (|a|^2 + |b|^2 - 2 a.b), clamped at 0 from above
-                            const double w =
-                                -2.0 * p.scale * pow2i(p.expB[brow + il] + ej + shift - 7 * (S + 1));
-                            const double x =
-                                fmin(fma((double)v64[col], w, aj + p.scale * p.normB[brow + il]), 0.0);
-                            kv = exp(x);
+                            // x = scale * (|a|^2 + |b|^2 - 2 a.b)
+                            const int ew = eb + ej + shift - 7 * (S + 1);
+                            const int ef = m2s_exp + ew;
+                            const double w = (m2s_exp > 0 && ef > 0 && ef < 2047)
+                                                 ? __longlong_as_double(m2s_bits + ((long long)ew << 52))
+                                                 : m2s * pow2i(ew);
+                            kv = exp_nonpos(fma((double)v64[col], w, aj + sb));
                             if (MODE == kKernelMatrix && p.lower && i == j) kv = 1.0 + p.diag_shift;
                         }
                         if (MODE == kKernelMatrix) {
