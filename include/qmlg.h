@@ -120,6 +120,38 @@ int qmlg_laplacian_kernel(const double *A, int64_t lda, int na, const double *B,
                           double diag_shift, void *stream);
 
 /*
+ * Linear kernel K(na, nb), K[j + i*ldk] = A_j . B_i.  Replaces flinear_kernel
+ * (qml/fkernels.f90:403-423), bound by qml.kernels.linear_kernel
+ * (qml/kernels.py:94-120).  FP64 arithmetic; flags and diag_shift as above.
+ */
+int qmlg_linear_kernel(const double *A, int64_t lda, int na, const double *B, int64_t ldb, int nb,
+                       int d, double *K, int64_t ldk, int flags, double diag_shift, void *stream);
+
+/*
+ * Matern kernel with the L2 distance d = |A_j - B_i|_2, order 0, 1 or 2:
+ *   0: exp(-d/sigma)
+ *   1: exp(-sqrt3 d/sigma) (1 + sqrt3 d/sigma)
+ *   2: exp(-sqrt5 d/sigma) (1 + sqrt5 d/sigma + 5 d^2 / (3 sigma^2))
+ * Replaces fmatern_kernel_l2 (qml/fkernels.f90:426-484), bound by
+ * qml.kernels.matern_kernel(metric="l2") (qml/kernels.py:158-215); the L1 metric is
+ * the Sargan kernel below, as the reference's wrapper maps it.  FP64 arithmetic.
+ */
+int qmlg_matern_kernel_l2(const double *A, int64_t lda, int na, const double *B, int64_t ldb,
+                          int nb, int d, double sigma, int order, double *K, int64_t ldk,
+                          int flags, double diag_shift, void *stream);
+
+/*
+ * Sargan kernel with the L1 distance d = |A_j - B_i|_1:
+ *   exp(-d/sigma) (1 + sum_{m=1..ngammas} gammas[m-1] (d/sigma)^m).
+ * gammas: device array of ngammas doubles (may be NULL when ngammas = 0, which gives
+ * the Laplacian kernel).  Replaces fsargan_kernel (qml/fkernels.f90:487-531), bound
+ * by qml.kernels.sargan_kernel (qml/kernels.py:122-156).  FP64 arithmetic.
+ */
+int qmlg_sargan_kernel(const double *A, int64_t lda, int na, const double *B, int64_t ldb, int nb,
+                       int d, double sigma, const double *gammas, int ngammas, double *K,
+                       int64_t ldk, int flags, double diag_shift, void *stream);
+
+/*
  * Gaussian kernel with the contraction a.b emulated to FP64 accuracy on the bf16
  * tensor cores (tcgen05): rows are scaled by powers of two and cut into base-128
  * digit planes; the digit products are summed exactly in tensor memory and

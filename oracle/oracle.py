@@ -63,6 +63,14 @@ def _load():
             fn = getattr(lib, name)
             fn.argtypes = [_dp, ctypes.c_int, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_double, _dp]
             fn.restype = None
+        lib.oracle_linear_kernel.argtypes = [_dp, ctypes.c_int, _dp, ctypes.c_int, ctypes.c_int, _dp]
+        lib.oracle_linear_kernel.restype = None
+        lib.oracle_matern_kernel_l2.argtypes = [_dp, ctypes.c_int, _dp, ctypes.c_int, ctypes.c_int,
+                                                ctypes.c_double, ctypes.c_int, _dp]
+        lib.oracle_matern_kernel_l2.restype = None
+        lib.oracle_sargan_kernel.argtypes = [_dp, ctypes.c_int, _dp, ctypes.c_int, ctypes.c_int,
+                                             ctypes.c_double, _dp, ctypes.c_int, _dp]
+        lib.oracle_sargan_kernel.restype = None
         lib.oracle_residual_dd.argtypes = [_dp, ctypes.c_int, ctypes.c_int64, ctypes.c_double,
                                            _dp, _dp, _dp]
         lib.oracle_residual_dd.restype = None
@@ -156,6 +164,36 @@ def laplacian_kernel(A, B, sigma):
     K = np.empty((A.shape[0], B.shape[0]), order="F")
     _load().oracle_laplacian_kernel(_ptr(A), A.shape[0], _ptr(B), B.shape[0], A.shape[1],
                                     float(sigma), _ptr(K))
+    return K
+
+
+def linear_kernel(A, B):
+    """K (na, nb) = A . B^T in Fortran order (qml/fkernels.f90:403-423)."""
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    B = np.ascontiguousarray(B, dtype=np.float64)
+    K = np.empty((A.shape[0], B.shape[0]), order="F")
+    _load().oracle_linear_kernel(_ptr(A), A.shape[0], _ptr(B), B.shape[0], A.shape[1], _ptr(K))
+    return K
+
+
+def matern_kernel_l2(A, B, sigma, order):
+    """Matern kernel with the L2 distance (qml/fkernels.f90:426-484)."""
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    B = np.ascontiguousarray(B, dtype=np.float64)
+    K = np.empty((A.shape[0], B.shape[0]), order="F")
+    _load().oracle_matern_kernel_l2(_ptr(A), A.shape[0], _ptr(B), B.shape[0], A.shape[1],
+                                    float(sigma), int(order), _ptr(K))
+    return K
+
+
+def sargan_kernel(A, B, sigma, gammas):
+    """Sargan kernel (qml/fkernels.f90:487-531)."""
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    B = np.ascontiguousarray(B, dtype=np.float64)
+    g = np.ascontiguousarray(gammas, dtype=np.float64).reshape(-1)
+    K = np.empty((A.shape[0], B.shape[0]), order="F")
+    _load().oracle_sargan_kernel(_ptr(A), A.shape[0], _ptr(B), B.shape[0], A.shape[1],
+                                 float(sigma), _ptr(g) if g.size else None, int(g.size), _ptr(K))
     return K
 
 

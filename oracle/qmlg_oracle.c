@@ -169,6 +169,89 @@ void oracle_laplacian_kernel(const double *a, int na, const double *b, int nb, i
     }
 }
 
+/*
+ * Linear kernel, Fortran order: k[j + i*na] = dot(a_j, b_i).
+ * Follows qml/fkernels.f90:403-423 (flinear_kernel): dot_product over the feature
+ * index ascending.
+ */
+void oracle_linear_kernel(const double *a, int na, const double *b, int nb, int d, double *k)
+{
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < nb; ++i) {
+        const double *bi = b + (size_t)i * d;
+        for (int j = 0; j < na; ++j) {
+            const double *aj = a + (size_t)j * d;
+            double s = 0.0;
+            for (int t = 0; t < d; ++t) s = s + aj[t] * bi[t];
+            k[(size_t)j + (size_t)i * na] = s;
+        }
+    }
+}
+
+/*
+ * Matern kernel with the L2 distance, Fortran order.  Follows qml/fkernels.f90:426-484
+ * (fmatern_kernel_l2): d2 = sum((a_j - b_i)^2), d = sqrt(d2);
+ *   order 0: inv_sigma = -1/sigma,        k = exp(inv_sigma d)
+ *   order 1: inv_sigma = -sqrt(3)/sigma,  k = exp(inv_sigma d) (1 - inv_sigma d)
+ *   other:   inv_sigma = -sqrt(5)/sigma, inv_sigma2 = 5/(3 sigma^2),
+ *            k = exp(inv_sigma d) (1 - inv_sigma d + inv_sigma2 d2)
+ */
+void oracle_matern_kernel_l2(const double *a, int na, const double *b, int nb, int d,
+                             double sigma, int order, double *k)
+{
+    /* the reference's branches: order 0, order 1, anything else */
+    const int form = order == 0 ? 0 : (order == 1 ? 1 : 2);
+    double inv_sigma = -1.0 / sigma, inv_sigma2 = 0.0;
+    if (form == 1) inv_sigma = -sqrt(3.0) / sigma;
+    if (form == 2) {
+        inv_sigma = -sqrt(5.0) / sigma;
+        inv_sigma2 = 5.0 / (3.0 * sigma * sigma);
+    }
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < nb; ++i) {
+        const double *bi = b + (size_t)i * d;
+        for (int j = 0; j < na; ++j) {
+            const double *aj = a + (size_t)j * d;
+            double d2 = 0.0;
+            for (int t = 0; t < d; ++t) {
+                double u = aj[t] - bi[t];
+                d2 = d2 + u * u;
+            }
+            const double dd = sqrt(d2);
+            double v = exp(inv_sigma * dd);
+            if (form == 1) v = v * (1.0 - inv_sigma * dd);
+            if (form == 2) v = v * (1.0 - inv_sigma * dd + inv_sigma2 * d2);
+            k[(size_t)j + (size_t)i * na] = v;
+        }
+    }
+}
+
+/*
+ * Sargan kernel, Fortran order.  Follows qml/fkernels.f90:487-531 (fsargan_kernel):
+ * d = sum|a_j - b_i|, inv_sigma = -1/sigma,
+ * k = exp(inv_sigma d) (1 + sum_m gammas[m-1] (-inv_sigma d)^m), m = 1..ng.
+ */
+void oracle_sargan_kernel(const double *a, int na, const double *b, int nb, int d, double sigma,
+                          const double *gammas, int ng, double *k)
+{
+    const double inv_sigma = -1.0 / sigma;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < nb; ++i) {
+        const double *bi = b + (size_t)i * d;
+        for (int j = 0; j < na; ++j) {
+            const double *aj = a + (size_t)j * d;
+            double s = 0.0;
+            for (int t = 0; t < d; ++t) s = s + fabs(aj[t] - bi[t]);
+            double pre = 0.0, p = 1.0;
+            for (int m = 0; m < ng; ++m) {
+                p = p * (-inv_sigma * s);
+                pre = pre + gammas[m] * p;
+            }
+            k[(size_t)j + (size_t)i * na] = exp(inv_sigma * s) * (1.0 + pre);
+        }
+    }
+}
+
 /* Error-free transformations (Knuth two-sum, fma two-product). */
 static inline void two_sum(double a, double b, double *s, double *e)
 {

@@ -124,12 +124,16 @@ def _rows(X: torch.Tensor) -> Tuple[torch.Tensor, int]:
 
 def kernel_matrix(kind: str, A: torch.Tensor, B: torch.Tensor, sigma: float,
                   symmetric: bool = False, diag_shift: float = 0.0,
-                  out: Optional[torch.Tensor] = None, emulated: bool = False) -> torch.Tensor:
+                  out: Optional[torch.Tensor] = None, emulated: bool = False,
+                  order: int = 0, gammas=None) -> torch.Tensor:
     """K (na, nb), Fortran-ordered like the reference, as a (na, nb) view of a
-    column-major buffer.  symmetric=True requires B is A.  emulated=True takes the
-    fast exact-within-1e-12 paths: the Gaussian contraction on the tensor cores
-    (qmlg_gaussian_kernel_emulated), the Laplacian L1 sums in fixed-point integers
-    (qmlg_laplacian_kernel_fixed)."""
+    column-major buffer.  symmetric=True requires B is A.
+
+    kind: "gaussian", "laplacian", "linear" (sigma unused), "matern_l2" (with
+    order 0/1/2) or "sargan" (with gammas, a sequence or 1-D tensor).
+    emulated=True takes the fast exact-within-1e-12 paths: the Gaussian contraction
+    on the tensor cores (qmlg_gaussian_kernel_emulated), the Laplacian L1 sums in
+    fixed-point integers (qmlg_laplacian_kernel_fixed)."""
     _require_cuda(A, B)
     A, lda = _rows(A)
     if symmetric:
@@ -164,9 +168,30 @@ def kernel_matrix(kind: str, A: torch.Tensor, B: torch.Tensor, sigma: float,
                                                 _stream(A.device)),
               "qmlg_laplacian_kernel_fixed")
         return buf.T
+    st = _stream(A.device)
+    if kind == "linear":
+        check(lib().qmlg_linear_kernel(A.data_ptr(), lda, na, B.data_ptr(), ldb, nb, d,
+                                       buf.data_ptr(), na, flags, float(diag_shift), st),
+              "qmlg_linear_kernel")
+        return buf.T
+    if kind == "matern_l2":
+        check(lib().qmlg_matern_kernel_l2(A.data_ptr(), lda, na, B.data_ptr(), ldb, nb, d,
+                                          float(sigma), int(order), buf.data_ptr(), na, flags,
+                                          float(diag_shift), st), "qmlg_matern_kernel_l2")
+        return buf.T
+    if kind == "sargan":
+        g = torch.as_tensor(gammas if gammas is not None else [], dtype=torch.float64)
+        g = g.reshape(-1).to(A.device).contiguous()
+        check(lib().qmlg_sargan_kernel(A.data_ptr(), lda, na, B.data_ptr(), ldb, nb, d,
+                                       float(sigma), g.data_ptr() if g.numel() else None,
+                                       int(g.numel()), buf.data_ptr(), na, flags,
+                                       float(diag_shift), st), "qmlg_sargan_kernel")
+        return buf.T
+    if kind not in ("gaussian", "laplacian"):
+        raise ValueError("unknown kernel kind %r" % (kind,))
     fn = lib().qmlg_gaussian_kernel if kind == "gaussian" else lib().qmlg_laplacian_kernel
     check(fn(A.data_ptr(), lda, na, B.data_ptr(), ldb, nb, d, float(sigma), buf.data_ptr(), na,
-             flags, float(diag_shift), _stream(A.device)), "qmlg_%s_kernel" % kind)
+             flags, float(diag_shift), st), "qmlg_%s_kernel" % kind)
     return buf.T
 
 

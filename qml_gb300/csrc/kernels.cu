@@ -1,11 +1,15 @@
-// FP64 Gaussian and Laplacian kernel matrices and the prediction that uses them.
+// FP64 kernel matrices and the prediction that uses them.
 //
-// Restates fgaussian_kernel / flaplacian_kernel (qml/fkernels.f90:340-400):
-//   Gaussian:  K[j + i*ldk] = exp(-0.5/sigma^2 * |A_j - B_i|^2)
-//   Laplacian: K[j + i*ldk] = exp(-1/sigma * |A_j - B_i|_1)
-// with K in Fortran order like the reference.  The Gaussian distance is formed as
-// |a|^2 + |b|^2 - 2 a.b (norms in FP64); the Laplacian keeps the direct difference
-// form (an L1 distance is not a contraction).
+// Restates the global kernels of qml/fkernels.f90, K in Fortran order like the
+// reference (K[j + i*ldk] for A row j, B row i):
+//   Gaussian  (:340-372)  exp(-0.5/sigma^2 * |A_j - B_i|^2)
+//   Laplacian (:374-400)  exp(-1/sigma * |A_j - B_i|_1)
+//   linear    (:403-423)  A_j . B_i
+//   Matern L2 (:426-484)  d = |A_j - B_i|_2, order 0: exp(-d/s), 1: exp(-r3 d/s)(1 + r3 d/s),
+//                         2: exp(-r5 d/s)(1 + r5 d/s + 5 d^2 / (3 s^2))  (r3 = sqrt 3, r5 = sqrt 5)
+//   Sargan    (:487-531)  d = |A_j - B_i|_1, exp(-d/s) (1 + sum_m gamma_m (d/s)^m)
+// The Gaussian distance is formed as |a|^2 + |b|^2 - 2 a.b (norms in FP64); the
+// other distances keep the reference's direct difference form.
 //
 // Tiling: a CTA computes a 64 (j, rows of A) x 64 (i, rows of B) tile with 256
 // threads, 4x4 outputs per thread, the feature dimension streamed through shared
@@ -26,7 +30,17 @@ constexpr int TI = 64;   // tile cols (B side)
 constexpr int TK = 16;   // feature chunk
 constexpr int NT = 256;  // threads
 
-enum Kind { kGauss = 0, kLaplace = 1 };
+enum Kind { kGauss = 0, kLaplace = 1, kLinear = 2, kMaternL2 = 3, kSargan = 4 };
+
+// Epilogue constants: s1 the exponent's factor (Matern: -sqrt(2 order + 1)/sigma),
+// s2 the Matern order-2 quadratic factor 5/(3 sigma^2), gammas[0..ng) the Sargan
+// polynomial (device memory).
+struct EpiParams {
+    double s1 = 0.0, s2 = 0.0;
+    int order = 0;
+    const double *gammas = nullptr;
+    int ng = 0;
+};
 
 // Maps a linear block id onto a lower-triangular tile pair (bi >= bj).
 __device__ __forceinline__ void tri_index(int64_t t, int &bi, int &bj)
@@ -88,8 +102,11 @@ __device__ __forceinline__ void tile_accumulate(const double *__restrict__ A, in
             for (int a = 0; a < 4; ++a)
 #pragma unroll
                 for (int b = 0; b < 4; ++b) {
-                    if (KIND == kGauss) {
+                    if (KIND == kGauss || KIND == kLinear) {
                         acc[a][b] = fma(av[a], bv[b], acc[a][b]);
+                    } else if (KIND == kMaternL2) {
+                        const double t = av[a] - bv[b];
+                        acc[a][b] = fma(t, t, acc[a][b]);
                     } else {
                         acc[a][b] += fabs(av[a] - bv[b]);
                     }
@@ -108,7 +125,7 @@ template <int KIND>
 __global__ void __launch_bounds__(NT)
 kernel_matrix_kernel(const double *__restrict__ A, int64_t lda, int na,
                      const double *__restrict__ B, int64_t ldb, int nb, int d,
-                     double scale, double *__restrict__ K, int64_t ldk, int symmetric,
+                     EpiParams ep, double *__restrict__ K, int64_t ldk, int symmetric,
                      double diag_shift)
 {
     // operand chunks during accumulation, the output tile (for the mirror) after
@@ -142,9 +159,25 @@ kernel_matrix_kernel(const double *__restrict__ A, int64_t lda, int na,
                 if (j < na && i < nb)
                     d2 = fmax(a2s[tx + 16 * a] + b2s[ty + 16 * b] - 2.0 * acc[a][b], 0.0);
                 if (symmetric && i == j) d2 = 0.0;
-                v = exp(scale * d2);
+                v = exp(ep.s1 * d2);
+            } else if (KIND == kLaplace) {
+                v = exp(ep.s1 * acc[a][b]);
+            } else if (KIND == kLinear) {
+                v = acc[a][b];
+            } else if (KIND == kMaternL2) {
+                const double d2 = acc[a][b], dd = sqrt(d2);
+                v = exp(ep.s1 * dd);
+                if (ep.order == 1) v *= 1.0 - ep.s1 * dd;
+                else if (ep.order == 2) v *= 1.0 - ep.s1 * dd + ep.s2 * d2;
             } else {
-                v = exp(scale * acc[a][b]);
+                // exp(-d/s) (1 + sum_m gamma_m t^m), t = d/s
+                const double dd = acc[a][b], t = -ep.s1 * dd;
+                double pw = 1.0, sum = 0.0;
+                for (int m = 0; m < ep.ng; ++m) {
+                    pw *= t;
+                    sum += ep.gammas[m] * pw;
+                }
+                v = exp(ep.s1 * dd) * (1.0 + sum);
             }
             if (symmetric && i == j) v += diag_shift;
             if (j < na && i < nb) K[(int64_t)i * ldk + j] = v;
@@ -243,9 +276,19 @@ int check_common(const double *A, int64_t lda, int na, const double *B, int64_t 
     return QMLG_OK;
 }
 
+template <int KIND>
+void launch_kernel_matrix(dim3 grid, cudaStream_t s, const double *A, int64_t lda, int na,
+                          const double *B, int64_t ldb, int nb, int d, const EpiParams &ep,
+                          double *K, int64_t ldk, int symmetric, double diag_shift)
+{
+    kernel_matrix_kernel<KIND><<<grid, NT, 0, s>>>(A, lda, na, B, ldb, nb, d, ep, K, ldk, symmetric,
+                                                   diag_shift);
+    qmlg::count_launches(1);
+}
+
 int kernel_matrix(int kind, const double *A, int64_t lda, int na, const double *B,
                   int64_t ldb, int nb, int d, double sigma, double *K, int64_t ldk, int flags,
-                  double diag_shift, void *stream)
+                  double diag_shift, void *stream, EpiParams ep = EpiParams())
 {
     int st = check_common(A, lda, na, B, ldb, nb, d, sigma);
     if (st != QMLG_OK) return st;
@@ -255,15 +298,18 @@ int kernel_matrix(int kind, const double *A, int64_t lda, int na, const double *
     if (na == 0 || nb == 0) return QMLG_OK;
     cudaStream_t s = qmlg::as_stream(stream);
 
-    const double scale = kind == kGauss ? -0.5 / (sigma * sigma) : -1.0 / sigma;
+    if (kind == kGauss) ep.s1 = -0.5 / (sigma * sigma);
+    else if (kind == kLaplace || kind == kSargan) ep.s1 = -1.0 / sigma;
     const int tj = (int)qmlg::ceil_div(na, TJ), ti = (int)qmlg::ceil_div(nb, TI);
     dim3 grid = symmetric ? dim3((unsigned)((int64_t)tj * (tj + 1) / 2)) : dim3(tj, ti);
-    if (kind == kGauss)
-        { kernel_matrix_kernel<kGauss><<<grid, NT, 0, s>>>(A, lda, na, B, ldb, nb, d, scale, K, ldk,
-                                                        symmetric, diag_shift); qmlg::count_launches(1); }
-    else
-        { kernel_matrix_kernel<kLaplace><<<grid, NT, 0, s>>>(A, lda, na, B, ldb, nb, d, scale, K,
-                                                          ldk, symmetric, diag_shift); qmlg::count_launches(1); }
+    const int sym = symmetric ? 1 : 0;
+    switch (kind) {
+    case kGauss: launch_kernel_matrix<kGauss>(grid, s, A, lda, na, B, ldb, nb, d, ep, K, ldk, sym, diag_shift); break;
+    case kLaplace: launch_kernel_matrix<kLaplace>(grid, s, A, lda, na, B, ldb, nb, d, ep, K, ldk, sym, diag_shift); break;
+    case kLinear: launch_kernel_matrix<kLinear>(grid, s, A, lda, na, B, ldb, nb, d, ep, K, ldk, sym, diag_shift); break;
+    case kMaternL2: launch_kernel_matrix<kMaternL2>(grid, s, A, lda, na, B, ldb, nb, d, ep, K, ldk, sym, diag_shift); break;
+    default: launch_kernel_matrix<kSargan>(grid, s, A, lda, na, B, ldb, nb, d, ep, K, ldk, sym, diag_shift); break;
+    }
     return qmlg::check_launch();
 }
 
@@ -283,6 +329,43 @@ extern "C" int qmlg_laplacian_kernel(const double *A, int64_t lda, int na, const
 {
     return kernel_matrix(kLaplace, A, lda, na, B, ldb, nb, d, sigma, K, ldk, flags, diag_shift,
                          stream);
+}
+
+extern "C" int qmlg_linear_kernel(const double *A, int64_t lda, int na, const double *B,
+                                  int64_t ldb, int nb, int d, double *K, int64_t ldk, int flags,
+                                  double diag_shift, void *stream)
+{
+    return kernel_matrix(kLinear, A, lda, na, B, ldb, nb, d, 1.0, K, ldk, flags, diag_shift,
+                         stream);
+}
+
+extern "C" int qmlg_matern_kernel_l2(const double *A, int64_t lda, int na, const double *B,
+                                     int64_t ldb, int nb, int d, double sigma, int order,
+                                     double *K, int64_t ldk, int flags, double diag_shift,
+                                     void *stream)
+{
+    if (order < 0 || order > 2) return QMLG_E_ARG;
+    EpiParams ep;
+    ep.order = order;
+    // the reference's inv_sigma and inv_sigma2 (qml/fkernels.f90:446-479)
+    ep.s1 = -std::sqrt((double)(2 * order + 1)) / sigma;
+    if (order == 0) ep.s1 = -1.0 / sigma;
+    ep.s2 = 5.0 / (3.0 * sigma * sigma);
+    return kernel_matrix(kMaternL2, A, lda, na, B, ldb, nb, d, sigma, K, ldk, flags, diag_shift,
+                         stream, ep);
+}
+
+extern "C" int qmlg_sargan_kernel(const double *A, int64_t lda, int na, const double *B,
+                                  int64_t ldb, int nb, int d, double sigma, const double *gammas,
+                                  int ngammas, double *K, int64_t ldk, int flags,
+                                  double diag_shift, void *stream)
+{
+    if (ngammas < 0 || (ngammas > 0 && gammas == nullptr)) return QMLG_E_ARG;
+    EpiParams ep;
+    ep.gammas = gammas;
+    ep.ng = ngammas;
+    return kernel_matrix(kSargan, A, lda, na, B, ldb, nb, d, sigma, K, ldk, flags, diag_shift,
+                         stream, ep);
 }
 
 extern "C" int qmlg_predict_gemv(const double *Ks, int64_t ldk, int ntrain, int ntest,

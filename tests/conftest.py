@@ -20,6 +20,16 @@ def load_golden(name):
         return {k: f[k] for k in f.files}
 
 
+def more_kernel_inputs():
+    """The seeded inputs of the reference's linear/Matern/Sargan tests, redrawn in the
+    same order as there (see tests/golden/make_golden.py)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(GOLDEN, "make_golden.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.more_kernel_inputs()
+
+
 @pytest.fixture(scope="session")
 def oracle():
     from oracle import oracle as o

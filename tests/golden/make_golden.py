@@ -14,6 +14,11 @@ Outputs (small .npz files, committed):
   kernels_seed666.npz   the inputs of tests/test_kernels.py:34-90 (np.random.seed(666),
                         X = rand(25, 1000), Xs = rand(20, 1000), sigma = 100) with the
                         reference test's own NumPy-loop expectations
+  kernels_more_seed666.npz
+                        the NumPy-loop expectations of tests/test_kernels.py:93-214
+                        (linear, Matern and Sargan kernels) and the Sargan gammas; the
+                        inputs are not stored: tests redraw them with
+                        more_kernel_inputs() (NumPy's legacy seeded stream is frozen)
 """
 import os
 import sys
@@ -64,6 +69,69 @@ def main(ref):
             kg[i, j] = np.exp(np.sum(np.square(X[i] - Xs[j])) / (-2.0 * sigma ** 2))
     np.savez_compressed(os.path.join(here, "kernels_seed666.npz"), X=X, Xs=Xs, sigma=sigma,
                         laplacian=kl, gaussian=kg)
+    more_kernels(here)
+
+
+def more_kernel_inputs():
+    """The inputs of tests/test_kernels.py:93-214, in draw order: each of those tests
+    seeds 666 once and draws its inputs in sequence (Matern: l1 then l2, orders 0, 1,
+    2; Sargan: 0, 1, 2 gammas, each followed by X and Xs).  Returns a dict of
+    key -> (X, Xs) and key -> gammas for the Sargan cases."""
+    out = {}
+    np.random.seed(666)
+    out["linear"] = (np.random.rand(25, 1000), np.random.rand(20, 1000))
+    np.random.seed(666)
+    for metric in ("l1", "l2"):
+        for order in (0, 1, 2):
+            out["matern_%s_%d" % (metric, order)] = (np.random.rand(25, 1000),
+                                                    np.random.rand(20, 1000))
+    np.random.seed(666)
+    for ng in (0, 1, 2):
+        gammas = np.random.random(ng)
+        out["sargan_%d" % ng] = (np.random.rand(25, 1000), np.random.rand(20, 1000))
+        out["sargan_%d_gammas" % ng] = gammas
+    return out
+
+
+def more_kernels(here):
+    """Expectations of tests/test_kernels.py:93-214, computed by those tests' loops."""
+    inp = more_kernel_inputs()
+    sigma = 100.0
+    out = {"sigma": sigma}
+    X, Xs = inp["linear"]
+    out["linear"] = np.array([[np.dot(X[i], Xs[j]) for j in range(20)] for i in range(25)])
+    for metric in ("l1", "l2"):
+        for order in (0, 1, 2):
+            X, Xs = inp["matern_%s_%d" % (metric, order)]
+            K = np.zeros((25, 20))
+            for i in range(25):
+                for j in range(20):
+                    if metric == "l1":
+                        d = np.sum(abs(X[i] - Xs[j]))
+                    else:
+                        d = np.sqrt(np.sum((X[i] - Xs[j]) ** 2))
+                    if order == 0:
+                        K[i, j] = np.exp(-d / sigma)
+                    elif order == 1:
+                        K[i, j] = np.exp(-np.sqrt(3) * d / sigma) * (1 + np.sqrt(3) * d / sigma)
+                    else:
+                        K[i, j] = np.exp(-np.sqrt(5) * d / sigma) * \
+                            (1 + np.sqrt(5) * d / sigma + 5.0 / 3 * d ** 2 / sigma ** 2)
+            out["matern_%s_%d" % (metric, order)] = K
+    for ng in (0, 1, 2):
+        gammas = inp["sargan_%d_gammas" % ng]
+        X, Xs = inp["sargan_%d" % ng]
+        K = np.zeros((25, 20))
+        for i in range(25):
+            for j in range(20):
+                d = np.sum(abs(X[i] - Xs[j]))
+                factor = 1
+                for k, gamma in enumerate(gammas):
+                    factor += gamma / sigma ** (k + 1) * d ** (k + 1)
+                K[i, j] = np.exp(-d / sigma) * factor
+        out["sargan_%d" % ng] = K
+        out["sargan_%d_gammas" % ng] = gammas
+    np.savez_compressed(os.path.join(here, "kernels_more_seed666.npz"), **out)
 
 
 if __name__ == "__main__":

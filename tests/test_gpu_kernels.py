@@ -1,12 +1,13 @@
-"""Gaussian / Laplacian kernel matrices and prediction on the GPU vs the oracle
-(relative error <= 1e-12 per entry, the FP64-path bar)."""
+"""Kernel matrices (Gaussian, Laplacian, linear, Matern, Sargan) and prediction on
+the GPU vs the oracle (relative error <= 1e-12 per entry, the FP64-path bar)."""
 import numpy as np
 import pytest
 import torch
 
-from conftest import load_golden
-from qml_gb300 import core
-from qml_gb300.kernels import gaussian_kernel, laplacian_kernel
+from conftest import load_golden, more_kernel_inputs
+from qml_gb300 import _lib, core
+from qml_gb300.kernels import (gaussian_kernel, laplacian_kernel, linear_kernel, matern_kernel,
+                               sargan_kernel)
 from qml_gb300.synthetic import generate_molecules
 
 pytestmark = pytest.mark.gpu
@@ -164,3 +165,78 @@ def test_fixed_point_laplacian_reference_test_and_fallback(cuda, oracle):
         assert relerr(K, oracle.laplacian_kernel(X, Xs, s)) <= RTOL
         if s == float(g["sigma"]):
             assert np.allclose(K, g["laplacian"])
+
+
+def test_more_kernels_reference_tests(cuda, oracle):
+    # tests/test_kernels.py:93-214 through the drop-in API: the reference test's own
+    # expectations (allclose) and the oracle (1e-12), plus the symmetric K(X, X)
+    g = load_golden("kernels_more_seed666.npz")
+    inp = more_kernel_inputs()
+    s = float(g["sigma"])
+    X, Xs = inp["linear"]
+    K = linear_kernel(X, Xs)
+    assert K.flags.f_contiguous and K.shape == (25, 20)
+    assert np.allclose(K, g["linear"]) and relerr(K, oracle.linear_kernel(X, Xs)) <= RTOL
+    Ks = linear_kernel(X, X)
+    assert np.array_equal(Ks, Ks.T) and relerr(Ks, oracle.linear_kernel(X, X)) <= RTOL
+    for metric in ("l1", "l2"):
+        for order in (0, 1, 2):
+            key = "matern_%s_%d" % (metric, order)
+            X, Xs = inp[key]
+            K = matern_kernel(X, Xs, s, order=order, metric=metric)
+            assert K.flags.f_contiguous and np.allclose(K, g[key])
+            assert relerr(K, g[key]) <= RTOL
+            Ks = matern_kernel(X, X, s, order=order, metric=metric)
+            assert np.array_equal(Ks, Ks.T)
+    for ng in (0, 1, 2):
+        X, Xs = inp["sargan_%d" % ng]
+        gam = inp["sargan_%d_gammas" % ng]
+        K = sargan_kernel(X, Xs, s, gam)
+        assert np.allclose(K, g["sargan_%d" % ng])
+        assert relerr(K, oracle.sargan_kernel(X, Xs, s, gam)) <= RTOL
+        Ks = sargan_kernel(X, X, s, gam)
+        assert np.array_equal(Ks, Ks.T)
+
+
+@pytest.mark.parametrize("na,nb", [(1, 1), (63, 65), (130, 77)])
+def test_more_kernels_cm_features(cuda, oracle, cm_features, na, nb):
+    # odd shapes on CM features (sigma 1000), C-order inputs through core, and the
+    # symmetric one-triangle path against the oracle
+    A, B = cm_features[:na], cm_features[200:200 + nb]
+    At, Bt = torch.from_numpy(A).to(cuda), torch.from_numpy(B).to(cuda)
+    gam = np.array([0.7, 0.2, 0.05])
+    cases = [("linear", {}, lambda a, b: oracle.linear_kernel(a, b)),
+             ("sargan", {"gammas": gam}, lambda a, b: oracle.sargan_kernel(a, b, 1000.0, gam))]
+    for order in (0, 1, 2):
+        cases.append(("matern_l2", {"order": order},
+                      lambda a, b, o=order: oracle.matern_kernel_l2(a, b, 1000.0, o)))
+    for kind, kw, ofn in cases:
+        K = core.kernel_matrix(kind, At, Bt, 1000.0, **kw).cpu().numpy()
+        assert relerr(K, ofn(A, B)) <= RTOL, kind
+        Ks = core.kernel_matrix(kind, At, At, 1000.0, symmetric=True, **kw).cpu().numpy()
+        Ko = ofn(A, A)
+        assert np.array_equal(Ks, Ks.T), kind
+        assert relerr(Ks, Ko) <= RTOL, kind
+
+
+def test_more_kernels_arguments(cuda, cm_features):
+    # the C-ABI rejects a Matern order outside 0..2 and a missing gamma array; the
+    # drop-in maps orders beyond 2 to the Fortran's third branch, and no gammas to
+    # the Laplacian kernel, like the reference wrapper
+    A = cm_features[:20]
+    At = torch.from_numpy(A).to(cuda)
+    K = torch.empty((20, 20), dtype=torch.float64, device=cuda)
+    lib = _lib.load()
+    st = lib.qmlg_matern_kernel_l2(At.data_ptr(), 276, 20, At.data_ptr(), 276, 20, 276, 1000.0, 3,
+                                   K.data_ptr(), 20, 0, 0.0, None)
+    assert st == _lib.QMLG_E_ARG
+    st = lib.qmlg_sargan_kernel(At.data_ptr(), 276, 20, At.data_ptr(), 276, 20, 276, 1000.0, None,
+                                2, K.data_ptr(), 20, 0, 0.0, None)
+    assert st == _lib.QMLG_E_ARG
+    assert np.array_equal(matern_kernel(A, A[:7], 1000.0, order=3, metric="l2"),
+                          matern_kernel(A, A[:7], 1000.0, order=2, metric="l2"))
+    assert np.array_equal(sargan_kernel(A, A[:7], 1000.0, []), laplacian_kernel(A, A[:7], 1000.0))
+    with pytest.raises(SystemExit):
+        matern_kernel(A, A, 1000.0, order=3, metric="l1")
+    with pytest.raises(SystemExit):
+        matern_kernel(A, A, 1000.0, metric="l3")

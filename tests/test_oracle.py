@@ -4,7 +4,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import load_golden
+from conftest import load_golden, more_kernel_inputs
 from qml_gb300.synthetic import generate_molecules
 
 REF = "/root/reference"
@@ -66,6 +66,37 @@ def test_kernel_oracle_matches_reference_test(oracle):
     Ks = oracle.gaussian_kernel(g["X"], g["X"], float(g["sigma"]))
     assert np.allclose(Ks, Ks.T)
     assert K.flags.f_contiguous
+
+
+def _close(K, expect):
+    # the reference test's bar (allclose) and this build's (1e-12 relative)
+    return np.allclose(K, expect) and float(np.max(np.abs(K / expect - 1))) < 1e-12
+
+
+def test_more_kernel_oracles_match_reference_tests(oracle):
+    # tests/test_kernels.py:93-214: linear, Matern (L1 through the Sargan mapping of
+    # qml/kernels.py:187-200, L2) and Sargan, on the same seeded inputs
+    g = load_golden("kernels_more_seed666.npz")
+    inp = more_kernel_inputs()
+    s = float(g["sigma"])
+    X, Xs = inp["linear"]
+    K = oracle.linear_kernel(X, Xs)
+    assert K.flags.f_contiguous and _close(K, g["linear"])
+    l1_map = {0: ([], 1.0), 1: ([1.0], np.sqrt(3)), 2: ([1.0, 1 / 3.0], np.sqrt(5))}
+    for order in (0, 1, 2):
+        X, Xs = inp["matern_l2_%d" % order]
+        assert _close(oracle.matern_kernel_l2(X, Xs, s, order), g["matern_l2_%d" % order])
+        X, Xs = inp["matern_l1_%d" % order]
+        gam, div = l1_map[order]
+        assert _close(oracle.sargan_kernel(X, Xs, s / div, gam), g["matern_l1_%d" % order])
+    for ng in (0, 1, 2):
+        X, Xs = inp["sargan_%d" % ng]
+        gam = inp["sargan_%d_gammas" % ng]
+        assert np.array_equal(gam, g["sargan_%d_gammas" % ng])
+        assert _close(oracle.sargan_kernel(X, Xs, s, gam), g["sargan_%d" % ng])
+    # the Fortran's third Matern branch takes every other order
+    X, Xs = inp["matern_l2_2"]
+    assert np.array_equal(oracle.matern_kernel_l2(X, Xs, s, 5), oracle.matern_kernel_l2(X, Xs, s, 2))
 
 
 def test_cho_solve_oracle_matches_reference_test(oracle):
