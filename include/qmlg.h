@@ -94,6 +94,34 @@ int qmlg_coulomb_matrix(const double *charges, const double *coordinates,
                         const int64_t *atom_offsets, int n_mol, int size, int sorting,
                         double *out, int *status, void *stream);
 
+/*
+ * Atomic (local) Coulomb matrices: one row of size*(size+1)/2 per central atom.
+ * Replaces fgenerate_local_coulomb_matrix (sorting 1, "row-norm",
+ * qml/frepresentations.f90:207-415) and fgenerate_atomic_coulomb_matrix (sorting
+ * 0, "distance", :417-595), bound by
+ * qml.representations.generate_atomic_coulomb_matrix (qml/representations.py:121-230),
+ * which handles one molecule per call.
+ *   atom_offsets    [n_mol + 1]  molecule m owns atoms offsets[m] .. offsets[m+1]-1
+ *   central_offsets [n_mol + 1], central_atoms [n_central]: the central atoms of
+ *                   molecule m (indices within the molecule) are
+ *                   central_atoms[central_offsets[m] .. central_offsets[m+1]-1];
+ *                   both NULL: every atom is central (n_central = total atoms)
+ *   out             [n_central * size*(size+1)/2], rows in central-atom order
+ *   cutoffs/decays  as the reference: negative = none; adjusted like :254-271
+ *   status          [1] device int: QMLG_E_TOO_MANY_ATOMS if a molecule has more
+ *                   than 32 atoms or more than `size` atoms within the central
+ *                   cutoff (the reference stops there), QMLG_E_ARG for a bad
+ *                   central index; may be NULL
+ * Where no cutoff mask applies the values and the atom order are the reference's
+ * arithmetic bit for bit (no FMA contraction, Z^2.4 from the host table).
+ */
+int qmlg_atomic_coulomb_matrix(const double *charges, const double *coordinates,
+                               const int64_t *atom_offsets, int n_mol,
+                               const int64_t *central_offsets, const int *central_atoms,
+                               int n_central, int size, int sorting, double central_cutoff,
+                               double central_decay, double interaction_cutoff,
+                               double interaction_decay, double *out, int *status, void *stream);
+
 /* ---- kernel matrices ----------------------------------------------------- */
 
 #define QMLG_KERNEL_SYMMETRIC 1   /* A == B: compute one triangle, mirror it */
@@ -150,6 +178,22 @@ int qmlg_matern_kernel_l2(const double *A, int64_t lda, int na, const double *B,
 int qmlg_sargan_kernel(const double *A, int64_t lda, int na, const double *B, int64_t ldb, int nb,
                        int d, double sigma, const double *gammas, int ngammas, double *K,
                        int64_t ldk, int flags, double diag_shift, void *stream);
+
+/*
+ * Local (atomic) kernels, kind 0 Gaussian / 1 Laplacian, for several sigmas:
+ *   K[s + nsigmas*(a + nm1*b)] = sum_{i in molecule a} sum_{j in molecule b}
+ *                                exp(-|A_i - B_j|_2^2 / (2 sigma_s^2))  (Gaussian)
+ *                                exp(-|A_i - B_j|_1 / sigma_s)          (Laplacian)
+ * A, B: atom rows (lda, ldb >= d) grouped by molecule through offsets_a [nm1 + 1]
+ * and offsets_b [nm2 + 1]; sigmas: device array; K: nsigmas x nm1 x nm2 with sigma
+ * fastest (the reference's Fortran-ordered (nsigmas, nm1, nm2)).  Replaces
+ * fget_local_kernels_gaussian / _laplacian (qml/fkernels.f90:23-196), bound by
+ * qml.kernels.get_local_kernels_* (qml/kernels.py:218-299).  FP64 arithmetic.
+ * flags: QMLG_KERNEL_SYMMETRIC (A == B, same offsets) computes b >= a and mirrors.
+ */
+int qmlg_local_kernels(int kind, const double *A, int64_t lda, const int64_t *offsets_a, int nm1,
+                       const double *B, int64_t ldb, const int64_t *offsets_b, int nm2, int d,
+                       const double *sigmas, int nsigmas, double *K, int flags, void *stream);
 
 /*
  * Gaussian kernel with the contraction a.b emulated to FP64 accuracy on the bf16

@@ -71,6 +71,14 @@ def _load():
         lib.oracle_sargan_kernel.argtypes = [_dp, ctypes.c_int, _dp, ctypes.c_int, ctypes.c_int,
                                              ctypes.c_double, _dp, ctypes.c_int, _dp]
         lib.oracle_sargan_kernel.restype = None
+        _ip = ctypes.POINTER(ctypes.c_int)
+        lib.oracle_atomic_cm.argtypes = [_dp, _dp, ctypes.c_int, _ip, ctypes.c_int, ctypes.c_int,
+                                         ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                         ctypes.c_double, ctypes.c_double, _dp]
+        lib.oracle_atomic_cm.restype = ctypes.c_int
+        lib.oracle_local_kernels.argtypes = [ctypes.c_int, _dp, _ip, ctypes.c_int, _dp, _ip,
+                                             ctypes.c_int, ctypes.c_int, _dp, ctypes.c_int, _dp]
+        lib.oracle_local_kernels.restype = None
         lib.oracle_residual_dd.argtypes = [_dp, ctypes.c_int, ctypes.c_int64, ctypes.c_double,
                                            _dp, _dp, _dp]
         lib.oracle_residual_dd.restype = None
@@ -146,6 +154,43 @@ def cm_sorted_numpy(charges, coordinates, size=23):
         for b in range(a + 1):
             out[base + b] = m[order[a], order[b]]
     return out
+
+
+def atomic_cm(charges, coordinates, central=None, size=23, sorting="distance",
+              central_cutoff=1e6, central_decay=-1.0, interaction_cutoff=1e6,
+              interaction_decay=-1.0):
+    """Atomic Coulomb matrices of one molecule, one row per central atom (0-based
+    indices, default all), like generate_atomic_coulomb_matrix (qml/representations.py:
+    121-230) with sorting "row-norm" or "distance"."""
+    z = np.ascontiguousarray(charges, dtype=np.float64)
+    r = np.ascontiguousarray(coordinates, dtype=np.float64).reshape(-1, 3)
+    if central is None:
+        central = np.arange(z.shape[0])
+    c = np.ascontiguousarray(central, dtype=np.int32).reshape(-1)
+    out = np.zeros((c.shape[0], size * (size + 1) // 2))
+    st = _load().oracle_atomic_cm(_ptr(z), _ptr(r), z.shape[0], _ptr(c, ctypes.POINTER(ctypes.c_int)),
+                                  c.shape[0], size, 1 if sorting == "row-norm" else 0,
+                                  float(central_cutoff), float(central_decay),
+                                  float(interaction_cutoff), float(interaction_decay), _ptr(out))
+    if st != 0:
+        raise ValueError("atomic Coulomb matrix: bad central index or too many atoms within the cutoff")
+    return out
+
+
+def local_kernels(kind, A, B, na, nb, sigmas):
+    """get_local_kernels_gaussian / _laplacian (qml/kernels.py:218-299): shape
+    (nsigmas, len(na), len(nb))."""
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    B = np.ascontiguousarray(B, dtype=np.float64)
+    n1 = np.ascontiguousarray(na, dtype=np.int32)
+    n2 = np.ascontiguousarray(nb, dtype=np.int32)
+    sg = np.ascontiguousarray(sigmas, dtype=np.float64).reshape(-1)
+    K = np.zeros((sg.shape[0], n1.shape[0], n2.shape[0]), order="F")
+    ip = ctypes.POINTER(ctypes.c_int)
+    _load().oracle_local_kernels(0 if kind == "gaussian" else 1, _ptr(A), _ptr(n1, ip), n1.shape[0],
+                                 _ptr(B), _ptr(n2, ip), n2.shape[0], A.shape[1], _ptr(sg),
+                                 sg.shape[0], _ptr(K))
+    return K
 
 
 def gaussian_kernel(A, B, sigma):

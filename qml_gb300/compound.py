@@ -1,14 +1,11 @@
-"""Minimal drop-in for qml.Compound's XYZ reading and Coulomb matrix
-(qml/compound.py:38-105, read_xyz at :296-326)."""
+"""Minimal drop-in for qml.Compound's XYZ reading and Coulomb matrices
+(qml/compound.py:38-105 and :134-216, read_xyz at :296-326)."""
 from __future__ import annotations
 
 import numpy as np
 
-from .representations import generate_coulomb_matrix
-
-NUCLEAR_CHARGE = {"H": 1, "He": 2, "Li": 3, "Be": 4, "B": 5, "C": 6, "N": 7, "O": 8, "F": 9,
-                  "Ne": 10, "Na": 11, "Mg": 12, "Al": 13, "Si": 14, "P": 15, "S": 16, "Cl": 17,
-                  "Ar": 18, "K": 19, "Ca": 20, "Br": 35, "I": 53}
+from .representations import (NUCLEAR_CHARGE, generate_atomic_coulomb_matrix,
+                              generate_coulomb_matrix)
 
 
 class Compound:
@@ -42,3 +39,14 @@ class Compound:
     def generate_coulomb_matrix(self, size=23, sorting="row-norm"):
         self.representation = generate_coulomb_matrix(self.nuclear_charges, self.coordinates,
                                                       size=size, sorting=sorting)
+
+    def generate_atomic_coulomb_matrix(self, size=23, sorting="row-norm", central_cutoff=1e6,
+                                       central_decay=-1, interaction_cutoff=1e6,
+                                       interaction_decay=-1, indices=None):
+        """Atomic Coulomb matrices of this molecule (note: the method defaults to
+        "row-norm" sorting, the module function to "distance", as in the reference)."""
+        self.representation = generate_atomic_coulomb_matrix(
+            self.nuclear_charges, self.coordinates, size=size, sorting=sorting,
+            central_cutoff=central_cutoff, central_decay=central_decay,
+            interaction_cutoff=interaction_cutoff, interaction_decay=interaction_decay,
+            indices=indices)

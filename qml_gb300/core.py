@@ -92,6 +92,76 @@ def coulomb_matrix_batch(charges: torch.Tensor, coordinates: torch.Tensor,
     return out
 
 
+def atomic_coulomb_matrix_batch(charges: torch.Tensor, coordinates: torch.Tensor,
+                                offsets: torch.Tensor, size: int = 23,
+                                sorting: str = "distance", central_cutoff: float = 1e6,
+                                central_decay: float = -1.0, interaction_cutoff: float = 1e6,
+                                interaction_decay: float = -1.0,
+                                central_offsets: Optional[torch.Tensor] = None,
+                                central_atoms: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """Atomic Coulomb matrices of a ragged batch: one row per central atom (every
+    atom, or central_atoms grouped by central_offsets), (n_central,
+    size*(size+1)//2) float64 on the GPU.  sorting "row-norm" or "distance"."""
+    if sorting not in ("row-norm", "distance"):
+        raise ValueError("Unknown sorting scheme requested: %r" % (sorting,))
+    _require_cuda(charges, coordinates, offsets)
+    charges = charges.contiguous()
+    coordinates = coordinates.contiguous()
+    offsets = offsets.to(torch.int64).contiguous()
+    n_mol = offsets.shape[0] - 1
+    if central_atoms is None:
+        n_central = int(charges.shape[0])
+        co = ca = None
+    else:
+        central_offsets = central_offsets.to(device=charges.device, dtype=torch.int64).contiguous()
+        central_atoms = central_atoms.to(device=charges.device, dtype=torch.int32).contiguous()
+        n_central = int(central_atoms.shape[0])
+        co, ca = central_offsets.data_ptr(), central_atoms.data_ptr()
+    out = torch.empty((n_central, size * (size + 1) // 2), dtype=torch.float64,
+                      device=charges.device)
+    status = torch.zeros(1, dtype=torch.int32, device=charges.device)
+    check(lib().qmlg_atomic_coulomb_matrix(charges.data_ptr(), coordinates.data_ptr(),
+                                           offsets.data_ptr(), n_mol, co, ca, n_central, size,
+                                           1 if sorting == "row-norm" else 0,
+                                           float(central_cutoff), float(central_decay),
+                                           float(interaction_cutoff), float(interaction_decay),
+                                           out.data_ptr(), status.data_ptr(),
+                                           _stream(charges.device)),
+          "qmlg_atomic_coulomb_matrix")
+    torch.cuda.current_stream(charges.device).synchronize()
+    st = int(status.item())
+    if st != 0:
+        _lib.check(st, "qmlg_atomic_coulomb_matrix")
+    return out
+
+
+def local_kernels(kind: str, A: torch.Tensor, B: torch.Tensor, offsets_a: torch.Tensor,
+                  offsets_b: torch.Tensor, sigmas, symmetric: bool = False) -> torch.Tensor:
+    """Local kernels (nsigmas, nm1, nm2) float64 on the GPU (a Fortran-ordered view)
+    for atom rows A, B grouped by molecule offsets.  kind "gaussian" or "laplacian"."""
+    if kind not in ("gaussian", "laplacian"):
+        raise ValueError("unknown local kernel %r" % (kind,))
+    _require_cuda(A, B)
+    A, lda = _rows(A)
+    if symmetric:
+        B, ldb, offsets_b = A, lda, offsets_a
+    else:
+        B, ldb = _rows(B)
+    if A.shape[1] != B.shape[1]:
+        raise ValueError("A and B have different representation sizes")
+    offsets_a = offsets_a.to(device=A.device, dtype=torch.int64).contiguous()
+    offsets_b = offsets_a if symmetric else offsets_b.to(device=A.device, dtype=torch.int64).contiguous()
+    sg = torch.as_tensor(sigmas, dtype=torch.float64).reshape(-1).to(A.device).contiguous()
+    nm1, nm2, ns = offsets_a.shape[0] - 1, offsets_b.shape[0] - 1, sg.shape[0]
+    buf = torch.zeros((nm2, nm1, ns), dtype=torch.float64, device=A.device)
+    check(lib().qmlg_local_kernels(0 if kind == "gaussian" else 1, A.data_ptr(), lda,
+                                   offsets_a.data_ptr(), nm1, B.data_ptr(), ldb,
+                                   offsets_b.data_ptr(), nm2, A.shape[1], sg.data_ptr(), ns,
+                                   buf.data_ptr(), _lib.QMLG_KERNEL_SYMMETRIC if symmetric else 0,
+                                   _stream(A.device)), "qmlg_local_kernels")
+    return buf.permute(2, 1, 0)
+
+
 def coulomb_matrix_batch_async(charges: torch.Tensor, coordinates: torch.Tensor,
                                offsets: torch.Tensor, size: int = 23, sorting: str = "row-norm",
                                status: Optional[torch.Tensor] = None) -> torch.Tensor:

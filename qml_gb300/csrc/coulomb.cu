@@ -130,6 +130,212 @@ coulomb_kernel(const double *__restrict__ charges, const double *__restrict__ co
     for (int64_t e = filled + lane; e < len; e += 32) dst[e] = 0.0;
 }
 
+// ------------------------------------------------------------ atomic CM --
+//
+// Atomic (local) Coulomb matrices, one warp per central atom, restating
+// fgenerate_local_coulomb_matrix ("row-norm", qml/frepresentations.f90:207-415) and
+// fgenerate_atomic_coulomb_matrix ("distance", :417-595) in their single-thread
+// arithmetic order, with no FMA contraction:
+//   D_ij = sqrt((dx*dx + dy*dy) + dz*dz); count_i = 1 + #{j != i: D_ij < cc};
+//   masks applied as pref = 0.5 (cos(pi (d - c + w)/w) + 1) and p = (p 0.5)(cos + 1);
+//   row-norm: lane r adds its row norm's terms in the order the reference's loop
+//     does (pairs (i, r), i < r; the diagonal; pairs (r, j), j > r), so the order
+//     of the selection (first index of the maximum, the central atom first) is the
+//     reference's; distance: first index of the minimum distance to the central atom.
+// Lane i owns atom i (molecules of at most 32 atoms).  Bit-identical to the
+// reference arithmetic where no cutoff mask applies (the default cutoffs); inside
+// the mask the device cos can differ from the host's in the last bits.
+constexpr int kAcmWarps = 2;
+
+struct AcmParams {
+    double cc, cd, ic, id;  // adjusted central / interaction cutoff and decay
+    int size, sorting;
+};
+
+__device__ __forceinline__ double acm_cos1(double d, double c, double w)
+{
+    const double pi = 3.141592653589793;  // 4 atan(1) in FP64
+    return __dadd_rn(cos(__ddiv_rn(__dmul_rn(pi, __dadd_rn(__dsub_rn(d, c), w)), w)), 1.0);
+}
+
+__device__ __forceinline__ double acm_pref(double dik, const AcmParams &q)
+{
+    return dik > q.cc - q.cd ? __dmul_rn(0.5, acm_cos1(dik, q.cc, q.cd)) : 1.0;
+}
+
+__global__ void __launch_bounds__(kAcmWarps * 32)
+atomic_cm_kernel(const double *__restrict__ charges, const double *__restrict__ coords,
+                 const int64_t *__restrict__ offsets, int n_mol,
+                 const int64_t *__restrict__ central_offsets, const int *__restrict__ central,
+                 int n_central, AcmParams q, double *__restrict__ out, int *__restrict__ status)
+{
+    __shared__ double sD[kAcmWarps][kMaxAtoms][kMaxAtoms + 1];
+    __shared__ double sP[kAcmWarps][kMaxAtoms][kMaxAtoms + 1];
+    __shared__ int sOrd[kAcmWarps][kMaxAtoms];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int task = blockIdx.x * kAcmWarps + warp;
+    if (task >= n_central) return;
+    const int64_t len = (int64_t)q.size * (q.size + 1) / 2;
+    double *dst = out + (int64_t)task * len;
+    // molecule of this central atom: last m with coff[m] <= task
+    const int64_t *coff = central_offsets != nullptr ? central_offsets : offsets;
+    int lo = 0, hi = n_mol - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (coff[mid] <= task) lo = mid;
+        else hi = mid - 1;
+    }
+    const int mol = lo;
+    const int64_t first = offsets[mol];
+    const int natoms = (int)(offsets[mol + 1] - first);
+    const int k = central != nullptr ? central[task] : (int)(task - coff[mol]);
+    for (int64_t e = lane; e < len; e += 32) dst[e] = 0.0;
+    if (natoms > kMaxAtoms || natoms < 1 || k < 0 || k >= natoms) {
+        if (lane == 0 && status != nullptr) atomicMin(status, natoms > kMaxAtoms ? QMLG_E_TOO_MANY_ATOMS : QMLG_E_ARG);
+        return;
+    }
+    const bool live = lane < natoms;
+    double z = 0.0, x = 0.0, y = 0.0, w = 0.0;
+    if (live) {
+        z = charges[first + lane];
+        x = coords[3 * (first + lane) + 0];
+        y = coords[3 * (first + lane) + 1];
+        w = coords[3 * (first + lane) + 2];
+    }
+    double zp = 0.0;
+    const int zi = (int)z;
+    if ((double)zi == z && zi >= 0 && zi < kZTable) zp = c_zpow[zi];
+    else zp = pow(z, 2.4);
+    // distances and cutoff counts
+    int cnt = 1;
+    for (int j = 0; j < natoms; ++j) {
+        const double xj = __shfl_sync(0xffffffffu, x, j);
+        const double yj = __shfl_sync(0xffffffffu, y, j);
+        const double wj = __shfl_sync(0xffffffffu, w, j);
+        if (!live) continue;
+        double dd = 0.0;
+        if (j != lane) {
+            const double dx = __dsub_rn(xj, x), dy = __dsub_rn(yj, y), dz = __dsub_rn(wj, w);
+            double s2 = __dmul_rn(dx, dx);
+            s2 = __dadd_rn(s2, __dmul_rn(dy, dy));
+            s2 = __dadd_rn(s2, __dmul_rn(dz, dz));
+            dd = __dsqrt_rn(s2);
+            if (dd < q.cc) ++cnt;
+        }
+        sD[warp][lane][j] = dd;
+    }
+    __syncwarp();
+    const int cntk = __shfl_sync(0xffffffffu, cnt, k);
+    if (cntk > q.size) {
+        if (lane == 0 && status != nullptr) atomicMin(status, QMLG_E_TOO_MANY_ATOMS);
+        return;
+    }
+    const double dk = live ? sD[warp][lane][k] : 0.0;  // this atom's distance to the centre
+    if (q.sorting == 1) {
+        // pair value P(a, b), a < b, as the reference's loop forms it (0 when skipped)
+        auto pair = [&](int a, int b, double za, double zb) -> double {
+            const double dak = sD[warp][a][k], dbk = sD[warp][b][k], dab = sD[warp][a][b];
+            if (dak > q.cc || dbk > q.cc || dab > q.ic) return 0.0;
+            double pn = __ddiv_rn(__dmul_rn(__dmul_rn(acm_pref(dak, q), za), zb), sD[warp][b][a]);
+            if (dab > q.ic - q.id) pn = __dmul_rn(__dmul_rn(pn, 0.5), acm_cos1(dab, q.ic, q.id));
+            if (dbk > q.cc - q.cd) pn = __dmul_rn(__dmul_rn(pn, 0.5), acm_cos1(dbk, q.cc, q.cd));
+            return pn;
+        };
+        double rn = 0.0;
+        for (int i = 0; i < natoms; ++i) {
+            const double zo = __shfl_sync(0xffffffffu, z, i);
+            if (!live) continue;
+            double p;
+            if (i < lane) {
+                p = pair(i, lane, zo, z);
+                if (sD[warp][i][k] <= q.cc && dk <= q.cc && sD[warp][i][lane] <= q.ic)
+                    rn = __dadd_rn(rn, __dmul_rn(p, p));
+            } else if (i == lane) {
+                p = 0.0;
+                if (dk <= q.cc) {
+                    const double pr = acm_pref(dk, q);
+                    p = __dmul_rn(__dmul_rn(__dmul_rn(pr, pr), 0.5), zp);
+                    rn = __dadd_rn(rn, __dmul_rn(p, p));
+                }
+            } else {
+                p = pair(lane, i, z, zo);
+                if (dk <= q.cc && sD[warp][i][k] <= q.cc && sD[warp][lane][i] <= q.ic)
+                    rn = __dadd_rn(rn, __dmul_rn(p, p));
+            }
+            sP[warp][lane][i] = p;
+        }
+        double key = live ? (lane == k ? DBL_MAX : rn) : -INFINITY;
+        for (int m = 0; m < cntk; ++m) {
+            double bv = key;
+            int bi = lane;
+            for (int off = 16; off > 0; off >>= 1) {
+                const double ov = __shfl_xor_sync(0xffffffffu, bv, off);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+                if (ov > bv || (ov == bv && oi < bi)) {
+                    bv = ov;
+                    bi = oi;
+                }
+            }
+            if (lane == 0) sOrd[warp][m] = bi;
+            if (lane == bi) key = 0.0;
+        }
+        __syncwarp();
+        for (int m = 0; m < cntk; ++m) {
+            const int idx = (m * m + m) / 2, a = sOrd[warp][m];
+            for (int n = lane; n <= m; n += 32) dst[idx + n] = sP[warp][a][sOrd[warp][n]];
+        }
+    } else {
+        // centre-independent pair matrix
+        for (int j = 0; j < natoms; ++j) {
+            const double zo = __shfl_sync(0xffffffffu, z, j);
+            if (!live) continue;
+            double p;
+            if (j == lane) {
+                p = __dmul_rn(0.5, zp);
+            } else {
+                const double dij = sD[warp][lane][j];
+                p = 0.0;
+                if (!(dij > q.ic)) {
+                    const double za = j < lane ? zo : z, zb = j < lane ? z : zo;
+                    p = __ddiv_rn(__dmul_rn(za, zb), dij);
+                    if (dij > q.ic - q.id) p = __dmul_rn(__dmul_rn(p, 0.5), acm_cos1(dij, q.ic, q.id));
+                }
+            }
+            sP[warp][lane][j] = p;
+        }
+        double key = live ? dk : INFINITY;
+        for (int m = 0; m < cntk; ++m) {
+            double bv = key;
+            int bi = lane;
+            for (int off = 16; off > 0; off >>= 1) {
+                const double ov = __shfl_xor_sync(0xffffffffu, bv, off);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+                if (ov < bv || (ov == bv && oi < bi)) {
+                    bv = ov;
+                    bi = oi;
+                }
+            }
+            if (lane == 0) sOrd[warp][m] = bi;
+            if (lane == bi) key = DBL_MAX;
+        }
+        __syncwarp();
+        for (int m = 0; m < cntk; ++m) {
+            const int i = sOrd[warp][m];
+            const double dik = sD[warp][i][k];
+            if (dik > q.cc) continue;
+            const double pr = acm_pref(dik, q);
+            const int idx = (m * m + m) / 2;
+            for (int n = lane; n <= m; n += 32) {
+                const int j = sOrd[warp][n];
+                double pn = __dmul_rn(pr, sP[warp][i][j]);
+                const double djk = sD[warp][j][k];
+                if (djk > q.cc - q.cd) pn = __dmul_rn(__dmul_rn(pn, 0.5), acm_cos1(djk, q.cc, q.cd));
+                dst[idx + n] = pn;
+            }
+        }
+    }
+}
+
 std::once_flag g_table_once;
 int g_table_status = QMLG_OK;
 
@@ -158,5 +364,39 @@ extern "C" int qmlg_coulomb_matrix(const double *charges, const double *coordina
     const int blocks = (int)qmlg::ceil_div(n_mol, kWarpsPerBlock);
     { coulomb_kernel<<<blocks, kWarpsPerBlock * 32, 0, qmlg::as_stream(stream)>>>(
         charges, coordinates, atom_offsets, n_mol, size, sorting ? 1 : 0, out, status); qmlg::count_launches(1); }
+    return qmlg::check_launch();
+}
+
+extern "C" int qmlg_atomic_coulomb_matrix(const double *charges, const double *coordinates,
+                                          const int64_t *atom_offsets, int n_mol,
+                                          const int64_t *central_offsets, const int *central_atoms,
+                                          int n_central, int size, int sorting,
+                                          double central_cutoff, double central_decay,
+                                          double interaction_cutoff, double interaction_decay,
+                                          double *out, int *status, void *stream)
+{
+    if (n_mol < 0 || n_central < 0 || size < 1 || (sorting != 0 && sorting != 1)) return QMLG_E_ARG;
+    if (n_mol == 0 || n_central == 0) return QMLG_OK;
+    if (atom_offsets == nullptr || out == nullptr || charges == nullptr || coordinates == nullptr)
+        return QMLG_E_ARG;
+    if ((central_offsets == nullptr) != (central_atoms == nullptr)) return QMLG_E_ARG;
+    int st = upload_table();
+    if (st != QMLG_OK) return st;
+    // the reference's cutoff adjustments (qml/frepresentations.f90:254-271)
+    AcmParams q;
+    const double huge = DBL_MAX;
+    q.cc = central_cutoff < 0 ? huge : central_cutoff;
+    q.ic = (interaction_cutoff < 0 || interaction_cutoff > 2 * q.cc) ? 2 * q.cc : interaction_cutoff;
+    q.cd = central_decay < 0 ? 0.0 : (central_decay > q.cc ? q.cc : central_decay);
+    q.id = interaction_decay < 0 ? 0.0 : (interaction_decay > q.ic ? q.ic : interaction_decay);
+    q.size = size;
+    q.sorting = sorting;
+    const int blocks = (int)qmlg::ceil_div(n_central, kAcmWarps);
+    {
+        atomic_cm_kernel<<<blocks, kAcmWarps * 32, 0, qmlg::as_stream(stream)>>>(
+            charges, coordinates, atom_offsets, n_mol, central_offsets, central_atoms, n_central, q,
+            out, status);
+        qmlg::count_launches(1);
+    }
     return qmlg::check_launch();
 }

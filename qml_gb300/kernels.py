@@ -1,5 +1,6 @@
-"""Drop-ins for the global kernels of qml.kernels (qml/kernels.py:36-215):
-gaussian_kernel, laplacian_kernel, linear_kernel, sargan_kernel, matern_kernel.
+"""Drop-ins for qml.kernels (qml/kernels.py:36-299): gaussian_kernel,
+laplacian_kernel, linear_kernel, sargan_kernel, matern_kernel and the local kernels
+get_local_kernels_gaussian / get_local_kernels_laplacian.
 
 Host arrays in, a Fortran-ordered (na, nb) float64 ndarray out, exactly like the
 reference; the matrix is computed on the GPU (qmlg_gaussian_kernel,
@@ -81,3 +82,35 @@ def matern_kernel(A, B, sigma, order=0, metric="l1"):
         raise SystemExit
     # the reference's Fortran takes every order other than 0 and 1 as order 2
     return _kernel("matern_l2", A, B, sigma, order=order if order in (0, 1) else 2)
+
+
+def _local(kind, A, B, na, nb, sigmas):
+    A = np.asarray(A, dtype=np.float64)
+    B = np.asarray(B, dtype=np.float64)
+    assert np.sum(na) == A.shape[0], "Error in A input"
+    assert np.sum(nb) == B.shape[0], "Error in B input"
+    assert A.shape[1] == B.shape[1], "Error in representation sizes"
+    same = B is A or (A.shape == B.shape and np.shares_memory(A, B) and np.array_equal(A, B))
+    na = np.asarray(na, dtype=np.int64).reshape(-1)
+    nb = np.asarray(nb, dtype=np.int64).reshape(-1)
+    same = same and np.array_equal(na, nb)
+    At = _to_dev(A)
+    Bt = At if same else _to_dev(B)
+    oa = torch.from_numpy(np.concatenate([[0], np.cumsum(na)]).astype(np.int64))
+    ob = torch.from_numpy(np.concatenate([[0], np.cumsum(nb)]).astype(np.int64))
+    K = core.local_kernels(kind, At, Bt, oa, ob, np.asarray(sigmas, dtype=np.float64),
+                           symmetric=same)
+    return np.asfortranarray(K.cpu().numpy())
+
+
+def get_local_kernels_gaussian(A, B, na, nb, sigmas):
+    """K[s, i, j] = sum_{a in i} sum_{b in j} exp(-|A_a - B_b|_2^2 / (2 sigma_s^2)),
+    shape (nsigmas, len(na), len(nb)); atom rows concatenated by molecule
+    (qml/kernels.py:218-257)."""
+    return _local("gaussian", A, B, na, nb, sigmas)
+
+
+def get_local_kernels_laplacian(A, B, na, nb, sigmas):
+    """K[s, i, j] = sum_{a in i} sum_{b in j} exp(-|A_a - B_b|_1 / sigma_s)
+    (qml/kernels.py:259-299)."""
+    return _local("laplacian", A, B, na, nb, sigmas)

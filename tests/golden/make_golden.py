@@ -14,6 +14,16 @@ Outputs (small .npz files, committed):
   kernels_seed666.npz   the inputs of tests/test_kernels.py:34-90 (np.random.seed(666),
                         X = rand(25, 1000), Xs = rand(20, 1000), sigma = 100) with the
                         reference test's own NumPy-loop expectations
+  atomic_cm_qm7_0101_0110.npz
+                        the reference's atomic Coulomb-matrix known answers
+                        (tests/test_representations.py:92-158) for the same ten
+                        molecules: distance- and row-norm-sorted, with and without the
+                        soft cutoffs (central 4.0/0.5, interaction 5.0/1.0), from
+                        tests/data/atomic_coulomb_matrix_representation_*.txt
+  local_krr_qm7.npz     the atomic-CM KRR tests (tests/test_energy_krr_atomic_cmat.py):
+                        the 200 training and 100 test molecules that the test's seed-666
+                        shuffle of the first 1000 sorted QM7 names selects (Z, R, heats
+                        of formation) and tests/data/K_local_*.txt, Ks_local_*.txt
   kernels_more_seed666.npz
                         the NumPy-loop expectations of tests/test_kernels.py:93-214
                         (linear, Matern and Sargan kernels) and the Sargan gammas; the
@@ -70,6 +80,43 @@ def main(ref):
     np.savez_compressed(os.path.join(here, "kernels_seed666.npz"), X=X, Xs=Xs, sigma=sigma,
                         laplacian=kl, gaussian=kg)
     more_kernels(here)
+    atomic(ref, here)
+    local_krr(ref, here)
+
+
+def atomic(ref, here):
+    d = os.path.join(ref, "tests", "data")
+    names = ["distance_sorted", "distance_sorted_no_indices", "row-norm_sorted",
+             "distance_sorted_with_cutoff", "row-norm_sorted_with_cutoff"]
+    np.savez_compressed(os.path.join(here, "atomic_cm_qm7_0101_0110.npz"),
+                        **{n: np.loadtxt(os.path.join(d, "atomic_coulomb_matrix_representation_%s.txt" % n))
+                           for n in names})
+
+
+def local_krr(ref, here):
+    energies = {}
+    with open(os.path.join(ref, "tests", "data", "hof_qm7.txt")) as f:
+        for line in f:
+            t = line.split()
+            energies[t[0]] = float(t[1])
+    names = sorted(energies.keys())[:1000]
+    idx = list(range(len(names)))
+    np.random.seed(666)
+    np.random.shuffle(idx)
+    sel = idx[:200] + idx[-100:]
+    mols = [read_xyz(os.path.join(ref, "tests", "qm7", names[k])) for k in sel]
+    counts = np.array([z.shape[0] for z, _ in mols], dtype=np.int64)
+    d = os.path.join(ref, "tests", "data")
+    np.savez_compressed(
+        os.path.join(here, "local_krr_qm7.npz"),
+        charges=np.concatenate([z for z, _ in mols]),
+        coordinates=np.concatenate([r for _, r in mols]),
+        offsets=np.concatenate([[0], np.cumsum(counts)]).astype(np.int64),
+        energies=np.array([energies[names[k]] for k in sel]),
+        K_gaussian=np.loadtxt(os.path.join(d, "K_local_gaussian.txt")),
+        Ks_gaussian=np.loadtxt(os.path.join(d, "Ks_local_gaussian.txt")),
+        K_laplacian=np.loadtxt(os.path.join(d, "K_local_laplacian.txt")),
+        Ks_laplacian=np.loadtxt(os.path.join(d, "Ks_local_laplacian.txt")))
 
 
 def more_kernel_inputs():

@@ -1,0 +1,132 @@
+"""Atomic Coulomb matrices and local kernels on the GPU against the oracle and the
+reference's fixtures (tests/test_representations.py:92-158,
+tests/test_energy_krr_atomic_cmat.py)."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import load_golden
+from test_oracle import ATOMIC_CUTOFFS, atomic_rows, local_krr_features
+from qml_gb300 import core
+from qml_gb300.compound import Compound
+from qml_gb300.kernels import get_local_kernels_gaussian, get_local_kernels_laplacian
+from qml_gb300.math import cho_solve
+from qml_gb300.representations import (generate_atomic_coulomb_matrix,
+                                       generate_atomic_coulomb_matrix_batch)
+from qml_gb300.synthetic import generate_molecules
+from qml_gb300.wrappers import get_atomic_kernels_gaussian, get_atomic_kernels_laplacian
+
+pytestmark = pytest.mark.gpu
+RTOL = 1e-12
+
+
+def relerr(a, b):
+    return float(np.max(np.abs(a - b) / np.abs(b)))
+
+
+def drop_in_rows(g, sorting, **kw):
+    z, r, off, size = g["charges"], g["coordinates"], g["offsets"], int(g["size"])
+    return np.concatenate([generate_atomic_coulomb_matrix(z[off[m]:off[m + 1]], r[off[m]:off[m + 1]],
+                                                          size=size, sorting=sorting, **kw)
+                           for m in range(len(off) - 1)])
+
+
+def test_atomic_cm_reference_fixtures(cuda, oracle):
+    # the reference's known answers through the drop-in; without cutoffs bit-identical
+    # to the oracle's restatement, with the soft cutoffs (device cos) within 1e-13
+    g = load_golden("cm_qm7_0101_0110.npz")
+    a = load_golden("atomic_cm_qm7_0101_0110.npz")
+    for name, sorting, kw in (("distance_sorted", "distance", {}),
+                              ("row-norm_sorted", "row-norm", {}),
+                              ("distance_sorted_with_cutoff", "distance", ATOMIC_CUTOFFS),
+                              ("row-norm_sorted_with_cutoff", "row-norm", ATOMIC_CUTOFFS)):
+        X = drop_in_rows(g, sorting, **kw)
+        assert np.allclose(X, a[name]), name
+        Xo = atomic_rows(oracle, g, sorting, **kw)
+        if kw:
+            assert np.max(np.abs(X - Xo)) <= 1e-13 * np.max(np.abs(Xo)), name
+        else:
+            assert np.array_equal(X, Xo), name
+
+
+def test_atomic_cm_indices(cuda, oracle):
+    g = load_golden("cm_qm7_0101_0110.npz")
+    z, r, off = g["charges"], g["coordinates"], g["offsets"]
+    for sorting in ("distance", "row-norm"):
+        for m in range(10):
+            zm, rm = z[off[m]:off[m + 1]], r[off[m]:off[m + 1]]
+            full = generate_atomic_coulomb_matrix(zm, rm, size=17, sorting=sorting)
+            sub = generate_atomic_coulomb_matrix(zm, rm, size=17, sorting=sorting, indices=[1, 2])
+            assert np.array_equal(sub, full[1:3])
+            carbons = generate_atomic_coulomb_matrix(zm, rm, size=17, sorting=sorting, indices="C")
+            assert np.array_equal(carbons, full[zm == 6])
+    zm, rm = z[off[0]:off[1]], r[off[0]:off[1]]
+    assert generate_atomic_coulomb_matrix(zm, rm, size=17, indices="Cl").shape == (0, 0)
+    with pytest.raises(SystemExit):
+        generate_atomic_coulomb_matrix(zm, rm, size=17, indices="Xx")
+    with pytest.raises(SystemExit):
+        generate_atomic_coulomb_matrix(zm, rm, size=17, sorting="eigen")
+    with pytest.raises(Exception):
+        generate_atomic_coulomb_matrix(zm, rm, size=3)  # more atoms in the cutoff than size
+
+
+@pytest.mark.parametrize("sorting", ["distance", "row-norm"])
+def test_atomic_cm_batch_bit_exact(cuda, oracle, sorting):
+    # one launch over a synthetic batch against the per-molecule oracle
+    b = generate_molecules(300, seed=11)
+    X = generate_atomic_coulomb_matrix_batch(b.charges, b.coordinates, b.offsets, size=23,
+                                             sorting=sorting).cpu().numpy()
+    Xo = np.concatenate([oracle.atomic_cm(*b.molecule(m), None, 23, sorting) for m in range(300)])
+    assert np.array_equal(X, Xo)
+
+
+def test_local_kernels_vs_oracle(cuda, oracle):
+    L = load_golden("local_krr_qm7.npz")
+    X, Xs, N, Ns = local_krr_features(oracle, L)
+    sigmas = [200.0, 724.0, 10 ** 3.6]
+    for kind, fn in (("gaussian", get_local_kernels_gaussian),
+                     ("laplacian", get_local_kernels_laplacian)):
+        K = fn(X, X, N, N, sigmas)
+        assert K.shape == (3, 200, 200) and K.flags.f_contiguous
+        assert relerr(K, oracle.local_kernels(kind, X, X, N, N, sigmas)) <= RTOL
+        for s in range(3):
+            assert np.array_equal(K[s], K[s].T)
+        Ks = fn(Xs, X, Ns, N, sigmas)
+        assert relerr(Ks, oracle.local_kernels(kind, Xs, X, Ns, N, sigmas)) <= RTOL
+
+
+def test_local_krr_reference_end_to_end(cuda):
+    # tests/test_energy_krr_atomic_cmat.py with every step on the GPU: atomic CMs
+    # through Compound, local kernels, the reference's fixtures and KRR errors
+    L = load_golden("local_krr_qm7.npz")
+    z, r, off = L["charges"], L["coordinates"], L["offsets"]
+    mols = []
+    for m in range(300):
+        c = Compound()
+        c.nuclear_charges = z[off[m]:off[m + 1]].astype(int)
+        c.coordinates = r[off[m]:off[m + 1]]
+        c.natoms = int(off[m + 1] - off[m])
+        c.generate_atomic_coulomb_matrix(size=23, sorting="row-norm")
+        mols.append(c)
+    training, test = mols[:200], mols[200:]
+    X = np.concatenate([m.representation for m in training])
+    Xs = np.concatenate([m.representation for m in test])
+    N = np.array([m.natoms for m in training])
+    Ns = np.array([m.natoms for m in test])
+    Y, Ys = L["energies"][:200], L["energies"][200:]
+    for kind, fn, wrap, sigma, lam, mae_ref in (
+            ("gaussian", get_local_kernels_gaussian, get_atomic_kernels_gaussian, 724.0,
+             10 ** (-6.5), 19.0),
+            ("laplacian", get_local_kernels_laplacian, get_atomic_kernels_laplacian, 10 ** 3.6,
+             10 ** (-12.0), 8.7)):
+        K = fn(X, X, N, N, [sigma])[0]
+        assert np.allclose(K, K.T) and np.allclose(K, L["K_" + kind])
+        assert np.allclose(K, wrap(training, training, [sigma])[0])
+        Ks = fn(Xs, X, Ns, N, [sigma])[0]
+        assert len(set(np.where(Ks - L["Ks_" + kind] > 1e-7)[0])) < 5
+        assert np.allclose(Ks, wrap(test, training, [sigma])[0])
+        K = np.ascontiguousarray(K)
+        K[np.diag_indices_from(K)] += lam
+        alpha = cho_solve(K, Y)
+        mae = np.mean(np.abs(Ys - Ks @ alpha))
+        assert abs(mae_ref - mae) < 1.0, (kind, mae)

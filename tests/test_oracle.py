@@ -99,6 +99,63 @@ def test_more_kernel_oracles_match_reference_tests(oracle):
     assert np.array_equal(oracle.matern_kernel_l2(X, Xs, s, 5), oracle.matern_kernel_l2(X, Xs, s, 2))
 
 
+ATOMIC_CUTOFFS = dict(central_cutoff=4.0, central_decay=0.5, interaction_cutoff=5.0,
+                      interaction_decay=1.0)
+
+
+def atomic_rows(oracle, g, sorting, central=None, **kw):
+    z, r, off, size = g["charges"], g["coordinates"], g["offsets"], int(g["size"])
+    return np.concatenate([oracle.atomic_cm(z[off[m]:off[m + 1]], r[off[m]:off[m + 1]], central,
+                                            size, sorting, **kw) for m in range(len(off) - 1)])
+
+
+def test_atomic_cm_oracle_matches_reference_fixtures(oracle):
+    # tests/test_representations.py:92-158 on qm7/0101..0110 (size 17)
+    g = load_golden("cm_qm7_0101_0110.npz")
+    a = load_golden("atomic_cm_qm7_0101_0110.npz")
+    for name, sorting, kw in (("distance_sorted", "distance", {}),
+                              ("distance_sorted_no_indices", "distance", {}),
+                              ("row-norm_sorted", "row-norm", {}),
+                              ("distance_sorted_with_cutoff", "distance", ATOMIC_CUTOFFS),
+                              ("row-norm_sorted_with_cutoff", "row-norm", ATOMIC_CUTOFFS)):
+        X = atomic_rows(oracle, g, sorting, **kw)
+        assert X.shape == a[name].shape and np.allclose(X, a[name]), name
+    # central-atom subsets are the matching rows of the full set
+    z, r, off = g["charges"], g["coordinates"], g["offsets"]
+    for sorting in ("distance", "row-norm"):
+        for m in range(10):
+            zm, rm = z[off[m]:off[m + 1]], r[off[m]:off[m + 1]]
+            full = oracle.atomic_cm(zm, rm, None, 17, sorting)
+            assert np.array_equal(oracle.atomic_cm(zm, rm, [1, 2], 17, sorting), full[1:3])
+
+
+def local_krr_features(oracle, L, sorting="row-norm"):
+    z, r, off = L["charges"], L["coordinates"], L["offsets"]
+    X = [oracle.atomic_cm(z[off[m]:off[m + 1]], r[off[m]:off[m + 1]], None, 23, sorting)
+         for m in range(len(off) - 1)]
+    n = np.array([x.shape[0] for x in X])
+    return np.concatenate(X[:200]), np.concatenate(X[200:]), n[:200], n[200:]
+
+
+def test_local_kernel_oracle_matches_reference_krr(oracle):
+    # tests/test_energy_krr_atomic_cmat.py: K vs K_local_*.txt (allclose), Ks vs
+    # Ks_local_*.txt (fewer than 5 molecules off by > 1e-7, the reference's
+    # allowance), and the KRR mean absolute errors
+    L = load_golden("local_krr_qm7.npz")
+    X, Xs, N, Ns = local_krr_features(oracle, L)
+    Y, Ys = L["energies"][:200], L["energies"][200:]
+    for kind, sigma, lam, mae_ref in (("gaussian", 724.0, 10 ** (-6.5), 19.0),
+                                      ("laplacian", 10 ** 3.6, 10 ** (-12.0), 8.7)):
+        K = oracle.local_kernels(kind, X, X, N, N, [sigma])[0]
+        assert np.allclose(K, K.T) and np.allclose(K, L["K_" + kind])
+        Ks = oracle.local_kernels(kind, Xs, X, Ns, N, [sigma])[0]
+        assert len(set(np.where(Ks - L["Ks_" + kind] > 1e-7)[0])) < 5
+        K[np.diag_indices_from(K)] += lam
+        alpha = oracle.cho_solve(K, Y)
+        mae = np.mean(np.abs(Ys - Ks @ alpha))
+        assert abs(mae_ref - mae) < 1.0, (kind, mae)
+
+
 def test_cho_solve_oracle_matches_reference_test(oracle):
     # tests/test_math.py:32-52
     g = load_golden("cho_solve_k_local_gaussian.npz")
