@@ -53,6 +53,8 @@ def parse():
     p.add_argument("--serve-seconds", type=float, default=10.0)
     p.add_argument("--serve-fit-every", type=int, default=50, help="every k-th arrival is a fit")
     p.add_argument("--no-batching", action="store_true", help="skip the batched-fits measurement")
+    p.add_argument("--no-extra", action="store_true",
+                   help="skip the atomic-CM / local-kernel measurement")
     p.add_argument("--batch-count", type=int, default=64)
     return p.parse_args()
 
@@ -241,6 +243,59 @@ def run_serving(a, dev):
     return st
 
 
+def run_extra(a, dev, batch):
+    """The components beyond the KRR hot path (atomic Coulomb matrices, local
+    kernels), each timed on the GPU (CUDA events) and on a bounded CPU sample of the
+    oracle restatement, on the bench's synthetic molecules."""
+    import numpy as np
+    from oracle import oracle as orc
+    import time as _t
+    import torch
+    from qml_gb300 import core
+    from qml_gb300.krr import molecules_to_device
+    z, r, o = molecules_to_device(batch)
+    out = {}
+
+    def gpu_time(fn, reps=3):
+        fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps / 1e3
+
+    nmol = batch.n_mol
+    t = gpu_time(lambda: core.atomic_coulomb_matrix_batch(z, r, o, 23, "row-norm"))
+    ns = 200
+    c0 = _t.perf_counter()
+    for m in range(ns):
+        orc.atomic_cm(*batch.molecule(m), None, 23, "row-norm")
+    cpu = (_t.perf_counter() - c0) * nmol / ns
+    out["atomic_cm_rownorm"] = {"molecules": nmol, "atoms": int(batch.offsets[-1]), "gpu_s": t,
+                                "cpu_oracle_s_scaled": cpu,
+                                "cpu_sample": "%d molecules, 1 thread, scaled" % ns}
+    nl = 2000
+    sub = batch.slice(0, nl)
+    zs, rs, os_ = molecules_to_device(sub)
+    Xa = core.atomic_coulomb_matrix_batch(zs, rs, os_, 23, "row-norm")
+    t = gpu_time(lambda: core.local_kernels("gaussian", Xa, Xa, os_, os_, [724.0], symmetric=True),
+                 reps=1)
+    Xh = Xa.cpu().numpy()
+    nh = np.diff(sub.offsets)
+    rows = 50
+    c0 = _t.perf_counter()
+    orc.local_kernels("gaussian", Xh[:int(sub.offsets[rows])], Xh, nh[:rows], nh, [724.0])
+    cpu = (_t.perf_counter() - c0) * nl / rows
+    out["local_gaussian_kernel"] = {"molecules": nl, "gpu_s": t, "cpu_oracle_s_scaled": cpu,
+                                    "cpu_sample": "%d of %d rows, OpenMP on %d cores, scaled"
+                                                  % (rows, nl, os.cpu_count())}
+    return out
+
+
 def run_batching(a, dev):
     """64 fits of uneven size (N log-uniform in [500, 8000]), each with its own
     sigma in {250, 500, 1000, 2000} and lambda in {1e-4, 1e-6, 1e-8}, recorded into
@@ -396,20 +451,26 @@ def run_ours(a):
     del K
 
     # the Laplacian kernel of the same training set: FP64 and fixed-point paths
-    def time_kernel(kind, emulated, reps=2):
-        core.kernel_matrix(kind, X[:ntr], X[:ntr], a.sigma, symmetric=True, emulated=emulated)
+    def time_kernel(kind, emulated, reps=2, **kw):
+        core.kernel_matrix(kind, X[:ntr], X[:ntr], a.sigma, symmetric=True, emulated=emulated,
+                           **kw)
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(reps):
-            core.kernel_matrix(kind, X[:ntr], X[:ntr], a.sigma, symmetric=True, emulated=emulated)
+            core.kernel_matrix(kind, X[:ntr], X[:ntr], a.sigma, symmetric=True, emulated=emulated,
+                               **kw)
         e1.record(stream)
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / reps / 1e3
     kernels_s = {"gaussian_fp64": time_kernel("gaussian", False),
                  "gaussian_tensor": time_kernel("gaussian", True),
                  "laplacian_fp64": time_kernel("laplacian", False),
-                 "laplacian_fixed": time_kernel("laplacian", True)}
+                 "laplacian_fixed": time_kernel("laplacian", True),
+                 "linear_fp64": time_kernel("linear", False, reps=1),
+                 "matern_l2_order2_fp64": time_kernel("matern_l2", False, reps=1, order=2),
+                 "sargan_2gammas_fp64": time_kernel("sargan", False, reps=1,
+                                                    gammas=[1.0, 1.0 / 3.0])}
 
     # dominant kernel: the emulated trailing update of the mixed Cholesky
     # (first outer step of this workload: C (n-512)^2 lower, P (n-512) x 512)
@@ -463,6 +524,9 @@ def run_ours(a):
     batching_stats = None
     if not a.no_batching:
         batching_stats = run_batching(a, dev)
+    extra_stats = None
+    if not a.no_extra and rank == 0:
+        extra_stats = run_extra(a, dev, batch)
 
     if rank != 0:
         return 0
@@ -506,6 +570,7 @@ def run_ours(a):
             "fits_per_s": replicas.job_throughput(1.0, ms / 1e3, world),
             "serving": serving_stats,
             "batching": batching_stats,
+            "other_paths": extra_stats,
             "gpu_launches": launches, "clocks": clocks.summary(), "roofline": roofline,
             "cpu_baseline": cpu, "stages_s": stages,
             "train_kernel_matrix_s": kernels_s, "solve_report": rep_m,
