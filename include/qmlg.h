@@ -404,6 +404,21 @@ int qmlg_solve_async(double *A, int n, int64_t lda, const double *y, double *x, 
                      size_t ws_bytes, void *stream);
 
 /*
+ * Inverse of a symmetric positive-definite matrix: Ainv (column-major, ldi) =
+ * A^-1, both triangles written.  Reads A's column-major lower triangle, as
+ * dpotrf("L") + dpotri("L") in fcho_invert (qml/fcho_solve.f90:54-73), bound by
+ * qml.math.cho_invert (qml/math.py:33-58).  Computed as the Schur complement left
+ * by the first ceil64(n) Cholesky pivots of [[A, I], [I, 0]] (A padded with an
+ * identity), with the FP64 (QMLG_PREC_FP64) or the tensor-core (QMLG_PREC_MIXED)
+ * factorisation.  Returns 0, or LAPACK's info (> 0: the leading minor of that order
+ * is not positive definite; Ainv is then unusable, where the reference prints a
+ * warning and returns whatever dpotri produced).  A is not modified.
+ */
+size_t qmlg_cho_invert_workspace_size(int n, int precision);
+int qmlg_cho_invert(const double *A, int n, int64_t lda, double *Ainv, int64_t ldi, int precision,
+                    void *workspace, size_t ws_bytes, void *stream);
+
+/*
  * r = y - (A + lambda I) x with every product and sum carried in double-double,
  * using A's strictly lower triangle (column-major, untouched by the factorisation)
  * and the diagonal vector diag (the diagonal of A before factorising).

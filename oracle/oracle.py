@@ -253,6 +253,20 @@ def cho_solve(A, y):
     return x
 
 
+def cho_invert(A):
+    """LAPACK dpotrf("L") + dpotri("L") on a copy (qml/fcho_solve.f90:54-73), the
+    lower triangle mirrored to the upper one like qml/math.py:52-56."""
+    from scipy.linalg import lapack
+    a = np.array(A, dtype=np.float64, order="F", copy=True)
+    c, info = lapack.dpotrf(a, lower=1, overwrite_a=1, clean=1)
+    if info != 0:
+        raise np.linalg.LinAlgError("dpotrf info=%d" % info)
+    inv, info = lapack.dpotri(c, lower=1)
+    il = np.tril_indices_from(inv)
+    inv.T[il] = inv[il]
+    return inv
+
+
 def residual_dd(A, lam, x, y):
     """y - (A + lam I) x with double-double accumulation, rounded to FP64."""
     A = np.ascontiguousarray(A, dtype=np.float64)

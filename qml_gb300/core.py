@@ -427,6 +427,25 @@ def syrk_emulated(C: torch.Tensor, P: torch.Tensor) -> None:
           "qmlg_syrk_emulated")
 
 
+def cho_invert(A: torch.Tensor, precision: str = "fp64"):
+    """A^-1 of a symmetric positive-definite A (its column-major lower triangle is
+    read, like dpotrf("L")).  Returns (Ainv, info): Ainv a Fortran-ordered (n, n)
+    float64 view, info LAPACK's (0 = ok)."""
+    _require_cuda(A)
+    if precision not in _PRECISIONS:
+        raise ValueError("precision must be 'fp64' or 'mixed'")
+    Acm, lda = _colmajor(A)
+    n = Acm.shape[0]
+    p = _PRECISIONS[precision]
+    out = torch.empty((n, n), dtype=torch.float64, device=A.device)  # rows = columns of Ainv
+    ws = workspaces.get(lib().qmlg_cho_invert_workspace_size(n, p), A.device)
+    st = lib().qmlg_cho_invert(Acm.data_ptr(), n, lda, out.data_ptr(), n, p, ws.data_ptr(),
+                               ws.numel(), _stream(A.device))
+    if st < 0:
+        check(st, "qmlg_cho_invert")
+    return out.T, st
+
+
 def cholesky_solve_factored(U: torch.Tensor, y: torch.Tensor) -> torch.Tensor:
     """dpotrs("U", nrhs=1) with a factor from cholesky()."""
     _require_cuda(U, y)

@@ -952,9 +952,13 @@ __global__ void fill_nan_kernel(double *__restrict__ x, int n)
 
 namespace qmlg {
 
-int cholesky_fp64(double *A, int n, int64_t lda, double shift, int *d_info, cudaStream_t s)
+int cholesky_fp64(double *A, int n, int64_t lda, double shift, int *d_info, cudaStream_t s,
+                  int npiv)
 {
-    for (int k0 = 0; k0 < n; k0 += NB) {
+    // npiv < n (a multiple of 64): only the first npiv pivots; the trailing
+    // (n - npiv) block is left holding its Schur complement
+    const int np = (npiv < 0 || npiv > n) ? n : npiv;
+    for (int k0 = 0; k0 < np; k0 += NB) {
         { potrf_diag_kernel<<<1, 256, 0, s>>>(A, lda, n, k0, shift, d_info); qmlg::count_launches(1); }
         const int below = n - (k0 + NB);
         if (below > 0) {
@@ -1085,8 +1089,11 @@ int factor_panel(double *A, int n, int64_t lda, double shift, int K0, int K1, in
 // free, while the next panel's 64-wide FP64 chain runs on the auxiliary stream in
 // those SMs.  The two touch disjoint columns; the next outer step joins them.
 int emulated_factor(double *A, int n, int64_t lda, double shift, Workspace &ws, int *d_info,
-                    EmulatedFactor &f, cudaStream_t s, int slices)
+                    EmulatedFactor &f, cudaStream_t s, int slices, int npiv)
 {
+    // npiv < n (a multiple of 64): only the first npiv pivots; the trailing
+    // (n - npiv) block is left holding its Schur complement
+    const int np = (npiv < 0 || npiv > n) ? n : npiv;
     const int rpad = (int)ceil_div(n, 128) * 128;
     __nv_bfloat16 *dig_out = ws.take<__nv_bfloat16>((size_t)kEmuMaxSlices * rpad * NBO);
     int *exp_out = ws.take<int>((size_t)rpad);
@@ -1108,21 +1115,23 @@ int emulated_factor(double *A, int n, int64_t lda, double shift, Workspace &ws, 
     // (cooperative kernels off, e.g. batched fits) keep one stream per solve and
     // skip the look-ahead, so concurrent solves do not share the auxiliary stream.
     const int reserve = (sms >= 64 && cooperative_on()) ? 8 : 0;
-    st = factor_panel(A, n, lda, shift, 0, std::min(NBO, n), rpad, slices, dig_in, exp_in, d_info,
+    st = factor_panel(A, n, lda, shift, 0, std::min(NBO, np), rpad, slices, dig_in, exp_in, d_info,
                       d_err, s, 0);
-    for (int K0 = 0; K0 < n && st == QMLG_OK; K0 += NBO) {
-        const int K1 = std::min(K0 + NBO, n);
+    for (int K0 = 0; K0 < np && st == QMLG_OK; K0 += NBO) {
+        const int K1 = std::min(K0 + NBO, np);
         if (K1 >= n) break;
-        const int K2 = std::min(K1 + NBO, n);
+        const int K2 = std::min(K1 + NBO, np);  // the next panel's pivot columns [K1, K2)
+        const bool more = K2 > K1;
         const int kw = K1 - K0;
         const int kp = (int)ceil_div(kw, 64) * 64;
         st = slice_rows(A, lda, K1, n - K1, K0, kw, kp, rpad, slices, dig_out, exp_out, d_info, s);
         if (st != QMLG_OK) break;
         // (1) the next panel's columns
-        st = emu_tc_update(A, lda, K1, K2, K1, n, dig_out, exp_out, kp, rpad, slices, 0, 0, 1, d_err,
-                           s, 0);
+        if (more)
+            st = emu_tc_update(A, lda, K1, K2, K1, n, dig_out, exp_out, kp, rpad, slices, 0, 0, 1,
+                               d_err, s, 0);
         if (st != QMLG_OK) break;
-        if (K2 < n && reserve > 0) {
+        if (more && K2 < n && reserve > 0) {
             // fork: the next panel's chain on the auxiliary stream
             if ((e = cudaEventRecord(aux->fork, s)) != cudaSuccess ||
                 (e = cudaStreamWaitEvent(aux->stream, aux->fork, 0)) != cudaSuccess) {
@@ -1143,13 +1152,16 @@ int emulated_factor(double *A, int n, int64_t lda, double shift, Workspace &ws, 
             if (K2 < n)
                 st = emu_tc_update(A, lda, K2, n, K2, n, dig_out, exp_out, kp, rpad, slices, K2 - K1,
                                    K2 - K1, 1, d_err, s, 0);
-            if (st == QMLG_OK)
+            if (st == QMLG_OK && more)
                 st = factor_panel(A, n, lda, shift, K1, K2, rpad, slices, dig_in, exp_in, d_info,
                                   d_err, s, 0);
         }
     }
     if (st != QMLG_OK) return st;
-    { invert_diag_blocks_kernel<<<(unsigned)ceil_div(n, NB), 64, 0, s>>>(A, lda, n, linv); count_launches(1); }
+    if (np == n) {
+        invert_diag_blocks_kernel<<<(unsigned)ceil_div(n, NB), 64, 0, s>>>(A, lda, n, linv);
+        count_launches(1);
+    }
     f.A = A;
     f.n = n;
     f.lda = lda;
@@ -1514,4 +1526,99 @@ extern "C" int qmlg_solve_async(double *A, int n, int64_t lda, const double *y, 
         if (e != cudaSuccess) return qmlg::set_cuda_error(e);
     }
     return qmlg::check_launch();
+}
+
+// ------------------------------------------------------------ cho_invert --
+//
+// Inverse of an SPD matrix through the Schur complement of an augmented matrix:
+// the first np pivots of the Cholesky factorisation of
+//     M = [ A_p  E ]   (A_p = A padded with an identity to np = ceil64(n) rows,
+//         [ E^T  0 ]    E = [I_n; 0], size np + n)
+// give L11 = chol(A_p), L21 = E^T L11^-T and leave 0 - L21 L21^T = -A^-1 in the
+// trailing n x n block.  The TRSM, the trailing updates and (mixed precision) the
+// emulated tensor-core products are the factorisation's own kernels.
+
+namespace {
+
+// M's lower triangle (row-major view, ldm = N): A's column-major lower triangle
+// (the triangle dpotrf("L") reads), identity padding, the identity coupling block.
+__global__ void build_augmented_kernel(const double *__restrict__ A, int64_t lda, int n, int np,
+                                       double *__restrict__ M, int64_t ldm)
+{
+    const int N = np + n;
+    const int64_t total = (int64_t)N * N;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int r = (int)(e / N), c = (int)(e % N);
+        if (c > r) continue;
+        double v = 0.0;
+        if (r < np) {
+            if (r < n) v = A[(int64_t)r + (int64_t)c * lda];  // c <= r < n
+            else v = (r == c) ? 1.0 : 0.0;
+        } else if (c < np) {
+            v = (c == r - np) ? 1.0 : 0.0;
+        }
+        M[(int64_t)r * ldm + c] = v;
+    }
+}
+
+// Ainv (column-major, ldi) = -S, S the trailing block's lower triangle, mirrored.
+__global__ void extract_inverse_kernel(const double *__restrict__ M, int64_t ldm, int np, int n,
+                                       double *__restrict__ Ainv, int64_t ldi)
+{
+    const int64_t total = (int64_t)n * n;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(e % n), j = (int)(e / n);
+        const int hi = i > j ? i : j, lo = i > j ? j : i;
+        Ainv[(int64_t)i + (int64_t)j * ldi] = -M[(int64_t)(np + hi) * ldm + (np + lo)];
+    }
+}
+
+}  // namespace
+
+extern "C" size_t qmlg_cho_invert_workspace_size(int n, int precision)
+{
+    if (n < 1) n = 1;
+    const int np = (int)qmlg::ceil_div(n, NB) * NB, N = np + n;
+    qmlg::WorkspacePlan p;
+    p.add<int>(4);
+    p.add<double>((size_t)N * N);
+    if (precision == QMLG_PREC_MIXED) p.add<char>(qmlg::emulated_factor_ws(N));
+    return p.total();
+}
+
+extern "C" int qmlg_cho_invert(const double *A, int n, int64_t lda, double *Ainv, int64_t ldi,
+                               int precision, void *workspace, size_t ws_bytes, void *stream)
+{
+    if (n < 0 || lda < n || ldi < n || (precision != QMLG_PREC_FP64 && precision != QMLG_PREC_MIXED))
+        return QMLG_E_ARG;
+    if (n == 0) return QMLG_OK;
+    if (A == nullptr || Ainv == nullptr) return QMLG_E_ARG;
+    if (ws_bytes < qmlg_cho_invert_workspace_size(n, precision)) return QMLG_E_WORKSPACE;
+    cudaStream_t s = qmlg::as_stream(stream);
+    qmlg::Workspace ws(workspace, ws_bytes);
+    const int np = (int)qmlg::ceil_div(n, NB) * NB, N = np + n;
+    int *d_info = ws.take<int>(4);
+    double *M = ws.take<double>((size_t)N * N);
+    cudaError_t e = cudaMemsetAsync(d_info, 0, sizeof(int), s);
+    if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+    const int blocks = (int)std::min<int64_t>(qmlg::ceil_div((int64_t)N * N, 256), 152 * 64);
+    { build_augmented_kernel<<<blocks, 256, 0, s>>>(A, lda, n, np, M, N); qmlg::count_launches(1); }
+    int st;
+    if (precision == QMLG_PREC_MIXED) {
+        qmlg::EmulatedFactor f;
+        st = qmlg::emulated_factor(M, N, N, 0.0, ws, d_info, f, s, 8, np);
+        if (st == QMLG_OK) st = qmlg::read_device_flag(f.d_err, s);
+    } else {
+        st = qmlg::cholesky_fp64(M, N, N, 0.0, d_info, s, np);
+    }
+    if (st != QMLG_OK) return st;
+    const int eb = (int)std::min<int64_t>(qmlg::ceil_div((int64_t)n * n, 256), 152 * 64);
+    { extract_inverse_kernel<<<eb, 256, 0, s>>>(M, N, np, n, Ainv, ldi); qmlg::count_launches(1); }
+    int info = 0;
+    st = qmlg::read_back(&info, d_info, sizeof(int), s);
+    if (st != QMLG_OK) return st;
+    // a pivot in the identity padding cannot fail; report A's pivot index like dpotrf
+    return info > n ? n : info;
 }

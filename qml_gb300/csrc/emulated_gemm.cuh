@@ -52,13 +52,16 @@ struct EmulatedFactor {
 };
 
 size_t emulated_factor_ws(int n);
+// npiv (a multiple of 64, or -1 for n): take only the first npiv pivots, leaving the
+// Schur complement in the trailing block.
 int emulated_factor(double *A, int n, int64_t lda, double shift, Workspace &ws, int *d_info,
-                    EmulatedFactor &f, cudaStream_t s, int slices = 8);
+                    EmulatedFactor &f, cudaStream_t s, int slices = 8, int npiv = -1);
 int emulated_potrs(const EmulatedFactor &f, double *x, cudaStream_t s);
 int read_device_flag(const int *d_flag, cudaStream_t s);
 
 // Shared with the FP64 path (cholesky.cu).
-int cholesky_fp64(double *A, int n, int64_t lda, double shift, int *d_info, cudaStream_t s);
+int cholesky_fp64(double *A, int n, int64_t lda, double shift, int *d_info, cudaStream_t s,
+                  int npiv = -1);
 int potrs_fp64(const double *A, int n, int64_t lda, double *x, cudaStream_t s);
 int mirror_upper_to_lower(double *A, int n, int64_t lda, const double *diag, cudaStream_t s);
 

@@ -1,9 +1,11 @@
-"""Drop-in for qml.math.cho_solve (qml/math.py:60-97, qml/fcho_solve.f90:23-52).
+"""Drop-ins for qml.math.cho_solve and cho_invert (qml/math.py:33-97,
+qml/fcho_solve.f90:23-73).
 
-Solves A x = y with the GPU Cholesky (dpotrf("U") + dpotrs("U") semantics: the
-upper triangle of A is read).  Like the reference wrapper it raises ValueError on
-shape errors, returns a new x, and leaves A symmetrised from its lower triangle
-with the diagonal restored; a non-positive-definite A prints LAPACK's warning.
+cho_solve solves A x = y with the GPU Cholesky (dpotrf("U") + dpotrs("U")
+semantics: the upper triangle of A is read).  Like the reference wrapper it raises
+ValueError on shape errors, returns a new x, and leaves A symmetrised from its lower
+triangle with the diagonal restored; a non-positive-definite A prints LAPACK's
+warning.  cho_invert returns A^-1 like the reference's dpotrf("L") + dpotri("L").
 """
 from __future__ import annotations
 
@@ -33,3 +35,31 @@ def cho_solve(A, y):
         i_lower = np.tril_indices_from(A)
         A.T[i_lower] = A[i_lower]
     return x.cpu().numpy()
+
+
+def cho_invert(A, precision="fp64"):
+    """Inverse of a symmetric positive-definite matrix (qml/math.py:33-58).
+
+    As in the reference, the result is np.asfortranarray(A): a new array unless A
+    already is a Fortran-ordered float64 array, which then receives the inverse in
+    place.  A's lower triangle is read (dpotrf("L")); the result is symmetric.  The
+    Cholesky factorisation runs in plain FP64 by default, like LAPACK's; with
+    precision="mixed" it runs on the tensor cores, several times faster but only
+    for well-conditioned matrices: an inverse gets no refinement, so the emulated
+    factor's error (~1e-11 relative) is amplified by the condition number.  A matrix
+    that is not positive definite prints the reference's warning.
+    """
+    if len(A.shape) != 2 or A.shape[0] != A.shape[1]:
+        raise ValueError('expected square matrix')
+    if not torch.cuda.is_available():
+        raise RuntimeError("qml_gb300 needs a CUDA device (no CPU fallback)")
+    I = np.asfortranarray(A)
+    if A.shape[0] == 0:
+        return I
+    # the rows of this C-ordered array are the columns of I
+    At = torch.from_numpy(np.ascontiguousarray(I.T, dtype=np.float64)).cuda()
+    Ainv, info = core.cho_invert(At.T, precision=precision)
+    if info > 0:
+        print("WARNING: Cholesky decomposition DPOTRF() exited with error code:", info)
+    I[...] = Ainv.cpu().numpy()
+    return I

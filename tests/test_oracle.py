@@ -163,6 +163,14 @@ def test_cho_solve_oracle_matches_reference_test(oracle):
     assert np.allclose(x, np.linalg.solve(g["A"], g["y"]))
 
 
+def test_cho_invert_oracle_matches_reference_test(oracle):
+    # tests/test_math.py:54-71
+    A = load_golden("cho_solve_k_local_gaussian.npz")["A"]
+    Ai = oracle.cho_invert(A)
+    assert np.allclose(A @ Ai, np.eye(A.shape[0]), atol=1e-7)
+    assert np.array_equal(Ai, Ai.T)
+
+
 def test_refined_solve_residual(oracle):
     b = generate_molecules(400, seed=5)
     X = oracle.cm_sorted_batch(b.charges, b.coordinates, b.offsets, 23)
