@@ -293,6 +293,18 @@ def run_extra(a, dev, batch):
     out["local_gaussian_kernel"] = {"molecules": nl, "gpu_s": t, "cpu_oracle_s_scaled": cpu,
                                     "cpu_sample": "%d of %d rows, OpenMP on %d cores, scaled"
                                                   % (rows, nl, os.cpu_count())}
+    # cho_invert of an N=5000 Gaussian KRR matrix (K + 1e-4 I)
+    ni = 5000
+    Xi = core.coulomb_matrix_batch(*molecules_to_device(batch.slice(0, ni)), 23)
+    Ki = core.kernel_matrix("gaussian", Xi, Xi, 1000.0, symmetric=True, diag_shift=1e-4)
+    tf = gpu_time(lambda: core.cho_invert(Ki, "fp64"), reps=1)
+    tm = gpu_time(lambda: core.cho_invert(Ki, "mixed"), reps=1)
+    Kh = np.asfortranarray(Ki.cpu().numpy())
+    c0 = _t.perf_counter()
+    orc.cho_invert(Kh)
+    cpu = _t.perf_counter() - c0
+    out["cho_invert"] = {"n": ni, "gpu_fp64_s": tf, "gpu_mixed_s": tm, "cpu_lapack_s": cpu,
+                         "cpu_sample": "scipy dpotrf + dpotri, full size, OpenBLAS threads"}
     return out
 
 
