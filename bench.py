@@ -305,6 +305,19 @@ def run_extra(a, dev, batch):
     cpu = _t.perf_counter() - c0
     out["cho_invert"] = {"n": ni, "gpu_fp64_s": tf, "gpu_mixed_s": tm, "cpu_lapack_s": cpu,
                          "cpu_sample": "scipy dpotrf + dpotri, full size, OpenBLAS threads"}
+    # Bunch-Kaufman solve and inverse of the same matrix
+    yi = torch.ones(ni, dtype=torch.float64, device=dev)
+    ts = gpu_time(lambda: core.bkf_solve(Ki, yi), reps=1)
+    tv = gpu_time(lambda: core.bkf_invert(Ki), reps=1)
+    c0 = _t.perf_counter()
+    orc.bkf_solve(Kh, np.ones(ni))
+    cs = _t.perf_counter() - c0
+    c0 = _t.perf_counter()
+    orc.bkf_invert(Kh)
+    cv = _t.perf_counter() - c0
+    out["bkf"] = {"n": ni, "gpu_solve_s": ts, "gpu_invert_s": tv, "cpu_lapack_solve_s": cs,
+                  "cpu_lapack_invert_s": cv,
+                  "cpu_sample": "scipy dsytrf + dsytrs / dsytri, full size, OpenBLAS threads"}
     return out
 
 

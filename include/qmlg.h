@@ -419,6 +419,29 @@ int qmlg_cho_invert(const double *A, int n, int64_t lda, double *Ainv, int64_t l
                     void *workspace, size_t ws_bytes, void *stream);
 
 /*
+ * Symmetric (possibly indefinite) solve A x = y by Bunch-Kaufman diagonal pivoting,
+ * restating dsytrf("L") + dsytrs("L") as fbkf_solve calls them
+ * (qml/fcho_solve.f90:115-150), bound by qml.math.bkf_solve (qml/math.py:125-164).
+ * Reads A's column-major lower triangle; A is not modified.  Returns 0, or LAPACK's
+ * info (> 0: D(info, info) is exactly zero, x is then unusable, where the reference
+ * prints a warning).
+ */
+size_t qmlg_bkf_solve_workspace_size(int n);
+int qmlg_bkf_solve(const double *A, int n, int64_t lda, const double *y, double *x,
+                   void *workspace, size_t ws_bytes, void *stream);
+
+/*
+ * Inverse of a symmetric (possibly indefinite) matrix by Bunch-Kaufman pivoting, as
+ * dsytrf("L") + dsytri("L") in fbkf_invert (qml/fcho_solve.f90:76-112), bound by
+ * qml.math.bkf_invert (qml/math.py:100-122): Ainv (column-major, ldi, both
+ * triangles) = A^-1, computed as the Schur complement left by n pivot steps on
+ * [[A, I], [I, 0]] with the pivots searched among A's rows.  Returns 0 or info.
+ */
+size_t qmlg_bkf_invert_workspace_size(int n);
+int qmlg_bkf_invert(const double *A, int n, int64_t lda, double *Ainv, int64_t ldi,
+                    void *workspace, size_t ws_bytes, void *stream);
+
+/*
  * r = y - (A + lambda I) x with every product and sum carried in double-double,
  * using A's strictly lower triangle (column-major, untouched by the factorisation)
  * and the diagonal vector diag (the diagonal of A before factorising).

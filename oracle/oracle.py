@@ -267,6 +267,27 @@ def cho_invert(A):
     return inv
 
 
+def bkf_solve(A, y):
+    """LAPACK dsytrf("L") + dsytrs("L") on a copy (qml/fcho_solve.f90:115-150)."""
+    from scipy.linalg import lapack
+    a = np.array(A, dtype=np.float64, order="F", copy=True)
+    ldu, ipiv, info = lapack.dsytrf(a, lower=1)
+    x, info2 = lapack.dsytrs(ldu, ipiv, np.asarray(y, dtype=np.float64), lower=1)
+    return x, info
+
+
+def bkf_invert(A):
+    """LAPACK dsytrf("L") + dsytri("L") on a copy (qml/fcho_solve.f90:76-112), the
+    lower triangle mirrored like qml/math.py:117-120."""
+    from scipy.linalg import lapack
+    a = np.array(A, dtype=np.float64, order="F", copy=True)
+    ldu, ipiv, info = lapack.dsytrf(a, lower=1)
+    inv, info2 = lapack.dsytri(ldu, ipiv, lower=1)
+    il = np.tril_indices_from(inv)
+    inv.T[il] = inv[il]
+    return inv, info
+
+
 def residual_dd(A, lam, x, y):
     """y - (A + lam I) x with double-double accumulation, rounded to FP64."""
     A = np.ascontiguousarray(A, dtype=np.float64)

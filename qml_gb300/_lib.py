@@ -85,6 +85,10 @@ SIGNATURES = {
     "qmlg_local_kernels": (_I, [_I, _P, _I64, _P, _I, _P, _I64, _P, _I, _I, _P, _I, _P, _I, _P]),
     "qmlg_cho_invert_workspace_size": (_SZ, [_I, _I]),
     "qmlg_cho_invert": (_I, [_P, _I, _I64, _P, _I64, _I, _P, _SZ, _P]),
+    "qmlg_bkf_solve_workspace_size": (_SZ, [_I]),
+    "qmlg_bkf_solve": (_I, [_P, _I, _I64, _P, _P, _P, _SZ, _P]),
+    "qmlg_bkf_invert_workspace_size": (_SZ, [_I]),
+    "qmlg_bkf_invert": (_I, [_P, _I, _I64, _P, _I64, _P, _SZ, _P]),
     "qmlg_linear_kernel": (_I, [_P, _I64, _I, _P, _I64, _I, _I, _P, _I64, _I, _D, _P]),
     "qmlg_matern_kernel_l2": (_I, [_P, _I64, _I, _P, _I64, _I, _I, _D, _I, _P, _I64, _I, _D, _P]),
     "qmlg_sargan_kernel": (_I, [_P, _I64, _I, _P, _I64, _I, _I, _D, _P, _I, _P, _I64, _I, _D,

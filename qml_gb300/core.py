@@ -446,6 +446,39 @@ def cho_invert(A: torch.Tensor, precision: str = "fp64"):
     return out.T, st
 
 
+def bkf_solve(A: torch.Tensor, y: torch.Tensor):
+    """x with A x = y by Bunch-Kaufman pivoting (A's column-major lower triangle is
+    read).  Returns (x, info), info LAPACK's (0 = ok)."""
+    _require_cuda(A, y)
+    Acm, lda = _colmajor(A)
+    n = Acm.shape[0]
+    if y.shape != (n,):
+        raise ValueError("expected matrix and vector of same stride size")
+    y = y.contiguous()
+    x = torch.empty_like(y)
+    ws = workspaces.get(lib().qmlg_bkf_solve_workspace_size(n), A.device)
+    st = lib().qmlg_bkf_solve(Acm.data_ptr(), n, lda, y.data_ptr(), x.data_ptr(), ws.data_ptr(),
+                              ws.numel(), _stream(A.device))
+    if st < 0:
+        check(st, "qmlg_bkf_solve")
+    return x, st
+
+
+def bkf_invert(A: torch.Tensor):
+    """A^-1 by Bunch-Kaufman pivoting.  Returns (Ainv, info), Ainv a Fortran-ordered
+    (n, n) float64 view."""
+    _require_cuda(A)
+    Acm, lda = _colmajor(A)
+    n = Acm.shape[0]
+    out = torch.empty((n, n), dtype=torch.float64, device=A.device)
+    ws = workspaces.get(lib().qmlg_bkf_invert_workspace_size(n), A.device)
+    st = lib().qmlg_bkf_invert(Acm.data_ptr(), n, lda, out.data_ptr(), n, ws.data_ptr(),
+                               ws.numel(), _stream(A.device))
+    if st < 0:
+        check(st, "qmlg_bkf_invert")
+    return out.T, st
+
+
 def cholesky_solve_factored(U: torch.Tensor, y: torch.Tensor) -> torch.Tensor:
     """dpotrs("U", nrhs=1) with a factor from cholesky()."""
     _require_cuda(U, y)

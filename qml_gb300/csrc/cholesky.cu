@@ -1528,6 +1528,18 @@ extern "C" int qmlg_solve_async(double *A, int n, int64_t lda, const double *y, 
     return qmlg::check_launch();
 }
 
+namespace qmlg {
+
+int launch_cooperative_serialised(const void *fn, int grid, int threads, void **args,
+                                  cudaStream_t s)
+{
+    return launch_cooperative(fn, grid, threads, args, s);
+}
+
+bool cooperative_allowed_on(cudaStream_t s) { return cooperative_allowed(s); }
+
+}  // namespace qmlg
+
 // ------------------------------------------------------------ cho_invert --
 //
 // Inverse of an SPD matrix through the Schur complement of an augmented matrix:

@@ -57,6 +57,12 @@ size_t emulated_factor_ws(int n);
 int emulated_factor(double *A, int n, int64_t lda, double shift, Workspace &ws, int *d_info,
                     EmulatedFactor &f, cudaStream_t s, int slices = 8, int npiv = -1);
 int emulated_potrs(const EmulatedFactor &f, double *x, cudaStream_t s);
+// A cooperative launch ordered after every earlier one of this process on the
+// device (so two whole-GPU grids are never resident together), and whether one is
+// allowed on the stream (not while capturing, not on threads that turned them off).
+int launch_cooperative_serialised(const void *fn, int grid, int threads, void **args,
+                                  cudaStream_t s);
+bool cooperative_allowed_on(cudaStream_t s);
 int read_device_flag(const int *d_flag, cudaStream_t s);
 
 // Shared with the FP64 path (cholesky.cu).

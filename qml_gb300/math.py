@@ -1,11 +1,13 @@
-"""Drop-ins for qml.math.cho_solve and cho_invert (qml/math.py:33-97,
-qml/fcho_solve.f90:23-73).
+"""Drop-ins for qml.math.cho_solve, cho_invert, bkf_solve and bkf_invert
+(qml/math.py:33-164, qml/fcho_solve.f90:23-150).
 
 cho_solve solves A x = y with the GPU Cholesky (dpotrf("U") + dpotrs("U")
 semantics: the upper triangle of A is read).  Like the reference wrapper it raises
 ValueError on shape errors, returns a new x, and leaves A symmetrised from its lower
 triangle with the diagonal restored; a non-positive-definite A prints LAPACK's
-warning.  cho_invert returns A^-1 like the reference's dpotrf("L") + dpotri("L").
+warning.  cho_invert returns A^-1 like the reference's dpotrf("L") + dpotri("L");
+bkf_solve / bkf_invert do the same by Bunch-Kaufman pivoting (dsytrf + dsytrs /
+dsytri), so they also take symmetric indefinite matrices.
 """
 from __future__ import annotations
 
@@ -63,3 +65,44 @@ def cho_invert(A, precision="fp64"):
         print("WARNING: Cholesky decomposition DPOTRF() exited with error code:", info)
     I[...] = Ainv.cpu().numpy()
     return I
+
+
+def bkf_invert(A):
+    """Inverse of a symmetric matrix by Bunch-Kaufman pivoting (qml/math.py:100-122):
+    the result is np.asfortranarray(A) (in place for a Fortran-ordered float64 A),
+    A's lower triangle is read, the result is symmetric."""
+    if len(A.shape) != 2 or A.shape[0] != A.shape[1]:
+        raise ValueError('expected square matrix')
+    if not torch.cuda.is_available():
+        raise RuntimeError("qml_gb300 needs a CUDA device (no CPU fallback)")
+    I = np.asfortranarray(A)
+    if A.shape[0] == 0:
+        return I
+    At = torch.from_numpy(np.ascontiguousarray(I.T, dtype=np.float64)).cuda()
+    Ainv, info = core.bkf_invert(At.T)
+    if info > 0:
+        print("WARNING: Bunch-Kaufman factorization DSYTRI() exited with error code:", info)
+    I[...] = Ainv.cpu().numpy()
+    return I
+
+
+def bkf_solve(A, y):
+    """x with A x = y for a symmetric A by Bunch-Kaufman pivoting
+    (qml/math.py:125-164).  Raises ValueError on shape errors like the reference,
+    returns a new x and leaves A symmetrised from its lower triangle."""
+    if len(A.shape) != 2 or A.shape[0] != A.shape[1]:
+        raise ValueError('expected square matrix')
+    if len(y.shape) != 1 or y.shape[0] != A.shape[1]:
+        raise ValueError('expected matrix and vector of same stride size')
+    if not torch.cuda.is_available():
+        raise RuntimeError("qml_gb300 needs a CUDA device (no CPU fallback)")
+    n = A.shape[0]
+    Af = torch.from_numpy(np.asfortranarray(A, dtype=np.float64).T.copy()).cuda()
+    yt = torch.from_numpy(np.ascontiguousarray(y, dtype=np.float64)).cuda()
+    x, info = core.bkf_solve(Af.T, yt)
+    if info > 0:
+        print("WARNING: Bunch-Kaufman factorization DSYTRI() exited with error code:", info)
+    if n > 0:
+        i_lower = np.tril_indices_from(A)
+        A.T[i_lower] = A[i_lower]
+    return x.cpu().numpy()

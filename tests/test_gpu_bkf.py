@@ -1,0 +1,67 @@
+"""bkf_solve / bkf_invert (Bunch-Kaufman pivoting) on the GPU against the reference
+tests (tests/test_math.py:74-112) and LAPACK dsytrf + dsytrs / dsytri."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import load_golden
+from qml_gb300 import core
+from qml_gb300.math import bkf_invert, bkf_solve
+
+pytestmark = pytest.mark.gpu
+
+
+def test_reference_bkf_solve_and_invert(cuda, oracle):
+    g = load_golden("cho_solve_k_local_gaussian.npz")
+    A_ref, y_ref = g["A"], g["y"]
+    A, y = A_ref.copy(), y_ref.copy()
+    x = bkf_solve(A, y)
+    assert np.allclose(y, y_ref) and np.allclose(A, A_ref)
+    assert np.allclose(x, np.linalg.solve(A_ref, y_ref))
+    A = A_ref.copy()
+    Ai = bkf_invert(A)
+    assert np.allclose(A, A_ref)
+    eye = np.eye(A.shape[0])
+    assert np.allclose(A @ Ai, eye, atol=1e-7)
+    # held to LAPACK's residual on this ill-conditioned matrix
+    Ao, _ = oracle.bkf_invert(A_ref)
+    assert np.max(np.abs(A @ Ai - eye)) <= 10 * np.max(np.abs(A @ Ao - eye))
+
+
+def indefinite(n, seed):
+    # symmetric, well-conditioned, with eigenvalues of both signs: 2x2 pivots and
+    # interchanges happen
+    rng = np.random.default_rng(seed)
+    Q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    ev = rng.uniform(0.5, 2.0, n) * np.where(rng.random(n) < 0.5, -1.0, 1.0)
+    A = (Q * ev) @ Q.T
+    return (A + A.T) / 2
+
+
+@pytest.mark.parametrize("n", [1, 2, 7, 64, 129, 300, 700])
+def test_bkf_vs_lapack_indefinite(cuda, oracle, n):
+    A = indefinite(n, n)
+    y = np.random.default_rng(n + 1).standard_normal(n)
+    x = bkf_solve(A.copy(), y.copy())
+    xo, info = oracle.bkf_solve(A, y)
+    assert info == 0
+    assert np.max(np.abs(x - xo)) <= 1e-11 * max(1.0, np.max(np.abs(xo)))
+    Ai = bkf_invert(A.copy())
+    Ao, _ = oracle.bkf_invert(A)
+    assert np.max(np.abs(Ai - Ao)) <= 1e-11 * np.max(np.abs(Ao))
+    assert np.array_equal(Ai, Ai.T)
+
+
+def test_bkf_pivot_cases(cuda, oracle):
+    # zero diagonal (forces 2x2 pivots), a swap, and a singular matrix (info)
+    A = np.array([[0.0, 1.0, 2.0], [1.0, 0.0, 3.0], [2.0, 3.0, 0.0]])
+    y = np.array([1.0, 2.0, 3.0])
+    assert np.allclose(bkf_solve(A.copy(), y.copy()), np.linalg.solve(A, y))
+    assert np.allclose(bkf_invert(A.copy()), np.linalg.inv(A))
+    S = np.zeros((3, 3))
+    S[0, 0] = 1.0
+    _, info = core.bkf_solve(torch.from_numpy(S).to(cuda), torch.ones(3, dtype=torch.float64,
+                                                                      device=cuda))
+    assert info == 2
+    with pytest.raises(ValueError):
+        bkf_solve(np.zeros((3, 3)), np.zeros(4))

@@ -171,6 +171,16 @@ def test_cho_invert_oracle_matches_reference_test(oracle):
     assert np.array_equal(Ai, Ai.T)
 
 
+def test_bkf_oracle_matches_reference_tests(oracle):
+    # tests/test_math.py:74-112
+    g = load_golden("cho_solve_k_local_gaussian.npz")
+    A, y = g["A"], g["y"]
+    x, info = oracle.bkf_solve(A, y)
+    assert info == 0 and np.allclose(x, np.linalg.solve(A, y))
+    Ai, info = oracle.bkf_invert(A)
+    assert info == 0 and np.allclose(A @ Ai, np.eye(A.shape[0]), atol=1e-7)
+
+
 def test_refined_solve_residual(oracle):
     b = generate_molecules(400, seed=5)
     X = oracle.cm_sorted_batch(b.charges, b.coordinates, b.offsets, 23)
