@@ -48,6 +48,16 @@ class KRR:
         self.K = K if keep_kernel else None
         return self
 
+    def save(self, path: str) -> None:
+        """Write the fitted model to one .npz file (see qml_gb300.io)."""
+        from .io import save_krr
+        save_krr(path, self)
+
+    @staticmethod
+    def load(path: str, device="cuda") -> "KRR":
+        from .io import load_krr
+        return load_krr(path, device)
+
     def predict(self, Xs: torch.Tensor) -> torch.Tensor:
         if self.alpha is None:
             raise RuntimeError("fit() first")

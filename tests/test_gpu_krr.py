@@ -37,3 +37,25 @@ def test_krr_pipeline(cuda, oracle, kernel, sigma, lam, precision):
     mae_ref = np.mean(np.abs(yo - b.labels[ntr:]))
     assert abs(mae_gpu - mae_ref) < 1e-6 * mae_ref
     assert model.report["status"] == 0
+
+
+def test_xyz_ingestion_and_model_file(cuda, oracle, tmp_path):
+    # XYZ files -> one ragged batch on the device -> Coulomb matrices (bit-exact vs
+    # the oracle); a fitted model saved and loaded predicts bit for bit the same
+    from test_io import write_fixture_xyz
+    from qml_gb300.io import xyz_to_device
+    from qml_gb300.krr import KRR
+    paths, z, r, off = write_fixture_xyz(tmp_path)
+    zt, rt, ot = xyz_to_device(paths)
+    X = core.coulomb_matrix_batch(zt, rt, ot, 17).cpu().numpy()
+    Xo = oracle.cm_sorted_batch(z, r, off, 17)
+    assert np.array_equal(X, Xo)
+    b = generate_molecules(600, seed=5)
+    zb, rb, ob = molecules_to_device(b)
+    Xb = core.coulomb_matrix_batch(zb, rb, ob, 23)
+    y = torch.from_numpy(b.labels).to(cuda)
+    m = KRR(sigma=1000.0, lam=1e-8).fit(Xb[:500], y[:500])
+    path = str(tmp_path / "krr.npz")
+    m.save(path)
+    m2 = KRR.load(path)
+    assert torch.equal(m2.predict(Xb[500:]), m.predict(Xb[500:]))
