@@ -308,7 +308,7 @@ int qmlg_predict_emulated_async(const double *Xtrain, int64_t ldtrain, int ntrai
 /* ---- Cholesky solve ------------------------------------------------------- */
 
 #define QMLG_PREC_FP64 0   /* plain FP64 blocked Cholesky (LAPACK dpotrf semantics) */
-#define QMLG_PREC_MIXED 1  /* emulated-FP64 tensor-core factor + double-double refinement */
+#define QMLG_PREC_MIXED 1  /* emulated-FP64 tensor-core factor + exact-residual refinement */
 
 typedef struct QmlgSolveReport {
     int precision_used;     /* QMLG_PREC_* of the factor the answer came from */
@@ -376,7 +376,7 @@ int qmlg_cholesky_solve_factored(const double *U, int n, int64_t lda, const doub
  * Full solve (A + lambda I) x = y, the fcho_solve of qml/fcho_solve.f90:23-52 with
  * the KRR lambda folded in.  precision QMLG_PREC_FP64 factorises A in place like
  * the reference (upper triangle overwritten); QMLG_PREC_MIXED factorises in place
- * the same way with qmlg_cholesky_mixed, then refines with a double-double
+ * the same way with qmlg_cholesky_mixed, then refines with an exact
  * residual read from the untouched triangle, and falls back to a plain FP64
  * refactorisation when refinement stalls (opts->allow_fallback).  In both modes
  * the column-major strictly lower triangle of A is never written.  opts and
@@ -391,7 +391,7 @@ int qmlg_solve(double *A, int n, int64_t lda, const double *y, double *x, double
 /*
  * Capture-safe mixed solve (A + lambda I) x = y for batched, graph-recorded
  * work: the qmlg_cholesky_mixed factorisation, one solve and exactly
- * refine_steps double-double refinement steps, with no host synchronisation and
+ * refine_steps exact-residual refinement steps, with no host synchronisation and
  * no host decision.  Results stay on the device: d_status[0] = Cholesky info
  * (0 = ok), d_status[1] = bounded-wait flags (bit 1: a tensor-core pipeline
  * wait, bit 2: a triangular-solve wait gave up); d_correction (optional, 2
@@ -442,9 +442,12 @@ int qmlg_bkf_invert(const double *A, int n, int64_t lda, double *Ainv, int64_t l
                     void *workspace, size_t ws_bytes, void *stream);
 
 /*
- * r = y - (A + lambda I) x with every product and sum carried in double-double,
- * using A's strictly lower triangle (column-major, untouched by the factorisation)
- * and the diagonal vector diag (the diagonal of A before factorising).
+ * r = y - (A + lambda I) x summed exactly (every product formed from the 53-bit
+ * significands and added into 256-bit fixed point on the integer pipes) and
+ * rounded once: each r[i] is the correctly rounded exact residual, independent of
+ * the summation order.  Uses A's strictly lower triangle (column-major, untouched
+ * by the factorisation) and the diagonal vector diag (the diagonal of A before
+ * factorising).  The name is kept from its first, double-double form.
  * ws: qmlg_residual_workspace_size(n).
  */
 size_t qmlg_residual_workspace_size(int n);

@@ -23,6 +23,7 @@
 
 #include "common.cuh"
 #include "emulated_gemm.cuh"
+#include "exact_acc.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -362,21 +363,42 @@ syrk_update_kernel(double *__restrict__ A, int64_t lda, int n, int k0,
 constexpr int RES_ROWS = 64;
 constexpr int RES_CHUNK = 1024;
 
-// Partial double-double row sums of the symmetric matrix held in R's strictly
-// upper triangle plus diag: one CTA per (64 rows, 1024 columns).  Dot2 of
-// Ogita, Rump and Oishi (TwoProduct + TwoSum), 4 threads per row.
+// Partial row sums of the symmetric matrix held in R's strictly upper triangle plus
+// diag, times x: one CTA per (64 rows, 1024 columns), 4 threads per row, each
+// product added exactly into a 256-bit fixed-point accumulator (exact_acc.cuh).
+struct AccPart {
+    unsigned long long l0, l1, l2, l3;
+    int f, bad;
+};
+
+__device__ __forceinline__ void acc_shfl_xor_add(qmlg::Acc &a, int off)
+{
+    qmlg::Acc b;
+    b.l0 = __shfl_xor_sync(0xffffffffu, a.l0, off);
+    b.l1 = __shfl_xor_sync(0xffffffffu, a.l1, off);
+    b.l2 = __shfl_xor_sync(0xffffffffu, a.l2, off);
+    b.l3 = __shfl_xor_sync(0xffffffffu, a.l3, off);
+    b.f = __shfl_xor_sync(0xffffffffu, a.f, off);
+    b.bad = __shfl_xor_sync(0xffffffffu, a.bad, off);
+    qmlg::acc_add_acc(a, b);
+}
+
 __global__ void __launch_bounds__(256)
-symv_dd_partial_kernel(const double *__restrict__ A, int64_t lda, int n,
-                       const double *__restrict__ diag, const double *__restrict__ x,
-                       double2 *__restrict__ partial)
+symv_exact_partial_kernel(const double *__restrict__ A, int64_t lda, int n,
+                          const double *__restrict__ diag, const double *__restrict__ x,
+                          AccPart *__restrict__ partial)
 {
     __shared__ double S[64][64 + 1];
-    __shared__ double xs[64];
+    __shared__ unsigned long long xm[64];
+    __shared__ int xe[64];
+    __shared__ unsigned char xn[64];
     const int tid = threadIdx.x;
     const int i0 = blockIdx.x * RES_ROWS;
     const int c0 = blockIdx.y * RES_CHUNK;
     const int lr = tid >> 2, part = tid & 3;
-    double hi = 0.0, lo = 0.0;
+    qmlg::Acc acc;
+    qmlg::acc_init(acc);
+    int xbad = 0;
     for (int j0 = c0; j0 < min(n, c0 + RES_CHUNK); j0 += 64) {
         __syncthreads();
         // S[r][c] = A_sym(i0 + r, j0 + c)
@@ -397,43 +419,66 @@ symv_dd_partial_kernel(const double *__restrict__ A, int64_t lda, int n,
             const int i = i0 + r, j = j0 + c;
             if (i < n && j < n && j < i) S[r][c] = A[(int64_t)j * lda + i];
         }
-        if (tid < 64) xs[tid] = (j0 + tid < n) ? x[j0 + tid] : 0.0;
+        if (tid < 64) {
+            unsigned long long m;
+            int ex, bd = 0;
+            bool ng;
+            qmlg::dbl_split((j0 + tid < n) ? x[j0 + tid] : 0.0, m, ex, ng, bd);
+            xm[tid] = m;
+            xe[tid] = ex;
+            xn[tid] = ng ? 1 : 0;
+            xbad |= bd;
+        }
         __syncthreads();
 #pragma unroll 4
         for (int c = part * 16; c < part * 16 + 16; ++c) {
-            const double a = S[lr][c], b = xs[c];
-            const double p = a * b;
-            const double pe = fma(a, b, -p);
-            double s, e;
-            qmlg_two_sum(hi, p, s, e);
-            hi = s;
-            lo += e + pe;
+            unsigned long long ma;
+            int ea;
+            bool na;
+            qmlg::dbl_split(S[lr][c], ma, ea, na, acc.bad);
+            const unsigned long long mb = xm[c];
+            qmlg::acc_add_mag(acc, __umul64hi(ma, mb), ma * mb, ea + xe[c], na != (xn[c] != 0));
         }
     }
-    // combine the 4 parts of a row
-    for (int off = 1; off < 4; off <<= 1) {
-        const double oh = __shfl_xor_sync(0xffffffffu, hi, off);
-        const double ol = __shfl_xor_sync(0xffffffffu, lo, off);
-        qmlg_dd_add(hi, lo, oh, ol);
-    }
+    acc.bad |= xbad;
+    // combine the 4 parts of a row (exact)
+    acc_shfl_xor_add(acc, 1);
+    acc_shfl_xor_add(acc, 2);
     const int i = i0 + lr;
-    if (part == 0 && i < n) partial[(int64_t)blockIdx.y * n + i] = make_double2(hi, lo);
+    if (part == 0 && i < n) {
+        AccPart &o = partial[(int64_t)blockIdx.y * n + i];
+        o.l0 = acc.l0;
+        o.l1 = acc.l1;
+        o.l2 = acc.l2;
+        o.l3 = acc.l3;
+        o.f = acc.f;
+        o.bad = acc.bad;
+    }
 }
 
-// r[i] = y[i] - lambda x[i] - sum_chunks partial  (double-double, rounded once)
-__global__ void residual_finish_kernel(const double2 *__restrict__ partial, int nchunks, int n,
+// r[i] = y[i] - lambda x[i] - sum_chunks partial, summed exactly, rounded once.
+__global__ void residual_finish_kernel(const AccPart *__restrict__ partial, int nchunks, int n,
                                        double lambda, const double *__restrict__ x,
                                        const double *__restrict__ y, double *__restrict__ r)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    double hi = y[i], lo = 0.0;
-    qmlg_dd_fma(hi, lo, -lambda, x[i]);
+    qmlg::Acc a;
+    qmlg::acc_init(a);
+    qmlg::acc_add_prod(a, y[i], 1.0);
+    qmlg::acc_add_prod(a, lambda, x[i], true);
     for (int c = 0; c < nchunks; ++c) {
-        const double2 p = partial[(int64_t)c * n + i];
-        qmlg_dd_add(hi, lo, -p.x, -p.y);
+        const AccPart p = partial[(int64_t)c * n + i];
+        qmlg::Acc b;
+        b.l0 = p.l0;
+        b.l1 = p.l1;
+        b.l2 = p.l2;
+        b.l3 = p.l3;
+        b.f = p.f;
+        b.bad = p.bad;
+        qmlg::acc_add_acc(a, b, true);
     }
-    r[i] = hi + lo;
+    r[i] = qmlg::acc_to_double(a);
 }
 
 // ---------------------------------------------------------------- vectors --
@@ -1212,7 +1257,7 @@ int emulated_potrs(const EmulatedFactor &f, double *x, cudaStream_t s)
 size_t residual_ws(int n)
 {
     WorkspacePlan p;
-    p.add<double2>((size_t)ceil_div(n, RES_CHUNK) * (size_t)n);
+    p.add<AccPart>((size_t)ceil_div(n, RES_CHUNK) * (size_t)n);
     return p.total();
 }
 
@@ -1220,9 +1265,9 @@ int residual_dd(const double *A, int n, int64_t lda, const double *diag, double 
                 const double *x, const double *y, double *r, Workspace &ws, cudaStream_t s)
 {
     const int nchunks = (int)ceil_div(n, RES_CHUNK);
-    double2 *partial = ws.take<double2>((size_t)nchunks * n);
+    AccPart *partial = ws.take<AccPart>((size_t)nchunks * n);
     if (partial == nullptr) return QMLG_E_WORKSPACE;
-    { symv_dd_partial_kernel<<<dim3((unsigned)ceil_div(n, RES_ROWS), nchunks), 256, 0, s>>>(
+    { symv_exact_partial_kernel<<<dim3((unsigned)ceil_div(n, RES_ROWS), nchunks), 256, 0, s>>>(
         A, lda, n, diag, x, partial); qmlg::count_launches(1); }
     { residual_finish_kernel<<<(int)ceil_div(n, 256), 256, 0, s>>>(partial, nchunks, n, lambda, x,
                                                                  y, r); qmlg::count_launches(1); }

@@ -136,6 +136,27 @@ def test_residual_dd_exact(cuda):
     assert np.array_equal(r.cpu().numpy(), np.zeros(130))
 
 
+def test_residual_is_correctly_rounded(cuda):
+    # y - (A + lam I) x summed exactly (256-bit fixed point) and rounded once: every
+    # row equals the correctly rounded exact value (Fractions), also under heavy
+    # cancellation and with entries spread over many binades
+    from fractions import Fraction
+    rng = np.random.default_rng(7)
+    n = 90
+    A = rng.standard_normal((n, n)) * np.exp2(rng.integers(-30, 30, size=(n, n)))
+    A = (A + A.T) / 2
+    x = rng.standard_normal(n) * np.exp2(rng.integers(-20, 20, size=n))
+    lam = 1e-3
+    y = (A + lam * np.eye(n)) @ x * (1 + 1e-13 * rng.standard_normal(n))
+    At = torch.from_numpy(A).to(cuda)
+    r = core.residual_dd(At, torch.from_numpy(np.diag(A).copy()).to(cuda), lam,
+                         torch.from_numpy(x).to(cuda), torch.from_numpy(y).to(cuda)).cpu().numpy()
+    for i in range(n):
+        ex = Fraction(y[i]) - Fraction(lam) * Fraction(x[i]) - sum(
+            Fraction(A[i, j]) * Fraction(x[j]) for j in range(n))
+        assert r[i] == float(ex), (i, r[i], float(ex))
+
+
 @pytest.mark.parametrize("n", [65, 700, 1100, 1500])
 def test_mixed_factor_matches_fp64_factor(cuda, oracle, krr_system, n):
     # the tensor-core factor (emulated FP64 trailing updates) against the plain FP64 one
