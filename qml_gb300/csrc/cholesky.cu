@@ -70,7 +70,6 @@ constexpr int POTRF_THREADS = 256;
 // scheduler's FP64 pipe (warp 7 only joins the barriers).
 constexpr int POTRF_WORKERS = 192;
 constexpr int POTRF_PIVOT = 96;
-constexpr int POTRF_BATCH = 3;  // elements whose loads are issued before their FMAs
 
 // Pivot of column c: rd[c] <- 1/sqrt(S_cc) (> 0), rd2[c] <- 1/S_cc; S_cc keeps the
 // pivot (the factor's diagonal sqrt(S_cc) = S_cc rd[c] is formed at write-back).
@@ -91,24 +90,34 @@ __device__ __forceinline__ void potrf_pivot(double (*S)[NB + 1], double *rd, dou
     rd2[c] = y * y;
 }
 
+// Barrier of the 192 worker threads only (the pivot warp does not wait for it).
+__device__ __forceinline__ void potrf_workers_sync()
+{
+    asm volatile("bar.sync 1, 192;" ::: "memory");
+}
+
 __global__ void __launch_bounds__(POTRF_THREADS)
 potrf_diag_kernel(double *__restrict__ A, int64_t lda, int n, int k0, double shift,
                   int *__restrict__ info)
 {
-    // Right-looking in shared memory, one barrier per column.  In phase c every
-    // element with c < s <= r takes S_rs -= S_rc S_sc / S_cc (the unscaled column c
-    // and rd2[c] = 1/S_cc).  The elements are listed in `order` by s descending, r
+    // Right-looking in shared memory.  One FP64 warp instruction occupies a
+    // scheduler's FP64 pipe for ~64 cycles whatever its active lanes, so the
+    // update is laid out for dense warps and one FMA per element.  Phase c: warps
+    // 0 and 4 scale column c (lc[r] = S_rc / S_cc, with rd2[c] = 1/S_cc), the workers
+    // meet at their own barrier, then every element with c < s <= r takes
+    // S_rs -= lc[r] S_sc.  The elements are listed in `order` by s descending, r
     // descending, so phase c's are the first tri_prefix(c) entries and the last of
-    // them is the next diagonal S_{c+1,c+1}: the workers share the others evenly,
-    // while the pivot thread updates that diagonal and takes its pivot at once, so
-    // the pivot latency overlaps the updates.  rd[c] is written one phase before it
-    // is read, so rd[c] == 0 is a race-free failure signal.  Columns are scaled by rd
-    // at write-back.
+    // them is the next diagonal S_{c+1,c+1}: the workers take the others in turn
+    // (each issues the next element's loads before this one's store), while the
+    // pivot thread updates that diagonal and takes its pivot at once, so the pivot
+    // latency overlaps the updates.  rd[c] is written one phase before it is read,
+    // so rd[c] == 0 is a race-free failure signal.  Columns are scaled by rd at
+    // write-back.
     __shared__ double S[NB][NB + 1];
-    __shared__ double rd[NB], rd2[NB];
+    __shared__ double rd[NB], rd2[NB], lc[NB];
     __shared__ unsigned short order[tri_prefix(0)];
     if (*info != 0) return;
-    const int tid = threadIdx.x, warp = tid >> 5;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int nb = min(NB, n - k0);
 #pragma unroll
     for (int e = tid; e < NB * NB; e += POTRF_THREADS) {  // loads issued back to back
@@ -128,41 +137,55 @@ potrf_diag_kernel(double *__restrict__ A, int64_t lda, int n, int k0, double shi
     if (tid == POTRF_PIVOT) potrf_pivot(S, rd, rd2, 0, k0, nb, info);
     __syncthreads();
     const bool worker = warp != 3 && warp != 7;
-    const int wid = (warp < 3 ? warp : warp - 1) * 32 + (tid & 31);
-    for (int c = 0; c < NB; ++c) {
+    const int wid = (warp < 3 ? warp : warp - 1) * 32 + lane;
+    for (int c = 0; c + 1 < NB; ++c) {
         if (__double_as_longlong(rd[c]) == 0) return;
         const double y2 = rd2[c];
         if (tid == POTRF_PIVOT) {
-            if (c + 1 < NB) {
-                const double v = S[c + 1][c];
-                S[c + 1][c + 1] = fma(-v * y2, v, S[c + 1][c + 1]);
-                potrf_pivot(S, rd, rd2, c + 1, k0, nb, info);
-            }
+            const double v = S[c + 1][c];
+            S[c + 1][c + 1] = fma(-v * y2, v, S[c + 1][c + 1]);
+            potrf_pivot(S, rd, rd2, c + 1, k0, nb, info);
         } else if (worker) {
+            if (warp == 0 || warp == 4) {
+                const int r = c + 1 + lane + (warp == 4 ? 32 : 0);
+                if (r < NB) lc[r] = S[r][c] * y2;
+            }
+            potrf_workers_sync();
             const int cnt = tri_prefix(c) - 1;
-            for (int e0 = wid; e0 < cnt; e0 += POTRF_BATCH * POTRF_WORKERS) {
-                // loads of a batch of elements first, then their FMAs and stores
-                int rr[POTRF_BATCH], ss[POTRF_BATCH];
-                double x[POTRF_BATCH], u[POTRF_BATCH], v[POTRF_BATCH];
-#pragma unroll
-                for (int k = 0; k < POTRF_BATCH; ++k) {
-                    const int e = e0 + k * POTRF_WORKERS;
-                    if (e < cnt) {
-                        const unsigned code = order[e];
-                        rr[k] = (int)(code >> 8);
-                        ss[k] = (int)(code & 255u);
-                        x[k] = S[rr[k]][ss[k]];
-                        u[k] = S[rr[k]][c];
-                        v[k] = S[ss[k]][c];
-                    }
+            int e = wid, r = 0, sc = 0;
+            double x = 0.0, a = 0.0, b = 0.0;
+            if (e < cnt) {
+                const unsigned code = order[e];
+                r = (int)(code >> 8);
+                sc = (int)(code & 255u);
+                x = S[r][sc];
+                a = lc[r];
+                b = S[sc][c];
+            }
+            while (e < cnt) {
+                const int en = e + POTRF_WORKERS;
+                int rn = 0, sn = 0;
+                double xn = 0.0, an = 0.0, bn = 0.0;
+                if (en < cnt) {
+                    const unsigned code = order[en];
+                    rn = (int)(code >> 8);
+                    sn = (int)(code & 255u);
+                    xn = S[rn][sn];
+                    an = lc[rn];
+                    bn = S[sn][c];
                 }
-#pragma unroll
-                for (int k = 0; k < POTRF_BATCH; ++k)
-                    if (e0 + k * POTRF_WORKERS < cnt) S[rr[k]][ss[k]] = fma(-u[k] * y2, v[k], x[k]);
+                S[r][sc] = fma(-a, b, x);
+                e = en;
+                r = rn;
+                sc = sn;
+                x = xn;
+                a = an;
+                b = bn;
             }
         }
         __syncthreads();
     }
+    if (__double_as_longlong(rd[NB - 1]) == 0) return;
     for (int e = tid; e < nb * NB; e += blockDim.x) {
         const int r = e >> 6, c = e & 63;
         if (c <= r) A[(int64_t)(k0 + r) * lda + (k0 + c)] = S[r][c] * rd[c];
@@ -714,144 +737,253 @@ __device__ __forceinline__ double gemv64_col(const double *__restrict__ M, int64
     return s;
 }
 
-// Flag-driven triangular solves with the block inverses, one cooperative launch per
-// direction and no grid-wide barrier.  CTA b owns row blocks b, b + grid, ... in
-// solve order.  For its block i it applies every finished block k (forward: k < i,
-// L[i][k] z_k; backward: k > i, L[k][i]^T x_k) as soon as k's ready flag is set,
-// then applies the diagonal-block inverse and publishes block i (stores, fence,
-// release flag).  All CTAs are resident (cooperative launch) and each takes its
-// blocks in solve order, so the lowest unfinished block always has its inputs and
-// every wait ends; a wait is still bounded: after kFlagWaitLimit polls the CTA sets
-// bit 2 of *err and returns, and the CTAs that wait on it follow.  Solved values
-// are read with ld.global.cg (L2), never through a possibly stale L1 line.
+// Triangular solves with the block inverses, one cooperative launch per direction
+// and no flag or fence: each solved entry is its own ready signal.  The output
+// vectors are first filled with a signalling-NaN sentinel that no arithmetic result
+// carries; a solved entry is stored once with a relaxed store, and a reader polls
+// exactly the entries it needs until none is the sentinel.  With the couplings of
+// neighbouring blocks
+//   M_i = L_ii^-1 L_i,i-1        P_i = (L_i+1,i L_ii^-1)^T
+// block i of L z = b is
+//   z_i = L_ii^-1 (b_i - sum_{k < i-1} L_ik z_k) - M_i z_{i-1}
+// and block i of L^T x = z is
+//   x_i = L_ii^-T (z_i - sum_{k > i+1} L_ki^T x_k) - P_i x_{i+1},
+// so between a neighbour's result and this block's lies one 64 x 64 product; the
+// rest is done while the neighbour is being solved, with this block's operands
+// loaded before any wait.  CTA b owns blocks b, b + grid, ... in solve order and all
+// CTAs are resident (cooperative launch), so the lowest unsolved block always has
+// its inputs and every wait ends.  A wait is still bounded: after kFlagWaitLimit
+// polls, or once another CTA has given up, the thread sets bit 2 of *err, the
+// entries it still lacks read as zero, and the launch runs to its end.
 
 constexpr int kFlagWaitLimit = 1 << 21;
+constexpr unsigned long long kUnsolved = 0x7FF0DEADBEEFCAFEull;  // a signalling NaN
 
-__device__ __forceinline__ int ld_acquire(const int *p)
+__device__ __forceinline__ double ld_relaxed_f64(const double *p)
 {
-    int v;
-    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    double v;
+    asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];" : "=d"(v) : "l"(p) : "memory");
     return v;
 }
 
-__device__ __forceinline__ void st_release(int *p, int v)
+__device__ __forceinline__ int ld_relaxed_s32(const int *p)
 {
-    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+    int v;
+    asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
 }
 
-__device__ __forceinline__ bool wait_flag(const int *p)
+__device__ __forceinline__ bool is_unsolved(double v)
 {
-    for (int it = 0; it < kFlagWaitLimit; ++it) {
-        if (ld_acquire(p) != 0) return true;
-        __nanosleep(64);
+    return (unsigned long long)__double_as_longlong(v) == kUnsolved;
+}
+
+// Arithmetic never returns the sentinel's payload; a NaN that somehow carries it is
+// stored as the canonical NaN so that it still reads as solved.
+__device__ __forceinline__ void st_solved(double *p, double v)
+{
+    if (is_unsolved(v)) v = __longlong_as_double(0x7FFFFFFFFFFFFFFFll);
+    asm volatile("st.relaxed.gpu.global.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
+}
+
+// z[c] = v[4c] for 4c < count (c < 16; the rest are zero), once none is unsolved.
+__device__ __forceinline__ void read_solved16(const double *v, int count, double (&z)[16],
+                                              int *err, volatile int *abort)
+{
+    for (int it = 0;; ++it) {
+        bool ok = true;
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+            z[c] = 4 * c < count ? ld_relaxed_f64(v + 4 * c) : 0.0;
+            ok &= !is_unsolved(z[c]);
+        }
+        if (ok) return;
+        bool give_up = *abort != 0 || it >= kFlagWaitLimit;
+        if (!give_up && (it & 1023) == 1023) give_up = (ld_relaxed_s32(err) & 2) != 0;
+        if (give_up) {
+            *abort = 1;
+            atomicOr(err, 2);
+#pragma unroll
+            for (int c = 0; c < 16; ++c)
+                if (is_unsolved(z[c])) z[c] = 0.0;
+            return;
+        }
+        __nanosleep(32);
     }
-    return false;
 }
 
-// Publishes a solved block: every thread's stores are fenced before the flag.
-__device__ __forceinline__ void publish_block(int *flag)
+__global__ void fill_unsolved_kernel(double *__restrict__ v, int count)
 {
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) st_release(flag, 1);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) v[i] = __longlong_as_double((long long)kUnsolved);
 }
 
+// The couplings M_i (i >= 1) and P_i (i < last) of the solves above, 64 x 64
+// row-major each, one CTA per block; rows of L beyond n read as zero (the diagonal
+// inverse of a short last block is padded with the identity).
+__global__ void __launch_bounds__(256)
+trsv_couple_kernel(const double *__restrict__ A, int64_t lda, int n,
+                   const double *__restrict__ Linv, double *__restrict__ M,
+                   double *__restrict__ P)
+{
+    __shared__ double T[NB][NB + 1];
+    const int i = blockIdx.x, i0 = i * NB, nblk = (n + NB - 1) / NB;
+    const int tid = threadIdx.x, r = tid >> 2, q = tid & 3;
+    const double *Li = Linv + (int64_t)i * NB * NB;
+    if (i > 0) {
+        // M_i[r][c] = sum_{u <= r} Linv_i[r][u] L_i,i-1[u][c]
+        const int nb = min(NB, n - i0);
+        for (int e = tid; e < NB * NB; e += blockDim.x) {
+            const int u = e >> 6, c = e & 63;
+            T[u][c] = u < nb ? A[(int64_t)(i0 + u) * lda + (i0 - NB + c)] : 0.0;
+        }
+        __syncthreads();
+        double acc[16];
+#pragma unroll
+        for (int c = 0; c < 16; ++c) acc[c] = 0.0;
+        for (int u = 0; u <= r; ++u) {
+            const double l = Li[r * NB + u];
+#pragma unroll
+            for (int c = 0; c < 16; ++c) acc[c] = fma(l, T[u][q + 4 * c], acc[c]);
+        }
+        double *dst = M + (int64_t)i * NB * NB + r * NB + q;
+#pragma unroll
+        for (int c = 0; c < 16; ++c) dst[4 * c] = acc[c];
+        __syncthreads();
+    }
+    if (i + 1 < nblk) {
+        // P_i[t][c] = sum_{u >= t} Linv_i[u][t] L_i+1,i[c][u]
+        const int nb1 = min(NB, n - i0 - NB), t = r;
+        for (int e = tid; e < NB * NB; e += blockDim.x) {
+            const int c = e >> 6, u = e & 63;
+            T[c][u] = c < nb1 ? A[(int64_t)(i0 + NB + c) * lda + (i0 + u)] : 0.0;
+        }
+        __syncthreads();
+        double acc[16];
+#pragma unroll
+        for (int c = 0; c < 16; ++c) acc[c] = 0.0;
+        for (int u = t; u < NB; ++u) {
+            const double l = Li[u * NB + t];
+#pragma unroll
+            for (int c = 0; c < 16; ++c) acc[c] = fma(l, T[q + 4 * c][u], acc[c]);
+        }
+        double *dst = P + (int64_t)i * NB * NB + t * NB + q;
+#pragma unroll
+        for (int c = 0; c < 16; ++c) dst[4 * c] = acc[c];
+    }
+}
+
+// L z = b.  Thread (r, q) = (tid / 4, tid % 4) owns row r of a block and the
+// columns q, q + 4, ..., q + 60; the four threads of a row combine by shuffles.
 __global__ void __launch_bounds__(TRSV_THREADS)
-trsv_fwd_flag_kernel(const double *__restrict__ A, int64_t lda, int n,
-                     const double *__restrict__ Linv, double *x, int *flags, int *err)
+trsv_fwd_solved_kernel(const double *__restrict__ A, int64_t lda, int n,
+                       const double *__restrict__ Linv, const double *__restrict__ M,
+                       const double *__restrict__ b, double *z, int *err)
 {
-    __shared__ double bb[NB];
-    __shared__ int ready;
+    __shared__ double bb[2][NB];
+    __shared__ int abort_flag;
+    if (threadIdx.x == 0) abort_flag = 0;
+    __syncthreads();
     const int tid = threadIdx.x, r = tid >> 2, q = tid & 3;
     const int nblk = (n + NB - 1) / NB;
-    for (int i = blockIdx.x; i < nblk; i += gridDim.x) {
+    int par = 0;
+    for (int i = blockIdx.x; i < nblk; i += gridDim.x, par ^= 1) {
         const int i0 = i * NB, nb = min(NB, n - i0);
         const bool live = r < nb;
+        const int64_t blk = (int64_t)i * NB * NB + r * NB + q;
+        double li[16], mi[16];
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+            li[c] = Linv[blk + 4 * c];
+            mi[c] = i > 0 ? M[blk + 4 * c] : 0.0;
+        }
+        const double br = live ? b[i0 + r] : 0.0;
         const double *arow = A + (int64_t)(i0 + (live ? r : 0)) * lda + q;
         double s = 0.0;
-        int k = 0;
-        while (k < i) {
-            if (tid == 0) {
-                int kk = k;
-                if (!wait_flag(flags + kk)) {
-                    atomicOr(err, 2);
-                    kk = -1;
-                } else {
-                    ++kk;
-                    while (kk < i && ld_acquire(flags + kk) != 0) ++kk;
-                }
-                ready = kk;
-            }
-            __syncthreads();
-            const int kend = ready;
-            __syncthreads();
-            if (kend < 0) return;
-            if (live)
-                for (; k < kend; ++k) {
-                    const double *lp = arow + k * NB;
-                    const double *zp = x + k * NB + q;
+        for (int k = 0; k + 1 < i; ++k) {  // blocks k < i - 1 are full
+            double lk[16], zk[16];
 #pragma unroll
-                    for (int c = 0; c < 16; ++c) s = fma(lp[4 * c], __ldcg(zp + 4 * c), s);
-                }
-            k = kend;
+            for (int c = 0; c < 16; ++c) lk[c] = live ? arow[(int64_t)k * NB + 4 * c] : 0.0;
+            read_solved16(z + k * NB + q, NB - q, zk, err, &abort_flag);
+#pragma unroll
+            for (int c = 0; c < 16; ++c) s = fma(lk[c], zk[c], s);
         }
         s += __shfl_xor_sync(0xffffffffu, s, 1);
         s += __shfl_xor_sync(0xffffffffu, s, 2);
-        if (q == 0) bb[r] = live ? x[i0 + r] - s : 0.0;
+        if (q == 0) bb[par][r] = br - s;
         __syncthreads();
-        const double z = gemv64_row(Linv + (int64_t)i * NB * NB, NB, bb, tid, NB);
-        if (q == 0 && live) x[i0 + r] = z;
-        publish_block(flags + i);
+        double w = 0.0;
+#pragma unroll
+        for (int c = 0; c < 16; ++c) w = fma(li[c], bb[par][q + 4 * c], w);
+        if (i > 0) {
+            double zk[16];
+            read_solved16(z + (i - 1) * NB + q, NB - q, zk, err, &abort_flag);
+#pragma unroll
+            for (int c = 0; c < 16; ++c) w = fma(-mi[c], zk[c], w);
+        }
+        w += __shfl_xor_sync(0xffffffffu, w, 1);
+        w += __shfl_xor_sync(0xffffffffu, w, 2);
+        if (q == 0 && live) st_solved(z + i0 + r, w);
     }
 }
 
+// L^T x = z, blocks in reverse order.  Thread (t, q) owns column t of a block and the
+// rows q, q + 4, ..., q + 60 of the blocks below it.  The solution goes to x and, as
+// the ready signal, to xs.
 __global__ void __launch_bounds__(TRSV_THREADS)
-trsv_bwd_flag_kernel(const double *__restrict__ A, int64_t lda, int n,
-                     const double *__restrict__ Linv, double *x, int *flags, int *err)
+trsv_bwd_solved_kernel(const double *__restrict__ A, int64_t lda, int n,
+                       const double *__restrict__ Linv, const double *__restrict__ P,
+                       const double *__restrict__ z, double *xs, double *__restrict__ x,
+                       int *err)
 {
-    __shared__ double bb[NB];
-    __shared__ int ready;
+    __shared__ double bb[2][NB];
+    __shared__ int abort_flag;
+    if (threadIdx.x == 0) abort_flag = 0;
+    __syncthreads();
     const int tid = threadIdx.x, t = tid >> 2, q = tid & 3;
     const int nblk = (n + NB - 1) / NB;
-    for (int j = blockIdx.x; j < nblk; j += gridDim.x) {
-        const int i = nblk - 1 - j;
-        const int i0 = i * NB, nb = min(NB, n - i0);
-        double s = 0.0;
-        int k = nblk - 1;
-        while (k > i) {
-            if (tid == 0) {
-                int kk = k;
-                if (!wait_flag(flags + kk)) {
-                    atomicOr(err, 2);
-                    kk = -2;
-                } else {
-                    --kk;
-                    while (kk > i && ld_acquire(flags + kk) != 0) --kk;
-                }
-                ready = kk;
-            }
-            __syncthreads();
-            const int kend = ready;
-            __syncthreads();
-            if (kend == -2) return;
-            // i < nblk - 1 here, so block i is full and columns i0 + t exist
-            for (; k > kend; --k) {
-                const int k0 = k * NB, nbk = min(NB, n - k0);
+    int par = 0;
+    for (int j = blockIdx.x; j < nblk; j += gridDim.x, par ^= 1) {
+        const int i = nblk - 1 - j, i0 = i * NB, nb = min(NB, n - i0);
+        const int64_t blk = (int64_t)i * NB * NB;
+        double li[16], pi[16];
 #pragma unroll
-                for (int c = 0; c < 16; ++c) {
-                    const int rr = q + 4 * c;
-                    if (rr < nbk)
-                        s = fma(A[(int64_t)(k0 + rr) * lda + i0 + t], __ldcg(x + k0 + rr), s);
-                }
-            }
+        for (int c = 0; c < 16; ++c) {
+            li[c] = Linv[blk + (q + 4 * c) * NB + t];
+            pi[c] = i + 1 < nblk ? P[blk + t * NB + q + 4 * c] : 0.0;
+        }
+        const double zt = t < nb ? z[i0 + t] : 0.0;
+        double s = 0.0;
+        for (int k = nblk - 1; k > i + 1; --k) {  // block i is full here
+            const int k0 = k * NB, cnt = min(NB, n - k0) - q;
+            double lk[16], xk[16];
+#pragma unroll
+            for (int c = 0; c < 16; ++c)
+                lk[c] = 4 * c < cnt ? A[(int64_t)(k0 + q + 4 * c) * lda + i0 + t] : 0.0;
+            read_solved16(xs + k0 + q, cnt, xk, err, &abort_flag);
+#pragma unroll
+            for (int c = 0; c < 16; ++c) s = fma(lk[c], xk[c], s);
         }
         s += __shfl_xor_sync(0xffffffffu, s, 1);
         s += __shfl_xor_sync(0xffffffffu, s, 2);
-        if (q == 0) bb[t] = t < nb ? x[i0 + t] - s : 0.0;
+        if (q == 0) bb[par][t] = zt - s;
         __syncthreads();
-        const double v = gemv64_col(Linv + (int64_t)i * NB * NB, NB, bb, tid);
-        if (q == 0 && t < nb) x[i0 + t] = v;
-        publish_block(flags + i);
+        double w = 0.0;
+#pragma unroll
+        for (int c = 0; c < 16; ++c) w = fma(li[c], bb[par][q + 4 * c], w);
+        if (i + 1 < nblk) {
+            const int k0 = i0 + NB;
+            double xk[16];
+            read_solved16(xs + k0 + q, min(NB, n - k0) - q, xk, err, &abort_flag);
+#pragma unroll
+            for (int c = 0; c < 16; ++c) w = fma(-pi[c], xk[c], w);
+        }
+        w += __shfl_xor_sync(0xffffffffu, w, 1);
+        w += __shfl_xor_sync(0xffffffffu, w, 2);
+        if (q == 0 && t < nb) {
+            st_solved(xs + i0 + t, w);
+            x[i0 + t] = w;
+        }
     }
 }
 
@@ -963,10 +1095,10 @@ int trsv_grid(int &grid)
             e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, trsv_bwd_coop_kernel,
                                                               TRSV_THREADS, 0);
         if (e == cudaSuccess)
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm3, trsv_fwd_flag_kernel,
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm3, trsv_fwd_solved_kernel,
                                                               TRSV_THREADS, 0);
         if (e == cudaSuccess)
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm4, trsv_bwd_flag_kernel,
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm4, trsv_bwd_solved_kernel,
                                                               TRSV_THREADS, 0);
         if (e != cudaSuccess) {
             status = qmlg::set_cuda_error(e);
@@ -1074,7 +1206,8 @@ size_t emulated_factor_ws(int n)
     p.add<int>(rpad);
     p.add<int>(4);                                             // device error flag
     p.add<double>((size_t)ceil_div(n < 1 ? 1 : n, NB) * NB * NB);  // diagonal-block inverses
-    p.add<int>((size_t)2 * ceil_div(n < 1 ? 1 : n, NB));           // triangular-solve flags
+    p.add<double>((size_t)2 * ceil_div(n < 1 ? 1 : n, NB) * NB * NB);  // block couplings
+    p.add<double>((size_t)2 * ceil_div(n < 1 ? 1 : n, NB) * NB);       // solved entries
     return p.total();
 }
 
@@ -1146,9 +1279,10 @@ int emulated_factor(double *A, int n, int64_t lda, double shift, Workspace &ws, 
     int *exp_in = ws.take<int>((size_t)rpad);
     int *d_err = ws.take<int>(4);
     double *linv = ws.take<double>((size_t)ceil_div(n, NB) * NB * NB);
-    int *flags = ws.take<int>((size_t)2 * ceil_div(n, NB));
+    double *couple = ws.take<double>((size_t)2 * ceil_div(n, NB) * NB * NB);
+    double *solved = ws.take<double>((size_t)2 * ceil_div(n, NB) * NB);
     if (dig_out == nullptr || exp_out == nullptr || dig_in == nullptr || exp_in == nullptr ||
-        d_err == nullptr || linv == nullptr || flags == nullptr)
+        d_err == nullptr || linv == nullptr || couple == nullptr || solved == nullptr)
         return QMLG_E_WORKSPACE;
     cudaError_t e = cudaMemsetAsync(d_err, 0, sizeof(int), s);
     if (e != cudaSuccess) return set_cuda_error(e);
@@ -1203,9 +1337,12 @@ int emulated_factor(double *A, int n, int64_t lda, double shift, Workspace &ws, 
         }
     }
     if (st != QMLG_OK) return st;
+    const unsigned nblk = (unsigned)ceil_div(n, NB);
     if (np == n) {
-        invert_diag_blocks_kernel<<<(unsigned)ceil_div(n, NB), 64, 0, s>>>(A, lda, n, linv);
-        count_launches(1);
+        invert_diag_blocks_kernel<<<nblk, 64, 0, s>>>(A, lda, n, linv);
+        trsv_couple_kernel<<<nblk, 256, 0, s>>>(A, lda, n, linv, couple,
+                                                couple + (size_t)nblk * NB * NB);
+        count_launches(2);
     }
     f.A = A;
     f.n = n;
@@ -1213,7 +1350,9 @@ int emulated_factor(double *A, int n, int64_t lda, double shift, Workspace &ws, 
     f.slices = slices;
     f.d_err = d_err;
     f.Linv = linv;
-    f.flags = flags;
+    f.M = couple;
+    f.P = couple + (size_t)nblk * NB * NB;
+    f.solved = solved;
     return check_launch();
 }
 
@@ -1240,17 +1379,18 @@ int emulated_potrs(const EmulatedFactor &f, double *x, cudaStream_t s)
         { trsv_single_cta_kernel<<<1, TRSV1_THREADS, 0, s>>>(A, lda, n, Linv, x); count_launches(1); }
         return check_launch();
     }
-    const int nblk = (int)ceil_div(n, NB);
-    cudaError_t e = cudaMemsetAsync(f.flags, 0, sizeof(int) * 2 * (size_t)nblk, s);
-    if (e != cudaSuccess) return set_cuda_error(e);
-    int *fwd_flags = f.flags, *bwd_flags = f.flags + nblk, *err = f.d_err;
-    void *fa[] = {(void *)&A, (void *)&lda, (void *)&n, (void *)&Linv, (void *)&x,
-                  (void *)&fwd_flags, (void *)&err};
-    void *ba[] = {(void *)&A, (void *)&lda, (void *)&n, (void *)&Linv, (void *)&x,
-                  (void *)&bwd_flags, (void *)&err};
-    st = launch_cooperative((const void *)trsv_fwd_flag_kernel, grid, TRSV_THREADS, fa, s);
+    const int nblk = (int)ceil_div(n, NB), count = 2 * nblk * NB;
+    { fill_unsolved_kernel<<<(unsigned)ceil_div(count, 256), 256, 0, s>>>(f.solved, count); count_launches(1); }
+    const double *M = f.M, *P = f.P, *zc = f.solved;
+    double *z = f.solved, *xs = f.solved + (size_t)nblk * NB;
+    int *err = f.d_err;
+    void *fa[] = {(void *)&A, (void *)&lda, (void *)&n, (void *)&Linv, (void *)&M,
+                  (void *)&x, (void *)&z, (void *)&err};
+    void *ba[] = {(void *)&A, (void *)&lda, (void *)&n, (void *)&Linv, (void *)&P,
+                  (void *)&zc, (void *)&xs, (void *)&x, (void *)&err};
+    st = launch_cooperative((const void *)trsv_fwd_solved_kernel, grid, TRSV_THREADS, fa, s);
     if (st == QMLG_OK)
-        st = launch_cooperative((const void *)trsv_bwd_flag_kernel, grid, TRSV_THREADS, ba, s);
+        st = launch_cooperative((const void *)trsv_bwd_solved_kernel, grid, TRSV_THREADS, ba, s);
     return st;
 }
 

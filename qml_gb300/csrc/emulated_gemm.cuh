@@ -48,7 +48,9 @@ struct EmulatedFactor {
     int slices = 0;
     int *d_err = nullptr;  // device flag: a bounded tensor-core wait gave up
     const double *Linv = nullptr;  // [n/64][64][64] inverses of the diagonal blocks
-    int *flags = nullptr;          // [2][n/64] ready flags of the triangular solves
+    const double *M = nullptr;     // [n/64][64][64] L_ii^-1 L_i,i-1 (the solves' couplings)
+    const double *P = nullptr;     // [n/64][64][64] (L_i+1,i L_ii^-1)^T
+    double *solved = nullptr;      // [2][n/64][64] solved entries of the two solves
 };
 
 size_t emulated_factor_ws(int n);
