@@ -987,8 +987,90 @@ trsv_bwd_solved_kernel(const double *__restrict__ A, int64_t lda, int n,
     }
 }
 
+// Capture-safe triangular solves with the block inverses: one launch per 64-row
+// block and direction, so no CTA ever waits for another and any number of them may
+// run side by side (batched, graph-recorded solves).  Launch k of L z = b: CTA 0
+// applies z_{k-1} to block k and solves it with the block inverse, while CTAs 1..
+// apply z_{k-1} to the rows below block k (a warp per row).  Launch k of L^T x = z
+// (k descending): CTA 0 applies x_{k+1} to block k and solves it with the
+// transposed inverse, while CTAs 1.. apply x_{k+1} to the entries left of block k
+// (four threads per entry).
+constexpr int STEP_THREADS = 256;
+
+__global__ void __launch_bounds__(STEP_THREADS)
+trsv_fwd_step_kernel(const double *__restrict__ A, int64_t lda, int n,
+                     const double *__restrict__ Linv, double *__restrict__ x, int k)
+{
+    __shared__ double zp[NB], bb[NB];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int k0 = k * NB, nb = min(NB, n - k0), kp = k0 - NB;  // block k-1 is full
+    if (k > 0 && tid < NB) zp[tid] = x[kp + tid];
+    __syncthreads();
+    if (blockIdx.x == 0) {
+        const double s = k > 0 ? gemv64_row(A + (int64_t)k0 * lda + kp, lda, zp, tid, nb) : 0.0;
+        if ((tid & 3) == 0) bb[tid >> 2] = (tid >> 2) < nb ? x[k0 + (tid >> 2)] - s : 0.0;
+        __syncthreads();
+        const double z = gemv64_row(Linv + (int64_t)k * NB * NB, NB, bb, tid, NB);
+        if ((tid & 3) == 0 && (tid >> 2) < nb) x[k0 + (tid >> 2)] = z;
+    } else if (k > 0) {
+        constexpr int nw = STEP_THREADS / 32;
+        const int tw = (gridDim.x - 1) * nw;
+        for (int r = k0 + NB + (blockIdx.x - 1) * nw + warp; r < n; r += tw) {
+            const double *row = A + (int64_t)r * lda + kp;
+            double sum = fma(row[lane], zp[lane], row[lane + 32] * zp[lane + 32]);
+            for (int off = 16; off > 0; off >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, off);
+            if (lane == 0) x[r] -= sum;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(STEP_THREADS)
+trsv_bwd_step_kernel(const double *__restrict__ A, int64_t lda, int n,
+                     const double *__restrict__ Linv, double *__restrict__ x, int k)
+{
+    __shared__ double xp[NB], bb[NB];
+    const int tid = threadIdx.x, t = tid >> 2, q = tid & 3;
+    const int nblk = (n + NB - 1) / NB;
+    const int k0 = k * NB, nb = min(NB, n - k0), k1 = k0 + NB;
+    const int nbp = k + 1 < nblk ? min(NB, n - k1) : 0;  // rows of block k+1
+    if (tid < NB) xp[tid] = tid < nbp ? x[k1 + tid] : 0.0;
+    __syncthreads();
+    if (blockIdx.x == 0) {
+        // block k is full when block k+1 exists
+        double s = 0.0;
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+            const int r = q + 4 * c;
+            if (r < nbp) s = fma(A[(int64_t)(k1 + r) * lda + k0 + t], xp[r], s);
+        }
+        s += __shfl_xor_sync(0xffffffffu, s, 1);
+        s += __shfl_xor_sync(0xffffffffu, s, 2);
+        if (q == 0) bb[t] = t < nb ? x[k0 + t] - s : 0.0;
+        __syncthreads();
+        const double v = gemv64_col(Linv + (int64_t)k * NB * NB, NB, bb, tid);
+        if (q == 0 && t < nb) x[k0 + t] = v;
+    } else if (nbp > 0) {
+        constexpr int per = STEP_THREADS / 4;
+        const int tc = (gridDim.x - 1) * per;
+        for (int c0 = (blockIdx.x - 1) * per; c0 < k0; c0 += tc) {
+            const int c = c0 + t;
+            double s = 0.0;
+            if (c < k0) {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int r = q + 4 * j;
+                    if (r < nbp) s = fma(A[(int64_t)(k1 + r) * lda + c], xp[r], s);
+                }
+            }
+            s += __shfl_xor_sync(0xffffffffu, s, 1);
+            s += __shfl_xor_sync(0xffffffffu, s, 2);
+            if (q == 0 && c < k0) x[c] -= s;
+        }
+    }
+}
+
 // Both triangular solves in one CTA, with the block inverses: no waiting between
-// CTAs, so any number of these may run at once (batched, graph-recorded solves).
+// CTAs (used for matrices of one or two blocks, where one launch is cheapest).
 constexpr int TRSV1_THREADS = 512;
 
 __global__ void __launch_bounds__(TRSV1_THREADS)
@@ -1376,7 +1458,22 @@ int emulated_potrs(const EmulatedFactor &f, double *x, cudaStream_t s)
     int64_t lda = f.lda;
     int n = f.n;
     if (!cooperative_allowed(s)) {
-        { trsv_single_cta_kernel<<<1, TRSV1_THREADS, 0, s>>>(A, lda, n, Linv, x); count_launches(1); }
+        const int nblk = (int)ceil_div(n, NB);
+        if (nblk <= 2) {
+            { trsv_single_cta_kernel<<<1, TRSV1_THREADS, 0, s>>>(A, lda, n, Linv, x); count_launches(1); }
+            return check_launch();
+        }
+        const int64_t cap = 4 * (int64_t)std::max(1, tc_sm_count());
+        for (int k = 0; k < nblk; ++k) {
+            const int below = n - (k + 1) * NB;
+            const int extra = (k > 0 && below > 0) ? (int)std::min<int64_t>(ceil_div(below, 32), cap) : 0;
+            trsv_fwd_step_kernel<<<1 + extra, STEP_THREADS, 0, s>>>(A, lda, n, Linv, x, k);
+        }
+        for (int k = nblk - 1; k >= 0; --k) {
+            const int extra = (k + 1 < nblk && k > 0) ? (int)std::min<int64_t>(ceil_div(k * NB, 64), cap) : 0;
+            trsv_bwd_step_kernel<<<1 + extra, STEP_THREADS, 0, s>>>(A, lda, n, Linv, x, k);
+        }
+        count_launches(2 * nblk);
         return check_launch();
     }
     const int nblk = (int)ceil_div(n, NB), count = 2 * nblk * NB;

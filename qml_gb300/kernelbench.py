@@ -5,9 +5,13 @@
     python -m qml_gb300.kernelbench lapl  --n 8192               # fixed-point Laplacian K
     python -m qml_gb300.kernelbench predict --n 20000 --m 5000   # tensor-core fused prediction
     python -m qml_gb300.kernelbench cm    --n 25000              # sorted Coulomb matrices
+    python -m qml_gb300.kernelbench factor --n 20000             # mixed Cholesky of the KRR K
+    python -m qml_gb300.kernelbench solve  --n 20000             # mixed solve with refinement
 
 Each command runs the kernel `--reps` times after one warm-up call and prints the
-mean time per call (CUDA events on the launching stream).
+mean time per call (CUDA events on the launching stream).  `factor` and `solve` work
+on the Gaussian K (sigma, lambda = 1e-8) of seeded synthetic molecules and restore K
+before every call, outside the timed region.
 """
 from __future__ import annotations
 
@@ -29,12 +33,13 @@ def _features(n, seed):
 
 def main(argv=None):
     p = argparse.ArgumentParser()
-    p.add_argument("kernel", choices=["syrk", "gauss", "lapl", "predict", "cm"])
+    p.add_argument("kernel", choices=["syrk", "gauss", "lapl", "predict", "cm", "factor", "solve"])
     p.add_argument("--n", type=int, default=8192)
     p.add_argument("--m", type=int, default=2048)
     p.add_argument("--k", type=int, default=512)
     p.add_argument("--sigma", type=float, default=1000.0)
     p.add_argument("--reps", type=int, default=2)
+    p.add_argument("--lam", type=float, default=1e-8)
     a = p.parse_args(argv)
     dev = torch.device("cuda")
     g = torch.Generator(device=dev).manual_seed(7)
@@ -53,6 +58,30 @@ def main(argv=None):
         alpha = torch.rand(a.n, dtype=torch.float64, device=dev, generator=g)
         run = lambda: core.predict("gaussian", X[:a.n], X[a.n:], a.sigma, alpha,  # noqa: E731
                                    emulated=True)
+    elif a.kernel in ("factor", "solve"):
+        X, _ = _features(a.n, 2024)
+        K0 = torch.empty((a.n, a.n), dtype=torch.float64, device=dev).T
+        core.kernel_matrix("gaussian", X, X, a.sigma, symmetric=True, emulated=True, out=K0)
+        K = torch.empty_like(K0)
+        y = torch.rand(a.n, dtype=torch.float64, device=dev, generator=g)
+        if a.kernel == "factor":
+            run = lambda: core.cholesky(K, a.lam, "mixed")  # noqa: E731
+        else:
+            run = lambda: core.solve(K, y, a.lam, "mixed")  # noqa: E731
+        total = 0.0
+        for i in range(a.reps + 1):
+            K.copy_(K0)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            run()
+            e1.record()
+            torch.cuda.synchronize()
+            if i > 0:
+                total += e0.elapsed_time(e1)
+        print(json.dumps({"kernel": a.kernel, "n": a.n, "ms_per_call": total / max(a.reps, 1)}))
+        return
     else:
         _, (z, r, o) = _features(a.n, 3)
         run = lambda: core.coulomb_matrix_batch(z, r, o, 23)  # noqa: E731

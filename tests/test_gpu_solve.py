@@ -124,6 +124,24 @@ def test_mixed_solve_deterministic(cuda, oracle, krr_system):
     assert np.array_equal(runs[0], runs[1])
 
 
+@pytest.mark.parametrize("n", [129, 1000])
+def test_mixed_solve_stepped_triangular_solves(cuda, oracle, krr_system, n):
+    # with cooperative launches off (batched and graph-recorded solves), the
+    # triangular solves run one launch per block; the refined answer is the same
+    X, y = krr_system
+    K = np.ascontiguousarray(oracle.gaussian_kernel(X[:n], X[:n], 1000.0))
+    xr = oracle.refined_solve(K, y[:n], 1e-8)
+    lib = core.lib()
+    lib.qmlg_set_thread_cooperative(0)
+    try:
+        x, rep = core.solve(torch.from_numpy(K).to(cuda), torch.from_numpy(y[:n]).to(cuda), 1e-8,
+                            precision="mixed")
+    finally:
+        lib.qmlg_set_thread_cooperative(1)
+    assert rep["status"] == 0 and rep["fell_back"] == 0, rep
+    assert rel(x.cpu().numpy(), xr) <= 1e-8, rep
+
+
 def test_residual_dd_exact(cuda):
     rng = np.random.default_rng(0)
     A = rng.integers(-1000, 1000, size=(130, 130)).astype(np.float64)
