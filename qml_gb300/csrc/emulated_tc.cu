@@ -7,16 +7,19 @@
 // scale per row.  Level l = s + t of the digit products is accumulated exactly in
 // FP32 in tensor memory:
 //   TMEM lane   = j (128 per tile; the contiguous index of C, so stores coalesce)
-//   TMEM column = l * 64 + (i - i0)   (64 per level, 8 levels = all 512 columns)
-// A tile runs kchunks 64-deep K chunks.  Per chunk the 8 digit planes of the 64 i-rows
-// are loaded once (double-buffered) and the 8 planes of the 128 j-rows stream
-// through a 3-slot ring; each j-plane s meets the i-planes t <= S-1-s.
+//   TMEM column = b * 8 TN + l * TN + (i - i0)   (TN per level, 8 levels)
+// The trailing update takes TN = 64 (8 levels fill the 512 columns, one accumulator
+// b = 0); the Gaussian epilogues take TN = 32 and two accumulators, so one tile's MMAs
+// run while the epilogue drains the previous tile.  A tile runs kchunks 64-deep K
+// chunks.  Per chunk the 8 digit planes of the TN i-rows are loaded once
+// (double-buffered) and the 8 planes of the 128 j-rows stream through a ring; each
+// j-plane s meets the i-planes t <= S-1-s in MMAs of N = TN cnt <= 256.
 // Exactness: a level sums at most 8 * (64*kchunks) * 4096 products, so kchunks <= 8
 // keeps every partial sum below 2^24.
 //
 // Warp roles (320 threads): warp 0 issues TMA loads, warp 1 owns TMEM and issues
 // the MMAs from one thread, warps 2-9 run the epilogue, two per TMEM lane quarter
-// (one per half of the 64 columns, so each scheduler interleaves two epilogue
+// (one per half of the TN columns, so each scheduler interleaves two epilogue
 // warps): the levels are merged in 64-bit integers, converted once to FP64, scaled
 // by 2^(e_i + e_j) and subtracted from C.  Waits are bounded; a timeout sets *err.
 #include <cuda.h>
@@ -36,20 +39,34 @@ namespace {
 using namespace qmlg::tc;
 
 constexpr int TM = 128;         // TMEM lanes per tile (j)
-constexpr int TN = 64;          // columns per level (i)
 constexpr int KC = 64;          // K chunk: one 128-byte swizzled row of bf16
 constexpr int S_MAX = 8;
 constexpr int THREADS = 320;    // 2 producer warps + 8 epilogue warps
 constexpr int EPI_THREADS = 256;
 constexpr int EG = 8;           // columns per epilogue step
-constexpr int A_STAGES = 5;
 constexpr int A_BYTES = TM * KC * 2;  // 16 KB
-constexpr int B_BYTES = TN * KC * 2;  // 8 KB
-constexpr int RED_BYTES = 4 * TN * 8;  // predict: per-warp column sums
-constexpr int SMEM_BYTES =
-    2 * S_MAX * B_BYTES + A_STAGES * A_BYTES + 1024 /*align*/ + 256 /*barriers*/ + RED_BYTES;
 
 enum Mode { kSyrk = 0, kKernelMatrix = 1, kPredict = 2 };
+
+// Tile shape per mode.  The trailing update (memory-heavy epilogue, operand reuse
+// matters) takes 64 i-columns per level: 8 levels fill TMEM's 512 columns, one
+// accumulator.  The Gaussian epilogues (FP64-bound) take 32 i-columns, so two
+// accumulators fit and one tile's MMAs run while the epilogue drains the other;
+// their B buffers are half as large, which leaves room for a deeper A ring.
+template <int MODE>
+struct Shape {
+    static constexpr int TN = MODE == kSyrk ? 64 : 32;  // i columns per level
+    static constexpr int NBUF = MODE == kSyrk ? 1 : 2;  // accumulators in TMEM
+    static constexpr int A_STAGES = MODE == kSyrk ? 5 : 9;
+    static constexpr int B_BYTES = TN * KC * 2;
+    static constexpr int TBUF = 8 * TN;                 // TMEM columns per accumulator
+};
+constexpr int RED_BYTES = 4 * 64 * 8;  // predict: per-warp column sums
+constexpr int SMEM_BYTES = 2 * S_MAX * Shape<kSyrk>::B_BYTES + Shape<kSyrk>::A_STAGES * A_BYTES +
+                           1024 /*align*/ + 256 /*barriers*/ + RED_BYTES;
+static_assert(2 * S_MAX * Shape<kKernelMatrix>::B_BYTES + Shape<kKernelMatrix>::A_STAGES * A_BYTES +
+                      1024 + 256 + RED_BYTES <= SMEM_BYTES,
+              "shared memory of the Gaussian tile shape");
 
 struct TileArgs {
     int ntiles;        // tiles in the (lower-triangular or full) tile list
@@ -75,16 +92,17 @@ struct TileArgs {
     double *partial;      // kPredict: [tiles along j][iend - ibase] partial sums
 };
 
-// Walks the tile list in increasing order.  With `lower`, row-block it (64 rows of
-// i) holds the j-blocks jt with jbase + 128 jt <= ibase + 64 it + 63 (the tiles that
-// reach the lower triangle); otherwise every jt.
+// Walks the tile list in increasing order.  With `lower`, row-block it (TN rows of
+// i) holds the j-blocks jt with jbase + 128 jt <= ibase + TN it + TN - 1 (the tiles
+// that reach the lower triangle); otherwise every jt.
+template <int TN>
 struct TileCursor {
     int it = 0, base = 0;
     __device__ __forceinline__ int count(const TileArgs &p, int r) const
     {
         if (!p.lower) return p.tj;
-        const int lim = p.ibase - p.jbase + 64 * r + 63;
-        return lim < 0 ? 0 : min(p.tj, lim / 128 + 1);
+        const int lim = p.ibase - p.jbase + TN * r + TN - 1;
+        return lim < 0 ? 0 : min(p.tj, lim / TM + 1);
     }
     __device__ __forceinline__ void locate(const TileArgs &p, int t, int &jt, int &itl)
     {
@@ -139,6 +157,8 @@ __global__ void __launch_bounds__(THREADS, 1)
 emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
               TileArgs p)
 {
+    using SH = Shape<MODE>;
+    constexpr int TN = SH::TN, A_STAGES = SH::A_STAGES, B_BYTES = SH::B_BYTES, TBUF = SH::TBUF;
     extern __shared__ unsigned char smem_raw[];
     unsigned char *base =
         (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -146,8 +166,8 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
     unsigned char *Aring = base + 2 * S_MAX * B_BYTES;        // [A_STAGES][A_BYTES]
     uint64_t *bars = (uint64_t *)(Aring + A_STAGES * A_BYTES);
     uint64_t *bFull = bars, *bEmpty = bars + 2, *aFull = bars + 4, *aEmpty = bars + 4 + A_STAGES,
-             *tFull = bars + 4 + 2 * A_STAGES, *tEmpty = tFull + 1;
-    uint32_t *tmem_holder = (uint32_t *)(tEmpty + 1);
+             *tFull = bars + 4 + 2 * A_STAGES, *tEmpty = tFull + 2;
+    uint32_t *tmem_holder = (uint32_t *)(tEmpty + 2);
     double(*red)[TN] = (double(*)[TN])(bars + 32);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -162,8 +182,10 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
             mbar_init(&aFull[k], 1);
             mbar_init(&aEmpty[k], 1);
         }
-        mbar_init(tFull, 1);
-        mbar_init(tEmpty, EPI_THREADS);
+        for (int k = 0; k < 2; ++k) {
+            mbar_init(&tFull[k], 1);
+            mbar_init(&tEmpty[k], EPI_THREADS);
+        }
         fence_barrier_init();
     }
     if (warp == 0 && lane == 0) {
@@ -181,7 +203,7 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
             // ---------------- TMA producer: runs ahead across tiles.  The i-planes of
             // chunk g+1 are requested halfway through the j-planes of chunk g, so they
             // are in flight while chunk g's MMAs run.
-            TileCursor cur, nxt;
+            TileCursor<TN> cur, nxt;
             int g = 0, it = 0;
             bool ok = true;
             int b_issued = -1;  // highest chunk index whose i-planes are requested
@@ -239,7 +261,10 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
             int g = 0, it = 0, u = 0;
             bool ok = true;
             for (int t = blockIdx.x; t < p.ntiles && ok; t += gridDim.x, ++u) {
-                if (u > 0 && !mbar_wait(tEmpty, (u - 1) & 1)) {
+                // accumulator tb, its use-th use: wait for the epilogue to have
+                // drained the previous one
+                const int tb = SH::NBUF == 2 ? (u & 1) : 0, use = SH::NBUF == 2 ? (u >> 1) : u;
+                if (use >= 1 && !mbar_wait(&tEmpty[tb], (use - 1) & 1)) {
                     ok = false;
                     break;
                 }
@@ -260,13 +285,13 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
                         fence_after_sync();
                         const uint64_t da = desc_sw128(Aring + st * A_BYTES);
                         // the i-planes v .. v+cnt-1 sit back to back in shared memory, so
-                        // one MMA with N = 64 cnt (<= 256) accumulates levels s+v ..
-                        // s+v+cnt-1, each into its own 64 TMEM columns
+                        // one MMA with N = TN cnt (<= 256) accumulates levels s+v ..
+                        // s+v+cnt-1, each into its own TN TMEM columns
                         for (int v = 0; v + s < S;) {
-                            const int cnt = min(4, S - s - v);
+                            const int cnt = min(256 / TN, S - s - v);
                             const uint32_t idn = idesc_bf16_f32(TM, TN * cnt);
                             const uint64_t db = desc_sw128(Bbuf + (bb * S_MAX + v) * B_BYTES);
-                            const uint32_t dst = tmem + (uint32_t)((s + v) * TN);
+                            const uint32_t dst = tmem + (uint32_t)(tb * TBUF + (s + v) * TN);
 #pragma unroll
                             for (int kk = 0; kk < KC / 16; ++kk) {
                                 const uint32_t acc = (c > 0 || s > 0 || kk > 0) ? 1u : 0u;
@@ -278,20 +303,21 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
                     }
                     mma_commit(&bEmpty[bb]);
                 }
-                mma_commit(tFull);
+                mma_commit(&tFull[tb]);
             }
             if (!ok) atomicOr(p.err, 2);
         }
     } else {
         // ---------------- epilogue: warps 2..9 -> TMEM lane quarter q = warp & 3,
-        // columns 32h .. 32h+31 of each level with h = (warp - 2) / 4
+        // columns HC h .. HC h + HC-1 of each level with h = (warp - 2) / 4
+        constexpr int HC = TN / 2;
         const int q = warp & 3, h = (warp - 2) >> 2;
         const int jl = q * 32 + lane;
         const int H = (S + 1) / 2;
         const int lo_levels = S - H;
         const int shift = lo_levels >= 2 ? 12 : 0;
         const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
-        TileCursor cur;
+        TileCursor<TN> cur;
         int u = 0;
         bool ok = true;
         for (int t = blockIdx.x; t < p.ntiles; t += gridDim.x, ++u) {
@@ -300,18 +326,20 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
             const int j0 = p.jbase + jt * TM, i0 = p.ibase + itl * TN;
             const int arow = p.a_row0 + jt * TM, brow = p.b_row0 + itl * TN;
             const int j = j0 + jl;
+            const int tb = SH::NBUF == 2 ? (u & 1) : 0, use = SH::NBUF == 2 ? (u >> 1) : u;
+            const uint32_t tbuf = lane_base + (uint32_t)(tb * TBUF);  // this tile's accumulator
             // every (j, i) of the tile is inside the updated range
             const bool interior = j0 + TM <= p.jend && i0 + TN <= p.iend &&
                                   (!p.lower || j0 + TM - 1 <= i0);
             if (MODE == kSyrk && j < p.jend) {
                 // while the MMAs run, pull this thread's part of C into L2 so the
                 // read-modify-write below does not wait on DRAM
-                const int ilo = i0 + h * 32, ilim = min(ilo + 32, p.iend);
+                const int ilo = i0 + h * HC, ilim = min(ilo + HC, p.iend);
                 for (int i = ilo; i < ilim; ++i)
                     if (interior || !p.lower || j <= i)
                         asm volatile("prefetch.global.L2 [%0];" ::"l"(p.C + (int64_t)i * p.ldc + j));
             }
-            if (ok && !mbar_wait(tFull, u & 1)) {
+            if (ok && !mbar_wait(&tFull[tb], use & 1)) {
                 ok = false;
                 if (lane == 0) atomicOr(p.err, 4);
             }
@@ -356,24 +384,24 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
                 }
             };
             if (MODE == kSyrk) {
-                // (1) merge all 32 of this warp's columns, then hand TMEM back, so the
-                // next tile's MMAs overlap (2), the read-modify-write of C
-                long long v64[32];
+                // (1) merge all HC of this warp's columns, then hand the accumulator
+                // back, then (2) the read-modify-write of C
+                long long v64[HC];
 #pragma unroll
-                for (int gq = 0; gq < 32 / EG; ++gq) {
+                for (int gq = 0; gq < HC / EG; ++gq) {
                     uint32_t v[S_MAX][EG];
 #pragma unroll
                     for (int l = 0; l < S_MAX; ++l)
-                        if (l < S) tmem_ld8(lane_base + (uint32_t)(l * TN + h * 32 + gq * EG), v[l]);
+                        if (l < S) tmem_ld8(tbuf + (uint32_t)(l * TN + h * HC + gq * EG), v[l]);
                     tmem_ld_wait();
                     merge8(v, v64 + gq * EG);
                 }
                 fence_before_sync();
-                mbar_arrive(tEmpty);
+                mbar_arrive(&tEmpty[tb]);
                 if (ok) {
 #pragma unroll
-                    for (int gq = 0; gq < 32 / EG; ++gq) {
-                        const int cb = h * 32 + gq * EG;
+                    for (int gq = 0; gq < HC / EG; ++gq) {
+                        const int cb = h * HC + gq * EG;
                         double cv[EG];
 #pragma unroll
                         for (int col = 0; col < EG; ++col) {
@@ -397,23 +425,23 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
                 // TMEM released once the last eight are in registers.  The per-column
                 // terms (scale |b|^2, b's exponent) are loaded once per tile by the lane
                 // of that column and broadcast; -2 scale 2^e is formed on the bits.
-                const int ibl = i0 + h * 32 + lane;
-                const bool ilv = ibl < p.iend;
-                const double sBl = ilv ? p.scale * p.normB[brow + h * 32 + lane] : 0.0;
-                const int eBl = ilv ? p.expB[brow + h * 32 + lane] : 0;
+                const int ibl = i0 + h * HC + lane;
+                const bool ilv = lane < HC && ibl < p.iend;
+                const double sBl = ilv ? p.scale * p.normB[brow + h * HC + lane] : 0.0;
+                const int eBl = ilv ? p.expB[brow + h * HC + lane] : 0;
                 const double m2s = -2.0 * p.scale;
                 const long long m2s_bits = __double_as_longlong(m2s);
                 const int m2s_exp = (int)((m2s_bits >> 52) & 0x7ff);
-                for (int gq = 0; gq < 32 / EG; ++gq) {
-                    const int cb = h * 32 + gq * EG;
+                for (int gq = 0; gq < HC / EG; ++gq) {
+                    const int cb = h * HC + gq * EG;
                     uint32_t v[S_MAX][EG];
 #pragma unroll
                     for (int l = 0; l < S_MAX; ++l)
-                        if (l < S) tmem_ld8(lane_base + (uint32_t)(l * TN + cb), v[l]);
+                        if (l < S) tmem_ld8(tbuf + (uint32_t)(l * TN + cb), v[l]);
                     tmem_ld_wait();
-                    if (gq == 32 / EG - 1) {
+                    if (gq == HC / EG - 1) {
                         fence_before_sync();
-                        mbar_arrive(tEmpty);
+                        mbar_arrive(&tEmpty[tb]);
                     }
                     if (!ok) continue;
                     long long v64[EG];
@@ -613,15 +641,15 @@ int tile_grid(int ntiles)
 }
 
 // Same tile list as TileCursor on the device.
-int count_tiles(int jbase, int jend, int ibase, int iend, int lower, int &tj)
+int count_tiles(int jbase, int jend, int ibase, int iend, int lower, int TN, int &tj)
 {
     tj = (int)qmlg::ceil_div(jend - jbase, TM);
     const int ti = (int)qmlg::ceil_div(iend - ibase, TN);
     if (!lower) return tj * ti;
     int total = 0;
     for (int r = 0; r < ti; ++r) {
-        const int lim = ibase - jbase + 64 * r + 63;
-        total += lim < 0 ? 0 : std::min(tj, lim / 128 + 1);
+        const int lim = ibase - jbase + TN * r + TN - 1;
+        total += lim < 0 ? 0 : std::min(tj, lim / TM + 1);
     }
     return total;
 }
@@ -706,11 +734,11 @@ int emu_tc_update(double *C, int64_t ldc, int jbase, int jend, int ibase, int ie
     if (slices < 1 || slices > S_MAX || kp % KC != 0 || kp / KC > 8) return QMLG_E_ARG;
     CUtensorMap mA, mB;
     int st = make_plane_map(&mA, digits, kp, rpad, slices, TM);
-    if (st == QMLG_OK) st = make_plane_map(&mB, digits, kp, rpad, slices, TN);
+    if (st == QMLG_OK) st = make_plane_map(&mB, digits, kp, rpad, slices, Shape<kSyrk>::TN);
     if (st != QMLG_OK) return st;
     set_smem_attrs();
     TileArgs a{};
-    a.ntiles = count_tiles(jbase, jend, ibase, iend, lower, a.tj);
+    a.ntiles = count_tiles(jbase, jend, ibase, iend, lower, Shape<kSyrk>::TN, a.tj);
     if (a.ntiles == 0) return QMLG_OK;
     a.C = C;
     a.ldc = ldc;
@@ -826,11 +854,11 @@ int launch_gauss(int mode, const GaussBufs &b, int na, int nb, int d, int S, dou
     const int kp = feature_pad(d), rpa = rows_pad(na), rpb = rows_pad(nb);
     CUtensorMap mA, mB;
     int st = make_plane_map(&mA, b.dA, kp, rpa, S, TM);
-    if (st == QMLG_OK) st = make_plane_map(&mB, b.dB, kp, rpb, S, TN);
+    if (st == QMLG_OK) st = make_plane_map(&mB, b.dB, kp, rpb, S, Shape<kKernelMatrix>::TN);
     if (st != QMLG_OK) return st;
     set_smem_attrs();
     TileArgs a{};
-    a.ntiles = count_tiles(0, na, 0, nb, sym ? 1 : 0, a.tj);
+    a.ntiles = count_tiles(0, na, 0, nb, sym ? 1 : 0, Shape<kKernelMatrix>::TN, a.tj);
     a.C = K;
     a.ldc = ldk;
     a.jbase = 0;
@@ -1041,11 +1069,11 @@ extern "C" int qmlg_predict_emulated_async(const double *Xtrain, int64_t ldtrain
     // launch without the trailing flag read (launch_gauss reads it synchronously)
     CUtensorMap mA, mB;
     st = make_plane_map(&mA, b.dA, kp, rpa, S_MAX, TM);
-    if (st == QMLG_OK) st = make_plane_map(&mB, b.dB, kp, rpb, S_MAX, TN);
+    if (st == QMLG_OK) st = make_plane_map(&mB, b.dB, kp, rpb, S_MAX, Shape<kKernelMatrix>::TN);
     if (st != QMLG_OK) return st;
     set_smem_attrs();
     TileArgs a{};
-    a.ntiles = count_tiles(0, ntrain, 0, ntest, 0, a.tj);
+    a.ntiles = count_tiles(0, ntrain, 0, ntest, 0, Shape<kPredict>::TN, a.tj);
     a.jend = ntrain;
     a.iend = ntest;
     a.kchunks = kp / KC;
@@ -1103,11 +1131,11 @@ extern "C" int qmlg_gaussian_kernel_emulated_async(const double *A, int64_t lda,
     if (st != QMLG_OK) return st;
     CUtensorMap mA, mB;
     st = make_plane_map(&mA, b.dA, kp, rpa, S_MAX, TM);
-    if (st == QMLG_OK) st = make_plane_map(&mB, b.dB, kp, rpb, S_MAX, TN);
+    if (st == QMLG_OK) st = make_plane_map(&mB, b.dB, kp, rpb, S_MAX, Shape<kKernelMatrix>::TN);
     if (st != QMLG_OK) return st;
     set_smem_attrs();
     TileArgs a{};
-    a.ntiles = count_tiles(0, na, 0, nb, sym ? 1 : 0, a.tj);
+    a.ntiles = count_tiles(0, na, 0, nb, sym ? 1 : 0, Shape<kKernelMatrix>::TN, a.tj);
     a.C = K;
     a.ldc = ldk;
     a.jend = na;
