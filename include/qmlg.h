@@ -455,6 +455,16 @@ int qmlg_residual_dd(const double *A, int n, int64_t lda, const double *diag, do
                      const double *x, const double *y, double *r, void *workspace,
                      size_t ws_bytes, void *stream);
 
+/*
+ * Self-test of the bounded device-side waits (no reference counterpart): one CTA
+ * polls entries of a triangular-solve output that nothing ever writes, with the
+ * same wait routine the cooperative solves use.  The wait gives up after its poll
+ * limit (about a second) and the call returns QMLG_E_TIMEOUT; the context stays
+ * usable.  ws: qmlg_selftest_wait_timeout_workspace_size().
+ */
+size_t qmlg_selftest_wait_timeout_workspace_size(void);
+int qmlg_selftest_wait_timeout(void *workspace, size_t ws_bytes, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -812,6 +812,17 @@ __device__ __forceinline__ void read_solved16(const double *v, int count, double
     }
 }
 
+// Self-test: polls solved entries that nothing writes, so every wait runs out.
+__global__ void wait_timeout_selftest_kernel(const double *v, int *err)
+{
+    __shared__ int abort_flag;
+    if (threadIdx.x == 0) abort_flag = 0;
+    __syncthreads();
+    double z[16];
+    const int q = threadIdx.x & 3;
+    read_solved16(v + q, NB - q, z, err, &abort_flag);
+}
+
 __global__ void fill_unsolved_kernel(double *__restrict__ v, int count)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1565,6 +1576,32 @@ extern "C" int qmlg_cholesky_mixed(double *A, int n, int64_t lda, double lambda,
     int info = 0;
     st = qmlg::read_back(&info, d_info, sizeof(int), s);
     return st != QMLG_OK ? st : info;
+}
+
+extern "C" size_t qmlg_selftest_wait_timeout_workspace_size(void)
+{
+    qmlg::WorkspacePlan p;
+    p.add<double>(NB);
+    p.add<int>(4);
+    return p.total();
+}
+
+extern "C" int qmlg_selftest_wait_timeout(void *workspace, size_t ws_bytes, void *stream)
+{
+    qmlg::Workspace ws(workspace, ws_bytes);
+    double *v = ws.take<double>(NB);
+    int *err = ws.take<int>(4);
+    if (v == nullptr || err == nullptr) return QMLG_E_WORKSPACE;
+    cudaStream_t s = qmlg::as_stream(stream);
+    cudaError_t e = cudaMemsetAsync(err, 0, sizeof(int), s);
+    if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+    { fill_unsolved_kernel<<<1, NB, 0, s>>>(v, NB); qmlg::count_launches(1); }
+    { wait_timeout_selftest_kernel<<<1, NB, 0, s>>>(v, err); qmlg::count_launches(1); }
+    int st = qmlg::check_launch();
+    if (st != QMLG_OK) return st;
+    int h = 0;
+    if ((st = qmlg::read_back(&h, err, sizeof(int), s)) != QMLG_OK) return st;
+    return (h & 2) ? QMLG_E_TIMEOUT : QMLG_OK;
 }
 
 extern "C" int qmlg_cholesky_solve_factored(const double *U, int n, int64_t lda, const double *y,

@@ -216,3 +216,20 @@ def test_syrk_emulated(cuda):
     scale = np.abs(P) @ np.abs(P).T + np.abs(C)
     assert np.max(np.abs(out[tri] - ref[tri]) / scale[tri]) < 1e-14
     assert np.array_equal(np.triu(out, 1), np.triu(C, 1))
+
+
+def test_bounded_wait_gives_up(cuda, oracle, krr_system):
+    # a wait on solved entries that nothing writes runs out after its poll limit and
+    # the call reports QMLG_E_TIMEOUT; the context stays usable afterwards
+    lib = core.lib()
+    ws = torch.empty(lib.qmlg_selftest_wait_timeout_workspace_size(), dtype=torch.uint8,
+                     device=cuda)
+    st = lib.qmlg_selftest_wait_timeout(ws.data_ptr(), ws.numel(),
+                                        torch.cuda.current_stream(cuda).cuda_stream)
+    assert st == -6
+    X, y = krr_system
+    K = np.ascontiguousarray(oracle.gaussian_kernel(X[:300], X[:300], 1000.0))
+    x, rep = core.solve(torch.from_numpy(K).to(cuda), torch.from_numpy(y[:300]).to(cuda), 1e-6,
+                        precision="mixed")
+    assert rep["status"] == 0, rep
+    assert rel(x.cpu().numpy(), oracle.refined_solve(K, y[:300], 1e-6)) <= 1e-8
