@@ -493,7 +493,8 @@ def cholesky_solve_factored(U: torch.Tensor, y: torch.Tensor) -> torch.Tensor:
 
 def residual_dd(A: torch.Tensor, diag: torch.Tensor, lam: float, x: torch.Tensor,
                 y: torch.Tensor) -> torch.Tensor:
-    """y - (A + lam I) x in double-double, using A's untouched triangle and diag."""
+    """y - (A + lam I) x summed exactly and rounded once, using A's untouched
+    triangle and diag."""
     _require_cuda(A, diag, x, y)
     Acm, lda = _colmajor(A)
     n = Acm.shape[0]
