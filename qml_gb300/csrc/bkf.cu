@@ -16,7 +16,9 @@
 // One cooperative kernel runs the whole factorisation, four grid barriers per
 // pivot step: CTA 0 decides the pivot (block reductions), the grid swaps, copies
 // the pivot columns and multipliers, then updates the trailing triangle one row per
-// warp while writing the L columns.  The inverse is the Schur complement left by
+// warp (four independent elements per lane in flight) while writing the L columns.
+// Everything another CTA wrote since the last barrier is read through L2
+// (ld.global.cg), never through a possibly stale L1 line.  The inverse is the Schur complement left by
 // the first n steps on [[A, I], [I, 0]] with the pivot search confined to A's rows
 // (a symmetric permutation inside A's block leaves that complement -A^-1).
 #include <algorithm>
@@ -31,7 +33,7 @@ namespace cg = cooperative_groups;
 
 namespace {
 
-constexpr int BK_THREADS = 256;
+constexpr int BK_THREADS = 1024;
 
 struct BkArgs {
     double *W;
@@ -99,14 +101,14 @@ __global__ void __launch_bounds__(BK_THREADS) bk_factor_kernel(BkArgs a)
             double cm = 0.0;
             int imax = k;
             for (int i = k + 1 + tid; i < ns; i += BK_THREADS) {
-                const double v = fabs(W[(int64_t)i * ld + k]);
+                const double v = fabs(__ldcg(W + (int64_t)i * ld + k));
                 if (v > cm) {
                     cm = v;
                     imax = i;
                 }
             }
             block_argmax(cm, imax, sv, si);
-            const double absakk = fabs(W[(int64_t)k * ld + k]);
+            const double absakk = fabs(__ldcg(W + (int64_t)k * ld + k));
             int kp = k, kstep = 1, zero = 0;
             if (fmax(absakk, cm) == 0.0) {
                 zero = 1;
@@ -115,13 +117,13 @@ __global__ void __launch_bounds__(BK_THREADS) bk_factor_kernel(BkArgs a)
                 double rm = 0.0;
                 int jdummy = 0;
                 for (int j = k + tid; j < imax; j += BK_THREADS)
-                    rm = fmax(rm, fabs(W[(int64_t)imax * ld + j]));
+                    rm = fmax(rm, fabs(__ldcg(W + (int64_t)imax * ld + j)));
                 for (int i = imax + 1 + tid; i < ns; i += BK_THREADS)
-                    rm = fmax(rm, fabs(W[(int64_t)i * ld + imax]));
+                    rm = fmax(rm, fabs(__ldcg(W + (int64_t)i * ld + imax)));
                 block_argmax(rm, jdummy, sv, si);
                 if (absakk >= alpha * cm * (cm / rm)) {
                     kp = k;
-                } else if (fabs(W[(int64_t)imax * ld + imax]) >= alpha * rm) {
+                } else if (fabs(__ldcg(W + (int64_t)imax * ld + imax)) >= alpha * rm) {
                     kp = imax;
                 } else {
                     kp = imax;
@@ -136,7 +138,7 @@ __global__ void __launch_bounds__(BK_THREADS) bk_factor_kernel(BkArgs a)
             }
         }
         bk_sync(g);
-        const int kp = a.dec[0], kstep = a.dec[1], zero = a.dec[2];
+        const int kp = __ldcg(a.dec), kstep = __ldcg(a.dec + 1), zero = __ldcg(a.dec + 2);
         const int kk = k + kstep - 1;
         // ---- symmetric interchange of kk and kp in the trailing block
         if (!zero && kp != kk) {
@@ -162,8 +164,8 @@ __global__ void __launch_bounds__(BK_THREADS) bk_factor_kernel(BkArgs a)
                     p = W + (int64_t)i * ld + kk;
                     q = W + (int64_t)i * ld + kp;
                 }
-                const double tmp = *p;
-                *p = *q;
+                const double tmp = __ldcg(p);
+                *p = __ldcg(q);
                 *q = tmp;
             }
         }
@@ -171,15 +173,15 @@ __global__ void __launch_bounds__(BK_THREADS) bk_factor_kernel(BkArgs a)
         // ---- pivot columns (copies) and 2x2 multipliers
         if (!zero) {
             if (kstep == 1) {
-                for (int64_t i = k + 1 + gt; i < N; i += gsz) a.x0[i] = W[i * ld + k];
+                for (int64_t i = k + 1 + gt; i < N; i += gsz) a.x0[i] = __ldcg(W + i * ld + k);
             } else {
-                const double d21 = W[(int64_t)(k + 1) * ld + k];
-                const double d11 = W[(int64_t)(k + 1) * ld + k + 1] / d21;
-                const double d22 = W[(int64_t)k * ld + k] / d21;
+                const double d21 = __ldcg(W + (int64_t)(k + 1) * ld + k);
+                const double d11 = __ldcg(W + (int64_t)(k + 1) * ld + k + 1) / d21;
+                const double d22 = __ldcg(W + (int64_t)k * ld + k) / d21;
                 const double t = 1.0 / (d11 * d22 - 1.0);
                 const double e21 = t / d21;
                 for (int64_t j = k + 2 + gt; j < N; j += gsz) {
-                    const double ajk = W[j * ld + k], ajk1 = W[j * ld + k + 1];
+                    const double ajk = __ldcg(W + j * ld + k), ajk1 = __ldcg(W + j * ld + k + 1);
                     a.x0[j] = e21 * (d11 * ajk - ajk1);   // wk
                     a.x1[j] = e21 * (d22 * ajk1 - ajk);   // wkp1
                 }
@@ -188,21 +190,45 @@ __global__ void __launch_bounds__(BK_THREADS) bk_factor_kernel(BkArgs a)
         bk_sync(g);
         // ---- trailing update (one row per warp) and the L columns
         if (!zero) {
+            const double *x0 = a.x0, *x1 = a.x1;
             if (kstep == 1) {
-                const double r = 1.0 / W[(int64_t)k * ld + k];
+                const double r = 1.0 / __ldcg(W + (int64_t)k * ld + k);
                 for (int i = k + 1 + warp_g; i < N; i += nwarps) {
-                    const double xi = a.x0[i];
+                    const double xi = __ldcg(x0 + i);
                     const double f = -xi * r;
                     double *row = W + (int64_t)i * ld;
-                    for (int j = k + 1 + lane; j <= i; j += 32) row[j] = fma(f, a.x0[j], row[j]);
+                    int j = k + 1 + lane;
+                    for (; j + 96 <= i; j += 128) {  // loads of four elements, then their FMAs
+                        const double r0 = __ldcg(row + j), r1 = __ldcg(row + j + 32);
+                        const double r2 = __ldcg(row + j + 64), r3 = __ldcg(row + j + 96);
+                        const double y0 = __ldcg(x0 + j), y1 = __ldcg(x0 + j + 32);
+                        const double y2 = __ldcg(x0 + j + 64), y3 = __ldcg(x0 + j + 96);
+                        row[j] = fma(f, y0, r0);
+                        row[j + 32] = fma(f, y1, r1);
+                        row[j + 64] = fma(f, y2, r2);
+                        row[j + 96] = fma(f, y3, r3);
+                    }
+                    for (; j <= i; j += 32) row[j] = fma(f, __ldcg(x0 + j), __ldcg(row + j));
                     if (lane == 0) row[k] = xi * r;
                 }
             } else {
                 for (int i = k + 2 + warp_g; i < N; i += nwarps) {
                     double *row = W + (int64_t)i * ld;
-                    const double aik = row[k], aik1 = row[k + 1];
-                    for (int j = k + 2 + lane; j <= i; j += 32)
-                        row[j] = row[j] - (aik * a.x0[j] + aik1 * a.x1[j]);
+                    const double aik = __ldcg(row + k), aik1 = __ldcg(row + k + 1);
+                    int j = k + 2 + lane;
+                    for (; j + 96 <= i; j += 128) {
+                        double rv[4], u[4], v[4];
+#pragma unroll
+                        for (int t = 0; t < 4; ++t) {
+                            rv[t] = __ldcg(row + j + 32 * t);
+                            u[t] = __ldcg(x0 + j + 32 * t);
+                            v[t] = __ldcg(x1 + j + 32 * t);
+                        }
+#pragma unroll
+                        for (int t = 0; t < 4; ++t) row[j + 32 * t] = rv[t] - (aik * u[t] + aik1 * v[t]);
+                    }
+                    for (; j <= i; j += 32)
+                        row[j] = __ldcg(row + j) - (aik * __ldcg(x0 + j) + aik1 * __ldcg(x1 + j));
                 }
             }
         }
