@@ -263,6 +263,21 @@ int qmlg_predict_fused(int kind, const double *Xtrain, int64_t ldtrain, int ntra
                        void *stream);
 
 /*
+ * Laplacian prediction yhat = K(Xtest, Xtrain) alpha with the L1 sums in 64-bit
+ * fixed point, as qmlg_laplacian_kernel_fixed (same grid, same bound: every kernel
+ * entry within 1e-12 of FP64), fused like qmlg_predict_fused: no kernel matrix is
+ * written and the partial sums are reduced in a fixed order.  When the data do not
+ * fit the fixed-point grid it runs qmlg_predict_fused's FP64 kernel.  The call
+ * reads two maxima back to the host (it synchronises the stream once).
+ * ws: qmlg_predict_laplacian_fixed_workspace_size(ntrain, ntest, d).
+ */
+size_t qmlg_predict_laplacian_fixed_workspace_size(int ntrain, int ntest, int d);
+int qmlg_predict_laplacian_fixed(const double *Xtrain, int64_t ldtrain, int ntrain,
+                                 const double *Xtest, int64_t ldtest, int ntest, int d,
+                                 double sigma, const double *alpha, double *yhat,
+                                 void *workspace, size_t ws_bytes, void *stream);
+
+/*
  * qmlg_predict_fused without a workspace, for callers that cannot allocate device
  * memory (for example a serving process whose memory manager reserves all of its
  * HBM at start-up and forbids later cudaMalloc calls, which synchronise the device

@@ -123,6 +123,8 @@ SIGNATURES = {
     "qmlg_solve_async": (_I, [_P, _I, _I64, _P, _P, _D, _I, _P, _P, _P, _SZ, _P]),
     "qmlg_residual_workspace_size": (_SZ, [_I]),
     "qmlg_residual_dd": (_I, [_P, _I, _I64, _P, _D, _P, _P, _P, _P, _SZ, _P]),
+    "qmlg_predict_laplacian_fixed_workspace_size": (_SZ, [_I, _I, _I]),
+    "qmlg_predict_laplacian_fixed": (_I, [_P, _I64, _I, _P, _I64, _I, _I, _D, _P, _P, _P, _SZ, _P]),
     "qmlg_selftest_wait_timeout_workspace_size": (_SZ, []),
     "qmlg_selftest_wait_timeout": (_I, [_P, _SZ, _P]),
 }

@@ -279,7 +279,8 @@ def predict(kind: str, Xtrain: torch.Tensor, Xtest: torch.Tensor, sigma: float,
             alpha: torch.Tensor, out: Optional[torch.Tensor] = None,
             emulated: bool = False) -> torch.Tensor:
     """yhat = K(Xtest, Xtrain) alpha without materialising the kernel matrix.
-    emulated=True (Gaussian only) uses the tensor-core contraction."""
+    emulated=True uses the fast exact paths: the tensor-core contraction for the
+    Gaussian, 64-bit fixed-point L1 sums for the Laplacian."""
     _require_cuda(Xtrain, Xtest, alpha)
     Xtrain, ldtr = _rows(Xtrain)
     Xtest, ldte = _rows(Xtest)
@@ -294,6 +295,15 @@ def predict(kind: str, Xtrain: torch.Tensor, Xtest: torch.Tensor, sigma: float,
                                           d, float(sigma), alpha.data_ptr(), out.data_ptr(),
                                           ws.data_ptr(), ws.numel(), _stream(Xtrain.device)),
               "qmlg_predict_emulated")
+        return out
+    if emulated and kind == "laplacian":
+        ws_bytes = lib().qmlg_predict_laplacian_fixed_workspace_size(ntr, nte, d)
+        ws = workspaces.get(ws_bytes, Xtrain.device)
+        check(lib().qmlg_predict_laplacian_fixed(Xtrain.data_ptr(), ldtr, ntr, Xtest.data_ptr(), ldte,
+                                                 nte, d, float(sigma), alpha.data_ptr(),
+                                                 out.data_ptr(), ws.data_ptr(), ws.numel(),
+                                                 _stream(Xtrain.device)),
+              "qmlg_predict_laplacian_fixed")
         return out
     ws_bytes = lib().qmlg_predict_workspace_size(ntr, nte)
     ws = workspaces.get(ws_bytes, Xtrain.device)

@@ -615,6 +615,71 @@ laplace_fixed_kernel(const long long *__restrict__ A, int na, const long long *_
     }
 }
 
+// Fused Laplacian prediction in fixed point: the L1 sums of laplace_fixed_kernel for
+// a (training tile, test tile), then the per-test-column partial sums of k * alpha
+// over the tile's training rows (in the same fixed order as predict_partial_kernel).
+__global__ void __launch_bounds__(NT)
+laplace_fixed_predict_kernel(const long long *__restrict__ A, int na, const long long *__restrict__ B,
+                             int nb, int d, double inv_scale, double neg_inv_sigma,
+                             const double *__restrict__ alpha, double *__restrict__ partial)
+{
+    __shared__ double smem[TI * (TJ + 1)];
+    long long(*As)[TJ + 1] = reinterpret_cast<long long(*)[TJ + 1]>(smem);
+    long long(*Bs)[TI + 1] = reinterpret_cast<long long(*)[TI + 1]>(smem + TK * (TJ + 1));
+    double(*red)[TI + 1] = reinterpret_cast<double(*)[TI + 1]>(smem);
+    const int bj = blockIdx.x, bi = blockIdx.y;
+    const int j0 = bj * TJ, i0 = bi * TI;
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    long long acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = 0;
+    for (int t0 = 0; t0 < d; t0 += TK) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int e = tid + q * NT;
+            const int r = e >> 4, c = e & 15;
+            const int t = t0 + c;
+            As[c][r] = (j0 + r < na && t < d) ? A[(int64_t)(j0 + r) * d + t] : 0;
+            Bs[c][r] = (i0 + r < nb && t < d) ? B[(int64_t)(i0 + r) * d + t] : 0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int c = 0; c < TK; ++c) {
+            long long av[4], bv[4];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) av[a] = As[c][tx + 16 * a];
+#pragma unroll
+            for (int b = 0; b < 4; ++b) bv[b] = Bs[c][ty + 16 * b];
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int b = 0; b < 4; ++b) acc[a][b] += iabs64(av[a] - bv[b]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+        const int i = i0 + ty + 16 * b;
+        double sum = 0.0;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const int j = j0 + tx + 16 * a;
+            if (j < na && i < nb)
+                sum = fma(exp(neg_inv_sigma * ((double)acc[a][b] * inv_scale)), alpha[j], sum);
+        }
+        red[tx][ty + 16 * b] = sum;
+    }
+    __syncthreads();
+    if (tid < TI) {
+        double sum = 0.0;
+        for (int q = 0; q < 16; ++q) sum += red[q][tid];
+        const int i = i0 + tid;
+        if (i < nb) partial[(int64_t)bj * nb + i] = sum;
+    }
+}
+
 }  // namespace
 
 extern "C" size_t qmlg_laplacian_kernel_fixed_workspace_size(int na, int nb, int d, int flags)
@@ -679,5 +744,78 @@ extern "C" int qmlg_laplacian_kernel_fixed(const double *A, int64_t lda, int na,
     laplace_fixed_kernel<<<grid, NT, 0, s>>>(qa, na, qb, nb, d, inv_scale, -1.0 / sigma, K, ldk,
                                              symmetric ? 1 : 0, diag_shift);
     qmlg::count_launches(1);
+    return qmlg::check_launch();
+}
+
+extern "C" size_t qmlg_predict_laplacian_fixed_workspace_size(int ntrain, int ntest, int d)
+{
+    qmlg::WorkspacePlan p;
+    p.add<double>((size_t)qmlg::ceil_div(ntrain < 1 ? 1 : ntrain, TJ) * (size_t)ntest);  // partials
+    p.add<long long>((size_t)ntrain * d);
+    p.add<long long>((size_t)ntest * d);
+    p.add<unsigned long long>(2);
+    return p.total();
+}
+
+extern "C" int qmlg_predict_laplacian_fixed(const double *Xtrain, int64_t ldtrain, int ntrain,
+                                            const double *Xtest, int64_t ldtest, int ntest, int d,
+                                            double sigma, const double *alpha, double *yhat,
+                                            void *workspace, size_t ws_bytes, void *stream)
+{
+    int st = check_common(Xtrain, ldtrain, ntrain, Xtest, ldtest, ntest, d, sigma);
+    if (st != QMLG_OK) return st;
+    if (ntest == 0) return QMLG_OK;
+    if (yhat == nullptr || (ntrain > 0 && alpha == nullptr)) return QMLG_E_ARG;
+    cudaStream_t s = qmlg::as_stream(stream);
+    if (ntrain == 0) {
+        cudaError_t e = cudaMemsetAsync(yhat, 0, sizeof(double) * (size_t)ntest, s);
+        return e == cudaSuccess ? QMLG_OK : qmlg::set_cuda_error(e);
+    }
+    if (ws_bytes < qmlg_predict_laplacian_fixed_workspace_size(ntrain, ntest, d))
+        return QMLG_E_WORKSPACE;
+    qmlg::Workspace ws(workspace, ws_bytes);
+    const int tj = (int)qmlg::ceil_div(ntrain, TJ), ti = (int)qmlg::ceil_div(ntest, TI);
+    double *partial = ws.take<double>((size_t)tj * ntest);
+    long long *qa = ws.take<long long>((size_t)ntrain * d);
+    long long *qb = ws.take<long long>((size_t)ntest * d);
+    unsigned long long *mx = ws.take<unsigned long long>(2);
+    if (partial == nullptr || qa == nullptr || qb == nullptr || mx == nullptr)
+        return QMLG_E_WORKSPACE;
+    cudaError_t e = cudaMemsetAsync(mx, 0, 2 * sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+    auto blocks = [](int64_t total) { return (int)std::min<int64_t>(qmlg::ceil_div(total, 256), 2432); };
+    max_abs_rows_kernel<<<blocks((int64_t)ntrain * d), 256, 0, s>>>(Xtrain, ldtrain, ntrain, d, mx);
+    max_abs_rows_kernel<<<blocks((int64_t)ntest * d), 256, 0, s>>>(Xtest, ldtest, ntest, d, mx + 1);
+    qmlg::count_launches(2);
+    unsigned long long h[2] = {0, 0};
+    if ((st = qmlg::read_back(h, mx, sizeof(h), s)) != QMLG_OK) return st;
+    double ma, mb;
+    std::memcpy(&ma, &h[0], sizeof(double));
+    std::memcpy(&mb, &h[1], sizeof(double));
+    const double m = std::fmax(ma, mb);
+    // the same fixed-point grid and 1e-12 bound as qmlg_laplacian_kernel_fixed
+    int F = 0;
+    bool fixed = std::isfinite(m);
+    if (fixed) {
+        int em = 0;
+        if (m > 0.0) std::frexp(m, &em);
+        int ed = 0;
+        std::frexp((double)(2 * (int64_t)(d < 1 ? 1 : d)), &ed);
+        F = std::min(62 - ed - em, 1000);
+        fixed = std::ldexp((double)d, -F) / sigma <= 0.5e-12;
+    }
+    if (fixed) {
+        const double scale = std::ldexp(1.0, F), inv_scale = std::ldexp(1.0, -F);
+        to_fixed_kernel<<<blocks((int64_t)ntrain * d), 256, 0, s>>>(Xtrain, ldtrain, ntrain, d, scale, qa);
+        to_fixed_kernel<<<blocks((int64_t)ntest * d), 256, 0, s>>>(Xtest, ldtest, ntest, d, scale, qb);
+        laplace_fixed_predict_kernel<<<dim3(tj, ti), NT, 0, s>>>(qa, ntrain, qb, ntest, d, inv_scale,
+                                                                 -1.0 / sigma, alpha, partial);
+        qmlg::count_launches(3);
+    } else {
+        predict_partial_kernel<kLaplace><<<dim3(tj, ti), NT, 0, s>>>(
+            Xtrain, ldtrain, ntrain, Xtest, ldtest, ntest, d, -1.0 / sigma, alpha, partial);
+        qmlg::count_launches(1);
+    }
+    { reduce_partial_kernel<<<(int)qmlg::ceil_div(ntest, 256), 256, 0, s>>>(partial, tj, ntest, yhat); qmlg::count_launches(1); }
     return qmlg::check_launch();
 }

@@ -93,6 +93,24 @@ def test_predict_fused_and_gemv(cuda, oracle, cm_features, kind):
     assert np.array_equal(y, y3)
 
 
+@pytest.mark.parametrize("sigma", [1000.0, 1e5])
+def test_predict_laplacian_fixed(cuda, oracle, cm_features, sigma):
+    # fused Laplacian prediction with fixed-point L1 sums (and the FP64 kernel when the
+    # grid cannot meet the bound, sigma = 1e5 still fits): within 1e-12 of the oracle
+    # relative to sum |k alpha|, deterministic
+    rng = np.random.default_rng(5)
+    Xtr, Xte = cm_features[:900], cm_features[900:]
+    alpha = rng.normal(size=900)
+    Ks = oracle.laplacian_kernel(Xtr, Xte, sigma)
+    expect = Ks.T @ alpha
+    scale = np.abs(Ks.T) @ np.abs(alpha)
+    args = (torch.from_numpy(Xtr).to(cuda), torch.from_numpy(Xte).to(cuda), sigma,
+            torch.from_numpy(alpha).to(cuda))
+    y = core.predict("laplacian", *args, emulated=True).cpu().numpy()
+    assert np.max(np.abs(y - expect) / scale) <= 1e-12
+    assert np.array_equal(y, core.predict("laplacian", *args, emulated=True).cpu().numpy())
+
+
 @pytest.mark.parametrize("sigma", [250.0, 1000.0, 2000.0])
 def test_emulated_gaussian_kernel(cuda, oracle, cm_features, sigma):
     # tensor-core (digit-plane) contraction: every entry within 1e-12 of the oracle
