@@ -233,3 +233,16 @@ def test_bounded_wait_gives_up(cuda, oracle, krr_system):
                         precision="mixed")
     assert rep["status"] == 0, rep
     assert rel(x.cpu().numpy(), oracle.refined_solve(K, y[:300], 1e-6)) <= 1e-8
+
+
+def test_mixed_solve_many_panels(cuda, oracle):
+    # eight 512-column panels with the look-ahead between them, on an ill-conditioned
+    # Gaussian K (lambda = 1e-8): alpha within 1e-8 of the refined oracle solve
+    b = generate_molecules(4096, seed=77)
+    X = oracle.cm_sorted_batch(b.charges, b.coordinates, b.offsets, 23)
+    K = np.ascontiguousarray(oracle.gaussian_kernel(X, X, 1000.0))
+    xr = oracle.refined_solve(K, b.labels, 1e-8)
+    x, rep = core.solve(torch.from_numpy(K).to(cuda), torch.from_numpy(b.labels).to(cuda), 1e-8,
+                        precision="mixed")
+    assert rep["status"] == 0 and rep["fell_back"] == 0, rep
+    assert rel(x.cpu().numpy(), xr) <= 1e-8, rep
