@@ -17,11 +17,12 @@
 // Exactness: a level sums at most 8 * (64*kchunks) * 4096 products, so kchunks <= 8
 // keeps every partial sum below 2^24.
 //
-// Warp roles (320 threads): warp 0 issues TMA loads, warp 1 owns TMEM and issues
-// the MMAs from one thread, warps 2-9 run the epilogue, two per TMEM lane quarter
-// (one per half of the TN columns, so each scheduler interleaves two epilogue
-// warps): the levels are merged in 64-bit integers, converted once to FP64, scaled
-// by 2^(e_i + e_j) and subtracted from C.  Waits are bounded; a timeout sets *err.
+// Warp roles (576 threads): warp 0 issues TMA loads, warp 1 owns TMEM and issues
+// the MMAs from one thread, warps 2-17 run the epilogue, four per TMEM lane quarter
+// (one per quarter of the TN columns, four columns per step, so each scheduler
+// interleaves four epilogue warps): the levels are merged in 64-bit integers,
+// converted once to FP64, scaled by 2^(e_i + e_j) and subtracted from C.  Waits are
+// bounded; a timeout sets *err.
 #include <cuda.h>
 
 #include <algorithm>
@@ -41,9 +42,10 @@ using namespace qmlg::tc;
 constexpr int TM = 128;         // TMEM lanes per tile (j)
 constexpr int KC = 64;          // K chunk: one 128-byte swizzled row of bf16
 constexpr int S_MAX = 8;
-constexpr int THREADS = 320;    // 2 producer warps + 8 epilogue warps
-constexpr int EPI_THREADS = 256;
-constexpr int EG = 8;           // columns per epilogue step
+constexpr int EPI_WARPS = 16;   // four per TMEM lane quarter
+constexpr int THREADS = 64 + 32 * EPI_WARPS;  // producer + MMA warps, then the epilogue
+constexpr int EPI_THREADS = 32 * EPI_WARPS;
+constexpr int EG = 4;           // columns per epilogue step
 constexpr int A_BYTES = TM * KC * 2;  // 16 KB
 
 enum Mode { kSyrk = 0, kKernelMatrix = 1, kPredict = 2 };
@@ -324,7 +326,7 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
     } else {
         // ---------------- epilogue: warps 2..9 -> TMEM lane quarter q = warp & 3,
         // columns HC h .. HC h + HC-1 of each level with h = (warp - 2) / 4
-        constexpr int HC = TN / 2;
+        constexpr int HC = TN / (EPI_WARPS / 4);
         const int q = warp & 3, h = (warp - 2) >> 2;
         const int jl = q * 32 + lane;
         const int H = (S + 1) / 2;
@@ -406,7 +408,7 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
                     uint32_t v[S_MAX][EG];
 #pragma unroll
                     for (int l = 0; l < S_MAX; ++l)
-                        if (l < S) tmem_ld8(tbuf + (uint32_t)(l * TN + h * HC + gq * EG), v[l]);
+                        if (l < S) tmem_ld4(tbuf + (uint32_t)(l * TN + h * HC + gq * EG), v[l]);
                     tmem_ld_wait();
                     merge8(v, v64 + gq * EG);
                 }
@@ -451,7 +453,7 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
                     uint32_t v[S_MAX][EG];
 #pragma unroll
                     for (int l = 0; l < S_MAX; ++l)
-                        if (l < S) tmem_ld8(tbuf + (uint32_t)(l * TN + cb), v[l]);
+                        if (l < S) tmem_ld4(tbuf + (uint32_t)(l * TN + cb), v[l]);
                     tmem_ld_wait();
                     if (gq == HC / EG - 1) {
                         fence_before_sync();
@@ -493,12 +495,12 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
             }
             if (MODE == kPredict) {
                 // the four quarters' column sums are added in a fixed order
-                asm volatile("bar.sync 1, 256;" ::: "memory");
+                asm volatile("bar.sync 1, %0;" ::"n"(EPI_THREADS) : "memory");
                 const int tt = threadIdx.x - 64;
                 if (ok && tt < TN && i0 + tt < p.iend)
                     p.partial[(int64_t)jt * (p.iend - p.ibase) + (i0 - p.ibase) + tt] =
                         ((red[0][tt] + red[1][tt]) + red[2][tt]) + red[3][tt];
-                asm volatile("bar.sync 1, 256;" ::: "memory");
+                asm volatile("bar.sync 1, %0;" ::"n"(EPI_THREADS) : "memory");
             }
         }
     }
