@@ -527,23 +527,34 @@ __global__ void slice_rows_kernel(const double *__restrict__ A, int64_t lda, int
     if (warp >= rpad) return;
     const bool live = warp < nrows;
     const double *row = A + (int64_t)(r0 + warp) * lda + c0;
-    double m = 0.0, sq = 0.0;
+    // max |x| on the bits (the integer order of non-negative doubles is their order;
+    // an infinity or NaN comes out non-finite), and the sum of squares only if asked
+    unsigned long long mb = 0ull;
+    double sq = 0.0;
     if (live)
         for (int k = lane; k < kw; k += 32) {
-            m = fmax(m, fabs(row[k]));
-            sq = fma(row[k], row[k], sq);
+            const double v = row[k];
+            const unsigned long long bv =
+                (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+            mb = bv > mb ? bv : mb;
+            if (norms != nullptr) sq = fma(v, v, sq);
         }
     for (int off = 16; off > 0; off >>= 1) {
-        m = fmax(m, __shfl_xor_sync(0xffffffffu, m, off));
-        sq += __shfl_xor_sync(0xffffffffu, sq, off);
+        const unsigned long long o = __shfl_xor_sync(0xffffffffu, mb, off);
+        mb = o > mb ? o : mb;
+        if (norms != nullptr) sq += __shfl_xor_sync(0xffffffffu, sq, off);
     }
     if (norms != nullptr && lane == 0) norms[warp] = sq;
+    const double m = __longlong_as_double((long long)mb);
     int e = 0;
     if (m > 0.0 && isfinite(m)) {
         frexp(m, &e);
         e += 1;  // |x| * 2^-e < 1/2
     }
-    const double scale = pow2i(7 * slices - e);
+    // x * 2^ks on the exponent bits (exact; |x * 2^ks| < 2^(7S-1)); a result below
+    // 2^-1022 rounds to 0, and a subnormal x takes the FP64 multiply
+    const int ks = 7 * slices - e;
+    const double scale = pow2i(ks);
     const int64_t plane = (int64_t)rpad * kp;
     __nv_bfloat16 *dst = digits + (int64_t)warp * kp;
     for (int k0 = lane * 8; k0 < kp; k0 += 256) {
@@ -551,7 +562,19 @@ __global__ void slice_rows_kernel(const double *__restrict__ A, int64_t lda, int
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
             const int k = k0 + u;
-            q[u] = (live && k < kw) ? __double2ll_rn(row[k] * scale) : 0;
+            long long qv = 0;
+            if (live && k < kw) {
+                const double v = row[k];
+                const unsigned long long bv = (unsigned long long)__double_as_longlong(v);
+                const int E = (int)((bv >> 52) & 0x7ff);
+                if (E == 0) {
+                    if ((bv & 0x000fffffffffffffull) != 0ull) qv = __double2ll_rn(v * scale);
+                } else if (E + ks > 0) {
+                    qv = __double2ll_rn(__longlong_as_double(
+                        (long long)(bv + ((unsigned long long)(long long)ks << 52))));
+                }
+            }
+            q[u] = qv;
         }
         for (int s = slices - 1; s >= 0; --s) {
             __align__(16) __nv_bfloat16 b[8];
