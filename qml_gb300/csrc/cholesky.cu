@@ -258,20 +258,39 @@ trsm_panel_kernel(double *__restrict__ A, int64_t lda, int n, int k0,
 #pragma unroll
         for (int j = 0; j < 16; ++j) row[s0 + 4 * j] = x[j];
     if (digits == nullptr) return;
-    double m = 0.0;
+    // max |x| on the bits and the power-of-two scaling on the exponent field, as in
+    // slice_rows (no FP64 instruction unless an entry is subnormal)
+    unsigned long long mb = 0ull;
 #pragma unroll
-    for (int j = 0; j < 16; ++j) m = fmax(m, fabs(x[j]));
-    m = fmax(m, __shfl_xor_sync(0xffffffffu, m, 1));
-    m = fmax(m, __shfl_xor_sync(0xffffffffu, m, 2));
+    for (int j = 0; j < 16; ++j) {
+        const unsigned long long bv = (unsigned long long)__double_as_longlong(x[j]) & 0x7fffffffffffffffull;
+        mb = bv > mb ? bv : mb;
+    }
+#pragma unroll
+    for (int off = 1; off <= 2; off <<= 1) {
+        const unsigned long long o = __shfl_xor_sync(0xffffffffu, mb, off);
+        mb = o > mb ? o : mb;
+    }
+    const double m = __longlong_as_double((long long)mb);
     int e = 0;
     if (m > 0.0 && isfinite(m)) {
         frexp(m, &e);
         e += 1;  // |x| * 2^-e < 1/2
     }
-    const double scale = scalbn(1.0, 7 * slices - e);
+    const int ks = 7 * slices - e;
     long long q[16];
 #pragma unroll
-    for (int j = 0; j < 16; ++j) q[j] = __double2ll_rn(x[j] * scale);
+    for (int j = 0; j < 16; ++j) {
+        const unsigned long long bv = (unsigned long long)__double_as_longlong(x[j]);
+        const int E = (int)((bv >> 52) & 0x7ff);
+        long long qv = 0;
+        if (E == 0) {
+            if ((bv & 0x000fffffffffffffull) != 0ull) qv = __double2ll_rn(x[j] * scalbn(1.0, ks));
+        } else if (E + ks > 0) {
+            qv = __double2ll_rn(__longlong_as_double((long long)(bv + ((unsigned long long)(long long)ks << 52))));
+        }
+        q[j] = qv;
+    }
     if (s0 == 0 && grow < drows) expo[grow] = e;
     const int64_t plane = (int64_t)rpad * NB;
     for (int sl = slices - 1; sl >= 0; --sl) {
