@@ -1373,6 +1373,16 @@ int factor_panel(double *A, int n, int64_t lda, double shift, int K0, int K1, in
     return check_launch();
 }
 
+// SMs kept free for the panel chain while the rest of the trailing matrix, of order
+// m, is updated beside it.  The update's work grows as m^2 and the chain's as m, so
+// the share grows as m falls: 16, 32 then 48 of 152 SMs.  The bands come from
+// per-step timings at N = 20000 and 40000 with fixed reserves of 4 to 64 SMs.
+inline int chain_reserve(int sms, int m)
+{
+    const int per152 = m >= 30000 ? 16 : (m >= 17000 ? 32 : 48);
+    return std::max(1, per152 * sms / 152);
+}
+
 // Look-ahead schedule.  After panel p is factorised its rank-512 update is split:
 // (1) the next panel's columns [K1, K2) on the caller's stream; then (2) all
 // columns right of K2 on the caller's stream with a grid that leaves a few SMs
@@ -1405,7 +1415,7 @@ int emulated_factor(double *A, int n, int64_t lda, double shift, Workspace &ws, 
     // SMs left to the panel chain.  Threads that run many solves side by side
     // (cooperative kernels off, e.g. batched fits) keep one stream per solve and
     // skip the look-ahead, so concurrent solves do not share the auxiliary stream.
-    const int reserve = (sms >= 64 && cooperative_on()) ? 8 : 0;
+    const bool lookahead = sms >= 64 && cooperative_on();
     st = factor_panel(A, n, lda, shift, 0, std::min(NBO, np), rpad, slices, dig_in, exp_in, d_info,
                       d_err, s, 0);
     for (int K0 = 0; K0 < np && st == QMLG_OK; K0 += NBO) {
@@ -1422,7 +1432,8 @@ int emulated_factor(double *A, int n, int64_t lda, double shift, Workspace &ws, 
             st = emu_tc_update(A, lda, K1, K2, K1, n, dig_out, exp_out, kp, rpad, slices, 0, 0, 1,
                                d_err, s, 0);
         if (st != QMLG_OK) break;
-        if (more && K2 < n && reserve > 0) {
+        if (more && K2 < n && lookahead) {
+            const int reserve = chain_reserve(sms, n - K2);
             // fork: the next panel's chain on the auxiliary stream
             if ((e = cudaEventRecord(aux->fork, s)) != cudaSuccess ||
                 (e = cudaStreamWaitEvent(aux->stream, aux->fork, 0)) != cudaSuccess) {
