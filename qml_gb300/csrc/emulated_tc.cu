@@ -96,26 +96,55 @@ struct TileArgs {
 
 // Walks the tile list in increasing order.  With `lower`, row-block it (TN rows of
 // i) holds the j-blocks jt with jbase + 128 jt <= ibase + TN it + TN - 1 (the tiles
-// that reach the lower triangle); otherwise every jt.
+// that reach the lower triangle); otherwise every jt.  The list runs in bands of
+// kBand row-blocks (1024 rows of i): inside a band j-block by j-block, each across
+// the band's row-blocks that hold it.  The CTAs working at the same time then share
+// one band's i-planes and a few j-planes, which stay in L2.
 template <int TN>
 struct TileCursor {
-    int it = 0, base = 0;
+    static constexpr int kBand = 1024 / TN;
+    int band = 0, jt = 0, base = 0, rows = -1;
     __device__ __forceinline__ int count(const TileArgs &p, int r) const
     {
         if (!p.lower) return p.tj;
         const int lim = p.ibase - p.jbase + TN * r + TN - 1;
         return lim < 0 ? 0 : min(p.tj, lim / TM + 1);
     }
-    __device__ __forceinline__ void locate(const TileArgs &p, int t, int &jt, int &itl)
+    // first row-block that holds j-block j (count(it) > j from there on)
+    __device__ __forceinline__ int first_it(const TileArgs &p, int j) const
     {
-        int c = count(p, it);
-        while (base + c <= t) {
-            base += c;
-            ++it;
-            c = count(p, it);
+        if (!p.lower) return 0;
+        const int need = j * TM - (p.ibase - p.jbase) - TN + 1;
+        return need <= 0 ? 0 : (need + TN - 1) / TN;
+    }
+    // t < ntiles; successive calls take nondecreasing t
+    __device__ __forceinline__ void locate(const TileArgs &p, int t, int &jto, int &itl)
+    {
+        const int ti = (p.iend - p.ibase + TN - 1) / TN;
+        for (;;) {
+            const int b0 = band * kBand, b1 = min(b0 + kBand, ti);
+            if (b0 >= ti) {  // past the list: not reached for t < ntiles
+                jto = 0;
+                itl = 0;
+                return;
+            }
+            if (rows < 0) rows = count(p, b1 - 1);
+            if (jt < rows) {
+                const int i0 = max(b0, first_it(p, jt));
+                const int len = b1 - i0;
+                if (base + len > t) {
+                    jto = jt;
+                    itl = i0 + (t - base);
+                    return;
+                }
+                base += len;
+                ++jt;
+            } else {
+                ++band;
+                jt = 0;
+                rows = -1;
+            }
         }
-        jt = t - base;
-        itl = it;
     }
 };
 
