@@ -121,6 +121,16 @@ struct TileCursor {
     __device__ __forceinline__ void locate(const TileArgs &p, int t, int &jto, int &itl)
     {
         const int ti = (p.iend - p.ibase + TN - 1) / TN;
+        if (!p.lower) {
+            // every band holds tj rows of its width: found directly, so a CTA that
+            // takes one tile (one CTA per tile) does not walk the list
+            const int b = t / (p.tj * kBand);
+            const int b0 = b * kBand, len = min(kBand, ti - b0);
+            const int rem = t - b * (p.tj * kBand);
+            jto = rem / len;
+            itl = b0 + rem % len;
+            return;
+        }
         for (;;) {
             const int b0 = band * kBand, b1 = min(b0 + kBand, ti);
             if (b0 >= ti) {  // past the list: not reached for t < ntiles
@@ -128,7 +138,23 @@ struct TileCursor {
                 itl = 0;
                 return;
             }
-            if (rows < 0) rows = count(p, b1 - 1);
+            if (rows < 0) {
+                // entering a band: skip it whole when t lies beyond it (its size
+                // summed over rows or over row-blocks, whichever are fewer)
+                const int nr = count(p, b1 - 1);
+                int tot = 0;
+                if (nr <= b1 - b0) {
+                    for (int j = 0; j < nr; ++j) tot += b1 - max(b0, first_it(p, j));
+                } else {
+                    for (int it = b0; it < b1; ++it) tot += count(p, it);
+                }
+                if (base + tot <= t) {
+                    base += tot;
+                    ++band;
+                    continue;
+                }
+                rows = nr;
+            }
             if (jt < rows) {
                 const int i0 = max(b0, first_it(p, jt));
                 const int len = b1 - i0;
