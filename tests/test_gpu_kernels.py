@@ -258,3 +258,47 @@ def test_more_kernels_arguments(cuda, cm_features):
         matern_kernel(A, A, 1000.0, order=3, metric="l1")
     with pytest.raises(SystemExit):
         matern_kernel(A, A, 1000.0, metric="l3")
+
+
+@pytest.mark.parametrize("persistent", [1, 0])
+def test_emulated_tiles_across_bands(cuda, oracle, persistent):
+    # The tensor-core kernels visit their tiles in bands of 1024 i-rows.  Sizes
+    # spanning several bands, with a persistent grid and with one CTA per tile:
+    # entries, predictions and the trailing update against the oracle and FP64, and
+    # bit-identical between the two launch shapes.
+    b = generate_molecules(3700, seed=21)
+    X = oracle.cm_sorted_batch(b.charges, b.coordinates, b.offsets, 23)
+    A, B = X[:2600], X[2600:]
+    At, Bt = torch.from_numpy(A).to(cuda), torch.from_numpy(B).to(cuda)
+    rng = np.random.default_rng(12)
+    alpha = rng.normal(size=2600)
+    P = rng.normal(size=(2100, 512)) * np.exp(rng.normal(size=(2100, 1)))
+    C = rng.normal(size=(2100, 2100))
+    lib = core.lib()
+    outs = {}
+    try:
+        for mode in (1, persistent):
+            lib.qmlg_set_thread_persistent(mode)
+            K = core.kernel_matrix("gaussian", At, Bt, 400.0, emulated=True).cpu().numpy()
+            Ks = core.kernel_matrix("gaussian", At, At, 400.0, symmetric=True,
+                                    emulated=True).cpu().numpy()
+            y = core.predict("gaussian", At, Bt, 400.0, torch.from_numpy(alpha).to(cuda),
+                             emulated=True).cpu().numpy()
+            Ct = torch.from_numpy(C.copy()).to(cuda)
+            core.syrk_emulated(Ct, torch.from_numpy(P).to(cuda))
+            outs[mode] = (K, Ks, y, Ct.cpu().numpy())
+    finally:
+        lib.qmlg_set_thread_persistent(1)
+    K, Ks, y, Cout = outs[persistent]
+    Ko = oracle.gaussian_kernel(A, B, 400.0)
+    assert relerr(K, Ko) <= RTOL
+    assert np.array_equal(Ks, Ks.T)
+    assert relerr(Ks, oracle.gaussian_kernel(A, A, 400.0)) <= RTOL
+    assert np.max(np.abs(y - Ko.T @ alpha) / (np.abs(Ko.T) @ np.abs(alpha))) <= 1e-12
+    tri = np.tril_indices(2100)
+    ref = C - P @ P.T
+    scale = np.abs(P) @ np.abs(P).T + np.abs(C)
+    assert np.max(np.abs(Cout[tri] - ref[tri]) / scale[tri]) < 1e-14
+    assert np.array_equal(np.triu(Cout, 1), np.triu(C, 1))
+    for u, v in zip(outs[1], outs[persistent]):
+        assert np.array_equal(u, v)
