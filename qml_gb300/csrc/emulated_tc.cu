@@ -503,6 +503,10 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
                 const double m2s = -2.0 * p.scale;
                 const long long m2s_bits = __double_as_longlong(m2s);
                 const int m2s_exp = (int)((m2s_bits >> 52) & 0x7ff);
+                double cs[HC];  // kPredict: this thread's k(a_j, b_i) alpha_j, i = column
+#pragma unroll
+                for (int k = 0; k < HC; ++k) cs[k] = 0.0;
+#pragma unroll
                 for (int gq = 0; gq < HC / EG; ++gq) {
                     const int cb = h * HC + gq * EG;
                     uint32_t v[S_MAX][EG];
@@ -541,11 +545,30 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
                                 if (p.lower && j < i) p.C[(int64_t)j * p.ldc + i] = kv;
                             }
                         } else {
-                            double c = valid ? kv * aw : 0.0;
-                            for (int off = 16; off > 0; off >>= 1) c += __shfl_xor_sync(0xffffffffu, c, off);
-                            if (lane == 0) red[q][il] = c;
+                            cs[gq * EG + col] = valid ? kv * aw : 0.0;
                         }
                     }
+                }
+                if constexpr (MODE == kPredict) {
+                    // column sums over the warp's 32 rows by recursive halving: each
+                    // step a lane keeps half of its columns and adds its partner's
+                    // values for them (9 FP64 adds for 8 columns, not 5 per column);
+                    // lanes 4m end with the sum of column (lane bits 4, 3, 2)
+                    static_assert(HC == 8, "the halving below is written for 8 columns");
+                    const bool h16 = (lane & 16) != 0, h8 = (lane & 8) != 0, h4 = (lane & 4) != 0;
+                    double v4[4], v2[2];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        v4[k] = (h16 ? cs[k + 4] : cs[k]) +
+                                __shfl_xor_sync(0xffffffffu, h16 ? cs[k] : cs[k + 4], 16);
+#pragma unroll
+                    for (int k = 0; k < 2; ++k)
+                        v2[k] = (h8 ? v4[k + 2] : v4[k]) +
+                                __shfl_xor_sync(0xffffffffu, h8 ? v4[k] : v4[k + 2], 8);
+                    double v1 = (h4 ? v2[1] : v2[0]) + __shfl_xor_sync(0xffffffffu, h4 ? v2[0] : v2[1], 4);
+                    v1 += __shfl_xor_sync(0xffffffffu, v1, 2);
+                    v1 += __shfl_xor_sync(0xffffffffu, v1, 1);
+                    if ((lane & 3) == 0) red[q][h * HC + (h16 ? 4 : 0) + (h8 ? 2 : 0) + (h4 ? 1 : 0)] = v1;
                 }
             }
             if (MODE == kPredict) {
