@@ -180,46 +180,82 @@ __device__ __forceinline__ double pow2i(int e)
     return ldexp(1.0, e);
 }
 
+// A double of magnitude below 2^128 truncated to FP32 on the bits (magnitudes below
+// 2^-126 read as 0), and an FP32 (normal or zero) as the exact FP64, on the bits.
+__device__ __forceinline__ float trunc_to_float(double x)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int e32 = (int)((b >> 52) & 0x7ff) - 896;
+    return e32 > 0 ? __uint_as_float((uint32_t)((b >> 32) & 0x80000000u) | ((uint32_t)e32 << 23) |
+                                     (uint32_t)((b >> 29) & 0x7fffffu))
+                   : 0.0f;
+}
+
+__device__ __forceinline__ double float_to_double_bits(float f)
+{
+    const uint32_t b = __float_as_uint(f);
+    const uint32_t e = (b >> 23) & 0xffu;
+    return e ? __longlong_as_double((long long)(((unsigned long long)(b & 0x80000000u) << 32) |
+                                                ((unsigned long long)(e + 896u) << 52) |
+                                                ((unsigned long long)(b & 0x7fffffu) << 29)))
+             : 0.0;
+}
+
 // exp(x) for the Gaussian epilogues, x <= 0 after clamping, by table-driven reduction
 // (P. T. P. Tang, "Table-driven implementation of the exponential function in IEEE
 // floating-point arithmetic", ACM TOMS 15(2), 1989):
-//   x = (128 m + j) ln2/128 + r,  |r| <= ln2/256,  exp(x) = 2^m 2^(j/128) e^r,
-// 2^(j/128) from a (lead, trail) table and 2^m applied to the exponent bits.  e^r - 1
-// is r + r^2/2 + c with c = r^3/6 + r^4/24 + r^5/120 (|c| < 3.3e-9, the next term is
-// below 6e-19): r^2/2 in FP64 (r/2 taken on the exponent bits), c in FP32 from r's
-// leading bits, where its relative error of ~6e-7 is below 2e-15 of e^r.  8 FP64
-// instructions; the range checks and FP32 <-> FP64 moves are integer operations on
-// the bits.  x > 0 (and +NaN) is clamped to 0, as the distance formula can round
-// slightly above it; x <= -700 and -NaN go to the library exp.
+//   x = (128 m + j) ln2/128 + r,  exp(x) = 2^m 2^(j/128) e^r,
+// 2^(j/128) from a (lead, trail) table and 2^m applied to the exponent bits.  FP64
+// instructions cost ~64 cycles of a scheduler's FP64 pipe here, FP32 ones one cycle,
+// so only four are FP64: the two FMAs of r = x - n ln2/128 (ln2/128 as hi + lo) and
+// the two of the reconstruction.  The rest runs in FP32 and on the bits:
+// - n = round(x 128/ln2) from x's leading 24 bits; it can be one off the nearest, so
+//   |r| <= 0.53 ln2/128.
+// - r = rh + rl: rh its leading 24 bits, rl the other 29 rounded to FP32.
+// - e^r - 1 = r + r^2/2 + c with c = r^3/6 + r^4/24 + r^5/120 (|c| < 4e-9, the next
+//   term is below 1e-18), c in FP32 from rh (relative error ~6e-7, below 3e-15 of
+//   e^r).  r^2/2 = hp + lo with hp = rh^2/2 (rh^2 exact as an FMA pair), and
+//   rh + hp = s + err exactly (Dekker's fast two-sum, |rh| >= |hp|); then
+//   e^r - 1 = s + t with t = rl + lo + c + err in FP32 (|t| < 5e-9).
+// - e^x = 2^m (T + T s + (T t + Tt)) with 2^(j/128) = T + Tt, T t + Tt in FP32.
+// Against an 80-bit reference over 2e7 arguments in [-700, 0] the relative error
+// stays below 2e-15.  x > 0 (and +NaN) is clamped to 0, as the distance formula can
+// round slightly above it; x <= -700 and -NaN go to the library exp.
 __device__ __forceinline__ double exp_nonpos(double x)
 {
     const long long xs = __double_as_longlong(x);
     if (xs > 0) return 1.0;
     if ((unsigned long long)xs >= 0xC085E00000000000ull) return exp(x);  // bits of -700.0
-    const double t = fma(x, k128OverLn2, 0x1.8p52);  // 1.5 * 2^52 + round(x * 128 / ln2)
-    const int n = (int)(__double_as_longlong(t) - 0x4338000000000000ll);
-    const double nd = t - 0x1.8p52;
+    const int n = __float2int_rn(__fmul_rn(trunc_to_float(x), 184.66496523378731f));  // 128/ln2
+    const double nd = float_to_double_bits(__int2float_rn(n));  // |n| < 2^17: exact
     double r = fma(-nd, kLn2Over128Hi, x);
     r = fma(-nd, kLn2Over128Lo, r);
     const unsigned long long rb = (unsigned long long)__double_as_longlong(r);
     const int ef = (int)((rb >> 52) & 0x7ff);
-    // r as FP32, truncated (|r| below 2^-126 reads as 0)
-    const int e32 = ef - 896;
-    const float rf = e32 > 0 ? __uint_as_float((uint32_t)((rb >> 32) & 0x80000000u) |
-                                               ((uint32_t)e32 << 23) | (uint32_t)((rb >> 29) & 0x7fffffu))
-                             : 0.0f;
-    const float cf = (rf * rf) * (rf * fmaf(rf, fmaf(rf, 1.0f / 120.0f, 1.0f / 24.0f), 1.0f / 6.0f));
-    // cf (normal or zero) as FP64
-    const uint32_t cb = __float_as_uint(cf);
-    const uint32_t ce = (cb >> 23) & 0xffu;
-    const double c = ce ? __longlong_as_double((long long)(((unsigned long long)(cb & 0x80000000u) << 32) |
-                                                           ((unsigned long long)(ce + 896u) << 52) |
-                                                           ((unsigned long long)(cb & 0x7fffffu) << 29)))
-                        : 0.0;
-    const double hr = ef >= 2 ? __longlong_as_double((long long)(rb - (1ull << 52))) : 0.0;  // r / 2
-    const double w = r + fma(r, hr, c);  // e^r - 1
+    const float rh = trunc_to_float(r);
+    float rl = 0.0f;
+    const uint32_t low = (uint32_t)(rb & 0x1fffffffu);
+    if (ef > 896 && low != 0u) {
+        // low * 2^(ef - 1075), rounded to FP32, with r's sign
+        const uint32_t lb = __float_as_uint(__uint2float_rn(low));
+        const int le = (int)((lb >> 23) & 0xffu) + (ef - 1075);
+        if (le > 0)
+            rl = __uint_as_float((uint32_t)((rb >> 32) & 0x80000000u) | ((uint32_t)le << 23) |
+                                 (lb & 0x7fffffu));
+    }
+    const float c = __fmul_rn(__fmul_rn(rh, rh),
+                              __fmul_rn(rh, __fmaf_rn(rh, __fmaf_rn(rh, 1.0f / 120.0f, 1.0f / 24.0f),
+                                                      1.0f / 6.0f)));
+    const float p = __fmul_rn(rh, rh);
+    const float pe = __fmaf_rn(rh, rh, -p);
+    const float hp = __fmul_rn(0.5f, p);
+    const float lo = __fmaf_rn(rh, rl, __fmul_rn(0.5f, pe));
+    const float sum = __fadd_rn(rh, hp);
+    const float err = __fsub_rn(hp, __fsub_rn(sum, rh));
+    const float t = __fadd_rn(__fadd_rn(__fadd_rn(rl, lo), c), err);
     const double2 T = kExp2Tab128[n & 127];
-    const double v = T.x + fma(T.x, w, T.y);
+    const float corr = __fmaf_rn(trunc_to_float(T.x), t, trunc_to_float(T.y));
+    const double v = T.x + fma(T.x, float_to_double_bits(sum), float_to_double_bits(corr));
     return __longlong_as_double(__double_as_longlong(v) + ((long long)(n >> 7) << 52));
 }
 
