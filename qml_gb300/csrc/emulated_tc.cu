@@ -218,9 +218,11 @@ __device__ __forceinline__ double float_to_double_bits(float f)
 //   rh + hp = s + err exactly (Dekker's fast two-sum, |rh| >= |hp|); then
 //   e^r - 1 = s + t with t = rl + lo + c + err in FP32 (|t| < 5e-9).
 // - e^x = 2^m (T + T s + (T t + Tt)) with 2^(j/128) = T + Tt, T t + Tt in FP32.
-// Against an 80-bit reference over 2e7 arguments in [-700, 0] the relative error
-// stays below 2e-15.  x > 0 (and +NaN) is clamped to 0, as the distance formula can
-// round slightly above it; x <= -700 and -NaN go to the library exp.
+// A host emulation of these steps stays below 2e-15 relative error against an 80-bit
+// reference over 2e7 arguments in [-700, 0]; on the GPU it is within 14 ulp of the
+// library exp over 16M points per range.  x > 0 (and +NaN) is clamped to 0, as the
+// distance formula can round slightly above it; x <= -700 and -NaN go to the
+// library exp.
 __device__ __forceinline__ double exp_nonpos(double x)
 {
     const long long xs = __double_as_longlong(x);
