@@ -27,3 +27,25 @@ def test_library_exports_every_declared_symbol():
         assert hasattr(lib, name), name
         assert name in _lib.SIGNATURES, name
     assert b"sm_103a" in lib.qmlg_version()
+
+
+def test_no_cpu_fallback():
+    # without a GPU the product path refuses to run instead of computing on the host
+    import numpy as np
+    import pytest
+    import torch
+
+    from qml_gb300 import core
+    from qml_gb300.kernels import gaussian_kernel
+    from qml_gb300.math import cho_solve
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    X = torch.rand(10, 276, dtype=torch.float64)
+    with pytest.raises(TypeError):
+        core.kernel_matrix("gaussian", X, X, 1000.0)
+    with pytest.raises(RuntimeError):
+        gaussian_kernel(np.random.rand(5, 276), np.random.rand(4, 276), 100.0)
+    A = np.eye(4) * 2.0
+    with pytest.raises(RuntimeError):
+        cho_solve(A, np.ones(4))
