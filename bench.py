@@ -1,18 +1,24 @@
 """KRR fit+predict benchmark on one GB300 (per-rank replicas when launched with N > 1).
 
-Workload (the "kernel and solve at scale" configuration): seeded synthetic molecules
-(QM7-like: n_atoms ~ U{5..23}, Z in {1,6,7,8,16}), sorted Coulomb matrix size 23
-(276 features, FP64), Gaussian kernel sigma = 1000, lambda = 1e-8, 20000 training
-and 5000 test molecules.  One step is one KRR fit + predict over molecules already
-in HBM:
-    CM of 25000 molecules -> K = k(X, X) (20000^2, symmetric) -> alpha = solve(K + lambda I, y)
+Workload (the mixed-precision target size): seeded synthetic molecules (QM7-like:
+n_atoms ~ U{5..23}, Z in {1,6,7,8,16}), sorted Coulomb matrix size 23 (276 features,
+FP64), Gaussian kernel sigma = 1000, lambda = 1e-8, 40000 training and 10000 test
+molecules.  One step is one KRR fit + predict over molecules already in HBM:
+    CM of 50000 molecules -> K = k(X, X) (40000^2, symmetric) -> alpha = solve(K + lambda I, y)
     -> yhat = k(Xs, X) alpha (fused, Ks not materialised)
-with the solve in the mixed mode (emulated-FP64 tensor-core factor + double-double
-refinement).  The plain FP64 path is timed once beside it.
+with the solve in the mixed mode (emulated-FP64 tensor-core factor + refinement on
+an exactly summed residual).  Beside it, in the same run:
+  * the plain FP64 GPU path, timed --fp64-reps times (median), and the mixed alpha
+    against the FP64-refined alpha on the same FP64 K;
+  * 60000 train x 10000 test Gaussian and Laplacian fits (a 28.8 GB K);
+  * continuous-batching serving against a resident 50000-molecule model (p50/p99);
+  * 64 uneven fits recorded into one CUDA graph;
+  * a bounded CPU sample of the reference's path on the host cores.
 
-Prints ONE JSON line (rank 0).  ``--impl reference`` times the CPU path instead:
-the oracle's C/OpenMP restatement of the reference's Fortran routines plus SciPy
-LAPACK dpotrf/dpotrs (the routines the reference calls) on the host cores.
+Prints ONE JSON line (rank 0); a compact "headline" object closes the line.
+``--impl reference`` times the CPU path instead: the oracle's C/OpenMP restatement of
+the reference's Fortran routines plus SciPy LAPACK dpotrf/dpotrs (the routines the
+reference calls) on the host cores.
 """
 from __future__ import annotations
 
@@ -33,19 +39,20 @@ METRIC = "KRR fit+predict s & p99 query latency: mixed vs FP64 on GB300 at 1e-8 
 UNIT = "s"
 
 
-def parse():
+def parse(argv=None):
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--ntrain", type=int, default=20000)
-    p.add_argument("--ntest", type=int, default=5000)
+    p.add_argument("--ntrain", type=int, default=40000)
+    p.add_argument("--ntest", type=int, default=10000)
     p.add_argument("--sigma", type=float, default=1000.0)
     p.add_argument("--lam", type=float, default=1e-8)
     p.add_argument("--kernel", default="gaussian", choices=["gaussian", "laplacian"])
     p.add_argument("--seed", type=int, default=2024)
-    p.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison")
+    p.add_argument("--fp64-reps", type=int, default=3,
+                   help="plain FP64 GPU fit+predict repeats (0 skips the comparison)")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     p.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
     p.add_argument("--serve-n", type=int, default=50000, help="resident model size")
@@ -53,10 +60,15 @@ def parse():
     p.add_argument("--serve-seconds", type=float, default=10.0)
     p.add_argument("--serve-fit-every", type=int, default=50, help="every k-th arrival is a fit")
     p.add_argument("--no-batching", action="store_true", help="skip the batched-fits measurement")
-    p.add_argument("--no-extra", action="store_true",
-                   help="skip the atomic-CM / local-kernel measurement")
     p.add_argument("--batch-count", type=int, default=64)
-    return p.parse_args()
+    p.add_argument("--no-large", action="store_true",
+                   help="skip the 60000 x 10000 Gaussian and Laplacian fits")
+    p.add_argument("--large-train", type=int, default=60000)
+    p.add_argument("--large-test", type=int, default=10000)
+    p.add_argument("--no-extra", action="store_true",
+                   help="skip the other kernel matrices and the atomic-CM / local-kernel / "
+                        "inverse measurements")
+    return p.parse_args(argv)
 
 
 def workload_config(a):
@@ -70,74 +82,122 @@ def workload_config(a):
 
 # ----------------------------------------------------------------- CPU leg --
 
-def cpu_pipeline_sample(batch, a, sample=8):
-    """The reference's CPU path on a bounded sample of the workload, scaled to one
-    full fit+predict: all Coulomb matrices; 1/sample of the rows of the training and
-    test kernel matrices (scaled by sample); LAPACK dpotrf + dpotrs on an N/2
-    sub-problem (scaled by 8, the N^3 ratio); the prediction GEMV on the sampled
-    rows (scaled by sample)."""
-    import numpy as np
-    from scipy.linalg import lapack
-
+def _kernel_fn(kind):
     from oracle import oracle
-    ntr, nte = a.ntrain, a.ntest
-    kfn = oracle.gaussian_kernel if a.kernel == "gaussian" else oracle.laplacian_kernel
-    t = {}
+    return oracle.gaussian_kernel if kind == "gaussian" else oracle.laplacian_kernel
+
+
+def cpu_cm(batch):
+    from oracle import oracle
     t0 = time.perf_counter()
     X = oracle.cm_sorted_batch(batch.charges, batch.coordinates, batch.offsets, 23)
-    t["cm"] = time.perf_counter() - t0
+    return X, time.perf_counter() - t0
+
+
+def cpu_test_side(Xtr, Xte, a, frac):
+    """K_test on 1/frac of the test rows and the prediction GEMV on them, each
+    scaled by frac (the rows are independent, so the work scales linearly)."""
+    import numpy as np
+    kfn = _kernel_fn(a.kernel)
+    nte = Xte.shape[0]
+    rows = max(1, nte // frac)
+    t0 = time.perf_counter()
+    Ks = kfn(Xtr, Xte[:rows], a.sigma)
+    t_k = (time.perf_counter() - t0) * (nte / rows)
+    alpha = np.random.default_rng(0).normal(size=Xtr.shape[0])
+    t0 = time.perf_counter()
+    _ = Ks.T @ alpha
+    t_p = (time.perf_counter() - t0) * (nte / rows)
+    return t_k, t_p
+
+
+def cpu_baseline_sample(batch, a):
+    """Bounded CPU sample (about ten seconds) of the reference's path, scaled to one
+    full fit+predict: all Coulomb matrices; 1/16 of the rows of K_train and K_test
+    (scaled by 16); LAPACK dpotrf + dpotrs on the leading N/2 block (scaled by 8,
+    the N^3 ratio); the prediction GEMV on the sampled test rows (scaled by 16)."""
+    import numpy as np
+    from scipy.linalg import lapack
+    kfn = _kernel_fn(a.kernel)
+    ntr, nte = a.ntrain, a.ntest
+    t = {}
+    X, t["cm"] = cpu_cm(batch)
     Xtr, Xte = X[:ntr], X[ntr:ntr + nte]
-    rows = max(1, ntr // sample)
+    rows = max(1, ntr // 16)
     t0 = time.perf_counter()
-    Kpart = kfn(Xtr, Xtr[:rows], a.sigma)
+    kfn(Xtr, Xtr[:rows], a.sigma)
     t["kernel_train"] = (time.perf_counter() - t0) * (ntr / rows)
-    trows = max(1, nte // sample)
-    t0 = time.perf_counter()
-    Ks = kfn(Xtr, Xte[:trows], a.sigma)
-    t["kernel_test"] = (time.perf_counter() - t0) * (nte / trows)
-    nh = ntr // 2
+    t["kernel_test"], t["predict"] = cpu_test_side(Xtr, Xte, a, 16)
+    nh = max(1, ntr // 2)
     Kh = kfn(Xtr[:nh], Xtr[:nh], a.sigma)
     Kh[np.diag_indices_from(Kh)] += a.lam
     t0 = time.perf_counter()
     c, info = lapack.dpotrf(Kh, lower=0, overwrite_a=1, clean=0)
-    x, _ = lapack.dpotrs(c, batch.labels[:nh], lower=0)
+    lapack.dpotrs(c, batch.labels[:nh], lower=0)
     t["cholesky"] = (time.perf_counter() - t0) * (ntr / nh) ** 3
-    alpha = np.random.default_rng(0).normal(size=ntr)
-    t0 = time.perf_counter()
-    _ = Ks.T @ alpha
-    t["predict"] = (time.perf_counter() - t0) * (nte / trows)
-    del Kpart
-    total = sum(t.values())
-    return total, t
-
-
-def cpu_sample_text(a):
-    return ("all %d CMs; 1/8 of the rows of K_train (%dx%d) and K_test (%dx%d), scaled x8; "
-            "dpotrf+dpotrs at N=%d scaled x8 (N^3); predict GEMV on the sampled rows x8"
-            % (a.ntrain + a.ntest, a.ntrain, a.ntrain, a.ntrain, a.ntest, a.ntrain // 2))
+    sample = ("all %d CMs; 1/16 of the rows of K_train (%dx%d) and K_test (%dx%d), scaled x16; "
+              "dpotrf+dpotrs at N=%d scaled x%.0f (N^3); predict GEMV on the sampled rows x16"
+              % (ntr + nte, ntr, ntr, ntr, nte, nh, (ntr / nh) ** 3))
+    return sum(t.values()), t, sample
 
 
 def run_reference(a):
+    """The reference's CPU path on the host cores.  The two stages that hold ~95% of
+    the time run once at full size: K_train (the oracle's OpenMP restatement of
+    fgaussian_kernel, all N^2 entries as the reference computes them) and LAPACK
+    dpotrf + dpotrs on K_train + lambda I at full N.  Each step then times the
+    Coulomb matrices of every molecule and, on 1/16 of the test rows scaled by 16,
+    K_test and the prediction GEMV.  value = the full-size stages + the mean step."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
+    import numpy as np
+    from scipy.linalg import lapack
+
     from qml_gb300.synthetic import generate_molecules
-    batch = generate_molecules(a.ntrain + a.ntest, seed=a.seed)
+    kfn = _kernel_fn(a.kernel)
+    ntr, nte = a.ntrain, a.ntest
+    batch = generate_molecules(ntr + nte, seed=a.seed)
+    X, _ = cpu_cm(batch)
+    Xtr, Xte = X[:ntr], X[ntr:ntr + nte]
+
+    def step():
+        _, t_cm = cpu_cm(batch)
+        t_k, t_p = cpu_test_side(Xtr, Xte, a, 16)
+        return {"cm": t_cm, "kernel_test": t_k, "predict": t_p}
+
     for _ in range(a.warmup):
-        cpu_pipeline_sample(batch, a)
-    times = []
-    for _ in range(a.steps):
-        total, parts = cpu_pipeline_sample(batch, a)
-        times.append(total)
-    v = statistics.mean(times)
+        step()
+    # the dominant stages at full size, once
+    t0 = time.perf_counter()
+    K = kfn(Xtr, Xtr, a.sigma)
+    t_ktrain = time.perf_counter() - t0
+    K[np.diag_indices_from(K)] += a.lam
+    t0 = time.perf_counter()
+    c, info = lapack.dpotrf(K, lower=0, overwrite_a=1, clean=0)
+    lapack.dpotrs(c, batch.labels[:ntr], lower=0)
+    t_chol = time.perf_counter() - t0
+    del K, c
+    steps = [step() for _ in range(a.steps)]
+    parts = {k: statistics.mean(s[k] for s in steps) for k in steps[0]}
+    parts["kernel_train"] = t_ktrain
+    parts["cholesky"] = t_chol
+    v = sum(parts.values())
     cores = os.cpu_count()
+    sample = ("estimate: K_train (%dx%d) and dpotrf+dpotrs at N=%d timed once at full size; "
+              "per step all %d CMs at full size, K_test and the predict GEMV on 1/16 of the "
+              "%d test rows, scaled x16" % (ntr, ntr, ntr, ntr + nte, nte))
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": workload_config(a), "impl": "reference",
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": cpu_sample_text(a)},
+                             "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "estimate": True,
+            "full_size_stages": ["kernel_train", "cholesky", "cm"],
+            "scaled_stages": {"kernel_test": 16, "predict": 16},
+            "dpotrf_info": int(info),
             "stages_s": parts}
     print(json.dumps(line), flush=True)
     return 0
@@ -202,6 +262,15 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def _events(n):
+    import torch
+    return [torch.cuda.Event(enable_timing=True) for _ in range(n)]
+
+
+def _span(e0, e1):
+    return e0.elapsed_time(e1) / 1e3
+
+
 def run_serving(a, dev):
     """Continuous-batching serving: one resident Gaussian model of serve_n molecules,
     Poisson query arrivals (1..4096 molecules, log-uniform), fits of N in
@@ -234,90 +303,103 @@ def run_serving(a, dev):
                               model_sizes={"main": a.serve_n})
     done = serving.Server(ex, sched).run(reqs)
     st = serving.latency_stats(done)
+    fits = st.pop("fit_latency_ms")
     st.update({"resident_n": a.serve_n, "resident_fit_s": fit_s, "rate_hz": a.serve_rate,
                "duration_s": a.serve_seconds, "query_molecules": "log-uniform 1..4096",
                "fit_sizes": "log-uniform 1000..20000", "hbm_budget_gb": 64,
-               "precision": "mixed"})
-    st["fit_latency_ms"] = {"n": len(st["fit_latency_ms"]),
-                            "max": max(st["fit_latency_ms"]) if st["fit_latency_ms"] else None}
+               "fit_latency_max_ms": max(fits) if fits else None})
     return st
 
 
-def run_extra(a, dev, batch):
-    """The components beyond the KRR hot path (atomic Coulomb matrices, local
-    kernels), each timed on the GPU (CUDA events) and on a bounded CPU sample of the
-    oracle restatement, on the bench's synthetic molecules."""
+def run_extra(a, dev, batch, X, stream):
+    """Paths beside the KRR hot path, each timed on the GPU (CUDA events) and, where
+    the CPU side is cheap, on the host: the other training kernel matrices, atomic
+    Coulomb matrices, local kernels, the inverses and Bunch-Kaufman."""
     import numpy as np
-    from oracle import oracle as orc
-    import time as _t
     import torch
+
+    from oracle import oracle as orc
     from qml_gb300 import core
     from qml_gb300.krr import molecules_to_device
-    z, r, o = molecules_to_device(batch)
+    ntr = a.ntrain
     out = {}
 
-    def gpu_time(fn, reps=3):
+    def gpu_time(fn, reps=1):
         fn()
         torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record()
+        e0, e1 = _events(2)
+        e0.record(stream)
         for _ in range(reps):
             fn()
-        e1.record()
+        e1.record(stream)
         torch.cuda.synchronize()
-        return e0.elapsed_time(e1) / reps / 1e3
+        return _span(e0, e1) / reps
 
-    nmol = batch.n_mol
-    t = gpu_time(lambda: core.atomic_coulomb_matrix_batch(z, r, o, 23, "row-norm"))
+    Xtr = X[:ntr]
+
+    def kernel(kind, emulated, **kw):
+        return lambda: core.kernel_matrix(kind, Xtr, Xtr, a.sigma, symmetric=True,
+                                          emulated=emulated, **kw)
+    out["train_kernel_matrix_s"] = {
+        "n": ntr,
+        "gaussian_fp64": gpu_time(kernel("gaussian", False)),
+        "gaussian_tensor": gpu_time(kernel("gaussian", True), reps=3),
+        "laplacian_fp64": gpu_time(kernel("laplacian", False)),
+        "laplacian_fixed": gpu_time(kernel("laplacian", True), reps=3),
+        "linear_fp64": gpu_time(kernel("linear", False)),
+        "matern_l2_order2_fp64": gpu_time(kernel("matern_l2", False, order=2)),
+        "sargan_2gammas_fp64": gpu_time(kernel("sargan", False, gammas=[1.0, 1.0 / 3.0]))}
+    torch.cuda.empty_cache()
+
+    sub = batch.slice(0, 25000)
+    z, r, o = molecules_to_device(sub)
+    t = gpu_time(lambda: core.atomic_coulomb_matrix_batch(z, r, o, 23, "row-norm"), reps=3)
     ns = 200
-    c0 = _t.perf_counter()
+    c0 = time.perf_counter()
     for m in range(ns):
-        orc.atomic_cm(*batch.molecule(m), None, 23, "row-norm")
-    cpu = (_t.perf_counter() - c0) * nmol / ns
-    out["atomic_cm_rownorm"] = {"molecules": nmol, "atoms": int(batch.offsets[-1]), "gpu_s": t,
-                                "cpu_oracle_s_scaled": cpu,
+        orc.atomic_cm(*sub.molecule(m), None, 23, "row-norm")
+    cpu = (time.perf_counter() - c0) * sub.n_mol / ns
+    out["atomic_cm_rownorm"] = {"molecules": sub.n_mol, "atoms": int(sub.offsets[-1]),
+                                "gpu_s": t, "cpu_oracle_s_scaled": cpu,
                                 "cpu_sample": "%d molecules, 1 thread, scaled" % ns}
     nl = 2000
     sub = batch.slice(0, nl)
     zs, rs, os_ = molecules_to_device(sub)
     Xa = core.atomic_coulomb_matrix_batch(zs, rs, os_, 23, "row-norm")
-    t = gpu_time(lambda: core.local_kernels("gaussian", Xa, Xa, os_, os_, [724.0], symmetric=True),
-                 reps=1)
+    t = gpu_time(lambda: core.local_kernels("gaussian", Xa, Xa, os_, os_, [724.0], symmetric=True))
     Xh = Xa.cpu().numpy()
     nh = np.diff(sub.offsets)
     rows = 50
-    c0 = _t.perf_counter()
+    c0 = time.perf_counter()
     orc.local_kernels("gaussian", Xh[:int(sub.offsets[rows])], Xh, nh[:rows], nh, [724.0])
-    cpu = (_t.perf_counter() - c0) * nl / rows
+    cpu = (time.perf_counter() - c0) * nl / rows
     out["local_gaussian_kernel"] = {"molecules": nl, "gpu_s": t, "cpu_oracle_s_scaled": cpu,
                                     "cpu_sample": "%d of %d rows, OpenMP on %d cores, scaled"
                                                   % (rows, nl, os.cpu_count())}
-    # cho_invert of an N=5000 Gaussian KRR matrix (K + 1e-4 I)
+    # cho_invert, Bunch-Kaufman solve and inverse of an N=5000 Gaussian KRR matrix
     ni = 5000
-    Xi = core.coulomb_matrix_batch(*molecules_to_device(batch.slice(0, ni)), 23)
+    Xi = X[:ni]
     Ki = core.kernel_matrix("gaussian", Xi, Xi, 1000.0, symmetric=True, diag_shift=1e-4)
-    tf = gpu_time(lambda: core.cho_invert(Ki, "fp64"), reps=1)
-    tm = gpu_time(lambda: core.cho_invert(Ki, "mixed"), reps=1)
-    Kh = np.asfortranarray(Ki.cpu().numpy())
-    c0 = _t.perf_counter()
-    orc.cho_invert(Kh)
-    cpu = _t.perf_counter() - c0
-    out["cho_invert"] = {"n": ni, "gpu_fp64_s": tf, "gpu_mixed_s": tm, "cpu_lapack_s": cpu,
-                         "cpu_sample": "scipy dpotrf + dpotri, full size, OpenBLAS threads"}
-    # Bunch-Kaufman solve and inverse of the same matrix
+    tf = gpu_time(lambda: core.cho_invert(Ki, "fp64"))
+    tm = gpu_time(lambda: core.cho_invert(Ki, "mixed"))
     yi = torch.ones(ni, dtype=torch.float64, device=dev)
-    ts = gpu_time(lambda: core.bkf_solve(Ki, yi), reps=1)
-    tv = gpu_time(lambda: core.bkf_invert(Ki), reps=1)
-    c0 = _t.perf_counter()
+    ts = gpu_time(lambda: core.bkf_solve(Ki, yi))
+    tv = gpu_time(lambda: core.bkf_invert(Ki))
+    Kh = np.asfortranarray(Ki.cpu().numpy())
+    c0 = time.perf_counter()
+    orc.cho_invert(Kh)
+    ci = time.perf_counter() - c0
+    c0 = time.perf_counter()
     orc.bkf_solve(Kh, np.ones(ni))
-    cs = _t.perf_counter() - c0
-    c0 = _t.perf_counter()
+    cs = time.perf_counter() - c0
+    c0 = time.perf_counter()
     orc.bkf_invert(Kh)
-    cv = _t.perf_counter() - c0
-    out["bkf"] = {"n": ni, "gpu_solve_s": ts, "gpu_invert_s": tv, "cpu_lapack_solve_s": cs,
-                  "cpu_lapack_invert_s": cv,
-                  "cpu_sample": "scipy dsytrf + dsytrs / dsytri, full size, OpenBLAS threads"}
+    cv = time.perf_counter() - c0
+    out["inverses_n5000"] = {"cho_invert_gpu_fp64_s": tf, "cho_invert_gpu_mixed_s": tm,
+                             "cho_invert_lapack_s": ci, "bkf_solve_gpu_s": ts,
+                             "bkf_solve_lapack_s": cs, "bkf_invert_gpu_s": tv,
+                             "bkf_invert_lapack_s": cv,
+                             "cpu_sample": "scipy LAPACK, full size, OpenBLAS threads"}
     return out
 
 
@@ -355,46 +437,78 @@ def run_batching(a, dev):
     stream = torch.cuda.current_stream(dev)
     b.replay()
     torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
+    e0, e1 = _events(2)
     reps = 3
     e0.record(stream)
     for _ in range(reps):
         b.replay()
     e1.record(stream)
     torch.cuda.synchronize()
-    graph_s = e0.elapsed_time(e1) / reps / 1e3
+    graph_s = _span(e0, e1) / reps
     alphas, reports = b.results()
     ok = sum(1 for rp in reports if rp["info"] == 0 and rp["flags"] == 0)
     # the same fits one after another (kernel + mixed solve each, host-driven)
     t0 = time.perf_counter()
-    seq_alpha = []
     for p in probs:
-        m = KRR(sigma=p.sigma, lam=p.lam, precision="mixed").fit(p.X, p.y)
-        seq_alpha.append(m.alpha)
+        KRR(sigma=p.sigma, lam=p.lam, precision="mixed").fit(p.X, p.y)
     torch.cuda.synchronize()
     seq_s = time.perf_counter() - t0
-    worst = max(float(torch.linalg.norm(x - y) / torch.linalg.norm(y))
-                for x, y in zip(alphas, seq_alpha))
     sizes = [p.X.shape[0] for p in probs]
     return {"fits": len(probs), "n_min": min(sizes), "n_max": max(sizes),
             "n_sum": int(sum(sizes)), "graph_s": graph_s, "sequential_s": seq_s,
-            "speedup": seq_s / graph_s, "converged": ok, "schedule": tuned,
-            "alpha_rel_diff_vs_sequential_max": worst,
-            "note": "same kernel matrices? no: the sequential fits choose the digit-plane "
-                    "count per fit, the graph always uses 8; both within 1e-12 of FP64"}
+            "speedup": seq_s / graph_s, "converged": ok,
+            "schedule": {k: tuned[k] for k in tuned if k != "ms"}}
 
 
-def run_ours(a):
-    import numpy as np
+def run_large(a, dev, stream):
+    """The 60000 train x 10000 test fits (Gaussian and Laplacian, sigma 1000, lambda
+    1e-8, mixed), each timed twice after one warm-up (the median is reported)."""
     import torch
-    import torch.distributed as dist
 
     from qml_gb300 import core
     from qml_gb300.krr import KRR, molecules_to_device
     from qml_gb300.synthetic import generate_molecules
+    ntr, nte = a.large_train, a.large_test
+    batch = generate_molecules(ntr + nte, seed=a.seed + 5)
+    z, r, off = molecules_to_device(batch, device=dev)
+    y = torch.from_numpy(batch.labels).to(dev)
+    out = {"n_train": ntr, "n_test": nte, "sigma": a.sigma, "lambda": a.lam}
+    for kind in ("gaussian", "laplacian"):
+        times, rep = [], None
+        for k in range(3):
+            torch.cuda.synchronize()
+            e = _events(5)
+            e[0].record(stream)
+            X = core.coulomb_matrix_batch(z, r, off, 23)
+            e[1].record(stream)
+            K = core.kernel_matrix(kind, X[:ntr], X[:ntr], a.sigma, symmetric=True, emulated=True)
+            e[2].record(stream)
+            alpha, rep = core.solve(K, y[:ntr], a.lam, precision="mixed")
+            e[3].record(stream)
+            core.predict(kind, X[:ntr], X[ntr:ntr + nte], a.sigma, alpha, emulated=True)
+            e[4].record(stream)
+            torch.cuda.synchronize()
+            del K
+            if k > 0:
+                times.append([_span(e[0], e[4]), _span(e[1], e[2]), _span(e[2], e[3]),
+                              _span(e[3], e[4])])
+        times.sort()
+        med = times[len(times) // 2]
+        out[kind] = {"fit_predict_s": med[0], "kernel_s": med[1], "solve_s": med[2],
+                     "predict_s": med[3], "refine_steps": rep["outer_iterations"],
+                     "fell_back": rep["fell_back"]}
+        torch.cuda.empty_cache()
+    return out
 
-    from qml_gb300 import replicas
+
+def run_ours(a):
+    import torch
+    import torch.distributed as dist
+
+    from qml_gb300 import core, replicas
+    from qml_gb300.krr import KRR, molecules_to_device
+    from qml_gb300.synthetic import generate_molecules
+
     world, rank, local = replicas.rank_info()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
@@ -422,8 +536,7 @@ def run_ours(a):
         step()
     barrier()
     with ClockSampler(local) as clocks:
-        ev0 = torch.cuda.Event(enable_timing=True)
-        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0, ev1 = _events(2)
         ev0.record(stream)
         for _ in range(a.steps):
             yhat, model = step()
@@ -431,6 +544,7 @@ def run_ours(a):
         barrier()
     ms = replicas.max_over_ranks(ev0.elapsed_time(ev1) / a.steps, device=dev)
     report = model.report
+    del model, yhat
 
     # end to end through the public API with host buffers (pinned), copies inside
     hz = torch.from_numpy(batch.charges).pin_memory()
@@ -449,91 +563,85 @@ def run_ours(a):
 
     e2e_step()
     barrier()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
+    e0, e1 = _events(2)
     e0.record(stream)
     for _ in range(a.steps):
         e2e_step()
     e1.record(stream)
     barrier()
-    e2e_s = replicas.max_over_ranks(e0.elapsed_time(e1) / a.steps / 1e3, device=dev)
+    e2e_s = replicas.max_over_ranks(_span(e0, e1) / a.steps, device=dev)
 
-    # per-stage times of one mixed step (events between stages)
-    stages = {}
-    evs = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+    # per-stage times of one mixed step (events between stages), and the mixed
+    # factorisation alone on a copy of the same K
+    evs = _events(5)
     evs[0].record(stream)
     X = core.coulomb_matrix_batch(z, r, off, 23)
     evs[1].record(stream)
     K = core.kernel_matrix(a.kernel, X[:ntr], X[:ntr], a.sigma, symmetric=True, emulated=True)
+    Kf = K.clone()
     evs[2].record(stream)
     alpha, rep = core.solve(K, y[:ntr], a.lam, precision="mixed")
     evs[3].record(stream)
     core.predict(a.kernel, X[:ntr], X[ntr:ntr + nte], a.sigma, alpha, emulated=True)
     evs[4].record(stream)
     torch.cuda.synchronize()
-    for k, name in enumerate(["cm", "kernel_train", "solve", "predict"]):
-        stages[name] = evs[k].elapsed_time(evs[k + 1]) / 1e3
-    del K
-
-    # the Laplacian kernel of the same training set: FP64 and fixed-point paths
-    def time_kernel(kind, emulated, reps=2, **kw):
-        core.kernel_matrix(kind, X[:ntr], X[:ntr], a.sigma, symmetric=True, emulated=emulated,
-                           **kw)
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(reps):
-            core.kernel_matrix(kind, X[:ntr], X[:ntr], a.sigma, symmetric=True, emulated=emulated,
-                               **kw)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        return e0.elapsed_time(e1) / reps / 1e3
-    kernels_s = {"gaussian_fp64": time_kernel("gaussian", False),
-                 "gaussian_tensor": time_kernel("gaussian", True),
-                 "laplacian_fp64": time_kernel("laplacian", False),
-                 "laplacian_fixed": time_kernel("laplacian", True),
-                 "linear_fp64": time_kernel("linear", False, reps=1),
-                 "matern_l2_order2_fp64": time_kernel("matern_l2", False, reps=1, order=2),
-                 "sargan_2gammas_fp64": time_kernel("sargan", False, reps=1,
-                                                    gammas=[1.0, 1.0 / 3.0])}
+    stages = {name: _span(evs[k], evs[k + 1])
+              for k, name in enumerate(["cm", "kernel_train", "solve", "predict"])}
+    f0, f1 = _events(2)
+    f0.record(stream)
+    core.cholesky(Kf, a.lam, precision="mixed")
+    f1.record(stream)
+    torch.cuda.synchronize()
+    stages["factor"] = _span(f0, f1)
+    del K, Kf
 
     # dominant kernel: the emulated trailing update of the mixed Cholesky
     # (first outer step of this workload: C (n-512)^2 lower, P (n-512) x 512)
-    nsy = ntr - 512
-    ksy = 512
+    nsy, ksy = ntr - 512, 512
     Csy = torch.rand((nsy, nsy), dtype=torch.float64, device=dev)
     Psy = torch.rand((nsy, ksy), dtype=torch.float64, device=dev)
     core.syrk_emulated(Csy, Psy)
-    kev0 = torch.cuda.Event(enable_timing=True)
-    kev1 = torch.cuda.Event(enable_timing=True)
+    k0, k1 = _events(2)
     nk = 3
-    kev0.record(stream)
+    k0.record(stream)
     for _ in range(nk):
         core.syrk_emulated(Csy, Psy)
-    kev1.record(stream)
+    k1.record(stream)
     torch.cuda.synchronize()
-    syrk_s = kev0.elapsed_time(kev1) / nk / 1e3
+    syrk_s = _span(k0, k1) / nk
     del Csy, Psy
+    torch.cuda.empty_cache()
 
-    # accuracy: mixed alpha vs FP64 + double-double refinement on the same K
+    # the plain FP64 GPU path: fit + predict timed --fp64-reps times; the first
+    # repeat's alpha (FP64 factor + refinement) is compared with the mixed solve of
+    # the identical FP64 K
     fp64 = {}
-    K = core.kernel_matrix(a.kernel, X[:ntr], X[:ntr], a.sigma, symmetric=True)
-    Kc = K.clone()
-    alpha_m, rep_m = core.solve(K, y[:ntr], a.lam, precision="mixed")
-    if not a.no_fp64:
-        f0 = torch.cuda.Event(enable_timing=True)
-        f1 = torch.cuda.Event(enable_timing=True)
-        f0.record(stream)
-        yf, mf = step("fp64")
-        f1.record(stream)
-        torch.cuda.synchronize()
-        fp64["fit_predict_s"] = f0.elapsed_time(f1) / 1e3
-        alpha_f, rep_f = core.solve(Kc, y[:ntr], a.lam, precision="fp64", max_outer=10, tol=1e-16)
-        fp64["alpha_rel_err_mixed_vs_fp64_refined"] = float(
-            torch.linalg.norm(alpha_m - alpha_f) / torch.linalg.norm(alpha_f))
-        fp64["speedup_mixed_vs_fp64"] = fp64["fit_predict_s"] / (ms / 1e3)
-        fp64["fp64_report"] = rep_f
-    del K, Kc
+    if a.fp64_reps > 0:
+        times, err, rep_f = [], None, None
+        for k in range(a.fp64_reps):
+            e = _events(5)
+            e[0].record(stream)
+            X = core.coulomb_matrix_batch(z, r, off, 23)
+            K64 = core.kernel_matrix(a.kernel, X[:ntr], X[:ntr], a.sigma, symmetric=True)
+            e[1].record(stream)
+            Kc = K64.clone() if k == 0 else None
+            e[2].record(stream)
+            alpha_f, rep_f = core.solve(K64, y[:ntr], a.lam, precision="fp64")
+            core.predict(a.kernel, X[:ntr], X[ntr:ntr + nte], a.sigma, alpha_f)
+            e[3].record(stream)
+            torch.cuda.synchronize()
+            times.append(_span(e[0], e[1]) + _span(e[2], e[3]))
+            del K64
+            if k == 0:
+                alpha_m, rep_m = core.solve(Kc, y[:ntr], a.lam, precision="mixed")
+                err = float(torch.linalg.norm(alpha_m - alpha_f) / torch.linalg.norm(alpha_f))
+                del Kc
+            torch.cuda.empty_cache()
+        med = statistics.median(times)
+        fp64 = {"fit_predict_s_median": med, "fit_predict_s": times,
+                "speedup_mixed_vs_fp64": med / (ms / 1e3),
+                "alpha_rel_err_mixed_vs_fp64_refined": err,
+                "fp64_refine_steps": rep_f["outer_iterations"]}
 
     # our kernel launches per step, counted by the library itself
     lib = core.lib()
@@ -543,31 +651,32 @@ def run_ours(a):
     torch.cuda.synchronize()
     launches = int(lib.qmlg_launch_count() - c0) * a.steps
 
-    serving_stats = None
-    if not a.no_serving:
-        serving_stats = run_serving(a, dev)
-    batching_stats = None
-    if not a.no_batching:
-        batching_stats = run_batching(a, dev)
-    extra_stats = None
+    large = run_large(a, dev, stream) if not a.no_large and rank == 0 else None
+    serving_stats = run_serving(a, dev) if not a.no_serving else None
+    batching_stats = run_batching(a, dev) if not a.no_batching else None
+    extra = None
     if not a.no_extra and rank == 0:
-        extra_stats = run_extra(a, dev, batch)
+        X = core.coulomb_matrix_batch(z, r, off, 23)
+        extra = run_extra(a, dev, batch, X, stream)
 
     if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
         return 0
-    # roofline of the dominant kernel (the emulated trailing update): its algorithm
-    # is 36 bf16 digit-plane products of the lower triangle, 36 * n(n+1) * k flops
-    # per launch; the FP64-equivalent rate (n(n+1)k flops) is reported beside it.
-    import json as _json
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            peaks = _json.load(f)
+            peaks = json.load(f)
     except OSError:
         pass
+    peak = peaks.get("bf16_tflops", 1900.0)
+    # roofline of the dominant kernel (the emulated trailing update): 36 bf16
+    # digit-plane products of the lower triangle, 36 n(n+1) k flops per launch; the
+    # FP64-equivalent rate (n(n+1) k flops) beside it; and the whole mixed
+    # factorisation's digit-plane rate, 36 N^3 / 3 flops over its measured time
     flops = 36.0 * nsy * (nsy + 1) * ksy
     achieved = flops / syrk_s / 1e12
-    peak = peaks.get("bf16_tflops", 1900.0)
+    fact_tflops = 36.0 * ntr ** 3 / 3.0 / stages["factor"] / 1e12
     roofline = {"kernel": "emu_tc_kernel<syrk> (C %dx%d lower -= P P^T, k=%d, 8 digit planes)"
                 % (nsy, nsy, ksy),
                 "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
@@ -579,26 +688,41 @@ def run_ours(a):
                 "algorithmic_bytes": 8.0 * nsy * (nsy + 1) + 8.0 * nsy * ksy + 16.0 * nsy * ksy,
                 "peak_source": "measured bf16 (MEASURED_PEAKS.json)" if peaks else "fallback",
                 "launch_s": syrk_s,
-                "fp64_equivalent_tflops": nsy * (nsy + 1) * ksy / syrk_s / 1e12}
+                "fp64_equivalent_tflops": nsy * (nsy + 1) * ksy / syrk_s / 1e12,
+                "factorisation_tflops": fact_tflops, "factorisation_frac": fact_tflops / peak}
     cpu = None
     if not a.no_cpu:
-        total, parts = cpu_pipeline_sample(batch, a)
+        total, parts, sample = cpu_baseline_sample(batch, a)
         cpu = {"value": total, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-               "sample": cpu_sample_text(a), "stages_s": parts}
-    line = {"metric": METRIC, "value": ms / 1e3 if world == 1 else ms / 1e3, "unit": UNIT,
+               "sample": sample, "stages_s": parts}
+    headline = {"fit_predict_s": ms / 1e3, "e2e_s": e2e_s,
+                "fp64_fit_predict_s": fp64.get("fit_predict_s_median"),
+                "speedup_mixed_vs_fp64": fp64.get("speedup_mixed_vs_fp64"),
+                "alpha_rel_err_vs_fp64_refined": fp64.get("alpha_rel_err_mixed_vs_fp64_refined"),
+                "refine_steps": report.get("outer_iterations"),
+                "fell_back": report.get("fell_back")}
+    if serving_stats:
+        headline.update({"serving_p50_ms": serving_stats["p50_ms"],
+                         "serving_p99_ms": serving_stats["p99_ms"],
+                         "serving_molecules_per_s": serving_stats["molecules_per_s"]})
+    if large:
+        headline.update({"fit60000_gaussian_s": large["gaussian"]["fit_predict_s"],
+                         "fit60000_laplacian_s": large["laplacian"]["fit_predict_s"]})
+    if batching_stats:
+        headline["batch64_graph_s"] = batching_stats["graph_s"]
+    line = {"metric": METRIC, "value": ms / 1e3, "unit": UNIT,
             "n_gpus": world, "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": workload_config(a),
             "e2e": {"value": e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "fits_per_s": replicas.job_throughput(1.0, ms / 1e3, world),
-            "serving": serving_stats,
-            "batching": batching_stats,
-            "other_paths": extra_stats,
             "gpu_launches": launches, "clocks": clocks.summary(), "roofline": roofline,
-            "cpu_baseline": cpu, "stages_s": stages,
-            "train_kernel_matrix_s": kernels_s, "solve_report": rep_m,
-            "fp64_path": fp64}
+            "cpu_baseline": cpu,
+            "fits_per_s": replicas.job_throughput(1.0, ms / 1e3, world),
+            "other_paths": extra, "batching": batching_stats, "large": large,
+            "serving": serving_stats, "stages_s": stages, "solve_report": report,
+            "fp64_path": fp64,
+            "headline": headline}
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

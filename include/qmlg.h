@@ -338,10 +338,15 @@ typedef struct QmlgSolveReport {
 
 typedef struct QmlgRefineOpts {
     int max_outer;          /* refinement steps (default 10) */
-    int max_inner;          /* GMRES iterations per step (default 50) */
-    double tol;             /* stop when |dx|/|x| <= tol (default 1e-14) */
-    double shift;           /* FP32 factor shift; <= 0 picks one from the matrix */
+    int max_inner;          /* not used: each step solves with the factor directly */
+    double tol;             /* stop when |dx|/|x| <= tol (default 1e-15) */
+    double shift;           /* not used: the factor takes no extra diagonal shift */
     int allow_fallback;     /* refactorise in FP64 when refinement stalls (default 1) */
+    int slices;             /* digit planes of the mixed factor's tensor-core products,
+                               4..8 (0 = 8).  Fewer planes give a faster factor with a
+                               larger error; when refinement cannot recover from it (an
+                               ill-conditioned matrix) the solve stalls and takes the
+                               FP64 refactorisation (report->fell_back = 1). */
 } QmlgRefineOpts;
 
 /*

@@ -82,6 +82,9 @@ def _load():
         lib.oracle_residual_dd.argtypes = [_dp, ctypes.c_int, ctypes.c_int64, ctypes.c_double,
                                            _dp, _dp, _dp]
         lib.oracle_residual_dd.restype = None
+        lib.oracle_rows_residual_dd.argtypes = [_dp, ctypes.c_int, ctypes.c_int, ctypes.c_int64,
+                                                _dp, _dp, _dp]
+        lib.oracle_rows_residual_dd.restype = None
         _lib = lib
     return _lib
 
@@ -298,6 +301,19 @@ def residual_dd(A, lam, x, y):
     r = np.empty_like(x)
     _load().oracle_residual_dd(_ptr(A), A.shape[0], A.strides[0] // 8, float(lam), _ptr(x),
                                _ptr(y), _ptr(r))
+    return r
+
+
+def rows_residual_dd(A, x, y):
+    """y - A x for an (m, n) block of rows, with double-double accumulation."""
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    if A.ndim != 2 or x.shape != (A.shape[1],) or y.shape != (A.shape[0],):
+        raise ValueError("A (m, n), x (n,), y (m,)")
+    r = np.empty(A.shape[0])
+    _load().oracle_rows_residual_dd(_ptr(A), A.shape[0], A.shape[1], A.strides[0] // 8, _ptr(x),
+                                    _ptr(y), _ptr(r))
     return r
 
 

@@ -499,3 +499,21 @@ void oracle_residual_dd(const double *A, int n, int64_t lda, double lambda, cons
         r[i] = hi + lo;
     }
 }
+
+/*
+ * r = y - A x for an m x n block of rows (leading dimension lda), every product and
+ * sum carried in double-double and rounded to double at the end: the residual of a
+ * sample of rows of a larger system, for backward-error checks at sizes where the
+ * whole matrix is not copied to the host.
+ */
+void oracle_rows_residual_dd(const double *A, int m, int n, int64_t lda, const double *x,
+                             const double *y, double *r)
+{
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < m; ++i) {
+        const double *row = A + (size_t)i * (size_t)lda;
+        double hi = y[i], lo = 0.0;
+        for (int j = 0; j < n; ++j) dd_add_prod(&hi, &lo, -row[j], x[j]);
+        r[i] = hi + lo;
+    }
+}

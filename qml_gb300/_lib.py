@@ -60,7 +60,8 @@ class QmlgSolveReport(ctypes.Structure):
 
 class QmlgRefineOpts(ctypes.Structure):
     _fields_ = [("max_outer", ctypes.c_int), ("max_inner", ctypes.c_int), ("tol", ctypes.c_double),
-                ("shift", ctypes.c_double), ("allow_fallback", ctypes.c_int)]
+                ("shift", ctypes.c_double), ("allow_fallback", ctypes.c_int),
+                ("slices", ctypes.c_int)]
 
 
 _P = ctypes.c_void_p

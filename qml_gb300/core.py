@@ -367,15 +367,17 @@ def _colmajor(A: torch.Tensor) -> Tuple[torch.Tensor, int]:
 
 def solve(A: torch.Tensor, y: torch.Tensor, lam: float = 0.0, precision: str = "mixed",
           max_outer: int = 10, tol: float = 1e-14, allow_fallback: bool = True,
-          raise_on_info: bool = True):
+          raise_on_info: bool = True, slices: int = 0):
     """Solve (A + lam I) x = y on the GPU.  Returns (x, report dict).
 
     precision "fp64": blocked FP64 Cholesky in place (A's upper triangle in
     column-major terms is overwritten, like dpotrf("U")), then dpotrs and, when
-    max_outer > 0, double-double refinement.  precision "mixed": the same factor
-    with its trailing updates emulated on the bf16 tensor cores, refined in FP64
-    with a double-double residual; falls back to the plain FP64 factor when the
-    refinement stalls.  The other triangle of A is never written.
+    max_outer > 0, refinement with the exactly summed residual.  precision "mixed":
+    the same factor with its trailing updates emulated on the bf16 tensor cores
+    (`slices` digit planes, 4..8, 0 = 8), refined in FP64 with the exact residual;
+    falls back to the plain FP64 factor when the refinement stalls.  The other
+    triangle of A is never written (after a fallback the factorised triangle holds
+    the FP64 factor).
     """
     _require_cuda(A, y)
     if precision not in _PRECISIONS:
@@ -389,7 +391,8 @@ def solve(A: torch.Tensor, y: torch.Tensor, lam: float = 0.0, precision: str = "
     p = _PRECISIONS[precision]
     ws_bytes = lib().qmlg_solve_workspace_size(n, p)
     ws = workspaces.get(ws_bytes, A.device)
-    opts = QmlgRefineOpts(int(max_outer), 50, float(tol), 0.0, 1 if allow_fallback else 0)
+    opts = QmlgRefineOpts(int(max_outer), 0, float(tol), 0.0, 1 if allow_fallback else 0,
+                          int(slices))
     rep = QmlgSolveReport()
     st = lib().qmlg_solve(Acm.data_ptr(), n, lda, y.data_ptr(), x.data_ptr(), float(lam), p,
                           ctypes.byref(opts), ctypes.byref(rep), ws.data_ptr(), ws.numel(),

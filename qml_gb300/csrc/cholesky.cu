@@ -1756,8 +1756,10 @@ extern "C" int qmlg_solve(double *A, int n, int64_t lda, const double *y, double
     }
     if (A == nullptr || y == nullptr || x == nullptr) return QMLG_E_ARG;
     if (ws_bytes < qmlg_solve_workspace_size(n, precision)) return QMLG_E_WORKSPACE;
-    QmlgRefineOpts o{10, 50, 1e-15, 0.0, 1};
+    QmlgRefineOpts o{10, 50, 1e-15, 0.0, 1, 0};
     if (opts) o = *opts;
+    const int slices = o.slices == 0 ? qmlg::kEmuMaxSlices : o.slices;
+    if (slices < 4 || slices > qmlg::kEmuMaxSlices) return QMLG_E_ARG;
 
     cudaStream_t s = qmlg::as_stream(stream);
     qmlg::Workspace ws(workspace, ws_bytes);
@@ -1773,7 +1775,7 @@ extern "C" int qmlg_solve(double *A, int n, int64_t lda, const double *y, double
     if (precision == QMLG_PREC_MIXED) {
         // Emulated-FP64 factor on the tensor cores, in place like the FP64 one.
         qmlg::EmulatedFactor f;
-        st = qmlg::emulated_factor(A, n, lda, lambda, ws, c.d_info, f, s);
+        st = qmlg::emulated_factor(A, n, lda, lambda, ws, c.d_info, f, s, slices);
         if (st != QMLG_OK) return st;
         if ((st = read_info(c, info)) != QMLG_OK) return st;
         if ((st = qmlg::read_device_flag(f.d_err, s)) != QMLG_OK) return st;

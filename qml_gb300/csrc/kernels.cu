@@ -52,6 +52,26 @@ __device__ __forceinline__ void tri_index(int64_t t, int &bi, int &bj)
     bj = (int)(t - r * (r + 1) / 2);
 }
 
+// Maps a linear block id onto a rectangular tile pair: bj (A side, fastest, tj
+// tiles) and bi (B side).  One grid dimension takes up to 2^31 - 1 blocks, where a
+// second one would stop at 65535 tiles (4.19M rows).
+__device__ __forceinline__ void rect_index(int tj, int &bj, int &bi)
+{
+    bj = (int)(blockIdx.x % (unsigned)tj);
+    bi = (int)(blockIdx.x / (unsigned)tj);
+}
+
+// One-dimensional grid over a tile list: tj * ti rectangular tiles, or the
+// tj (tj + 1) / 2 tiles on and below the diagonal; false when the list is longer
+// than one grid dimension takes.
+inline bool tile_list_grid(int tj, int ti, bool symmetric, dim3 &grid)
+{
+    const int64_t t = symmetric ? (int64_t)tj * (tj + 1) / 2 : (int64_t)tj * ti;
+    if (t > 0x7fffffffLL) return false;
+    grid = dim3((unsigned)t);
+    return true;
+}
+
 // Accumulates the 4x4 micro-tile over the feature dimension.
 template <int KIND>
 __device__ __forceinline__ void tile_accumulate(const double *__restrict__ A, int64_t lda, int na,
@@ -139,8 +159,7 @@ kernel_matrix_kernel(const double *__restrict__ A, int64_t lda, int na,
     if (symmetric) {
         tri_index(blockIdx.x, bi, bj);  // bi >= bj: B-tile index >= A-tile index
     } else {
-        bj = blockIdx.x;
-        bi = blockIdx.y;
+        rect_index((na + TJ - 1) / TJ, bj, bi);
     }
     const int j0 = bj * TJ, i0 = bi * TI;
     double acc[4][4];
@@ -206,7 +225,8 @@ predict_partial_kernel(const double *__restrict__ Xtr, int64_t ldtr, int ntr,
     __shared__ double Bs[TK][TI + 1];
     __shared__ double a2s[TJ], b2s[TI];
     __shared__ double red[16][TI + 1];
-    const int bj = blockIdx.x, bi = blockIdx.y;
+    int bj, bi;
+    rect_index((ntr + TJ - 1) / TJ, bj, bi);
     const int j0 = bj * TJ, i0 = bi * TI;
     double acc[4][4];
     tile_accumulate<KIND>(Xtr, ldtr, ntr, Xte, ldte, nte, d, j0, i0, acc, As, Bs, a2s, b2s);
@@ -301,7 +321,8 @@ int kernel_matrix(int kind, const double *A, int64_t lda, int na, const double *
     if (kind == kGauss) ep.s1 = -0.5 / (sigma * sigma);
     else if (kind == kLaplace || kind == kSargan) ep.s1 = -1.0 / sigma;
     const int tj = (int)qmlg::ceil_div(na, TJ), ti = (int)qmlg::ceil_div(nb, TI);
-    dim3 grid = symmetric ? dim3((unsigned)((int64_t)tj * (tj + 1) / 2)) : dim3(tj, ti);
+    dim3 grid;
+    if (!tile_list_grid(tj, ti, symmetric, grid)) return QMLG_E_ARG;
     const int sym = symmetric ? 1 : 0;
     switch (kind) {
     case kGauss: launch_kernel_matrix<kGauss>(grid, s, A, lda, na, B, ldb, nb, d, ep, K, ldk, sym, diag_shift); break;
@@ -404,14 +425,16 @@ extern "C" int qmlg_predict_fused(int kind, const double *Xtrain, int64_t ldtrai
     if (ws_bytes < qmlg_predict_workspace_size(ntrain, ntest)) return QMLG_E_WORKSPACE;
     qmlg::Workspace ws(workspace, ws_bytes);
     const int tj = (int)qmlg::ceil_div(ntrain, TJ), ti = (int)qmlg::ceil_div(ntest, TI);
+    dim3 grid;
+    if (!tile_list_grid(tj, ti, false, grid)) return QMLG_E_ARG;
     double *partial = ws.take<double>((size_t)tj * ntest);
     if (partial == nullptr) return QMLG_E_WORKSPACE;
     const double scale = kind == QMLG_KIND_GAUSSIAN ? -0.5 / (sigma * sigma) : -1.0 / sigma;
     if (kind == QMLG_KIND_GAUSSIAN)
-        { predict_partial_kernel<kGauss><<<dim3(tj, ti), NT, 0, s>>>(
+        { predict_partial_kernel<kGauss><<<grid, NT, 0, s>>>(
             Xtrain, ldtrain, ntrain, Xtest, ldtest, ntest, d, scale, alpha, partial); qmlg::count_launches(1); }
     else
-        { predict_partial_kernel<kLaplace><<<dim3(tj, ti), NT, 0, s>>>(
+        { predict_partial_kernel<kLaplace><<<grid, NT, 0, s>>>(
             Xtrain, ldtrain, ntrain, Xtest, ldtest, ntest, d, scale, alpha, partial); qmlg::count_launches(1); }
     { reduce_partial_kernel<<<(int)qmlg::ceil_div(ntest, 256), 256, 0, s>>>(partial, tj, ntest, yhat); qmlg::count_launches(1); }
     return qmlg::check_launch();
@@ -485,15 +508,17 @@ extern "C" int qmlg_predict_fused_noalloc(int kind, const double *Xtrain, int64_
     }
     const int tj = (int)qmlg::ceil_div(ntrain, TJ), ti = (int)qmlg::ceil_div(ntest, TI);
     if ((size_t)tj * (size_t)ntest > kNoAllocPartials) return QMLG_E_TOO_LARGE;
+    dim3 grid;  // tj * ti <= tj * ntest, far below the one-dimensional grid limit
+    if (!tile_list_grid(tj, ti, false, grid)) return QMLG_E_TOO_LARGE;
     double *partial = nullptr;
     st = noalloc_scratch(&partial);
     if (st != QMLG_OK) return st;
     const double scale = kind == QMLG_KIND_GAUSSIAN ? -0.5 / (sigma * sigma) : -1.0 / sigma;
     if (kind == QMLG_KIND_GAUSSIAN) {
-        predict_partial_kernel<kGauss><<<dim3(tj, ti), NT, 0, s>>>(
+        predict_partial_kernel<kGauss><<<grid, NT, 0, s>>>(
             Xtrain, ldtrain, ntrain, Xtest, ldtest, ntest, d, scale, alpha, partial);
     } else {
-        predict_partial_kernel<kLaplace><<<dim3(tj, ti), NT, 0, s>>>(
+        predict_partial_kernel<kLaplace><<<grid, NT, 0, s>>>(
             Xtrain, ldtrain, ntrain, Xtest, ldtest, ntest, d, scale, alpha, partial);
     }
     qmlg::count_launches(1);
@@ -561,8 +586,7 @@ laplace_fixed_kernel(const long long *__restrict__ A, int na, const long long *_
     if (symmetric) {
         tri_index(blockIdx.x, bi, bj);
     } else {
-        bj = blockIdx.x;
-        bi = blockIdx.y;
+        rect_index((na + TJ - 1) / TJ, bj, bi);
     }
     const int j0 = bj * TJ, i0 = bi * TI;
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
@@ -627,7 +651,8 @@ laplace_fixed_predict_kernel(const long long *__restrict__ A, int na, const long
     long long(*As)[TJ + 1] = reinterpret_cast<long long(*)[TJ + 1]>(smem);
     long long(*Bs)[TI + 1] = reinterpret_cast<long long(*)[TI + 1]>(smem + TK * (TJ + 1));
     double(*red)[TI + 1] = reinterpret_cast<double(*)[TI + 1]>(smem);
-    const int bj = blockIdx.x, bi = blockIdx.y;
+    int bj, bi;
+    rect_index((na + TJ - 1) / TJ, bj, bi);
     const int j0 = bj * TJ, i0 = bi * TI;
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
     long long acc[4][4];
@@ -702,6 +727,9 @@ extern "C" int qmlg_laplacian_kernel_fixed(const double *A, int64_t lda, int na,
     const bool symmetric = (flags & QMLG_KERNEL_SYMMETRIC) != 0;
     if (symmetric && (na != nb || A != B || lda != ldb)) return QMLG_E_ARG;
     if (na == 0 || nb == 0) return QMLG_OK;
+    const int tj = (int)qmlg::ceil_div(na, TJ), ti = (int)qmlg::ceil_div(nb, TI);
+    dim3 grid;
+    if (!tile_list_grid(tj, ti, symmetric, grid)) return QMLG_E_ARG;
     if (ws_bytes < qmlg_laplacian_kernel_fixed_workspace_size(na, nb, d, flags))
         return QMLG_E_WORKSPACE;
     cudaStream_t s = qmlg::as_stream(stream);
@@ -739,8 +767,6 @@ extern "C" int qmlg_laplacian_kernel_fixed(const double *A, int64_t lda, int na,
     to_fixed_kernel<<<blocks((int64_t)na * d), 256, 0, s>>>(A, lda, na, d, scale, qa);
     if (!symmetric) to_fixed_kernel<<<blocks((int64_t)nb * d), 256, 0, s>>>(B, ldb, nb, d, scale, qb);
     qmlg::count_launches(symmetric ? 1 : 2);
-    const int tj = (int)qmlg::ceil_div(na, TJ), ti = (int)qmlg::ceil_div(nb, TI);
-    dim3 grid = symmetric ? dim3((unsigned)((int64_t)tj * (tj + 1) / 2)) : dim3(tj, ti);
     laplace_fixed_kernel<<<grid, NT, 0, s>>>(qa, na, qb, nb, d, inv_scale, -1.0 / sigma, K, ldk,
                                              symmetric ? 1 : 0, diag_shift);
     qmlg::count_launches(1);
@@ -775,6 +801,8 @@ extern "C" int qmlg_predict_laplacian_fixed(const double *Xtrain, int64_t ldtrai
         return QMLG_E_WORKSPACE;
     qmlg::Workspace ws(workspace, ws_bytes);
     const int tj = (int)qmlg::ceil_div(ntrain, TJ), ti = (int)qmlg::ceil_div(ntest, TI);
+    dim3 grid;
+    if (!tile_list_grid(tj, ti, false, grid)) return QMLG_E_ARG;
     double *partial = ws.take<double>((size_t)tj * ntest);
     long long *qa = ws.take<long long>((size_t)ntrain * d);
     long long *qb = ws.take<long long>((size_t)ntest * d);
@@ -808,11 +836,11 @@ extern "C" int qmlg_predict_laplacian_fixed(const double *Xtrain, int64_t ldtrai
         const double scale = std::ldexp(1.0, F), inv_scale = std::ldexp(1.0, -F);
         to_fixed_kernel<<<blocks((int64_t)ntrain * d), 256, 0, s>>>(Xtrain, ldtrain, ntrain, d, scale, qa);
         to_fixed_kernel<<<blocks((int64_t)ntest * d), 256, 0, s>>>(Xtest, ldtest, ntest, d, scale, qb);
-        laplace_fixed_predict_kernel<<<dim3(tj, ti), NT, 0, s>>>(qa, ntrain, qb, ntest, d, inv_scale,
-                                                                 -1.0 / sigma, alpha, partial);
+        laplace_fixed_predict_kernel<<<grid, NT, 0, s>>>(qa, ntrain, qb, ntest, d, inv_scale,
+                                                         -1.0 / sigma, alpha, partial);
         qmlg::count_launches(3);
     } else {
-        predict_partial_kernel<kLaplace><<<dim3(tj, ti), NT, 0, s>>>(
+        predict_partial_kernel<kLaplace><<<grid, NT, 0, s>>>(
             Xtrain, ldtrain, ntrain, Xtest, ldtest, ntest, d, -1.0 / sigma, alpha, partial);
         qmlg::count_launches(1);
     }

@@ -1,6 +1,7 @@
 """Builds the golden fixtures in this folder from the reference's own test data.
 
-Run where the reference tree is mounted (default /root/reference, or pass a path).
+Run where the reference tree is mounted: pass its path, or set QML_REFERENCE_TREE
+(default /root/reference).  Without the tree the script exits with a message.
 Outputs (small .npz files, committed):
   cm_qm7_0101_0110.npz  inputs and expected outputs of the reference's Coulomb-matrix
                         known-answer test (tests/test_representations.py:46-90):
@@ -182,4 +183,8 @@ def more_kernels(here):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    tree = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("QML_REFERENCE_TREE",
+                                                                 "/root/reference")
+    if not os.path.isdir(os.path.join(tree, "tests", "data")):
+        sys.exit("reference tree not found at %s (pass its path or set QML_REFERENCE_TREE)" % tree)
+    main(tree)

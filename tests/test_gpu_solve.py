@@ -246,3 +246,63 @@ def test_mixed_solve_many_panels(cuda, oracle):
                         precision="mixed")
     assert rep["status"] == 0 and rep["fell_back"] == 0, rep
     assert rel(x.cpu().numpy(), xr) <= 1e-8, rep
+
+
+def test_mixed_fallback_refactorises_in_fp64(cuda, oracle, krr_system):
+    # With four digit planes the tensor-core factor carries an error near 2^-28,
+    # far too coarse for cond(K + 1e-8 I) ~ 1e10: refinement stalls (or a pivot
+    # fails) and the solve restores the factorised triangle from the untouched one
+    # and refactorises in FP64.  (fcho_solve.f90:36-42 prints a warning and carries
+    # on after a failed dpotrf; here the FP64 factor takes over.)  The FP64
+    # refinement then meets the same bar against the refined oracle.
+    X, y = krr_system
+    n, lam = 1500, 1e-8
+    K = np.ascontiguousarray(oracle.gaussian_kernel(X[:n], X[:n], 1000.0))
+    xr = oracle.refined_solve(K, y[:n], lam)
+    A = torch.from_numpy(K).to(cuda)
+    x, rep = core.solve(A, torch.from_numpy(y[:n]).to(cuda), lam, precision="mixed", slices=4)
+    assert rep["fell_back"] == 1 and rep["precision_used"] == 0, rep
+    assert rep["info"] == 0 and rep["status"] == 0, rep
+    assert rel(x.cpu().numpy(), xr) <= 1e-8, rep
+    F = A.cpu().numpy()
+    # the other triangle (row-major strictly upper = column-major strictly lower) is K
+    assert np.array_equal(np.triu(F, 1), np.triu(K, 1))
+    # the factorised triangle holds an FP64 factor of K + lam I: U^T U = K + lam I to
+    # FP64 backward-error level (the restore fed the FP64 factor the original K)
+    L = np.tril(F)
+    berr = np.linalg.norm(L @ L.T - (K + lam * np.eye(n))) / np.linalg.norm(K)
+    assert berr <= 1e-14, berr
+
+
+def test_mixed_fewer_planes_recover_when_well_conditioned(cuda, oracle, krr_system):
+    # six planes at lambda = 1e-4 (cond ~ 1e7): refinement recovers, no fallback
+    X, y = krr_system
+    n, lam = 1500, 1e-4
+    K = np.ascontiguousarray(oracle.gaussian_kernel(X[:n], X[:n], 1000.0))
+    xr = oracle.refined_solve(K, y[:n], lam)
+    x, rep = core.solve(torch.from_numpy(K).to(cuda), torch.from_numpy(y[:n]).to(cuda), lam,
+                        precision="mixed", slices=6)
+    assert rep["fell_back"] == 0 and rep["precision_used"] == 1 and rep["status"] == 0, rep
+    assert rel(x.cpu().numpy(), xr) <= 1e-8, rep
+
+
+def test_mixed_solve_not_positive_definite_falls_back_to_lapack_info(cuda):
+    from scipy.linalg import lapack
+    rng = np.random.default_rng(2)
+    M = rng.normal(size=(700, 700))
+    S = M @ M.T + np.eye(700)
+    S[600, 600] = -5.0
+    _, info = lapack.dpotrf(np.asfortranarray(S), lower=0)
+    assert info > 0
+    x, rep = core.solve(torch.from_numpy(S).to(cuda), torch.ones(700, dtype=torch.float64,
+                        device=cuda), 0.0, precision="mixed", raise_on_info=False)
+    assert rep["status"] == info and rep["info"] == info and rep["fell_back"] == 1, rep
+    assert torch.isnan(x).all()
+
+
+def test_solve_rejects_bad_plane_count(cuda):
+    from qml_gb300._lib import QmlgError
+    K = torch.eye(8, dtype=torch.float64, device=cuda)
+    with pytest.raises(QmlgError):
+        core.solve(K, torch.ones(8, dtype=torch.float64, device=cuda), 0.0, precision="mixed",
+                   slices=3)

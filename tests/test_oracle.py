@@ -7,7 +7,9 @@ import pytest
 from conftest import load_golden, more_kernel_inputs
 from qml_gb300.synthetic import generate_molecules
 
-REF = "/root/reference"
+# The reference's source tree (read-only; its QM7 files feed the end-to-end check
+# below, which is skipped where the tree is not mounted).
+REF = os.environ.get("QML_REFERENCE_TREE", "/root/reference")
 
 
 def test_cm_oracle_matches_reference_fixture(oracle):
@@ -232,3 +234,16 @@ def test_oracle_krr_cmat_reference_accuracy(oracle):
     Ks = oracle.laplacian_kernel(X, Xs, sigma)
     mae = np.mean(np.abs(Ys - Ks.T @ alpha))
     assert mae < 6.0
+
+
+def test_rows_residual_dd_matches_square_residual(oracle):
+    # the rectangular double-double residual equals the square one on the same rows
+    rng = np.random.default_rng(4)
+    A = rng.normal(size=(60, 60))
+    A = A + A.T
+    x = rng.normal(size=60)
+    y = rng.normal(size=60)
+    full = oracle.residual_dd(A, 0.0, x, y)
+    rows = np.array([0, 7, 33, 59])
+    part = oracle.rows_residual_dd(A[rows], x, y[rows])
+    assert np.array_equal(part, full[rows])

@@ -59,12 +59,14 @@ def test_noalloc_matches_workspace_version_twice(kind):
         assert np.max(np.abs(y_na - y_ws)) <= TOL * scale
 
 
-def test_noalloc_rejects_oversized_problem():
+@pytest.mark.parametrize("ntr,nte", [(64 * 4097, 1025),  # 4097 * 1025 partial sums > 4194304
+                                      (1, 4194305)])      # one test molecule past the limit
+def test_noalloc_rejects_oversized_problem(ntr, nte):
     if not torch.cuda.is_available():
         pytest.fail("GPU test run without a CUDA device")
     lib = _lib.load()
     dev = torch.device("cuda")
-    ntr, nte, d = 64 * 4097, 1025, 1  # 4097 * 1025 partial sums > 4194304
+    d = 1
     Xtr = torch.zeros((ntr, d), dtype=torch.float64, device=dev)
     Xte = torch.zeros((nte, d), dtype=torch.float64, device=dev)
     alpha = torch.zeros(ntr, dtype=torch.float64, device=dev)
@@ -73,3 +75,27 @@ def test_noalloc_rejects_oversized_problem():
                                         Xte.data_ptr(), d, nte, d, 1.0, alpha.data_ptr(),
                                         y.data_ptr(), torch.cuda.current_stream().cuda_stream)
     assert st == _lib.QMLG_E_TOO_LARGE
+
+
+def test_noalloc_at_the_limit_with_65536_test_tiles():
+    # one training row and 4194304 test rows: exactly the array's capacity, and
+    # 65536 tiles of test rows (one more than a second grid dimension could hold)
+    if not torch.cuda.is_available():
+        pytest.fail("GPU test run without a CUDA device")
+    lib = _lib.load()
+    dev = torch.device("cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    gen = torch.Generator(device=dev).manual_seed(5)
+    ntr, nte, d = 1, 4194304, 2
+    Xtr = torch.rand((ntr, d), dtype=torch.float64, device=dev, generator=gen)
+    Xte = torch.rand((nte, d), dtype=torch.float64, device=dev, generator=gen)
+    alpha = torch.full((ntr,), 0.75, dtype=torch.float64, device=dev)
+    for kind in (_lib.QMLG_KIND_GAUSSIAN, _lib.QMLG_KIND_LAPLACIAN):
+        y_ws, y_na = _call_both(lib, kind, Xtr, Xte, 0.5, alpha, stream)
+        assert np.all(np.isfinite(y_na))
+        assert np.max(np.abs(y_na - y_ws)) <= TOL * np.max(np.abs(y_ws))
+        # and against the closed form of the single-row sum
+        diff = (Xte - Xtr).cpu().numpy()
+        ref = 0.75 * (np.exp(-0.5 / 0.25 * np.sum(diff * diff, axis=1))
+                      if kind == _lib.QMLG_KIND_GAUSSIAN else np.exp(-np.sum(np.abs(diff), axis=1) / 0.5))
+        assert np.max(np.abs(y_na - ref)) <= 1e-12
