@@ -228,6 +228,20 @@ int qmlg_laplacian_kernel_fixed(const double *A, int64_t lda, int na, const doub
                                 void *stream);
 
 /*
+ * Capture-safe qmlg_laplacian_kernel_fixed (replaces flaplacian_kernel,
+ * qml/fkernels.f90:374-400, in batched and graph-recorded fits): no host
+ * synchronisation and no host decision.  The fixed-point grid and its 1e-12 bound
+ * are decided on the device; when the bound fails, the FP64 kernel (launched beside
+ * the fixed-point one, and returning at once otherwise) writes K and 8 is ORed into
+ * the caller's device int *d_flag (may be NULL).  K is always written.  Same layout,
+ * flags and workspace size as qmlg_laplacian_kernel_fixed.
+ */
+int qmlg_laplacian_kernel_fixed_async(const double *A, int64_t lda, int na, const double *B,
+                                      int64_t ldb, int nb, int d, double sigma, double *K,
+                                      int64_t ldk, int flags, double diag_shift, int *d_flag,
+                                      void *workspace, size_t ws_bytes, void *stream);
+
+/*
  * Capture-safe qmlg_gaussian_kernel_emulated: no host synchronisation (so it can
  * be recorded into a CUDA graph); always 8 digit planes; the 1e-12 bound is
  * checked on the device and a failure ORs 8 into the caller's device int
@@ -276,6 +290,20 @@ int qmlg_predict_laplacian_fixed(const double *Xtrain, int64_t ldtrain, int ntra
                                  const double *Xtest, int64_t ldtest, int ntest, int d,
                                  double sigma, const double *alpha, double *yhat,
                                  void *workspace, size_t ws_bytes, void *stream);
+
+/*
+ * qmlg_predict_laplacian_fixed without any host synchronisation, for serving loops
+ * (the np.dot(Ks.T, alpha) of tests/test_energy_krr_cmat.py:109 with the Laplacian
+ * Ks of qml/kernels.py:36-63): the grid is decided on the device; when its bound
+ * fails the FP64 fused kernel (launched beside the fixed-point one) writes yhat and
+ * 8 is ORed into *d_flag (may be NULL).  yhat is always written.  Same workspace
+ * size as qmlg_predict_laplacian_fixed.
+ */
+int qmlg_predict_laplacian_fixed_async(const double *Xtrain, int64_t ldtrain, int ntrain,
+                                       const double *Xtest, int64_t ldtest, int ntest, int d,
+                                       double sigma, const double *alpha, double *yhat,
+                                       int *d_flag, void *workspace, size_t ws_bytes,
+                                       void *stream);
 
 /*
  * qmlg_predict_fused without a workspace, for callers that cannot allocate device

@@ -126,6 +126,10 @@ SIGNATURES = {
     "qmlg_residual_dd": (_I, [_P, _I, _I64, _P, _D, _P, _P, _P, _P, _SZ, _P]),
     "qmlg_predict_laplacian_fixed_workspace_size": (_SZ, [_I, _I, _I]),
     "qmlg_predict_laplacian_fixed": (_I, [_P, _I64, _I, _P, _I64, _I, _I, _D, _P, _P, _P, _SZ, _P]),
+    "qmlg_predict_laplacian_fixed_async": (_I, [_P, _I64, _I, _P, _I64, _I, _I, _D, _P, _P, _P, _P,
+                                                _SZ, _P]),
+    "qmlg_laplacian_kernel_fixed_async": (_I, [_P, _I64, _I, _P, _I64, _I, _I, _D, _P, _I64, _I,
+                                               _D, _P, _P, _SZ, _P]),
     "qmlg_selftest_wait_timeout_workspace_size": (_SZ, []),
     "qmlg_selftest_wait_timeout": (_I, [_P, _SZ, _P]),
 }

@@ -3,9 +3,10 @@
 Learning curves and sigma x lambda grids are many independent fits of uneven size.
 BatchedKRR lays out one kernel matrix, workspace and solution per fit, then records
 all of them into a single CUDA graph.  The fits are spread over several streams
-forked from the capture stream.  Each fit is a capture-safe tensor-core Gaussian
-kernel (qmlg_gaussian_kernel_emulated_async) followed by the capture-safe mixed
-solve (qmlg_solve_async) with a fixed number of double-double refinement steps.
+forked from the capture stream.  Each fit is a capture-safe kernel matrix (the
+tensor-core Gaussian, qmlg_gaussian_kernel_emulated_async, or the fixed-point
+Laplacian, qmlg_laplacian_kernel_fixed_async) followed by the capture-safe mixed
+solve (qmlg_solve_async) with a fixed number of exact-residual refinement steps.
 Replaying the graph reruns every fit with one host call; the host checks the
 per-fit status words afterwards.
 
@@ -34,6 +35,7 @@ class Problem:
     y: torch.Tensor          # (n,) float64 CUDA
     sigma: float
     lam: float
+    kernel: str = "gaussian"  # or "laplacian"
 
 
 class BatchedKRR:
@@ -51,8 +53,12 @@ class BatchedKRR:
             n, d = p.X.shape
             if p.X.dtype != torch.float64 or p.X.stride(1) != 1 or p.y.shape != (n,):
                 raise ValueError("X must be (n, d) row-major float64 and y (n,)")
-            ws_bytes = max(lib.qmlg_gaussian_kernel_emulated_workspace_size(
-                n, n, d, _lib.QMLG_KERNEL_SYMMETRIC), lib.qmlg_solve_async_workspace_size(n))
+            if p.kernel not in ("gaussian", "laplacian"):
+                raise ValueError("unknown kernel %r" % (p.kernel,))
+            size_fn = (lib.qmlg_gaussian_kernel_emulated_workspace_size if p.kernel == "gaussian"
+                       else lib.qmlg_laplacian_kernel_fixed_workspace_size)
+            ws_bytes = max(size_fn(n, n, d, _lib.QMLG_KERNEL_SYMMETRIC),
+                           lib.qmlg_solve_async_workspace_size(n))
             self.K.append(torch.empty((n, n), dtype=torch.float64, device=self.device))
             self.x.append(torch.empty(n, dtype=torch.float64, device=self.device))
             self.ws.append(torch.empty(ws_bytes, dtype=torch.uint8, device=self.device))
@@ -76,10 +82,12 @@ class BatchedKRR:
         s = torch.cuda.current_stream(self.device).cuda_stream
         K = self.K[i]
         self.flag[i].zero_()
-        _lib.check(lib.qmlg_gaussian_kernel_emulated_async(
-            p.X.data_ptr(), p.X.stride(0), n, p.X.data_ptr(), p.X.stride(0), n, d, float(p.sigma),
-            K.data_ptr(), n, _lib.QMLG_KERNEL_SYMMETRIC, 0.0, self.flag[i].data_ptr(),
-            self.ws[i].data_ptr(), self.ws[i].numel(), s), "qmlg_gaussian_kernel_emulated_async")
+        fn, name = ((lib.qmlg_gaussian_kernel_emulated_async, "qmlg_gaussian_kernel_emulated_async")
+                    if p.kernel == "gaussian" else
+                    (lib.qmlg_laplacian_kernel_fixed_async, "qmlg_laplacian_kernel_fixed_async"))
+        _lib.check(fn(p.X.data_ptr(), p.X.stride(0), n, p.X.data_ptr(), p.X.stride(0), n, d,
+                      float(p.sigma), K.data_ptr(), n, _lib.QMLG_KERNEL_SYMMETRIC, 0.0,
+                      self.flag[i].data_ptr(), self.ws[i].data_ptr(), self.ws[i].numel(), s), name)
         _lib.check(lib.qmlg_solve_async(
             K.data_ptr(), n, n, p.y.data_ptr(), self.x[i].data_ptr(), float(p.lam),
             self.refine_steps, self.status[i].data_ptr(), self.corr[i].data_ptr(),
@@ -131,23 +139,32 @@ class BatchedKRR:
 
     # ------------------------------------------------------------- results --
     def results(self):
-        """(alpha list, report list) after the work has completed."""
+        """(alpha list, report list) after the work has completed.  "flags" nonzero
+        means the fit needs a rerun (a bounded wait gave up, or the Gaussian
+        tensor-core bound failed); "kernel_path" says which kernel formed K (a
+        Laplacian whose fixed-point bound failed was formed by the FP64 kernel in
+        the same graph, which is not an error)."""
         torch.cuda.synchronize(self.device)
         reports = []
-        for i in range(len(self.problems)):
+        for i, p in enumerate(self.problems):
             st = self.status[i].cpu().tolist()
             fl = int(self.flag[i].item())
             c = self.corr[i].cpu().tolist()
-            reports.append({"info": st[0], "flags": st[1] | fl,
+            if p.kernel == "laplacian":
+                path = "fp64" if fl & 8 else "fixed"
+                fl &= ~8
+            else:
+                path = "tensor"
+            reports.append({"info": st[0], "flags": st[1] | fl, "kernel_path": path,
                             "last_correction": (c[0] ** 0.5) / max(c[1] ** 0.5, 1e-300)})
         return self.x, reports
 
     # ------------------------------------------------------------ autotuning --
     def autotune(self, candidates=None, reps: int = 2) -> dict:
         """Time graph replays for each scheduling choice and keep the fastest.
-        Cached per (device name, sorted problem sizes)."""
+        Cached per (device name, sorted problem sizes and kernels)."""
         key = (torch.cuda.get_device_name(self.device),
-               tuple(sorted(p.X.shape[0] for p in self.problems)))
+               tuple(sorted((p.X.shape[0], p.kernel) for p in self.problems)))
         if key in _TUNED:
             self.config = dict(_TUNED[key])
             self.graph = None

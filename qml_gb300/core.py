@@ -336,6 +336,29 @@ def predict_async(Xtrain: torch.Tensor, Xtest: torch.Tensor, sigma: float, alpha
     return out
 
 
+def predict_laplacian_async(Xtrain: torch.Tensor, Xtest: torch.Tensor, sigma: float,
+                            alpha: torch.Tensor, flag: Optional[torch.Tensor] = None,
+                            out: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """Laplacian prediction with fixed-point L1 sums and no host synchronisation
+    (qmlg_predict_laplacian_fixed_async).  The result is always complete; flag (a
+    zeroed int32 CUDA tensor, optional) receives 8 when the FP64 kernel produced it
+    because the fixed-point bound was not met."""
+    _require_cuda(Xtrain, Xtest, alpha)
+    Xtrain, ldtr = _rows(Xtrain)
+    Xtest, ldte = _rows(Xtest)
+    alpha = alpha.contiguous()
+    ntr, nte, d = Xtrain.shape[0], Xtest.shape[0], Xtrain.shape[1]
+    if out is None:
+        out = torch.empty(nte, dtype=torch.float64, device=Xtrain.device)
+    ws_bytes = lib().qmlg_predict_laplacian_fixed_workspace_size(ntr, nte, d)
+    ws = workspaces.get(ws_bytes, Xtrain.device)
+    check(lib().qmlg_predict_laplacian_fixed_async(
+        Xtrain.data_ptr(), ldtr, ntr, Xtest.data_ptr(), ldte, nte, d, float(sigma),
+        alpha.data_ptr(), out.data_ptr(), flag.data_ptr() if flag is not None else None,
+        ws.data_ptr(), ws.numel(), _stream(Xtrain.device)), "qmlg_predict_laplacian_fixed_async")
+    return out
+
+
 def predict_gemv(Ks: torch.Tensor, alpha: torch.Tensor) -> torch.Tensor:
     """yhat = Ks^T alpha for a Fortran-ordered Ks (ntrain, ntest) (np.dot(Ks.T, alpha))."""
     _require_cuda(Ks, alpha)

@@ -146,8 +146,11 @@ __global__ void __launch_bounds__(NT)
 kernel_matrix_kernel(const double *__restrict__ A, int64_t lda, int na,
                      const double *__restrict__ B, int64_t ldb, int nb, int d,
                      EpiParams ep, double *__restrict__ K, int64_t ldk, int symmetric,
-                     double diag_shift)
+                     double diag_shift, const int *__restrict__ skip)
 {
+    // skip (may be null): *skip != 0 means another kernel of the same launch
+    // sequence writes K (the fixed-point Laplacian when its grid is fine enough)
+    if (skip != nullptr && *skip != 0) return;
     // operand chunks during accumulation, the output tile (for the mirror) after
     __shared__ double smem[TI * (TJ + 1)];
     __shared__ double a2s[TJ], b2s[TI];
@@ -219,8 +222,9 @@ __global__ void __launch_bounds__(NT)
 predict_partial_kernel(const double *__restrict__ Xtr, int64_t ldtr, int ntr,
                        const double *__restrict__ Xte, int64_t ldte, int nte, int d,
                        double scale, const double *__restrict__ alpha,
-                       double *__restrict__ partial)
+                       double *__restrict__ partial, const int *__restrict__ skip)
 {
+    if (skip != nullptr && *skip != 0) return;  // as in kernel_matrix_kernel
     __shared__ double As[TK][TJ + 1];
     __shared__ double Bs[TK][TI + 1];
     __shared__ double a2s[TJ], b2s[TI];
@@ -302,7 +306,7 @@ void launch_kernel_matrix(dim3 grid, cudaStream_t s, const double *A, int64_t ld
                           double *K, int64_t ldk, int symmetric, double diag_shift)
 {
     kernel_matrix_kernel<KIND><<<grid, NT, 0, s>>>(A, lda, na, B, ldb, nb, d, ep, K, ldk, symmetric,
-                                                   diag_shift);
+                                                   diag_shift, nullptr);
     qmlg::count_launches(1);
 }
 
@@ -432,10 +436,10 @@ extern "C" int qmlg_predict_fused(int kind, const double *Xtrain, int64_t ldtrai
     const double scale = kind == QMLG_KIND_GAUSSIAN ? -0.5 / (sigma * sigma) : -1.0 / sigma;
     if (kind == QMLG_KIND_GAUSSIAN)
         { predict_partial_kernel<kGauss><<<grid, NT, 0, s>>>(
-            Xtrain, ldtrain, ntrain, Xtest, ldtest, ntest, d, scale, alpha, partial); qmlg::count_launches(1); }
+            Xtrain, ldtrain, ntrain, Xtest, ldtest, ntest, d, scale, alpha, partial, nullptr); qmlg::count_launches(1); }
     else
         { predict_partial_kernel<kLaplace><<<grid, NT, 0, s>>>(
-            Xtrain, ldtrain, ntrain, Xtest, ldtest, ntest, d, scale, alpha, partial); qmlg::count_launches(1); }
+            Xtrain, ldtrain, ntrain, Xtest, ldtest, ntest, d, scale, alpha, partial, nullptr); qmlg::count_launches(1); }
     { reduce_partial_kernel<<<(int)qmlg::ceil_div(ntest, 256), 256, 0, s>>>(partial, tj, ntest, yhat); qmlg::count_launches(1); }
     return qmlg::check_launch();
 }
@@ -516,10 +520,10 @@ extern "C" int qmlg_predict_fused_noalloc(int kind, const double *Xtrain, int64_
     const double scale = kind == QMLG_KIND_GAUSSIAN ? -0.5 / (sigma * sigma) : -1.0 / sigma;
     if (kind == QMLG_KIND_GAUSSIAN) {
         predict_partial_kernel<kGauss><<<grid, NT, 0, s>>>(
-            Xtrain, ldtrain, ntrain, Xtest, ldtest, ntest, d, scale, alpha, partial);
+            Xtrain, ldtrain, ntrain, Xtest, ldtest, ntest, d, scale, alpha, partial, nullptr);
     } else {
         predict_partial_kernel<kLaplace><<<grid, NT, 0, s>>>(
-            Xtrain, ldtrain, ntrain, Xtest, ldtest, ntest, d, scale, alpha, partial);
+            Xtrain, ldtrain, ntrain, Xtest, ldtest, ntest, d, scale, alpha, partial, nullptr);
     }
     qmlg::count_launches(1);
     reduce_partial_kernel<<<(int)qmlg::ceil_div(ntest, 256), 256, 0, s>>>(partial, tj, ntest, yhat);
@@ -559,9 +563,46 @@ __global__ void max_abs_rows_kernel(const double *__restrict__ X, int64_t ldx, i
     if ((threadIdx.x & 31) == 0) atomicMax(out, m);
 }
 
-__global__ void to_fixed_kernel(const double *__restrict__ X, int64_t ldx, int rows, int cols,
-                                double scale, long long *__restrict__ Q)
+// Fixed-point grid decided on the device, for the entry points that take no host
+// decision: the same rule as the host code below, ok = 0 when the bound fails.
+struct FixedPlan {
+    double scale, inv_scale;
+    int ok, pad;
+};
+
+// plan->{scale, inv_scale, ok} from the largest |x| of the operands (the bits in
+// maxbits[0 .. nmax-1], as max_abs_rows_kernel leaves them); a failed bound ORs 8
+// into *flag (may be null).
+__global__ void fixed_plan_kernel(const unsigned long long *__restrict__ maxbits, int nmax, int d,
+                                  double sigma, FixedPlan *__restrict__ plan, int *__restrict__ flag)
 {
+    double m = 0.0;
+    for (int k = 0; k < nmax; ++k) m = fmax(m, __longlong_as_double((long long)maxbits[k]));
+    bool ok = isfinite(m);
+    int F = 0;
+    if (ok) {
+        int em = 0, ed = 0;
+        if (m > 0.0) frexp(m, &em);
+        frexp((double)(2 * (long long)(d < 1 ? 1 : d)), &ed);
+        F = min(62 - ed - em, 1000);
+        ok = ldexp((double)d, -F) / sigma <= 0.5e-12;
+    }
+    plan->scale = ok ? ldexp(1.0, F) : 0.0;
+    plan->inv_scale = ok ? ldexp(1.0, -F) : 0.0;
+    plan->ok = ok ? 1 : 0;
+    if (!ok && flag != nullptr) atomicOr(flag, 8);
+}
+
+// Q = round(X * scale); with a plan the scale is the plan's, and nothing is done
+// when the plan failed.
+__global__ void to_fixed_kernel(const double *__restrict__ X, int64_t ldx, int rows, int cols,
+                                double scale, long long *__restrict__ Q,
+                                const FixedPlan *__restrict__ plan)
+{
+    if (plan != nullptr) {
+        if (!plan->ok) return;
+        scale = plan->scale;
+    }
     const int64_t total = (int64_t)rows * cols;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
@@ -575,8 +616,13 @@ __device__ __forceinline__ long long iabs64(long long v) { return v < 0 ? -v : v
 __global__ void __launch_bounds__(NT)
 laplace_fixed_kernel(const long long *__restrict__ A, int na, const long long *__restrict__ B,
                      int nb, int d, double inv_scale, double neg_inv_sigma,
-                     double *__restrict__ K, int64_t ldk, int symmetric, double diag_shift)
+                     double *__restrict__ K, int64_t ldk, int symmetric, double diag_shift,
+                     const FixedPlan *__restrict__ plan)
 {
+    if (plan != nullptr) {  // the device-side grid: nothing to do when it failed
+        if (!plan->ok) return;
+        inv_scale = plan->inv_scale;
+    }
     // operand chunks during the sums, the output tile (for the mirror) after
     __shared__ double smem[TI * (TJ + 1)];
     long long(*As)[TJ + 1] = reinterpret_cast<long long(*)[TJ + 1]>(smem);
@@ -645,8 +691,13 @@ laplace_fixed_kernel(const long long *__restrict__ A, int na, const long long *_
 __global__ void __launch_bounds__(NT)
 laplace_fixed_predict_kernel(const long long *__restrict__ A, int na, const long long *__restrict__ B,
                              int nb, int d, double inv_scale, double neg_inv_sigma,
-                             const double *__restrict__ alpha, double *__restrict__ partial)
+                             const double *__restrict__ alpha, double *__restrict__ partial,
+                             const FixedPlan *__restrict__ plan)
 {
+    if (plan != nullptr) {
+        if (!plan->ok) return;
+        inv_scale = plan->inv_scale;
+    }
     __shared__ double smem[TI * (TJ + 1)];
     long long(*As)[TJ + 1] = reinterpret_cast<long long(*)[TJ + 1]>(smem);
     long long(*Bs)[TI + 1] = reinterpret_cast<long long(*)[TI + 1]>(smem + TK * (TJ + 1));
@@ -713,6 +764,7 @@ extern "C" size_t qmlg_laplacian_kernel_fixed_workspace_size(int na, int nb, int
     p.add<long long>((size_t)na * d);
     if (!(flags & QMLG_KERNEL_SYMMETRIC)) p.add<long long>((size_t)nb * d);
     p.add<unsigned long long>(2);
+    p.add<FixedPlan>(1);
     return p.total();
 }
 
@@ -764,11 +816,12 @@ extern "C" int qmlg_laplacian_kernel_fixed(const double *A, int64_t lda, int na,
         return qmlg_laplacian_kernel(A, lda, na, B, ldb, nb, d, sigma, K, ldk, flags, diag_shift,
                                      stream);
     const double scale = std::ldexp(1.0, F), inv_scale = std::ldexp(1.0, -F);
-    to_fixed_kernel<<<blocks((int64_t)na * d), 256, 0, s>>>(A, lda, na, d, scale, qa);
-    if (!symmetric) to_fixed_kernel<<<blocks((int64_t)nb * d), 256, 0, s>>>(B, ldb, nb, d, scale, qb);
+    to_fixed_kernel<<<blocks((int64_t)na * d), 256, 0, s>>>(A, lda, na, d, scale, qa, nullptr);
+    if (!symmetric)
+        to_fixed_kernel<<<blocks((int64_t)nb * d), 256, 0, s>>>(B, ldb, nb, d, scale, qb, nullptr);
     qmlg::count_launches(symmetric ? 1 : 2);
     laplace_fixed_kernel<<<grid, NT, 0, s>>>(qa, na, qb, nb, d, inv_scale, -1.0 / sigma, K, ldk,
-                                             symmetric ? 1 : 0, diag_shift);
+                                             symmetric ? 1 : 0, diag_shift, nullptr);
     qmlg::count_launches(1);
     return qmlg::check_launch();
 }
@@ -780,6 +833,7 @@ extern "C" size_t qmlg_predict_laplacian_fixed_workspace_size(int ntrain, int nt
     p.add<long long>((size_t)ntrain * d);
     p.add<long long>((size_t)ntest * d);
     p.add<unsigned long long>(2);
+    p.add<FixedPlan>(1);
     return p.total();
 }
 
@@ -834,16 +888,120 @@ extern "C" int qmlg_predict_laplacian_fixed(const double *Xtrain, int64_t ldtrai
     }
     if (fixed) {
         const double scale = std::ldexp(1.0, F), inv_scale = std::ldexp(1.0, -F);
-        to_fixed_kernel<<<blocks((int64_t)ntrain * d), 256, 0, s>>>(Xtrain, ldtrain, ntrain, d, scale, qa);
-        to_fixed_kernel<<<blocks((int64_t)ntest * d), 256, 0, s>>>(Xtest, ldtest, ntest, d, scale, qb);
+        to_fixed_kernel<<<blocks((int64_t)ntrain * d), 256, 0, s>>>(Xtrain, ldtrain, ntrain, d,
+                                                                    scale, qa, nullptr);
+        to_fixed_kernel<<<blocks((int64_t)ntest * d), 256, 0, s>>>(Xtest, ldtest, ntest, d, scale,
+                                                                   qb, nullptr);
         laplace_fixed_predict_kernel<<<grid, NT, 0, s>>>(qa, ntrain, qb, ntest, d, inv_scale,
-                                                         -1.0 / sigma, alpha, partial);
+                                                         -1.0 / sigma, alpha, partial, nullptr);
         qmlg::count_launches(3);
     } else {
         predict_partial_kernel<kLaplace><<<grid, NT, 0, s>>>(
-            Xtrain, ldtrain, ntrain, Xtest, ldtest, ntest, d, -1.0 / sigma, alpha, partial);
+            Xtrain, ldtrain, ntrain, Xtest, ldtest, ntest, d, -1.0 / sigma, alpha, partial, nullptr);
         qmlg::count_launches(1);
     }
     { reduce_partial_kernel<<<(int)qmlg::ceil_div(ntest, 256), 256, 0, s>>>(partial, tj, ntest, yhat); qmlg::count_launches(1); }
+    return qmlg::check_launch();
+}
+
+// ---------------------------------------------------------------------------
+// Capture-safe fixed-point Laplacian entry points.
+//
+// They take no host decision and read nothing back, so they can be recorded into a
+// CUDA graph and issued by serving threads that keep several streams busy.  The
+// fixed-point grid is decided on the device by the host rule above
+// (fixed_plan_kernel).  The FP64 kernel is launched beside the fixed-point one:
+// whichever of the two the plan does not select returns at once, so the result is
+// always written, and a failed bound ORs 8 into *d_flag (may be null) to record
+// that the FP64 kernel produced it.
+// ---------------------------------------------------------------------------
+
+extern "C" int qmlg_laplacian_kernel_fixed_async(const double *A, int64_t lda, int na,
+                                                 const double *B, int64_t ldb, int nb, int d,
+                                                 double sigma, double *K, int64_t ldk, int flags,
+                                                 double diag_shift, int *d_flag, void *workspace,
+                                                 size_t ws_bytes, void *stream)
+{
+    int st = check_common(A, lda, na, B, ldb, nb, d, sigma);
+    if (st != QMLG_OK) return st;
+    if (K == nullptr || ldk < na) return QMLG_E_ARG;
+    const bool symmetric = (flags & QMLG_KERNEL_SYMMETRIC) != 0;
+    if (symmetric && (na != nb || A != B || lda != ldb)) return QMLG_E_ARG;
+    if (na == 0 || nb == 0) return QMLG_OK;
+    const int tj = (int)qmlg::ceil_div(na, TJ), ti = (int)qmlg::ceil_div(nb, TI);
+    dim3 grid;
+    if (!tile_list_grid(tj, ti, symmetric, grid)) return QMLG_E_ARG;
+    if (ws_bytes < qmlg_laplacian_kernel_fixed_workspace_size(na, nb, d, flags))
+        return QMLG_E_WORKSPACE;
+    cudaStream_t s = qmlg::as_stream(stream);
+    qmlg::Workspace ws(workspace, ws_bytes);
+    long long *qa = ws.take<long long>((size_t)na * d);
+    long long *qb = symmetric ? qa : ws.take<long long>((size_t)nb * d);
+    unsigned long long *mx = ws.take<unsigned long long>(2);
+    FixedPlan *plan = ws.take<FixedPlan>(1);
+    if (qa == nullptr || qb == nullptr || mx == nullptr || plan == nullptr) return QMLG_E_WORKSPACE;
+    cudaError_t e = cudaMemsetAsync(mx, 0, 2 * sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+    auto blocks = [](int64_t total) { return (int)std::min<int64_t>(qmlg::ceil_div(total, 256), 2432); };
+    max_abs_rows_kernel<<<blocks((int64_t)na * d), 256, 0, s>>>(A, lda, na, d, mx);
+    if (!symmetric) max_abs_rows_kernel<<<blocks((int64_t)nb * d), 256, 0, s>>>(B, ldb, nb, d, mx + 1);
+    fixed_plan_kernel<<<1, 1, 0, s>>>(mx, symmetric ? 1 : 2, d, sigma, plan, d_flag);
+    to_fixed_kernel<<<blocks((int64_t)na * d), 256, 0, s>>>(A, lda, na, d, 0.0, qa, plan);
+    if (!symmetric)
+        to_fixed_kernel<<<blocks((int64_t)nb * d), 256, 0, s>>>(B, ldb, nb, d, 0.0, qb, plan);
+    laplace_fixed_kernel<<<grid, NT, 0, s>>>(qa, na, qb, nb, d, 0.0, -1.0 / sigma, K, ldk,
+                                             symmetric ? 1 : 0, diag_shift, plan);
+    EpiParams ep;
+    ep.s1 = -1.0 / sigma;
+    kernel_matrix_kernel<kLaplace><<<grid, NT, 0, s>>>(A, lda, na, B, ldb, nb, d, ep, K, ldk,
+                                                       symmetric ? 1 : 0, diag_shift, &plan->ok);
+    qmlg::count_launches(symmetric ? 5 : 7);
+    return qmlg::check_launch();
+}
+
+extern "C" int qmlg_predict_laplacian_fixed_async(const double *Xtrain, int64_t ldtrain, int ntrain,
+                                                  const double *Xtest, int64_t ldtest, int ntest,
+                                                  int d, double sigma, const double *alpha,
+                                                  double *yhat, int *d_flag, void *workspace,
+                                                  size_t ws_bytes, void *stream)
+{
+    int st = check_common(Xtrain, ldtrain, ntrain, Xtest, ldtest, ntest, d, sigma);
+    if (st != QMLG_OK) return st;
+    if (ntest == 0) return QMLG_OK;
+    if (yhat == nullptr || (ntrain > 0 && alpha == nullptr)) return QMLG_E_ARG;
+    cudaStream_t s = qmlg::as_stream(stream);
+    if (ntrain == 0) {
+        cudaError_t e = cudaMemsetAsync(yhat, 0, sizeof(double) * (size_t)ntest, s);
+        return e == cudaSuccess ? QMLG_OK : qmlg::set_cuda_error(e);
+    }
+    if (ws_bytes < qmlg_predict_laplacian_fixed_workspace_size(ntrain, ntest, d))
+        return QMLG_E_WORKSPACE;
+    qmlg::Workspace ws(workspace, ws_bytes);
+    const int tj = (int)qmlg::ceil_div(ntrain, TJ), ti = (int)qmlg::ceil_div(ntest, TI);
+    dim3 grid;
+    if (!tile_list_grid(tj, ti, false, grid)) return QMLG_E_ARG;
+    double *partial = ws.take<double>((size_t)tj * ntest);
+    long long *qa = ws.take<long long>((size_t)ntrain * d);
+    long long *qb = ws.take<long long>((size_t)ntest * d);
+    unsigned long long *mx = ws.take<unsigned long long>(2);
+    FixedPlan *plan = ws.take<FixedPlan>(1);
+    if (partial == nullptr || qa == nullptr || qb == nullptr || mx == nullptr || plan == nullptr)
+        return QMLG_E_WORKSPACE;
+    cudaError_t e = cudaMemsetAsync(mx, 0, 2 * sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+    auto blocks = [](int64_t total) { return (int)std::min<int64_t>(qmlg::ceil_div(total, 256), 2432); };
+    max_abs_rows_kernel<<<blocks((int64_t)ntrain * d), 256, 0, s>>>(Xtrain, ldtrain, ntrain, d, mx);
+    max_abs_rows_kernel<<<blocks((int64_t)ntest * d), 256, 0, s>>>(Xtest, ldtest, ntest, d, mx + 1);
+    fixed_plan_kernel<<<1, 1, 0, s>>>(mx, 2, d, sigma, plan, d_flag);
+    to_fixed_kernel<<<blocks((int64_t)ntrain * d), 256, 0, s>>>(Xtrain, ldtrain, ntrain, d, 0.0, qa,
+                                                                plan);
+    to_fixed_kernel<<<blocks((int64_t)ntest * d), 256, 0, s>>>(Xtest, ldtest, ntest, d, 0.0, qb, plan);
+    laplace_fixed_predict_kernel<<<grid, NT, 0, s>>>(qa, ntrain, qb, ntest, d, 0.0, -1.0 / sigma,
+                                                     alpha, partial, plan);
+    predict_partial_kernel<kLaplace><<<grid, NT, 0, s>>>(Xtrain, ldtrain, ntrain, Xtest, ldtest,
+                                                         ntest, d, -1.0 / sigma, alpha, partial,
+                                                         &plan->ok);
+    reduce_partial_kernel<<<(int)qmlg::ceil_div(ntest, 256), 256, 0, s>>>(partial, tj, ntest, yhat);
+    qmlg::count_launches(9);
     return qmlg::check_launch();
 }

@@ -11,8 +11,9 @@ The scheduler runs one host loop.  On every turn it does three things:
   * it admits queued requests while slots are free and the HBM budget allows.
 
 Admitted predictions of the same model are merged into one launch.  The merged
-launch is one Coulomb-matrix kernel and one fused tensor-core prediction, and the
-results are split back per request.  It runs on one of several CUDA streams, so
+launch is one Coulomb-matrix kernel and one fused prediction (tensor cores for a
+Gaussian model, fixed-point L1 sums for a Laplacian one), and the results are split
+back per request.  It runs on one of several CUDA streams, so
 it overlaps with other batches and with fits.  Fits synchronise internally (the
 solve takes refinement decisions on the host), so they run on a worker thread
 with their own stream.  The host loop keeps admitting predictions meanwhile.
@@ -54,8 +55,9 @@ class Request:
     done: float = math.nan
     result: Optional[np.ndarray] = None
     error: Optional[str] = None
-    path: str = ""               # "tensor" or "fp64" (recomputed when the digit bound failed)
+    path: str = ""               # "tensor" / "fixed", or "fp64" when the fast path's bound failed
     flag: int = 0
+    kernel: str = "gaussian"     # fit requests: the kernel of the model they create
 
     @property
     def n_mol(self) -> int:
@@ -73,13 +75,17 @@ def fit_bytes(n: int) -> int:
     return 8 * n * n + 16 * rp * 576 + 8 * (-(-n // 64)) * 4096 + 64 * n + (64 << 20)
 
 
-def predict_bytes(n_query: int, n_train: int) -> int:
-    """HBM a prediction batch holds: query molecules and CMs, digit planes of
-    both sides (8 planes x 320 bf16 per row), partial sums."""
+def predict_bytes(n_query: int, n_train: int, kernel: str = "gaussian") -> int:
+    """HBM a prediction batch holds: query molecules and CMs, then for a Gaussian
+    model the digit planes of both sides (8 planes x 320 bf16 per row) and partial
+    sums per 128 training rows; for a Laplacian model the fixed-point features of
+    both sides (8 bytes per value) and partial sums per 64 training rows."""
     rq = -(-n_query // 128) * 128
     rt = -(-n_train // 128) * 128
-    return (n_query * (FEATURES * 8 + 23 * 32) + 16 * 320 * (rq + rt)
-            + 8 * n_query * (-(-n_train // 128)) + (8 << 20))
+    base = n_query * (FEATURES * 8 + 23 * 32) + (8 << 20)
+    if kernel == "laplacian":
+        return base + 8 * FEATURES * (n_query + n_train) + 8 * n_query * (-(-n_train // 64))
+    return base + 16 * 320 * (rq + rt) + 8 * n_query * (-(-n_train // 128))
 
 
 class Scheduler:
@@ -88,7 +94,8 @@ class Scheduler:
     `max_batch_molecules` caps one merged prediction launch."""
 
     def __init__(self, budget_bytes: int, max_slots: int = 8, max_batch_molecules: int = 8192,
-                 model_sizes: Optional[Dict[str, int]] = None):
+                 model_sizes: Optional[Dict[str, int]] = None,
+                 model_kinds: Optional[Dict[str, str]] = None):
         self.budget = int(budget_bytes)
         self.max_slots = max_slots
         self.max_batch = max_batch_molecules
@@ -97,6 +104,11 @@ class Scheduler:
         self.slots = 0
         self.fit_running = False
         self.model_sizes: Dict[str, int] = dict(model_sizes or {})
+        self.model_kinds: Dict[str, str] = dict(model_kinds or {})
+
+    def _predict_cost(self, model: str, mols: int) -> int:
+        return predict_bytes(mols, self.model_sizes.get(model, 0),
+                             self.model_kinds.get(model, "gaussian"))
 
     def submit(self, req: Request):
         self.queue.append(req)
@@ -104,7 +116,7 @@ class Scheduler:
     def cost(self, req: Request) -> int:
         if req.kind == "fit":
             return fit_bytes(req.n_mol)
-        return predict_bytes(req.n_mol, self.model_sizes.get(req.model, 0))
+        return self._predict_cost(req.model, req.n_mol)
 
     def next_batch(self) -> Optional[List[Request]]:
         """The next admissible unit of work, or None.  Fits go one at a time (one
@@ -157,7 +169,7 @@ class Scheduler:
             else:
                 rest.append(r)
         self.queue = rest + self.queue
-        cost = predict_bytes(mols, self.model_sizes.get(head.model, 0))
+        cost = self._predict_cost(head.model, mols)
         if self.in_use + cost > self.budget:
             for r in reversed(batch):
                 self.queue.appendleft(r)
@@ -174,9 +186,10 @@ class Scheduler:
             self.fit_running = False
             if batch[0].error is None:
                 self.model_sizes[batch[0].model] = batch[0].n_mol
+                self.model_kinds[batch[0].model] = batch[0].kernel
         else:
             mols = sum(r.n_mol for r in batch)
-            self.in_use -= predict_bytes(mols, self.model_sizes.get(batch[0].model, 0))
+            self.in_use -= self._predict_cost(batch[0].model, mols)
             self.slots -= 1
 
 
@@ -235,9 +248,11 @@ class GpuExecutor:
             })
         self.free = list(range(n_streams))
 
-    def add_model(self, name, X, alpha, sigma):
+    def add_model(self, name, X, alpha, sigma, kernel: str = "gaussian"):
+        if kernel not in ("gaussian", "laplacian"):
+            raise ValueError("unknown kernel %r" % (kernel,))
         with self.lock:
-            self.models[name] = (X, alpha, sigma)
+            self.models[name] = (X, alpha, sigma, kernel)
 
     def set_query_persistence(self, on: bool):
         """Query kernels are launched from the serving thread: one CTA per tile
@@ -252,7 +267,7 @@ class GpuExecutor:
         slot = self.free.pop()
         stream, st = self.streams[slot], self.staging[slot]
         with self.lock:
-            X, alpha, sigma = self.models[batch[0].model]
+            X, alpha, sigma, kernel = self.models[batch[0].model]
         charges, coords, offsets, ranges = merge_molecules(batch)
         n, na = offsets.shape[0] - 1, charges.shape[0]
         if n > self.max_mols or na * 3 > st["coords"].numel():
@@ -266,25 +281,33 @@ class GpuExecutor:
             r = st["coords"][:3 * na].to(self.device, non_blocking=True).view(na, 3)
             o = st["offsets"][:n + 1].to(self.device, non_blocking=True)
             Xq = self.core.coulomb_matrix_batch_async(z, r, o, CM_SIZE)
-            if self.precision == "mixed":
+            fast = self.precision == "mixed"
+            if fast:
                 st["dflag"].zero_()
-                y = self.core.predict_async(X, Xq, sigma, alpha, st["dflag"])
+                if kernel == "laplacian":
+                    y = self.core.predict_laplacian_async(X, Xq, sigma, alpha, st["dflag"])
+                else:
+                    y = self.core.predict_async(X, Xq, sigma, alpha, st["dflag"])
                 st["flag"].copy_(st["dflag"], non_blocking=True)
             else:
-                y = self.core.predict("gaussian", X, Xq, sigma, alpha)
+                y = self.core.predict(kernel, X, Xq, sigma, alpha)
             st["out"][:n].copy_(y, non_blocking=True)
             ev = torch.cuda.Event()
             ev.record(stream)
 
         def finish():
             vals = st["out"].numpy()[:n]
-            flag = int(st["flag"][0]) if self.precision == "mixed" else 0
-            path = "tensor" if self.precision == "mixed" else "fp64"
-            if flag != 0:
+            flag = int(st["flag"][0]) if fast else 0
+            path = ("fixed" if kernel == "laplacian" else "tensor") if fast else "fp64"
+            if kernel == "laplacian" and flag & 8:
+                # the fixed-point bound was not met: the FP64 kernel launched beside
+                # it already wrote the result
+                path = "fp64"
+            elif flag != 0:
                 # the tensor-core bound was not met (or a bounded wait gave up):
                 # recompute this batch with the FP64 kernel
                 with torch.cuda.stream(stream):
-                    vals = self.core.predict("gaussian", X, Xq, sigma, alpha).cpu().numpy()
+                    vals = self.core.predict(kernel, X, Xq, sigma, alpha).cpu().numpy()
                 path = "fp64"
             for req, (a, b) in zip(batch, ranges):
                 req.result = vals[a:b].copy()
@@ -306,9 +329,10 @@ class GpuExecutor:
             o = torch.from_numpy(np.ascontiguousarray(req.offsets)).to(self.device)
             y = torch.from_numpy(np.ascontiguousarray(req.labels)).to(self.device)
             X = self.core.coulomb_matrix_batch(z, r, o, CM_SIZE)
-            m = KRR(sigma=req.sigma, lam=req.lam, precision=self.precision).fit(X, y)
+            m = KRR(kernel=req.kernel, sigma=req.sigma, lam=req.lam,
+                    precision=self.precision).fit(X, y)
             self.fit_stream.synchronize()
-        self.add_model(req.model, X, m.alpha, req.sigma)
+        self.add_model(req.model, X, m.alpha, req.sigma, req.kernel)
         req.result = np.array([m.report.get("outer_iterations", 0)], dtype=np.float64)
 
 
@@ -407,11 +431,13 @@ class Server:
 
 def poisson_workload(rate_hz: float, duration_s: float, pool, model: str,
                      fit_every: int = 0, fit_sizes=(1000, 20000), seed: int = 0,
-                     max_query: int = 4096) -> List[Request]:
+                     max_query: int = 4096, fit_kernel: str = "gaussian",
+                     fit_sigma: float = 1000.0) -> List[Request]:
     """Poisson arrivals of prediction queries (molecule count log-uniform in
     1..max_query) and, every `fit_every`-th arrival, a fit request with N
-    log-uniform in fit_sizes.  Molecules are consecutive slices of `pool` (a
-    MoleculeBatch with labels) starting at random offsets."""
+    log-uniform in fit_sizes (kernel fit_kernel, width fit_sigma).  Molecules are
+    consecutive slices of `pool` (a MoleculeBatch with labels) starting at random
+    offsets."""
     rng = np.random.default_rng(seed)
     t, rid, out = 0.0, 0, []
 
@@ -428,7 +454,7 @@ def poisson_workload(rate_hz: float, duration_s: float, pool, model: str,
             n = int(round(math.exp(rng.uniform(math.log(fit_sizes[0]), math.log(fit_sizes[1])))))
             b = take(n)
             out.append(Request(rid, "fit", "fit-%d" % rid, b.charges, b.coordinates, b.offsets, t,
-                               labels=b.labels))
+                               labels=b.labels, kernel=fit_kernel, sigma=fit_sigma))
         else:
             n = int(round(math.exp(rng.uniform(0.0, math.log(max_query)))))
             b = take(n)

@@ -70,3 +70,42 @@ def test_autotuned_schedule(cuda, batch_problems):
     ref.run_eager()
     for a, r in zip(alphas, ref.results()[0]):
         assert np.array_equal(a.cpu().numpy(), r.cpu().numpy())
+
+
+def test_batched_laplacian_and_gaussian_fits(cuda, oracle):
+    # Laplacian fits in the same graph as Gaussian ones: K from the capture-safe
+    # fixed-point kernel (sigma = 10 takes the FP64 kernel in the same graph), alpha
+    # within 1e-8 of the refined oracle on each fit's own K
+    pool = generate_molecules(2600, seed=406)
+    Xo = oracle.cm_sorted_batch(pool.charges, pool.coordinates, pool.offsets, 23)
+    spec = [(1500, "laplacian", 10 ** 4.2, 1e-10), (900, "gaussian", 1000.0, 1e-8),
+            (700, "laplacian", 1000.0, 1e-8), (400, "laplacian", 10.0, 1e-6)]
+    probs, starts = [], []
+    for k, (n, kind, s, lam) in enumerate(spec):
+        st = (k * 277) % (2600 - n + 1)
+        starts.append(st)
+        probs.append(Problem(torch.from_numpy(np.ascontiguousarray(Xo[st:st + n])).cuda(),
+                             torch.from_numpy(np.ascontiguousarray(pool.labels[st:st + n])).cuda(),
+                             s, lam, kernel=kind))
+    b = BatchedKRR(probs, refine_steps=3, streams=2)
+    b.run_eager()
+    alphas, reps = b.results()
+    eager = [a.cpu().numpy().copy() for a in alphas]
+    for i, ((n, kind, s, lam), st) in enumerate(zip(spec, starts)):
+        rep = reps[i]
+        assert rep["info"] == 0 and rep["flags"] == 0, rep
+        want = "tensor" if kind == "gaussian" else ("fp64" if s == 10.0 else "fixed")
+        assert rep["kernel_path"] == want, rep
+        F = b.K[i].cpu().numpy()
+        U = np.triu(F, 1)
+        K = U + U.T + np.eye(n)
+        kfn = oracle.gaussian_kernel if kind == "gaussian" else oracle.laplacian_kernel
+        Ko = kfn(Xo[st:st + n], Xo[st:st + n], s)
+        assert np.max(np.abs(K - Ko) / Ko) <= 1e-12
+        ref = oracle.refined_solve(K, pool.labels[st:st + n], lam)
+        assert np.linalg.norm(eager[i] - ref) / np.linalg.norm(ref) <= 1e-8, (spec[i], rep)
+    b.capture()
+    b.replay()
+    alphas, _ = b.results()
+    for a, e in zip(alphas, eager):
+        assert np.array_equal(a.cpu().numpy(), e)

@@ -302,3 +302,40 @@ def test_emulated_tiles_across_bands(cuda, oracle, persistent):
     assert np.array_equal(np.triu(Cout, 1), np.triu(C, 1))
     for u, v in zip(outs[1], outs[persistent]):
         assert np.array_equal(u, v)
+
+
+@pytest.mark.parametrize("sigma", [10.0, 1000.0])
+def test_laplacian_async_entries_match_synchronous(cuda, cm_features, sigma):
+    # The capture-safe fixed-point entries decide the grid on the device: K and the
+    # predictions equal the synchronous entries' bit for bit.  At sigma = 10 the
+    # fixed-point bound d 2^-F / sigma <= 0.5e-12 fails for CM features, so the FP64
+    # kernel launched beside the fixed-point one writes the result and 8 is flagged.
+    X = cm_features
+    At = torch.from_numpy(X[:700]).to(cuda)
+    Bt = torch.from_numpy(X[700:]).to(cuda)
+    lib = core.lib()
+    stream = torch.cuda.current_stream().cuda_stream
+    want_flag = 8 if sigma == 10.0 else 0
+    for sym in (False, True):
+        B = At if sym else Bt
+        nb = B.shape[0]
+        flags = _lib.QMLG_KERNEL_SYMMETRIC if sym else 0
+        ref = core.kernel_matrix("laplacian", At, B, sigma, symmetric=sym, emulated=True)
+        buf = torch.full((nb, 700), float("nan"), dtype=torch.float64, device=cuda)
+        flag = torch.zeros(1, dtype=torch.int32, device=cuda)
+        ws_bytes = lib.qmlg_laplacian_kernel_fixed_workspace_size(700, nb, 276, flags)
+        ws = torch.empty(ws_bytes, dtype=torch.uint8, device=cuda)
+        st = lib.qmlg_laplacian_kernel_fixed_async(At.data_ptr(), 276, 700, B.data_ptr(), 276, nb,
+                                                   276, sigma, buf.data_ptr(), 700, flags, 0.0,
+                                                   flag.data_ptr(), ws.data_ptr(), ws_bytes, stream)
+        assert st == 0
+        torch.cuda.synchronize()
+        assert torch.equal(buf.T, ref)
+        assert int(flag.item()) == want_flag
+    alpha = torch.from_numpy(np.random.default_rng(2).normal(size=700)).to(cuda)
+    yref = core.predict("laplacian", At, Bt, sigma, alpha, emulated=True)
+    flag = torch.zeros(1, dtype=torch.int32, device=cuda)
+    y = core.predict_laplacian_async(At, Bt, sigma, alpha, flag)
+    torch.cuda.synchronize()
+    assert torch.equal(y, yref)
+    assert int(flag.item()) == want_flag

@@ -52,3 +52,43 @@ def test_serving_mix_equals_alone(cuda, oracle):
         expect = Ks.T @ alpha
         scale = np.abs(Ks.T) @ np.abs(alpha)
         assert np.max(np.abs(req.result - expect) / scale) <= 1e-12
+
+
+def test_serving_laplacian_model_mix_equals_alone(cuda, oracle):
+    # a Laplacian model (the reference's end-to-end KRR test uses the Laplacian
+    # kernel, sigma = 10^4.2, lambda = 1e-10: tests/test_energy_krr_cmat.py:97-113):
+    # queries take the fixed-point fused prediction, fits in the mix create
+    # Laplacian models too, and each query's result is the same alone and in the mix
+    sigma, lam, ntr = 10 ** 4.2, 1e-10, 3000
+    train = generate_molecules(ntr, seed=111)
+    z, r, o = molecules_to_device(train)
+    X = core.coulomb_matrix_batch(z, r, o, 23)
+    y = torch.from_numpy(train.labels).to(cuda)
+    model = KRR(kernel="laplacian", sigma=sigma, lam=lam, precision="mixed").fit(X, y)
+    ex = serving.GpuExecutor(n_streams=3)
+    ex.add_model("lap", X, model.alpha, sigma, kernel="laplacian")
+    pool = generate_molecules(4000, seed=112)
+    reqs = serving.poisson_workload(400.0, 0.5, pool, "lap", fit_every=40, fit_sizes=(500, 1500),
+                                    seed=6, max_query=512, fit_kernel="laplacian", fit_sigma=sigma)
+    sched = serving.Scheduler(budget_bytes=8 << 30, max_slots=3, model_sizes={"lap": ntr},
+                              model_kinds={"lap": "laplacian"})
+    done = serving.Server(ex, sched).run(reqs)
+    assert len(done) == len(reqs) and all(r.error is None for r in done)
+    fits = [r for r in done if r.kind == "fit"]
+    assert fits and all(ex.models[r.model][3] == "laplacian" for r in fits)
+    preds = [r for r in done if r.kind == "predict"]
+    assert len(preds) > 50
+    assert all(r.path == "fixed" and r.flag == 0 for r in preds), \
+        sorted({(r.path, r.flag) for r in preds})
+    Xo = oracle.cm_sorted_batch(train.charges, train.coordinates, train.offsets, 23)
+    alpha = model.alpha.cpu().numpy()
+    for req in preds[:12]:
+        alone = serving.Request(-1, "predict", "lap", req.charges, req.coordinates, req.offsets, 0.0)
+        ev, finish = ex.launch_predict([alone])
+        ev.synchronize()
+        finish()
+        assert np.array_equal(alone.result, req.result)
+        Xq = oracle.cm_sorted_batch(req.charges, req.coordinates, req.offsets, 23)
+        Ks = oracle.laplacian_kernel(Xo, Xq, sigma)
+        scale = np.abs(Ks.T) @ np.abs(alpha)
+        assert np.max(np.abs(req.result - Ks.T @ alpha) / scale) <= 1e-12
