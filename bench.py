@@ -406,8 +406,9 @@ def run_extra(a, dev, batch, X, stream):
 def run_batching(a, dev):
     """64 fits of uneven size (N log-uniform in [500, 8000]), each with its own
     sigma in {250, 500, 1000, 2000} and lambda in {1e-4, 1e-6, 1e-8}, recorded into
-    one CUDA graph with an autotuned schedule; compared with running the same fits
-    one after another through the ordinary mixed solve."""
+    one CUDA graph: the grouped path (one grouped launch per phase for all fits,
+    autotuned tile parameters), beside the per-fit stream schedule in a graph and the
+    same fits run one after another through the ordinary mixed solve."""
     import math
 
     import numpy as np
@@ -430,23 +431,38 @@ def run_batching(a, dev):
         probs.append(Problem(Xall[start:start + n].contiguous(), yall[start:start + n].contiguous(),
                              float(rng.choice([250.0, 500.0, 1000.0, 2000.0])),
                              float(rng.choice([1e-4, 1e-6, 1e-8]))))
-    b = BatchedKRR(probs, refine_steps=3)
-    tuned = b.autotune(candidates=[{"streams": s, "order": "size", "persistent": p}
-                                   for s in (4, 8, 16) for p in (True, False)], reps=1)
-    b.capture()
     stream = torch.cuda.current_stream(dev)
-    b.replay()
-    torch.cuda.synchronize()
-    e0, e1 = _events(2)
-    reps = 3
-    e0.record(stream)
-    for _ in range(reps):
+
+    def replay_time(b, reps=3):
+        b.capture()
         b.replay()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    graph_s = _span(e0, e1) / reps
+        torch.cuda.synchronize()
+        e0, e1 = _events(2)
+        e0.record(stream)
+        for _ in range(reps):
+            b.replay()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return _span(e0, e1) / reps
+
+    # the grouped path (one grouped launch per phase), autotuned tile parameters
+    b = BatchedKRR(probs, refine_steps=3)
+    tuned = b.autotune(reps=1)
+    graph_s = replay_time(b)
     alphas, reports = b.results()
     ok = sum(1 for rp in reports if rp["info"] == 0 and rp["flags"] == 0)
+    lib = core.lib()
+    torch.cuda.synchronize()
+    c0 = lib.qmlg_launch_count()
+    b.run_eager()
+    grouped_launches = int(lib.qmlg_launch_count() - c0)
+    del b
+    torch.cuda.empty_cache()
+    # the earlier schedule: each fit's own launches spread over 16 streams
+    bs = BatchedKRR(probs, refine_steps=3, mode="streams", streams=16)
+    streams_s = replay_time(bs)
+    del bs
+    torch.cuda.empty_cache()
     # the same fits one after another (kernel + mixed solve each, host-driven)
     t0 = time.perf_counter()
     for p in probs:
@@ -455,9 +471,10 @@ def run_batching(a, dev):
     seq_s = time.perf_counter() - t0
     sizes = [p.X.shape[0] for p in probs]
     return {"fits": len(probs), "n_min": min(sizes), "n_max": max(sizes),
-            "n_sum": int(sum(sizes)), "graph_s": graph_s, "sequential_s": seq_s,
+            "n_sum": int(sum(sizes)), "graph_s": graph_s, "launches": grouped_launches,
+            "streams_graph_s": streams_s, "sequential_s": seq_s,
             "speedup": seq_s / graph_s, "converged": ok,
-            "schedule": {k: tuned[k] for k in tuned if k != "ms"}}
+            "tuned": {k: tuned[k] for k in ("tile_cols", "trsm_rows") if k in tuned}}
 
 
 def run_large(a, dev, stream):

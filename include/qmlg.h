@@ -452,6 +452,55 @@ int qmlg_solve_async(double *A, int n, int64_t lda, const double *y, double *x, 
                      size_t ws_bytes, void *stream);
 
 /*
+ * Batched KRR fits: many independent fits of uneven size, as the learning curves and
+ * sigma x lambda grids of docs/source/tutorial.rst:168-174 run them, each the
+ * gaussian_kernel / laplacian_kernel + K[diag] += lambda + cho_solve sequence of
+ * tests/test_energy_krr_cmat.py:97-106 (qml/kernels.py:36-92, qml/fcho_solve.f90:23-52).
+ * Every phase is one grouped launch over all fits instead of one launch per fit:
+ *   - the symmetric Gaussian kernel matrices of every Gaussian fit, on the tensor
+ *     cores as qmlg_gaussian_kernel_emulated_async (8 digit planes; a fit whose data
+ *     miss the 1e-12 bound gets 8 in its flags); Laplacian fits take
+ *     qmlg_laplacian_kernel_fixed_async each;
+ *   - the mixed factorisation in lockstep 64-column steps: FP64 diagonal blocks of
+ *     every fit in one launch, their panel solves in one, the K = 64 updates in one
+ *     tensor-core launch, and every 512 columns one tensor-core launch for all
+ *     trailing matrices;
+ *   - the block inverses, then the triangular solves one 64-row block per launch for
+ *     all fits at once, and refine_steps exact-residual refinement steps.
+ * No host synchronisation and no host decision: the call can be recorded into a CUDA
+ * graph.  All pointers are device pointers except the problem array itself, which
+ * is read during the call only.  At most 128 fits per call.
+ *   K       n x n column-major buffer per fit: receives K in its strictly lower
+ *           triangle (the factor in the upper one, as qmlg_cholesky)
+ *   status  device int[2] per fit: [0] Cholesky info (0 = ok); [1] flags: 8 = the
+ *           kernel's fast path missed its bound (Gaussian: refit that fit with
+ *           qmlg_solve; Laplacian: the FP64 kernel formed K, nothing to do),
+ *           1/2/4 = a bounded tensor-core wait gave up
+ *   correction  optional device double[2]: |dx|^2 and |x|^2 of the last step
+ * tile_cols: i-columns per tensor-core tile of the factorisation's updates, 64 or
+ * 32; trsm_rows: rows per CTA of the panel solves, 32..128 (multiple of 8).  0 takes
+ * the defaults (64, 128); a batch autotuner picks them per size bucket.
+ */
+typedef struct QmlgBatchProblem {
+    const double *X;      /* n x d representations, row-major */
+    int64_t ldx;
+    int n;
+    int kind;             /* QMLG_KIND_GAUSSIAN or QMLG_KIND_LAPLACIAN */
+    double sigma;
+    double lambda;
+    const double *y;      /* n labels */
+    double *alpha;        /* n weights, written */
+    double *K;            /* n x n, leading dimension n */
+    int *status;          /* device int[2] */
+    double *correction;   /* device double[2] or NULL */
+} QmlgBatchProblem;
+
+size_t qmlg_fit_batched_workspace_size(const QmlgBatchProblem *problems, int count, int d);
+int qmlg_fit_batched_async(const QmlgBatchProblem *problems, int count, int d, int refine_steps,
+                           int tile_cols, int trsm_rows, void *workspace, size_t ws_bytes,
+                           void *stream);
+
+/*
  * Inverse of a symmetric positive-definite matrix: Ainv (column-major, ldi) =
  * A^-1, both triangles written.  Reads A's column-major lower triangle, as
  * dpotrf("L") + dpotri("L") in fcho_invert (qml/fcho_solve.f90:54-73), bound by

@@ -64,6 +64,13 @@ class QmlgRefineOpts(ctypes.Structure):
                 ("slices", ctypes.c_int)]
 
 
+class QmlgBatchProblem(ctypes.Structure):
+    _fields_ = [("X", ctypes.c_void_p), ("ldx", ctypes.c_int64), ("n", ctypes.c_int),
+                ("kind", ctypes.c_int), ("sigma", ctypes.c_double), ("lam", ctypes.c_double),
+                ("y", ctypes.c_void_p), ("alpha", ctypes.c_void_p), ("K", ctypes.c_void_p),
+                ("status", ctypes.c_void_p), ("correction", ctypes.c_void_p)]
+
+
 _P = ctypes.c_void_p
 _I = ctypes.c_int
 _I64 = ctypes.c_int64
@@ -130,6 +137,9 @@ SIGNATURES = {
                                                 _SZ, _P]),
     "qmlg_laplacian_kernel_fixed_async": (_I, [_P, _I64, _I, _P, _I64, _I, _I, _D, _P, _I64, _I,
                                                _D, _P, _P, _SZ, _P]),
+    "qmlg_fit_batched_workspace_size": (_SZ, [ctypes.POINTER(QmlgBatchProblem), _I, _I]),
+    "qmlg_fit_batched_async": (_I, [ctypes.POINTER(QmlgBatchProblem), _I, _I, _I, _I, _I, _P, _SZ,
+                                    _P]),
     "qmlg_selftest_wait_timeout_workspace_size": (_SZ, []),
     "qmlg_selftest_wait_timeout": (_I, [_P, _SZ, _P]),
 }

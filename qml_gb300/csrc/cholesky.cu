@@ -96,9 +96,8 @@ __device__ __forceinline__ void potrf_workers_sync()
     asm volatile("bar.sync 1, 192;" ::: "memory");
 }
 
-__global__ void __launch_bounds__(POTRF_THREADS)
-potrf_diag_kernel(double *__restrict__ A, int64_t lda, int n, int k0, double shift,
-                  int *__restrict__ info)
+__device__ __forceinline__ void potrf_diag_block(double *__restrict__ A, int64_t lda, int n, int k0,
+                                                 double shift, int *__restrict__ info)
 {
     // Right-looking in shared memory.  One FP64 warp instruction occupies a
     // scheduler's FP64 pipe for ~64 cycles whatever its active lanes, so the
@@ -192,6 +191,13 @@ potrf_diag_kernel(double *__restrict__ A, int64_t lda, int n, int k0, double shi
     }
 }
 
+__global__ void __launch_bounds__(POTRF_THREADS)
+potrf_diag_kernel(double *__restrict__ A, int64_t lda, int n, int k0, double shift,
+                  int *__restrict__ info)
+{
+    potrf_diag_block(A, lda, n, k0, shift, info);
+}
+
 constexpr int TRSM_MAX_ROWS = 128;  // rows per CTA: 4 threads per row
 
 // Rows per TRSM CTA for `rows` rows on `sms` SMs: a multiple of 8 up to 128, chosen
@@ -214,10 +220,10 @@ inline size_t trsm_smem(int rpc) { return (size_t)rpc * (NB + 8) * sizeof(__nv_b
 // update that follows): per-row exponents and the `slices` balanced base-128 digit
 // planes, digits[s][row][64] with row = global row - (k0 + 64), for the rows below
 // drows (zeros past the matrix).
-__global__ void __launch_bounds__(4 * TRSM_MAX_ROWS)
-trsm_panel_kernel(double *__restrict__ A, int64_t lda, int n, int k0,
-                  const int *__restrict__ info, int slices, int rpad, int drows,
-                  __nv_bfloat16 *__restrict__ digits, int *__restrict__ expo)
+__device__ __forceinline__ void trsm_panel_rows(double *__restrict__ A, int64_t lda, int n, int k0,
+                                                const int *__restrict__ info, int slices, int rpad,
+                                                int drows, __nv_bfloat16 *__restrict__ digits,
+                                                int *__restrict__ expo, int bid)
 {
     __shared__ double L[NB][NB + 1];
     __shared__ double rdg[NB];
@@ -228,7 +234,7 @@ trsm_panel_kernel(double *__restrict__ A, int64_t lda, int n, int k0,
     const int rpc = blockDim.x >> 2;
     const int nb = min(NB, n - k0);
     const int r1 = k0 + nb, nrows = n - r1;
-    const int rbase = blockIdx.x * rpc;
+    const int rbase = bid * rpc;
 #pragma unroll 8
     for (int e = tid; e < NB * NB; e += blockDim.x) {
         const int r = e >> 6, c = e & 63;
@@ -310,6 +316,14 @@ trsm_panel_kernel(double *__restrict__ A, int64_t lda, int n, int k0,
         }
         __syncthreads();
     }
+}
+
+__global__ void __launch_bounds__(4 * TRSM_MAX_ROWS)
+trsm_panel_kernel(double *__restrict__ A, int64_t lda, int n, int k0,
+                  const int *__restrict__ info, int slices, int rpad, int drows,
+                  __nv_bfloat16 *__restrict__ digits, int *__restrict__ expo)
+{
+    trsm_panel_rows(A, lda, n, k0, info, slices, rpad, drows, digits, expo, blockIdx.x);
 }
 
 // Launches the TRSM of the rows below diagonal block k0 (with `digits`: the digit
@@ -425,18 +439,19 @@ __device__ __forceinline__ void acc_shfl_xor_add(qmlg::Acc &a, int off)
     qmlg::acc_add_acc(a, b);
 }
 
-__global__ void __launch_bounds__(256)
-symv_exact_partial_kernel(const double *__restrict__ A, int64_t lda, int n,
-                          const double *__restrict__ diag, const double *__restrict__ x,
-                          AccPart *__restrict__ partial)
+__device__ __forceinline__ void symv_exact_partial_block(const double *__restrict__ A, int64_t lda,
+                                                         int n, const double *__restrict__ diag,
+                                                         const double *__restrict__ x,
+                                                         AccPart *__restrict__ partial, int bx,
+                                                         int by)
 {
     __shared__ double S[64][64 + 1];
     __shared__ unsigned long long xm[64];
     __shared__ int xe[64];
     __shared__ unsigned char xn[64];
     const int tid = threadIdx.x;
-    const int i0 = blockIdx.x * RES_ROWS;
-    const int c0 = blockIdx.y * RES_CHUNK;
+    const int i0 = bx * RES_ROWS;
+    const int c0 = by * RES_CHUNK;
     const int lr = tid >> 2, part = tid & 3;
     qmlg::Acc acc;
     qmlg::acc_init(acc);
@@ -488,7 +503,7 @@ symv_exact_partial_kernel(const double *__restrict__ A, int64_t lda, int n,
     acc_shfl_xor_add(acc, 2);
     const int i = i0 + lr;
     if (part == 0 && i < n) {
-        AccPart &o = partial[(int64_t)blockIdx.y * n + i];
+        AccPart &o = partial[(int64_t)by * n + i];
         o.l0 = acc.l0;
         o.l1 = acc.l1;
         o.l2 = acc.l2;
@@ -498,12 +513,22 @@ symv_exact_partial_kernel(const double *__restrict__ A, int64_t lda, int n,
     }
 }
 
-// r[i] = y[i] - lambda x[i] - sum_chunks partial, summed exactly, rounded once.
-__global__ void residual_finish_kernel(const AccPart *__restrict__ partial, int nchunks, int n,
-                                       double lambda, const double *__restrict__ x,
-                                       const double *__restrict__ y, double *__restrict__ r)
+__global__ void __launch_bounds__(256)
+symv_exact_partial_kernel(const double *__restrict__ A, int64_t lda, int n,
+                          const double *__restrict__ diag, const double *__restrict__ x,
+                          AccPart *__restrict__ partial)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    symv_exact_partial_block(A, lda, n, diag, x, partial, blockIdx.x, blockIdx.y);
+}
+
+// r[i] = y[i] - lambda x[i] - sum_chunks partial, summed exactly, rounded once.
+__device__ __forceinline__ void residual_finish_block(const AccPart *__restrict__ partial,
+                                                      int nchunks, int n, double lambda,
+                                                      const double *__restrict__ x,
+                                                      const double *__restrict__ y,
+                                                      double *__restrict__ r, int bid)
+{
+    const int i = bid * blockDim.x + threadIdx.x;
     if (i >= n) return;
     qmlg::Acc a;
     qmlg::acc_init(a);
@@ -523,6 +548,13 @@ __global__ void residual_finish_kernel(const AccPart *__restrict__ partial, int 
     r[i] = qmlg::acc_to_double(a);
 }
 
+__global__ void residual_finish_kernel(const AccPart *__restrict__ partial, int nchunks, int n,
+                                       double lambda, const double *__restrict__ x,
+                                       const double *__restrict__ y, double *__restrict__ r)
+{
+    residual_finish_block(partial, nchunks, n, lambda, x, y, r, blockIdx.x);
+}
+
 // ---------------------------------------------------------------- vectors --
 
 __global__ void copy_diag_kernel(const double *__restrict__ A, int64_t lda, int n,
@@ -532,12 +564,13 @@ __global__ void copy_diag_kernel(const double *__restrict__ A, int64_t lda, int 
     if (i < n) d[i] = A[(int64_t)i * lda + i];
 }
 
-__global__ void axpy_norms_kernel(double *__restrict__ x, const double *__restrict__ dx, int n,
-                                  double *__restrict__ sums)
+__device__ __forceinline__ void axpy_norms_block(double *__restrict__ x,
+                                                 const double *__restrict__ dx, int n,
+                                                 double *__restrict__ sums, int bid)
 {
     // x += dx; sums[0] += |dx|^2, sums[1] += |x|^2 (block partials, then atomics)
     __shared__ double s0[8], s1[8];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = bid * blockDim.x + threadIdx.x;
     double a = 0.0, b = 0.0;
     if (i < n) {
         const double d = dx[i];
@@ -565,6 +598,12 @@ __global__ void axpy_norms_kernel(double *__restrict__ x, const double *__restri
         atomicAdd(&sums[0], ta);
         atomicAdd(&sums[1], tb);
     }
+}
+
+__global__ void axpy_norms_kernel(double *__restrict__ x, const double *__restrict__ dx, int n,
+                                  double *__restrict__ sums)
+{
+    axpy_norms_block(x, dx, n, sums, blockIdx.x);
 }
 
 // ------------------------------------------- cooperative triangular solves --
@@ -699,13 +738,12 @@ trsv_bwd_coop_kernel(const double *__restrict__ A, int64_t lda, int n, double *_
 // Inverse of every 64 x 64 diagonal block of the factor (lower triangular), one CTA
 // per block: column c of L_kk^{-1} by forward substitution (thread c).  Blocks of
 // a short last block are padded with the identity.
-__global__ void __launch_bounds__(64)
-invert_diag_blocks_kernel(const double *__restrict__ A, int64_t lda, int n,
-                          double *__restrict__ Linv)
+__device__ __forceinline__ void invert_diag_block(const double *__restrict__ A, int64_t lda, int n,
+                                                  double *__restrict__ Linv, int kb)
 {
     __shared__ double L[NB][NB + 1];
     __shared__ double X[NB][NB + 1];
-    const int kb = blockIdx.x, k0 = kb * NB, nb = min(NB, n - k0);
+    const int k0 = kb * NB, nb = min(NB, n - k0);
     const int tid = threadIdx.x;
     for (int e = tid; e < NB * NB; e += blockDim.x) {
         const int r = e >> 6, c = e & 63;
@@ -723,6 +761,13 @@ invert_diag_blocks_kernel(const double *__restrict__ A, int64_t lda, int n,
     __syncthreads();
     double *dst = Linv + (int64_t)kb * NB * NB;
     for (int e = tid; e < NB * NB; e += blockDim.x) dst[e] = X[e >> 6][e & 63];
+}
+
+__global__ void __launch_bounds__(64)
+invert_diag_blocks_kernel(const double *__restrict__ A, int64_t lda, int n,
+                          double *__restrict__ Linv)
+{
+    invert_diag_block(A, lda, n, Linv, blockIdx.x);
 }
 
 // y[0..64) = M v for a 64 x 64 row-major M (M in global memory, v in shared memory);
@@ -1027,16 +1072,16 @@ trsv_bwd_solved_kernel(const double *__restrict__ A, int64_t lda, int n,
 // (four threads per entry).
 constexpr int STEP_THREADS = 256;
 
-__global__ void __launch_bounds__(STEP_THREADS)
-trsv_fwd_step_kernel(const double *__restrict__ A, int64_t lda, int n,
-                     const double *__restrict__ Linv, double *__restrict__ x, int k)
+__device__ __forceinline__ void trsv_fwd_step(const double *__restrict__ A, int64_t lda, int n,
+                                              const double *__restrict__ Linv,
+                                              double *__restrict__ x, int k, int bid, int nctas)
 {
     __shared__ double zp[NB], bb[NB];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int k0 = k * NB, nb = min(NB, n - k0), kp = k0 - NB;  // block k-1 is full
     if (k > 0 && tid < NB) zp[tid] = x[kp + tid];
     __syncthreads();
-    if (blockIdx.x == 0) {
+    if (bid == 0) {
         const double s = k > 0 ? gemv64_row(A + (int64_t)k0 * lda + kp, lda, zp, tid, nb) : 0.0;
         if ((tid & 3) == 0) bb[tid >> 2] = (tid >> 2) < nb ? x[k0 + (tid >> 2)] - s : 0.0;
         __syncthreads();
@@ -1044,8 +1089,8 @@ trsv_fwd_step_kernel(const double *__restrict__ A, int64_t lda, int n,
         if ((tid & 3) == 0 && (tid >> 2) < nb) x[k0 + (tid >> 2)] = z;
     } else if (k > 0) {
         constexpr int nw = STEP_THREADS / 32;
-        const int tw = (gridDim.x - 1) * nw;
-        for (int r = k0 + NB + (blockIdx.x - 1) * nw + warp; r < n; r += tw) {
+        const int tw = (nctas - 1) * nw;
+        for (int r = k0 + NB + (bid - 1) * nw + warp; r < n; r += tw) {
             const double *row = A + (int64_t)r * lda + kp;
             double sum = fma(row[lane], zp[lane], row[lane + 32] * zp[lane + 32]);
             for (int off = 16; off > 0; off >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, off);
@@ -1055,8 +1100,15 @@ trsv_fwd_step_kernel(const double *__restrict__ A, int64_t lda, int n,
 }
 
 __global__ void __launch_bounds__(STEP_THREADS)
-trsv_bwd_step_kernel(const double *__restrict__ A, int64_t lda, int n,
+trsv_fwd_step_kernel(const double *__restrict__ A, int64_t lda, int n,
                      const double *__restrict__ Linv, double *__restrict__ x, int k)
+{
+    trsv_fwd_step(A, lda, n, Linv, x, k, blockIdx.x, gridDim.x);
+}
+
+__device__ __forceinline__ void trsv_bwd_step(const double *__restrict__ A, int64_t lda, int n,
+                                              const double *__restrict__ Linv,
+                                              double *__restrict__ x, int k, int bid, int nctas)
 {
     __shared__ double xp[NB], bb[NB];
     const int tid = threadIdx.x, t = tid >> 2, q = tid & 3;
@@ -1065,7 +1117,7 @@ trsv_bwd_step_kernel(const double *__restrict__ A, int64_t lda, int n,
     const int nbp = k + 1 < nblk ? min(NB, n - k1) : 0;  // rows of block k+1
     if (tid < NB) xp[tid] = tid < nbp ? x[k1 + tid] : 0.0;
     __syncthreads();
-    if (blockIdx.x == 0) {
+    if (bid == 0) {
         // block k is full when block k+1 exists
         double s = 0.0;
 #pragma unroll
@@ -1081,8 +1133,8 @@ trsv_bwd_step_kernel(const double *__restrict__ A, int64_t lda, int n,
         if (q == 0 && t < nb) x[k0 + t] = v;
     } else if (nbp > 0) {
         constexpr int per = STEP_THREADS / 4;
-        const int tc = (gridDim.x - 1) * per;
-        for (int c0 = (blockIdx.x - 1) * per; c0 < k0; c0 += tc) {
+        const int tc = (nctas - 1) * per;
+        for (int c0 = (bid - 1) * per; c0 < k0; c0 += tc) {
             const int c = c0 + t;
             double s = 0.0;
             if (c < k0) {
@@ -1097,6 +1149,13 @@ trsv_bwd_step_kernel(const double *__restrict__ A, int64_t lda, int n,
             if (q == 0 && c < k0) x[c] -= s;
         }
     }
+}
+
+__global__ void __launch_bounds__(STEP_THREADS)
+trsv_bwd_step_kernel(const double *__restrict__ A, int64_t lda, int n,
+                     const double *__restrict__ Linv, double *__restrict__ x, int k)
+{
+    trsv_bwd_step(A, lda, n, Linv, x, k, blockIdx.x, gridDim.x);
 }
 
 // Both triangular solves in one CTA, with the block inverses: no waiting between
@@ -1984,4 +2043,485 @@ extern "C" int qmlg_cho_invert(const double *A, int n, int64_t lda, double *Ainv
     if (st != QMLG_OK) return st;
     // a pivot in the identity padding cannot fail; report A's pivot index like dpotrf
     return info > n ? n : info;
+}
+
+// ============================================================ batched fits ==
+//
+// qmlg_fit_batched_async: every phase of many independent fits as one grouped
+// launch.  A grouped launch runs several problems' grids back to back in one grid:
+// problem p owns CTAs [cta_base, cta_base + ctas) and its kernel body sees them as
+// blocks 0 .. ctas-1 (the bodies above take the block index as an argument).  The
+// table travels in the kernel parameter (a few KB), so the launch can be recorded
+// into a graph with no host-to-device copy.
+
+namespace {
+
+constexpr int kMaxBatch = 128;
+
+struct BatchEntry {
+    double *A;
+    int64_t lda;
+    int n, k;              // k: the 64-row block this step works on
+    double lambda;
+    int *status;           // [0] Cholesky info, [1] flags
+    double *Linv;
+    double *x;
+    const double *y;
+    double *r;
+    double *diag;
+    AccPart *partial;
+    double *sums;
+    double *correction;
+    __nv_bfloat16 *digits;  // panel solve: this problem's rows of the shared inner planes
+    int *expo;
+    int drows;
+    int cta_base, ctas;
+};
+
+struct BatchGroup {
+    int count, pad;
+    BatchEntry e[kMaxBatch];
+};
+
+__device__ __forceinline__ const BatchEntry &batch_entry(const BatchGroup &g, int &local)
+{
+    const int bid = (int)blockIdx.x;
+    int lo = 0, hi = g.count - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (g.e[mid].cta_base <= bid) lo = mid;
+        else hi = mid - 1;
+    }
+    local = bid - g.e[lo].cta_base;
+    return g.e[lo];
+}
+
+__global__ void __launch_bounds__(POTRF_THREADS) potrf_group_kernel(const __grid_constant__ BatchGroup g)
+{
+    int b;
+    const BatchEntry &e = batch_entry(g, b);
+    potrf_diag_block(e.A, e.lda, e.n, e.k * NB, e.lambda, e.status);
+}
+
+__global__ void __launch_bounds__(4 * TRSM_MAX_ROWS)
+trsm_group_kernel(const __grid_constant__ BatchGroup g, int slices, int rows_total)
+{
+    int b;
+    const BatchEntry &e = batch_entry(g, b);
+    trsm_panel_rows(e.A, e.lda, e.n, e.k * NB, e.status, slices, rows_total, e.drows, e.digits,
+                    e.expo, b);
+}
+
+__global__ void __launch_bounds__(64) invert_group_kernel(const __grid_constant__ BatchGroup g)
+{
+    int b;
+    const BatchEntry &e = batch_entry(g, b);
+    invert_diag_block(e.A, e.lda, e.n, e.Linv, b);
+}
+
+__global__ void __launch_bounds__(STEP_THREADS) fwd_group_kernel(const __grid_constant__ BatchGroup g)
+{
+    int b;
+    const BatchEntry &e = batch_entry(g, b);
+    trsv_fwd_step(e.A, e.lda, e.n, e.Linv, e.x, e.k, b, e.ctas);
+}
+
+__global__ void __launch_bounds__(STEP_THREADS) bwd_group_kernel(const __grid_constant__ BatchGroup g)
+{
+    int b;
+    const BatchEntry &e = batch_entry(g, b);
+    trsv_bwd_step(e.A, e.lda, e.n, e.Linv, e.x, e.k, b, e.ctas);
+}
+
+__global__ void __launch_bounds__(256) symv_group_kernel(const __grid_constant__ BatchGroup g)
+{
+    int b;
+    const BatchEntry &e = batch_entry(g, b);
+    const int rb = (e.n + RES_ROWS - 1) / RES_ROWS;
+    symv_exact_partial_block(e.A, e.lda, e.n, e.diag, e.x, e.partial, b % rb, b / rb);
+}
+
+__global__ void __launch_bounds__(256) finish_group_kernel(const __grid_constant__ BatchGroup g)
+{
+    int b;
+    const BatchEntry &e = batch_entry(g, b);
+    residual_finish_block(e.partial, (e.n + RES_CHUNK - 1) / RES_CHUNK, e.n, e.lambda, e.x, e.y,
+                          e.r, b);
+}
+
+__global__ void __launch_bounds__(256) axpy_group_kernel(const __grid_constant__ BatchGroup g)
+{
+    int b;
+    const BatchEntry &e = batch_entry(g, b);
+    axpy_norms_block(e.x, e.r, e.n, e.sums, b);
+}
+
+enum VecOp { kCopyDiag = 0, kCopyY = 1, kZeroSums = 2, kFinishFlags = 3 };
+
+// Small per-problem vector work: K's diagonal saved, x = y, the norm sums cleared,
+// and at the end the group's wait flags ORed into every status and the last
+// correction copied out.
+__global__ void __launch_bounds__(256) vec_group_kernel(const __grid_constant__ BatchGroup g, int op,
+                                                        const int *__restrict__ err)
+{
+    int b;
+    const BatchEntry &e = batch_entry(g, b);
+    const int i = b * 256 + (int)threadIdx.x;
+    if (op == kCopyDiag) {
+        if (i < e.n) e.diag[i] = e.A[(int64_t)i * e.lda + i];
+    } else if (op == kCopyY) {
+        if (i < e.n) e.x[i] = e.y[i];
+    } else if (op == kZeroSums) {
+        if (i < 2) e.sums[i] = 0.0;
+    } else if (b == 0 && threadIdx.x == 0) {
+        const int f = *err;
+        if (f != 0) atomicOr(e.status + 1, f);
+        if (e.correction != nullptr) {
+            e.correction[0] = e.sums[0];
+            e.correction[1] = e.sums[1];
+        }
+    }
+}
+
+// Host staging of one grouped launch (the table is copied into the launch).
+struct BatchLauncher {
+    BatchGroup g;
+    int total = 0;
+    void begin()
+    {
+        g.count = 0;
+        total = 0;
+    }
+    BatchEntry *add(int ctas)
+    {
+        if (ctas <= 0 || g.count >= kMaxBatch) return nullptr;
+        BatchEntry &e = g.e[g.count++];
+        e = BatchEntry{};
+        e.cta_base = total;
+        e.ctas = ctas;
+        total += ctas;
+        return &e;
+    }
+};
+
+// Per-fit state of a batch, carved from the workspace.
+struct BatchFit {
+    const QmlgBatchProblem *q;
+    int n, nblk, row_k, row_p;
+    double *diag, *r, *sums, *linv;
+    AccPart *partial;
+    void *lws;
+    size_t lws_bytes;
+};
+
+struct BatchBufs {
+    __nv_bfloat16 *kdig, *pdig, *idig;
+    int *kexp, *pexp, *iexp, *err;
+    double *knorm;
+    unsigned long long *maxbuf;
+    int RK, RT;
+};
+
+// The workspace layout of a batch; with base == nullptr only the size is computed.
+size_t batch_carve(const QmlgBatchProblem *probs, int count, int d, char *base, BatchBufs &b,
+                   std::vector<BatchFit> *fits)
+{
+    size_t used = 0;
+    auto take = [&](size_t bytes) -> char * {
+        const size_t off = qmlg::align_up(used, 256);
+        used = off + bytes;
+        return base != nullptr ? base + off : nullptr;
+    };
+    const int kp = qmlg::plane_cols(d);
+    b.RK = 0;
+    b.RT = 0;
+    for (int p = 0; p < count; ++p) {
+        if (probs[p].kind == QMLG_KIND_GAUSSIAN) b.RK += qmlg::plane_rows(probs[p].n);
+        b.RT += qmlg::plane_rows(probs[p].n);
+    }
+    const int RK = std::max(b.RK, 128), RT = std::max(b.RT, 128);
+    b.kdig = (__nv_bfloat16 *)take((size_t)qmlg::kEmuMaxSlices * RK * kp * 2);
+    b.kexp = (int *)take((size_t)RK * 4);
+    b.knorm = (double *)take((size_t)RK * 8);
+    b.maxbuf = (unsigned long long *)take((size_t)std::max(count, 1) * 8);
+    b.err = (int *)take(16);
+    b.pdig = (__nv_bfloat16 *)take((size_t)qmlg::kEmuMaxSlices * RT * 512 * 2);
+    b.pexp = (int *)take((size_t)RT * 4);
+    b.idig = (__nv_bfloat16 *)take((size_t)qmlg::kEmuMaxSlices * RT * NB * 2);
+    b.iexp = (int *)take((size_t)RT * 4);
+    int rk = 0, rp = 0;
+    for (int p = 0; p < count; ++p) {
+        const int n = std::max(probs[p].n, 0);
+        BatchFit f{};
+        f.q = &probs[p];
+        f.n = n;
+        f.nblk = (int)qmlg::ceil_div(n, NB);
+        f.row_k = probs[p].kind == QMLG_KIND_GAUSSIAN ? rk : -1;
+        if (probs[p].kind == QMLG_KIND_GAUSSIAN) rk += qmlg::plane_rows(n);
+        f.row_p = rp;
+        rp += qmlg::plane_rows(n);
+        f.diag = (double *)take((size_t)n * 8);
+        f.r = (double *)take((size_t)n * 8);
+        f.sums = (double *)take(16);
+        f.linv = (double *)take((size_t)f.nblk * NB * NB * 8);
+        f.partial = (AccPart *)take((size_t)qmlg::ceil_div(n, RES_CHUNK) * n * sizeof(AccPart));
+        f.lws = nullptr;
+        f.lws_bytes = 0;
+        if (probs[p].kind == QMLG_KIND_LAPLACIAN) {
+            f.lws_bytes = qmlg_laplacian_kernel_fixed_workspace_size(n, n, d, QMLG_KERNEL_SYMMETRIC);
+            f.lws = take(f.lws_bytes);
+        }
+        if (fits != nullptr) fits->push_back(f);
+    }
+    return qmlg::align_up(used, 256) + 256;
+}
+
+}  // namespace
+
+extern "C" size_t qmlg_fit_batched_workspace_size(const QmlgBatchProblem *problems, int count,
+                                                  int d)
+{
+    if (problems == nullptr || count <= 0) return 256;
+    BatchBufs b{};
+    return batch_carve(problems, count, d, nullptr, b, nullptr);
+}
+
+extern "C" int qmlg_fit_batched_async(const QmlgBatchProblem *problems, int count, int d,
+                                      int refine_steps, int tile_cols, int trsm_rows,
+                                      void *workspace, size_t ws_bytes, void *stream)
+{
+    if (count == 0) return QMLG_OK;
+    if (problems == nullptr || count < 0 || count > kMaxBatch || d < 1 || refine_steps < 0)
+        return QMLG_E_ARG;
+    if (tile_cols == 0) tile_cols = 64;
+    if (trsm_rows == 0) trsm_rows = TRSM_MAX_ROWS;
+    if ((tile_cols != 32 && tile_cols != 64) || trsm_rows < 32 || trsm_rows > TRSM_MAX_ROWS ||
+        trsm_rows % 8 != 0)
+        return QMLG_E_ARG;
+    for (int p = 0; p < count; ++p) {
+        const QmlgBatchProblem &q = problems[p];
+        if (q.n < 1 || q.X == nullptr || q.ldx < d || q.y == nullptr || q.alpha == nullptr ||
+            q.K == nullptr || q.status == nullptr || !(q.sigma > 0.0) || !(q.lambda >= 0.0) ||
+            (q.kind != QMLG_KIND_GAUSSIAN && q.kind != QMLG_KIND_LAPLACIAN))
+            return QMLG_E_ARG;
+    }
+    if (workspace == nullptr || ws_bytes < qmlg_fit_batched_workspace_size(problems, count, d))
+        return QMLG_E_WORKSPACE;
+    cudaStream_t s = qmlg::as_stream(stream);
+    BatchBufs b{};
+    std::vector<BatchFit> fits;
+    fits.reserve((size_t)count);
+    batch_carve(problems, count, d, static_cast<char *>(workspace), b, &fits);
+    const int RK = std::max(b.RK, 128), RT = std::max(b.RT, 128);
+    static std::once_flag once;
+    static cudaError_t attr = cudaSuccess;
+    std::call_once(once, [] {
+        attr = cudaFuncSetAttribute(trsm_group_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)trsm_smem(TRSM_MAX_ROWS));
+    });
+    if (attr != cudaSuccess) return qmlg::set_cuda_error(attr);
+    static BatchLauncher L;  // 18 KB of staging, kept off the stack
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lock(mu);
+    cudaError_t e = cudaMemsetAsync(b.err, 0, sizeof(int), s);
+    for (int p = 0; p < count && e == cudaSuccess; ++p)
+        e = cudaMemsetAsync(problems[p].status, 0, 2 * sizeof(int), s);
+    if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+
+    // one grouped launch; `fill` sets a problem's entry (returns its CTA count, 0 = skip)
+    auto run = [&](auto launch, auto fill) -> int {
+        L.begin();
+        for (BatchFit &f : fits) {
+            BatchEntry tmp{};
+            const int ctas = fill(f, tmp);
+            if (ctas <= 0) continue;
+            BatchEntry *en = L.add(ctas);
+            const int base = en->cta_base;
+            *en = tmp;
+            en->cta_base = base;
+            en->ctas = ctas;
+        }
+        if (L.total == 0) return QMLG_OK;
+        launch(L.total);
+        qmlg::count_launches(1);
+        return qmlg::check_launch();
+    };
+    auto base_entry = [&](const BatchFit &f, BatchEntry &en) {
+        en.A = f.q->K;
+        en.lda = f.n;
+        en.n = f.n;
+        en.lambda = f.q->lambda;
+        en.status = f.q->status;
+        en.Linv = f.linv;
+        en.y = f.q->y;
+        en.r = f.r;
+        en.diag = f.diag;
+        en.partial = f.partial;
+        en.sums = f.sums;
+        en.correction = f.q->correction;
+    };
+    auto vec = [&](int op, auto ctas_of, double *(*xsel)(const BatchFit &)) -> int {
+        return run([&](int grid) { vec_group_kernel<<<grid, 256, 0, s>>>(L.g, op, b.err); },
+                   [&](const BatchFit &f, BatchEntry &en) {
+                       base_entry(f, en);
+                       en.x = xsel(f);
+                       return ctas_of(f);
+                   });
+    };
+    auto per_256 = [](const BatchFit &f) { return (int)qmlg::ceil_div(f.n, 256); };
+    auto one = [](const BatchFit &) { return 1; };
+    int st = QMLG_OK;
+
+    // ---- kernel matrices
+    std::vector<qmlg::GaussItem> gi;
+    for (BatchFit &f : fits) {
+        const QmlgBatchProblem &q = *f.q;
+        if (q.kind == QMLG_KIND_GAUSSIAN)
+            gi.push_back(qmlg::GaussItem{q.X, q.ldx, f.n, q.sigma, q.K, (int64_t)f.n, f.row_k,
+                                         q.status + 1});
+    }
+    st = qmlg::gauss_group_kernel_matrix(gi.data(), (int)gi.size(), d, b.kdig, b.kexp, b.knorm,
+                                         b.maxbuf, RK, b.err, s);
+    for (BatchFit &f : fits) {
+        if (st != QMLG_OK) return st;
+        const QmlgBatchProblem &q = *f.q;
+        if (q.kind == QMLG_KIND_LAPLACIAN)
+            st = qmlg_laplacian_kernel_fixed_async(q.X, q.ldx, f.n, q.X, q.ldx, f.n, d, q.sigma, q.K,
+                                                   f.n, QMLG_KERNEL_SYMMETRIC, 0.0, q.status + 1,
+                                                   f.lws, f.lws_bytes, stream);
+    }
+    if (st != QMLG_OK) return st;
+    st = vec(kCopyDiag, per_256, [](const BatchFit &f) { return f.r; });
+    if (st != QMLG_OK) return st;
+
+    // ---- factorisation, lockstep over 64-column steps
+    int maxn = 0;
+    for (const BatchFit &f : fits) maxn = std::max(maxn, f.n);
+    std::vector<qmlg::GroupItem> items;
+    std::vector<qmlg::SliceItem> slices;
+    for (int k0 = 0; k0 < maxn && st == QMLG_OK; k0 += NB) {
+        const int kb = k0 / NB, r1 = k0 + NB, K0 = k0 / qmlg::NBO * qmlg::NBO;
+        st = run([&](int grid) { potrf_group_kernel<<<grid, POTRF_THREADS, 0, s>>>(L.g); },
+                 [&](const BatchFit &f, BatchEntry &en) {
+                     if (f.n <= k0) return 0;
+                     base_entry(f, en);
+                     en.k = kb;
+                     return 1;
+                 });
+        if (st != QMLG_OK) break;
+        st = run([&](int grid) {
+                     trsm_group_kernel<<<grid, 4 * trsm_rows, trsm_smem(trsm_rows), s>>>(
+                         L.g, qmlg::kEmuMaxSlices, RT);
+                 },
+                 [&](const BatchFit &f, BatchEntry &en) {
+                     if (f.n <= r1) return 0;
+                     const int K1 = std::min(K0 + qmlg::NBO, f.n);
+                     const bool inner = r1 < K1;
+                     base_entry(f, en);
+                     en.k = kb;
+                     en.drows = inner ? std::min(qmlg::plane_rows(f.n),
+                                                 (int)qmlg::ceil_div(f.n - r1, 128) * 128)
+                                      : 0;
+                     en.digits = inner ? b.idig + (size_t)f.row_p * NB : nullptr;
+                     en.expo = inner ? b.iexp + f.row_p : nullptr;
+                     const int rows = inner ? en.drows : f.n - r1;
+                     return (int)qmlg::ceil_div(rows, trsm_rows);
+                 });
+        if (st != QMLG_OK) break;
+        items.clear();
+        for (const BatchFit &f : fits) {
+            const int K1 = std::min(K0 + qmlg::NBO, f.n);
+            if (f.n > r1 && r1 < K1)
+                items.push_back(qmlg::GroupItem{f.q->K, (int64_t)f.n, r1, K1, r1, f.n, f.row_p,
+                                                f.row_p, 0.0});
+        }
+        st = qmlg::emu_tc_group_update(items.data(), (int)items.size(), b.idig, b.iexp, NB, RT,
+                                       qmlg::kEmuMaxSlices, b.err, s, tile_cols);
+        if (st != QMLG_OK || r1 % qmlg::NBO != 0) continue;
+        // the end of a 512-column panel: its digit planes, then every trailing update
+        slices.clear();
+        items.clear();
+        for (const BatchFit &f : fits) {
+            if (f.n <= r1) continue;
+            slices.push_back(qmlg::SliceItem{f.q->K, (int64_t)f.n, r1, f.n - r1, K0, qmlg::NBO, f.row_p,
+                                             f.q->status});
+            items.push_back(qmlg::GroupItem{f.q->K, (int64_t)f.n, r1, f.n, r1, f.n, f.row_p,
+                                            f.row_p, 0.0});
+        }
+        st = qmlg::slice_rows_group(slices.data(), (int)slices.size(), qmlg::NBO, RT,
+                                    qmlg::kEmuMaxSlices, b.pdig, b.pexp, s);
+        if (st == QMLG_OK)
+            st = qmlg::emu_tc_group_update(items.data(), (int)items.size(), b.pdig, b.pexp, qmlg::NBO,
+                                           RT, qmlg::kEmuMaxSlices, b.err, s, tile_cols);
+    }
+    if (st != QMLG_OK) return st;
+    st = run([&](int grid) { invert_group_kernel<<<grid, 64, 0, s>>>(L.g); },
+             [&](const BatchFit &f, BatchEntry &en) {
+                 base_entry(f, en);
+                 return f.nblk;
+             });
+    if (st != QMLG_OK) return st;
+
+    // ---- solves: alpha = y, L L^T alpha = y, then refine_steps refinement steps
+    int maxblk = 0;
+    for (const BatchFit &f : fits) maxblk = std::max(maxblk, f.nblk);
+    const int cap = 4 * std::max(1, qmlg::tc_sm_count());
+    auto solve = [&](double *(*xsel)(const BatchFit &)) -> int {
+        int rc = QMLG_OK;
+        for (int t = 0; t < maxblk && rc == QMLG_OK; ++t)
+            rc = run([&](int grid) { fwd_group_kernel<<<grid, STEP_THREADS, 0, s>>>(L.g); },
+                     [&](const BatchFit &f, BatchEntry &en) {
+                         if (t >= f.nblk) return 0;
+                         base_entry(f, en);
+                         en.x = xsel(f);
+                         en.k = t;
+                         const int below = f.n - (t + 1) * NB;
+                         return 1 + ((t > 0 && below > 0)
+                                         ? (int)std::min<int64_t>(qmlg::ceil_div(below, 32), cap)
+                                         : 0);
+                     });
+        for (int t = 0; t < maxblk && rc == QMLG_OK; ++t)
+            rc = run([&](int grid) { bwd_group_kernel<<<grid, STEP_THREADS, 0, s>>>(L.g); },
+                     [&](const BatchFit &f, BatchEntry &en) {
+                         if (t >= f.nblk) return 0;
+                         const int k = f.nblk - 1 - t;
+                         base_entry(f, en);
+                         en.x = xsel(f);
+                         en.k = k;
+                         return 1 + ((k + 1 < f.nblk && k > 0)
+                                         ? (int)std::min<int64_t>(qmlg::ceil_div(k * NB, 64), cap)
+                                         : 0);
+                     });
+        return rc;
+    };
+    auto sel_alpha = [](const BatchFit &f) { return f.q->alpha; };
+    auto sel_r = [](const BatchFit &f) { return f.r; };
+    st = vec(kCopyY, per_256, sel_alpha);
+    if (st == QMLG_OK) st = solve(sel_alpha);
+    for (int it = 0; it < refine_steps && st == QMLG_OK; ++it) {
+        st = run([&](int grid) { symv_group_kernel<<<grid, 256, 0, s>>>(L.g); },
+                 [&](const BatchFit &f, BatchEntry &en) {
+                     base_entry(f, en);
+                     en.x = f.q->alpha;
+                     return (int)(qmlg::ceil_div(f.n, RES_ROWS) * qmlg::ceil_div(f.n, RES_CHUNK));
+                 });
+        if (st == QMLG_OK)
+            st = run([&](int grid) { finish_group_kernel<<<grid, 256, 0, s>>>(L.g); },
+                     [&](const BatchFit &f, BatchEntry &en) {
+                         base_entry(f, en);
+                         en.x = f.q->alpha;
+                         return (int)qmlg::ceil_div(f.n, 256);
+                     });
+        if (st == QMLG_OK) st = solve(sel_r);
+        if (st == QMLG_OK) st = vec(kZeroSums, one, sel_alpha);
+        if (st == QMLG_OK)
+            st = run([&](int grid) { axpy_group_kernel<<<grid, 256, 0, s>>>(L.g); },
+                     [&](const BatchFit &f, BatchEntry &en) {
+                         base_entry(f, en);
+                         en.x = f.q->alpha;
+                         return (int)qmlg::ceil_div(f.n, 256);
+                     });
+    }
+    if (st == QMLG_OK) st = vec(kFinishFlags, one, sel_alpha);
+    return st;
 }

@@ -22,6 +22,10 @@ namespace qmlg {
 
 constexpr int kEmuMaxSlices = 8;
 
+// Rows reserved per problem in a shared plane buffer, and the padded feature width.
+inline int plane_rows(int n) { return (int)ceil_div(n < 1 ? 1 : n, 128) * 128; }
+inline int plane_cols(int d) { return (int)ceil_div(d < 1 ? 1 : d, 64) * 64; }
+
 // tcgen05 path (emulated_tc.cu).
 // Digit planes of rows r0 .. r0+nrows-1, columns c0 .. c0+kw-1 of a row-major matrix:
 // digits [slices][rpad][kp] bf16 (kp a multiple of 64, zero-padded), expo [rpad].
@@ -39,6 +43,58 @@ int emu_tc_update(double *C, int64_t ldc, int jbase, int jend, int ibase, int ie
                   int a_row0, int b_row0, int lower, int *d_err, cudaStream_t s, int max_ctas = 0);
 // SM count of the current device, after the calling thread's cap.
 int tc_sm_count();
+
+// Grouped launches: the tiles of many independent problems in one persistent launch
+// (groups of up to 128 problems per launch).  Every problem's digit rows lie in one
+// shared plane buffer: planes [slices][rows_total][kp] bf16, exponents [rows_total].
+struct GroupItem {
+    double *C;            // row-major C of the trailing update / column-major K
+    int64_t ldc;
+    int jbase, jend;      // lanes: contiguous index range of C
+    int ibase, iend;      // TMEM columns
+    int a_row0, b_row0;   // digit rows of j = jbase and i = ibase in the shared buffer
+    double scale;         // Gaussian: -0.5 / sigma^2 (unused by the update)
+};
+// C_g[i][j] -= sum_k P[i][k] P[j][k] on the lower triangle (j <= i) of each item's
+// range, K = kp <= 512 for all items.
+// tile_cols: i-columns per tile, 64 (one TMEM accumulator) or 32 (two).
+int emu_tc_group_update(const GroupItem *items, int count, const __nv_bfloat16 *digits,
+                        const int *expo, int kp, int rows_total, int slices, int *d_err,
+                        cudaStream_t s, int tile_cols = 64);
+
+// Digit planes of many problems' row blocks in one launch, each into the shared plane
+// buffer at its row0 (plane_rows(nrows) rows reserved): rows r0 .. r0+nrows-1,
+// columns c0 .. c0+kw-1 of its row-major A, as slice_rows does.  info (may be null):
+// nothing is done for a problem whose factorisation has failed.
+struct SliceItem {
+    const double *A;
+    int64_t lda;
+    int r0, nrows, c0, kw;
+    int row0;
+    const int *info;
+};
+int slice_rows_group(const SliceItem *items, int count, int kp, int rows_total, int slices,
+                     __nv_bfloat16 *digits, int *expo, cudaStream_t s);
+
+// Symmetric Gaussian kernel matrices of many problems, K = exp(-|x_i - x_j|^2 /
+// (2 sigma^2)) in each problem's column-major K (ldk), K_ii = 1, with 8 digit planes:
+// each problem's rows are sliced into the shared buffer at row0 (rows_pad(n) rows
+// reserved; norms [rows_total] receive |x|^2), its 1e-12 bound is checked on the
+// device (8 ORed into *flag when not met), then one grouped launch forms every K.
+struct GaussItem {
+    const double *X;
+    int64_t ldx;
+    int n;
+    double sigma;
+    double *K;
+    int64_t ldk;
+    int row0;
+    int *flag;
+};
+int gauss_group_kernel_matrix(const GaussItem *items, int count, int d, __nv_bfloat16 *digits,
+                              int *expo, double *norms, unsigned long long *maxbuf,
+                              int rows_total, int *d_err, cudaStream_t s);
+
 
 // In-place factor with emulated trailing updates; storage as the FP64 factor.
 struct EmulatedFactor {

@@ -29,6 +29,7 @@
 #include <cmath>
 #include <cstring>
 #include <mutex>
+#include <vector>
 
 #include "common.cuh"
 #include "emulated_gemm.cuh"
@@ -50,18 +51,21 @@ constexpr int A_BYTES = TM * KC * 2;  // 16 KB
 
 enum Mode { kSyrk = 0, kKernelMatrix = 1, kPredict = 2 };
 
-// Tile shape per mode.  The trailing update (memory-heavy epilogue, operand reuse
-// matters) takes 64 i-columns per level: 8 levels fill TMEM's 512 columns, one
-// accumulator.  The Gaussian epilogues (FP64-bound) take 32 i-columns, so two
-// accumulators fit and one tile's MMAs run while the epilogue drains the other;
-// their B buffers are half as large, which leaves room for a deeper A ring.
-template <int MODE>
+// Tile shapes.  TN = 64 i-columns per level: 8 levels fill TMEM's 512 columns, one
+// accumulator, so the next tile's MMAs wait for the epilogue's level merge; each A
+// tile (128 rows x 8 planes) feeds 64 columns.  TN = 32: two accumulators, one
+// tile's MMAs run while the epilogue drains the other, the B buffers are half as
+// large (room for a deeper A ring), but each A tile feeds half as many outputs.
+// The trailing update takes 64 (at 39488^2 x 512: 1501 TF/s against 1083 with 32,
+// where the operand feed sets the pace); the FP64-bound Gaussian epilogues take 32.
+// Grouped launches can take either (a batch autotuner chooses).
+template <int MODE, int TN_ = (MODE == kSyrk ? 64 : 32)>
 struct Shape {
-    static constexpr int TN = MODE == kSyrk ? 64 : 32;  // i columns per level
-    static constexpr int NBUF = MODE == kSyrk ? 1 : 2;  // accumulators in TMEM
-    static constexpr int A_STAGES = MODE == kSyrk ? 5 : 9;
+    static constexpr int TN = TN_;                  // i columns per level
+    static constexpr int NBUF = TN_ == 64 ? 1 : 2;  // accumulators in TMEM
+    static constexpr int A_STAGES = TN_ == 64 ? 5 : 9;
     static constexpr int B_BYTES = TN * KC * 2;
-    static constexpr int TBUF = 8 * TN;                 // TMEM columns per accumulator
+    static constexpr int TBUF = 8 * TN;             // TMEM columns per accumulator
 };
 constexpr int RED_BYTES = 4 * 64 * 8;  // predict: per-warp column sums
 constexpr int SMEM_BYTES = 2 * S_MAX * Shape<kSyrk>::B_BYTES + Shape<kSyrk>::A_STAGES * A_BYTES +
@@ -261,12 +265,82 @@ __device__ __forceinline__ double exp_nonpos(double x)
     return __longlong_as_double(__double_as_longlong(v) + ((long long)(n >> 7) << 52));
 }
 
-template <int MODE>
-__global__ void __launch_bounds__(THREADS, 1)
-emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
-              TileArgs p)
+// Grouped launches: the tiles of up to kMaxGroup independent problems in one
+// persistent launch.  The problems share the two tensor maps (their digit rows lie at
+// different offsets of one plane buffer), K width, plane count and the per-row
+// arrays; each has its own output, ranges, digit-row offsets and Gaussian scale.
+// Problem g owns tiles [tile_base, tile_base + its count) of the launch's list, in
+// the order of its own tile cursor.
+constexpr int kMaxGroup = 128;
+
+struct GroupEntry {
+    double *C;
+    int64_t ldc;
+    double scale;
+    int jbase, jend, ibase, iend;
+    int a_row0, b_row0;
+    int tj, tile_base;
+};
+
+struct TileGroup {
+    int count, pad;
+    GroupEntry e[kMaxGroup];
+};
+
+// Maps a tile index to (jt, itl) and returns the arguments that hold for that tile:
+// the launch's own, or (grouped) a copy with its problem's fields.  A CTA visits its
+// tiles in increasing order, so the problem index only grows and each problem's
+// cursor starts fresh.
+template <int TN, bool GROUPED>
+struct TileWalker;
+
+template <int TN>
+struct TileWalker<TN, false> {
+    TileCursor<TN> cur;
+    __device__ __forceinline__ const TileArgs &locate(const TileArgs &p, const TileGroup *, int t,
+                                                      int &jt, int &itl)
+    {
+        cur.locate(p, t, jt, itl);
+        return p;
+    }
+};
+
+template <int TN>
+struct TileWalker<TN, true> {
+    TileCursor<TN> cur;
+    int g = -1;
+    TileArgs q;
+    __device__ __forceinline__ const TileArgs &locate(const TileArgs &p, const TileGroup *grp, int t,
+                                                      int &jt, int &itl)
+    {
+        int gg = g < 0 ? 0 : g;
+        while (gg + 1 < grp->count && grp->e[gg + 1].tile_base <= t) ++gg;
+        if (gg != g) {
+            const GroupEntry &e = grp->e[gg];
+            g = gg;
+            cur = TileCursor<TN>();
+            q = p;
+            q.C = e.C;
+            q.ldc = e.ldc;
+            q.scale = e.scale;
+            q.jbase = e.jbase;
+            q.jend = e.jend;
+            q.ibase = e.ibase;
+            q.iend = e.iend;
+            q.a_row0 = e.a_row0;
+            q.b_row0 = e.b_row0;
+            q.tj = e.tj;
+        }
+        cur.locate(q, t - grp->e[g].tile_base, jt, itl);
+        return q;
+    }
+};
+
+template <int MODE, bool GROUPED, int TNX = Shape<MODE>::TN>
+__device__ __forceinline__ void emu_tc_body(const CUtensorMap &mapA, const CUtensorMap &mapB,
+                                            const TileArgs &p, const TileGroup *grp)
 {
-    using SH = Shape<MODE>;
+    using SH = Shape<MODE, TNX>;
     constexpr int TN = SH::TN, A_STAGES = SH::A_STAGES, B_BYTES = SH::B_BYTES, TBUF = SH::TBUF;
     extern __shared__ unsigned char smem_raw[];
     unsigned char *base =
@@ -312,7 +386,7 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
             // ---------------- TMA producer: runs ahead across tiles.  The i-planes of
             // chunk g+1 are requested halfway through the j-planes of chunk g, so they
             // are in flight while chunk g's MMAs run.
-            TileCursor<TN> cur, nxt;
+            TileWalker<TN, GROUPED> cur, nxt;
             int g = 0, it = 0;
             bool ok = true;
             int b_issued = -1;  // highest chunk index whose i-planes are requested
@@ -327,15 +401,15 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
             };
             for (int t = blockIdx.x; t < p.ntiles && ok; t += gridDim.x) {
                 int jt, itl;
-                cur.locate(p, t, jt, itl);
-                const int arow = p.a_row0 + jt * TM, brow = p.b_row0 + itl * TN;
+                const TileArgs &pt = cur.locate(p, grp, t, jt, itl);
+                const int arow = pt.a_row0 + jt * TM, brow = pt.b_row0 + itl * TN;
                 // the chunk after this tile's last one belongs to the next tile
                 int brow_next = -1;
                 if (t + (int)gridDim.x < p.ntiles) {
                     int jt2, it2;
                     nxt = cur;
-                    nxt.locate(p, t + gridDim.x, jt2, it2);
-                    brow_next = p.b_row0 + it2 * TN;
+                    const TileArgs &pn = nxt.locate(p, grp, t + gridDim.x, jt2, it2);
+                    brow_next = pn.b_row0 + it2 * TN;
                 }
                 for (int c = 0; c < p.kchunks && ok; ++c, ++g) {
                     if (b_issued < g && !issue_b(g, brow, c)) {
@@ -426,38 +500,38 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
         const int lo_levels = S - H;
         const int shift = lo_levels >= 2 ? 12 : 0;
         const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
-        TileCursor<TN> cur;
+        TileWalker<TN, GROUPED> cur;
         int u = 0;
         bool ok = true;
         for (int t = blockIdx.x; t < p.ntiles; t += gridDim.x, ++u) {
             int jt, itl;
-            cur.locate(p, t, jt, itl);
-            const int j0 = p.jbase + jt * TM, i0 = p.ibase + itl * TN;
-            const int arow = p.a_row0 + jt * TM, brow = p.b_row0 + itl * TN;
+            const TileArgs &pt = cur.locate(p, grp, t, jt, itl);
+            const int j0 = pt.jbase + jt * TM, i0 = pt.ibase + itl * TN;
+            const int arow = pt.a_row0 + jt * TM, brow = pt.b_row0 + itl * TN;
             const int j = j0 + jl;
             const int tb = SH::NBUF == 2 ? (u & 1) : 0, use = SH::NBUF == 2 ? (u >> 1) : u;
             const uint32_t tbuf = lane_base + (uint32_t)(tb * TBUF);  // this tile's accumulator
             // every (j, i) of the tile is inside the updated range
-            const bool interior = j0 + TM <= p.jend && i0 + TN <= p.iend &&
+            const bool interior = j0 + TM <= pt.jend && i0 + TN <= pt.iend &&
                                   (!p.lower || j0 + TM - 1 <= i0);
-            if (MODE == kSyrk && j < p.jend) {
+            if (MODE == kSyrk && j < pt.jend) {
                 // while the MMAs run, pull this thread's part of C into L2 so the
                 // read-modify-write below does not wait on DRAM
-                const int ilo = i0 + h * HC, ilim = min(ilo + HC, p.iend);
+                const int ilo = i0 + h * HC, ilim = min(ilo + HC, pt.iend);
                 for (int i = ilo; i < ilim; ++i)
                     if (interior || !p.lower || j <= i)
-                        asm volatile("prefetch.global.L2 [%0];" ::"l"(p.C + (int64_t)i * p.ldc + j));
+                        asm volatile("prefetch.global.L2 [%0];" ::"l"(pt.C + (int64_t)i * pt.ldc + j));
             }
             if (ok && !mbar_wait(&tFull[tb], use & 1)) {
                 ok = false;
                 if (lane == 0) atomicOr(p.err, 4);
             }
             fence_after_sync();
-            const bool jvalid = j < p.jend;
+            const bool jvalid = j < pt.jend;
             const int ej = jvalid ? p.expA[arow + jl] : 0;
             double aj = 0.0, aw = 0.0;
             if (MODE != kSyrk && jvalid) {
-                aj = p.scale * p.normA[arow + jl];
+                aj = pt.scale * p.normA[arow + jl];
                 if (MODE == kPredict) aw = p.alpha[j];
             }
             // Levels of eight columns -> exact integers (value in units of 2^(shift -
@@ -515,16 +589,16 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
 #pragma unroll
                         for (int col = 0; col < EG; ++col) {
                             const int i = i0 + cb + col;
-                            cv[col] = (interior || (jvalid && i < p.iend && (!p.lower || j <= i)))
-                                          ? p.C[(int64_t)i * p.ldc + j] : 0.0;
+                            cv[col] = (interior || (jvalid && i < pt.iend && (!p.lower || j <= i)))
+                                          ? pt.C[(int64_t)i * pt.ldc + j] : 0.0;
                         }
 #pragma unroll
                         for (int col = 0; col < EG; ++col) {
                             const int il = cb + col;
                             const int i = i0 + il;
-                            if (interior || (jvalid && i < p.iend && (!p.lower || j <= i))) {
+                            if (interior || (jvalid && i < pt.iend && (!p.lower || j <= i))) {
                                 const double sc = pow2i(p.expB[brow + il] + ej + shift - 7 * (S + 1));
-                                p.C[(int64_t)i * p.ldc + j] = fma(-(double)v64[gq * EG + col], sc, cv[col]);
+                                pt.C[(int64_t)i * pt.ldc + j] = fma(-(double)v64[gq * EG + col], sc, cv[col]);
                             }
                         }
                     }
@@ -535,10 +609,10 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
                 // terms (scale |b|^2, b's exponent) are loaded once per tile by the lane
                 // of that column and broadcast; -2 scale 2^e is formed on the bits.
                 const int ibl = i0 + h * HC + lane;
-                const bool ilv = lane < HC && ibl < p.iend;
-                const double sBl = ilv ? p.scale * p.normB[brow + h * HC + lane] : 0.0;
+                const bool ilv = lane < HC && ibl < pt.iend;
+                const double sBl = ilv ? pt.scale * p.normB[brow + h * HC + lane] : 0.0;
                 const int eBl = ilv ? p.expB[brow + h * HC + lane] : 0;
-                const double m2s = -2.0 * p.scale;
+                const double m2s = -2.0 * pt.scale;
                 const long long m2s_bits = __double_as_longlong(m2s);
                 const int m2s_exp = (int)((m2s_bits >> 52) & 0x7ff);
                 double cs[HC];  // kPredict: this thread's k(a_j, b_i) alpha_j, i = column
@@ -565,7 +639,7 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
                         const int i = i0 + il;
                         const double sb = __shfl_sync(0xffffffffu, sBl, gq * EG + col);
                         const int eb = __shfl_sync(0xffffffffu, eBl, gq * EG + col);
-                        const bool valid = jvalid && i < p.iend;
+                        const bool valid = jvalid && i < pt.iend;
                         double kv = 0.0;
                         if (valid) {
                             // x = scale * (|a|^2 + |b|^2 - 2 a.b)
@@ -579,8 +653,8 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
                         }
                         if (MODE == kKernelMatrix) {
                             if (valid && (!p.lower || j <= i)) {
-                                p.C[(int64_t)i * p.ldc + j] = kv;
-                                if (p.lower && j < i) p.C[(int64_t)j * p.ldc + i] = kv;
+                                pt.C[(int64_t)i * pt.ldc + j] = kv;
+                                if (p.lower && j < i) pt.C[(int64_t)j * pt.ldc + i] = kv;
                             }
                         } else {
                             cs[gq * EG + col] = valid ? kv * aw : 0.0;
@@ -613,8 +687,8 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
                 // the four quarters' column sums are added in a fixed order
                 asm volatile("bar.sync 1, %0;" ::"n"(EPI_THREADS) : "memory");
                 const int tt = threadIdx.x - 64;
-                if (ok && tt < TN && i0 + tt < p.iend)
-                    p.partial[(int64_t)jt * (p.iend - p.ibase) + (i0 - p.ibase) + tt] =
+                if (ok && tt < TN && i0 + tt < pt.iend)
+                    p.partial[(int64_t)jt * (pt.iend - pt.ibase) + (i0 - pt.ibase) + tt] =
                         ((red[0][tt] + red[1][tt]) + red[2][tt]) + red[3][tt];
                 asm volatile("bar.sync 1, %0;" ::"n"(EPI_THREADS) : "memory");
             }
@@ -625,6 +699,23 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
     if (warp == 1) tmem_dealloc(tmem, 512);
 }
 
+template <int MODE>
+__global__ void __launch_bounds__(THREADS, 1)
+emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+              const __grid_constant__ TileArgs p)
+{
+    emu_tc_body<MODE, false>(mapA, mapB, p, nullptr);
+}
+
+template <int MODE, int TNX = Shape<MODE>::TN>
+__global__ void __launch_bounds__(THREADS, 1)
+emu_tc_group_kernel(const __grid_constant__ CUtensorMap mapA,
+                    const __grid_constant__ CUtensorMap mapB, const __grid_constant__ TileArgs p,
+                    const __grid_constant__ TileGroup grp)
+{
+    emu_tc_body<MODE, true, TNX>(mapA, mapB, p, &grp);
+}
+
 // One warp per row: power-of-two row scale over the K-range and S digit planes.
 // src rows r0 .. r0+nrows-1, columns c0 .. c0+kw-1 of the row-major matrix;
 // digits [S][rpad][kp] bf16 (zero beyond kw and beyond nrows), expo [rpad].
@@ -632,13 +723,13 @@ emu_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
 // (|q| <= 2^(7S-1)), then split into balanced base-128 digits with integer shifts,
 // least significant first: d = ((q + 64) mod 128) - 64, q <- (q - d) / 128; the most
 // significant digit takes what is left, which is at most 64 in magnitude.
-__global__ void slice_rows_kernel(const double *__restrict__ A, int64_t lda, int r0, int nrows,
-                                  int c0, int kw, int kp, int rpad, int slices,
-                                  __nv_bfloat16 *__restrict__ digits, int *__restrict__ expo,
-                                  double *__restrict__ norms, const int *__restrict__ info)
+__device__ __forceinline__ void slice_row(const double *__restrict__ A, int64_t lda, int r0,
+                                          int nrows, int c0, int kw, int kp, int rpad, int slices,
+                                          __nv_bfloat16 *__restrict__ digits,
+                                          int *__restrict__ expo, double *__restrict__ norms,
+                                          const int *__restrict__ info, int warp)
 {
     if (info != nullptr && *info != 0) return;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (warp >= rpad) return;
     const bool live = warp < nrows;
@@ -706,6 +797,49 @@ __global__ void slice_rows_kernel(const double *__restrict__ A, int64_t lda, int
         }
     }
     if (lane == 0) expo[warp] = e;
+}
+
+__global__ void slice_rows_kernel(const double *__restrict__ A, int64_t lda, int r0, int nrows,
+                                  int c0, int kw, int kp, int rpad, int slices,
+                                  __nv_bfloat16 *__restrict__ digits, int *__restrict__ expo,
+                                  double *__restrict__ norms, const int *__restrict__ info)
+{
+    slice_row(A, lda, r0, nrows, c0, kw, kp, rpad, slices, digits, expo, norms, info,
+              (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5));
+}
+
+// Rows of many problems sliced into one shared plane buffer in one launch: problem g
+// owns warps [warp_base, warp_base + its rows padded to 128) and its digit rows start
+// at row0 (the plane stride is the shared buffer's row count).
+struct SliceEntry {
+    const double *A;
+    int64_t lda;
+    int r0, nrows, c0, kw;
+    int row0, warp_base;
+    const int *info;
+};
+
+struct SliceGroup {
+    int count, pad;
+    SliceEntry e[kMaxGroup];
+};
+
+__global__ void slice_rows_group_kernel(const __grid_constant__ SliceGroup g, int kp, int rows_total,
+                                        int slices, __nv_bfloat16 *__restrict__ digits,
+                                        int *__restrict__ expo)
+{
+    const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    int lo = 0, hi = g.count - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (g.e[mid].warp_base <= warp) lo = mid;
+        else hi = mid - 1;
+    }
+    const SliceEntry &e = g.e[lo];
+    const int w = warp - e.warp_base;
+    if (w < 0 || w >= (e.nrows + 127) / 128 * 128) return;
+    slice_row(e.A, e.lda, e.r0, e.nrows, e.c0, e.kw, kp, rows_total, slices,
+              digits + (int64_t)e.row0 * kp, expo + e.row0, nullptr, e.info, w);
 }
 
 typedef CUresult (*EncodeFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
@@ -1309,3 +1443,199 @@ extern "C" int qmlg_gaussian_kernel_emulated_async(const double *A, int64_t lda,
     qmlg::count_launches(1);
     return qmlg::check_launch();
 }
+
+// -------------------------------------------------------- grouped launches --
+
+namespace {
+
+// The 1e-12 bound of a symmetric Gaussian K from the one max |x| of its rows.
+__global__ void bound_check_sym_kernel(const unsigned long long *__restrict__ maxbits, int kp,
+                                       double sigma, int *__restrict__ flag)
+{
+    const double m = __longlong_as_double((long long)maxbits[0]);
+    if (!isfinite(m)) {
+        atomicOr(flag, 8);
+        return;
+    }
+    int e = 0;
+    if (m > 0.0) frexp(m, &e);
+    const double bound = ldexp(1.0, 2 * (e + 1) - 7 * S_MAX) * kp * (S_MAX + 1) / 4.0;
+    if (bound / (sigma * sigma) > 0.5e-12) atomicOr(flag, 8);
+}
+
+void set_group_smem_attrs()
+{
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaFuncSetAttribute(emu_tc_group_kernel<kSyrk>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+        cudaFuncSetAttribute(emu_tc_group_kernel<kSyrk, 32>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+        cudaFuncSetAttribute(emu_tc_group_kernel<kKernelMatrix>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    });
+}
+
+// Launches the items' tiles in groups of at most kMaxGroup problems.
+template <int MODE, int TN = Shape<MODE>::TN>
+int launch_group(const qmlg::GroupItem *items, int count, const CUtensorMap &mA,
+                 const CUtensorMap &mB, const TileArgs &base, cudaStream_t s)
+{
+    set_group_smem_attrs();
+    static TileGroup grp;  // host staging of the kernel parameter (copied at launch)
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lock(mu);
+    for (int first = 0; first < count; first += kMaxGroup) {
+        const int m = std::min(kMaxGroup, count - first);
+        int total = 0;
+        grp.count = m;
+        for (int k = 0; k < m; ++k) {
+            const qmlg::GroupItem &it = items[first + k];
+            GroupEntry &e = grp.e[k];
+            int tj = 0;
+            const int nt = (it.jend > it.jbase && it.iend > it.ibase)
+                               ? count_tiles(it.jbase, it.jend, it.ibase, it.iend, 1, TN, tj)
+                               : 0;
+            e.C = it.C;
+            e.ldc = it.ldc;
+            e.scale = it.scale;
+            e.jbase = it.jbase;
+            e.jend = it.jend;
+            e.ibase = it.ibase;
+            e.iend = it.iend;
+            e.a_row0 = it.a_row0;
+            e.b_row0 = it.b_row0;
+            e.tj = tj;
+            e.tile_base = total;
+            total += nt;
+        }
+        if (total == 0) continue;
+        TileArgs a = base;
+        a.ntiles = total;
+        emu_tc_group_kernel<MODE, TN><<<tile_grid(total), THREADS, SMEM_BYTES, s>>>(mA, mB, a, grp);
+        qmlg::count_launches(1);
+        const int st = qmlg::check_launch();
+        if (st != QMLG_OK) return st;
+    }
+    return QMLG_OK;
+}
+
+}  // namespace
+
+namespace qmlg {
+
+int emu_tc_group_update(const GroupItem *items, int count, const __nv_bfloat16 *digits,
+                        const int *expo, int kp, int rows_total, int slices, int *d_err,
+                        cudaStream_t s, int tile_cols)
+{
+    if (count <= 0) return QMLG_OK;
+    if (items == nullptr || slices < 1 || slices > S_MAX || kp % KC != 0 || kp / KC > 8 ||
+        rows_total < 1 || (tile_cols != 32 && tile_cols != 64))
+        return QMLG_E_ARG;
+    CUtensorMap mA, mB;
+    int st = make_plane_map(&mA, digits, kp, rows_total, slices, TM);
+    if (st == QMLG_OK) st = make_plane_map(&mB, digits, kp, rows_total, slices, tile_cols);
+    if (st != QMLG_OK) return st;
+    TileArgs a{};
+    a.kchunks = kp / KC;
+    a.slices = slices;
+    a.expA = expo;
+    a.expB = expo;
+    a.lower = 1;
+    a.err = d_err;
+    return tile_cols == 32 ? launch_group<kSyrk, 32>(items, count, mA, mB, a, s)
+                           : launch_group<kSyrk, 64>(items, count, mA, mB, a, s);
+}
+
+int slice_rows_group(const SliceItem *items, int count, int kp, int rows_total, int slices,
+                     __nv_bfloat16 *digits, int *expo, cudaStream_t s)
+{
+    if (count <= 0) return QMLG_OK;
+    if (items == nullptr || slices < 1 || slices > S_MAX || kp % KC != 0 || rows_total < 1)
+        return QMLG_E_ARG;
+    static SliceGroup g;  // host staging of the kernel parameter (copied at launch)
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lock(mu);
+    for (int first = 0; first < count; first += kMaxGroup) {
+        const int m = std::min(kMaxGroup, count - first);
+        int warps = 0, used = 0;
+        for (int k = 0; k < m; ++k) {
+            const SliceItem &it = items[first + k];
+            if (it.nrows <= 0) continue;
+            if (it.kw > kp || it.row0 < 0 || it.row0 + plane_rows(it.nrows) > rows_total)
+                return QMLG_E_ARG;
+            SliceEntry &e = g.e[used++];
+            e.A = it.A;
+            e.lda = it.lda;
+            e.r0 = it.r0;
+            e.nrows = it.nrows;
+            e.c0 = it.c0;
+            e.kw = it.kw;
+            e.row0 = it.row0;
+            e.warp_base = warps;
+            e.info = it.info;
+            warps += plane_rows(it.nrows);
+        }
+        if (used == 0) continue;
+        g.count = used;
+        slice_rows_group_kernel<<<(unsigned)ceil_div((int64_t)warps * 32, 256), 256, 0, s>>>(
+            g, kp, rows_total, slices, digits, expo);
+        count_launches(1);
+        const int st = check_launch();
+        if (st != QMLG_OK) return st;
+    }
+    return QMLG_OK;
+}
+
+int gauss_group_kernel_matrix(const GaussItem *items, int count, int d, __nv_bfloat16 *digits,
+                              int *expo, double *norms, unsigned long long *maxbuf,
+                              int rows_total, int *d_err, cudaStream_t s)
+{
+    if (count <= 0) return QMLG_OK;
+    if (items == nullptr || d < 1 || rows_total < 1) return QMLG_E_ARG;
+    const int kp = feature_pad(d);
+    std::vector<GroupItem> g((size_t)count);
+    for (int k = 0; k < count; ++k) {
+        const GaussItem &it = items[k];
+        if (it.n < 0 || it.row0 < 0 || it.row0 + rows_pad(it.n) > rows_total || it.ldx < d ||
+            !(it.sigma > 0.0))
+            return QMLG_E_ARG;
+        if (it.n == 0) {
+            g[(size_t)k] = GroupItem{it.K, it.ldk, 0, 0, 0, 0, it.row0, it.row0, 0.0};
+            continue;
+        }
+        // the plane count is fixed at 8; a K that the bound says may be less accurate
+        // than 1e-12 is still formed and flagged (8) for the caller
+        cudaError_t e = cudaMemsetAsync(maxbuf + k, 0, sizeof(unsigned long long), s);
+        if (e != cudaSuccess) return set_cuda_error(e);
+        const int64_t total = (int64_t)it.n * d;
+        const int blocks = (int)std::min<int64_t>(ceil_div(total, 256), 1216);
+        max_abs_kernel<<<blocks, 256, 0, s>>>(it.X, it.ldx, it.n, d, maxbuf + k);
+        bound_check_sym_kernel<<<1, 1, 0, s>>>(maxbuf + k, kp, it.sigma, it.flag);
+        count_launches(2);
+        // rpad = rows_total keeps the planes' stride; the rows start at row0
+        const int st = slice_rows(it.X, it.ldx, 0, it.n, 0, d, kp, rows_total, S_MAX,
+                                  digits + (size_t)it.row0 * kp, expo + it.row0, nullptr, s,
+                                  norms + it.row0);
+        if (st != QMLG_OK) return st;
+        g[(size_t)k] = GroupItem{it.K, it.ldk, 0, it.n, 0, it.n, it.row0, it.row0,
+                                 -0.5 / (it.sigma * it.sigma)};
+    }
+    CUtensorMap mA, mB;
+    int st = make_plane_map(&mA, digits, kp, rows_total, S_MAX, TM);
+    if (st == QMLG_OK) st = make_plane_map(&mB, digits, kp, rows_total, S_MAX, Shape<kKernelMatrix>::TN);
+    if (st != QMLG_OK) return st;
+    TileArgs a{};
+    a.kchunks = kp / KC;
+    a.slices = S_MAX;
+    a.expA = expo;
+    a.expB = expo;
+    a.normA = norms;
+    a.normB = norms;
+    a.lower = 1;
+    a.diag_shift = 0.0;
+    a.err = d_err;
+    return launch_group<kKernelMatrix>(g.data(), count, mA, mB, a, s);
+}
+
+}  // namespace qmlg

@@ -7,6 +7,7 @@
     python -m qml_gb300.kernelbench cm    --n 25000              # sorted Coulomb matrices
     python -m qml_gb300.kernelbench factor --n 20000             # mixed Cholesky of the KRR K
     python -m qml_gb300.kernelbench solve  --n 20000             # mixed solve with refinement
+    python -m qml_gb300.kernelbench krr --n 40000 --m 10000      # one mixed KRR fit + predict step
 
 Each command runs the kernel `--reps` times after one warm-up call and prints the
 mean time per call (CUDA events on the launching stream).  `factor` and `solve` work
@@ -33,7 +34,8 @@ def _features(n, seed):
 
 def main(argv=None):
     p = argparse.ArgumentParser()
-    p.add_argument("kernel", choices=["syrk", "gauss", "lapl", "predict", "cm", "factor", "solve"])
+    p.add_argument("kernel", choices=["syrk", "gauss", "lapl", "predict", "cm", "factor", "solve",
+                                      "krr"])
     p.add_argument("--n", type=int, default=8192)
     p.add_argument("--m", type=int, default=2048)
     p.add_argument("--k", type=int, default=512)
@@ -82,6 +84,18 @@ def main(argv=None):
                 total += e0.elapsed_time(e1)
         print(json.dumps({"kernel": a.kernel, "n": a.n, "ms_per_call": total / max(a.reps, 1)}))
         return
+    elif a.kernel == "krr":
+        # the bench's step: CMs of n + m molecules, tensor-core K of the n training
+        # ones, mixed solve, fused prediction of the m test molecules
+        from .krr import KRR
+        b = generate_molecules(a.n + a.m, seed=2024)
+        z, r, o = molecules_to_device(b)
+        y = torch.from_numpy(b.labels[:a.n]).to(dev)
+
+        def run():
+            X = core.coulomb_matrix_batch(z, r, o, 23)
+            m = KRR(sigma=a.sigma, lam=a.lam, precision="mixed").fit(X[:a.n], y)
+            m.predict(X[a.n:])
     else:
         _, (z, r, o) = _features(a.n, 3)
         run = lambda: core.coulomb_matrix_batch(z, r, o, 23)  # noqa: E731

@@ -57,19 +57,47 @@ def test_batched_fits_match_oracle_and_graph(cuda, oracle, batch_problems):
         assert np.array_equal(a.cpu().numpy(), e)
 
 
-def test_autotuned_schedule(cuda, batch_problems):
+def test_grouped_path_matches_stream_schedule_bit_for_bit(cuda, batch_problems):
+    # one grouped launch per phase for all fits computes the same arithmetic as each
+    # fit's own launches on streams: identical alpha and status, bit for bit
     probs, _ = batch_problems
+    g = BatchedKRR(probs, refine_steps=3, mode="grouped")
+    g.run_eager()
+    ga, gr = g.results()
+    s = BatchedKRR(probs, refine_steps=3, mode="streams", streams=3)
+    s.run_eager()
+    sa, sr = s.results()
+    for a, b, ra, rb in zip(ga, sa, gr, sr):
+        assert ra["info"] == rb["info"] == 0 and ra["flags"] == rb["flags"] == 0, (ra, rb)
+        assert np.array_equal(a.cpu().numpy(), b.cpu().numpy())
+
+
+def test_autotuned_tile_parameters(cuda, batch_problems):
+    # every candidate tile shape (32 or 64 columns per tensor-core tile, 64 or 128
+    # rows per panel-solve CTA) gives the same alpha bit for bit; the tuned choice
+    # is cached per size bucket
+    from qml_gb300 import batch as batch_mod
+    probs, _ = batch_problems
+    ref = BatchedKRR(probs, refine_steps=3)
+    ref.run_eager()
+    want = [a.cpu().numpy().copy() for a in ref.results()[0]]
+    for tc in (64, 32):
+        for tr in (128, 64):
+            b = BatchedKRR(probs, refine_steps=3, tile_cols=tc, trsm_rows=tr)
+            b.run_eager()
+            alphas, reps = b.results()
+            assert all(r["info"] == 0 and r["flags"] == 0 for r in reps)
+            for a, w in zip(alphas, want):
+                assert np.array_equal(a.cpu().numpy(), w), (tc, tr)
     b = BatchedKRR(probs, refine_steps=3)
-    best = b.autotune(candidates=[{"streams": 2, "order": "size", "persistent": True},
-                                  {"streams": 4, "order": "rr", "persistent": False}], reps=1)
-    assert best["streams"] in (2, 4)
+    best = b.autotune(reps=1)
+    assert best["tile_cols"] in (32, 64) and best["trsm_rows"] in (64, 128)
+    key = (torch.cuda.get_device_name(cuda), batch_mod.size_bucket(probs))
+    assert batch_mod._TUNED[key]["tile_cols"] == best["tile_cols"]
     b.replay()
     alphas, reps = b.results()
-    assert all(r["info"] == 0 and r["flags"] == 0 for r in reps)
-    ref = BatchedKRR(probs, refine_steps=3, streams=1)
-    ref.run_eager()
-    for a, r in zip(alphas, ref.results()[0]):
-        assert np.array_equal(a.cpu().numpy(), r.cpu().numpy())
+    for a, w in zip(alphas, want):
+        assert np.array_equal(a.cpu().numpy(), w)
 
 
 def test_batched_laplacian_and_gaussian_fits(cuda, oracle):
