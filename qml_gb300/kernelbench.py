@@ -8,6 +8,7 @@
     python -m qml_gb300.kernelbench factor --n 20000             # mixed Cholesky of the KRR K
     python -m qml_gb300.kernelbench solve  --n 20000             # mixed solve with refinement
     python -m qml_gb300.kernelbench krr --n 40000 --m 10000      # one mixed KRR fit + predict step
+    python -m qml_gb300.kernelbench batch --m 64                 # 64 batched fits, grouped path
 
 Each command runs the kernel `--reps` times after one warm-up call and prints the
 mean time per call (CUDA events on the launching stream).  `factor` and `solve` work
@@ -35,7 +36,7 @@ def _features(n, seed):
 def main(argv=None):
     p = argparse.ArgumentParser()
     p.add_argument("kernel", choices=["syrk", "gauss", "lapl", "predict", "cm", "factor", "solve",
-                                      "krr"])
+                                      "krr", "batch"])
     p.add_argument("--n", type=int, default=8192)
     p.add_argument("--m", type=int, default=2048)
     p.add_argument("--k", type=int, default=512)
@@ -84,6 +85,26 @@ def main(argv=None):
                 total += e0.elapsed_time(e1)
         print(json.dumps({"kernel": a.kernel, "n": a.n, "ms_per_call": total / max(a.reps, 1)}))
         return
+    elif a.kernel == "batch":
+        # the bench's batching workload: m fits of N log-uniform in [500, 8000], sigma
+        # and lambda drawn from the bench's sets, run eagerly on the grouped path
+        import math
+
+        import numpy as np
+
+        from .batch import BatchedKRR, Problem
+        rng = np.random.default_rng(2024 + 11)
+        X, _ = _features(16000, 2024 + 12)
+        y = torch.rand(16000, dtype=torch.float64, device=dev, generator=g)
+        probs = []
+        for _ in range(a.m):
+            n = int(round(math.exp(rng.uniform(math.log(500), math.log(8000)))))
+            s0 = int(rng.integers(0, 16000 - n + 1))
+            probs.append(Problem(X[s0:s0 + n].contiguous(), y[s0:s0 + n].contiguous(),
+                                 float(rng.choice([250.0, 500.0, 1000.0, 2000.0])),
+                                 float(rng.choice([1e-4, 1e-6, 1e-8]))))
+        b = BatchedKRR(probs, refine_steps=3, trsm_rows=64)
+        run = b.run_eager
     elif a.kernel == "krr":
         # the bench's step: CMs of n + m molecules, tensor-core K of the n training
         # ones, mixed solve, fused prediction of the m test molecules
