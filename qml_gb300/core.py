@@ -49,6 +49,11 @@ class _WorkspaceCache:
         key = (index, torch.cuda.current_stream(index).cuda_stream)
         buf = self._buf.get(key)
         if buf is None or buf.numel() < nbytes:
+            # drop the smaller buffer first: it was allocated on this stream, so the
+            # allocator may hand its memory to the next allocation on this stream, and
+            # the peak is the larger size rather than the sum of both
+            self._buf.pop(key, None)
+            del buf
             buf = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=dev)
             self._buf[key] = buf
         return buf

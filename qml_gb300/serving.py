@@ -68,30 +68,62 @@ class Request:
         return self.done - self.arrival
 
 
-def fit_bytes(n: int) -> int:
-    """HBM a fit holds while it runs: K (8 n^2), the factor workspace (digit planes
-    8 planes x 512 bf16 + 8 x 64 bf16 per row, block inverses) and small vectors."""
-    rp = -(-n // 128) * 128
-    return 8 * n * n + 16 * rp * 576 + 8 * (-(-n // 64)) * 4096 + 64 * n + (64 << 20)
+# Per-molecule device bytes of a request's own tensors: charges and coordinates of
+# up to CM_SIZE atoms (4 doubles each), the offset, the label or output, and the
+# Coulomb-matrix row.
+_MOL_BYTES = CM_SIZE * 4 * 8 + 8 + 8 + FEATURES * 8
+# torch's caching allocator rounds every block up (large ones to 2 MiB); a request
+# makes fewer than eight device allocations
+_ALLOC_SLACK = 16 << 20
+
+
+def _workspace(name: str, *args) -> int:
+    """A workspace size from the library (pure host arithmetic, no GPU needed)."""
+    from . import _lib
+    return int(getattr(_lib.load(), name)(*args))
+
+
+def fit_bytes(n: int, kernel: str = "gaussian") -> int:
+    """HBM a fit holds while it runs: its molecules and Coulomb matrices, K (8 n^2),
+    alpha, and the one workspace the kernel matrix and the mixed solve share (the
+    library's own sizes: digit planes, block inverses, residual partials)."""
+    if kernel == "laplacian":
+        kws = _workspace("qmlg_laplacian_kernel_fixed_workspace_size", n, n, FEATURES, 1)
+    else:
+        kws = _workspace("qmlg_gaussian_kernel_emulated_workspace_size", n, n, FEATURES, 1)
+    sws = _workspace("qmlg_solve_workspace_size", n, 1)
+    return 8 * n * n + (_MOL_BYTES + 8) * n + max(kws, sws) + _ALLOC_SLACK
+
+
+def resident_bytes(n: int) -> int:
+    """HBM a fitted model keeps: its training Coulomb matrices and alpha."""
+    return (FEATURES + 1) * 8 * n
 
 
 def predict_bytes(n_query: int, n_train: int, kernel: str = "gaussian") -> int:
-    """HBM a prediction batch holds: query molecules and CMs, then for a Gaussian
-    model the digit planes of both sides (8 planes x 320 bf16 per row) and partial
-    sums per 128 training rows; for a Laplacian model the fixed-point features of
-    both sides (8 bytes per value) and partial sums per 64 training rows."""
-    rq = -(-n_query // 128) * 128
-    rt = -(-n_train // 128) * 128
-    base = n_query * (FEATURES * 8 + 23 * 32) + (8 << 20)
+    """HBM a merged prediction batch holds: its molecules, Coulomb matrices and
+    outputs, and the fused prediction's workspace (the library's own size: digit
+    planes of both sides and partial sums for a Gaussian model, fixed-point
+    features and partial sums for a Laplacian one)."""
     if kernel == "laplacian":
-        return base + 8 * FEATURES * (n_query + n_train) + 8 * n_query * (-(-n_train // 64))
-    return base + 16 * 320 * (rq + rt) + 8 * n_query * (-(-n_train // 128))
+        ws = _workspace("qmlg_predict_laplacian_fixed_workspace_size", n_train, n_query, FEATURES)
+    else:
+        ws = _workspace("qmlg_predict_emulated_workspace_size", n_train, n_query, FEATURES)
+    return _MOL_BYTES * n_query + ws + _ALLOC_SLACK
 
 
 class Scheduler:
     """Host-side admission and batching (no GPU).  `budget_bytes` caps the HBM that
-    admitted work may hold; `max_slots` caps concurrent prediction batches;
-    `max_batch_molecules` caps one merged prediction launch."""
+    resident models and admitted work may hold together; `max_slots` caps concurrent
+    prediction batches; `max_batch_molecules` caps one merged prediction launch.
+
+    The costs are the library's workspace sizes plus each request's own tensors
+    (fit_bytes, predict_bytes, resident_bytes); a GPU test checks them against the
+    allocator's peak.  The per-stream workspace cache (core.workspaces) keeps the
+    largest workspace each stream has used, so the process holds that much more than
+    the admitted costs between requests.  A fit that fails (an allocation that fails
+    although the budget allowed it, for example) releases its cost, and the queries
+    waiting for its model are answered with the fit's error."""
 
     def __init__(self, budget_bytes: int, max_slots: int = 8, max_batch_molecules: int = 8192,
                  model_sizes: Optional[Dict[str, int]] = None,
@@ -105,6 +137,9 @@ class Scheduler:
         self.fit_running = False
         self.model_sizes: Dict[str, int] = dict(model_sizes or {})
         self.model_kinds: Dict[str, str] = dict(model_kinds or {})
+        self.failed_models: Dict[str, str] = {}
+        self.in_use = sum(resident_bytes(n) for n in self.model_sizes.values())
+        self._held: Dict[int, int] = {}   # admitted cost per unit of work (first request's id)
 
     def _predict_cost(self, model: str, mols: int) -> int:
         return predict_bytes(mols, self.model_sizes.get(model, 0),
@@ -115,7 +150,7 @@ class Scheduler:
 
     def cost(self, req: Request) -> int:
         if req.kind == "fit":
-            return fit_bytes(req.n_mol)
+            return fit_bytes(req.n_mol, req.kernel)
         return self._predict_cost(req.model, req.n_mol)
 
     def next_batch(self) -> Optional[List[Request]]:
@@ -126,19 +161,25 @@ class Scheduler:
         if not self.queue:
             return None
         head = self.queue[0]
+        if head.kind == "predict" and head.model in self.failed_models:
+            self.queue.popleft()
+            head.error = "model %r failed to fit: %s" % (head.model,
+                                                         self.failed_models[head.model])
+            return [head]
         if head.kind == "predict" and head.model not in self.model_sizes:
             # its model is still being fitted: look for other work behind it
             for k, r in enumerate(self.queue):
-                if r.kind == "fit" or r.model in self.model_sizes:
+                if r.kind == "fit" or r.model in self.model_sizes or r.model in self.failed_models:
                     self.queue.rotate(-k)
-                    head = self.queue[0]
-                    break
+                    return self.next_batch()
             else:
                 return None
         cost = self.cost(head)
         if cost > self.budget:
             self.queue.popleft()
             head.error = "request needs %d bytes, budget is %d" % (cost, self.budget)
+            if head.kind == "fit":
+                self.failed_models[head.model] = head.error
             return [head]
         if head.kind == "fit":
             if self.fit_running or self.in_use + cost > self.budget:
@@ -150,6 +191,7 @@ class Scheduler:
                 return None
             self.queue.popleft()
             self.in_use += cost
+            self._held[id(head)] = cost
             self.fit_running = True
             return [head]
         return self.next_batch_predict()
@@ -175,21 +217,25 @@ class Scheduler:
                 self.queue.appendleft(r)
             return None
         self.in_use += cost
+        self._held[id(batch[0])] = cost
         self.slots += 1
         return batch
 
     def release(self, batch: List[Request]):
         if not batch:
             return
+        held = self._held.pop(id(batch[0]), 0)
         if batch[0].kind == "fit":
-            self.in_use -= fit_bytes(batch[0].n_mol)
+            self.in_use -= held
             self.fit_running = False
             if batch[0].error is None:
                 self.model_sizes[batch[0].model] = batch[0].n_mol
                 self.model_kinds[batch[0].model] = batch[0].kernel
+                self.in_use += resident_bytes(batch[0].n_mol)
+            else:
+                self.failed_models[batch[0].model] = batch[0].error
         else:
-            mols = sum(r.n_mol for r in batch)
-            self.in_use -= self._predict_cost(batch[0].model, mols)
+            self.in_use -= held
             self.slots -= 1
 
 

@@ -92,3 +92,46 @@ def test_serving_laplacian_model_mix_equals_alone(cuda, oracle):
         Ks = oracle.laplacian_kernel(Xo, Xq, sigma)
         scale = np.abs(Ks.T) @ np.abs(alpha)
         assert np.max(np.abs(req.result - Ks.T @ alpha) / scale) <= 1e-12
+
+
+@pytest.mark.parametrize("kernel", ["gaussian", "laplacian"])
+def test_admission_costs_cover_the_allocator_peak(cuda, kernel):
+    # the scheduler admits work by fit_bytes / predict_bytes; the device memory a
+    # fit and a merged prediction really take (the caching allocator's peak above
+    # what was held before) must stay under those costs, and the costs may not
+    # overstate it by more than the per-molecule allowance and the rounding slack
+    ntr, nq = 3000, 700
+    ex = serving.GpuExecutor(n_streams=1)
+    torch.cuda.synchronize()
+    train = generate_molecules(ntr, seed=201)
+    req = serving.Request(0, "fit", "m", train.charges, train.coordinates, train.offsets, 0.0,
+                          labels=train.labels, kernel=kernel)
+    torch.cuda.reset_peak_memory_stats()
+    base = torch.cuda.memory_allocated()
+    try:
+        ex.run_fit(req)
+    finally:
+        core.lib().qmlg_set_thread_sm_limit(0)
+    torch.cuda.synchronize()
+    peak = torch.cuda.max_memory_allocated() - base
+    cost = serving.fit_bytes(ntr, kernel)
+    assert peak <= cost, (peak, cost)
+    assert cost - peak <= serving._ALLOC_SLACK + serving._MOL_BYTES * ntr, (peak, cost)
+    # what stays is the model: its Coulomb matrices and alpha (the workspace cache
+    # of the fit stream stays too, owned by the process, not by the model)
+    X, alpha, _, _ = ex.models["m"]
+    assert X.numel() * 8 + alpha.numel() * 8 == serving.resident_bytes(ntr)
+
+    q = generate_molecules(nq, seed=202)
+    qreq = serving.Request(1, "predict", "m", q.charges, q.coordinates, q.offsets, 0.0)
+    torch.cuda.synchronize()
+    torch.cuda.reset_peak_memory_stats()
+    base = torch.cuda.memory_allocated()
+    ev, finish = ex.launch_predict([qreq])
+    ev.synchronize()
+    peak = torch.cuda.max_memory_allocated() - base
+    finish()
+    cost = serving.predict_bytes(nq, ntr, kernel)
+    assert peak <= cost, (peak, cost)
+    assert cost - peak <= serving._ALLOC_SLACK + serving._MOL_BYTES * nq, (peak, cost)
+    assert qreq.result.shape == (nq,) and np.all(np.isfinite(qreq.result))

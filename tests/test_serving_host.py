@@ -5,7 +5,8 @@ import threading
 import numpy as np
 
 from qml_gb300 import serving
-from qml_gb300.serving import Request, Scheduler, Server, fit_bytes, merge_molecules, predict_bytes
+from qml_gb300.serving import (Request, Scheduler, Server, fit_bytes, merge_molecules,
+                                predict_bytes, resident_bytes)
 from qml_gb300.synthetic import generate_molecules
 
 
@@ -38,8 +39,9 @@ def test_predictions_merge_and_respect_slots():
 
 
 def test_budget_admission_and_rejection():
-    s = Scheduler(budget_bytes=fit_bytes(2000) + predict_bytes(10, 1000), max_slots=4,
-                  model_sizes={"m": 1000})
+    s = Scheduler(budget_bytes=fit_bytes(2000) + predict_bytes(10, 1000) + resident_bytes(1000),
+                  max_slots=4, model_sizes={"m": 1000})
+    assert s.in_use == resident_bytes(1000)
     s.submit(mk(0, "fit", "f", 2000, 0.0))
     s.submit(mk(1, "fit", "g", 1500, 0.0))
     s.submit(mk(2, "predict", "m", 10, 0.0))
@@ -125,3 +127,75 @@ def test_poisson_workload_shape():
     assert all(1 <= r.n_mol <= 64 for r in reqs if r.kind == "predict")
     assert sum(r.kind == "fit" for r in reqs) >= 5
     assert all(reqs[i].arrival <= reqs[i + 1].arrival for i in range(len(reqs) - 1))
+
+
+def test_costs_follow_the_library_workspace_sizes():
+    from qml_gb300 import _lib
+    lib = _lib.load()
+    n = 3000
+    ws = max(lib.qmlg_gaussian_kernel_emulated_workspace_size(n, n, 276, 1),
+             lib.qmlg_solve_workspace_size(n, 1))
+    assert fit_bytes(n) >= 8 * n * n + ws
+    assert fit_bytes(n, "laplacian") >= 8 * n * n + lib.qmlg_solve_workspace_size(n, 1)
+    assert predict_bytes(100, n) >= lib.qmlg_predict_emulated_workspace_size(n, 100, 276)
+    assert predict_bytes(100, n, "laplacian") >= \
+        lib.qmlg_predict_laplacian_fixed_workspace_size(n, 100, 276)
+    # grows with the problem
+    assert fit_bytes(2 * n) > fit_bytes(n) and predict_bytes(200, n) > predict_bytes(100, n)
+
+
+def test_fitted_models_stay_accounted():
+    s = Scheduler(budget_bytes=1 << 40, model_sizes={})
+    s.submit(mk(0, "fit", "f", 300, 0.0))
+    b = s.next_batch()
+    assert s.in_use == fit_bytes(300)
+    s.release(b)
+    assert s.in_use == resident_bytes(300) and s.model_sizes["f"] == 300
+
+
+def test_failed_fit_answers_its_waiting_queries():
+    # a fit that fails on the GPU (here: an allocation failure although the budget
+    # admitted it) releases its cost; the queries for its model get the fit's error
+    s = Scheduler(budget_bytes=1 << 40, model_sizes={"m": 100})
+    s.submit(mk(0, "fit", "f", 200, 0.0))
+    s.submit(mk(1, "predict", "f", 3, 0.0))
+    s.submit(mk(2, "predict", "m", 2, 0.0))
+    fit = s.next_batch()
+    assert fit[0].rid == 0
+    fit[0].error = "RuntimeError('CUDA out of memory')"
+    s.release(fit)
+    assert s.in_use == resident_bytes(100) and "f" not in s.model_sizes
+    out = [s.next_batch(), s.next_batch()]
+    rej = next(b for b in out if b[0].rid == 1)
+    assert rej[0].error is not None and "failed to fit" in rej[0].error
+    ok = next(b for b in out if b[0].rid == 2)
+    assert ok[0].error is None
+
+
+class FailingFitExecutor(FakeExecutor):
+    """A fake whose fits of one model raise the error an allocation failure raises."""
+
+    def run_fit(self, req):
+        if req.model == "bad":
+            raise RuntimeError("CUDA out of memory. Tried to allocate 3.20 GiB")
+        req.result = np.zeros(1)
+
+
+def test_server_survives_a_fit_that_fails_to_allocate():
+    import time
+    clock = time.perf_counter
+    ex = FailingFitExecutor(clock)
+    sched = Scheduler(budget_bytes=1 << 40, max_slots=2, model_sizes={"m": 100})
+    arrivals = [mk(0, "fit", "bad", 60, 0.0), mk(1, "predict", "bad", 2, 0.0005),
+                mk(2, "predict", "m", 3, 0.001), mk(3, "fit", "good", 40, 0.0015),
+                mk(4, "predict", "good", 2, 0.002), mk(5, "predict", "bad", 1, 0.003)]
+    done = Server(ex, sched, clock=clock).run(arrivals)
+    assert len(done) == 6
+    by = {r.rid: r for r in done}
+    assert "out of memory" in by[0].error
+    assert by[1].error is not None and by[5].error is not None
+    assert by[2].error is None and by[3].error is None and by[4].error is None
+    assert by[4].result is not None
+    # everything admitted was released; the two fitted models stay accounted
+    assert sched.in_use == resident_bytes(100) + resident_bytes(40)
+    assert sched.slots == 0 and not sched.fit_running
