@@ -420,23 +420,55 @@ constexpr int RES_ROWS = 64;
 constexpr int RES_CHUNK = 1024;
 
 // Partial row sums of the symmetric matrix held in R's strictly upper triangle plus
-// diag, times x: one CTA per (64 rows, 1024 columns), 4 threads per row, each
-// product added exactly into a 256-bit fixed-point accumulator (exact_acc.cuh).
+// diag, times x: one CTA per (64 rows, 1024 columns), each product added exactly
+// into a 256-bit fixed-point accumulator (exact_acc.cuh).
+//  * x's 1024 entries are split once, at the start, into shared memory.
+//  * The 64 x 64 tiles of the symmetric matrix are copied into shared memory with
+//    cp.async, two buffers deep, so the next tile's loads run under this tile's
+//    products.  Element (r, c) sits at r * 64 + (c ^ (r & 31)): row-wise and
+//    column-wise stores and the column reads below are all free of bank conflicts.
+//  * Warp w takes rows 32 (w & 1) .. +31 (a lane per row) and the column quarter
+//    w >> 1 of every tile, so all lanes of a warp meet the same x_j at once: x's
+//    sign and split are warp-uniform, and for a matrix without negative entries (a
+//    kernel matrix) so is the sign of every product.
+//  * The four quarter sums of a row are combined exactly at the end.
 struct AccPart {
     unsigned long long l0, l1, l2, l3;
     int f, bad;
 };
 
-__device__ __forceinline__ void acc_shfl_xor_add(qmlg::Acc &a, int off)
+constexpr int RES_TILE = 64 * 64;  // doubles per tile buffer
+constexpr size_t RES_SMEM = 2 * RES_TILE * sizeof(double) + RES_CHUNK * (sizeof(uint2) + sizeof(short));
+
+__device__ __forceinline__ void cp_async8(double *dst, const double *src)
 {
-    qmlg::Acc b;
-    b.l0 = __shfl_xor_sync(0xffffffffu, a.l0, off);
-    b.l1 = __shfl_xor_sync(0xffffffffu, a.l1, off);
-    b.l2 = __shfl_xor_sync(0xffffffffu, a.l2, off);
-    b.l3 = __shfl_xor_sync(0xffffffffu, a.l3, off);
-    b.f = __shfl_xor_sync(0xffffffffu, a.f, off);
-    b.bad = __shfl_xor_sync(0xffffffffu, a.bad, off);
-    qmlg::acc_add_acc(a, b);
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
+}
+
+// Copies the symmetric tile (rows i0.., columns j0..) into T (swizzled, zeros outside).
+__device__ __forceinline__ void res_stage(double *T, const double *__restrict__ A, int64_t lda, int n,
+                                          const double *__restrict__ diag, int i0, int j0, int tid)
+{
+    // the two loops write disjoint elements: (j >= i or outside) / (j < i inside)
+    for (int e = tid; e < RES_TILE; e += 256) {
+        const int rr = e >> 6, c = e & 63;
+        const int i = i0 + rr, j = j0 + c;
+        double *dst = T + rr * 64 + (c ^ (rr & 31));
+        if (i < n && j < n) {
+            if (j > i) cp_async8(dst, A + (int64_t)i * lda + j);
+            else if (j == i) cp_async8(dst, diag + i);
+        } else {
+            *dst = 0.0;
+        }
+    }
+    for (int e = tid; e < RES_TILE; e += 256) {
+        // lower part from the transposed upper tile: R[j][i] for j < i
+        const int c = e >> 6, rr = e & 63;
+        const int i = i0 + rr, j = j0 + c;
+        if (i < n && j < n && j < i) cp_async8(T + rr * 64 + (c ^ (rr & 31)), A + (int64_t)j * lda + i);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
 }
 
 __device__ __forceinline__ void symv_exact_partial_block(const double *__restrict__ A, int64_t lda,
@@ -445,65 +477,59 @@ __device__ __forceinline__ void symv_exact_partial_block(const double *__restric
                                                          AccPart *__restrict__ partial, int bx,
                                                          int by)
 {
-    __shared__ double S[64][64 + 1];
-    __shared__ unsigned long long xm[64];
-    __shared__ int xe[64];
-    __shared__ unsigned char xn[64];
-    const int tid = threadIdx.x;
+    extern __shared__ __align__(16) unsigned char res_smem[];
+    double *T = reinterpret_cast<double *>(res_smem);                         // [2][RES_TILE]
+    uint2 *xs = reinterpret_cast<uint2 *>(T + 2 * RES_TILE);                  // low 32 bits; high 21 | sign << 31
+    short *xe = reinterpret_cast<short *>(xs + RES_CHUNK);                    // exponent - 2150
+    __shared__ int xbad;
+    static_assert(RES_TILE * sizeof(double) >= 256 * sizeof(AccPart), "the combine reuses a tile buffer");
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int i0 = bx * RES_ROWS;
     const int c0 = by * RES_CHUNK;
-    const int lr = tid >> 2, part = tid & 3;
+    const int ntiles = (min(n, c0 + RES_CHUNK) - c0 + 63) / 64;
+    const int r = lane + 32 * (warp & 1), cq = 16 * (warp >> 1), sw = r & 31;
+    res_stage(T, A, lda, n, diag, i0, c0, tid);
+    if (tid == 0) xbad = 0;
+    __syncthreads();
+    for (int t = tid; t < RES_CHUNK; t += 256) {
+        const unsigned long long u =
+            (unsigned long long)__double_as_longlong((c0 + t < n) ? x[c0 + t] : 0.0);
+        const uint32_t hw = (uint32_t)(u >> 32), ef = (hw >> 20) & 0x7ffu;
+        xs[t] = make_uint2((uint32_t)u, (hw & 0x800fffffu) | (ef ? 0x100000u : 0u));
+        xe[t] = (short)((int)(ef ? ef : 1u) - 2 * 1075);
+        if (ef == 0x7ffu) xbad = 1;
+    }
     qmlg::Acc acc;
     qmlg::acc_init(acc);
-    int xbad = 0;
-    for (int j0 = c0; j0 < min(n, c0 + RES_CHUNK); j0 += 64) {
-        __syncthreads();
-        // S[r][c] = A_sym(i0 + r, j0 + c)
-        // the two loops write disjoint elements: (j >= i or outside) / (j < i inside)
-        for (int e = tid; e < 64 * 64; e += 256) {
-            const int r = e >> 6, c = e & 63;
-            const int i = i0 + r, j = j0 + c;
-            const bool inside = i < n && j < n;
-            if (inside && j < i) continue;
-            double v = 0.0;
-            if (inside && j > i) v = A[(int64_t)i * lda + j];
-            if (inside && j == i) v = diag[i];
-            S[r][c] = v;
-        }
-        for (int e = tid; e < 64 * 64; e += 256) {
-            // lower part from the transposed upper tile: R[j][i] for j < i
-            const int c = e >> 6, r = e & 63;
-            const int i = i0 + r, j = j0 + c;
-            if (i < n && j < n && j < i) S[r][c] = A[(int64_t)j * lda + i];
-        }
-        if (tid < 64) {
-            unsigned long long m;
-            int ex, bd = 0;
-            bool ng;
-            qmlg::dbl_split((j0 + tid < n) ? x[j0 + tid] : 0.0, m, ex, ng, bd);
-            xm[tid] = m;
-            xe[tid] = ex;
-            xn[tid] = ng ? 1 : 0;
-            xbad |= bd;
+    for (int k = 0; k < ntiles; ++k) {
+        if (k + 1 < ntiles) {
+            res_stage(T + ((k + 1) & 1) * RES_TILE, A, lda, n, diag, i0, c0 + 64 * (k + 1), tid);
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+        } else {
+            asm volatile("cp.async.wait_group 0;" ::: "memory");
         }
         __syncthreads();
+        const double *Tk = T + (k & 1) * RES_TILE + r * 64;
+        const uint2 *xk = xs + 64 * k;
+        const short *ek = xe + 64 * k;
 #pragma unroll 4
-        for (int c = part * 16; c < part * 16 + 16; ++c) {
-            unsigned long long ma;
-            int ea;
-            bool na;
-            qmlg::dbl_split(S[lr][c], ma, ea, na, acc.bad);
-            const unsigned long long mb = xm[c];
-            qmlg::acc_add_mag(acc, __umul64hi(ma, mb), ma * mb, ea + xe[c], na != (xn[c] != 0));
+        for (int c = cq; c < cq + 16; ++c) {
+            const unsigned long long ua = (unsigned long long)__double_as_longlong(Tk[c ^ sw]);
+            const uint32_t aw = (uint32_t)(ua >> 32), ef = (aw >> 20) & 0x7ffu;
+            const uint2 xb = xk[c];
+            unsigned long long hi, lo;
+            qmlg::mul53((uint32_t)ua, (aw & 0xfffffu) | (ef ? 0x100000u : 0u), xb.x, xb.y & 0x1fffffu,
+                        hi, lo);
+            acc.bad |= ef == 0x7ffu;
+            qmlg::acc_add_mag_fast(acc, hi, lo, (int)(ef ? ef : 1u) + ek[c], ((aw ^ xb.y) >> 31) != 0u);
         }
+        __syncthreads();  // the buffer is refilled by the next iteration's copies
     }
     acc.bad |= xbad;
-    // combine the 4 parts of a row (exact)
-    acc_shfl_xor_add(acc, 1);
-    acc_shfl_xor_add(acc, 2);
-    const int i = i0 + lr;
-    if (part == 0 && i < n) {
-        AccPart &o = partial[(int64_t)by * n + i];
+    // combine the four column quarters of each row (exact, fixed order)
+    AccPart *comb = reinterpret_cast<AccPart *>(T);  // [quarter][row]
+    {
+        AccPart &o = comb[(warp >> 1) * 64 + r];
         o.l0 = acc.l0;
         o.l1 = acc.l1;
         o.l2 = acc.l2;
@@ -511,6 +537,39 @@ __device__ __forceinline__ void symv_exact_partial_block(const double *__restric
         o.f = acc.f;
         o.bad = acc.bad;
     }
+    __syncthreads();
+    const int i = i0 + tid;
+    if (tid < 64 && i < n) {
+        qmlg::Acc a;
+        qmlg::acc_init(a);
+        for (int q = 0; q < 4; ++q) {
+            const AccPart &p = comb[q * 64 + tid];
+            qmlg::Acc b;
+            b.l0 = p.l0;
+            b.l1 = p.l1;
+            b.l2 = p.l2;
+            b.l3 = p.l3;
+            b.f = p.f;
+            b.bad = p.bad;
+            qmlg::acc_add_acc(a, b);
+        }
+        AccPart &o = partial[(int64_t)by * n + i];
+        o.l0 = a.l0;
+        o.l1 = a.l1;
+        o.l2 = a.l2;
+        o.l3 = a.l3;
+        o.f = a.f;
+        o.bad = a.bad;
+    }
+}
+
+// Opt-in to the residual's dynamic shared memory (once per process and kernel).
+template <typename K>
+int res_smem_attr(K kernel)
+{
+    const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)RES_SMEM);
+    return e == cudaSuccess ? QMLG_OK : qmlg::set_cuda_error(e);
 }
 
 __global__ void __launch_bounds__(256)
@@ -1604,7 +1663,11 @@ int residual_dd(const double *A, int n, int64_t lda, const double *diag, double 
     const int nchunks = (int)ceil_div(n, RES_CHUNK);
     AccPart *partial = ws.take<AccPart>((size_t)nchunks * n);
     if (partial == nullptr) return QMLG_E_WORKSPACE;
-    { symv_exact_partial_kernel<<<dim3((unsigned)ceil_div(n, RES_ROWS), nchunks), 256, 0, s>>>(
+    static std::once_flag once;
+    static int attr = QMLG_OK;
+    std::call_once(once, [] { attr = res_smem_attr(symv_exact_partial_kernel); });
+    if (attr != QMLG_OK) return attr;
+    { symv_exact_partial_kernel<<<dim3((unsigned)ceil_div(n, RES_ROWS), nchunks), 256, RES_SMEM, s>>>(
         A, lda, n, diag, x, partial); qmlg::count_launches(1); }
     { residual_finish_kernel<<<(int)ceil_div(n, 256), 256, 0, s>>>(partial, nchunks, n, lambda, x,
                                                                  y, r); qmlg::count_launches(1); }
@@ -2318,6 +2381,9 @@ extern "C" int qmlg_fit_batched_async(const QmlgBatchProblem *problems, int coun
     std::call_once(once, [] {
         attr = cudaFuncSetAttribute(trsm_group_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)trsm_smem(TRSM_MAX_ROWS));
+        if (attr == cudaSuccess)
+            attr = cudaFuncSetAttribute(symv_group_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)RES_SMEM);
     });
     if (attr != cudaSuccess) return qmlg::set_cuda_error(attr);
     static BatchLauncher L;  // 18 KB of staging, kept off the stack
@@ -2499,7 +2565,7 @@ extern "C" int qmlg_fit_batched_async(const QmlgBatchProblem *problems, int coun
     st = vec(kCopyY, per_256, sel_alpha);
     if (st == QMLG_OK) st = solve(sel_alpha);
     for (int it = 0; it < refine_steps && st == QMLG_OK; ++it) {
-        st = run([&](int grid) { symv_group_kernel<<<grid, 256, 0, s>>>(L.g); },
+        st = run([&](int grid) { symv_group_kernel<<<grid, 256, RES_SMEM, s>>>(L.g); },
                  [&](const BatchFit &f, BatchEntry &en) {
                      base_entry(f, en);
                      en.x = f.q->alpha;

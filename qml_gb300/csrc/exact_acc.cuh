@@ -120,6 +120,42 @@ __device__ __forceinline__ void acc_add_mag(Acc &a, unsigned long long hi, unsig
     else acc_addc(a, x0, x1, x2, x3);
 }
 
+// The common case of acc_add_mag, with no branch but the sign: a product that lands
+// inside the frame (0 <= s <= ACC_HEAD).  Anything else (the first product, one
+// above the head or below the frame, a zero) takes acc_add_mag.
+__device__ __forceinline__ void acc_add_mag_fast(Acc &a, unsigned long long hi, unsigned long long lo,
+                                                 int E, bool neg)
+{
+    const int s = E - a.f;
+    if (s < 0 || s > ACC_HEAD) {
+        acc_add_mag(a, hi, lo, E, neg);
+        return;
+    }
+    const int w = s >> 6, b = s & 63;  // w <= 2
+    // (hi:lo) << b in three limbs; the double shift keeps b = 0 defined
+    const unsigned long long t0 = lo << b;
+    const unsigned long long t1 = (hi << b) | ((lo >> 1) >> (63 - b));
+    const unsigned long long t2 = (hi >> 1) >> (63 - b);
+    const unsigned long long x0 = w == 0 ? t0 : 0ull;
+    const unsigned long long x1 = w == 0 ? t1 : (w == 1 ? t0 : 0ull);
+    const unsigned long long x2 = w == 0 ? t2 : (w == 1 ? t1 : t0);
+    const unsigned long long x3 = w == 0 ? 0ull : (w == 1 ? t2 : t1);
+    if (neg) acc_subc(a, x0, x1, x2, x3);
+    else acc_addc(a, x0, x1, x2, x3);
+}
+
+// The 106-bit product of two significands below 2^53, each given as its low 32 bits
+// and its high 21: four 32 x 32 -> 64-bit multiplies; hi < 2^43.
+__device__ __forceinline__ void mul53(uint32_t alo, uint32_t ahi, uint32_t blo, uint32_t bhi,
+                                      unsigned long long &hi, unsigned long long &lo)
+{
+    const unsigned long long p00 = (unsigned long long)alo * blo;
+    unsigned long long mid = (unsigned long long)ahi * blo + (p00 >> 32);  // < 2^53 + 2^32
+    mid += (unsigned long long)alo * bhi;                                  // < 2^54 + 2^32
+    hi = (unsigned long long)ahi * bhi + (mid >> 32);
+    lo = (mid << 32) | (p00 & 0xffffffffull);
+}
+
 // Significand (with the hidden bit) and exponent: v = m * 2^e.
 __device__ __forceinline__ void dbl_split(double v, unsigned long long &m, int &e, bool &neg,
                                           int &bad)

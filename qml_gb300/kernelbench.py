@@ -9,6 +9,7 @@
     python -m qml_gb300.kernelbench solve  --n 20000             # mixed solve with refinement
     python -m qml_gb300.kernelbench krr --n 40000 --m 10000      # one mixed KRR fit + predict step
     python -m qml_gb300.kernelbench batch --m 64                 # 64 batched fits, grouped path
+    python -m qml_gb300.kernelbench residual --n 20000           # exact residual y - (K + lam I) x
 
 Each command runs the kernel `--reps` times after one warm-up call and prints the
 mean time per call (CUDA events on the launching stream).  `factor` and `solve` work
@@ -36,7 +37,7 @@ def _features(n, seed):
 def main(argv=None):
     p = argparse.ArgumentParser()
     p.add_argument("kernel", choices=["syrk", "gauss", "lapl", "predict", "cm", "factor", "solve",
-                                      "krr", "batch"])
+                                      "krr", "batch", "residual"])
     p.add_argument("--n", type=int, default=8192)
     p.add_argument("--m", type=int, default=2048)
     p.add_argument("--k", type=int, default=512)
@@ -105,6 +106,16 @@ def main(argv=None):
                                  float(rng.choice([1e-4, 1e-6, 1e-8]))))
         b = BatchedKRR(probs, refine_steps=3, trsm_rows=64)
         run = b.run_eager
+    elif a.kernel == "residual":
+        # the refinement's exact residual on the Gaussian K of seeded molecules (the
+        # upper triangle and the diagonal are read; x of mixed signs and magnitudes)
+        X, _ = _features(a.n, 2024)
+        K = torch.empty((a.n, a.n), dtype=torch.float64, device=dev).T
+        core.kernel_matrix("gaussian", X, X, a.sigma, symmetric=True, emulated=True, out=K)
+        diag = torch.diagonal(K).contiguous()
+        x = torch.randn(a.n, dtype=torch.float64, device=dev, generator=g) * 1e6
+        y = torch.rand(a.n, dtype=torch.float64, device=dev, generator=g)
+        run = lambda: core.residual_dd(K, diag, a.lam, x, y)  # noqa: E731
     elif a.kernel == "krr":
         # the bench's step: CMs of n + m molecules, tensor-core K of the n training
         # ones, mixed solve, fused prediction of the m test molecules

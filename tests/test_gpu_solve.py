@@ -175,6 +175,48 @@ def test_residual_is_correctly_rounded(cuda):
         assert r[i] == float(ex), (i, r[i], float(ex))
 
 
+def _two_prod(a, b):
+    """a * b = p + e exactly (Dekker's product with Veltkamp's split; no overflow or
+    underflow in the ranges used here)."""
+    def split(v):
+        c = 134217729.0 * v
+        hi = c - (c - v)
+        return hi, v - hi
+    p = a * b
+    ah, al = split(a)
+    bh, bl = split(b)
+    e = ((ah * bh - p) + ah * bl + al * bh) + al * bl
+    return p, e
+
+
+@pytest.mark.parametrize("n", [1100, 2100])
+def test_residual_correctly_rounded_across_chunks(cuda, n):
+    # several 1024-column chunks and 64-row blocks: mixed signs (so the sign of the
+    # products differs across a warp), zeros, entries spread over 2^-250 .. 2^40 (so
+    # products land above the head and far below the frame), and heavy cancellation.
+    # Every row must equal the correctly rounded exact value: math.fsum of the exact
+    # two-product pieces
+    import math
+    rng = np.random.default_rng(n)
+    A = rng.standard_normal((n, n)) * np.exp2(rng.integers(-40, 40, size=(n, n)))
+    far = rng.random((n, n)) < 0.05
+    A[far] *= 2.0 ** -200
+    A[rng.random((n, n)) < 0.02] = 0.0
+    A = np.triu(A) + np.triu(A, 1).T
+    x = rng.standard_normal(n) * np.exp2(rng.integers(-20, 20, size=n))
+    lam = 3e-7
+    y = (A + lam * np.eye(n)) @ x * (1 + 1e-14 * rng.standard_normal(n))
+    At = torch.from_numpy(A).to(cuda)
+    r = core.residual_dd(At, torch.from_numpy(np.diag(A).copy()).to(cuda), lam,
+                         torch.from_numpy(x).to(cuda), torch.from_numpy(y).to(cuda)).cpu().numpy()
+    p, e = _two_prod(A, x[None, :])
+    lp, le = _two_prod(np.full(n, lam), x)
+    ref = np.array([math.fsum(np.concatenate(([y[i], -lp[i], -le[i]], -p[i], -e[i])))
+                    for i in range(n)])
+    bad = np.nonzero(r != ref)[0]
+    assert bad.size == 0, (bad[:5], r[bad[:5]], ref[bad[:5]])
+
+
 @pytest.mark.parametrize("n", [65, 700, 1100, 1500])
 def test_mixed_factor_matches_fp64_factor(cuda, oracle, krr_system, n):
     # the tensor-core factor (emulated FP64 trailing updates) against the plain FP64 one
