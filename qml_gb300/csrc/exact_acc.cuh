@@ -131,11 +131,17 @@ __device__ __forceinline__ void acc_add_mag_fast(Acc &a, unsigned long long hi, 
         acc_add_mag(a, hi, lo, E, neg);
         return;
     }
-    const int w = s >> 6, b = s & 63;  // w <= 2
-    // (hi:lo) << b in three limbs; the double shift keeps b = 0 defined
-    const unsigned long long t0 = lo << b;
-    const unsigned long long t1 = (hi << b) | ((lo >> 1) >> (63 - b));
-    const unsigned long long t2 = (hi >> 1) >> (63 - b);
+    // (hi:lo) << s in 32-bit words: a funnel shift by b = s mod 32 gives five words
+    // q0..q4, which then move up by h = (s >> 5) & 1 words and w = s >> 6 limbs (w <= 2)
+    const int b = s & 31, h = (s >> 5) & 1, w = s >> 6;
+    const uint32_t p0 = (uint32_t)lo, p1 = (uint32_t)(lo >> 32), p2 = (uint32_t)hi,
+                   p3 = (uint32_t)(hi >> 32);
+    const uint32_t q0 = p0 << b, q1 = __funnelshift_l(p0, p1, b), q2 = __funnelshift_l(p1, p2, b),
+                   q3 = __funnelshift_l(p2, p3, b), q4 = __funnelshift_l(p3, 0u, b);
+    // three limbs t0, t1, t2 of (hi:lo) << (s mod 64)
+    const unsigned long long t0 = h ? ((unsigned long long)q0 << 32) : (((unsigned long long)q1 << 32) | q0);
+    const unsigned long long t1 = h ? (((unsigned long long)q2 << 32) | q1) : (((unsigned long long)q3 << 32) | q2);
+    const unsigned long long t2 = h ? (((unsigned long long)q4 << 32) | q3) : (unsigned long long)q4;
     const unsigned long long x0 = w == 0 ? t0 : 0ull;
     const unsigned long long x1 = w == 0 ? t1 : (w == 1 ? t0 : 0ull);
     const unsigned long long x2 = w == 0 ? t2 : (w == 1 ? t1 : t0);
