@@ -8,9 +8,10 @@
 // FP32 in tensor memory:
 //   TMEM lane   = j (128 per tile; the contiguous index of C, so stores coalesce)
 //   TMEM column = b * 8 TN + l * TN + (i - i0)   (TN per level, 8 levels)
-// The trailing update takes TN = 64 (8 levels fill the 512 columns, one accumulator
-// b = 0); the Gaussian epilogues take TN = 32 and two accumulators, so one tile's MMAs
-// run while the epilogue drains the previous tile.  A tile runs kchunks 64-deep K
+// Every mode takes TN = 64 by default (8 levels fill the 512 columns, one accumulator
+// b = 0, handed back once the levels are merged, so the next tile's MMAs run under the
+// rest of the epilogue); TN = 32 gives two accumulators, so one tile's MMAs run while
+// the epilogue drains the previous tile.  A tile runs kchunks 64-deep K
 // chunks.  Per chunk the 8 digit planes of the TN i-rows are loaded once
 // (double-buffered) and the 8 planes of the 128 j-rows stream through a ring; each
 // j-plane s meets the i-planes t <= S-1-s in MMAs of N = TN cnt <= 256.
@@ -57,9 +58,10 @@ enum Mode { kSyrk = 0, kKernelMatrix = 1, kPredict = 2 };
 // tile's MMAs run while the epilogue drains the other, the B buffers are half as
 // large (room for a deeper A ring), but each A tile feeds half as many outputs.
 // The trailing update takes 64 (at 39488^2 x 512: 1501 TF/s against 1083 with 32,
-// where the operand feed sets the pace); the FP64-bound Gaussian epilogues take 32.
-// Grouped launches can take either (a batch autotuner chooses).
-template <int MODE, int TN_ = (MODE == kSyrk ? 64 : 32)>
+// where the operand feed sets the pace), and so do the Gaussian kernel matrix (4.53
+// against 4.98 ms at 20000^2) and the prediction.  Grouped updates can take either
+// (a batch autotuner chooses).
+template <int MODE, int TN_ = 64>
 struct Shape {
     static constexpr int TN = TN_;                  // i columns per level
     static constexpr int NBUF = TN_ == 64 ? 1 : 2;  // accumulators in TMEM
@@ -604,10 +606,9 @@ __device__ __forceinline__ void emu_tc_body(const CUtensorMap &mapA, const CUten
                     }
                 }
             } else {
-                // Gaussian epilogues: the FP64 exp dominates; eight columns at a time,
-                // TMEM released once the last eight are in registers.  The per-column
-                // terms (scale |b|^2, b's exponent) are loaded once per tile by the lane
-                // of that column and broadcast; -2 scale 2^e is formed on the bits.
+                // Gaussian epilogues.  The per-column terms (scale |b|^2, b's exponent)
+                // are loaded once per tile by the lane of that column and broadcast;
+                // -2 scale 2^e is formed on the bits.
                 const int ibl = i0 + h * HC + lane;
                 const bool ilv = lane < HC && ibl < pt.iend;
                 const double sBl = ilv ? pt.scale * p.normB[brow + h * HC + lane] : 0.0;
@@ -618,21 +619,45 @@ __device__ __forceinline__ void emu_tc_body(const CUtensorMap &mapA, const CUten
                 double cs[HC];  // kPredict: this thread's k(a_j, b_i) alpha_j, i = column
 #pragma unroll
                 for (int k = 0; k < HC; ++k) cs[k] = 0.0;
+                // one accumulator (TN = 64): merge every column's levels first and hand
+                // the accumulator back, so the next tile's MMAs run under the exps;
+                // two (TN = 32): drain and compute eight columns at a time
+                constexpr bool EARLY = SH::NBUF == 1;
+                long long v64all[EARLY ? HC : 1];
+                if constexpr (EARLY) {
+#pragma unroll
+                    for (int gq = 0; gq < HC / EG; ++gq) {
+                        uint32_t v[S_MAX][EG];
+#pragma unroll
+                        for (int l = 0; l < S_MAX; ++l)
+                            if (l < S) tmem_ld4(tbuf + (uint32_t)(l * TN + h * HC + gq * EG), v[l]);
+                        tmem_ld_wait();
+                        merge8(v, v64all + gq * EG);
+                    }
+                    fence_before_sync();
+                    mbar_arrive(&tEmpty[tb]);
+                }
 #pragma unroll
                 for (int gq = 0; gq < HC / EG; ++gq) {
                     const int cb = h * HC + gq * EG;
-                    uint32_t v[S_MAX][EG];
-#pragma unroll
-                    for (int l = 0; l < S_MAX; ++l)
-                        if (l < S) tmem_ld4(tbuf + (uint32_t)(l * TN + cb), v[l]);
-                    tmem_ld_wait();
-                    if (gq == HC / EG - 1) {
-                        fence_before_sync();
-                        mbar_arrive(&tEmpty[tb]);
-                    }
-                    if (!ok) continue;
                     long long v64[EG];
-                    merge8(v, v64);
+                    if constexpr (EARLY) {
+                        if (!ok) continue;
+#pragma unroll
+                        for (int col = 0; col < EG; ++col) v64[col] = v64all[gq * EG + col];
+                    } else {
+                        uint32_t v[S_MAX][EG];
+#pragma unroll
+                        for (int l = 0; l < S_MAX; ++l)
+                            if (l < S) tmem_ld4(tbuf + (uint32_t)(l * TN + cb), v[l]);
+                        tmem_ld_wait();
+                        if (gq == HC / EG - 1) {
+                            fence_before_sync();
+                            mbar_arrive(&tEmpty[tb]);
+                        }
+                        if (!ok) continue;
+                        merge8(v, v64);
+                    }
 #pragma unroll
                     for (int col = 0; col < EG; ++col) {
                         const int il = cb + col;
@@ -660,27 +685,34 @@ __device__ __forceinline__ void emu_tc_body(const CUtensorMap &mapA, const CUten
                             cs[gq * EG + col] = valid ? kv * aw : 0.0;
                         }
                     }
-                }
-                if constexpr (MODE == kPredict) {
-                    // column sums over the warp's 32 rows by recursive halving: each
-                    // step a lane keeps half of its columns and adds its partner's
-                    // values for them (9 FP64 adds for 8 columns, not 5 per column);
-                    // lanes 4m end with the sum of column (lane bits 4, 3, 2)
-                    static_assert(HC == 8, "the halving below is written for 8 columns");
-                    const bool h16 = (lane & 16) != 0, h8 = (lane & 8) != 0, h4 = (lane & 4) != 0;
-                    double v4[4], v2[2];
+                    if constexpr (MODE == kPredict) {
+                        if ((gq + 1) * EG % 8 == 0) {
+                            // eight columns complete: their sums over the warp's 32 rows
+                            // by recursive halving.  Each step a lane keeps half of its
+                            // columns and adds its partner's values for them (9 FP64
+                            // adds for 8 columns, not 5 per column); lanes 4m end with
+                            // the sum of column (lane bits 4, 3, 2).  The lanes are
+                            // paired by distance 16, 8, 4, 2, 1 for every column.
+                            const int hb = (gq + 1) * EG - 8;  // first column of the eight
+                            const bool h16 = (lane & 16) != 0, h8 = (lane & 8) != 0,
+                                       h4 = (lane & 4) != 0;
+                            double v4[4], v2[2];
 #pragma unroll
-                    for (int k = 0; k < 4; ++k)
-                        v4[k] = (h16 ? cs[k + 4] : cs[k]) +
-                                __shfl_xor_sync(0xffffffffu, h16 ? cs[k] : cs[k + 4], 16);
+                            for (int k = 0; k < 4; ++k)
+                                v4[k] = (h16 ? cs[hb + k + 4] : cs[hb + k]) +
+                                        __shfl_xor_sync(0xffffffffu, h16 ? cs[hb + k] : cs[hb + k + 4], 16);
 #pragma unroll
-                    for (int k = 0; k < 2; ++k)
-                        v2[k] = (h8 ? v4[k + 2] : v4[k]) +
-                                __shfl_xor_sync(0xffffffffu, h8 ? v4[k] : v4[k + 2], 8);
-                    double v1 = (h4 ? v2[1] : v2[0]) + __shfl_xor_sync(0xffffffffu, h4 ? v2[0] : v2[1], 4);
-                    v1 += __shfl_xor_sync(0xffffffffu, v1, 2);
-                    v1 += __shfl_xor_sync(0xffffffffu, v1, 1);
-                    if ((lane & 3) == 0) red[q][h * HC + (h16 ? 4 : 0) + (h8 ? 2 : 0) + (h4 ? 1 : 0)] = v1;
+                            for (int k = 0; k < 2; ++k)
+                                v2[k] = (h8 ? v4[k + 2] : v4[k]) +
+                                        __shfl_xor_sync(0xffffffffu, h8 ? v4[k] : v4[k + 2], 8);
+                            double v1 = (h4 ? v2[1] : v2[0]) +
+                                        __shfl_xor_sync(0xffffffffu, h4 ? v2[0] : v2[1], 4);
+                            v1 += __shfl_xor_sync(0xffffffffu, v1, 2);
+                            v1 += __shfl_xor_sync(0xffffffffu, v1, 1);
+                            if ((lane & 3) == 0)
+                                red[q][h * HC + hb + (h16 ? 4 : 0) + (h8 ? 2 : 0) + (h4 ? 1 : 0)] = v1;
+                        }
+                    }
                 }
             }
             if (MODE == kPredict) {
@@ -1143,11 +1175,12 @@ int launch_gauss(int mode, const GaussBufs &b, int na, int nb, int d, int S, dou
     const int kp = feature_pad(d), rpa = rows_pad(na), rpb = rows_pad(nb);
     CUtensorMap mA, mB;
     int st = make_plane_map(&mA, b.dA, kp, rpa, S, TM);
-    if (st == QMLG_OK) st = make_plane_map(&mB, b.dB, kp, rpb, S, Shape<kKernelMatrix>::TN);
+    const int TNm = mode == kKernelMatrix ? Shape<kKernelMatrix>::TN : Shape<kPredict>::TN;
+    if (st == QMLG_OK) st = make_plane_map(&mB, b.dB, kp, rpb, S, TNm);
     if (st != QMLG_OK) return st;
     set_smem_attrs();
     TileArgs a{};
-    a.ntiles = count_tiles(0, na, 0, nb, sym ? 1 : 0, Shape<kKernelMatrix>::TN, a.tj);
+    a.ntiles = count_tiles(0, na, 0, nb, sym ? 1 : 0, TNm, a.tj);
     a.C = K;
     a.ldc = ldk;
     a.jbase = 0;
@@ -1358,7 +1391,7 @@ extern "C" int qmlg_predict_emulated_async(const double *Xtrain, int64_t ldtrain
     // launch without the trailing flag read (launch_gauss reads it synchronously)
     CUtensorMap mA, mB;
     st = make_plane_map(&mA, b.dA, kp, rpa, S_MAX, TM);
-    if (st == QMLG_OK) st = make_plane_map(&mB, b.dB, kp, rpb, S_MAX, Shape<kKernelMatrix>::TN);
+    if (st == QMLG_OK) st = make_plane_map(&mB, b.dB, kp, rpb, S_MAX, Shape<kPredict>::TN);
     if (st != QMLG_OK) return st;
     set_smem_attrs();
     TileArgs a{};
