@@ -1121,37 +1121,71 @@ trsv_bwd_solved_kernel(const double *__restrict__ A, int64_t lda, int n,
     }
 }
 
-// Capture-safe triangular solves with the block inverses: one launch per 64-row
-// block and direction, so no CTA ever waits for another and any number of them may
-// run side by side (batched, graph-recorded solves).  Launch k of L z = b: CTA 0
-// applies z_{k-1} to block k and solves it with the block inverse, while CTAs 1..
-// apply z_{k-1} to the rows below block k (a warp per row).  Launch k of L^T x = z
-// (k descending): CTA 0 applies x_{k+1} to block k and solves it with the
-// transposed inverse, while CTAs 1.. apply x_{k+1} to the entries left of block k
-// (four threads per entry).
+// Capture-safe triangular solves with the block inverses: one launch per pair of
+// 64-row blocks and direction, so no CTA ever waits for another and any number of
+// them may run side by side (batched, graph-recorded solves).
+//  * Launch t of L z = b covers blocks 2t and 2t+1.  CTA 0 applies the previous
+//    pair z_{2t-2}, z_{2t-1} to the pair's 128 rows, solves block 2t with its
+//    inverse, applies z_{2t} to block 2t+1 and solves that; CTAs 1.. apply the
+//    previous pair to the rows below (a warp per row, 128 columns).
+//  * Launch u of L^T x = z covers blocks hi = nblk-1-2u and hi-1.  CTA 0 applies the
+//    pair above, x_{hi+1}, x_{hi+2}, to the pair's 128 entries, solves block hi with
+//    the transposed inverse, applies x_hi to block hi-1 and solves that; CTAs 1..
+//    apply the pair above to the entries left of the pair (four threads per entry).
+// Every row and entry is updated by one fixed thread group whatever the grid, so
+// the result does not depend on how many CTAs a launch has.
 constexpr int STEP_THREADS = 256;
 
 __device__ __forceinline__ void trsv_fwd_step(const double *__restrict__ A, int64_t lda, int n,
                                               const double *__restrict__ Linv,
-                                              double *__restrict__ x, int k, int bid, int nctas)
+                                              double *__restrict__ x, int t, int bid, int nctas)
 {
-    __shared__ double zp[NB], bb[NB];
+    __shared__ double zp[2 * NB], bb[2 * NB], zs[NB];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int k0 = k * NB, nb = min(NB, n - k0), kp = k0 - NB;  // block k-1 is full
-    if (k > 0 && tid < NB) zp[tid] = x[kp + tid];
+    const int nblk = (n + NB - 1) / NB;
+    const int b0 = 2 * t, b1 = b0 + 1, r0 = b0 * NB, pc = r0 - 2 * NB;  // the previous pair is full
+    if (t > 0 && tid < 2 * NB) zp[tid] = x[pc + tid];
     __syncthreads();
     if (bid == 0) {
-        const double s = k > 0 ? gemv64_row(A + (int64_t)k0 * lda + kp, lda, zp, tid, nb) : 0.0;
-        if ((tid & 3) == 0) bb[tid >> 2] = (tid >> 2) < nb ? x[k0 + (tid >> 2)] - s : 0.0;
+        // bb = the pair's rows of x less the previous pair's contribution (a thread
+        // pair per row, 64 columns each)
+        {
+            const int rl = tid >> 1, hf = tid & 1, r = r0 + rl;
+            double s = 0.0;
+            if (t > 0 && r < n) {
+                const double *row = A + (int64_t)r * lda + pc + hf * NB;
+#pragma unroll 16
+                for (int c = 0; c < NB; ++c) s = fma(row[c], zp[hf * NB + c], s);
+            }
+            s += __shfl_xor_sync(0xffffffffu, s, 1);
+            if (hf == 0) bb[rl] = r < n ? x[r] - s : 0.0;
+        }
         __syncthreads();
-        const double z = gemv64_row(Linv + (int64_t)k * NB * NB, NB, bb, tid, NB);
-        if ((tid & 3) == 0 && (tid >> 2) < nb) x[k0 + (tid >> 2)] = z;
-    } else if (k > 0) {
+        const int nb0 = min(NB, n - r0);
+        const double z0 = gemv64_row(Linv + (int64_t)b0 * NB * NB, NB, bb, tid, NB);
+        if ((tid & 3) == 0) {
+            const int rr = tid >> 2;
+            zs[rr] = rr < nb0 ? z0 : 0.0;
+            if (rr < nb0) x[r0 + rr] = z0;
+        }
+        if (b1 < nblk) {
+            __syncthreads();
+            const int r1 = r0 + NB, nb1 = min(NB, n - r1);  // block b0 is full here
+            const double s1 = gemv64_row(A + (int64_t)r1 * lda + r0, lda, zs, tid, nb1);
+            if ((tid & 3) == 0 && (tid >> 2) < nb1) bb[NB + (tid >> 2)] -= s1;
+            __syncthreads();
+            const double z1 = gemv64_row(Linv + (int64_t)b1 * NB * NB, NB, bb + NB, tid, NB);
+            if ((tid & 3) == 0 && (tid >> 2) < nb1) x[r1 + (tid >> 2)] = z1;
+        }
+    } else if (t > 0) {
         constexpr int nw = STEP_THREADS / 32;
         const int tw = (nctas - 1) * nw;
-        for (int r = k0 + NB + (bid - 1) * nw + warp; r < n; r += tw) {
-            const double *row = A + (int64_t)r * lda + kp;
-            double sum = fma(row[lane], zp[lane], row[lane + 32] * zp[lane + 32]);
+        for (int r = r0 + 2 * NB + (bid - 1) * nw + warp; r < n; r += tw) {
+            const double *row = A + (int64_t)r * lda + pc;
+            double sum = row[lane] * zp[lane];
+            sum = fma(row[lane + 32], zp[lane + 32], sum);
+            sum = fma(row[lane + 64], zp[lane + 64], sum);
+            sum = fma(row[lane + 96], zp[lane + 96], sum);
             for (int off = 16; off > 0; off >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, off);
             if (lane == 0) x[r] -= sum;
         }
@@ -1160,61 +1194,103 @@ __device__ __forceinline__ void trsv_fwd_step(const double *__restrict__ A, int6
 
 __global__ void __launch_bounds__(STEP_THREADS)
 trsv_fwd_step_kernel(const double *__restrict__ A, int64_t lda, int n,
-                     const double *__restrict__ Linv, double *__restrict__ x, int k)
+                     const double *__restrict__ Linv, double *__restrict__ x, int t)
 {
-    trsv_fwd_step(A, lda, n, Linv, x, k, blockIdx.x, gridDim.x);
+    trsv_fwd_step(A, lda, n, Linv, x, t, blockIdx.x, gridDim.x);
 }
 
 __device__ __forceinline__ void trsv_bwd_step(const double *__restrict__ A, int64_t lda, int n,
                                               const double *__restrict__ Linv,
-                                              double *__restrict__ x, int k, int bid, int nctas)
+                                              double *__restrict__ x, int u, int bid, int nctas)
 {
-    __shared__ double xp[NB], bb[NB];
-    const int tid = threadIdx.x, t = tid >> 2, q = tid & 3;
+    __shared__ double xp[2 * NB], bb[2 * NB], xs[NB];
+    const int tid = threadIdx.x;
     const int nblk = (n + NB - 1) / NB;
-    const int k0 = k * NB, nb = min(NB, n - k0), k1 = k0 + NB;
-    const int nbp = k + 1 < nblk ? min(NB, n - k1) : 0;  // rows of block k+1
-    if (tid < NB) xp[tid] = tid < nbp ? x[k1 + tid] : 0.0;
+    const int hi = nblk - 1 - 2 * u, lo = hi - 1;   // lo < 0: the pair is one block
+    const int a0 = (hi + 1) * NB;                    // first row of the pair above
+    const int na = max(0, min(2 * NB, n - a0));      // its rows
+    const int c0 = (lo >= 0 ? lo : hi) * NB;         // first entry of this pair
+    if (tid < 2 * NB) xp[tid] = tid < na ? x[a0 + tid] : 0.0;
     __syncthreads();
     if (bid == 0) {
-        // block k is full when block k+1 exists
-        double s = 0.0;
-#pragma unroll
-        for (int c = 0; c < 16; ++c) {
-            const int r = q + 4 * c;
-            if (r < nbp) s = fma(A[(int64_t)(k1 + r) * lda + k0 + t], xp[r], s);
+        // bb = the pair's entries of x less the pair above's contribution (a thread
+        // pair per entry, 64 rows each)
+        {
+            const int el = tid >> 1, hf = tid & 1, c = c0 + el;
+            const int cend = hi * NB + min(NB, n - hi * NB);
+            double s = 0.0;
+            if (c < cend) {
+                const int rb = hf * NB, rn = min(NB, na - rb);
+                for (int j = 0; j < rn; ++j) s = fma(A[(int64_t)(a0 + rb + j) * lda + c], xp[rb + j], s);
+            }
+            s += __shfl_xor_sync(0xffffffffu, s, 1);
+            if (hf == 0) bb[el] = c < cend ? x[c] - s : 0.0;
         }
-        s += __shfl_xor_sync(0xffffffffu, s, 1);
-        s += __shfl_xor_sync(0xffffffffu, s, 2);
-        if (q == 0) bb[t] = t < nb ? x[k0 + t] - s : 0.0;
         __syncthreads();
-        const double v = gemv64_col(Linv + (int64_t)k * NB * NB, NB, bb, tid);
-        if (q == 0 && t < nb) x[k0 + t] = v;
-    } else if (nbp > 0) {
+        const int t = tid >> 2, q = tid & 3;
+        const int bh = lo >= 0 ? NB : 0;             // block hi's offset in bb
+        const int nbh = min(NB, n - hi * NB);
+        const double v = gemv64_col(Linv + (int64_t)hi * NB * NB, NB, bb + bh, tid);
+        if (q == 0) {
+            xs[t] = t < nbh ? v : 0.0;
+            if (t < nbh) x[hi * NB + t] = v;
+        }
+        if (lo >= 0) {
+            __syncthreads();
+            // bb_lo[t] -= sum_r L[hi*64 + r][lo*64 + t] x_hi[r]
+            double s = 0.0;
+#pragma unroll
+            for (int c = 0; c < 16; ++c) {
+                const int r = q + 4 * c;
+                if (r < nbh) s = fma(A[(int64_t)(hi * NB + r) * lda + lo * NB + t], xs[r], s);
+            }
+            s += __shfl_xor_sync(0xffffffffu, s, 1);
+            s += __shfl_xor_sync(0xffffffffu, s, 2);
+            if (q == 0) bb[t] -= s;
+            __syncthreads();
+            const double w = gemv64_col(Linv + (int64_t)lo * NB * NB, NB, bb, tid);
+            if (q == 0) x[lo * NB + t] = w;
+        }
+    } else if (na > 0) {
+        const int t = tid >> 2, q = tid & 3;
         constexpr int per = STEP_THREADS / 4;
         const int tc = (nctas - 1) * per;
-        for (int c0 = (bid - 1) * per; c0 < k0; c0 += tc) {
-            const int c = c0 + t;
+        for (int e0 = (bid - 1) * per; e0 < c0; e0 += tc) {
+            const int c = e0 + t;
             double s = 0.0;
-            if (c < k0) {
-#pragma unroll
-                for (int j = 0; j < 16; ++j) {
+            if (c < c0) {
+#pragma unroll 8
+                for (int j = 0; j < 32; ++j) {
                     const int r = q + 4 * j;
-                    if (r < nbp) s = fma(A[(int64_t)(k1 + r) * lda + c], xp[r], s);
+                    if (r < na) s = fma(A[(int64_t)(a0 + r) * lda + c], xp[r], s);
                 }
             }
             s += __shfl_xor_sync(0xffffffffu, s, 1);
             s += __shfl_xor_sync(0xffffffffu, s, 2);
-            if (q == 0 && c < k0) x[c] -= s;
+            if (q == 0 && c < c0) x[c] -= s;
         }
     }
 }
 
 __global__ void __launch_bounds__(STEP_THREADS)
 trsv_bwd_step_kernel(const double *__restrict__ A, int64_t lda, int n,
-                     const double *__restrict__ Linv, double *__restrict__ x, int k)
+                     const double *__restrict__ Linv, double *__restrict__ x, int u)
 {
-    trsv_bwd_step(A, lda, n, Linv, x, k, blockIdx.x, gridDim.x);
+    trsv_bwd_step(A, lda, n, Linv, x, u, blockIdx.x, gridDim.x);
+}
+
+// CTAs beside CTA 0 in launch t of L z = b: 32 rows below the pair each (a warp
+// per row); in launch u of L^T x = z: 64 entries left of the pair each.
+inline int trsv_fwd_extra(int n, int t, int64_t cap)
+{
+    const int below = n - (2 * t + 2) * NB;
+    return (t > 0 && below > 0) ? (int)std::min<int64_t>((below + 31) / 32, cap) : 0;
+}
+
+inline int trsv_bwd_extra(int n, int u, int64_t cap)
+{
+    const int nblk = (n + NB - 1) / NB, lo = nblk - 2 - 2 * u;
+    return (u > 0 && lo > 0) ? (int)std::min<int64_t>(((int64_t)lo * NB + 63) / 64, cap) : 0;
 }
 
 // Both triangular solves in one CTA, with the block inverses: no waiting between
@@ -1623,16 +1699,12 @@ int emulated_potrs(const EmulatedFactor &f, double *x, cudaStream_t s)
             return check_launch();
         }
         const int64_t cap = 4 * (int64_t)std::max(1, tc_sm_count());
-        for (int k = 0; k < nblk; ++k) {
-            const int below = n - (k + 1) * NB;
-            const int extra = (k > 0 && below > 0) ? (int)std::min<int64_t>(ceil_div(below, 32), cap) : 0;
-            trsv_fwd_step_kernel<<<1 + extra, STEP_THREADS, 0, s>>>(A, lda, n, Linv, x, k);
-        }
-        for (int k = nblk - 1; k >= 0; --k) {
-            const int extra = (k + 1 < nblk && k > 0) ? (int)std::min<int64_t>(ceil_div(k * NB, 64), cap) : 0;
-            trsv_bwd_step_kernel<<<1 + extra, STEP_THREADS, 0, s>>>(A, lda, n, Linv, x, k);
-        }
-        count_launches(2 * nblk);
+        const int steps = (nblk + 1) / 2;
+        for (int t = 0; t < steps; ++t)
+            trsv_fwd_step_kernel<<<1 + trsv_fwd_extra(n, t, cap), STEP_THREADS, 0, s>>>(A, lda, n, Linv, x, t);
+        for (int u = 0; u < steps; ++u)
+            trsv_bwd_step_kernel<<<1 + trsv_bwd_extra(n, u, cap), STEP_THREADS, 0, s>>>(A, lda, n, Linv, x, u);
+        count_launches(2 * steps);
         return check_launch();
     }
     const int nblk = (int)ceil_div(n, NB), count = 2 * nblk * NB;
@@ -2534,29 +2606,25 @@ extern "C" int qmlg_fit_batched_async(const QmlgBatchProblem *problems, int coun
     const int cap = 4 * std::max(1, qmlg::tc_sm_count());
     auto solve = [&](double *(*xsel)(const BatchFit &)) -> int {
         int rc = QMLG_OK;
-        for (int t = 0; t < maxblk && rc == QMLG_OK; ++t)
+        // one launch per pair of 64-row blocks and direction (en.k: the pair)
+        const int maxsteps = (maxblk + 1) / 2;
+        for (int t = 0; t < maxsteps && rc == QMLG_OK; ++t)
             rc = run([&](int grid) { fwd_group_kernel<<<grid, STEP_THREADS, 0, s>>>(L.g); },
                      [&](const BatchFit &f, BatchEntry &en) {
-                         if (t >= f.nblk) return 0;
+                         if (2 * t >= f.nblk) return 0;
                          base_entry(f, en);
                          en.x = xsel(f);
                          en.k = t;
-                         const int below = f.n - (t + 1) * NB;
-                         return 1 + ((t > 0 && below > 0)
-                                         ? (int)std::min<int64_t>(qmlg::ceil_div(below, 32), cap)
-                                         : 0);
+                         return 1 + trsv_fwd_extra(f.n, t, cap);
                      });
-        for (int t = 0; t < maxblk && rc == QMLG_OK; ++t)
+        for (int u = 0; u < maxsteps && rc == QMLG_OK; ++u)
             rc = run([&](int grid) { bwd_group_kernel<<<grid, STEP_THREADS, 0, s>>>(L.g); },
                      [&](const BatchFit &f, BatchEntry &en) {
-                         if (t >= f.nblk) return 0;
-                         const int k = f.nblk - 1 - t;
+                         if (2 * u >= f.nblk) return 0;
                          base_entry(f, en);
                          en.x = xsel(f);
-                         en.k = k;
-                         return 1 + ((k + 1 < f.nblk && k > 0)
-                                         ? (int)std::min<int64_t>(qmlg::ceil_div(k * NB, 64), cap)
-                                         : 0);
+                         en.k = u;
+                         return 1 + trsv_bwd_extra(f.n, u, cap);
                      });
         return rc;
     };
