@@ -1,5 +1,5 @@
-// Blocked Cholesky factorisation, triangular solves, double-double residual and
-// the refinement driver behind qmlg_solve.
+// Blocked Cholesky factorisation, triangular solves, the exact residual and the
+// refinement driver behind qmlg_solve.
 //
 // Restates fcho_solve (qml/fcho_solve.f90:23-52): dpotrf("U") then dpotrs("U",
 // nrhs=1) on a column-major matrix.  Kernels work on the row-major view of the
@@ -1893,7 +1893,7 @@ int read_info(SolveCtx &c, int &info)
     return qmlg::read_back(&info, c.d_info, sizeof(int), c.s);
 }
 
-// Iterative refinement: r = y - (A + lambda I) x in double-double, dx = solve(r),
+// Iterative refinement: r = y - (A + lambda I) x summed exactly, dx = solve(r),
 // x += dx, until |dx|/|x| <= tol or the correction stops shrinking.
 template <class SolveFn>
 int refine(SolveCtx &c, const QmlgRefineOpts &o, SolveFn solve_fn, QmlgSolveReport &rep,

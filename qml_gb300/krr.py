@@ -9,7 +9,7 @@ tests and tutorial (tests/test_energy_krr_cmat.py:66-113, docs/source/tutorial.r
 precision "fp64" runs the plain FP64 kernels and factorisation; "mixed" forms the
 Gaussian contractions and the Cholesky trailing updates as emulated-FP64 products
 on the bf16 tensor cores (each kernel entry within 1e-12 of FP64) and refines
-alpha with a double-double residual.
+alpha on the exactly summed residual.
 
 All tensors stay in HBM; ``KRR`` keeps the training representations and alpha
 resident so that predictions reuse them.

@@ -1,5 +1,6 @@
 """Cholesky solve on the GPU: LAPACK semantics (plain FP64) and the mixed path
-(emulated-FP64 tensor-core factor + double-double refinement) against the oracle.
+(emulated-FP64 tensor-core factor + refinement on the exact residual) against the
+oracle.
 The mixed path's bar is <= 1e-8 relative error on alpha against the refined
 oracle solution for the same FP64 K."""
 import numpy as np
@@ -69,7 +70,7 @@ def test_fp64_solve_matches_lapack(cuda, oracle, krr_system, n):
     xr = oracle.refined_solve(K, y[:n], lam)
     # same algorithm class as LAPACK: forward error of the order cond * u
     assert rel(x, xr) < 1e-5 and rel(xl, xr) < 1e-5
-    # with double-double refinement: agrees with the refined oracle to <= 1e-12
+    # with refinement on the exact residual: agrees with the refined oracle to <= 1e-12
     x2, rep2 = core.solve(Kt.clone(), torch.from_numpy(y[:n]).to(cuda), lam, precision="fp64",
                           max_outer=10)
     assert rel(x2.cpu().numpy(), xr) < 1e-12
@@ -124,10 +125,11 @@ def test_mixed_solve_deterministic(cuda, oracle, krr_system):
     assert np.array_equal(runs[0], runs[1])
 
 
-@pytest.mark.parametrize("n", [129, 1000])
+@pytest.mark.parametrize("n", [129, 192, 257, 1000, 1500])
 def test_mixed_solve_stepped_triangular_solves(cuda, oracle, krr_system, n):
     # with cooperative launches off (batched and graph-recorded solves), the
-    # triangular solves run one launch per block; the refined answer is the same
+    # triangular solves run one launch per pair of 64-row blocks (odd and even block
+    # counts, full and short last blocks); the refined answer is the same
     X, y = krr_system
     K = np.ascontiguousarray(oracle.gaussian_kernel(X[:n], X[:n], 1000.0))
     xr = oracle.refined_solve(K, y[:n], 1e-8)
