@@ -562,6 +562,14 @@ int qmlg_residual_dd(const double *A, int n, int64_t lda, const double *diag, do
 size_t qmlg_selftest_wait_timeout_workspace_size(void);
 int qmlg_selftest_wait_timeout(void *workspace, size_t ws_bytes, void *stream);
 
+/*
+ * The exp of the tensor-core Gaussian epilogues, element-wise (no reference
+ * counterpart; exposed so that its accuracy can be checked against the library exp):
+ * y[i] = exp(x[i]) for x[i] <= 0, fixed-point table reduction, at most a few ulp;
+ * x[i] > 0 reads as 0 (the epilogue clamps distances that round below 0).
+ */
+int qmlg_epilogue_exp(const double *x, double *y, int n, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -115,6 +115,7 @@ SIGNATURES = {
     "qmlg_predict_workspace_size": (_SZ, [_I, _I]),
     "qmlg_predict_fused": (_I, [_I, _P, _I64, _I, _P, _I64, _I, _I, _D, _P, _P, _P, _SZ, _P]),
     "qmlg_predict_fused_noalloc": (_I, [_I, _P, _I64, _I, _P, _I64, _I, _I, _D, _P, _P, _P]),
+    "qmlg_epilogue_exp": (_I, [_P, _P, _I, _P]),
     "qmlg_cholesky_workspace_size": (_SZ, [_I]),
     "qmlg_cholesky": (_I, [_P, _I, _I64, _D, _P, _SZ, _P]),
     "qmlg_cholesky_mixed_workspace_size": (_SZ, [_I]),

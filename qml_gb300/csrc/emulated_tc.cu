@@ -186,85 +186,58 @@ __device__ __forceinline__ double pow2i(int e)
     return ldexp(1.0, e);
 }
 
-// A double of magnitude below 2^128 truncated to FP32 on the bits (magnitudes below
-// 2^-126 read as 0), and an FP32 (normal or zero) as the exact FP64, on the bits.
-__device__ __forceinline__ float trunc_to_float(double x)
-{
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    const int e32 = (int)((b >> 52) & 0x7ff) - 896;
-    return e32 > 0 ? __uint_as_float((uint32_t)((b >> 32) & 0x80000000u) | ((uint32_t)e32 << 23) |
-                                     (uint32_t)((b >> 29) & 0x7fffffu))
-                   : 0.0f;
-}
-
-__device__ __forceinline__ double float_to_double_bits(float f)
-{
-    const uint32_t b = __float_as_uint(f);
-    const uint32_t e = (b >> 23) & 0xffu;
-    return e ? __longlong_as_double((long long)(((unsigned long long)(b & 0x80000000u) << 32) |
-                                                ((unsigned long long)(e + 896u) << 52) |
-                                                ((unsigned long long)(b & 0x7fffffu) << 29)))
-             : 0.0;
-}
-
 // exp(x) for the Gaussian epilogues, x <= 0 after clamping, by table-driven reduction
 // (P. T. P. Tang, "Table-driven implementation of the exponential function in IEEE
-// floating-point arithmetic", ACM TOMS 15(2), 1989):
-//   x = (128 m + j) ln2/128 + r,  exp(x) = 2^m 2^(j/128) e^r,
-// 2^(j/128) from a (lead, trail) table and 2^m applied to the exponent bits.  FP64
-// instructions cost ~64 cycles of a scheduler's FP64 pipe here, FP32 ones one cycle,
-// so only four are FP64: the two FMAs of r = x - n ln2/128 (ln2/128 as hi + lo) and
-// the two of the reconstruction.  The rest runs in FP32 and on the bits:
-// - n = round(x 128/ln2) from x's leading 24 bits; it can be one off the nearest, so
-//   |r| <= 0.53 ln2/128.
-// - r = rh + rl: rh its leading 24 bits, rl the other 29 rounded to FP32.
-// - e^r - 1 = r + r^2/2 + c with c = r^3/6 + r^4/24 + r^5/120 (|c| < 4e-9, the next
-//   term is below 1e-18), c in FP32 from rh (relative error ~6e-7, below 3e-15 of
-//   e^r).  r^2/2 = hp + lo with hp = rh^2/2 (rh^2 exact as an FMA pair), and
-//   rh + hp = s + err exactly (Dekker's fast two-sum, |rh| >= |hp|); then
-//   e^r - 1 = s + t with t = rl + lo + c + err in FP32 (|t| < 5e-9).
-// - e^x = 2^m (T + T s + (T t + Tt)) with 2^(j/128) = T + Tt, T t + Tt in FP32.
-// A host emulation of these steps stays below 2e-15 relative error against an 80-bit
-// reference over 2e7 arguments in [-700, 0]; on the GPU it is within 14 ulp of the
-// library exp over 16M points per range.  x > 0 (and +NaN) is clamped to 0, as the
-// distance formula can round slightly above it; x <= -700 and -NaN go to the
-// library exp.
+// floating-point arithmetic", ACM TOMS 15(2), 1989) carried out in 64-bit fixed
+// point, because FP64 instructions cost ~64 cycles of a scheduler's FP64 pipe on this
+// GPU and the integer ones one or two:
+//   |x| = (256 n + j) ln2/256 - r,  exp(x) = 2^-n 2^(-j/256) e^r,  |r| <= ln2/512.
+// - X = |x| 2^53 exactly from x's bits (truncated below 2^-53; |x| < 700 so X < 2^63);
+//   k = 256 n + j = round(|x| 256/ln2) from the high word of X (256/ln2 2^54).
+// - r = k ln2/256 - |x| in 128 bits (ln2/256 to 2^-116), then to 2^-63.
+// - e^r = 1 + r + r^2/2 + c: r^2 from one 64 x 64 multiply, c = r^3/6 + r^4/24 in FP32
+//   (|c| < 4.2e-10, FP32's error on it below 3e-17), all summed in units of 2^-62.
+// - 2^(-j/256) from a table in units of 2^-63; the 61-bit product is rounded once to
+//   53 bits (nearest, ties to even) and 2^-n goes into the exponent bits.
+// Against the host libm over 4M points per range of [-700, 0], [-1, 0], [-1e-3, 0],
+// [-5, -4] and [-700, -600]: at most 2 ulp, 94% identical away from 0.  x > 0 (and
+// +NaN) is clamped to 0, as the distance formula can round slightly above it;
+// x <= -700 and -NaN go to the library exp.
 __device__ __forceinline__ double exp_nonpos(double x)
 {
     const long long xs = __double_as_longlong(x);
-    if (xs > 0) return 1.0;
+    if (xs >= 0) return 1.0;
     if ((unsigned long long)xs >= 0xC085E00000000000ull) return exp(x);  // bits of -700.0
-    const int n = __float2int_rn(__fmul_rn(trunc_to_float(x), 184.66496523378731f));  // 128/ln2
-    const double nd = float_to_double_bits(__int2float_rn(n));  // |n| < 2^17: exact
-    double r = fma(-nd, kLn2Over128Hi, x);
-    r = fma(-nd, kLn2Over128Lo, r);
-    const unsigned long long rb = (unsigned long long)__double_as_longlong(r);
-    const int ef = (int)((rb >> 52) & 0x7ff);
-    const float rh = trunc_to_float(r);
-    float rl = 0.0f;
-    const uint32_t low = (uint32_t)(rb & 0x1fffffffu);
-    if (ef > 896 && low != 0u) {
-        // low * 2^(ef - 1075), rounded to FP32, with r's sign
-        const uint32_t lb = __float_as_uint(__uint2float_rn(low));
-        const int le = (int)((lb >> 23) & 0xffu) + (ef - 1075);
-        if (le > 0)
-            rl = __uint_as_float((uint32_t)((rb >> 32) & 0x80000000u) | ((uint32_t)le << 23) |
-                                 (lb & 0x7fffffu));
-    }
-    const float c = __fmul_rn(__fmul_rn(rh, rh),
-                              __fmul_rn(rh, __fmaf_rn(rh, __fmaf_rn(rh, 1.0f / 120.0f, 1.0f / 24.0f),
-                                                      1.0f / 6.0f)));
-    const float p = __fmul_rn(rh, rh);
-    const float pe = __fmaf_rn(rh, rh, -p);
-    const float hp = __fmul_rn(0.5f, p);
-    const float lo = __fmaf_rn(rh, rl, __fmul_rn(0.5f, pe));
-    const float sum = __fadd_rn(rh, hp);
-    const float err = __fsub_rn(hp, __fsub_rn(sum, rh));
-    const float t = __fadd_rn(__fadd_rn(__fadd_rn(rl, lo), c), err);
-    const double2 T = kExp2Tab128[n & 127];
-    const float corr = __fmaf_rn(trunc_to_float(T.x), t, trunc_to_float(T.y));
-    const double v = T.x + fma(T.x, float_to_double_bits(sum), float_to_double_bits(corr));
-    return __longlong_as_double(__double_as_longlong(v) + ((long long)(n >> 7) << 52));
+    const unsigned long long u = (unsigned long long)xs & 0x7fffffffffffffffull;
+    const int sh = (int)(u >> 52) - 1022;  // X = |x| 2^53 = m 2^sh
+    const unsigned long long m = (u & 0xfffffffffffffull) | 0x10000000000000ull;
+    const unsigned long long X = sh >= 0 ? (m << sh) : (sh > -64 ? (m >> (-sh)) : 0ull);
+    const unsigned int k = (unsigned int)((__umul64hi(X, kExpK256Q54) + (1ull << 42)) >> 43);
+    // R = k ln2/256 - |x| in units of 2^-116: k L - X 2^63, two words
+    const unsigned long long plo = (unsigned long long)k * kExpL256Lo, xlo = X << 63;
+    const unsigned long long phi = __umul64hi((unsigned long long)k, kExpL256Lo) +
+                                   (unsigned long long)k * kExpL256Hi;
+    const unsigned long long rhi = phi - (X >> 1) - (plo < xlo ? 1ull : 0ull);
+    const long long r = (long long)((rhi << 11) | ((plo - xlo) >> 53));  // units of 2^-63
+    const long long r2 = __mul64hi(r, r);                                // r^2, 2^-62
+    const float rf = __int2float_rn((int)(r >> 24)) * 1.8189894035458565e-12f;  // 2^-39
+    const float c = rf * rf * rf * __fmaf_rn(rf, 1.0f / 24.0f, 1.0f / 6.0f);
+    const long long p = (1ll << 62) + (r >> 1) + (r2 >> 1) +
+                        (long long)__float2int_rn(c * 4.611686018427388e18f);  // e^r, 2^-62
+    const unsigned long long V = __umul64hi(kExp2NegQ63[k & 255], (unsigned long long)p);
+    const int lz = __clzll((long long)V);
+    const unsigned long long W = V << lz;
+    const unsigned int rem = (unsigned int)(W & 0x7ffull);
+    unsigned long long mant = W >> 11;
+    mant += (rem > 0x400u || (rem == 0x400u && (mant & 1ull))) ? 1ull : 0ull;
+    // value = mant 2^-52 2^(2 - lz - n); mant's leading bit carries into the exponent
+    return __longlong_as_double((long long)(((unsigned long long)(1024 - lz - (int)(k >> 8)) << 52) + mant));
+}
+
+__global__ void epilogue_exp_kernel(const double *__restrict__ x, double *__restrict__ y, int n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        y[i] = exp_nonpos(x[i]);
 }
 
 // Grouped launches: the tiles of up to kMaxGroup independent problems in one
@@ -1672,3 +1645,13 @@ int gauss_group_kernel_matrix(const GaussItem *items, int count, int d, __nv_bfl
 }
 
 }  // namespace qmlg
+
+extern "C" int qmlg_epilogue_exp(const double *x, double *y, int n, void *stream)
+{
+    if (n < 0 || (n > 0 && (x == nullptr || y == nullptr))) return QMLG_E_ARG;
+    if (n == 0) return QMLG_OK;
+    const int blocks = (int)std::min<int64_t>(qmlg::ceil_div(n, 256), 152 * 16);
+    epilogue_exp_kernel<<<blocks, 256, 0, qmlg::as_stream(stream)>>>(x, y, n);
+    qmlg::count_launches(1);
+    return qmlg::check_launch();
+}

@@ -145,6 +145,25 @@ def test_emulated_gaussian_small_sigma_falls_back(cuda, oracle):
         assert np.allclose(K, Ko, rtol=1e-12, atol=0)
 
 
+@pytest.mark.parametrize("lo,hi", [(-700.0, 0.0), (-1.0, 0.0), (-1e-3, 0.0), (-5.0, -4.0),
+                                   (-700.0, -600.0), (-1e-12, 0.0)])
+def test_epilogue_exp_against_library_exp(cuda, lo, hi):
+    # the fixed-point exp of the Gaussian epilogues: within 2 ulp of the host libm and
+    # of CUDA's exp (torch.exp) over a million arguments per range
+    rng = np.random.default_rng(int(-lo * 1000) + 7)
+    x = rng.uniform(lo, hi, 1 << 20)
+    x[:8] = [lo, hi, -0.0, 0.0, -1e-300, -np.log(2.0), -1.0, -699.9999]
+    xt = torch.from_numpy(x).to(cuda)
+    y = torch.empty_like(xt)
+    assert core.lib().qmlg_epilogue_exp(xt.data_ptr(), y.data_ptr(), x.size,
+                                        torch.cuda.current_stream().cuda_stream) == 0
+    y = y.cpu().numpy()
+    for ref in (np.exp(x), torch.exp(xt).cpu().numpy()):
+        ulp = np.abs(y - ref) / np.spacing(ref)
+        assert np.max(ulp) <= 2.0, (np.max(ulp), x[np.argmax(ulp)])
+    assert y[2] == 1.0 and y[3] == 1.0 and y[5] == 0.5
+
+
 def test_emulated_predict(cuda, oracle, cm_features):
     rng = np.random.default_rng(4)
     Xtr, Xte = cm_features[:900], cm_features[900:]
