@@ -1,4 +1,4 @@
-// exp(x) for x <= 0 in 64-bit fixed point (the Gaussian and Laplacian epilogues).
+// exp(x) for x <= 0 in 64-bit fixed point, for the tensor-core Gaussian epilogues.
 #pragma once
 
 #include <cstdint>
@@ -7,7 +7,7 @@
 
 namespace {
 
-// exp(x) for the kernel epilogues, x <= 0 after clamping, by table-driven reduction
+// exp(x) for the Gaussian epilogues, x <= 0 after clamping, by table-driven reduction
 // (P. T. P. Tang, "Table-driven implementation of the exponential function in IEEE
 // floating-point arithmetic", ACM TOMS 15(2), 1989) carried out in 64-bit fixed
 // point, because FP64 instructions cost ~64 cycles of a scheduler's FP64 pipe on this
