@@ -308,16 +308,25 @@ class GpuExecutor:
     def launch_predict(self, batch: List[Request]):
         """Enqueue one merged prediction on a free slot; returns (event, finish)
         where finish() copies the results into the requests once the event has
-        completed and frees the slot."""
-        torch = self.torch
+        completed and frees the slot.  If the launch fails (an allocation, for
+        example), the slot's stream is drained and the slot freed before the error
+        propagates, so its staging buffers are never rewritten under a copy."""
         slot = self.free.pop()
+        try:
+            return self._launch_on(slot, batch)
+        except Exception:
+            self.streams[slot].synchronize()
+            self.free.append(slot)
+            raise
+
+    def _launch_on(self, slot: int, batch: List[Request]):
+        torch = self.torch
         stream, st = self.streams[slot], self.staging[slot]
         with self.lock:
             X, alpha, sigma, kernel = self.models[batch[0].model]
         charges, coords, offsets, ranges = merge_molecules(batch)
         n, na = offsets.shape[0] - 1, charges.shape[0]
         if n > self.max_mols or na * 3 > st["coords"].numel():
-            self.free.append(slot)
             raise ValueError("batch larger than the staging buffers")
         st["charges"].numpy()[:na] = charges
         st["coords"].numpy()[:3 * na] = coords.reshape(-1)
@@ -342,23 +351,25 @@ class GpuExecutor:
             ev.record(stream)
 
         def finish():
-            vals = st["out"].numpy()[:n]
-            flag = int(st["flag"][0]) if fast else 0
-            path = ("fixed" if kernel == "laplacian" else "tensor") if fast else "fp64"
-            if kernel == "laplacian" and flag & 8:
-                # the fixed-point bound was not met: the FP64 kernel launched beside
-                # it already wrote the result
-                path = "fp64"
-            elif flag != 0:
-                # the tensor-core bound was not met (or a bounded wait gave up):
-                # recompute this batch with the FP64 kernel
-                with torch.cuda.stream(stream):
-                    vals = self.core.predict(kernel, X, Xq, sigma, alpha).cpu().numpy()
-                path = "fp64"
-            for req, (a, b) in zip(batch, ranges):
-                req.result = vals[a:b].copy()
-                req.path, req.flag = path, flag
-            self.free.append(slot)
+            try:
+                vals = st["out"].numpy()[:n]
+                flag = int(st["flag"][0]) if fast else 0
+                path = ("fixed" if kernel == "laplacian" else "tensor") if fast else "fp64"
+                if kernel == "laplacian" and flag & 8:
+                    # the fixed-point bound was not met: the FP64 kernel launched
+                    # beside it already wrote the result
+                    path = "fp64"
+                elif flag != 0:
+                    # the tensor-core bound was not met (or a bounded wait gave up):
+                    # recompute this batch with the FP64 kernel
+                    with torch.cuda.stream(stream):
+                        vals = self.core.predict(kernel, X, Xq, sigma, alpha).cpu().numpy()
+                    path = "fp64"
+                for req, (a, b) in zip(batch, ranges):
+                    req.result = vals[a:b].copy()
+                    req.path, req.flag = path, flag
+            finally:
+                self.free.append(slot)
         return ev, finish
 
     def run_fit(self, req: Request):
@@ -412,7 +423,11 @@ class Server:
         still = []
         for ev, finish, batch in self.inflight:
             if ev.query():
-                finish()
+                try:
+                    finish()
+                except Exception as e:  # reported on the requests, the server keeps going
+                    for r in batch:
+                        r.error, r.result = repr(e), None
                 t = self.clock()
                 for r in batch:
                     r.done = t
@@ -440,9 +455,16 @@ class Server:
                 continue
             if batch[0].kind == "fit":
                 self.fit_q.put(batch)
-            else:
+                continue
+            try:
                 ev, finish = self.ex.launch_predict(batch)
-                self.inflight.append((ev, finish, batch))
+            except Exception as e:  # reported on the requests, the server keeps going
+                for r in batch:
+                    r.error, r.done = repr(e), t
+                self.sched.release(batch)
+                self.completed.extend(batch)
+                continue
+            self.inflight.append((ev, finish, batch))
 
     def run(self, arrivals: List[Request], idle_sleep: float = 50e-6) -> List[Request]:
         """Serve `arrivals` (sorted by arrival time, relative to start) to completion."""

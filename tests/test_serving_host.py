@@ -199,3 +199,35 @@ def test_server_survives_a_fit_that_fails_to_allocate():
     # everything admitted was released; the two fitted models stay accounted
     assert sched.in_use == resident_bytes(100) + resident_bytes(40)
     assert sched.slots == 0 and not sched.fit_running
+
+
+class FailingLaunchExecutor(FakeExecutor):
+    """A fake whose prediction launches for one model raise (as an allocation that
+    fails would), and whose result copy for another model raises."""
+
+    def launch_predict(self, batch):
+        if batch[0].model == "oom":
+            raise RuntimeError("CUDA out of memory. Tried to allocate 1.00 GiB")
+        ev, finish = super().launch_predict(batch)
+        if batch[0].model == "bad_copy":
+            def fail():
+                raise RuntimeError("copy failed")
+            return ev, fail
+        return ev, finish
+
+
+def test_server_survives_failed_prediction_launches():
+    import time
+    clock = time.perf_counter
+    ex = FailingLaunchExecutor(clock)
+    sched = Scheduler(budget_bytes=1 << 40, max_slots=2,
+                      model_sizes={"m": 100, "oom": 100, "bad_copy": 100})
+    arrivals = [mk(0, "predict", "oom", 3, 0.0), mk(1, "predict", "m", 2, 0.0005),
+                mk(2, "predict", "bad_copy", 4, 0.001), mk(3, "predict", "m", 1, 0.0015)]
+    done = Server(ex, sched, clock=clock).run(arrivals)
+    by = {r.rid: r for r in done}
+    assert len(done) == 4
+    assert "out of memory" in by[0].error and "copy failed" in by[2].error
+    assert by[1].error is None and by[3].error is None and by[1].result is not None
+    # every admitted cost and slot was released
+    assert sched.slots == 0 and sched.in_use == 3 * resident_bytes(100)
