@@ -1569,11 +1569,13 @@ int factor_panel(double *A, int n, int64_t lda, double shift, int K0, int K1, in
 
 // SMs kept free for the panel chain while the rest of the trailing matrix, of order
 // m, is updated beside it.  The update's work grows as m^2 and the chain's as m, so
-// the share grows as m falls: 16, 32 then 48 of 152 SMs.  The bands come from
-// per-step timings at N = 20000 and 40000 with fixed reserves of 4 to 64 SMs.
+// the share grows as m falls: 12, 24 then 40 of 152 SMs.  The bands come from
+// per-step timings at N = 20000 and 40000 with fixed reserves of 4 to 64 SMs, then
+// whole factorisations: 12/24/40 took 639.0 ms at N = 40000 against 641.6 ms for
+// 16/32/48, 646.8 ms for 20/36/52 and 640.0 ms for five finer bands.
 inline int chain_reserve(int sms, int m)
 {
-    const int per152 = m >= 30000 ? 16 : (m >= 17000 ? 32 : 48);
+    const int per152 = m >= 30000 ? 12 : (m >= 17000 ? 24 : 40);
     return std::max(1, per152 * sms / 152);
 }
 
