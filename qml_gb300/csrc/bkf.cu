@@ -13,14 +13,27 @@
 // Storage: the row-major lower triangle W[i][j], i >= j (the column-major lower
 // triangle dsytrf("L") works on, seen transposed).
 //
-// One cooperative kernel runs the whole factorisation, four grid barriers per
-// pivot step: CTA 0 decides the pivot (block reductions), the grid swaps, copies
-// the pivot columns and multipliers, then updates the trailing triangle one row per
-// warp (four independent elements per lane in flight) while writing the L columns.
+// One cooperative kernel runs the whole factorisation, two grid barriers per pivot
+// step:
+//   1. CTA 0 decides the pivot.  Column k comes from a contiguous copy and its
+//      maximum from per-CTA partials, both left by the previous step's update; only
+//      the row-max search reads the matrix (row imax, and column imax, which it
+//      keeps).  CTA 0 then writes the pivot column(s) as they will be after the
+//      interchange and the 2x2 multipliers, all read from before it.
+//   2. The grid applies the interchange, the trailing update and the L columns in
+//      one pass.  Each moved element is read from the copy of row/column kk.  The
+//      trailing triangle is cut into 128-element row segments spread over all
+//      warps, four independent elements per lane.  The segments at the diagonal's
+//      left end also copy out columns k+kstep and k+kstep+1 and the partial maxima
+//      for the next step.
+// The arithmetic is dsytf2's, operation for operation.
 // Everything another CTA wrote since the last barrier is read through L2
-// (ld.global.cg), never through a possibly stale L1 line.  The inverse is the Schur complement left by
-// the first n steps on [[A, I], [I, 0]] with the pivot search confined to A's rows
-// (a symmetric permutation inside A's block leaves that complement -A^-1).
+// (ld.global.cg, never a possibly stale L1 line) by loads that the compiler may not
+// move across the barrier; the step's decision is read once per CTA, by the thread
+// that took part in the barrier's handshake, and shared through shared memory.
+// The inverse is the Schur complement left by the first n steps on [[A, I], [I, 0]]
+// with the pivot search confined to A's rows (a symmetric permutation inside A's
+// block leaves that complement -A^-1).
 #include <algorithm>
 #include <cmath>
 
@@ -42,7 +55,13 @@ struct BkArgs {
     int nsearch;  // pivots are taken, and searched for, among indices < nsearch
     int *ipiv;    // [nsearch]
     int *info;
-    double *x0, *x1;  // [N] copies of the pivot columns / 2x2 multipliers
+    double *col;      // [2][2][N] columns k and k+1 of the current matrix, two generations
+    double *ci;       // [N] column imax below imax, saved by the row-max search
+    double *p0, *p1;  // [N] the pivot column(s) after the interchange
+    double *w0, *w1;  // [N] the 2x2 pivot's multipliers
+    double *sc;       // [4] the pivot block after the interchange
+    double *pv;       // [grid] per-CTA partial column maxima (value, first index)
+    int *pi;
     int *dec;         // [4] the step's decision: kp, kstep, zero column
 };
 
@@ -82,52 +101,160 @@ __device__ void block_argmax(double &v, int &idx, double *sv, int *si)
     __syncthreads();
 }
 
+__device__ __forceinline__ int ld_relaxed_gpu(const int *p)
+{
+    int v;
+    asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Loads through L2 (never a possibly stale L1 line) of what other CTAs wrote before
+// the last grid barrier.  The memory clobber keeps the compiler from moving them
+// above the barrier.
+__device__ __forceinline__ double ld_l2(const double *p)
+{
+    double v;
+    asm volatile("ld.global.cg.f64 %0, [%1];" : "=d"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ int ld_l2(const int *p)
+{
+    int v;
+    asm volatile("ld.global.cg.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Keeps (max |v|, first index) over the values a thread sees.
+__device__ __forceinline__ void argmax_step(double v, int i, double &bv, int &bi)
+{
+    const double av = fabs(v);
+    if (av > bv || (av == bv && i < bi)) {
+        bv = av;
+        bi = i;
+    }
+}
+
+// Writes this CTA's (max, first index) to the partials (all threads take part).
+__device__ void publish_partial(const BkArgs &a, double bv, int bi, double *sv, int *si)
+{
+    block_argmax(bv, bi, sv, si);
+    if (threadIdx.x == 0) {
+        a.pv[blockIdx.x] = bv;
+        a.pi[blockIdx.x] = bi;
+    }
+}
+
+// Copies columns c and c+1 (rows >= c, resp. c+1) of W into column generation g and
+// publishes the partial maxima of column c over rows (c, ns).
+__device__ void load_columns(const BkArgs &a, int c, int gen, double *sv, int *si)
+{
+    const int N = a.N;
+    const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, gsz = (int64_t)gridDim.x * blockDim.x;
+    double *cA = a.col + (int64_t)(2 * gen) * N, *cB = cA + N;
+    double bv = 0.0;
+    int bi = c;
+    for (int64_t i = c + gt; i < N; i += gsz) {
+        const double v = ld_l2(a.W + i * a.ld + c);
+        cA[i] = v;
+        if (i > c && i < a.nsearch) argmax_step(v, (int)i, bv, bi);
+        if (i > c) cB[i] = ld_l2(a.W + i * a.ld + c + 1);
+    }
+    publish_partial(a, bv, bi, sv, si);
+}
+
 __global__ void __launch_bounds__(BK_THREADS) bk_factor_kernel(BkArgs a)
 {
     cg::grid_group g = cg::this_grid();
     __shared__ double sv[BK_THREADS / 32];
     __shared__ int si[BK_THREADS / 32];
+    __shared__ int sdec[3];
     const double alpha = (1.0 + sqrt(17.0)) / 8.0;
     double *W = a.W;
     const int64_t ld = a.ld;
     const int N = a.N, ns = a.nsearch;
     const int tid = threadIdx.x;
-    const int64_t gt = (int64_t)blockIdx.x * blockDim.x + tid, gsz = (int64_t)gridDim.x * blockDim.x;
-    const int warp_g = (int)(gt >> 5), nwarps = (int)(gsz >> 5), lane = tid & 31;
-    int k = 0;
+    const int64_t gt = (int64_t)blockIdx.x * blockDim.x + tid;
+    const unsigned warp_g = (unsigned)(gt >> 5), nwarps = (unsigned)((int64_t)gridDim.x * blockDim.x >> 5);
+    const int lane = tid & 31;
+    int k = 0, gen = 0;
+    load_columns(a, 0, 0, sv, si);
+    bk_sync(g);
     while (k < ns) {
-        // ---- decide the pivot (CTA 0)
+        const double *cA = a.col + (int64_t)(2 * gen) * N, *cB = cA + N;
+        // ---- decide the pivot (CTA 0) from the partial maxima of column k
         if (blockIdx.x == 0) {
             double cm = 0.0;
             int imax = k;
-            for (int i = k + 1 + tid; i < ns; i += BK_THREADS) {
-                const double v = fabs(__ldcg(W + (int64_t)i * ld + k));
-                if (v > cm) {
+            for (int b = tid; b < (int)gridDim.x; b += BK_THREADS) {
+                const double v = ld_l2(a.pv + b);
+                const int i = ld_l2(a.pi + b);
+                if (v > cm || (v == cm && i < imax)) {
                     cm = v;
                     imax = i;
                 }
             }
             block_argmax(cm, imax, sv, si);
-            const double absakk = fabs(__ldcg(W + (int64_t)k * ld + k));
+            const double absakk = fabs(ld_l2(cA + k));
             int kp = k, kstep = 1, zero = 0;
             if (fmax(absakk, cm) == 0.0) {
                 zero = 1;
             } else if (!(absakk >= alpha * cm)) {
-                // rowmax over row/column imax of the trailing block
+                // rowmax over row/column imax of the trailing block; column imax
+                // below imax is kept for the interchange
                 double rm = 0.0;
                 int jdummy = 0;
                 for (int j = k + tid; j < imax; j += BK_THREADS)
-                    rm = fmax(rm, fabs(__ldcg(W + (int64_t)imax * ld + j)));
-                for (int i = imax + 1 + tid; i < ns; i += BK_THREADS)
-                    rm = fmax(rm, fabs(__ldcg(W + (int64_t)i * ld + imax)));
+                    rm = fmax(rm, fabs(ld_l2(W + (int64_t)imax * ld + j)));
+                for (int i = imax + 1 + tid; i < N; i += BK_THREADS) {
+                    const double v = ld_l2(W + (int64_t)i * ld + imax);
+                    a.ci[i] = v;
+                    if (i < ns) rm = fmax(rm, fabs(v));
+                }
                 block_argmax(rm, jdummy, sv, si);
                 if (absakk >= alpha * cm * (cm / rm)) {
                     kp = k;
-                } else if (fabs(__ldcg(W + (int64_t)imax * ld + imax)) >= alpha * rm) {
+                } else if (fabs(ld_l2(W + (int64_t)imax * ld + imax)) >= alpha * rm) {
                     kp = imax;
                 } else {
                     kp = imax;
                     kstep = 2;
+                }
+            }
+            if (!zero) {
+                // The symmetric interchange of kk = k + kstep - 1 and kp, read from
+                // the matrix before it: new (i, j) = old (sig i, sig j).  Column k
+                // (and k+1) come from the column copies, row kp from W, column kp
+                // below kp from the copy the search made.
+                const double *rowp = W + (int64_t)kp * ld;
+                const double *ci = a.ci;
+                if (kstep == 1) {
+                    if (kp != k) {
+                        for (int i = k + 1 + tid; i < N; i += BK_THREADS)
+                            a.p0[i] = i < kp ? ld_l2(rowp + i) : (i == kp ? ld_l2(cA + kp) : ld_l2(ci + i));
+                        if (tid == 0) a.sc[0] = ld_l2(rowp + kp);
+                    } else if (tid == 0) {
+                        a.sc[0] = ld_l2(cA + k);
+                    }
+                } else {
+                    const double d21 = ld_l2(cA + kp);
+                    const double d11 = ld_l2(rowp + kp) / d21;
+                    const double d22 = ld_l2(cA + k) / d21;
+                    const double t = 1.0 / (d11 * d22 - 1.0);
+                    const double e21 = t / d21;
+                    for (int j = k + 2 + tid; j < N; j += BK_THREADS) {
+                        const double ajk = ld_l2(cA + (j == kp ? k + 1 : j));
+                        const double ajk1 = j < kp ? ld_l2(rowp + j) : (j == kp ? ld_l2(rowp + k + 1) : ld_l2(ci + j));
+                        a.p0[j] = ajk;
+                        a.p1[j] = ajk1;
+                        a.w0[j] = e21 * (d11 * ajk - ajk1);   // wk
+                        a.w1[j] = e21 * (d22 * ajk1 - ajk);   // wkp1
+                    }
+                    if (tid == 0) {
+                        a.sc[0] = ld_l2(cA + k);
+                        a.sc[1] = d21;
+                        a.sc[2] = ld_l2(rowp + kp);
+                    }
                 }
             }
             if (tid == 0) {
@@ -138,106 +265,98 @@ __global__ void __launch_bounds__(BK_THREADS) bk_factor_kernel(BkArgs a)
             }
         }
         bk_sync(g);
-        const int kp = __ldcg(a.dec), kstep = __ldcg(a.dec + 1), zero = __ldcg(a.dec + 2);
-        const int kk = k + kstep - 1;
-        // ---- symmetric interchange of kk and kp in the trailing block
-        if (!zero && kp != kk) {
-            // items: [0] the diagonal, (k..kk) row entries, (kk..kp) the middle,
-            // (kp..N) the columns below kp
-            const int nleft = kk - k, nmid = kp - kk - 1, nbelow = N - kp - 1;
-            const int64_t total = 1 + nleft + nmid + nbelow;
-            for (int64_t t = gt; t < total; t += gsz) {
-                double *p, *q;
-                if (t == 0) {
-                    p = W + (int64_t)kk * ld + kk;
-                    q = W + (int64_t)kp * ld + kp;
-                } else if (t <= nleft) {
-                    const int j = k + (int)(t - 1);
-                    p = W + (int64_t)kk * ld + j;
-                    q = W + (int64_t)kp * ld + j;
-                } else if (t <= nleft + nmid) {
-                    const int m = kk + 1 + (int)(t - 1 - nleft);
-                    p = W + (int64_t)m * ld + kk;
-                    q = W + (int64_t)kp * ld + m;
-                } else {
-                    const int i = kp + 1 + (int)(t - 1 - nleft - nmid);
-                    p = W + (int64_t)i * ld + kk;
-                    q = W + (int64_t)i * ld + kp;
-                }
-                const double tmp = __ldcg(p);
-                *p = __ldcg(q);
-                *q = tmp;
-            }
+        // the decision, read once per CTA by the thread that took part in the grid
+        // barrier's handshake and handed to the others through shared memory
+        if (tid == 0) {
+            sdec[0] = ld_relaxed_gpu(a.dec);
+            sdec[1] = ld_relaxed_gpu(a.dec + 1);
+            sdec[2] = ld_relaxed_gpu(a.dec + 2);
         }
-        bk_sync(g);
-        // ---- pivot columns (copies) and 2x2 multipliers
-        if (!zero) {
+        __syncthreads();
+        const int kp = sdec[0], kstep = sdec[1], zero = sdec[2];
+        const int kk = k + kstep - 1, kn = k + kstep;
+        const int ngen = gen ^ 1;
+        double *nA = a.col + (int64_t)(2 * ngen) * N, *nB = nA + N;
+        if (zero) {
+            // nothing to update: the next step's columns straight from W
+            load_columns(a, kn, ngen, sv, si);
+        } else {
+            // ---- the interchange, the trailing update and the L columns, the
+            // trailing triangle cut into 128-element row segments spread over all
+            // warps (four independent elements per lane); the segment at the
+            // diagonal's left end also saves columns kn and kn+1 for the next step
+            const bool swap = kp != kk;
+            // row/column kk before the interchange: column k or k+1 of the copy
+            const double *rkk = kstep == 1 ? cA : cB;
+            const double okk = swap ? ld_l2(rkk + kk) : 0.0;
+            const double *x0 = kstep == 1 ? (swap ? a.p0 : cA) : a.w0;
+            const double *x1 = a.w1;
+            const double *q0 = kstep == 1 ? x0 : a.p0, *q1 = a.p1;
+            double r = 0.0;
             if (kstep == 1) {
-                for (int64_t i = k + 1 + gt; i < N; i += gsz) a.x0[i] = __ldcg(W + i * ld + k);
-            } else {
-                const double d21 = __ldcg(W + (int64_t)(k + 1) * ld + k);
-                const double d11 = __ldcg(W + (int64_t)(k + 1) * ld + k + 1) / d21;
-                const double d22 = __ldcg(W + (int64_t)k * ld + k) / d21;
-                const double t = 1.0 / (d11 * d22 - 1.0);
-                const double e21 = t / d21;
-                for (int64_t j = k + 2 + gt; j < N; j += gsz) {
-                    const double ajk = __ldcg(W + j * ld + k), ajk1 = __ldcg(W + j * ld + k + 1);
-                    a.x0[j] = e21 * (d11 * ajk - ajk1);   // wk
-                    a.x1[j] = e21 * (d22 * ajk1 - ajk);   // wkp1
-                }
+                const double akk = ld_l2(a.sc);
+                r = 1.0 / akk;
+                if (gt == 0) W[(int64_t)k * ld + k] = akk;
+            } else if (gt == 0) {
+                W[(int64_t)k * ld + k] = ld_l2(a.sc);
+                W[(int64_t)(k + 1) * ld + k] = ld_l2(a.sc + 1);
+                W[(int64_t)(k + 1) * ld + k + 1] = ld_l2(a.sc + 2);
             }
-        }
-        bk_sync(g);
-        // ---- trailing update (one row per warp) and the L columns
-        if (!zero) {
-            const double *x0 = a.x0, *x1 = a.x1;
-            if (kstep == 1) {
-                const double r = 1.0 / __ldcg(W + (int64_t)k * ld + k);
-                for (int i = k + 1 + warp_g; i < N; i += nwarps) {
-                    const double xi = __ldcg(x0 + i);
+            double bv = 0.0;
+            int bi = kn;
+            const int m = N - kn;
+            const unsigned nseg = (unsigned)(m + 127) >> 7;
+            const unsigned items = (unsigned)m * nseg;
+            for (unsigned t = warp_g; t < items; t += nwarps) {
+                const unsigned c = t / (unsigned)m, rr = t - c * (unsigned)m;
+                const int i = kn + (int)rr, j0 = kn + (int)(c << 7);
+                if (j0 > i) continue;
+                double *row = W + (int64_t)i * ld;
+                const bool rowkp = swap && i == kp;
+                double ov[4], u[4], v[4];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const int j = j0 + lane + 32 * e;
+                    ov[e] = u[e] = v[e] = 0.0;
+                    if (j <= i) {
+                        // the value of new (i, j) before the update
+                        ov[e] = rowkp ? (j == i ? okk : ld_l2(rkk + j))
+                                      : (swap && j == kp ? ld_l2(rkk + i) : ld_l2(row + j));
+                        u[e] = ld_l2(x0 + j);
+                        if (kstep == 2) v[e] = ld_l2(x1 + j);
+                    }
+                }
+                double nv[4];
+                if (kstep == 1) {
+                    const double xi = ld_l2(q0 + i);
                     const double f = -xi * r;
-                    double *row = W + (int64_t)i * ld;
-                    int j = k + 1 + lane;
-                    for (; j + 96 <= i; j += 128) {  // loads of four elements, then their FMAs
-                        const double r0 = __ldcg(row + j), r1 = __ldcg(row + j + 32);
-                        const double r2 = __ldcg(row + j + 64), r3 = __ldcg(row + j + 96);
-                        const double y0 = __ldcg(x0 + j), y1 = __ldcg(x0 + j + 32);
-                        const double y2 = __ldcg(x0 + j + 64), y3 = __ldcg(x0 + j + 96);
-                        row[j] = fma(f, y0, r0);
-                        row[j + 32] = fma(f, y1, r1);
-                        row[j + 64] = fma(f, y2, r2);
-                        row[j + 96] = fma(f, y3, r3);
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) nv[e] = fma(f, u[e], ov[e]);
+                    if (c == 0 && lane == 0) row[k] = xi * r;
+                } else {
+                    const double aik = ld_l2(q0 + i), aik1 = ld_l2(q1 + i);
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) nv[e] = ov[e] - (aik * u[e] + aik1 * v[e]);
+                    if (c == 0 && lane == 0) {
+                        row[k] = ld_l2(x0 + i);
+                        row[k + 1] = ld_l2(x1 + i);
                     }
-                    for (; j <= i; j += 32) row[j] = fma(f, __ldcg(x0 + j), __ldcg(row + j));
-                    if (lane == 0) row[k] = xi * r;
                 }
-            } else {
-                for (int i = k + 2 + warp_g; i < N; i += nwarps) {
-                    double *row = W + (int64_t)i * ld;
-                    const double aik = __ldcg(row + k), aik1 = __ldcg(row + k + 1);
-                    int j = k + 2 + lane;
-                    for (; j + 96 <= i; j += 128) {
-                        double rv[4], u[4], v[4];
 #pragma unroll
-                        for (int t = 0; t < 4; ++t) {
-                            rv[t] = __ldcg(row + j + 32 * t);
-                            u[t] = __ldcg(x0 + j + 32 * t);
-                            v[t] = __ldcg(x1 + j + 32 * t);
-                        }
-#pragma unroll
-                        for (int t = 0; t < 4; ++t) row[j + 32 * t] = rv[t] - (aik * u[t] + aik1 * v[t]);
+                for (int e = 0; e < 4; ++e) {
+                    const int j = j0 + lane + 32 * e;
+                    if (j <= i) row[j] = nv[e];
+                }
+                if (c == 0) {
+                    if (lane == 0) {
+                        nA[i] = nv[0];
+                        if (i > kn && i < ns) argmax_step(nv[0], i, bv, bi);
+                    } else if (lane == 1 && i > kn) {
+                        nB[i] = nv[0];
                     }
-                    for (; j <= i; j += 32)
-                        row[j] = __ldcg(row + j) - (aik * __ldcg(x0 + j) + aik1 * __ldcg(x1 + j));
                 }
             }
-        }
-        bk_sync(g);
-        if (!zero && kstep == 2) {
-            for (int64_t j = k + 2 + gt; j < N; j += gsz) {
-                W[j * ld + k] = a.x0[j];
-                W[j * ld + k + 1] = a.x1[j];
-            }
+            publish_partial(a, bv, bi, sv, si);
         }
         if (gt == 0) {
             if (kstep == 1) {
@@ -248,7 +367,8 @@ __global__ void __launch_bounds__(BK_THREADS) bk_factor_kernel(BkArgs a)
             }
         }
         bk_sync(g);
-        k += kstep;
+        k = kn;
+        gen = ngen;
     }
 }
 
@@ -384,9 +504,11 @@ __global__ void bk_extract_kernel(const double *__restrict__ W, int n, double *_
     }
 }
 
+constexpr int BK_MAX_GRID = 1024;
+
 struct BkBufs {
-    int *info, *dec, *ipiv;
-    double *W, *x0, *x1;
+    int *info, *dec, *ipiv, *pi;
+    double *W, *col, *ci, *p0, *p1, *w0, *w1, *sc, *pv;
 };
 
 size_t bk_ws(int n, int N)
@@ -396,8 +518,11 @@ size_t bk_ws(int n, int N)
     p.add<int>(4);
     p.add<int>((size_t)std::max(n, 1));
     p.add<double>((size_t)N * N);
-    p.add<double>((size_t)N);
-    p.add<double>((size_t)N);
+    p.add<double>((size_t)4 * N);
+    for (int v = 0; v < 5; ++v) p.add<double>((size_t)N);
+    p.add<double>(4);
+    p.add<double>(BK_MAX_GRID);
+    p.add<int>(BK_MAX_GRID);
     return p.total();
 }
 
@@ -410,13 +535,20 @@ int bk_factor(const double *A, int64_t lda, int n, int N, void *workspace, size_
     b.dec = ws.take<int>(4);
     b.ipiv = ws.take<int>((size_t)std::max(n, 1));
     b.W = ws.take<double>((size_t)N * N);
-    b.x0 = ws.take<double>((size_t)N);
-    b.x1 = ws.take<double>((size_t)N);
+    b.col = ws.take<double>((size_t)4 * N);
+    b.ci = ws.take<double>((size_t)N);
+    b.p0 = ws.take<double>((size_t)N);
+    b.p1 = ws.take<double>((size_t)N);
+    b.w0 = ws.take<double>((size_t)N);
+    b.w1 = ws.take<double>((size_t)N);
+    b.sc = ws.take<double>(4);
+    b.pv = ws.take<double>(BK_MAX_GRID);
+    b.pi = ws.take<int>(BK_MAX_GRID);
     cudaError_t e = cudaMemsetAsync(b.info, 0, sizeof(int), s);
     if (e != cudaSuccess) return qmlg::set_cuda_error(e);
     const int blocks = (int)std::min<int64_t>(qmlg::ceil_div((int64_t)N * N, 256), 152 * 64);
     { bk_build_kernel<<<blocks, 256, 0, s>>>(A, lda, n, N, b.W); qmlg::count_launches(1); }
-    BkArgs a{b.W, (int64_t)N, N, n, b.ipiv, b.info, b.x0, b.x1, b.dec};
+    BkArgs a{b.W, (int64_t)N, N, n, b.ipiv, b.info, b.col, b.ci, b.p0, b.p1, b.w0, b.w1, b.sc, b.pv, b.pi, b.dec};
     int grid = 1;
     if (N > 256 && qmlg::cooperative_allowed_on(s)) {
         int dev = 0, sms = 0, per = 0;
@@ -425,7 +557,8 @@ int bk_factor(const double *A, int64_t lda, int n, int N, void *workspace, size_
             (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, bk_factor_kernel, BK_THREADS, 0)) !=
                 cudaSuccess)
             return qmlg::set_cuda_error(e);
-        grid = std::max(1, std::min(qmlg::sm_limit(sms), sms * std::max(per, 1)));
+        const int lim = qmlg::sm_limit(sms);
+        grid = std::max(1, std::min(lim < sms ? lim : sms * std::max(per, 1), BK_MAX_GRID));
     }
     if (grid > 1) {
         void *args[] = {(void *)&a};

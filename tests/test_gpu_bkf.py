@@ -65,3 +65,31 @@ def test_bkf_pivot_cases(cuda, oracle):
     assert info == 2
     with pytest.raises(ValueError):
         bkf_solve(np.zeros((3, 3)), np.zeros(4))
+
+
+@pytest.mark.parametrize("n", [300, 700])
+def test_bkf_singular_on_many_ctas(cuda, oracle, n):
+    # a zero row/column: the step that meets it is skipped (info), and every CTA must
+    # see that decision; the results are the same bits on every run
+    rng = np.random.default_rng(n)
+    B = rng.standard_normal((n, n))
+    j = n // 2
+    spd = B @ B.T / n + np.eye(n)
+    spd[:, j] = 0.0
+    spd[j, :] = 0.0
+    sym = B + B.T
+    sym[:, n // 3] = 0.0
+    sym[n // 3, :] = 0.0
+    y = torch.from_numpy(rng.standard_normal(n)).to(cuda)
+    for A, info_expected in ((spd, j + 1), (sym, None)):
+        At = torch.from_numpy(A).to(cuda)
+        runs = [(core.bkf_solve(At, y), core.bkf_invert(At)) for _ in range(3)]
+        (x0, si), (a0, vi) = runs[0]
+        assert si == vi and si > 0
+        if info_expected is not None:
+            assert si == info_expected
+            assert oracle.bkf_solve(A, y.cpu().numpy())[1] == info_expected
+        for (x, s), (ai, v) in runs[1:]:
+            assert (s, v) == (si, vi)
+            assert torch.equal(x.view(torch.int64), x0.view(torch.int64))
+            assert torch.equal(ai.contiguous().view(torch.int64), a0.contiguous().view(torch.int64))
