@@ -136,12 +136,12 @@ __device__ __forceinline__ void argmax_step(double v, int i, double &bv, int &bi
 }
 
 // Writes this CTA's (max, first index) to the partials (all threads take part).
-__device__ void publish_partial(const BkArgs &a, double bv, int bi, double *sv, int *si)
+__device__ void publish_partial(double *pv, int *pi, double bv, int bi, double *sv, int *si)
 {
     block_argmax(bv, bi, sv, si);
     if (threadIdx.x == 0) {
-        a.pv[blockIdx.x] = bv;
-        a.pi[blockIdx.x] = bi;
+        pv[blockIdx.x] = bv;
+        if (pi != nullptr) pi[blockIdx.x] = bi;
     }
 }
 
@@ -160,7 +160,7 @@ __device__ void load_columns(const BkArgs &a, int c, int gen, double *sv, int *s
         if (i > c && i < a.nsearch) argmax_step(v, (int)i, bv, bi);
         if (i > c) cB[i] = ld_l2(a.W + i * a.ld + c + 1);
     }
-    publish_partial(a, bv, bi, sv, si);
+    publish_partial(a.pv, a.pi, bv, bi, sv, si);
 }
 
 __global__ void __launch_bounds__(BK_THREADS) bk_factor_kernel(BkArgs a)
@@ -356,7 +356,7 @@ __global__ void __launch_bounds__(BK_THREADS) bk_factor_kernel(BkArgs a)
                     }
                 }
             }
-            publish_partial(a, bv, bi, sv, si);
+            publish_partial(a.pv, a.pi, bv, bi, sv, si);
         }
         if (gt == 0) {
             if (kstep == 1) {
@@ -369,6 +369,358 @@ __global__ void __launch_bounds__(BK_THREADS) bk_factor_kernel(BkArgs a)
         bk_sync(g);
         k = kn;
         gen = ngen;
+    }
+}
+
+// ---------------------------------------------------------------- blocked form --
+//
+// LAPACK's dsytrf with dlasyf (lower, qml/fcho_solve.f90:76-150 calls dsytrf):
+// panels of up to BK_NB columns are factorised with their trailing updates delayed
+// (each column of the panel is brought up to date on the fly from the panel's L
+// columns and the W = L D columns before it), then the trailing triangle takes the
+// whole panel at once, A22 -= L21 W21^T: an emulated-FP64 product on the tensor
+// cores (emu_tc_update) for the solve, FP64 for the inverse (bk_factor_blocked).  As in dlasyf a panel
+// stops one column early unless its last pivot is 2x2 (the row-max search needs a
+// spare W column), and the interchanges that a panel applied to its own earlier L
+// columns are undone afterwards, which leaves the factor in dsytf2's form.
+//
+// The panel kernel is cooperative, one thread block per SM, two grid barriers per
+// column (three when the row-max search runs).  Every CTA takes the pivot decision
+// itself from per-CTA partial maxima, so no barrier waits on one CTA's decision.
+// The W rows that an interchange swaps are written to a two-row stage and put in
+// place during the next column's update, because every CTA still reads them while
+// the interchange is applied.
+
+constexpr int BK_NB = 64;
+
+struct BkPanelArgs {
+    double *W;         // the matrix, row-major lower triangle
+    int64_t ld;
+    int N, nsearch;
+    int k0;            // the panel's first column
+    double *Wp;        // [N][BK_NB] the panel's W = L D columns, by matrix row
+    double *stage;     // [2][BK_NB] rows kk and kp of Wp after the last interchange
+    int *ipiv, *info;
+    double *pv, *pv2;  // [grid] partial column maxima and row maxima
+    int *pi;
+    int *kb_out;       // columns this panel factorised
+};
+
+// v = (the current, non-updated) A(i, col) - sum_{c < kc} L(i, k0 + c) Wp(rrow, c) for
+// rows i in [k, N), one warp per row; the result goes to Wp[i][dst].  src(i) gives
+// the element's address (row or column of A, whichever the lower triangle holds).
+template <class Src, class Keep>
+__device__ __forceinline__ void panel_column(const BkPanelArgs &a, int k, int kc, const double *rrow,
+                                             int dst, Src src, Keep keep)
+{
+    const int lane = threadIdx.x & 31;
+    const unsigned warp_g = (unsigned)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const unsigned nwarps = (unsigned)((int64_t)gridDim.x * blockDim.x >> 5);
+    const double r0 = lane < kc ? ld_l2(rrow + lane) : 0.0;
+    const double r1 = lane + 32 < kc ? ld_l2(rrow + lane + 32) : 0.0;
+    for (int i = k + (int)warp_g; i < a.N; i += (int)nwarps) {
+        const double *row = a.W + (int64_t)i * a.ld + a.k0;
+        const double l0 = lane < kc ? ld_l2(row + lane) : 0.0;
+        const double l1 = lane + 32 < kc ? ld_l2(row + lane + 32) : 0.0;
+        const double own = lane == 0 ? ld_l2(src(i)) : 0.0;
+        double dot = fma(l1, r1, l0 * r0);
+        for (int off = 16; off > 0; off >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, off);
+        if (lane == 0) {
+            const double v = own - dot;
+            a.Wp[(int64_t)i * BK_NB + dst] = v;
+            keep(v, i);
+        }
+    }
+}
+
+// Every CTA reduces the partials (value, first index) itself.
+__device__ void reduce_partials(const double *pv, const int *pi, double &v, int &idx, double *sv, int *si)
+{
+    v = 0.0;
+    idx = 0x7fffffff;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += BK_THREADS) {
+        const double x = ld_l2(pv + b);
+        const int i = pi != nullptr ? ld_l2(pi + b) : 0;
+        if (x > v || (x == v && i < idx)) {
+            v = x;
+            idx = i;
+        }
+    }
+    block_argmax(v, idx, sv, si);
+}
+
+__global__ void __launch_bounds__(BK_THREADS) bk_panel_kernel(BkPanelArgs a)
+{
+    cg::grid_group g = cg::this_grid();
+    __shared__ double sv[BK_THREADS / 32];
+    __shared__ int si[BK_THREADS / 32];
+    const double alpha = (1.0 + sqrt(17.0)) / 8.0;
+    double *W = a.W, *Wp = a.Wp;
+    const int64_t ld = a.ld;
+    const int N = a.N, ns = a.nsearch, k0 = a.k0;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int64_t gt = (int64_t)blockIdx.x * blockDim.x + tid, gsz = (int64_t)gridDim.x * blockDim.x;
+    auto wrow = [&](int i) { return Wp + (int64_t)i * BK_NB; };
+    // the interchange of the previous column whose W rows are still in the stage
+    int pend = 0, pkk = 0, pkp = 0, pcols = 0;
+    int k = k0;
+    while (k < ns && k - k0 < BK_NB - 1) {
+        const int kc = k - k0;
+        // ---- column k brought up to date: Wp[:, kc], partial max over rows (k, ns)
+        {
+            const double *rrow = (pend && k == pkp) ? a.stage + BK_NB : wrow(k);
+            double bv = 0.0;
+            int bi = 0x7fffffff;
+            panel_column(a, k, kc, rrow, kc, [&](int i) { return W + (int64_t)i * ld + k; },
+                         [&](double v, int i) {
+                             if (i > k && i < ns) argmax_step(v, i, bv, bi);
+                         });
+            if (pend && blockIdx.x == 0 && warp == 0) {
+                for (int c = lane; c < pcols; c += 32) {
+                    wrow(pkk)[c] = ld_l2(a.stage + c);
+                    wrow(pkp)[c] = ld_l2(a.stage + BK_NB + c);
+                }
+            }
+            pend = 0;
+            publish_partial(a.pv, a.pi, bv, bi, sv, si);
+        }
+        bk_sync(g);
+        // ---- the pivot decision, taken by every CTA
+        double colmax;
+        int imax;
+        reduce_partials(a.pv, a.pi, colmax, imax, sv, si);
+        const double absakk = fabs(ld_l2(wrow(k) + kc));
+        int kp = k, kstep = 1, zero = 0, copy = 0;
+        if (fmax(absakk, colmax) == 0.0) {
+            zero = 1;
+        } else if (!(absakk >= alpha * colmax)) {
+            // column imax brought up to date into Wp[:, kc+1]; row max over it
+            // without its diagonal, within the search rows
+            double rv = 0.0;
+            int rdummy = 0;
+            const int im = imax;
+            panel_column(a, k, kc, wrow(im), kc + 1,
+                         [&](int i) { return i < im ? W + (int64_t)im * ld + i : W + (int64_t)i * ld + im; },
+                         [&](double v, int i) {
+                             if (i != im && i < ns) rv = fmax(rv, fabs(v));
+                         });
+            publish_partial(a.pv2, nullptr, rv, rdummy, sv, si);
+            bk_sync(g);
+            double rowmax;
+            reduce_partials(a.pv2, nullptr, rowmax, rdummy, sv, si);
+            if (absakk >= alpha * colmax * (colmax / rowmax)) {
+                kp = k;
+            } else if (fabs(ld_l2(wrow(im) + kc + 1)) >= alpha * rowmax) {
+                kp = im;
+                copy = 1;  // W column kc takes the updated column imax
+            } else {
+                kp = im;
+                kstep = 2;
+            }
+        }
+        const int kk = k + kstep - 1;
+        const bool swap = !zero && kp != kk;
+        // W row r after the interchange (and the copy): rows kk and kp trade places
+        auto sig = [&](int r) { return !swap ? r : (r == kk ? kp : (r == kp ? kk : r)); };
+        const int src = copy ? kc + 1 : kc;
+        // ---- the interchange, the L columns and D
+        if (zero) {
+            // dsytf2 leaves the (current) column and takes no update from it
+            for (int64_t i = k + gt; i < N; i += gsz) {
+                double *w = wrow((int)i) + kc;
+                W[i * ld + k] = ld_l2(w);
+                *w = 0.0;
+            }
+        } else if (kstep == 1) {
+            const double d = ld_l2(wrow(sig(k)) + src);
+            const double r = 1.0 / d;
+            for (int64_t ii = k + gt; ii < N; ii += gsz) {
+                const int i = (int)ii;
+                if (swap && (i == kk || i == kp)) continue;
+                double *wi = wrow(i);
+                const double oldkk = (swap && i > kk) ? ld_l2(W + ii * ld + kk) : 0.0;
+                const double v = ld_l2(wi + src);
+                if (copy) wi[kc] = v;
+                if (i == k) W[ii * ld + k] = d;
+                else W[ii * ld + k] = v * r;
+                if (swap && i > kk) {
+                    if (i < kp) W[(int64_t)kp * ld + i] = oldkk;
+                    else W[ii * ld + kp] = oldkk;
+                }
+            }
+            if (swap && gt == 0) {
+                W[(int64_t)kp * ld + kp] = ld_l2(W + (int64_t)kk * ld + kk);
+                W[(int64_t)k * ld + k] = d;
+                W[(int64_t)kp * ld + k] = ld_l2(wrow(kk) + src) * r;
+            }
+        } else {
+            const double d21 = ld_l2(wrow(sig(k + 1)) + kc);
+            const double d11 = ld_l2(wrow(sig(k + 1)) + kc + 1) / d21;
+            const double d22 = ld_l2(wrow(k) + kc) / d21;
+            const double t = 1.0 / (d11 * d22 - 1.0);
+            const double e21 = t / d21;
+            for (int64_t ii = k + gt; ii < N; ii += gsz) {
+                const int i = (int)ii;
+                if (swap && (i == kk || i == kp)) continue;
+                const double *wi = wrow(i);
+                const double oldkk = (swap && i > kk) ? ld_l2(W + ii * ld + kk) : 0.0;
+                if (i == k) {
+                    W[ii * ld + k] = ld_l2(wi + kc);
+                } else if (i == k + 1) {
+                    W[ii * ld + k] = ld_l2(wi + kc);
+                    W[ii * ld + k + 1] = ld_l2(wi + kc + 1);
+                } else {
+                    const double u = ld_l2(wi + kc), w = ld_l2(wi + kc + 1);
+                    W[ii * ld + k] = e21 * (d11 * u - w);
+                    W[ii * ld + k + 1] = e21 * (d22 * w - u);
+                }
+                if (swap && i > kk) {
+                    if (i < kp) W[(int64_t)kp * ld + i] = oldkk;
+                    else W[ii * ld + kp] = oldkk;
+                }
+            }
+            if (swap && gt == 0) {
+                W[(int64_t)kp * ld + kp] = ld_l2(W + (int64_t)kk * ld + kk);
+                const double *wkk = wrow(kk), *wkp = wrow(kp);
+                W[(int64_t)(k + 1) * ld + k] = ld_l2(wkp + kc);
+                W[(int64_t)(k + 1) * ld + k + 1] = ld_l2(wkp + kc + 1);
+                const double u = ld_l2(wkk + kc), w = ld_l2(wkk + kc + 1);
+                W[(int64_t)kp * ld + k] = e21 * (d11 * u - w);
+                W[(int64_t)kp * ld + k + 1] = e21 * (d22 * w - u);
+            }
+        }
+        if (swap && blockIdx.x == 0 && warp == 0) {
+            // rows kk and kp of the panel's L columns before k trade places, and
+            // their W rows (after the copy) go to the stage
+            for (int c = k0 + lane; c < k; c += 32) {
+                double *x = W + (int64_t)kk * ld + c, *y = W + (int64_t)kp * ld + c;
+                const double tx = ld_l2(x), ty = ld_l2(y);
+                *x = ty;
+                *y = tx;
+            }
+            for (int c = lane; c <= kk - k0; c += 32) {
+                const int cs = (copy && c == kc) ? kc + 1 : c;
+                a.stage[c] = ld_l2(wrow(kp) + cs);
+                a.stage[BK_NB + c] = ld_l2(wrow(kk) + cs);
+            }
+        }
+        if (swap) {
+            pend = 1;
+            pkk = kk;
+            pkp = kp;
+            pcols = kk - k0 + 1;
+        }
+        if (gt == 0) {
+            if (kstep == 1) {
+                a.ipiv[k] = kp + 1;
+            } else {
+                a.ipiv[k] = -(kp + 1);
+                a.ipiv[k + 1] = -(kp + 1);
+            }
+            if (zero && *a.info == 0) *a.info = k + 1;
+        }
+        bk_sync(g);
+        k += kstep;
+    }
+    if (pend && blockIdx.x == 0 && warp == 0) {
+        for (int c = lane; c < pcols; c += 32) {
+            wrow(pkk)[c] = ld_l2(a.stage + c);
+            wrow(pkp)[c] = ld_l2(a.stage + BK_NB + c);
+        }
+    }
+    if (gt == 0) *a.kb_out = k - k0;
+}
+
+// W[i][j] -= sum_{c < kb} L(i, k0 + c) Wp(j, c) over the trailing lower triangle
+// i >= j >= k1, FP64, 64 x 64 tiles (the FP64 form of the panel's trailing update).
+__device__ __forceinline__ void bk_tri_index(int64_t t, int &bi, int &bj)
+{
+    int64_t r = (int64_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+    while (r * (r + 1) / 2 > t) --r;
+    while ((r + 1) * (r + 2) / 2 <= t) ++r;
+    bi = (int)r;
+    bj = (int)(t - r * (r + 1) / 2);
+}
+
+__global__ void __launch_bounds__(256)
+bk_update_fp64_kernel(double *__restrict__ W, int64_t ld, int N, int k0, int k1, int kb,
+                      const double *__restrict__ Wp)
+{
+    __shared__ double Ls[16][64 + 1];
+    __shared__ double Ws[16][64 + 1];
+    int bi, bj;
+    bk_tri_index(blockIdx.x, bi, bj);
+    const int i0 = k1 + bi * 64, j0 = k1 + bj * 64;
+    const int tid = threadIdx.x;
+    const int tx = tid & 15, ty = tid >> 4;  // tx -> j, ty -> i
+    double acc[4][4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = 0.0;
+    for (int t0 = 0; t0 < kb; t0 += 16) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int e = tid + q * 256;
+            const int r = e >> 4, c = e & 15;
+            const int ri = i0 + r, rj = j0 + r;
+            const bool in = t0 + c < kb;
+            Ls[c][r] = (ri < N && in) ? W[(int64_t)ri * ld + k0 + t0 + c] : 0.0;
+            Ws[c][r] = (rj < N && in) ? Wp[(int64_t)rj * BK_NB + t0 + c] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+            double lv[4], wv[4];
+#pragma unroll
+            for (int v = 0; v < 4; ++v) lv[v] = Ls[c][ty + 16 * v];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) wv[u] = Ws[c][tx + 16 * u];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int v = 0; v < 4; ++v) acc[u][v] = fma(lv[v], wv[u], acc[u][v]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+        const int i = i0 + ty + 16 * v;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int j = j0 + tx + 16 * u;
+            if (i < N && j <= i) W[(int64_t)i * ld + j] -= acc[u][v];
+        }
+    }
+}
+
+// Puts the panel's L columns in dsytf2's form: the interchange of each step is
+// undone on the panel's columns before that step, last step first (one thread per
+// column; a column's swaps run in order).
+__global__ void bk_panel_undo_kernel(double *__restrict__ W, int64_t ld, int k0, const int *__restrict__ kb_in,
+                                     const int *__restrict__ ipiv)
+{
+    const int kb = *kb_in;
+    const int c = k0 + (int)threadIdx.x;
+    if ((int)threadIdx.x >= kb) return;
+    int j = k0 + kb - 1;
+    while (j >= k0) {
+        int jp = ipiv[j];
+        const int jj = j;
+        if (jp < 0) {
+            jp = -jp;
+            --j;
+        }
+        --j;
+        jp -= 1;
+        // the step's first column is j + 1; its interchange swapped rows jj and jp
+        // on the columns before it
+        if (jp != jj && c <= j) {
+            double *x = W + (int64_t)jj * ld + c, *y = W + (int64_t)jp * ld + c;
+            const double t = *x;
+            *x = *y;
+            *y = t;
+        }
     }
 }
 
@@ -507,9 +859,15 @@ __global__ void bk_extract_kernel(const double *__restrict__ W, int n, double *_
 constexpr int BK_MAX_GRID = 1024;
 
 struct BkBufs {
-    int *info, *dec, *ipiv, *pi;
-    double *W, *col, *ci, *p0, *p1, *w0, *w1, *sc, *pv;
+    int *info, *dec, *ipiv, *pi, *kb, *err, *expo;
+    double *W, *col, *ci, *p0, *p1, *w0, *w1, *sc, *pv, *pv2, *Wp, *stage;
+    __nv_bfloat16 *dig;
 };
+
+constexpr int BK_SLICES = 8;
+
+// Digit-plane rows: the L21 rows at 0, the W21 rows at plane_rows(N).
+int bk_plane_rows(int N) { return 2 * qmlg::plane_rows(N); }
 
 size_t bk_ws(int n, int N)
 {
@@ -523,11 +881,70 @@ size_t bk_ws(int n, int N)
     p.add<double>(4);
     p.add<double>(BK_MAX_GRID);
     p.add<int>(BK_MAX_GRID);
+    // the blocked form
+    p.add<double>(BK_MAX_GRID);
+    p.add<double>((size_t)N * BK_NB);
+    p.add<double>(2 * BK_NB);
+    p.add<int>(4);
+    p.add<int>(4);
+    p.add<int>((size_t)bk_plane_rows(N));
+    p.add<__nv_bfloat16>((size_t)BK_SLICES * bk_plane_rows(N) * BK_NB);
     return p.total();
 }
 
+// The blocked factorisation (N > 256, cooperative launches allowed): per panel the
+// panel kernel, the trailing update, and (undo) the L columns put in dsytf2's form.
+// exact: the trailing update in FP64, else as an emulated-FP64 product.  The
+// emulated product is fixed point per row (each row scaled to its largest entry),
+// which is as accurate as FP64 where the rows are bounded, as the pivoting bounds
+// L for the solve.  The rows of the inverse's coupling block are not bounded (they
+// become rows of -A^-1): on the reference's 200 x 200 fixture (condition 4.4e9) the
+// emulated update gave max|A A^-1 - I| = 4.9e-2 against LAPACK's 1.4e-8, the FP64
+// update 2.4e-8, so the inverse takes the FP64 update.
+int bk_factor_blocked(BkBufs &b, int n, int N, int grid, bool undo, bool exact, cudaStream_t s)
+{
+    BkPanelArgs pa{b.W, (int64_t)N, N, n, 0, b.Wp, b.stage, b.ipiv, b.info, b.pv, b.pv2, b.pi, b.kb};
+    const int rpad = bk_plane_rows(N), roff = qmlg::plane_rows(N);
+    cudaError_t e = cudaMemsetAsync(b.err, 0, sizeof(int), s);
+    if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+    int st = QMLG_OK;
+    for (int k0 = 0; k0 < n;) {
+        pa.k0 = k0;
+        void *args[] = {(void *)&pa};
+        st = qmlg::launch_cooperative_serialised((const void *)bk_panel_kernel, grid, BK_THREADS, args, s);
+        if (st != QMLG_OK) return st;
+        int kb = 0;
+        if ((st = qmlg::read_back(&kb, b.kb, sizeof(int), s)) != QMLG_OK) return st;
+        if (kb < 1 || kb > BK_NB || k0 + kb > n) return QMLG_E_CUDA;
+        const int k1 = k0 + kb;
+        if (k1 < N && exact) {
+            const int64_t t = qmlg::ceil_div(N - k1, 64);
+            bk_update_fp64_kernel<<<(unsigned)(t * (t + 1) / 2), 256, 0, s>>>(b.W, N, N, k0, k1, kb, b.Wp);
+            qmlg::count_launches(1);
+            if ((st = qmlg::check_launch()) != QMLG_OK) return st;
+        } else if (k1 < N) {
+            st = qmlg::slice_rows(b.W, N, k1, N - k1, k0, kb, BK_NB, rpad, BK_SLICES, b.dig, b.expo,
+                                  nullptr, s);
+            if (st == QMLG_OK)
+                st = qmlg::slice_rows(b.Wp, BK_NB, k1, N - k1, 0, kb, BK_NB, rpad, BK_SLICES,
+                                      b.dig + (size_t)roff * BK_NB, b.expo + roff, nullptr, s);
+            if (st == QMLG_OK)
+                st = qmlg::emu_tc_update(b.W, N, k1, N, k1, N, b.dig, b.expo, BK_NB, rpad, BK_SLICES,
+                                         roff, 0, 1, b.err, s);
+            if (st != QMLG_OK) return st;
+        }
+        if (undo) {
+            bk_panel_undo_kernel<<<1, BK_NB, 0, s>>>(b.W, N, k0, b.kb, b.ipiv);
+            qmlg::count_launches(1);
+            if ((st = qmlg::check_launch()) != QMLG_OK) return st;
+        }
+        k0 = k1;
+    }
+    return qmlg::read_device_flag(b.err, s);
+}
+
 int bk_factor(const double *A, int64_t lda, int n, int N, void *workspace, size_t ws_bytes,
-              BkBufs &b, cudaStream_t s)
+              BkBufs &b, bool undo, bool exact, cudaStream_t s)
 {
     if (ws_bytes < bk_ws(n, N)) return QMLG_E_WORKSPACE;
     qmlg::Workspace ws(workspace, ws_bytes);
@@ -544,27 +961,32 @@ int bk_factor(const double *A, int64_t lda, int n, int N, void *workspace, size_
     b.sc = ws.take<double>(4);
     b.pv = ws.take<double>(BK_MAX_GRID);
     b.pi = ws.take<int>(BK_MAX_GRID);
+    b.pv2 = ws.take<double>(BK_MAX_GRID);
+    b.Wp = ws.take<double>((size_t)N * BK_NB);
+    b.stage = ws.take<double>(2 * BK_NB);
+    b.kb = ws.take<int>(4);
+    b.err = ws.take<int>(4);
+    b.expo = ws.take<int>((size_t)bk_plane_rows(N));
+    b.dig = ws.take<__nv_bfloat16>((size_t)BK_SLICES * bk_plane_rows(N) * BK_NB);
     cudaError_t e = cudaMemsetAsync(b.info, 0, sizeof(int), s);
     if (e != cudaSuccess) return qmlg::set_cuda_error(e);
     const int blocks = (int)std::min<int64_t>(qmlg::ceil_div((int64_t)N * N, 256), 152 * 64);
     { bk_build_kernel<<<blocks, 256, 0, s>>>(A, lda, n, N, b.W); qmlg::count_launches(1); }
-    BkArgs a{b.W, (int64_t)N, N, n, b.ipiv, b.info, b.col, b.ci, b.p0, b.p1, b.w0, b.w1, b.sc, b.pv, b.pi, b.dec};
     int grid = 1;
     if (N > 256 && qmlg::cooperative_allowed_on(s)) {
-        int dev = 0, sms = 0, per = 0;
+        int dev = 0, sms = 0, per = 0, per2 = 0;
         if ((e = cudaGetDevice(&dev)) != cudaSuccess ||
             (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ||
             (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, bk_factor_kernel, BK_THREADS, 0)) !=
+                cudaSuccess ||
+            (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, bk_panel_kernel, BK_THREADS, 0)) !=
                 cudaSuccess)
             return qmlg::set_cuda_error(e);
         const int lim = qmlg::sm_limit(sms);
-        grid = std::max(1, std::min(lim < sms ? lim : sms * std::max(per, 1), BK_MAX_GRID));
+        grid = std::max(1, std::min({lim, sms * std::max(std::min(per, per2), 1), BK_MAX_GRID}));
     }
-    if (grid > 1) {
-        void *args[] = {(void *)&a};
-        return qmlg::launch_cooperative_serialised((const void *)bk_factor_kernel, grid, BK_THREADS,
-                                                   args, s);
-    }
+    if (grid > 1) return bk_factor_blocked(b, n, N, grid, undo, exact, s);
+    BkArgs a{b.W, (int64_t)N, N, n, b.ipiv, b.info, b.col, b.ci, b.p0, b.p1, b.w0, b.w1, b.sc, b.pv, b.pi, b.dec};
     bk_factor_kernel<<<1, BK_THREADS, 0, s>>>(a);
     qmlg::count_launches(1);
     return qmlg::check_launch();
@@ -582,7 +1004,7 @@ extern "C" int qmlg_bkf_solve(const double *A, int n, int64_t lda, const double 
     if (A == nullptr || y == nullptr || x == nullptr) return QMLG_E_ARG;
     cudaStream_t s = qmlg::as_stream(stream);
     BkBufs b;
-    int st = bk_factor(A, lda, n, n, workspace, ws_bytes, b, s);
+    int st = bk_factor(A, lda, n, n, workspace, ws_bytes, b, true, false, s);
     if (st != QMLG_OK) return st;
     cudaError_t e = cudaMemcpyAsync(x, y, sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice, s);
     if (e != cudaSuccess) return qmlg::set_cuda_error(e);
@@ -603,7 +1025,7 @@ extern "C" int qmlg_bkf_invert(const double *A, int n, int64_t lda, double *Ainv
     if (A == nullptr || Ainv == nullptr) return QMLG_E_ARG;
     cudaStream_t s = qmlg::as_stream(stream);
     BkBufs b;
-    int st = bk_factor(A, lda, n, 2 * n, workspace, ws_bytes, b, s);
+    int st = bk_factor(A, lda, n, 2 * n, workspace, ws_bytes, b, false, true, s);
     if (st != QMLG_OK) return st;
     const int eb = (int)std::min<int64_t>(qmlg::ceil_div((int64_t)n * n, 256), 152 * 64);
     { bk_extract_kernel<<<eb, 256, 0, s>>>(b.W, n, Ainv, ldi); qmlg::count_launches(1); }

@@ -93,3 +93,23 @@ def test_bkf_singular_on_many_ctas(cuda, oracle, n):
             assert (s, v) == (si, vi)
             assert torch.equal(x.view(torch.int64), x0.view(torch.int64))
             assert torch.equal(ai.contiguous().view(torch.int64), a0.contiguous().view(torch.int64))
+
+
+def test_bkf_blocked_on_an_ill_conditioned_kernel_matrix(cuda, oracle):
+    # a Gaussian kernel matrix (condition ~1e5) above the blocked threshold, several
+    # panels: the solve (emulated trailing updates) and the inverse (FP64 ones) keep
+    # LAPACK's residuals
+    rng = np.random.default_rng(3)
+    n = 1500
+    X = rng.standard_normal((n, 20))
+    D2 = ((X[:, None, :] - X[None, :, :]) ** 2).sum(-1)
+    K = np.exp(-D2 / (2 * 4.0 ** 2)) + 1e-8 * np.eye(n)
+    y = rng.standard_normal(n)
+    x = bkf_solve(K.copy(), y.copy())
+    xo, info = oracle.bkf_solve(K, y)
+    assert info == 0
+    assert np.max(np.abs(K @ x - y)) <= 10 * np.max(np.abs(K @ xo - y))
+    Ki = bkf_invert(K.copy())
+    Ko, _ = oracle.bkf_invert(K)
+    eye = np.eye(n)
+    assert np.max(np.abs(K @ Ki - eye)) <= 10 * np.max(np.abs(K @ Ko - eye))
