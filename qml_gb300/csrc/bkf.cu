@@ -125,6 +125,42 @@ __device__ __forceinline__ int ld_l2(const int *p)
     return v;
 }
 
+// (max, first index) over a warp; every lane gets the result.
+__device__ __forceinline__ void warp_argmax(double &v, int &idx)
+{
+    for (int off = 16; off > 0; off >>= 1) {
+        const double ov = __shfl_xor_sync(0xffffffffu, v, off);
+        const int oi = __shfl_xor_sync(0xffffffffu, idx, off);
+        if (ov > v || (ov == v && oi < idx)) {
+            v = ov;
+            idx = oi;
+        }
+    }
+}
+
+// This CTA's (max, first index) to pv/pi[blockIdx.x]: warps reduce by shuffles, then
+// warp 0 over the warps' results (one block barrier; sv/si are free again after the
+// next one).
+__device__ void publish_partial_fast(double *pv, int *pi, double v, int idx, double *sv, int *si)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    warp_argmax(v, idx);
+    if (lane == 0) {
+        sv[warp] = v;
+        si[warp] = idx;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        v = lane < (int)(blockDim.x >> 5) ? sv[lane] : 0.0;
+        idx = lane < (int)(blockDim.x >> 5) ? si[lane] : 0x7fffffff;
+        warp_argmax(v, idx);
+        if (lane == 0) {
+            pv[blockIdx.x] = v;
+            if (pi != nullptr) pi[blockIdx.x] = idx;
+        }
+    }
+}
+
 // Keeps (max |v|, first index) over the values a thread sees.
 __device__ __forceinline__ void argmax_step(double v, int i, double &bv, int &bi)
 {
@@ -433,20 +469,31 @@ __device__ __forceinline__ void panel_column(const BkPanelArgs &a, int k, int kc
     }
 }
 
-// Every CTA reduces the partials (value, first index) itself.
-__device__ void reduce_partials(const double *pv, const int *pi, double &v, int &idx, double *sv, int *si)
+// Every CTA reduces the partials (value, first index) itself, in warp 0, and hands
+// the result to its threads through res (one block barrier).
+__device__ void reduce_partials(const double *pv, const int *pi, double &v, int &idx, double *res_v,
+                                int *res_i)
 {
-    v = 0.0;
-    idx = 0x7fffffff;
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += BK_THREADS) {
-        const double x = ld_l2(pv + b);
-        const int i = pi != nullptr ? ld_l2(pi + b) : 0;
-        if (x > v || (x == v && i < idx)) {
-            v = x;
-            idx = i;
+    if (threadIdx.x < 32) {
+        v = 0.0;
+        idx = 0x7fffffff;
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += 32) {
+            const double x = ld_l2(pv + b);
+            const int i = pi != nullptr ? ld_l2(pi + b) : 0;
+            if (x > v || (x == v && i < idx)) {
+                v = x;
+                idx = i;
+            }
+        }
+        warp_argmax(v, idx);
+        if (threadIdx.x == 0) {
+            *res_v = v;
+            *res_i = idx;
         }
     }
-    block_argmax(v, idx, sv, si);
+    __syncthreads();
+    v = *res_v;
+    idx = *res_i;
 }
 
 __global__ void __launch_bounds__(BK_THREADS) bk_panel_kernel(BkPanelArgs a)
@@ -454,6 +501,8 @@ __global__ void __launch_bounds__(BK_THREADS) bk_panel_kernel(BkPanelArgs a)
     cg::grid_group g = cg::this_grid();
     __shared__ double sv[BK_THREADS / 32];
     __shared__ int si[BK_THREADS / 32];
+    __shared__ double res_v[2];
+    __shared__ int res_i[2];
     const double alpha = (1.0 + sqrt(17.0)) / 8.0;
     double *W = a.W, *Wp = a.Wp;
     const int64_t ld = a.ld;
@@ -482,13 +531,13 @@ __global__ void __launch_bounds__(BK_THREADS) bk_panel_kernel(BkPanelArgs a)
                 }
             }
             pend = 0;
-            publish_partial(a.pv, a.pi, bv, bi, sv, si);
+            publish_partial_fast(a.pv, a.pi, bv, bi, sv, si);
         }
         bk_sync(g);
         // ---- the pivot decision, taken by every CTA
         double colmax;
         int imax;
-        reduce_partials(a.pv, a.pi, colmax, imax, sv, si);
+        reduce_partials(a.pv, a.pi, colmax, imax, res_v, res_i);
         const double absakk = fabs(ld_l2(wrow(k) + kc));
         int kp = k, kstep = 1, zero = 0, copy = 0;
         if (fmax(absakk, colmax) == 0.0) {
@@ -504,10 +553,10 @@ __global__ void __launch_bounds__(BK_THREADS) bk_panel_kernel(BkPanelArgs a)
                          [&](double v, int i) {
                              if (i != im && i < ns) rv = fmax(rv, fabs(v));
                          });
-            publish_partial(a.pv2, nullptr, rv, rdummy, sv, si);
+            publish_partial_fast(a.pv2, nullptr, rv, rdummy, sv, si);
             bk_sync(g);
             double rowmax;
-            reduce_partials(a.pv2, nullptr, rowmax, rdummy, sv, si);
+            reduce_partials(a.pv2, nullptr, rowmax, rdummy, res_v + 1, res_i + 1);
             if (absakk >= alpha * colmax * (colmax / rowmax)) {
                 kp = k;
             } else if (fabs(ld_l2(wrow(im) + kc + 1)) >= alpha * rowmax) {
@@ -724,105 +773,225 @@ __global__ void bk_panel_undo_kernel(double *__restrict__ W, int64_t ld, int k0,
     }
 }
 
-// dsytrs (lower, one right-hand side) with the factor above, in one CTA.
+// dsytrs (lower, one right-hand side) with the factor above, in one CTA.  SH: the
+// right-hand side is kept in shared memory for the whole solve (n <= BK_SOLVE_SMEM).
+// ipiv fixes every step in advance, so each step's L column(s) and D block are
+// loaded during the step before (the first BK_SOLVE_PF rows of each thread; the
+// rest inline), and a step waits on no global load.
+constexpr int BK_SOLVE_SMEM = 26624;
+constexpr int BK_SOLVE_PF = 4;
+
+template <bool SH>
 __global__ void __launch_bounds__(1024)
 bk_solve_kernel(const double *__restrict__ W, int64_t ld, int n, const int *__restrict__ ipiv,
-                double *__restrict__ b)
+                double *__restrict__ bg)
 {
-    __shared__ double red[32];
+    __shared__ double red0[32], red1[32], tot[2];
+    extern __shared__ double sb[];
+    double *b = SH ? sb : bg;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nt = blockDim.x;
-    auto block_sum = [&](double v) -> double {
-        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-        if (lane == 0) red[warp] = v;
+    if (SH) {
+        for (int i = tid; i < n; i += nt) sb[i] = bg[i];
         __syncthreads();
-        double s = 0.0;
-        if (tid == 0)
-            for (int w = 0; w < (nt + 31) / 32; ++w) s += red[w];
+    }
+    // sums of two values over the block; every thread gets both
+    auto block_sum2 = [&](double &v0, double &v1) {
+        for (int off = 16; off > 0; off >>= 1) {
+            v0 += __shfl_xor_sync(0xffffffffu, v0, off);
+            v1 += __shfl_xor_sync(0xffffffffu, v1, off);
+        }
+        if (lane == 0) {
+            red0[warp] = v0;
+            red1[warp] = v1;
+        }
         __syncthreads();
-        return s;  // valid in thread 0
+        if (warp == 0) {
+            double a0 = lane < (nt >> 5) ? red0[lane] : 0.0, a1 = lane < (nt >> 5) ? red1[lane] : 0.0;
+            for (int off = 16; off > 0; off >>= 1) {
+                a0 += __shfl_xor_sync(0xffffffffu, a0, off);
+                a1 += __shfl_xor_sync(0xffffffffu, a1, off);
+            }
+            if (lane == 0) {
+                tot[0] = a0;
+                tot[1] = a1;
+            }
+        }
+        __syncthreads();
+        v0 = tot[0];
+        v1 = tot[1];
     };
-    // L D x = b
+    const double *Wc = W;
+    // this thread's rows r0 + tid + j nt of columns c and (two) c + 1
+    auto fetch = [&](int c, bool two, int r0, double *x0, double *x1) {
+#pragma unroll
+        for (int j = 0; j < BK_SOLVE_PF; ++j) {
+            const int i = r0 + tid + j * nt;
+            x0[j] = i < n ? Wc[(int64_t)i * ld + c] : 0.0;
+            x1[j] = (two && i < n) ? Wc[(int64_t)i * ld + c + 1] : 0.0;
+        }
+    };
+    double c0[BK_SOLVE_PF], c1[BK_SOLVE_PF], d0 = 0.0, d1 = 0.0, d2 = 0.0;
+    // ---- L D x = b
     int k = 0;
+    if (n > 0) {
+        const bool two = ipiv[0] < 0;
+        fetch(0, two, two ? 2 : 1, c0, c1);
+        d0 = W[0];
+        if (two) {
+            d1 = W[ld];
+            d2 = W[ld + 1];
+        }
+    }
+    // thread 0's D solve of a step is stored at the start of the next one, when every
+    // thread has read the step's pivot values
+    int pk = -1;
+    bool ptwo = false;
+    double pr0 = 0.0, pr1 = 0.0;
     while (k < n) {
-        if (ipiv[k] > 0) {
-            const int kp = ipiv[k] - 1;
-            if (tid == 0 && kp != k) {
+        const int p = ipiv[k];
+        const bool two = p < 0;
+        const int kp = two ? -p - 1 : p - 1, kk = two ? k + 1 : k, r0 = kk + 1;
+        if (tid == 0) {
+            if (pk >= 0) {
+                b[pk] = pr0;
+                if (ptwo) b[pk + 1] = pr1;
+            }
+            if (kp != kk) {
+                const double t = b[kk];
+                b[kk] = b[kp];
+                b[kp] = t;
+            }
+        }
+        __syncthreads();
+        const double b0 = b[k], b1 = two ? b[k + 1] : 0.0;
+        // the next step's column(s) and D block, loaded while this step runs
+        const int kn = kk + 1;
+        double n0[BK_SOLVE_PF], n1[BK_SOLVE_PF], e0 = 0.0, e1 = 0.0, e2 = 0.0;
+        bool ntwo = false;
+        if (kn < n) {
+            ntwo = ipiv[kn] < 0;
+            fetch(kn, ntwo, kn + (ntwo ? 2 : 1), n0, n1);
+            e0 = W[(int64_t)kn * ld + kn];
+            if (ntwo) {
+                e1 = W[(int64_t)(kn + 1) * ld + kn];
+                e2 = W[(int64_t)(kn + 1) * ld + kn + 1];
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < BK_SOLVE_PF; ++j) {
+            const int i = r0 + tid + j * nt;
+            if (i < n) {
+                if (two) b[i] -= c0[j] * b0 + c1[j] * b1;
+                else b[i] -= c0[j] * b0;
+            }
+        }
+        for (int i = r0 + tid + BK_SOLVE_PF * nt; i < n; i += nt) {
+            if (two) b[i] -= W[(int64_t)i * ld + k] * b0 + W[(int64_t)i * ld + k + 1] * b1;
+            else b[i] -= W[(int64_t)i * ld + k] * b0;
+        }
+        if (tid == 0) {
+            pk = k;
+            ptwo = two;
+            if (!two) {
+                pr0 = b0 / d0;
+            } else {
+                const double akm1k = d1;
+                const double akm1 = d0 / akm1k;
+                const double ak = d2 / akm1k;
+                const double denom = akm1 * ak - 1.0;
+                const double bkm1 = b0 / akm1k, bk = b1 / akm1k;
+                pr0 = (ak * bkm1 - bk) / denom;
+                pr1 = (akm1 * bk - bkm1) / denom;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < BK_SOLVE_PF; ++j) {
+            c0[j] = n0[j];
+            c1[j] = n1[j];
+        }
+        d0 = e0;
+        d1 = e1;
+        d2 = e2;
+        k = kn;
+    }
+    if (tid == 0 && pk >= 0) {
+        b[pk] = pr0;
+        if (ptwo) b[pk + 1] = pr1;
+    }
+    __syncthreads();
+    // ---- L^T x = b, from the last step back
+    k = n - 1;
+    auto bstep = [&](int k, bool &two, int &c) {
+        two = ipiv[k] < 0;
+        c = two ? k - 1 : k;  // the step's first column
+    };
+    if (k >= 0) {
+        bool two;
+        int c;
+        bstep(k, two, c);
+        fetch(c, two, k + 1, c0, c1);
+    }
+    while (k >= 0) {
+        bool two;
+        int c;
+        bstep(k, two, c);
+        const int kp = (two ? -ipiv[k] : ipiv[k]) - 1;
+        // the next (earlier) step's columns, loaded while this step runs
+        const int kn = c - 1;
+        double n0[BK_SOLVE_PF], n1[BK_SOLVE_PF];
+        if (kn >= 0) {
+            bool ntwo;
+            int nc;
+            bstep(kn, ntwo, nc);
+            fetch(nc, ntwo, kn + 1, n0, n1);
+        }
+        // s1 over column k (the 1x1 pivot's, or the 2x2 block's second), s0 over
+        // the 2x2 block's first column
+        double s0 = 0.0, s1 = 0.0;
+#pragma unroll
+        for (int j = 0; j < BK_SOLVE_PF; ++j) {
+            const int i = k + 1 + tid + j * nt;
+            if (i < n) {
+                const double bi = b[i];
+                if (two) {
+                    s1 += c1[j] * bi;
+                    s0 += c0[j] * bi;
+                } else {
+                    s1 += c0[j] * bi;
+                }
+            }
+        }
+        for (int i = k + 1 + tid + BK_SOLVE_PF * nt; i < n; i += nt) {
+            const double bi = b[i];
+            if (two) {
+                s1 += W[(int64_t)i * ld + k] * bi;
+                s0 += W[(int64_t)i * ld + k - 1] * bi;
+            } else {
+                s1 += W[(int64_t)i * ld + k] * bi;
+            }
+        }
+        block_sum2(s0, s1);
+        if (tid == 0) {
+            b[k] -= s1;
+            if (two) b[k - 1] -= s0;
+            if (kp != k) {
                 const double t = b[k];
                 b[k] = b[kp];
                 b[kp] = t;
             }
-            __syncthreads();
-            const double bk = b[k];
-            for (int i = k + 1 + tid; i < n; i += nt) b[i] -= W[(int64_t)i * ld + k] * bk;
-            __syncthreads();
-            if (tid == 0) b[k] = bk / W[(int64_t)k * ld + k];
-            __syncthreads();
-            k += 1;
-        } else {
-            const int kp = -ipiv[k] - 1;
-            if (tid == 0 && kp != k + 1) {
-                const double t = b[k + 1];
-                b[k + 1] = b[kp];
-                b[kp] = t;
-            }
-            __syncthreads();
-            const double b0 = b[k], b1 = b[k + 1];
-            for (int i = k + 2 + tid; i < n; i += nt)
-                b[i] -= W[(int64_t)i * ld + k] * b0 + W[(int64_t)i * ld + k + 1] * b1;
-            __syncthreads();
-            if (tid == 0) {
-                const double akm1k = W[(int64_t)(k + 1) * ld + k];
-                const double akm1 = W[(int64_t)k * ld + k] / akm1k;
-                const double ak = W[(int64_t)(k + 1) * ld + k + 1] / akm1k;
-                const double denom = akm1 * ak - 1.0;
-                const double bkm1 = b0 / akm1k, bk = b1 / akm1k;
-                b[k] = (ak * bkm1 - bk) / denom;
-                b[k + 1] = (akm1 * bk - bkm1) / denom;
-            }
-            __syncthreads();
-            k += 2;
         }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < BK_SOLVE_PF; ++j) {
+            c0[j] = n0[j];
+            c1[j] = n1[j];
+        }
+        k = kn;
     }
-    // L^T x = b
-    k = n - 1;
-    while (k >= 0) {
-        if (ipiv[k] > 0) {
-            double s = 0.0;
-            for (int i = k + 1 + tid; i < n; i += nt) s += W[(int64_t)i * ld + k] * b[i];
-            s = block_sum(s);
-            if (tid == 0) {
-                b[k] -= s;
-                const int kp = ipiv[k] - 1;
-                if (kp != k) {
-                    const double t = b[k];
-                    b[k] = b[kp];
-                    b[kp] = t;
-                }
-            }
-            __syncthreads();
-            k -= 1;
-        } else {
-            // the 2x2 block (k-1, k)
-            double s0 = 0.0, s1 = 0.0;
-            for (int i = k + 1 + tid; i < n; i += nt) {
-                s1 += W[(int64_t)i * ld + k] * b[i];
-                s0 += W[(int64_t)i * ld + k - 1] * b[i];
-            }
-            s1 = block_sum(s1);
-            s0 = block_sum(s0);
-            if (tid == 0) {
-                b[k] -= s1;
-                b[k - 1] -= s0;
-                const int kp = -ipiv[k] - 1;
-                if (kp != k) {
-                    const double t = b[k];
-                    b[k] = b[kp];
-                    b[kp] = t;
-                }
-            }
-            __syncthreads();
-            k -= 2;
-        }
+    if (SH) {
+        __syncthreads();
+        for (int i = tid; i < n; i += nt) bg[i] = sb[i];
     }
 }
 
@@ -1008,7 +1177,16 @@ extern "C" int qmlg_bkf_solve(const double *A, int n, int64_t lda, const double 
     if (st != QMLG_OK) return st;
     cudaError_t e = cudaMemcpyAsync(x, y, sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice, s);
     if (e != cudaSuccess) return qmlg::set_cuda_error(e);
-    { bk_solve_kernel<<<1, 1024, 0, s>>>(b.W, n, n, b.ipiv, x); qmlg::count_launches(1); }
+    if (n <= BK_SOLVE_SMEM) {
+        const size_t smem = sizeof(double) * (size_t)n;
+        if ((e = cudaFuncSetAttribute(bk_solve_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)std::max<size_t>(smem, 1))) != cudaSuccess)
+            return qmlg::set_cuda_error(e);
+        bk_solve_kernel<true><<<1, 1024, smem, s>>>(b.W, n, n, b.ipiv, x);
+    } else {
+        bk_solve_kernel<false><<<1, 1024, 0, s>>>(b.W, n, n, b.ipiv, x);
+    }
+    qmlg::count_launches(1);
     if ((st = qmlg::check_launch()) != QMLG_OK) return st;
     int info = 0;
     st = qmlg::read_back(&info, b.info, sizeof(int), s);
