@@ -512,11 +512,13 @@ __global__ void __launch_bounds__(BK_THREADS) bk_panel_kernel(BkPanelArgs a)
     auto wrow = [&](int i) { return Wp + (int64_t)i * BK_NB; };
     // the interchange of the previous column whose W rows are still in the stage
     int pend = 0, pkk = 0, pkp = 0, pcols = 0;
+    const unsigned warp_g = (unsigned)(gt >> 5), nwarps = (unsigned)(gsz >> 5);
     int k = k0;
+    bool have_col = false;  // column k already brought up to date by the previous phase
     while (k < ns && k - k0 < BK_NB - 1) {
         const int kc = k - k0;
         // ---- column k brought up to date: Wp[:, kc], partial max over rows (k, ns)
-        {
+        if (!have_col) {
             const double *rrow = (pend && k == pkp) ? a.stage + BK_NB : wrow(k);
             double bv = 0.0;
             int bi = 0x7fffffff;
@@ -532,13 +534,15 @@ __global__ void __launch_bounds__(BK_THREADS) bk_panel_kernel(BkPanelArgs a)
             }
             pend = 0;
             publish_partial_fast(a.pv, a.pi, bv, bi, sv, si);
+            bk_sync(g);
         }
-        bk_sync(g);
+        have_col = false;
         // ---- the pivot decision, taken by every CTA
+        const double wkk = ld_l2(wrow(k) + kc);
         double colmax;
         int imax;
         reduce_partials(a.pv, a.pi, colmax, imax, res_v, res_i);
-        const double absakk = fabs(ld_l2(wrow(k) + kc));
+        const double absakk = fabs(wkk);
         int kp = k, kstep = 1, zero = 0, copy = 0;
         if (fmax(absakk, colmax) == 0.0) {
             zero = 1;
@@ -572,6 +576,98 @@ __global__ void __launch_bounds__(BK_THREADS) bk_panel_kernel(BkPanelArgs a)
         // W row r after the interchange (and the copy): rows kk and kp trade places
         auto sig = [&](int r) { return !swap ? r : (r == kk ? kp : (r == kp ? kk : r)); };
         const int src = copy ? kc + 1 : kc;
+        const int kn = k + kstep;
+        if (!zero && !swap && kn < ns && kn - k0 < BK_NB - 1) {
+            // ---- no interchange: the L column(s) and D of this step and the next
+            // column brought up to date in one phase, each row by one warp (lane 0
+            // forms the row's new L values and hands them to the lanes of the dot
+            // product); the arithmetic is that of the separate phases
+            const int kcn = kn - k0;
+            const double *rrow = wrow(kn);
+            const double r0 = lane < kcn ? ld_l2(rrow + lane) : 0.0;
+            const double r1 = lane + 32 < kcn ? ld_l2(rrow + lane + 32) : 0.0;
+            double d = 0.0, rcp = 0.0, d21 = 0.0, d11 = 0.0, d22 = 0.0, e21 = 0.0, wk1 = 0.0, wk11 = 0.0;
+            if (kstep == 1) {
+                d = wkk;
+                rcp = 1.0 / d;
+            } else {
+                wk1 = ld_l2(wrow(k + 1) + kc);
+                wk11 = ld_l2(wrow(k + 1) + kc + 1);
+                d21 = wk1;
+                d11 = wk11 / d21;
+                d22 = wkk / d21;
+                const double t = 1.0 / (d11 * d22 - 1.0);
+                e21 = t / d21;
+            }
+            double bv = 0.0;
+            int bi = 0x7fffffff;
+            for (int i = k + (int)warp_g; i < N; i += (int)nwarps) {
+                double *wrowi = W + (int64_t)i * ld;
+                const double *wi = wrow(i);
+                const double l0m = lane < kc ? ld_l2(wrowi + k0 + lane) : 0.0;
+                const double l1m = lane + 32 < kc ? ld_l2(wrowi + k0 + lane + 32) : 0.0;
+                const double own = (lane == 0 && i >= kn) ? ld_l2(wrowi + kn) : 0.0;
+                double la = 0.0, lb = 0.0;
+                if (lane == 0) {
+                    if (kstep == 1) {
+                        if (i == k) {
+                            wrowi[k] = d;
+                        } else {
+                            la = ld_l2(wi + kc) * rcp;
+                            wrowi[k] = la;
+                        }
+                    } else if (i == k) {
+                        wrowi[k] = wkk;
+                    } else if (i == k + 1) {
+                        wrowi[k] = wk1;
+                        wrowi[k + 1] = wk11;
+                    } else {
+                        const double u = ld_l2(wi + kc), w = ld_l2(wi + kc + 1);
+                        la = e21 * (d11 * u - w);
+                        lb = e21 * (d22 * w - u);
+                        wrowi[k] = la;
+                        wrowi[k + 1] = lb;
+                    }
+                }
+                if (i >= kn) {
+                    la = __shfl_sync(0xffffffffu, la, 0);
+                    lb = __shfl_sync(0xffffffffu, lb, 0);
+                    double l0 = l0m, l1 = l1m;
+                    if (kc < 32) {
+                        if (lane == kc) l0 = la;
+                    } else if (lane == kc - 32) {
+                        l1 = la;
+                    }
+                    if (kstep == 2) {
+                        if (kc + 1 < 32) {
+                            if (lane == kc + 1) l0 = lb;
+                        } else if (lane == kc + 1 - 32) {
+                            l1 = lb;
+                        }
+                    }
+                    double dot = fma(l1, r1, l0 * r0);
+                    for (int off = 16; off > 0; off >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, off);
+                    if (lane == 0) {
+                        const double v = own - dot;
+                        Wp[(int64_t)i * BK_NB + kcn] = v;
+                        if (i > kn && i < ns) argmax_step(v, i, bv, bi);
+                    }
+                }
+            }
+            publish_partial_fast(a.pv, a.pi, bv, bi, sv, si);
+            if (gt == 0) {
+                if (kstep == 1) {
+                    a.ipiv[k] = kp + 1;
+                } else {
+                    a.ipiv[k] = -(kp + 1);
+                    a.ipiv[k + 1] = -(kp + 1);
+                }
+            }
+            bk_sync(g);
+            k = kn;
+            have_col = true;
+            continue;
+        }
         // ---- the interchange, the L columns and D
         if (zero) {
             // dsytf2 leaves the (current) column and takes no update from it
