@@ -869,11 +869,33 @@ __global__ void bk_panel_undo_kernel(double *__restrict__ W, int64_t ld, int k0,
     }
 }
 
-// dsytrs (lower, one right-hand side) with the factor above, in one CTA.  SH: the
-// right-hand side is kept in shared memory for the whole solve (n <= BK_SOLVE_SMEM).
+// dsytrs (lower, one right-hand side) with the factor above, in one CTA.  L's
+// column c is read as row c of the upper triangle, where bk_transpose_kernel has put
+// L^T, so every load of a step is coalesced.  SH: the right-hand side is kept in
+// shared memory for the whole solve (n <= BK_SOLVE_SMEM).
 // ipiv fixes every step in advance, so each step's L column(s) and D block are
 // loaded during the step before (the first BK_SOLVE_PF rows of each thread; the
 // rest inline), and a step waits on no global load.
+// W[j][i] = W[i][j] for i > j: the strict lower triangle copied into the (unused)
+// upper one, 32 x 32 tiles through shared memory.
+__global__ void __launch_bounds__(256) bk_transpose_kernel(double *__restrict__ W, int64_t ld, int n)
+{
+    __shared__ double t[32][33];
+    int bi, bj;
+    bk_tri_index(blockIdx.x, bi, bj);
+    const int i0 = bi * 32, j0 = bj * 32;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int r = ty; r < 32; r += 8) {
+        const int i = i0 + r, j = j0 + tx;
+        t[r][tx] = (i < n && j < i) ? W[(int64_t)i * ld + j] : 0.0;
+    }
+    __syncthreads();
+    for (int r = ty; r < 32; r += 8) {
+        const int j = j0 + r, i = i0 + tx;  // writes row j, column i of the upper triangle
+        if (i < n && j < i) W[(int64_t)j * ld + i] = t[tx][r];
+    }
+}
+
 constexpr int BK_SOLVE_SMEM = 26624;
 constexpr int BK_SOLVE_PF = 4;
 
@@ -922,8 +944,8 @@ bk_solve_kernel(const double *__restrict__ W, int64_t ld, int n, const int *__re
 #pragma unroll
         for (int j = 0; j < BK_SOLVE_PF; ++j) {
             const int i = r0 + tid + j * nt;
-            x0[j] = i < n ? Wc[(int64_t)i * ld + c] : 0.0;
-            x1[j] = (two && i < n) ? Wc[(int64_t)i * ld + c + 1] : 0.0;
+            x0[j] = i < n ? Wc[(int64_t)c * ld + i] : 0.0;
+            x1[j] = (two && i < n) ? Wc[(int64_t)(c + 1) * ld + i] : 0.0;
         }
     };
     double c0[BK_SOLVE_PF], c1[BK_SOLVE_PF], d0 = 0.0, d1 = 0.0, d2 = 0.0;
@@ -982,8 +1004,8 @@ bk_solve_kernel(const double *__restrict__ W, int64_t ld, int n, const int *__re
             }
         }
         for (int i = r0 + tid + BK_SOLVE_PF * nt; i < n; i += nt) {
-            if (two) b[i] -= W[(int64_t)i * ld + k] * b0 + W[(int64_t)i * ld + k + 1] * b1;
-            else b[i] -= W[(int64_t)i * ld + k] * b0;
+            if (two) b[i] -= W[(int64_t)k * ld + i] * b0 + W[(int64_t)(k + 1) * ld + i] * b1;
+            else b[i] -= W[(int64_t)k * ld + i] * b0;
         }
         if (tid == 0) {
             pk = k;
@@ -1061,10 +1083,10 @@ bk_solve_kernel(const double *__restrict__ W, int64_t ld, int n, const int *__re
         for (int i = k + 1 + tid + BK_SOLVE_PF * nt; i < n; i += nt) {
             const double bi = b[i];
             if (two) {
-                s1 += W[(int64_t)i * ld + k] * bi;
-                s0 += W[(int64_t)i * ld + k - 1] * bi;
+                s1 += W[(int64_t)k * ld + i] * bi;
+                s0 += W[(int64_t)(k - 1) * ld + i] * bi;
             } else {
-                s1 += W[(int64_t)i * ld + k] * bi;
+                s1 += W[(int64_t)k * ld + i] * bi;
             }
         }
         block_sum2(s0, s1);
@@ -1089,6 +1111,171 @@ bk_solve_kernel(const double *__restrict__ W, int64_t ld, int n, const int *__re
         __syncthreads();
         for (int i = tid; i < n; i += nt) bg[i] = sb[i];
     }
+}
+
+// dsytrs as above with the L columns streamed into a shared-memory ring by cp.async,
+// DEPTH columns ahead of the step that uses them (column c's row of L^T, diagonal
+// included, in slot c mod (DEPTH + 2)), so that no step waits on a global load.
+// Needs (DEPTH + 3) n doubles of shared memory.
+__device__ __forceinline__ void cp_async8(double *smem, const double *gmem)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(gmem) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+
+// waits until at most `pending` (0 .. 7) of this thread's groups are in flight
+__device__ __forceinline__ void cp_async_wait_pending(int pending)
+{
+    switch (pending) {
+    case 0: asm volatile("cp.async.wait_group 0;" ::: "memory"); break;
+    case 1: asm volatile("cp.async.wait_group 1;" ::: "memory"); break;
+    case 2: asm volatile("cp.async.wait_group 2;" ::: "memory"); break;
+    case 3: asm volatile("cp.async.wait_group 3;" ::: "memory"); break;
+    case 4: asm volatile("cp.async.wait_group 4;" ::: "memory"); break;
+    case 5: asm volatile("cp.async.wait_group 5;" ::: "memory"); break;
+    case 6: asm volatile("cp.async.wait_group 6;" ::: "memory"); break;
+    default: asm volatile("cp.async.wait_group 7;" ::: "memory"); break;
+    }
+}
+
+// GB300 runs FP64 at about two operations per clock per SM, so in this one-CTA
+// kernel the FP64 work per step is kept to the update itself: the D solves wait
+// for one parallel pass after the forward substitution (the forward steps only
+// need the values before them), and the backward sums are reduced through shared
+// memory by one warp (32 additions a lane) instead of a shuffle tree in every warp.
+template <int DEPTH>
+__global__ void __launch_bounds__(1024)
+bk_solve_ring_kernel(const double *__restrict__ W, int64_t ld, int n, const int *__restrict__ ipiv,
+                     double *__restrict__ bg, int *__restrict__ steps)
+{
+    constexpr int NS = DEPTH + 2;
+    __shared__ double red0[1024], red1[1024];
+    extern __shared__ double sm[];
+    double *b = sm, *ring = sm + n;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nt = blockDim.x;
+    for (int i = tid; i < n; i += nt) b[i] = bg[i];
+    auto slot = [&](int c) { return ring + (int64_t)(c % NS) * n; };
+    auto issue = [&](int c) {
+        double *dst = slot(c);
+        const double *src = W + (int64_t)c * ld;
+        for (int i = c + tid; i < n; i += nt) cp_async8(dst + i, src + i);
+        cp_async_commit();
+    };
+    // ---- L x = P b (the D solves follow in one pass)
+    int issued = 0;  // columns [0, issued) are in flight or arrived
+    {
+        const int kk0 = n > 1 && ipiv[0] < 0 ? 1 : 0;
+        while (issued < n && issued <= kk0 + DEPTH) issue(issued++);
+        cp_async_wait_pending(issued - 1 - kk0);
+        __syncthreads();
+    }
+    int k = 0;
+    while (k < n) {
+        const int p = ipiv[k];
+        const bool two = p < 0;
+        const int kp = two ? -p - 1 : p - 1, kk = two ? k + 1 : k;
+        if (tid == 0) {
+            steps[k] = two ? 2 : 1;
+            if (two) steps[k + 1] = 0;
+            if (kp != kk) {
+                const double t = b[kk];
+                b[kk] = b[kp];
+                b[kp] = t;
+            }
+        }
+        __syncthreads();
+        const double *ck = slot(k), *ck1 = slot(k + 1);
+        const double b0 = b[k], b1 = two ? b[k + 1] : 0.0;
+        for (int i = kk + 1 + tid; i < n; i += nt) {
+            if (two) b[i] -= ck[i] * b0 + ck1[i] * b1;
+            else b[i] -= ck[i] * b0;
+        }
+        // the next step's columns: keep DEPTH ahead of it and wait for its own
+        const int kn = kk + 1;
+        if (kn < n) {
+            const int kkn = ipiv[kn] < 0 ? kn + 1 : kn;
+            __syncthreads();  // every thread is done with this step's slots
+            while (issued < n && issued <= kkn + DEPTH) issue(issued++);
+            cp_async_wait_pending(issued - 1 - kkn);
+        }
+        __syncthreads();
+        k = kn;
+    }
+    // ---- D x = b, every pivot block at once
+    for (int c = tid; c < n; c += nt) {
+        const int t = steps[c];
+        if (t == 1) {
+            b[c] = b[c] / W[(int64_t)c * ld + c];
+        } else if (t == 2) {
+            const double akm1k = W[(int64_t)(c + 1) * ld + c];
+            const double akm1 = W[(int64_t)c * ld + c] / akm1k;
+            const double ak = W[(int64_t)(c + 1) * ld + c + 1] / akm1k;
+            const double denom = akm1 * ak - 1.0;
+            const double bkm1 = b[c] / akm1k, bk = b[c + 1] / akm1k;
+            b[c] = (ak * bkm1 - bk) / denom;
+            b[c + 1] = (akm1 * bk - bkm1) / denom;
+        }
+    }
+    // ---- L^T x = b, from the last step back
+    cp_async_wait_pending(0);
+    __syncthreads();
+    auto first_col = [&](int k) { return ipiv[k] < 0 ? k - 1 : k; };
+    int low = n;  // columns [low, n) issued for this pass
+    if (n > 0) {
+        const int c0 = first_col(n - 1);
+        while (low > 0 && low > c0 - DEPTH) issue(--low);
+        cp_async_wait_pending(c0 - low);
+        __syncthreads();
+    }
+    k = n - 1;
+    while (k >= 0) {
+        const bool two = ipiv[k] < 0;
+        const int c = two ? k - 1 : k;
+        const int kp = (two ? -ipiv[k] : ipiv[k]) - 1;
+        const double *ck = slot(k), *cc = slot(c);
+        double s0 = 0.0, s1 = 0.0;
+        for (int i = k + 1 + tid; i < n; i += nt) {
+            const double bi = b[i];
+            s1 += ck[i] * bi;
+            if (two) s0 += cc[i] * bi;
+        }
+        red1[tid] = s1;
+        if (two) red0[tid] = s0;
+        __syncthreads();  // also: every thread is done with this step's slots
+        const int kn = c - 1;
+        if (warp == 0) {
+            double a0 = 0.0, a1 = 0.0;
+            for (int j = lane; j < nt; j += 32) {
+                a1 += red1[j];
+                if (two) a0 += red0[j];
+            }
+            for (int off = 16; off > 0; off >>= 1) {
+                a1 += __shfl_xor_sync(0xffffffffu, a1, off);
+                if (two) a0 += __shfl_xor_sync(0xffffffffu, a0, off);
+            }
+            if (lane == 0) {
+                b[k] -= a1;
+                if (two) b[k - 1] -= a0;
+                if (kp != k) {
+                    const double t = b[k];
+                    b[k] = b[kp];
+                    b[kp] = t;
+                }
+            }
+        }
+        if (kn >= 0) {
+            const int cn = first_col(kn);
+            while (low > 0 && low > cn - DEPTH) issue(--low);
+            cp_async_wait_pending(cn - low);
+        }
+        __syncthreads();
+        k = kn;
+    }
+    cp_async_wait_pending(0);
+    __syncthreads();
+    for (int i = tid; i < n; i += nt) bg[i] = b[i];
 }
 
 // W's lower triangle (ldw = N): A's column-major lower triangle, and for the inverse
@@ -1273,7 +1460,19 @@ extern "C" int qmlg_bkf_solve(const double *A, int n, int64_t lda, const double 
     if (st != QMLG_OK) return st;
     cudaError_t e = cudaMemcpyAsync(x, y, sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice, s);
     if (e != cudaSuccess) return qmlg::set_cuda_error(e);
-    if (n <= BK_SOLVE_SMEM) {
+    if (n > 1) {
+        const int64_t t = qmlg::ceil_div(n, 32);
+        bk_transpose_kernel<<<(unsigned)(t * (t + 1) / 2), 256, 0, s>>>(b.W, n, n);
+        qmlg::count_launches(1);
+    }
+    const size_t ring2 = sizeof(double) * 5 * (size_t)n;
+    // the kernel's 16 KB of static shared memory counts too
+    if (ring2 + 18 * 1024 <= (size_t)227 * 1024) {
+        if ((e = cudaFuncSetAttribute(bk_solve_ring_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)ring2)) != cudaSuccess)
+            return qmlg::set_cuda_error(e);
+        bk_solve_ring_kernel<2><<<1, 1024, ring2, s>>>(b.W, n, n, b.ipiv, x, reinterpret_cast<int *>(b.col));
+    } else if (n <= BK_SOLVE_SMEM) {
         const size_t smem = sizeof(double) * (size_t)n;
         if ((e = cudaFuncSetAttribute(bk_solve_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)std::max<size_t>(smem, 1))) != cudaSuccess)
