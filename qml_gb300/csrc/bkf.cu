@@ -125,37 +125,53 @@ __device__ __forceinline__ int ld_l2(const int *p)
     return v;
 }
 
-// (max, first index) over a warp; every lane gets the result.
-__device__ __forceinline__ void warp_argmax(double &v, int &idx)
+// The panel kernel's maxima compare |v| as integer keys (the bits of a non-negative
+// double order as its value), which keeps them off the FP64 pipe; a NaN gets key 0
+// and so never wins, as it never compares greater.
+__device__ __forceinline__ unsigned long long abs_key(double v)
+{
+    const unsigned long long u = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+    return u > 0x7ff0000000000000ull ? 0ull : u;
+}
+
+__device__ __forceinline__ void key_step(double v, int i, unsigned long long &bk, int &bi)
+{
+    const unsigned long long kv = abs_key(v);
+    if (kv > bk || (kv == bk && i < bi)) {
+        bk = kv;
+        bi = i;
+    }
+}
+
+__device__ __forceinline__ void warp_argmax_key(unsigned long long &key, int &idx)
 {
     for (int off = 16; off > 0; off >>= 1) {
-        const double ov = __shfl_xor_sync(0xffffffffu, v, off);
+        const unsigned long long ok = __shfl_xor_sync(0xffffffffu, key, off);
         const int oi = __shfl_xor_sync(0xffffffffu, idx, off);
-        if (ov > v || (ov == v && oi < idx)) {
-            v = ov;
+        if (ok > key || (ok == key && oi < idx)) {
+            key = ok;
             idx = oi;
         }
     }
 }
 
-// This CTA's (max, first index) to pv/pi[blockIdx.x]: warps reduce by shuffles, then
-// warp 0 over the warps' results (one block barrier; sv/si are free again after the
-// next one).
-__device__ void publish_partial_fast(double *pv, int *pi, double v, int idx, double *sv, int *si)
+// This CTA's (max, first index) to pv/pi[blockIdx.x] (pv as the double |v|).
+__device__ void publish_partial_key(double *pv, int *pi, unsigned long long key, int idx,
+                                    unsigned long long *sk, int *si)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    warp_argmax(v, idx);
+    warp_argmax_key(key, idx);
     if (lane == 0) {
-        sv[warp] = v;
+        sk[warp] = key;
         si[warp] = idx;
     }
     __syncthreads();
     if (warp == 0) {
-        v = lane < (int)(blockDim.x >> 5) ? sv[lane] : 0.0;
+        key = lane < (int)(blockDim.x >> 5) ? sk[lane] : 0ull;
         idx = lane < (int)(blockDim.x >> 5) ? si[lane] : 0x7fffffff;
-        warp_argmax(v, idx);
+        warp_argmax_key(key, idx);
         if (lane == 0) {
-            pv[blockIdx.x] = v;
+            pv[blockIdx.x] = __longlong_as_double((long long)key);
             if (pi != nullptr) pi[blockIdx.x] = idx;
         }
     }
@@ -475,19 +491,19 @@ __device__ void reduce_partials(const double *pv, const int *pi, double &v, int 
                                 int *res_i)
 {
     if (threadIdx.x < 32) {
-        v = 0.0;
+        unsigned long long key = 0ull;
         idx = 0x7fffffff;
         for (int b = threadIdx.x; b < (int)gridDim.x; b += 32) {
-            const double x = ld_l2(pv + b);
+            const unsigned long long x = (unsigned long long)__double_as_longlong(ld_l2(pv + b));
             const int i = pi != nullptr ? ld_l2(pi + b) : 0;
-            if (x > v || (x == v && i < idx)) {
-                v = x;
+            if (x > key || (x == key && i < idx)) {
+                key = x;
                 idx = i;
             }
         }
-        warp_argmax(v, idx);
+        warp_argmax_key(key, idx);
         if (threadIdx.x == 0) {
-            *res_v = v;
+            *res_v = __longlong_as_double((long long)key);
             *res_i = idx;
         }
     }
@@ -499,7 +515,7 @@ __device__ void reduce_partials(const double *pv, const int *pi, double &v, int 
 __global__ void __launch_bounds__(BK_THREADS) bk_panel_kernel(BkPanelArgs a)
 {
     cg::grid_group g = cg::this_grid();
-    __shared__ double sv[BK_THREADS / 32];
+    __shared__ unsigned long long sk[BK_THREADS / 32];
     __shared__ int si[BK_THREADS / 32];
     __shared__ double res_v[2];
     __shared__ int res_i[2];
@@ -520,11 +536,11 @@ __global__ void __launch_bounds__(BK_THREADS) bk_panel_kernel(BkPanelArgs a)
         // ---- column k brought up to date: Wp[:, kc], partial max over rows (k, ns)
         if (!have_col) {
             const double *rrow = (pend && k == pkp) ? a.stage + BK_NB : wrow(k);
-            double bv = 0.0;
+            unsigned long long bv = 0ull;
             int bi = 0x7fffffff;
             panel_column(a, k, kc, rrow, kc, [&](int i) { return W + (int64_t)i * ld + k; },
                          [&](double v, int i) {
-                             if (i > k && i < ns) argmax_step(v, i, bv, bi);
+                             if (i > k && i < ns) key_step(v, i, bv, bi);
                          });
             if (pend && blockIdx.x == 0 && warp == 0) {
                 for (int c = lane; c < pcols; c += 32) {
@@ -533,7 +549,7 @@ __global__ void __launch_bounds__(BK_THREADS) bk_panel_kernel(BkPanelArgs a)
                 }
             }
             pend = 0;
-            publish_partial_fast(a.pv, a.pi, bv, bi, sv, si);
+            publish_partial_key(a.pv, a.pi, bv, bi, sk, si);
             bk_sync(g);
         }
         have_col = false;
@@ -549,15 +565,18 @@ __global__ void __launch_bounds__(BK_THREADS) bk_panel_kernel(BkPanelArgs a)
         } else if (!(absakk >= alpha * colmax)) {
             // column imax brought up to date into Wp[:, kc+1]; row max over it
             // without its diagonal, within the search rows
-            double rv = 0.0;
+            unsigned long long rv = 0ull;
             int rdummy = 0;
             const int im = imax;
             panel_column(a, k, kc, wrow(im), kc + 1,
                          [&](int i) { return i < im ? W + (int64_t)im * ld + i : W + (int64_t)i * ld + im; },
                          [&](double v, int i) {
-                             if (i != im && i < ns) rv = fmax(rv, fabs(v));
+                             if (i != im && i < ns) {
+                                 const unsigned long long kv = abs_key(v);
+                                 rv = kv > rv ? kv : rv;
+                             }
                          });
-            publish_partial_fast(a.pv2, nullptr, rv, rdummy, sv, si);
+            publish_partial_key(a.pv2, nullptr, rv, rdummy, sk, si);
             bk_sync(g);
             double rowmax;
             reduce_partials(a.pv2, nullptr, rowmax, rdummy, res_v + 1, res_i + 1);
@@ -599,7 +618,7 @@ __global__ void __launch_bounds__(BK_THREADS) bk_panel_kernel(BkPanelArgs a)
                 const double t = 1.0 / (d11 * d22 - 1.0);
                 e21 = t / d21;
             }
-            double bv = 0.0;
+            unsigned long long bv = 0ull;
             int bi = 0x7fffffff;
             for (int i = k + (int)warp_g; i < N; i += (int)nwarps) {
                 double *wrowi = W + (int64_t)i * ld;
@@ -650,11 +669,11 @@ __global__ void __launch_bounds__(BK_THREADS) bk_panel_kernel(BkPanelArgs a)
                     if (lane == 0) {
                         const double v = own - dot;
                         Wp[(int64_t)i * BK_NB + kcn] = v;
-                        if (i > kn && i < ns) argmax_step(v, i, bv, bi);
+                        if (i > kn && i < ns) key_step(v, i, bv, bi);
                     }
                 }
             }
-            publish_partial_fast(a.pv, a.pi, bv, bi, sv, si);
+            publish_partial_key(a.pv, a.pi, bv, bi, sk, si);
             if (gt == 0) {
                 if (kstep == 1) {
                     a.ipiv[k] = kp + 1;
