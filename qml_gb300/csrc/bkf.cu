@@ -458,6 +458,18 @@ struct BkPanelArgs {
     int *kb_out;       // columns this panel factorised
 };
 
+// A row's dot product over the lanes of a warp: lane l holds the products of columns
+// l (l0 r0) and l + 32 (l1 r1); lanes at or above m (the number of columns) hold
+// zeros, and the levels of the reduction that would only add those zeros to lane 0
+// are skipped (the FP64 pipe is the scarce one).  The sum is valid in lane 0.
+__device__ __forceinline__ double row_dot(double l0, double r0, double l1, double r1, int m)
+{
+    double dot = m > 32 ? fma(l1, r1, l0 * r0) : l0 * r0;
+    const int top = m > 16 ? 16 : (m > 8 ? 8 : (m > 4 ? 4 : (m > 2 ? 2 : (m > 1 ? 1 : 0))));
+    for (int off = top; off > 0; off >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, off);
+    return dot;
+}
+
 // v = (the current, non-updated) A(i, col) - sum_{c < kc} L(i, k0 + c) Wp(rrow, c) for
 // rows i in [k, N), one warp per row; the result goes to Wp[i][dst].  src(i) gives
 // the element's address (row or column of A, whichever the lower triangle holds).
@@ -475,8 +487,7 @@ __device__ __forceinline__ void panel_column(const BkPanelArgs &a, int k, int kc
         const double l0 = lane < kc ? ld_l2(row + lane) : 0.0;
         const double l1 = lane + 32 < kc ? ld_l2(row + lane + 32) : 0.0;
         const double own = lane == 0 ? ld_l2(src(i)) : 0.0;
-        double dot = fma(l1, r1, l0 * r0);
-        for (int off = 16; off > 0; off >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, off);
+        const double dot = row_dot(l0, r0, l1, r1, kc);
         if (lane == 0) {
             const double v = own - dot;
             a.Wp[(int64_t)i * BK_NB + dst] = v;
@@ -664,8 +675,7 @@ __global__ void __launch_bounds__(BK_THREADS) bk_panel_kernel(BkPanelArgs a)
                             l1 = lb;
                         }
                     }
-                    double dot = fma(l1, r1, l0 * r0);
-                    for (int off = 16; off > 0; off >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, off);
+                    const double dot = row_dot(l0, r0, l1, r1, kcn);
                     if (lane == 0) {
                         const double v = own - dot;
                         Wp[(int64_t)i * BK_NB + kcn] = v;
