@@ -898,13 +898,6 @@ __global__ void bk_panel_undo_kernel(double *__restrict__ W, int64_t ld, int k0,
     }
 }
 
-// dsytrs (lower, one right-hand side) with the factor above, in one CTA.  L's
-// column c is read as row c of the upper triangle, where bk_transpose_kernel has put
-// L^T, so every load of a step is coalesced.  SH: the right-hand side is kept in
-// shared memory for the whole solve (n <= BK_SOLVE_SMEM).
-// ipiv fixes every step in advance, so each step's L column(s) and D block are
-// loaded during the step before (the first BK_SOLVE_PF rows of each thread; the
-// rest inline), and a step waits on no global load.
 // W[j][i] = W[i][j] for i > j: the strict lower triangle copied into the (unused)
 // upper one, 32 x 32 tiles through shared memory.
 __global__ void __launch_bounds__(256) bk_transpose_kernel(double *__restrict__ W, int64_t ld, int n)
@@ -925,15 +918,20 @@ __global__ void __launch_bounds__(256) bk_transpose_kernel(double *__restrict__ 
     }
 }
 
-constexpr int BK_SOLVE_SMEM = 26624;
-constexpr int BK_SOLVE_PF = 4;
+// dsytrs (lower, one right-hand side) with the factor above, in one CTA.  L's
+// column c is read as row c of the upper triangle, where bk_transpose_kernel has put
+// L^T, so every load of a step is coalesced.  SH: the right-hand side is kept in
+// shared memory for the whole solve (n <= BK_SOLVE_SMEM).  As in the ring kernel
+// below, the D solves wait for one parallel pass and the backward sums are reduced
+// through shared memory, since FP64 issue is what one SM has least of.
+constexpr int BK_SOLVE_SMEM = 26112;
 
 template <bool SH>
 __global__ void __launch_bounds__(1024)
 bk_solve_kernel(const double *__restrict__ W, int64_t ld, int n, const int *__restrict__ ipiv,
-                double *__restrict__ bg)
+                double *__restrict__ bg, int *__restrict__ steps)
 {
-    __shared__ double red0[32], red1[32], tot[2];
+    __shared__ double red0[1024], red1[1024];
     extern __shared__ double sb[];
     double *b = SH ? sb : bg;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nt = blockDim.x;
@@ -941,68 +939,15 @@ bk_solve_kernel(const double *__restrict__ W, int64_t ld, int n, const int *__re
         for (int i = tid; i < n; i += nt) sb[i] = bg[i];
         __syncthreads();
     }
-    // sums of two values over the block; every thread gets both
-    auto block_sum2 = [&](double &v0, double &v1) {
-        for (int off = 16; off > 0; off >>= 1) {
-            v0 += __shfl_xor_sync(0xffffffffu, v0, off);
-            v1 += __shfl_xor_sync(0xffffffffu, v1, off);
-        }
-        if (lane == 0) {
-            red0[warp] = v0;
-            red1[warp] = v1;
-        }
-        __syncthreads();
-        if (warp == 0) {
-            double a0 = lane < (nt >> 5) ? red0[lane] : 0.0, a1 = lane < (nt >> 5) ? red1[lane] : 0.0;
-            for (int off = 16; off > 0; off >>= 1) {
-                a0 += __shfl_xor_sync(0xffffffffu, a0, off);
-                a1 += __shfl_xor_sync(0xffffffffu, a1, off);
-            }
-            if (lane == 0) {
-                tot[0] = a0;
-                tot[1] = a1;
-            }
-        }
-        __syncthreads();
-        v0 = tot[0];
-        v1 = tot[1];
-    };
-    const double *Wc = W;
-    // this thread's rows r0 + tid + j nt of columns c and (two) c + 1
-    auto fetch = [&](int c, bool two, int r0, double *x0, double *x1) {
-#pragma unroll
-        for (int j = 0; j < BK_SOLVE_PF; ++j) {
-            const int i = r0 + tid + j * nt;
-            x0[j] = i < n ? Wc[(int64_t)c * ld + i] : 0.0;
-            x1[j] = (two && i < n) ? Wc[(int64_t)(c + 1) * ld + i] : 0.0;
-        }
-    };
-    double c0[BK_SOLVE_PF], c1[BK_SOLVE_PF], d0 = 0.0, d1 = 0.0, d2 = 0.0;
-    // ---- L D x = b
+    // ---- L x = P b (the D solves follow in one pass)
     int k = 0;
-    if (n > 0) {
-        const bool two = ipiv[0] < 0;
-        fetch(0, two, two ? 2 : 1, c0, c1);
-        d0 = W[0];
-        if (two) {
-            d1 = W[ld];
-            d2 = W[ld + 1];
-        }
-    }
-    // thread 0's D solve of a step is stored at the start of the next one, when every
-    // thread has read the step's pivot values
-    int pk = -1;
-    bool ptwo = false;
-    double pr0 = 0.0, pr1 = 0.0;
     while (k < n) {
         const int p = ipiv[k];
         const bool two = p < 0;
-        const int kp = two ? -p - 1 : p - 1, kk = two ? k + 1 : k, r0 = kk + 1;
+        const int kp = two ? -p - 1 : p - 1, kk = two ? k + 1 : k;
         if (tid == 0) {
-            if (pk >= 0) {
-                b[pk] = pr0;
-                if (ptwo) b[pk + 1] = pr1;
-            }
+            steps[k] = two ? 2 : 1;
+            if (two) steps[k + 1] = 0;
             if (kp != kk) {
                 const double t = b[kk];
                 b[kk] = b[kp];
@@ -1010,134 +955,71 @@ bk_solve_kernel(const double *__restrict__ W, int64_t ld, int n, const int *__re
             }
         }
         __syncthreads();
+        const double *ck = W + (int64_t)k * ld, *ck1 = ck + ld;
         const double b0 = b[k], b1 = two ? b[k + 1] : 0.0;
-        // the next step's column(s) and D block, loaded while this step runs
-        const int kn = kk + 1;
-        double n0[BK_SOLVE_PF], n1[BK_SOLVE_PF], e0 = 0.0, e1 = 0.0, e2 = 0.0;
-        bool ntwo = false;
-        if (kn < n) {
-            ntwo = ipiv[kn] < 0;
-            fetch(kn, ntwo, kn + (ntwo ? 2 : 1), n0, n1);
-            e0 = W[(int64_t)kn * ld + kn];
-            if (ntwo) {
-                e1 = W[(int64_t)(kn + 1) * ld + kn];
-                e2 = W[(int64_t)(kn + 1) * ld + kn + 1];
-            }
-        }
-#pragma unroll
-        for (int j = 0; j < BK_SOLVE_PF; ++j) {
-            const int i = r0 + tid + j * nt;
-            if (i < n) {
-                if (two) b[i] -= c0[j] * b0 + c1[j] * b1;
-                else b[i] -= c0[j] * b0;
-            }
-        }
-        for (int i = r0 + tid + BK_SOLVE_PF * nt; i < n; i += nt) {
-            if (two) b[i] -= W[(int64_t)k * ld + i] * b0 + W[(int64_t)(k + 1) * ld + i] * b1;
-            else b[i] -= W[(int64_t)k * ld + i] * b0;
-        }
-        if (tid == 0) {
-            pk = k;
-            ptwo = two;
-            if (!two) {
-                pr0 = b0 / d0;
-            } else {
-                const double akm1k = d1;
-                const double akm1 = d0 / akm1k;
-                const double ak = d2 / akm1k;
-                const double denom = akm1 * ak - 1.0;
-                const double bkm1 = b0 / akm1k, bk = b1 / akm1k;
-                pr0 = (ak * bkm1 - bk) / denom;
-                pr1 = (akm1 * bk - bkm1) / denom;
-            }
+        for (int i = kk + 1 + tid; i < n; i += nt) {
+            if (two) b[i] -= ck[i] * b0 + ck1[i] * b1;
+            else b[i] -= ck[i] * b0;
         }
         __syncthreads();
-#pragma unroll
-        for (int j = 0; j < BK_SOLVE_PF; ++j) {
-            c0[j] = n0[j];
-            c1[j] = n1[j];
-        }
-        d0 = e0;
-        d1 = e1;
-        d2 = e2;
-        k = kn;
+        k = kk + 1;
     }
-    if (tid == 0 && pk >= 0) {
-        b[pk] = pr0;
-        if (ptwo) b[pk + 1] = pr1;
+    // ---- D x = b, every pivot block at once
+    for (int c = tid; c < n; c += nt) {
+        const int t = steps[c];
+        if (t == 1) {
+            b[c] = b[c] / W[(int64_t)c * ld + c];
+        } else if (t == 2) {
+            const double akm1k = W[(int64_t)(c + 1) * ld + c];
+            const double akm1 = W[(int64_t)c * ld + c] / akm1k;
+            const double ak = W[(int64_t)(c + 1) * ld + c + 1] / akm1k;
+            const double denom = akm1 * ak - 1.0;
+            const double bkm1 = b[c] / akm1k, bk = b[c + 1] / akm1k;
+            b[c] = (ak * bkm1 - bk) / denom;
+            b[c + 1] = (akm1 * bk - bkm1) / denom;
+        }
     }
     __syncthreads();
     // ---- L^T x = b, from the last step back
     k = n - 1;
-    auto bstep = [&](int k, bool &two, int &c) {
-        two = ipiv[k] < 0;
-        c = two ? k - 1 : k;  // the step's first column
-    };
-    if (k >= 0) {
-        bool two;
-        int c;
-        bstep(k, two, c);
-        fetch(c, two, k + 1, c0, c1);
-    }
     while (k >= 0) {
-        bool two;
-        int c;
-        bstep(k, two, c);
+        const bool two = ipiv[k] < 0;
+        const int c = two ? k - 1 : k;
         const int kp = (two ? -ipiv[k] : ipiv[k]) - 1;
-        // the next (earlier) step's columns, loaded while this step runs
-        const int kn = c - 1;
-        double n0[BK_SOLVE_PF], n1[BK_SOLVE_PF];
-        if (kn >= 0) {
-            bool ntwo;
-            int nc;
-            bstep(kn, ntwo, nc);
-            fetch(nc, ntwo, kn + 1, n0, n1);
-        }
-        // s1 over column k (the 1x1 pivot's, or the 2x2 block's second), s0 over
-        // the 2x2 block's first column
+        const double *ck = W + (int64_t)k * ld, *cc = W + (int64_t)c * ld;
         double s0 = 0.0, s1 = 0.0;
-#pragma unroll
-        for (int j = 0; j < BK_SOLVE_PF; ++j) {
-            const int i = k + 1 + tid + j * nt;
-            if (i < n) {
-                const double bi = b[i];
-                if (two) {
-                    s1 += c1[j] * bi;
-                    s0 += c0[j] * bi;
-                } else {
-                    s1 += c0[j] * bi;
+        for (int i = k + 1 + tid; i < n; i += nt) {
+            const double bi = b[i];
+            s1 += ck[i] * bi;
+            if (two) s0 += cc[i] * bi;
+        }
+        red1[tid] = s1;
+        if (two) red0[tid] = s0;
+        __syncthreads();
+        if (warp == 0) {
+            double a0 = 0.0, a1 = 0.0;
+            for (int j = lane; j < nt; j += 32) {
+                a1 += red1[j];
+                if (two) a0 += red0[j];
+            }
+            for (int off = 16; off > 0; off >>= 1) {
+                a1 += __shfl_xor_sync(0xffffffffu, a1, off);
+                if (two) a0 += __shfl_xor_sync(0xffffffffu, a0, off);
+            }
+            if (lane == 0) {
+                b[k] -= a1;
+                if (two) b[k - 1] -= a0;
+                if (kp != k) {
+                    const double t = b[k];
+                    b[k] = b[kp];
+                    b[kp] = t;
                 }
             }
         }
-        for (int i = k + 1 + tid + BK_SOLVE_PF * nt; i < n; i += nt) {
-            const double bi = b[i];
-            if (two) {
-                s1 += W[(int64_t)k * ld + i] * bi;
-                s0 += W[(int64_t)(k - 1) * ld + i] * bi;
-            } else {
-                s1 += W[(int64_t)k * ld + i] * bi;
-            }
-        }
-        block_sum2(s0, s1);
-        if (tid == 0) {
-            b[k] -= s1;
-            if (two) b[k - 1] -= s0;
-            if (kp != k) {
-                const double t = b[k];
-                b[k] = b[kp];
-                b[kp] = t;
-            }
-        }
         __syncthreads();
-#pragma unroll
-        for (int j = 0; j < BK_SOLVE_PF; ++j) {
-            c0[j] = n0[j];
-            c1[j] = n1[j];
-        }
-        k = kn;
+        k = c - 1;
     }
     if (SH) {
-        __syncthreads();
         for (int i = tid; i < n; i += nt) bg[i] = sb[i];
     }
 }
@@ -1506,9 +1388,9 @@ extern "C" int qmlg_bkf_solve(const double *A, int n, int64_t lda, const double 
         if ((e = cudaFuncSetAttribute(bk_solve_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)std::max<size_t>(smem, 1))) != cudaSuccess)
             return qmlg::set_cuda_error(e);
-        bk_solve_kernel<true><<<1, 1024, smem, s>>>(b.W, n, n, b.ipiv, x);
+        bk_solve_kernel<true><<<1, 1024, smem, s>>>(b.W, n, n, b.ipiv, x, reinterpret_cast<int *>(b.col));
     } else {
-        bk_solve_kernel<false><<<1, 1024, 0, s>>>(b.W, n, n, b.ipiv, x);
+        bk_solve_kernel<false><<<1, 1024, 0, s>>>(b.W, n, n, b.ipiv, x, reinterpret_cast<int *>(b.col));
     }
     qmlg::count_launches(1);
     if ((st = qmlg::check_launch()) != QMLG_OK) return st;

@@ -113,3 +113,17 @@ def test_bkf_blocked_on_an_ill_conditioned_kernel_matrix(cuda, oracle):
     Ko, _ = oracle.bkf_invert(K)
     eye = np.eye(n)
     assert np.max(np.abs(K @ Ki - eye)) <= 10 * np.max(np.abs(K @ Ko - eye))
+
+
+def test_bkf_solve_above_the_shared_memory_ring(cuda, oracle):
+    # n = 6000: the solve's L columns no longer fit the shared-memory ring, so dsytrs
+    # reads them straight from the transposed copy; held to LAPACK's residual
+    rng = np.random.default_rng(6000)
+    n = 6000
+    B = rng.standard_normal((n, n))
+    A = B + B.T
+    y = rng.standard_normal(n)
+    x = bkf_solve(A.copy(), y.copy())
+    xo, info = oracle.bkf_solve(A, y)
+    assert info == 0
+    assert np.max(np.abs(A @ x - y)) <= 10 * np.max(np.abs(A @ xo - y))
