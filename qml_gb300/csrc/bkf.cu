@@ -456,6 +456,10 @@ struct BkPanelArgs {
     double *pv, *pv2;  // [grid] partial column maxima and row maxima
     int *pi;
     int *kb_out;       // columns this panel factorised
+    // the inverse's coupling rows (N > nsearch), else null: perm[p] is the original
+    // index at position p; tile_act[t] marks the 64-row tiles (of all N rows) that hold
+    // a coupling row whose pivot has been taken (the A rows' tiles are marked at start)
+    int *perm, *tile_act;
 };
 
 // A row's dot product over the lanes of a warp: lane l holds the products of columns
@@ -494,6 +498,21 @@ __device__ __forceinline__ void panel_column(const BkPanelArgs &a, int k, int kc
             keep(v, i);
         }
     }
+}
+
+// The inverse's coupling row n + j is zero in every column until the column that
+// holds its 1 (original index j, at position perm^-1(j)) becomes a pivot: the step's
+// interchange (kk <-> kp, kk < 0 for none) moves the original indices, and the rows of
+// the pivots it takes become live.  One thread.
+__device__ __forceinline__ void mark_coupling(const BkPanelArgs &a, int k, int kstep, int kk, int kp)
+{
+    if (a.perm == nullptr) return;
+    if (kk >= 0) {
+        const int t = a.perm[kk];
+        a.perm[kk] = a.perm[kp];
+        a.perm[kp] = t;
+    }
+    for (int p = k; p < k + kstep; ++p) a.tile_act[(a.nsearch + a.perm[p]) >> 6] = 1;
 }
 
 // Every CTA reduces the partials (value, first index) itself, in warp 0, and hands
@@ -691,6 +710,7 @@ __global__ void __launch_bounds__(BK_THREADS) bk_panel_kernel(BkPanelArgs a)
                     a.ipiv[k] = -(kp + 1);
                     a.ipiv[k + 1] = -(kp + 1);
                 }
+                mark_coupling(a, k, kstep, -1, kp);
             }
             bk_sync(g);
             k = kn;
@@ -792,6 +812,7 @@ __global__ void __launch_bounds__(BK_THREADS) bk_panel_kernel(BkPanelArgs a)
                 a.ipiv[k + 1] = -(kp + 1);
             }
             if (zero && *a.info == 0) *a.info = k + 1;
+            mark_coupling(a, k, kstep, swap ? kk : -1, kp);
         }
         bk_sync(g);
         k += kstep;
@@ -818,13 +839,19 @@ __device__ __forceinline__ void bk_tri_index(int64_t t, int &bi, int &bj)
 
 __global__ void __launch_bounds__(256)
 bk_update_fp64_kernel(double *__restrict__ W, int64_t ld, int N, int k0, int k1, int kb,
-                      const double *__restrict__ Wp)
+                      const double *__restrict__ Wp, const int *__restrict__ tile_act)
 {
     __shared__ double Ls[16][64 + 1];
     __shared__ double Ws[16][64 + 1];
     int bi, bj;
     bk_tri_index(blockIdx.x, bi, bj);
     const int i0 = k1 + bi * 64, j0 = k1 + bj * 64;
+    if (tile_act != nullptr) {
+        // rows (or columns) that are all coupling rows not yet live contribute zeros
+        const int T = (N + 63) >> 6;
+        auto live = [&](int r0) { return tile_act[r0 >> 6] != 0 || ((r0 + 63) >> 6 < T && tile_act[(r0 + 63) >> 6] != 0); };
+        if (!live(i0) || !live(j0)) return;
+    }
     const int tid = threadIdx.x;
     const int tx = tid & 15, ty = tid >> 4;  // tx -> j, ty -> i
     double acc[4][4];
@@ -866,6 +893,14 @@ bk_update_fp64_kernel(double *__restrict__ W, int64_t ld, int N, int k0, int k1,
             if (i < N && j <= i) W[(int64_t)i * ld + j] -= acc[u][v];
         }
     }
+}
+
+// perm = identity; the tiles holding A rows live, the coupling rows' tiles not yet.
+__global__ void bk_coupling_init_kernel(int *__restrict__ perm, int n, int *__restrict__ tile_act, int T)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) perm[i] = i;
+    if (i < T) tile_act[i] = (i << 6) < n ? 1 : 0;
 }
 
 // Puts the panel's L columns in dsytf2's form: the interchange of each step is
@@ -1222,7 +1257,7 @@ __global__ void bk_extract_kernel(const double *__restrict__ W, int n, double *_
 constexpr int BK_MAX_GRID = 1024;
 
 struct BkBufs {
-    int *info, *dec, *ipiv, *pi, *kb, *err, *expo;
+    int *info, *dec, *ipiv, *pi, *kb, *err, *expo, *perm, *tact;
     double *W, *col, *ci, *p0, *p1, *w0, *w1, *sc, *pv, *pv2, *Wp, *stage;
     __nv_bfloat16 *dig;
 };
@@ -1252,6 +1287,8 @@ size_t bk_ws(int n, int N)
     p.add<int>(4);
     p.add<int>((size_t)bk_plane_rows(N));
     p.add<__nv_bfloat16>((size_t)BK_SLICES * bk_plane_rows(N) * BK_NB);
+    p.add<int>((size_t)std::max(n, 1));
+    p.add<int>((size_t)(N + 63) / 64);
     return p.total();
 }
 
@@ -1266,10 +1303,18 @@ size_t bk_ws(int n, int N)
 // update 2.4e-8, so the inverse takes the FP64 update.
 int bk_factor_blocked(BkBufs &b, int n, int N, int grid, bool undo, bool exact, cudaStream_t s)
 {
-    BkPanelArgs pa{b.W, (int64_t)N, N, n, 0, b.Wp, b.stage, b.ipiv, b.info, b.pv, b.pv2, b.pi, b.kb};
+    BkPanelArgs pa{b.W, (int64_t)N, N, n, 0, b.Wp, b.stage, b.ipiv, b.info, b.pv, b.pv2, b.pi, b.kb,
+                   nullptr, nullptr};
     const int rpad = bk_plane_rows(N), roff = qmlg::plane_rows(N);
     cudaError_t e = cudaMemsetAsync(b.err, 0, sizeof(int), s);
     if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+    if (N > n) {
+        pa.perm = b.perm;
+        pa.tile_act = b.tact;
+        const int T = (N + 63) / 64;
+        bk_coupling_init_kernel<<<(unsigned)qmlg::ceil_div(std::max(n, T), 256), 256, 0, s>>>(b.perm, n, b.tact, T);
+        qmlg::count_launches(1);
+    }
     int st = QMLG_OK;
     for (int k0 = 0; k0 < n;) {
         pa.k0 = k0;
@@ -1282,7 +1327,8 @@ int bk_factor_blocked(BkBufs &b, int n, int N, int grid, bool undo, bool exact, 
         const int k1 = k0 + kb;
         if (k1 < N && exact) {
             const int64_t t = qmlg::ceil_div(N - k1, 64);
-            bk_update_fp64_kernel<<<(unsigned)(t * (t + 1) / 2), 256, 0, s>>>(b.W, N, N, k0, k1, kb, b.Wp);
+            bk_update_fp64_kernel<<<(unsigned)(t * (t + 1) / 2), 256, 0, s>>>(b.W, N, N, k0, k1, kb, b.Wp,
+                                                                               pa.tile_act);
             qmlg::count_launches(1);
             if ((st = qmlg::check_launch()) != QMLG_OK) return st;
         } else if (k1 < N) {
@@ -1331,6 +1377,8 @@ int bk_factor(const double *A, int64_t lda, int n, int N, void *workspace, size_
     b.err = ws.take<int>(4);
     b.expo = ws.take<int>((size_t)bk_plane_rows(N));
     b.dig = ws.take<__nv_bfloat16>((size_t)BK_SLICES * bk_plane_rows(N) * BK_NB);
+    b.perm = ws.take<int>((size_t)std::max(n, 1));
+    b.tact = ws.take<int>((size_t)(N + 63) / 64);
     cudaError_t e = cudaMemsetAsync(b.info, 0, sizeof(int), s);
     if (e != cudaSuccess) return qmlg::set_cuda_error(e);
     const int blocks = (int)std::min<int64_t>(qmlg::ceil_div((int64_t)N * N, 256), 152 * 64);

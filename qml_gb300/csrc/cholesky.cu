@@ -1436,19 +1436,23 @@ __global__ void fill_nan_kernel(double *__restrict__ x, int n)
 namespace qmlg {
 
 int cholesky_fp64(double *A, int n, int64_t lda, double shift, int *d_info, cudaStream_t s,
-                  int npiv)
+                  int npiv, bool coupled)
 {
     // npiv < n (a multiple of 64): only the first npiv pivots; the trailing
     // (n - npiv) block is left holding its Schur complement
     const int np = (npiv < 0 || npiv > n) ? n : npiv;
     for (int k0 = 0; k0 < np; k0 += NB) {
-        { potrf_diag_kernel<<<1, 256, 0, s>>>(A, lda, n, k0, shift, d_info); qmlg::count_launches(1); }
-        const int below = n - (k0 + NB);
+        // coupled: the rows from np + k0 + NB on are zero in this panel (their pivot
+        // has not come), so the panel solve and the trailing update stop there; the
+        // kernels take the row bound as their n
+        const int ne = coupled ? std::min(n, np + k0 + NB) : n;
+        { potrf_diag_kernel<<<1, 256, 0, s>>>(A, lda, ne, k0, shift, d_info); qmlg::count_launches(1); }
+        const int below = ne - (k0 + NB);
         if (below > 0) {
-            const int st = launch_trsm(A, lda, n, k0, d_info, 0, 0, 0, nullptr, nullptr, s);
+            const int st = launch_trsm(A, lda, ne, k0, d_info, 0, 0, 0, nullptr, nullptr, s);
             if (st != QMLG_OK) return st;
             const int64_t t = ceil_div(below, 64);
-            { syrk_update_kernel<<<(unsigned)(t * (t + 1) / 2), 256, 0, s>>>(A, lda, n, k0, d_info); qmlg::count_launches(1); }
+            { syrk_update_kernel<<<(unsigned)(t * (t + 1) / 2), 256, 0, s>>>(A, lda, ne, k0, d_info); qmlg::count_launches(1); }
         }
     }
     return check_launch();
@@ -2170,7 +2174,7 @@ extern "C" int qmlg_cho_invert(const double *A, int n, int64_t lda, double *Ainv
         st = qmlg::emulated_factor(M, N, N, 0.0, ws, d_info, f, s, 8, np);
         if (st == QMLG_OK) st = qmlg::read_device_flag(f.d_err, s);
     } else {
-        st = qmlg::cholesky_fp64(M, N, N, 0.0, d_info, s, np);
+        st = qmlg::cholesky_fp64(M, N, N, 0.0, d_info, s, np, true);
     }
     if (st != QMLG_OK) return st;
     const int eb = (int)std::min<int64_t>(qmlg::ceil_div((int64_t)n * n, 256), 152 * 64);

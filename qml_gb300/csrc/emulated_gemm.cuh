@@ -124,8 +124,11 @@ bool cooperative_allowed_on(cudaStream_t s);
 int read_device_flag(const int *d_flag, cudaStream_t s);
 
 // Shared with the FP64 path (cholesky.cu).
+// coupled: A is [[A_p, E], [E^T, 0]] with E = [I; 0] and npiv = A_p's size, so coupling
+// row npiv + j is zero before pivot j and each panel only touches rows below
+// npiv + (its last pivot + 1).
 int cholesky_fp64(double *A, int n, int64_t lda, double shift, int *d_info, cudaStream_t s,
-                  int npiv = -1);
+                  int npiv = -1, bool coupled = false);
 int potrs_fp64(const double *A, int n, int64_t lda, double *x, cudaStream_t s);
 int mirror_upper_to_lower(double *A, int n, int64_t lda, const double *diag, cudaStream_t s);
 
