@@ -523,12 +523,25 @@ __device__ void reduce_partials(const double *pv, const int *pi, double &v, int 
     if (threadIdx.x < 32) {
         unsigned long long key = 0ull;
         idx = 0x7fffffff;
-        for (int b = threadIdx.x; b < (int)gridDim.x; b += 32) {
-            const unsigned long long x = (unsigned long long)__double_as_longlong(ld_l2(pv + b));
-            const int i = pi != nullptr ? ld_l2(pi + b) : 0;
-            if (x > key || (x == key && i < idx)) {
-                key = x;
-                idx = i;
+        // the loads of a lane all issued before the first compare (a loop of load and
+        // compare would wait out one L2 round trip per partial)
+        constexpr int U = 8;
+        for (int b0 = threadIdx.x; b0 < (int)gridDim.x; b0 += 32 * U) {
+            double xv[U];
+            int iv[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int b = b0 + 32 * u;
+                xv[u] = b < (int)gridDim.x ? ld_l2(pv + b) : 0.0;
+                iv[u] = (b < (int)gridDim.x && pi != nullptr) ? ld_l2(pi + b) : 0x7fffffff;
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const unsigned long long x = (unsigned long long)__double_as_longlong(xv[u]);
+                if (x > key || (x == key && iv[u] < idx)) {
+                    key = x;
+                    idx = iv[u];
+                }
             }
         }
         warp_argmax_key(key, idx);
@@ -590,6 +603,9 @@ __global__ void __launch_bounds__(BK_THREADS) bk_panel_kernel(BkPanelArgs a)
         reduce_partials(a.pv, a.pi, colmax, imax, res_v, res_i);
         const double absakk = fabs(wkk);
         int kp = k, kstep = 1, zero = 0, copy = 0;
+        // row imax's updated entries in columns kc and kc+1 (the row-max search):
+        // with wkk they are the whole pivot block, after any interchange
+        double wimk = 0.0, wimim = 0.0;
         if (fmax(absakk, colmax) == 0.0) {
             zero = 1;
         } else if (!(absakk >= alpha * colmax)) {
@@ -608,11 +624,13 @@ __global__ void __launch_bounds__(BK_THREADS) bk_panel_kernel(BkPanelArgs a)
                          });
             publish_partial_key(a.pv2, nullptr, rv, rdummy, sk, si);
             bk_sync(g);
+            wimim = ld_l2(wrow(im) + kc + 1);  // issued before the reduction's loads
+            wimk = ld_l2(wrow(im) + kc);
             double rowmax;
             reduce_partials(a.pv2, nullptr, rowmax, rdummy, res_v + 1, res_i + 1);
             if (absakk >= alpha * colmax * (colmax / rowmax)) {
                 kp = k;
-            } else if (fabs(ld_l2(wrow(im) + kc + 1)) >= alpha * rowmax) {
+            } else if (fabs(wimim) >= alpha * rowmax) {
                 kp = im;
                 copy = 1;  // W column kc takes the updated column imax
             } else {
@@ -622,8 +640,6 @@ __global__ void __launch_bounds__(BK_THREADS) bk_panel_kernel(BkPanelArgs a)
         }
         const int kk = k + kstep - 1;
         const bool swap = !zero && kp != kk;
-        // W row r after the interchange (and the copy): rows kk and kp trade places
-        auto sig = [&](int r) { return !swap ? r : (r == kk ? kp : (r == kp ? kk : r)); };
         const int src = copy ? kc + 1 : kc;
         const int kn = k + kstep;
         if (!zero && !swap && kn < ns && kn - k0 < BK_NB - 1) {
@@ -640,8 +656,8 @@ __global__ void __launch_bounds__(BK_THREADS) bk_panel_kernel(BkPanelArgs a)
                 d = wkk;
                 rcp = 1.0 / d;
             } else {
-                wk1 = ld_l2(wrow(k + 1) + kc);
-                wk11 = ld_l2(wrow(k + 1) + kc + 1);
+                wk1 = wimk;  // no interchange: imax == k + 1
+                wk11 = wimim;
                 d21 = wk1;
                 d11 = wk11 / d21;
                 d22 = wkk / d21;
@@ -726,7 +742,7 @@ __global__ void __launch_bounds__(BK_THREADS) bk_panel_kernel(BkPanelArgs a)
                 *w = 0.0;
             }
         } else if (kstep == 1) {
-            const double d = ld_l2(wrow(sig(k)) + src);
+            const double d = kp == k ? wkk : wimim;  // W(sig k, src): row k, or imax's copied column
             const double r = 1.0 / d;
             for (int64_t ii = k + gt; ii < N; ii += gsz) {
                 const int i = (int)ii;
@@ -743,14 +759,15 @@ __global__ void __launch_bounds__(BK_THREADS) bk_panel_kernel(BkPanelArgs a)
                 }
             }
             if (swap && gt == 0) {
-                W[(int64_t)kp * ld + kp] = ld_l2(W + (int64_t)kk * ld + kk);
+                const double dkk = ld_l2(W + (int64_t)kk * ld + kk), vkp = ld_l2(wrow(kk) + src);
+                W[(int64_t)kp * ld + kp] = dkk;
                 W[(int64_t)k * ld + k] = d;
-                W[(int64_t)kp * ld + k] = ld_l2(wrow(kk) + src) * r;
+                W[(int64_t)kp * ld + k] = vkp * r;
             }
         } else {
-            const double d21 = ld_l2(wrow(sig(k + 1)) + kc);
-            const double d11 = ld_l2(wrow(sig(k + 1)) + kc + 1) / d21;
-            const double d22 = ld_l2(wrow(k) + kc) / d21;
+            const double d21 = wimk;  // sig(k + 1) == imax
+            const double d11 = wimim / d21;
+            const double d22 = wkk / d21;
             const double t = 1.0 / (d11 * d22 - 1.0);
             const double e21 = t / d21;
             for (int64_t ii = k + gt; ii < N; ii += gsz) {
@@ -774,28 +791,44 @@ __global__ void __launch_bounds__(BK_THREADS) bk_panel_kernel(BkPanelArgs a)
                 }
             }
             if (swap && gt == 0) {
-                W[(int64_t)kp * ld + kp] = ld_l2(W + (int64_t)kk * ld + kk);
                 const double *wkk = wrow(kk), *wkp = wrow(kp);
-                W[(int64_t)(k + 1) * ld + k] = ld_l2(wkp + kc);
-                W[(int64_t)(k + 1) * ld + k + 1] = ld_l2(wkp + kc + 1);
+                const double dkk = ld_l2(W + (int64_t)kk * ld + kk);
+                const double p0 = ld_l2(wkp + kc), p1 = ld_l2(wkp + kc + 1);
                 const double u = ld_l2(wkk + kc), w = ld_l2(wkk + kc + 1);
+                W[(int64_t)kp * ld + kp] = dkk;
+                W[(int64_t)(k + 1) * ld + k] = p0;
+                W[(int64_t)(k + 1) * ld + k + 1] = p1;
                 W[(int64_t)kp * ld + k] = e21 * (d11 * u - w);
                 W[(int64_t)kp * ld + k + 1] = e21 * (d22 * w - u);
             }
         }
         if (swap && blockIdx.x == 0 && warp == 0) {
             // rows kk and kp of the panel's L columns before k trade places, and
-            // their W rows (after the copy) go to the stage
-            for (int c = k0 + lane; c < k; c += 32) {
-                double *x = W + (int64_t)kk * ld + c, *y = W + (int64_t)kp * ld + c;
-                const double tx = ld_l2(x), ty = ld_l2(y);
-                *x = ty;
-                *y = tx;
+            // their W rows (after the copy) go to the stage; every load is issued
+            // before the first store (columns < BK_NB: two per lane)
+            double lx[2], ly[2], sa[2], sb[2];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int c = k0 + lane + 32 * h;
+                lx[h] = c < k ? ld_l2(W + (int64_t)kk * ld + c) : 0.0;
+                ly[h] = c < k ? ld_l2(W + (int64_t)kp * ld + c) : 0.0;
+                const int cw = lane + 32 * h;
+                const int cs = (copy && cw == kc) ? kc + 1 : cw;
+                sa[h] = cw <= kk - k0 ? ld_l2(wrow(kp) + cs) : 0.0;
+                sb[h] = cw <= kk - k0 ? ld_l2(wrow(kk) + cs) : 0.0;
             }
-            for (int c = lane; c <= kk - k0; c += 32) {
-                const int cs = (copy && c == kc) ? kc + 1 : c;
-                a.stage[c] = ld_l2(wrow(kp) + cs);
-                a.stage[BK_NB + c] = ld_l2(wrow(kk) + cs);
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int c = k0 + lane + 32 * h;
+                if (c < k) {
+                    W[(int64_t)kk * ld + c] = ly[h];
+                    W[(int64_t)kp * ld + c] = lx[h];
+                }
+                const int cw = lane + 32 * h;
+                if (cw <= kk - k0) {
+                    a.stage[cw] = sa[h];
+                    a.stage[BK_NB + cw] = sb[h];
+                }
             }
         }
         if (swap) {
