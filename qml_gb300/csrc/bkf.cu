@@ -13,8 +13,9 @@
 // Storage: the row-major lower triangle W[i][j], i >= j (the column-major lower
 // triangle dsytrf("L") works on, seen transposed).
 //
-// One cooperative kernel runs the whole factorisation, two grid barriers per pivot
-// step:
+// Two forms.  Above N = 256 (outside stream capture) the blocked form below (LAPACK's
+// dlasyf, "blocked form").  Otherwise one CTA runs the unblocked dsytf2 kernel
+// bk_factor_kernel, written for a cooperative grid, two barriers per pivot step:
 //   1. CTA 0 decides the pivot.  Column k comes from a contiguous copy and its
 //      maximum from per-CTA partials, both left by the previous step's update; only
 //      the row-max search reads the matrix (row imax, and column imax, which it
@@ -26,7 +27,7 @@
 //      warps, four independent elements per lane.  The segments at the diagonal's
 //      left end also copy out columns k+kstep and k+kstep+1 and the partial maxima
 //      for the next step.
-// The arithmetic is dsytf2's, operation for operation.
+// Its arithmetic is dsytf2's, operation for operation.
 // Everything another CTA wrote since the last barrier is read through L2
 // (ld.global.cg, never a possibly stale L1 line) by loads that the compiler may not
 // move across the barrier; the step's decision is read once per CTA, by the thread
@@ -431,13 +432,15 @@ __global__ void __launch_bounds__(BK_THREADS) bk_factor_kernel(BkArgs a)
 // (each column of the panel is brought up to date on the fly from the panel's L
 // columns and the W = L D columns before it), then the trailing triangle takes the
 // whole panel at once, A22 -= L21 W21^T: an emulated-FP64 product on the tensor
-// cores (emu_tc_update) for the solve, FP64 for the inverse (bk_factor_blocked).  As in dlasyf a panel
-// stops one column early unless its last pivot is 2x2 (the row-max search needs a
-// spare W column), and the interchanges that a panel applied to its own earlier L
-// columns are undone afterwards, which leaves the factor in dsytf2's form.
+// cores (emu_tc_update) for the solve, FP64 for the inverse (bk_factor_blocked).
+// As in dlasyf a panel stops one column early unless its last pivot is 2x2 (the
+// row-max search needs a spare W column), and the interchanges that a panel applied
+// to its own earlier L columns are undone afterwards, which leaves the factor in
+// dsytf2's form.
 //
 // The panel kernel is cooperative, one thread block per SM, two grid barriers per
-// column (three when the row-max search runs).  Every CTA takes the pivot decision
+// column (three when the row-max search runs, one when a step without interchange
+// shares its phase with the next column's update).  Every CTA takes the pivot decision
 // itself from per-CTA partial maxima, so no barrier waits on one CTA's decision.
 // The W rows that an interchange swaps are written to a two-row stage and put in
 // place during the next column's update, because every CTA still reads them while
