@@ -521,7 +521,9 @@ int qmlg_cho_invert(const double *A, int n, int64_t lda, double *Ainv, int64_t l
  * (qml/fcho_solve.f90:115-150), bound by qml.math.bkf_solve (qml/math.py:125-164).
  * Reads A's column-major lower triangle; A is not modified.  Returns 0, or LAPACK's
  * info (> 0: D(info, info) is exactly zero, x is then unusable, where the reference
- * prints a warning).
+ * prints a warning).  Above n = 256 (outside stream capture) the factorisation is
+ * dsytrf's blocked form (dlasyf panels) with the trailing updates as emulated-FP64
+ * tensor-core products; the call waits on the stream once per 64-column panel.
  */
 size_t qmlg_bkf_solve_workspace_size(int n);
 int qmlg_bkf_solve(const double *A, int n, int64_t lda, const double *y, double *x,
@@ -533,6 +535,8 @@ int qmlg_bkf_solve(const double *A, int n, int64_t lda, const double *y, double 
  * qml.math.bkf_invert (qml/math.py:100-122): Ainv (column-major, ldi, both
  * triangles) = A^-1, computed as the Schur complement left by n pivot steps on
  * [[A, I], [I, 0]] with the pivots searched among A's rows.  Returns 0 or info.
+ * Above n = 128 (outside stream capture) the factorisation is blocked as in
+ * qmlg_bkf_solve, with FP64 trailing updates.
  */
 size_t qmlg_bkf_invert_workspace_size(int n);
 int qmlg_bkf_invert(const double *A, int n, int64_t lda, double *Ainv, int64_t ldi,
