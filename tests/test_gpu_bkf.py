@@ -38,7 +38,7 @@ def indefinite(n, seed):
     return (A + A.T) / 2
 
 
-@pytest.mark.parametrize("n", [1, 2, 7, 64, 129, 300, 700])
+@pytest.mark.parametrize("n", [1, 2, 7, 64, 129, 300, 301, 700, 777])
 def test_bkf_vs_lapack_indefinite(cuda, oracle, n):
     A = indefinite(n, n)
     y = np.random.default_rng(n + 1).standard_normal(n)
