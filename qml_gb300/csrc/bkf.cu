@@ -459,10 +459,9 @@ struct BkPanelArgs {
     double *pv, *pv2;  // [grid] partial column maxima and row maxima
     int *pi;
     int *kb_out;       // columns this panel factorised
-    // the inverse's coupling rows (N > nsearch), else null: perm[p] is the original
-    // index at position p; tile_act[t] marks the 64-row tiles (of all N rows) that hold
-    // a coupling row whose pivot has been taken (the A rows' tiles are marked at start)
-    int *perm, *tile_act;
+    // the inverse (N > nsearch), else null: perm[p] is the original index at position
+    // p, kept through the interchanges (the coupling rows are ordered by it)
+    int *perm;
 };
 
 // A row's dot product over the lanes of a warp: lane l holds the products of columns
@@ -503,19 +502,14 @@ __device__ __forceinline__ void panel_column(const BkPanelArgs &a, int k, int kc
     }
 }
 
-// The inverse's coupling row n + j is zero in every column until the column that
-// holds its 1 (original index j, at position perm^-1(j)) becomes a pivot: the step's
-// interchange (kk <-> kp, kk < 0 for none) moves the original indices, and the rows of
-// the pivots it takes become live.  One thread.
+// The position-to-original-index map through the step's interchange (kk <-> kp,
+// kk < 0 for none).  One thread.
 __device__ __forceinline__ void mark_coupling(const BkPanelArgs &a, int k, int kstep, int kk, int kp)
 {
-    if (a.perm == nullptr) return;
-    if (kk >= 0) {
-        const int t = a.perm[kk];
-        a.perm[kk] = a.perm[kp];
-        a.perm[kp] = t;
-    }
-    for (int p = k; p < k + kstep; ++p) a.tile_act[(a.nsearch + a.perm[p]) >> 6] = 1;
+    if (a.perm == nullptr || kk < 0) return;
+    const int t = a.perm[kk];
+    a.perm[kk] = a.perm[kp];
+    a.perm[kp] = t;
 }
 
 // Every CTA reduces the partials (value, first index) itself, in warp 0, and hands
@@ -875,19 +869,13 @@ __device__ __forceinline__ void bk_tri_index(int64_t t, int &bi, int &bj)
 
 __global__ void __launch_bounds__(256)
 bk_update_fp64_kernel(double *__restrict__ W, int64_t ld, int N, int k0, int k1, int kb,
-                      const double *__restrict__ Wp, const int *__restrict__ tile_act)
+                      const double *__restrict__ Wp)
 {
     __shared__ double Ls[16][64 + 1];
     __shared__ double Ws[16][64 + 1];
     int bi, bj;
     bk_tri_index(blockIdx.x, bi, bj);
     const int i0 = k1 + bi * 64, j0 = k1 + bj * 64;
-    if (tile_act != nullptr) {
-        // rows (or columns) that are all coupling rows not yet live contribute zeros
-        const int T = (N + 63) >> 6;
-        auto live = [&](int r0) { return tile_act[r0 >> 6] != 0 || ((r0 + 63) >> 6 < T && tile_act[(r0 + 63) >> 6] != 0); };
-        if (!live(i0) || !live(j0)) return;
-    }
     const int tid = threadIdx.x;
     const int tx = tid & 15, ty = tid >> 4;  // tx -> j, ty -> i
     double acc[4][4];
@@ -931,12 +919,93 @@ bk_update_fp64_kernel(double *__restrict__ W, int64_t ld, int N, int k0, int k1,
     }
 }
 
-// perm = identity; the tiles holding A rows live, the coupling rows' tiles not yet.
-__global__ void bk_coupling_init_kernel(int *__restrict__ perm, int n, int *__restrict__ tile_act, int T)
+// ---- the inverse's coupling rows
+// In [[A, I], [I, 0]] the coupling row of original index j is zero in every column
+// until the column holding its 1 becomes a pivot, and each pivot brings one such row
+// to life.  After every panel the coupling block is permuted (rows and columns
+// together) so that coupling position p holds the row of the original index pivoted
+// at position p: the live coupling rows are then [n, n + k1), and the trailing
+// update only covers [k1, n + k1).  cpos/corig map original indices to coupling
+// positions and back; srcmap (identity between panels) gives, for a position, the
+// position its data comes from.
+
+__global__ void bk_coupling_init_kernel(int *__restrict__ perm, int *__restrict__ cpos,
+                                        int *__restrict__ corig, int *__restrict__ srcmap, int n,
+                                        int *__restrict__ naff)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) perm[i] = i;
-    if (i < T) tile_act[i] = (i << 6) < n ? 1 : 0;
+    if (i < n) perm[i] = cpos[i] = corig[i] = srcmap[i] = i;
+    if (i == 0) *naff = 0;
+}
+
+// One thread: the transpositions that bring the originals pivoted at positions
+// [k0, k1) to coupling positions [k0, k1), and the list of positions whose data moves.
+__global__ void bk_compact_plan_kernel(const int *__restrict__ perm, int k0, int k1, int *__restrict__ cpos,
+                                       int *__restrict__ corig, int *__restrict__ srcmap,
+                                       int *__restrict__ aff, int *__restrict__ naff)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int m = *naff;
+    for (int u = 0; u < m; ++u) srcmap[aff[u]] = aff[u];  // the last panel's moves are done
+    m = 0;
+    auto note = [&](int x) {
+        for (int u = 0; u < m; ++u)
+            if (aff[u] == x) return;
+        aff[m++] = x;
+    };
+    for (int p = k0; p < k1; ++p) {
+        const int j = perm[p], q = cpos[j];
+        if (q == p) continue;
+        const int jp = corig[p];
+        corig[p] = j;
+        cpos[j] = p;
+        corig[q] = jp;
+        cpos[jp] = q;
+        const int sp = srcmap[p];
+        srcmap[p] = srcmap[q];
+        srcmap[q] = sp;
+        note(p);
+        note(q);
+    }
+    *naff = m;
+}
+
+__device__ __forceinline__ double& wsym(double *W, int64_t ld, int r, int c)
+{
+    return r >= c ? W[(int64_t)r * ld + c] : W[(int64_t)c * ld + r];
+}
+
+// The old full (symmetric) rows of the positions that move, and their W rows, into
+// tmp (grid.y = row of the list).
+__global__ void bk_compact_gather_kernel(const double *__restrict__ W, int64_t ld, int N, int n,
+                                         const double *__restrict__ Wp, const int *__restrict__ aff,
+                                         const int *__restrict__ naff, const int *__restrict__ srcmap,
+                                         double *__restrict__ tmp, double *__restrict__ tmpw)
+{
+    const int u = blockIdx.y;
+    if (u >= *naff) return;
+    const int src = n + srcmap[aff[u]];
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
+        tmp[(int64_t)u * N + c] = src >= c ? W[(int64_t)src * ld + c] : W[(int64_t)c * ld + src];
+        if (c < BK_NB) tmpw[u * BK_NB + c] = Wp[(int64_t)src * BK_NB + c];
+    }
+}
+
+// new(r, c) = old(srcmap r, srcmap c) on the moved positions' rows (and so columns).
+// Where both r and c move, two threads write the same value.
+__global__ void bk_compact_scatter_kernel(double *__restrict__ W, int64_t ld, int N, int n,
+                                          double *__restrict__ Wp, const int *__restrict__ aff,
+                                          const int *__restrict__ naff, const int *__restrict__ srcmap,
+                                          const double *__restrict__ tmp, const double *__restrict__ tmpw)
+{
+    const int u = blockIdx.y;
+    if (u >= *naff) return;
+    const int r = n + aff[u];
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
+        const int cs = c >= n ? n + srcmap[c - n] : c;
+        wsym(W, ld, r, c) = tmp[(int64_t)u * N + cs];
+        if (c < BK_NB) Wp[(int64_t)r * BK_NB + c] = tmpw[u * BK_NB + c];
+    }
 }
 
 // Puts the panel's L columns in dsytf2's form: the interchange of each step is
@@ -1277,7 +1346,8 @@ __global__ void bk_build_kernel(const double *__restrict__ A, int64_t lda, int n
     }
 }
 
-__global__ void bk_extract_kernel(const double *__restrict__ W, int n, double *__restrict__ Ainv,
+__global__ void bk_extract_kernel(const double *__restrict__ W, int n, const int *__restrict__ cpos,
+                                  double *__restrict__ Ainv,
                                   int64_t ldi)
 {
     const int N = 2 * n;
@@ -1285,7 +1355,8 @@ __global__ void bk_extract_kernel(const double *__restrict__ W, int n, double *_
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
         const int i = (int)(e % n), j = (int)(e / n);
-        const int hi = i > j ? i : j, lo = i > j ? j : i;
+        const int pi = cpos[i], pj = cpos[j];  // the coupling positions of i and j
+        const int hi = pi > pj ? pi : pj, lo = pi > pj ? pj : pi;
         Ainv[(int64_t)i + (int64_t)j * ldi] = -W[(int64_t)(n + hi) * N + (n + lo)];
     }
 }
@@ -1293,8 +1364,8 @@ __global__ void bk_extract_kernel(const double *__restrict__ W, int n, double *_
 constexpr int BK_MAX_GRID = 1024;
 
 struct BkBufs {
-    int *info, *dec, *ipiv, *pi, *kb, *err, *expo, *perm, *tact;
-    double *W, *col, *ci, *p0, *p1, *w0, *w1, *sc, *pv, *pv2, *Wp, *stage;
+    int *info, *dec, *ipiv, *pi, *kb, *err, *expo, *perm, *cpos, *corig, *srcmap, *aff, *naff;
+    double *W, *col, *ci, *p0, *p1, *w0, *w1, *sc, *pv, *pv2, *Wp, *stage, *ctmp, *ctmpw;
     __nv_bfloat16 *dig;
 };
 
@@ -1323,8 +1394,10 @@ size_t bk_ws(int n, int N)
     p.add<int>(4);
     p.add<int>((size_t)bk_plane_rows(N));
     p.add<__nv_bfloat16>((size_t)BK_SLICES * bk_plane_rows(N) * BK_NB);
-    p.add<int>((size_t)std::max(n, 1));
-    p.add<int>((size_t)(N + 63) / 64);
+    for (int v = 0; v < 5; ++v) p.add<int>((size_t)std::max(n, 1));  // perm, cpos, corig, srcmap, aff
+    p.add<int>(4);
+    p.add<double>((size_t)2 * BK_NB * N);
+    p.add<double>((size_t)2 * BK_NB * BK_NB);
     return p.total();
 }
 
@@ -1340,17 +1413,12 @@ size_t bk_ws(int n, int N)
 int bk_factor_blocked(BkBufs &b, int n, int N, int grid, bool undo, bool exact, cudaStream_t s)
 {
     BkPanelArgs pa{b.W, (int64_t)N, N, n, 0, b.Wp, b.stage, b.ipiv, b.info, b.pv, b.pv2, b.pi, b.kb,
-                   nullptr, nullptr};
+                   nullptr};
     const int rpad = bk_plane_rows(N), roff = qmlg::plane_rows(N);
     cudaError_t e = cudaMemsetAsync(b.err, 0, sizeof(int), s);
     if (e != cudaSuccess) return qmlg::set_cuda_error(e);
-    if (N > n) {
-        pa.perm = b.perm;
-        pa.tile_act = b.tact;
-        const int T = (N + 63) / 64;
-        bk_coupling_init_kernel<<<(unsigned)qmlg::ceil_div(std::max(n, T), 256), 256, 0, s>>>(b.perm, n, b.tact, T);
-        qmlg::count_launches(1);
-    }
+    const bool coupled = N > n;  // the maps were set to the identity by bk_factor
+    if (coupled) pa.perm = b.perm;
     int st = QMLG_OK;
     for (int k0 = 0; k0 < n;) {
         pa.k0 = k0;
@@ -1361,10 +1429,22 @@ int bk_factor_blocked(BkBufs &b, int n, int N, int grid, bool undo, bool exact, 
         if ((st = qmlg::read_back(&kb, b.kb, sizeof(int), s)) != QMLG_OK) return st;
         if (kb < 1 || kb > BK_NB || k0 + kb > n) return QMLG_E_CUDA;
         const int k1 = k0 + kb;
-        if (k1 < N && exact) {
-            const int64_t t = qmlg::ceil_div(N - k1, 64);
-            bk_update_fp64_kernel<<<(unsigned)(t * (t + 1) / 2), 256, 0, s>>>(b.W, N, N, k0, k1, kb, b.Wp,
-                                                                               pa.tile_act);
+        if (coupled) {
+            // the coupling rows pivoted in this panel to positions [k0, k1)
+            bk_compact_plan_kernel<<<1, 32, 0, s>>>(b.perm, k0, k1, b.cpos, b.corig, b.srcmap, b.aff, b.naff);
+            const dim3 cg((unsigned)std::min<int64_t>(qmlg::ceil_div(N, 256), 64), 2 * BK_NB);
+            bk_compact_gather_kernel<<<cg, 256, 0, s>>>(b.W, N, N, n, b.Wp, b.aff, b.naff, b.srcmap, b.ctmp,
+                                                        b.ctmpw);
+            bk_compact_scatter_kernel<<<cg, 256, 0, s>>>(b.W, N, N, n, b.Wp, b.aff, b.naff, b.srcmap, b.ctmp,
+                                                         b.ctmpw);
+            qmlg::count_launches(3);
+            if ((st = qmlg::check_launch()) != QMLG_OK) return st;
+        }
+        // the live rows end at n + k1 (the coupling rows not yet pivoted are zero)
+        const int ne = coupled ? std::min(N, n + k1) : N;
+        if (k1 < ne && exact) {
+            const int64_t t = qmlg::ceil_div(ne - k1, 64);
+            bk_update_fp64_kernel<<<(unsigned)(t * (t + 1) / 2), 256, 0, s>>>(b.W, N, ne, k0, k1, kb, b.Wp);
             qmlg::count_launches(1);
             if ((st = qmlg::check_launch()) != QMLG_OK) return st;
         } else if (k1 < N) {
@@ -1414,11 +1494,22 @@ int bk_factor(const double *A, int64_t lda, int n, int N, void *workspace, size_
     b.expo = ws.take<int>((size_t)bk_plane_rows(N));
     b.dig = ws.take<__nv_bfloat16>((size_t)BK_SLICES * bk_plane_rows(N) * BK_NB);
     b.perm = ws.take<int>((size_t)std::max(n, 1));
-    b.tact = ws.take<int>((size_t)(N + 63) / 64);
+    b.cpos = ws.take<int>((size_t)std::max(n, 1));
+    b.corig = ws.take<int>((size_t)std::max(n, 1));
+    b.srcmap = ws.take<int>((size_t)std::max(n, 1));
+    b.aff = ws.take<int>((size_t)std::max(n, 1));
+    b.naff = ws.take<int>(4);
+    b.ctmp = ws.take<double>((size_t)2 * BK_NB * N);
+    b.ctmpw = ws.take<double>((size_t)2 * BK_NB * BK_NB);
     cudaError_t e = cudaMemsetAsync(b.info, 0, sizeof(int), s);
     if (e != cudaSuccess) return qmlg::set_cuda_error(e);
     const int blocks = (int)std::min<int64_t>(qmlg::ceil_div((int64_t)N * N, 256), 152 * 64);
     { bk_build_kernel<<<blocks, 256, 0, s>>>(A, lda, n, N, b.W); qmlg::count_launches(1); }
+    if (N > n) {  // the inverse: coupling positions start as the identity
+        bk_coupling_init_kernel<<<(unsigned)qmlg::ceil_div(n, 256), 256, 0, s>>>(b.perm, b.cpos, b.corig,
+                                                                                 b.srcmap, n, b.naff);
+        qmlg::count_launches(1);
+    }
     int grid = 1;
     if (N > 256 && qmlg::cooperative_allowed_on(s)) {
         int dev = 0, sms = 0, per = 0, per2 = 0;
@@ -1496,7 +1587,7 @@ extern "C" int qmlg_bkf_invert(const double *A, int n, int64_t lda, double *Ainv
     int st = bk_factor(A, lda, n, 2 * n, workspace, ws_bytes, b, false, true, s);
     if (st != QMLG_OK) return st;
     const int eb = (int)std::min<int64_t>(qmlg::ceil_div((int64_t)n * n, 256), 152 * 64);
-    { bk_extract_kernel<<<eb, 256, 0, s>>>(b.W, n, Ainv, ldi); qmlg::count_launches(1); }
+    { bk_extract_kernel<<<eb, 256, 0, s>>>(b.W, n, b.cpos, Ainv, ldi); qmlg::count_launches(1); }
     if ((st = qmlg::check_launch()) != QMLG_OK) return st;
     int info = 0;
     st = qmlg::read_back(&info, b.info, sizeof(int), s);
