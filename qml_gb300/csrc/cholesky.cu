@@ -1589,11 +1589,14 @@ inline int chain_reserve(int sms, int m)
 // free, while the next panel's 64-wide FP64 chain runs on the auxiliary stream in
 // those SMs.  The two touch disjoint columns; the next outer step joins them.
 int emulated_factor(double *A, int n, int64_t lda, double shift, Workspace &ws, int *d_info,
-                    EmulatedFactor &f, cudaStream_t s, int slices, int npiv)
+                    EmulatedFactor &f, cudaStream_t s, int slices, int npiv, bool coupled)
 {
     // npiv < n (a multiple of 64): only the first npiv pivots; the trailing
     // (n - npiv) block is left holding its Schur complement
     const int np = (npiv < 0 || npiv > n) ? n : npiv;
+    // coupled ([[A_p, E], [E^T, 0]], as cholesky_fp64): the rows live once the
+    // pivots before c are taken end at np + c; the launches stop there
+    auto live_end = [&](int c) { return coupled ? std::min(n, np + c) : n; };
     const int rpad = (int)ceil_div(n, 128) * 128;
     __nv_bfloat16 *dig_out = ws.take<__nv_bfloat16>((size_t)kEmuMaxSlices * rpad * NBO);
     int *exp_out = ws.take<int>((size_t)rpad);
@@ -1616,8 +1619,8 @@ int emulated_factor(double *A, int n, int64_t lda, double shift, Workspace &ws, 
     // (cooperative kernels off, e.g. batched fits) keep one stream per solve and
     // skip the look-ahead, so concurrent solves do not share the auxiliary stream.
     const bool lookahead = sms >= 64 && cooperative_on();
-    st = factor_panel(A, n, lda, shift, 0, std::min(NBO, np), rpad, slices, dig_in, exp_in, d_info,
-                      d_err, s, 0);
+    st = factor_panel(A, live_end(std::min(NBO, np)), lda, shift, 0, std::min(NBO, np), rpad, slices,
+                      dig_in, exp_in, d_info, d_err, s, 0);
     for (int K0 = 0; K0 < np && st == QMLG_OK; K0 += NBO) {
         const int K1 = std::min(K0 + NBO, np);
         if (K1 >= n) break;
@@ -1625,15 +1628,16 @@ int emulated_factor(double *A, int n, int64_t lda, double shift, Workspace &ws, 
         const bool more = K2 > K1;
         const int kw = K1 - K0;
         const int kp = (int)ceil_div(kw, 64) * 64;
-        st = slice_rows(A, lda, K1, n - K1, K0, kw, kp, rpad, slices, dig_out, exp_out, d_info, s);
+        const int ne = live_end(K1);  // rows with a nonzero entry in this panel end here
+        st = slice_rows(A, lda, K1, ne - K1, K0, kw, kp, rpad, slices, dig_out, exp_out, d_info, s);
         if (st != QMLG_OK) break;
         // (1) the next panel's columns
         if (more)
-            st = emu_tc_update(A, lda, K1, K2, K1, n, dig_out, exp_out, kp, rpad, slices, 0, 0, 1,
+            st = emu_tc_update(A, lda, K1, K2, K1, ne, dig_out, exp_out, kp, rpad, slices, 0, 0, 1,
                                d_err, s, 0);
         if (st != QMLG_OK) break;
-        if (more && K2 < n && lookahead) {
-            const int reserve = chain_reserve(sms, n - K2);
+        if (more && K2 < ne && lookahead) {
+            const int reserve = chain_reserve(sms, ne - K2);
             // fork: the next panel's chain on the auxiliary stream
             if ((e = cudaEventRecord(aux->fork, s)) != cudaSuccess ||
                 (e = cudaStreamWaitEvent(aux->stream, aux->fork, 0)) != cudaSuccess) {
@@ -1641,22 +1645,22 @@ int emulated_factor(double *A, int n, int64_t lda, double shift, Workspace &ws, 
                 break;
             }
             // (2) the rest of the trailing matrix, leaving `reserve` SMs free
-            st = emu_tc_update(A, lda, K2, n, K2, n, dig_out, exp_out, kp, rpad, slices, K2 - K1,
+            st = emu_tc_update(A, lda, K2, ne, K2, ne, dig_out, exp_out, kp, rpad, slices, K2 - K1,
                                K2 - K1, 1, d_err, s, sms - reserve);
             if (st == QMLG_OK)
-                st = factor_panel(A, n, lda, shift, K1, K2, rpad, slices, dig_in, exp_in, d_info,
-                                  d_err, aux->stream, -1);
+                st = factor_panel(A, live_end(K2), lda, shift, K1, K2, rpad, slices, dig_in, exp_in,
+                                  d_info, d_err, aux->stream, -1);
             // join before the next outer step reads the panel (and reuses dig_out)
             if (st == QMLG_OK && ((e = cudaEventRecord(aux->join, aux->stream)) != cudaSuccess ||
                                   (e = cudaStreamWaitEvent(s, aux->join, 0)) != cudaSuccess))
                 st = set_cuda_error(e);
         } else {
-            if (K2 < n)
-                st = emu_tc_update(A, lda, K2, n, K2, n, dig_out, exp_out, kp, rpad, slices, K2 - K1,
+            if (K2 < ne)
+                st = emu_tc_update(A, lda, K2, ne, K2, ne, dig_out, exp_out, kp, rpad, slices, K2 - K1,
                                    K2 - K1, 1, d_err, s, 0);
             if (st == QMLG_OK && more)
-                st = factor_panel(A, n, lda, shift, K1, K2, rpad, slices, dig_in, exp_in, d_info,
-                                  d_err, s, 0);
+                st = factor_panel(A, live_end(K2), lda, shift, K1, K2, rpad, slices, dig_in, exp_in,
+                                  d_info, d_err, s, 0);
         }
     }
     if (st != QMLG_OK) return st;
@@ -2171,7 +2175,7 @@ extern "C" int qmlg_cho_invert(const double *A, int n, int64_t lda, double *Ainv
     int st;
     if (precision == QMLG_PREC_MIXED) {
         qmlg::EmulatedFactor f;
-        st = qmlg::emulated_factor(M, N, N, 0.0, ws, d_info, f, s, 8, np);
+        st = qmlg::emulated_factor(M, N, N, 0.0, ws, d_info, f, s, 8, np, true);
         if (st == QMLG_OK) st = qmlg::read_device_flag(f.d_err, s);
     } else {
         st = qmlg::cholesky_fp64(M, N, N, 0.0, d_info, s, np, true);

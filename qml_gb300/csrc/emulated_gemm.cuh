@@ -112,8 +112,10 @@ struct EmulatedFactor {
 size_t emulated_factor_ws(int n);
 // npiv (a multiple of 64, or -1 for n): take only the first npiv pivots, leaving the
 // Schur complement in the trailing block.
+// coupled: as cholesky_fp64's (the inverse's augmented matrix).
 int emulated_factor(double *A, int n, int64_t lda, double shift, Workspace &ws, int *d_info,
-                    EmulatedFactor &f, cudaStream_t s, int slices = 8, int npiv = -1);
+                    EmulatedFactor &f, cudaStream_t s, int slices = 8, int npiv = -1,
+                    bool coupled = false);
 int emulated_potrs(const EmulatedFactor &f, double *x, cudaStream_t s);
 // A cooperative launch ordered after every earlier one of this process on the
 // device (so two whole-GPU grids are never resident together), and whether one is
