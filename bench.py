@@ -395,10 +395,28 @@ def run_extra(a, dev, batch, X, stream):
     c0 = time.perf_counter()
     orc.bkf_invert(Kh)
     cv = time.perf_counter() - c0
+    # the same on a random symmetric indefinite matrix, where Bunch-Kaufman pivots
+    # (2x2 pivots and interchanges at most steps)
+    rng = np.random.default_rng(5000)
+    Bh = rng.standard_normal((ni, ni))
+    Sh = Bh + Bh.T
+    Si = torch.from_numpy(Sh).to(dev)
+    tsi = gpu_time(lambda: core.bkf_solve(Si, yi))
+    tvi = gpu_time(lambda: core.bkf_invert(Si))
+    Shf = np.asfortranarray(Sh)
+    c0 = time.perf_counter()
+    orc.bkf_solve(Shf, np.ones(ni))
+    csi = time.perf_counter() - c0
+    c0 = time.perf_counter()
+    orc.bkf_invert(Shf)
+    cvi = time.perf_counter() - c0
     out["inverses_n5000"] = {"cho_invert_gpu_fp64_s": tf, "cho_invert_gpu_mixed_s": tm,
                              "cho_invert_lapack_s": ci, "bkf_solve_gpu_s": ts,
                              "bkf_solve_lapack_s": cs, "bkf_invert_gpu_s": tv,
                              "bkf_invert_lapack_s": cv,
+                             "indefinite": {"bkf_solve_gpu_s": tsi, "bkf_solve_lapack_s": csi,
+                                            "bkf_invert_gpu_s": tvi, "bkf_invert_lapack_s": cvi,
+                                            "matrix": "B + B^T, B standard normal, seed 5000"},
                              "cpu_sample": "scipy LAPACK, full size, OpenBLAS threads"}
     return out
 
