@@ -1071,7 +1071,7 @@ __global__ void __launch_bounds__(1024)
 bk_solve_kernel(const double *__restrict__ W, int64_t ld, int n, const int *__restrict__ ipiv,
                 double *__restrict__ bg, int *__restrict__ steps)
 {
-    __shared__ double red0[1024], red1[1024];
+    __shared__ double red0[1024], red1[1024], q0[4], q1[4];
     extern __shared__ double sb[];
     double *b = SH ? sb : bg;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nt = blockDim.x;
@@ -1136,9 +1136,9 @@ bk_solve_kernel(const double *__restrict__ W, int64_t ld, int n, const int *__re
         red1[tid] = s1;
         if (two) red0[tid] = s0;
         __syncthreads();
-        if (warp == 0) {
+        if (warp < 4) {  // four warps reduce a quarter each (as in the ring kernel)
             double a0 = 0.0, a1 = 0.0;
-            for (int j = lane; j < nt; j += 32) {
+            for (int j = warp * (nt >> 2) + lane; j < (warp + 1) * (nt >> 2); j += 32) {
                 a1 += red1[j];
                 if (two) a0 += red0[j];
             }
@@ -1147,8 +1147,13 @@ bk_solve_kernel(const double *__restrict__ W, int64_t ld, int n, const int *__re
                 if (two) a0 += __shfl_xor_sync(0xffffffffu, a0, off);
             }
             if (lane == 0) {
-                b[k] -= a1;
-                if (two) b[k - 1] -= a0;
+                q1[warp] = a1;
+                q0[warp] = a0;
+            }
+            asm volatile("bar.sync 1, 128;" ::: "memory");
+            if (tid == 0) {
+                b[k] -= (q1[0] + q1[1]) + (q1[2] + q1[3]);
+                if (two) b[k - 1] -= (q0[0] + q0[1]) + (q0[2] + q0[3]);
                 if (kp != k) {
                     const double t = b[k];
                     b[k] = b[kp];
@@ -1202,7 +1207,7 @@ bk_solve_ring_kernel(const double *__restrict__ W, int64_t ld, int n, const int 
                      double *__restrict__ bg, int *__restrict__ steps)
 {
     constexpr int NS = DEPTH + 2;
-    __shared__ double red0[1024], red1[1024];
+    __shared__ double red0[1024], red1[1024], q0[4], q1[4];
     extern __shared__ double sm[];
     double *b = sm, *ring = sm + n;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nt = blockDim.x;
@@ -1216,17 +1221,15 @@ bk_solve_ring_kernel(const double *__restrict__ W, int64_t ld, int n, const int 
     };
     // ---- L x = P b (the D solves follow in one pass)
     int issued = 0;  // columns [0, issued) are in flight or arrived
-    {
-        const int kk0 = n > 1 && ipiv[0] < 0 ? 1 : 0;
-        while (issued < n && issued <= kk0 + DEPTH) issue(issued++);
-        cp_async_wait_pending(issued - 1 - kk0);
-        __syncthreads();
-    }
     int k = 0;
     while (k < n) {
         const int p = ipiv[k];
         const bool two = p < 0;
         const int kp = two ? -p - 1 : p - 1, kk = two ? k + 1 : k;
+        // keep DEPTH columns ahead of this step and wait for its own: the slots
+        // refilled belong to columns before k, done with by the last barrier
+        while (issued < n && issued <= kk + DEPTH) issue(issued++);
+        cp_async_wait_pending(issued - 1 - kk);
         if (tid == 0) {
             steps[k] = two ? 2 : 1;
             if (two) steps[k + 1] = 0;
@@ -1243,16 +1246,8 @@ bk_solve_ring_kernel(const double *__restrict__ W, int64_t ld, int n, const int 
             if (two) b[i] -= ck[i] * b0 + ck1[i] * b1;
             else b[i] -= ck[i] * b0;
         }
-        // the next step's columns: keep DEPTH ahead of it and wait for its own
-        const int kn = kk + 1;
-        if (kn < n) {
-            const int kkn = ipiv[kn] < 0 ? kn + 1 : kn;
-            __syncthreads();  // every thread is done with this step's slots
-            while (issued < n && issued <= kkn + DEPTH) issue(issued++);
-            cp_async_wait_pending(issued - 1 - kkn);
-        }
         __syncthreads();
-        k = kn;
+        k = kk + 1;
     }
     // ---- D x = b, every pivot block at once
     for (int c = tid; c < n; c += nt) {
@@ -1296,9 +1291,11 @@ bk_solve_ring_kernel(const double *__restrict__ W, int64_t ld, int n, const int 
         if (two) red0[tid] = s0;
         __syncthreads();  // also: every thread is done with this step's slots
         const int kn = c - 1;
-        if (warp == 0) {
+        if (warp < 4) {
+            // four warps (one per scheduler's FP64 pipe) reduce a quarter each,
+            // then the first of them the four sums
             double a0 = 0.0, a1 = 0.0;
-            for (int j = lane; j < nt; j += 32) {
+            for (int j = warp * (nt >> 2) + lane; j < (warp + 1) * (nt >> 2); j += 32) {
                 a1 += red1[j];
                 if (two) a0 += red0[j];
             }
@@ -1307,8 +1304,13 @@ bk_solve_ring_kernel(const double *__restrict__ W, int64_t ld, int n, const int 
                 if (two) a0 += __shfl_xor_sync(0xffffffffu, a0, off);
             }
             if (lane == 0) {
-                b[k] -= a1;
-                if (two) b[k - 1] -= a0;
+                q1[warp] = a1;
+                q0[warp] = a0;
+            }
+            asm volatile("bar.sync 1, 128;" ::: "memory");
+            if (tid == 0) {
+                b[k] -= (q1[0] + q1[1]) + (q1[2] + q1[3]);
+                if (two) b[k - 1] -= (q0[0] + q0[1]) + (q0[2] + q0[3]);
                 if (kp != k) {
                     const double t = b[k];
                     b[k] = b[kp];
