@@ -1363,11 +1363,67 @@ __global__ void bk_extract_kernel(const double *__restrict__ W, int n, const int
     }
 }
 
+// r = y - A x in FP64 for the refinement step of the blocked solve, A the caller's
+// column-major lower triangle (lda).  Lower part with the diagonal: 256-row blocks
+// against 256-column chunks (column loads coalesced across the rows), partial sums
+// per chunk in P[chunk][row]; strictly upper part: one warp per column j dotting
+// column j below the diagonal with x.  The order of summation is fixed.
+constexpr int BK_RES_T = 256;
+
+__global__ void __launch_bounds__(BK_RES_T)
+bk_resid_lower_kernel(const double *__restrict__ A, int64_t lda, int n, const double *__restrict__ x,
+                      double *__restrict__ P)
+{
+    __shared__ double xs[BK_RES_T];
+    const int rb = blockIdx.x, cb = blockIdx.y;
+    if (cb > rb) return;
+    const int i = rb * BK_RES_T + threadIdx.x, j0 = cb * BK_RES_T;
+    const int j1 = min(n, j0 + BK_RES_T);
+    if (j0 + (int)threadIdx.x < n) xs[threadIdx.x] = x[j0 + threadIdx.x];
+    __syncthreads();
+    if (i >= n) return;
+    const int je = min(j1, i + 1);
+    double s = 0.0;
+    for (int j = j0; j < je; ++j) s = fma(A[(int64_t)i + (int64_t)j * lda], xs[j - j0], s);
+    P[(int64_t)cb * n + i] = s;
+}
+
+__global__ void bk_resid_upper_kernel(const double *__restrict__ A, int64_t lda, int n,
+                                      const double *__restrict__ x, double *__restrict__ U)
+{
+    const int lane = threadIdx.x & 31;
+    const int j = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+    if (j >= n) return;
+    const double *col = A + (int64_t)j * lda;
+    double s = 0.0;
+    for (int i = j + 1 + lane; i < n; i += 32) s = fma(col[i], x[i], s);
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    if (lane == 0) U[j] = s;
+}
+
+// r = y - (sum of the chunks in order + the upper part)
+__global__ void bk_resid_finish_kernel(int n, const double *__restrict__ y, const double *__restrict__ P,
+                                       const double *__restrict__ U, double *__restrict__ r)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double s = 0.0;
+    for (int cb = 0; cb <= i / BK_RES_T; ++cb) s += P[(int64_t)cb * n + i];
+    r[i] = y[i] - (s + U[i]);
+}
+
+__global__ void bk_axpy_kernel(int n, const double *__restrict__ d, double *__restrict__ x)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] += d[i];
+}
+
 constexpr int BK_MAX_GRID = 1024;
 
 struct BkBufs {
     int *info, *dec, *ipiv, *pi, *kb, *err, *expo, *perm, *cpos, *corig, *srcmap, *aff, *naff;
-    double *W, *col, *ci, *p0, *p1, *w0, *w1, *sc, *pv, *pv2, *Wp, *stage, *ctmp, *ctmpw;
+    double *W, *col, *ci, *p0, *p1, *w0, *w1, *sc, *pv, *pv2, *Wp, *stage, *ctmp, *ctmpw, *rP, *rU, *rr;
+    bool blocked = false;
     __nv_bfloat16 *dig;
 };
 
@@ -1400,6 +1456,10 @@ size_t bk_ws(int n, int N)
     p.add<int>(4);
     p.add<double>((size_t)2 * BK_NB * N);
     p.add<double>((size_t)2 * BK_NB * BK_NB);
+    // the solve's refinement: chunk partials, upper part, residual
+    p.add<double>((size_t)qmlg::ceil_div(std::max(n, 1), BK_RES_T) * std::max(n, 1));
+    p.add<double>((size_t)std::max(n, 1));
+    p.add<double>((size_t)std::max(n, 1));
     return p.total();
 }
 
@@ -1503,6 +1563,9 @@ int bk_factor(const double *A, int64_t lda, int n, int N, void *workspace, size_
     b.naff = ws.take<int>(4);
     b.ctmp = ws.take<double>((size_t)2 * BK_NB * N);
     b.ctmpw = ws.take<double>((size_t)2 * BK_NB * BK_NB);
+    b.rP = ws.take<double>((size_t)qmlg::ceil_div(std::max(n, 1), BK_RES_T) * std::max(n, 1));
+    b.rU = ws.take<double>((size_t)std::max(n, 1));
+    b.rr = ws.take<double>((size_t)std::max(n, 1));
     cudaError_t e = cudaMemsetAsync(b.info, 0, sizeof(int), s);
     if (e != cudaSuccess) return qmlg::set_cuda_error(e);
     const int blocks = (int)std::min<int64_t>(qmlg::ceil_div((int64_t)N * N, 256), 152 * 64);
@@ -1525,6 +1588,7 @@ int bk_factor(const double *A, int64_t lda, int n, int N, void *workspace, size_
         const int lim = qmlg::sm_limit(sms);
         grid = std::max(1, std::min({lim, sms * std::max(std::min(per, per2), 1), BK_MAX_GRID}));
     }
+    b.blocked = grid > 1;
     if (grid > 1) return bk_factor_blocked(b, n, N, grid, undo, exact, s);
     BkArgs a{b.W, (int64_t)N, N, n, b.ipiv, b.info, b.col, b.ci, b.p0, b.p1, b.w0, b.w1, b.sc, b.pv, b.pi, b.dec};
     bk_factor_kernel<<<1, BK_THREADS, 0, s>>>(a);
@@ -1553,27 +1617,49 @@ extern "C" int qmlg_bkf_solve(const double *A, int n, int64_t lda, const double 
         bk_transpose_kernel<<<(unsigned)(t * (t + 1) / 2), 256, 0, s>>>(b.W, n, n);
         qmlg::count_launches(1);
     }
-    const size_t ring2 = sizeof(double) * 5 * (size_t)n;
-    // the kernel's 16 KB of static shared memory counts too
-    if (ring2 + 18 * 1024 <= (size_t)227 * 1024) {
-        if ((e = cudaFuncSetAttribute(bk_solve_ring_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)ring2)) != cudaSuccess)
-            return qmlg::set_cuda_error(e);
-        bk_solve_ring_kernel<2><<<1, 1024, ring2, s>>>(b.W, n, n, b.ipiv, x, reinterpret_cast<int *>(b.col));
-    } else if (n <= BK_SOLVE_SMEM) {
-        const size_t smem = sizeof(double) * (size_t)n;
-        if ((e = cudaFuncSetAttribute(bk_solve_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)std::max<size_t>(smem, 1))) != cudaSuccess)
-            return qmlg::set_cuda_error(e);
-        bk_solve_kernel<true><<<1, 1024, smem, s>>>(b.W, n, n, b.ipiv, x, reinterpret_cast<int *>(b.col));
-    } else {
-        bk_solve_kernel<false><<<1, 1024, 0, s>>>(b.W, n, n, b.ipiv, x, reinterpret_cast<int *>(b.col));
-    }
-    qmlg::count_launches(1);
-    if ((st = qmlg::check_launch()) != QMLG_OK) return st;
+    // dsytrs on v in place with the factor (and L^T above its diagonal)
+    auto dsytrs = [&](double *v) -> int {
+        const size_t ring2 = sizeof(double) * 5 * (size_t)n;
+        // the kernel's 16 KB of static shared memory counts too
+        if (ring2 + 18 * 1024 <= (size_t)227 * 1024) {
+            if ((e = cudaFuncSetAttribute(bk_solve_ring_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)ring2)) != cudaSuccess)
+                return qmlg::set_cuda_error(e);
+            bk_solve_ring_kernel<2><<<1, 1024, ring2, s>>>(b.W, n, n, b.ipiv, v, reinterpret_cast<int *>(b.col));
+        } else if (n <= BK_SOLVE_SMEM) {
+            const size_t smem = sizeof(double) * (size_t)n;
+            if ((e = cudaFuncSetAttribute(bk_solve_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)std::max<size_t>(smem, 1))) != cudaSuccess)
+                return qmlg::set_cuda_error(e);
+            bk_solve_kernel<true><<<1, 1024, smem, s>>>(b.W, n, n, b.ipiv, v, reinterpret_cast<int *>(b.col));
+        } else {
+            bk_solve_kernel<false><<<1, 1024, 0, s>>>(b.W, n, n, b.ipiv, v, reinterpret_cast<int *>(b.col));
+        }
+        qmlg::count_launches(1);
+        return qmlg::check_launch();
+    };
+    if ((st = dsytrs(x)) != QMLG_OK) return st;
     int info = 0;
-    st = qmlg::read_back(&info, b.info, sizeof(int), s);
-    return st != QMLG_OK ? st : info;
+    if ((st = qmlg::read_back(&info, b.info, sizeof(int), s)) != QMLG_OK) return st;
+    if (info == 0 && b.blocked) {
+        // The blocked factor's trailing updates are emulated-FP64 products (fixed
+        // point per row), whose error can exceed FP64's where a row's entries spread
+        // widely (2x2 pivots everywhere: a residual 19x LAPACK's at n = 600).  One
+        // step of refinement on the FP64 residual of the caller's A brings x back to
+        // FP64 accuracy.
+        const unsigned rb = (unsigned)qmlg::ceil_div(n, BK_RES_T);
+        bk_resid_lower_kernel<<<dim3(rb, rb), BK_RES_T, 0, s>>>(A, lda, n, x, b.rP);
+        bk_resid_upper_kernel<<<(unsigned)qmlg::ceil_div((int64_t)n * 32, 256), 256, 0, s>>>(A, lda, n, x, b.rU);
+        bk_resid_finish_kernel<<<(unsigned)qmlg::ceil_div(n, 256), 256, 0, s>>>(n, y, b.rP, b.rU, b.rr);
+        qmlg::count_launches(3);
+        if ((st = qmlg::check_launch()) != QMLG_OK) return st;
+        if ((st = dsytrs(b.rr)) != QMLG_OK) return st;
+        bk_axpy_kernel<<<(unsigned)qmlg::ceil_div(n, 256), 256, 0, s>>>(n, b.rr, x);
+        qmlg::count_launches(1);
+        if ((st = qmlg::check_launch()) != QMLG_OK) return st;
+        if ((st = qmlg::read_back(&info, b.info, sizeof(int), s)) != QMLG_OK) return st;
+    }
+    return info;
 }
 
 extern "C" size_t qmlg_bkf_invert_workspace_size(int n) { return bk_ws(n, 2 * std::max(n, 1)); }

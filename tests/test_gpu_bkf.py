@@ -127,3 +127,22 @@ def test_bkf_solve_above_the_shared_memory_ring(cuda, oracle):
     xo, info = oracle.bkf_solve(A, y)
     assert info == 0
     assert np.max(np.abs(A @ x - y)) <= 10 * np.max(np.abs(A @ xo - y))
+
+
+@pytest.mark.parametrize("n", [600])
+def test_bkf_blocked_with_2x2_pivots_everywhere(cuda, oracle, n):
+    # a zero diagonal makes almost every pivot 2x2, including the ones that end a
+    # panel one column late; solve and inverse held to LAPACK
+    rng = np.random.default_rng(n + 7)
+    B = rng.standard_normal((n, n))
+    A = B + B.T
+    np.fill_diagonal(A, 0.0)
+    y = rng.standard_normal(n)
+    x = bkf_solve(A.copy(), y.copy())
+    xo, info = oracle.bkf_solve(A, y)
+    assert info == 0
+    assert np.max(np.abs(A @ x - y)) <= 10 * np.max(np.abs(A @ xo - y))
+    Ai = bkf_invert(A.copy())
+    Ao, _ = oracle.bkf_invert(A)
+    eye = np.eye(n)
+    assert np.max(np.abs(A @ Ai - eye)) <= 10 * np.max(np.abs(A @ Ao - eye))
