@@ -523,7 +523,8 @@ int qmlg_cho_invert(const double *A, int n, int64_t lda, double *Ainv, int64_t l
  * info (> 0: D(info, info) is exactly zero, x is then unusable, where the reference
  * prints a warning).  Above n = 256 (outside stream capture) the factorisation is
  * dsytrf's blocked form (dlasyf panels) with the trailing updates as emulated-FP64
- * tensor-core products; the call waits on the stream once per 64-column panel.
+ * tensor-core products, and x is refined once on the FP64 residual y - A x; the
+ * call waits on the stream once per 64-column panel.
  */
 size_t qmlg_bkf_solve_workspace_size(int n);
 int qmlg_bkf_solve(const double *A, int n, int64_t lda, const double *y, double *x,
