@@ -67,7 +67,7 @@ def parse(argv=None):
     p.add_argument("--large-test", type=int, default=10000)
     p.add_argument("--no-extra", action="store_true",
                    help="skip the other kernel matrices and the atomic-CM / local-kernel / "
-                        "inverse measurements")
+                        "inverse / unsorted-CM / file measurements")
     return p.parse_args(argv)
 
 
@@ -314,7 +314,8 @@ def run_serving(a, dev):
 def run_extra(a, dev, batch, X, stream):
     """Paths beside the KRR hot path, each timed on the GPU (CUDA events) and, where
     the CPU side is cheap, on the host: the other training kernel matrices, atomic
-    Coulomb matrices, local kernels, the inverses and Bunch-Kaufman."""
+    Coulomb matrices, local kernels, the inverses and Bunch-Kaufman, the unsorted
+    Coulomb matrix, XYZ file ingestion and model files."""
     import numpy as np
     import torch
 
@@ -418,7 +419,117 @@ def run_extra(a, dev, batch, X, stream):
                                             "bkf_invert_gpu_s": tvi, "bkf_invert_lapack_s": cvi,
                                             "matrix": "B + B^T, B standard normal, seed 5000"},
                              "cpu_sample": "scipy LAPACK, full size, OpenBLAS threads"}
+    torch.cuda.empty_cache()
+
+    # the other global kernels (GPU times in train_kernel_matrix_s) beside the OpenMP
+    # oracle on a row sample of the same N x N matrix, scaled to all N rows
+    Xg = X[:ntr].cpu().numpy()
+    rows = 100
+    g2 = [1.0, 1.0 / 3.0]
+    samples = (("linear", lambda A: orc.linear_kernel(A, Xg)),
+               ("matern_l2_order2", lambda A: orc.matern_kernel_l2(A, Xg, a.sigma, 2)),
+               ("sargan_2gammas", lambda A: orc.sargan_kernel(A, Xg, a.sigma, g2)))
+    other = {"n": ntr, "cpu_sample": "%d of %d rows, OpenMP on %d cores, scaled"
+                                     % (rows, ntr, os.cpu_count())}
+    for key, fn in samples:
+        c0 = time.perf_counter()
+        fn(Xg[:rows])
+        other[key] = {"gpu_s": out["train_kernel_matrix_s"][key + "_fp64"],
+                      "cpu_oracle_s_scaled": (time.perf_counter() - c0) * ntr / rows}
+    out["other_global_kernels"] = other
+    del Xg
+
+    # unsorted Coulomb matrices of the whole batch; the oracle is called once per
+    # molecule, like the reference's per-molecule representation call
+    zb, rb, ob = molecules_to_device(batch)
+    t = gpu_time(lambda: core.coulomb_matrix_batch(zb, rb, ob, 23, "unsorted"), reps=3)
+    ns = 2000
+    c0 = time.perf_counter()
+    for m in range(ns):
+        orc.cm_unsorted(*batch.molecule(m), 23)
+    cpu = (time.perf_counter() - c0) * batch.n_mol / ns
+    out["unsorted_cm"] = {"molecules": batch.n_mol, "gpu_s": t, "cpu_oracle_s_scaled": cpu,
+                          "cpu_sample": "%d molecules, 1 thread, scaled" % ns}
+    del zb, rb, ob
+
+    out["files"] = run_files(a, dev, batch, X)
     return out
+
+
+def run_files(a, dev, batch, X):
+    """The callers on either side of the path: XYZ files parsed into one ragged batch,
+    copied to the device and turned into sorted Coulomb matrices; and a fitted model
+    written to and read back from its .npz file. Wall-clock seconds on the host."""
+    import shutil
+    import tempfile
+
+    import numpy as np
+    import torch
+
+    from qml_gb300 import core
+    from qml_gb300 import io as qio
+    from qml_gb300.krr import KRR
+    from qml_gb300.representations import NUCLEAR_CHARGE
+    symbol = {v: k for k, v in NUCLEAR_CHARGE.items()}
+    nx = 5000
+    tmp = tempfile.mkdtemp(prefix="qmlg_files_")
+    try:
+        paths = []
+        for m in range(nx):
+            z, r = batch.molecule(m)
+            p = os.path.join(tmp, "%05d.xyz" % m)
+            with open(p, "w") as f:
+                f.write("%d\nsynthetic molecule %d\n" % (z.shape[0], m))
+                for zi, ri in zip(z, r):
+                    f.write("%s %.10f %.10f %.10f\n" % (symbol[int(zi)], ri[0], ri[1], ri[2]))
+            paths.append(p)
+        # one read_xyz per file, as a reference user builds one Compound per file
+        c0 = time.perf_counter()
+        for p in paths:
+            qio.read_xyz(p)
+        t_files = time.perf_counter() - c0
+        c0 = time.perf_counter()
+        qio.read_xyz_batch(paths, workers=1)
+        t_serial = time.perf_counter() - c0
+        c0 = time.perf_counter()
+        parsed = qio.read_xyz_batch(paths)
+        t_pool = time.perf_counter() - c0
+        ref = batch.slice(0, nx)
+        same = (np.array_equal(parsed.charges, ref.charges)
+                and np.array_equal(parsed.offsets, ref.offsets)
+                and float(np.max(np.abs(parsed.coordinates - ref.coordinates))) < 1e-9)
+
+        def files_to_cm():
+            z, r, o = qio.xyz_to_device(paths, dev)
+            return core.coulomb_matrix_batch(z, r, o, 23)
+        files_to_cm()
+        torch.cuda.synchronize()
+        c0 = time.perf_counter()
+        files_to_cm()
+        torch.cuda.synchronize()
+        t_cm = time.perf_counter() - c0
+
+        model = KRR(kernel=a.kernel, sigma=a.sigma, lam=a.lam)
+        model.X = X[:a.ntrain]
+        model.alpha = torch.linspace(-1.0, 1.0, a.ntrain, dtype=torch.float64, device=dev)
+        mpath = os.path.join(tmp, "model.npz")
+        c0 = time.perf_counter()
+        qio.save_krr(mpath, model)
+        t_save = time.perf_counter() - c0
+        c0 = time.perf_counter()
+        back = qio.load_krr(mpath, dev)
+        torch.cuda.synchronize()
+        t_load = time.perf_counter() - c0
+        exact = bool(torch.equal(back.X, model.X) and torch.equal(back.alpha, model.alpha))
+        return {"xyz": {"files": nx, "read_xyz_per_file_s": t_files,
+                        "native_1_thread_s": t_serial, "native_all_threads_s": t_pool,
+                        "threads": os.cpu_count(),
+                        "files_to_device_cm_s": t_cm, "parsed_equal_to_source": bool(same)},
+                "model_file": {"n_train": a.ntrain, "bytes": os.path.getsize(mpath),
+                               "save_s": t_save, "load_to_device_s": t_load,
+                               "round_trip_exact": exact}}
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
 
 
 def run_batching(a, dev):

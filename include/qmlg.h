@@ -575,6 +575,41 @@ int qmlg_selftest_wait_timeout(void *workspace, size_t ws_bytes, void *stream);
  */
 int qmlg_epilogue_exp(const double *x, double *y, int n, void *stream);
 
+/* ---- files ------------------------------------------------------------ */
+
+/*
+ * Reads many files on host threads (the open/readlines of each
+ * qml/compound.py:296-326 Compound.read_xyz call).  HOST pointers; no stream.
+ * paths: nfiles NUL-terminated names.  With buf == NULL it sets sizes[f] to the
+ * size of file f (-1 when it is not a regular file that stat can see).  The caller
+ * then places the files (starts, nfiles+1) and calls again with buf: file f is read
+ * into buf[starts[f] .. starts[f+1]), and status[f] = 1 when it could not be read
+ * in full or its size no longer matches sizes[f] (0 otherwise).  nthreads <= 0:
+ * one per hardware thread.  Returns 0 or QMLG_E_ARG.
+ */
+int qmlg_read_files(const char *const *paths, int nfiles, int nthreads, int64_t *sizes,
+                    char *buf, const int64_t *starts, int *status);
+
+/*
+ * Parses many XYZ files on host threads (replaces the per-file
+ * qml/compound.py:296-326 Compound.read_xyz loop a caller runs over a dataset).
+ * HOST pointers; no stream.  File f is text[starts[f] .. starts[f+1]); each is read
+ * as read_xyz reads it: the atom count on line 1, a comment line, then one atom per
+ * line (symbol x y z) until the count, the end of the file or a line with fewer than
+ * four fields.  Outputs: offsets (nfiles+1) = the files' atom ranges in
+ * charges (capacity) and coordinates (capacity x 3, row-major); status[f] = 0 when
+ * file f was parsed, 1 when this parser does not accept it (non-ASCII bytes, an
+ * atom count that is not a plain decimal integer >= 0, an element outside the
+ * qml/data.py:23 table, a number strtod does not read in full).  The caller parses
+ * a flagged file the reference's way, which gives its result or its error.  At
+ * most (line breaks in text + nfiles) atoms exist, so that capacity always suffices.
+ * nthreads <= 0: one per hardware thread.  Returns 0, QMLG_E_ARG, or
+ * QMLG_E_TOO_LARGE when the atoms exceed capacity.
+ */
+int qmlg_parse_xyz(const char *text, const int64_t *starts, int nfiles, int nthreads,
+                   int64_t *offsets, int *status, double *charges, double *coordinates,
+                   int64_t capacity);
+
 #ifdef __cplusplus
 }
 #endif

@@ -143,6 +143,8 @@ SIGNATURES = {
                                     _P]),
     "qmlg_selftest_wait_timeout_workspace_size": (_SZ, []),
     "qmlg_selftest_wait_timeout": (_I, [_P, _SZ, _P]),
+    "qmlg_read_files": (_I, [_P, _I, _I, _P, _P, _P, _P]),
+    "qmlg_parse_xyz": (_I, [_P, _P, _I, _I, _P, _P, _P, _P, _I64]),
 }
 
 _lib = None

@@ -1,4 +1,4 @@
-"""Builds libqmlg.so (all CUDA sources, sm_103a) in-tree with nvcc.
+"""Builds libqmlg.so (all CUDA sources, sm_103a, and the host C++ ones) in-tree with nvcc.
 
 Each translation unit compiles in parallel, then one link step.  Output:
 ``qml_gb300/_build/libqmlg.so``.  The build is skipped when the library is newer
@@ -27,7 +27,8 @@ def _nvcc():
 
 
 def _sources():
-    return sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    # *.cpp files are host-only C++; nvcc hands them to the host compiler
+    return sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
 
 
 def _deps():

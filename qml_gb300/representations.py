@@ -14,9 +14,14 @@ import torch
 
 from . import core
 
-NUCLEAR_CHARGE = {"H": 1, "He": 2, "Li": 3, "Be": 4, "B": 5, "C": 6, "N": 7, "O": 8, "F": 9,
-                  "Ne": 10, "Na": 11, "Mg": 12, "Al": 13, "Si": 14, "P": 15, "S": 16, "Cl": 17,
-                  "Ar": 18, "K": 19, "Ca": 20, "Br": 35, "I": 53}
+# element symbol -> nuclear charge, the table of qml/data.py:23 (elements 1-112, then
+# the placeholder names Uuq = 114 and Uuh = 116)
+_SYMBOLS = ("H He Li Be B C N O F Ne Na Mg Al Si P S Cl Ar K Ca Sc Ti V Cr Mn Fe Co Ni Cu Zn "
+            "Ga Ge As Se Br Kr Rb Sr Y Zr Nb Mo Tc Ru Rh Pd Ag Cd In Sn Sb Te I Xe Cs Ba La Ce "
+            "Pr Nd Pm Sm Eu Gd Tb Dy Ho Er Tm Yb Lu Hf Ta W Re Os Ir Pt Au Hg Tl Pb Bi Po At Rn "
+            "Fr Ra Ac Th Pa U Np Pu Am Cm Bk Cf Es Fm Md No Lr Rf Db Sg Bh Hs Mt Ds Rg Cn")
+NUCLEAR_CHARGE = {s: z for z, s in enumerate(_SYMBOLS.split(), start=1)}
+NUCLEAR_CHARGE.update(Uuq=114, Uuh=116)
 
 
 def _device():
