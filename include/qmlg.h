@@ -213,6 +213,21 @@ int qmlg_gaussian_kernel_emulated(const double *A, int64_t lda, int na, const do
                                   size_t ws_bytes, void *stream);
 
 /*
+ * The linear kernel K = A B^T (qml/fkernels.f90:403-423) on the tensor cores: the
+ * Gaussian tile kernel with the dot product itself as the entry.  Every row is cut
+ * into eight 7-bit digit planes; the plane products are summed exactly in integers
+ * and scaled to K with one rounding.  |K - A B^T| <= 2^(eA + eB - 56) * kp * 9/4 for
+ * each entry, with 2^eA > max|a_j| and 2^eB > max|b_i| over the two rows and kp = d
+ * rounded up to 64.  Layouts, flags and diag_shift as qmlg_linear_kernel; input
+ * that is not finite takes qmlg_linear_kernel.
+ * ws: qmlg_linear_kernel_emulated_workspace_size(na, nb, d, flags).
+ */
+size_t qmlg_linear_kernel_emulated_workspace_size(int na, int nb, int d, int flags);
+int qmlg_linear_kernel_emulated(const double *A, int64_t lda, int na, const double *B,
+                                int64_t ldb, int nb, int d, double *K, int64_t ldk, int flags,
+                                double diag_shift, void *workspace, size_t ws_bytes, void *stream);
+
+/*
  * Laplacian kernel with the L1 distances summed exactly in 64-bit fixed point on
  * the integer pipes: features rounded once to multiples of 2^-F (F from max |x|
  * and d so that sums cannot overflow), |a - b| summed exactly, converted to FP64

@@ -208,7 +208,9 @@ def kernel_matrix(kind: str, A: torch.Tensor, B: torch.Tensor, sigma: float,
     order 0/1/2) or "sargan" (with gammas, a sequence or 1-D tensor).
     emulated=True takes the fast exact-within-1e-12 paths: the Gaussian contraction
     on the tensor cores (qmlg_gaussian_kernel_emulated), the Laplacian L1 sums in
-    fixed-point integers (qmlg_laplacian_kernel_fixed)."""
+    fixed-point integers (qmlg_laplacian_kernel_fixed), the linear kernel's dot
+    products on the tensor cores (qmlg_linear_kernel_emulated); Matern and Sargan
+    always take their FP64 kernels."""
     _require_cuda(A, B)
     A, lda = _rows(A)
     if symmetric:
@@ -233,6 +235,14 @@ def kernel_matrix(kind: str, A: torch.Tensor, B: torch.Tensor, sigma: float,
                                                   float(diag_shift), ws.data_ptr(), ws.numel(),
                                                   _stream(A.device)),
               "qmlg_gaussian_kernel_emulated")
+        return buf.T
+    if emulated and kind == "linear":
+        ws_bytes = lib().qmlg_linear_kernel_emulated_workspace_size(na, nb, d, flags)
+        ws = workspaces.get(ws_bytes, A.device)
+        check(lib().qmlg_linear_kernel_emulated(A.data_ptr(), lda, na, B.data_ptr(), ldb, nb, d,
+                                                buf.data_ptr(), na, flags, float(diag_shift),
+                                                ws.data_ptr(), ws.numel(), _stream(A.device)),
+              "qmlg_linear_kernel_emulated")
         return buf.T
     if emulated and kind == "laplacian":
         ws_bytes = lib().qmlg_laplacian_kernel_fixed_workspace_size(na, nb, d, flags)

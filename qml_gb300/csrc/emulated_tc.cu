@@ -50,7 +50,9 @@ constexpr int EPI_THREADS = 32 * EPI_WARPS;
 constexpr int EG = 4;           // columns per epilogue step
 constexpr int A_BYTES = TM * KC * 2;  // 16 KB
 
-enum Mode { kSyrk = 0, kKernelMatrix = 1, kPredict = 2 };
+// kLinear: the linear kernel matrix K = A B^T (the kKernelMatrix tiles, stores and
+// symmetric mirror with the dot product itself as the entry)
+enum Mode { kSyrk = 0, kKernelMatrix = 1, kPredict = 2, kLinear = 3 };
 
 // Tile shapes.  TN = 64 i-columns per level: 8 levels fill TMEM's 512 columns, one
 // accumulator, so the next tile's MMAs wait for the epilogue's level merge; each A
@@ -457,7 +459,7 @@ __device__ __forceinline__ void emu_tc_body(const CUtensorMap &mapA, const CUten
             const bool jvalid = j < pt.jend;
             const int ej = jvalid ? p.expA[arow + jl] : 0;
             double aj = 0.0, aw = 0.0;
-            if (MODE != kSyrk && jvalid) {
+            if (MODE != kSyrk && MODE != kLinear && jvalid) {
                 aj = pt.scale * p.normA[arow + jl];
                 if (MODE == kPredict) aw = p.alpha[j];
             }
@@ -592,16 +594,22 @@ __device__ __forceinline__ void emu_tc_body(const CUtensorMap &mapA, const CUten
                         const bool valid = jvalid && i < pt.iend;
                         double kv = 0.0;
                         if (valid) {
-                            // x = scale * (|a|^2 + |b|^2 - 2 a.b)
                             const int ew = eb + ej + shift - 7 * (S + 1);
-                            const int ef = m2s_exp + ew;
-                            const double w = (m2s_exp > 0 && ef > 0 && ef < 2047)
-                                                 ? __longlong_as_double(m2s_bits + ((long long)ew << 52))
-                                                 : m2s * pow2i(ew);
-                            kv = exp_nonpos(fma((double)v64[col], w, aj + sb));
-                            if (MODE == kKernelMatrix && p.lower && i == j) kv = 1.0 + p.diag_shift;
+                            if constexpr (MODE == kLinear) {
+                                // a.b = v 2^ew: one rounding, in the integer-to-double step
+                                kv = (double)v64[col] * pow2i(ew);
+                                if (p.lower && i == j) kv += p.diag_shift;
+                            } else {
+                                // x = scale * (|a|^2 + |b|^2 - 2 a.b)
+                                const int ef = m2s_exp + ew;
+                                const double w = (m2s_exp > 0 && ef > 0 && ef < 2047)
+                                                     ? __longlong_as_double(m2s_bits + ((long long)ew << 52))
+                                                     : m2s * pow2i(ew);
+                                kv = exp_nonpos(fma((double)v64[col], w, aj + sb));
+                                if (MODE == kKernelMatrix && p.lower && i == j) kv = 1.0 + p.diag_shift;
+                            }
                         }
-                        if (MODE == kKernelMatrix) {
+                        if (MODE == kKernelMatrix || MODE == kLinear) {
                             if (valid && (!p.lower || j <= i)) {
                                 pt.C[(int64_t)i * pt.ldc + j] = kv;
                                 if (p.lower && j < i) pt.C[(int64_t)j * pt.ldc + i] = kv;
@@ -908,6 +916,8 @@ void set_smem_attrs()
                              SMEM_BYTES);
         cudaFuncSetAttribute(emu_tc_kernel<kKernelMatrix>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+        cudaFuncSetAttribute(emu_tc_kernel<kLinear>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
         cudaFuncSetAttribute(emu_tc_kernel<kPredict>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
     });
@@ -1100,7 +1110,8 @@ int launch_gauss(int mode, const GaussBufs &b, int na, int nb, int d, int S, dou
     const int kp = feature_pad(d), rpa = rows_pad(na), rpb = rows_pad(nb);
     CUtensorMap mA, mB;
     int st = make_plane_map(&mA, b.dA, kp, rpa, S, TM);
-    const int TNm = mode == kKernelMatrix ? Shape<kKernelMatrix>::TN : Shape<kPredict>::TN;
+    const int TNm = mode == kPredict ? Shape<kPredict>::TN : Shape<kKernelMatrix>::TN;
+    static_assert(Shape<kLinear>::TN == Shape<kKernelMatrix>::TN, "linear tiles");
     if (st == QMLG_OK) st = make_plane_map(&mB, b.dB, kp, rpb, S, TNm);
     if (st != QMLG_OK) return st;
     set_smem_attrs();
@@ -1127,6 +1138,8 @@ int launch_gauss(int mode, const GaussBufs &b, int na, int nb, int d, int S, dou
     const int grid = tile_grid(a.ntiles);
     if (mode == kKernelMatrix)
         emu_tc_kernel<kKernelMatrix><<<grid, THREADS, SMEM_BYTES, s>>>(mA, mB, a);
+    else if (mode == kLinear)
+        emu_tc_kernel<kLinear><<<grid, THREADS, SMEM_BYTES, s>>>(mA, mB, a);
     else
         emu_tc_kernel<kPredict><<<grid, THREADS, SMEM_BYTES, s>>>(mA, mB, a);
     qmlg::count_launches(1);
@@ -1175,6 +1188,51 @@ extern "C" int qmlg_gaussian_kernel_emulated(const double *A, int64_t lda, int n
         return qmlg_gaussian_kernel(A, lda, na, B, ldb, nb, d, sigma, K, ldk, flags, diag_shift,
                                     stream);
     return launch_gauss(kKernelMatrix, b, na, nb, d, S, sigma, K, ldk, sym, diag_shift, nullptr,
+                        nullptr, s);
+}
+
+extern "C" size_t qmlg_linear_kernel_emulated_workspace_size(int na, int nb, int d, int flags)
+{
+    return qmlg_gaussian_kernel_emulated_workspace_size(na, nb, d, flags);
+}
+
+// The linear kernel on the Gaussian tiles: every row sliced into S_MAX digit planes
+// (the most the tiles hold), the merged integer dot product scaled to K once.
+// |K - A B^T| <= 2^(eA + eB - 56) * kp * 9/4 entry by entry, 2^eA > max|a_j|,
+// 2^eB > max|b_i| of the two rows.  Non-finite input takes the FP64 kernel.
+extern "C" int qmlg_linear_kernel_emulated(const double *A, int64_t lda, int na, const double *B,
+                                           int64_t ldb, int nb, int d, double *K, int64_t ldk,
+                                           int flags, double diag_shift, void *workspace,
+                                           size_t ws_bytes, void *stream)
+{
+    const bool sym = (flags & QMLG_KERNEL_SYMMETRIC) != 0;
+    if (na < 0 || nb < 0 || d < 0) return QMLG_E_ARG;
+    if ((na > 0 && (A == nullptr || lda < d)) || (nb > 0 && (B == nullptr || ldb < d)))
+        return QMLG_E_ARG;
+    if (K == nullptr || ldk < na) return QMLG_E_ARG;
+    if (sym && (na != nb || A != B || lda != ldb)) return QMLG_E_ARG;
+    if (na == 0 || nb == 0) return QMLG_OK;
+    if (ws_bytes < qmlg_linear_kernel_emulated_workspace_size(na, nb, d, flags))
+        return QMLG_E_WORKSPACE;
+    cudaStream_t s = qmlg::as_stream(stream);
+    qmlg::Workspace ws(workspace, ws_bytes);
+    GaussBufs b;
+    if (!take_gauss(ws, na, nb, d, sym, false, b)) return QMLG_E_WORKSPACE;
+    double ma = 0.0, mb = 0.0;
+    int st = read_max(A, lda, na, d, b.maxbuf, ma, s);
+    if (st == QMLG_OK && !sym) st = read_max(B, ldb, nb, d, b.maxbuf, mb, s);
+    if (st != QMLG_OK) return st;
+    if (sym) mb = ma;
+    if (!std::isfinite(ma) || !std::isfinite(mb))
+        return qmlg_linear_kernel(A, lda, na, B, ldb, nb, d, K, ldk, flags, diag_shift, stream);
+    const int kp = feature_pad(d), rpa = rows_pad(na), rpb = rows_pad(nb);
+    cudaError_t e = cudaMemsetAsync(b.err, 0, sizeof(int), s);
+    if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+    st = qmlg::slice_rows(A, lda, 0, na, 0, d, kp, rpa, S_MAX, b.dA, b.eA, nullptr, s, b.nA);
+    if (st == QMLG_OK && !sym)
+        st = qmlg::slice_rows(B, ldb, 0, nb, 0, d, kp, rpb, S_MAX, b.dB, b.eB, nullptr, s, b.nB);
+    if (st != QMLG_OK) return st;
+    return launch_gauss(kLinear, b, na, nb, d, S_MAX, 1.0, K, ldk, sym, diag_shift, nullptr,
                         nullptr, s);
 }
 

@@ -358,3 +358,55 @@ def test_laplacian_async_entries_match_synchronous(cuda, cm_features, sigma):
     torch.cuda.synchronize()
     assert torch.equal(y, yref)
     assert int(flag.item()) == want_flag
+
+
+def linear_emulated_tolerance(A, B):
+    # the documented bound, |K - A B^T| <= 2^(eA + eB - 56) kp 9/4 with 2^eA > max|a_j|
+    # and 2^eB > max|b_i| of the two rows, plus the oracle's own FP64 rounding
+    kp = -(-A.shape[1] // 64) * 64
+    ea = np.frexp(np.max(np.abs(A), axis=1))[1]
+    eb = np.frexp(np.max(np.abs(B), axis=1))[1]
+    bound = np.ldexp(1.0, ea[:, None] + eb[None, :] - 56) * kp * 9 / 4
+    return bound + A.shape[1] * 2.0 ** -53 * (np.abs(A) @ np.abs(B).T)
+
+
+@pytest.mark.parametrize("na,nb", [(1, 1), (63, 65), (130, 77), (300, 173)])
+def test_linear_kernel_emulated(cuda, oracle, cm_features, na, nb):
+    # the tensor-core linear kernel against the oracle, entry by entry within its
+    # bound, on CM features and on rows whose scales span twelve decades
+    rng = np.random.default_rng(na * 1000 + nb)
+    scaled = rng.standard_normal((na + nb, 45)) * 10.0 ** rng.uniform(-6, 6, (na + nb, 1))
+    for A, B in ((cm_features[:na], cm_features[300:300 + nb]), (scaled[:na], scaled[na:])):
+        At, Bt = torch.from_numpy(A).to(cuda), torch.from_numpy(B).to(cuda)
+        K = core.kernel_matrix("linear", At, Bt, 1.0, emulated=True).cpu().numpy()
+        Ko = oracle.linear_kernel(A, B)
+        assert np.all(np.abs(K - Ko) <= linear_emulated_tolerance(A, B))
+        Ks = core.kernel_matrix("linear", At, At, 1.0, symmetric=True, diag_shift=0.5,
+                                emulated=True).cpu().numpy()
+        Kso = oracle.linear_kernel(A, A) + 0.5 * np.eye(na)
+        assert np.array_equal(Ks, Ks.T)
+        assert np.all(np.abs(Ks - Kso) <= linear_emulated_tolerance(A, A) + 2.0 ** -53)
+    # CM features: within 1e-12 of the largest entry
+    A, B = cm_features[:na], cm_features[300:300 + nb]
+    K = core.kernel_matrix("linear", torch.from_numpy(A).to(cuda), torch.from_numpy(B).to(cuda),
+                           1.0, emulated=True).cpu().numpy()
+    Ko = oracle.linear_kernel(A, B)
+    assert np.max(np.abs(K - Ko)) <= 1e-12 * np.max(np.abs(Ko))
+
+
+def test_linear_kernel_emulated_non_finite_and_reference(cuda, oracle):
+    # input that is not finite goes to the FP64 kernel (the same NaN/inf pattern);
+    # the reference test's inputs give its expectations
+    g = load_golden("kernels_more_seed666.npz")
+    X, Xs = more_kernel_inputs()["linear"]
+    Xt, Xst = torch.from_numpy(X).to(cuda), torch.from_numpy(Xs).to(cuda)
+    K = core.kernel_matrix("linear", Xt, Xst, 1.0, emulated=True).cpu().numpy()
+    assert np.allclose(K, g["linear"])
+    assert np.all(np.abs(K - oracle.linear_kernel(X, Xs)) <= linear_emulated_tolerance(X, Xs))
+    Xbad = X.copy()
+    Xbad[3, 2] = np.inf
+    Xbad[5, 0] = np.nan
+    Xb = torch.from_numpy(Xbad).to(cuda)
+    Ke = core.kernel_matrix("linear", Xb, Xst, 1.0, emulated=True).cpu().numpy()
+    Kf = core.kernel_matrix("linear", Xb, Xst, 1.0).cpu().numpy()
+    assert np.array_equal(Ke, Kf, equal_nan=True)
