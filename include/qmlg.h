@@ -213,6 +213,21 @@ int qmlg_gaussian_kernel_emulated(const double *A, int64_t lda, int na, const do
                                   size_t ws_bytes, void *stream);
 
 /*
+ * The Matern L2 kernel (qml/fkernels.f90:426-484) of order 1 or 2 on the tensor
+ * cores: the Gaussian tile kernel's d^2 = |a|^2 + |b|^2 - 2 a.b with the Matern
+ * epilogue.  Both orders are flat at d = 0, so |K - K_exact| / K stays below
+ * 0.25e-12 whenever the digit bound allows (the same test as the Gaussian's, with
+ * three times the margin); otherwise, for order 0 and for input that is not
+ * finite, qmlg_matern_kernel_l2 runs.  Arguments as qmlg_matern_kernel_l2.
+ * ws: qmlg_matern_kernel_l2_emulated_workspace_size(na, nb, d, flags).
+ */
+size_t qmlg_matern_kernel_l2_emulated_workspace_size(int na, int nb, int d, int flags);
+int qmlg_matern_kernel_l2_emulated(const double *A, int64_t lda, int na, const double *B,
+                                   int64_t ldb, int nb, int d, double sigma, int order, double *K,
+                                   int64_t ldk, int flags, double diag_shift, void *workspace,
+                                   size_t ws_bytes, void *stream);
+
+/*
  * The linear kernel K = A B^T (qml/fkernels.f90:403-423) on the tensor cores: the
  * Gaussian tile kernel with the dot product itself as the entry.  Every row is cut
  * into eight 7-bit digit planes; the plane products are summed exactly in integers

@@ -209,8 +209,9 @@ def kernel_matrix(kind: str, A: torch.Tensor, B: torch.Tensor, sigma: float,
     emulated=True takes the fast exact-within-1e-12 paths: the Gaussian contraction
     on the tensor cores (qmlg_gaussian_kernel_emulated), the Laplacian L1 sums in
     fixed-point integers (qmlg_laplacian_kernel_fixed), the linear kernel's dot
-    products on the tensor cores (qmlg_linear_kernel_emulated); Matern and Sargan
-    always take their FP64 kernels."""
+    products and the Matern L2 orders 1 and 2 on the tensor cores
+    (qmlg_linear_kernel_emulated, qmlg_matern_kernel_l2_emulated); Matern order 0
+    and Sargan take their FP64 kernels."""
     _require_cuda(A, B)
     A, lda = _rows(A)
     if symmetric:
@@ -243,6 +244,15 @@ def kernel_matrix(kind: str, A: torch.Tensor, B: torch.Tensor, sigma: float,
                                                 buf.data_ptr(), na, flags, float(diag_shift),
                                                 ws.data_ptr(), ws.numel(), _stream(A.device)),
               "qmlg_linear_kernel_emulated")
+        return buf.T
+    if emulated and kind == "matern_l2":
+        ws_bytes = lib().qmlg_matern_kernel_l2_emulated_workspace_size(na, nb, d, flags)
+        ws = workspaces.get(ws_bytes, A.device)
+        check(lib().qmlg_matern_kernel_l2_emulated(A.data_ptr(), lda, na, B.data_ptr(), ldb, nb,
+                                                   d, float(sigma), int(order), buf.data_ptr(), na,
+                                                   flags, float(diag_shift), ws.data_ptr(),
+                                                   ws.numel(), _stream(A.device)),
+              "qmlg_matern_kernel_l2_emulated")
         return buf.T
     if emulated and kind == "laplacian":
         ws_bytes = lib().qmlg_laplacian_kernel_fixed_workspace_size(na, nb, d, flags)

@@ -51,8 +51,9 @@ constexpr int EG = 4;           // columns per epilogue step
 constexpr int A_BYTES = TM * KC * 2;  // 16 KB
 
 // kLinear: the linear kernel matrix K = A B^T (the kKernelMatrix tiles, stores and
-// symmetric mirror with the dot product itself as the entry)
-enum Mode { kSyrk = 0, kKernelMatrix = 1, kPredict = 2, kLinear = 3 };
+// symmetric mirror with the dot product itself as the entry).  kMatern: the Matern
+// L2 kernel of order 1 or 2 on the same tiles, from d^2 = |a|^2 + |b|^2 - 2 a.b.
+enum Mode { kSyrk = 0, kKernelMatrix = 1, kPredict = 2, kLinear = 3, kMatern = 4 };
 
 // Tile shapes.  TN = 64 i-columns per level: 8 levels fill TMEM's 512 columns, one
 // accumulator, so the next tile's MMAs wait for the epilogue's level merge; each A
@@ -96,8 +97,10 @@ struct TileArgs {
     // Gaussian epilogues
     const double *normA;  // |x|^2 per digit row
     const double *normB;
-    double scale;         // -0.5 / sigma^2
+    double scale;         // -0.5 / sigma^2 (kMatern: 1, the FMA then gives d^2)
     double diag_shift;
+    int order;            // kMatern: 1 or 2
+    double s1, s2;        // kMatern: -sqrt(2 order + 1) / sigma, 5 / (3 sigma^2)
     const double *alpha;  // kPredict: weights of the j rows
     double *partial;      // kPredict: [tiles along j][iend - ibase] partial sums
 };
@@ -605,11 +608,21 @@ __device__ __forceinline__ void emu_tc_body(const CUtensorMap &mapA, const CUten
                                 const double w = (m2s_exp > 0 && ef > 0 && ef < 2047)
                                                      ? __longlong_as_double(m2s_bits + ((long long)ew << 52))
                                                      : m2s * pow2i(ew);
-                                kv = exp_nonpos(fma((double)v64[col], w, aj + sb));
-                                if (MODE == kKernelMatrix && p.lower && i == j) kv = 1.0 + p.diag_shift;
+                                const double x = fma((double)v64[col], w, aj + sb);
+                                if constexpr (MODE == kMatern) {
+                                    // d^2 rounds below 0 only for (near) equal rows
+                                    const double d2 = fmax(x, 0.0), dd = sqrt(d2);
+                                    double poly = 1.0 - p.s1 * dd;
+                                    if (p.order == 2) poly += p.s2 * d2;
+                                    kv = exp_nonpos(p.s1 * dd) * poly;
+                                } else {
+                                    kv = exp_nonpos(x);
+                                }
+                                if ((MODE == kKernelMatrix || MODE == kMatern) && p.lower && i == j)
+                                    kv = 1.0 + p.diag_shift;
                             }
                         }
-                        if (MODE == kKernelMatrix || MODE == kLinear) {
+                        if (MODE == kKernelMatrix || MODE == kLinear || MODE == kMatern) {
                             if (valid && (!p.lower || j <= i)) {
                                 pt.C[(int64_t)i * pt.ldc + j] = kv;
                                 if (p.lower && j < i) pt.C[(int64_t)j * pt.ldc + i] = kv;
@@ -918,6 +931,8 @@ void set_smem_attrs()
                              cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
         cudaFuncSetAttribute(emu_tc_kernel<kLinear>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+        cudaFuncSetAttribute(emu_tc_kernel<kMatern>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
         cudaFuncSetAttribute(emu_tc_kernel<kPredict>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
     });
@@ -931,7 +946,7 @@ int rows_pad(int n) { return (int)qmlg::ceil_div(n < 1 ? 1 : n, TM) * TM; }
 // 0.5e-12: |dot error| <= 2^(eA + eB - 7S) * kp * (S + 1) / 4 (truncated digit
 // levels plus the rounding of the fixed-point values), and the relative error of
 // K = exp(-d^2 / (2 sigma^2)) is that error / sigma^2.  0 if no S <= 8 reaches it.
-int choose_slices(double maxA, double maxB, int kp, double sigma)
+int choose_slices(double maxA, double maxB, int kp, double sigma, double gain = 1.0)
 {
     int ea = 0, eb = 0;
     if (maxA > 0.0) std::frexp(maxA, &ea);
@@ -940,7 +955,7 @@ int choose_slices(double maxA, double maxB, int kp, double sigma)
     eb += 1;
     for (int S = 4; S <= S_MAX; ++S) {
         const double bound = std::ldexp(1.0, ea + eb - 7 * S) * kp * (S + 1) / 4.0;
-        if (bound / (sigma * sigma) <= 0.5e-12) return S;
+        if (gain * bound / (sigma * sigma) <= 0.5e-12) return S;
     }
     return 0;
 }
@@ -1081,7 +1096,8 @@ bool take_gauss(qmlg::Workspace &ws, int na, int nb, int d, bool share_b, bool p
 
 // Slices A (and B), picks S; returns S, 0 when the bound cannot be met.
 int prepare_gauss(const double *A, int64_t lda, int na, const double *B, int64_t ldb, int nb,
-                  int d, double sigma, bool share_b, GaussBufs &b, int &S, cudaStream_t s)
+                  int d, double sigma, bool share_b, GaussBufs &b, int &S, cudaStream_t s,
+                  double gain = 1.0)
 {
     const int kp = feature_pad(d), rpa = rows_pad(na), rpb = rows_pad(nb);
     double ma = 0.0, mb = 0.0;
@@ -1093,7 +1109,7 @@ int prepare_gauss(const double *A, int64_t lda, int na, const double *B, int64_t
         S = 0;
         return QMLG_OK;
     }
-    S = choose_slices(ma, mb, kp, sigma);
+    S = choose_slices(ma, mb, kp, sigma, gain);
     if (S == 0) return QMLG_OK;
     cudaError_t e = cudaMemsetAsync(b.err, 0, sizeof(int), s);
     if (e != cudaSuccess) return qmlg::set_cuda_error(e);
@@ -1105,13 +1121,14 @@ int prepare_gauss(const double *A, int64_t lda, int na, const double *B, int64_t
 
 int launch_gauss(int mode, const GaussBufs &b, int na, int nb, int d, int S, double sigma,
                  double *K, int64_t ldk, bool sym, double diag_shift, const double *alpha,
-                 double *yhat, cudaStream_t s)
+                 double *yhat, cudaStream_t s, int order = 0)
 {
     const int kp = feature_pad(d), rpa = rows_pad(na), rpb = rows_pad(nb);
     CUtensorMap mA, mB;
     int st = make_plane_map(&mA, b.dA, kp, rpa, S, TM);
     const int TNm = mode == kPredict ? Shape<kPredict>::TN : Shape<kKernelMatrix>::TN;
-    static_assert(Shape<kLinear>::TN == Shape<kKernelMatrix>::TN, "linear tiles");
+    static_assert(Shape<kLinear>::TN == Shape<kKernelMatrix>::TN &&
+                      Shape<kMatern>::TN == Shape<kKernelMatrix>::TN, "kernel-matrix tiles");
     if (st == QMLG_OK) st = make_plane_map(&mB, b.dB, kp, rpb, S, TNm);
     if (st != QMLG_OK) return st;
     set_smem_attrs();
@@ -1135,11 +1152,19 @@ int launch_gauss(int mode, const GaussBufs &b, int na, int nb, int d, int S, dou
     a.diag_shift = diag_shift;
     a.alpha = alpha;
     a.partial = b.partial;
+    if (mode == kMatern) {
+        a.scale = 1.0;
+        a.order = order;
+        a.s1 = -std::sqrt(2.0 * order + 1.0) / sigma;
+        a.s2 = 5.0 / (3.0 * sigma * sigma);
+    }
     const int grid = tile_grid(a.ntiles);
     if (mode == kKernelMatrix)
         emu_tc_kernel<kKernelMatrix><<<grid, THREADS, SMEM_BYTES, s>>>(mA, mB, a);
     else if (mode == kLinear)
         emu_tc_kernel<kLinear><<<grid, THREADS, SMEM_BYTES, s>>>(mA, mB, a);
+    else if (mode == kMatern)
+        emu_tc_kernel<kMatern><<<grid, THREADS, SMEM_BYTES, s>>>(mA, mB, a);
     else
         emu_tc_kernel<kPredict><<<grid, THREADS, SMEM_BYTES, s>>>(mA, mB, a);
     qmlg::count_launches(1);
@@ -1234,6 +1259,48 @@ extern "C" int qmlg_linear_kernel_emulated(const double *A, int64_t lda, int na,
     if (st != QMLG_OK) return st;
     return launch_gauss(kLinear, b, na, nb, d, S_MAX, 1.0, K, ldk, sym, diag_shift, nullptr,
                         nullptr, s);
+}
+
+extern "C" size_t qmlg_matern_kernel_l2_emulated_workspace_size(int na, int nb, int d, int flags)
+{
+    return qmlg_gaussian_kernel_emulated_workspace_size(na, nb, d, flags);
+}
+
+// Matern orders 1 and 2 on the Gaussian tiles.  Both are flat at d = 0, so the error
+// of d^2 passes into K like the Gaussian's: |dK|/K <= 1.5 |d(d^2)| / sigma^2 (order
+// 1; 5/6 for order 2).  The digit count is chosen with three times the Gaussian's
+// margin on |d(d^2)| / sigma^2, which keeps |dK|/K below 0.25e-12; where no count
+// meets it, and for order 0 (whose slope at d = 0 is not 0), the FP64 kernel runs.
+extern "C" int qmlg_matern_kernel_l2_emulated(const double *A, int64_t lda, int na, const double *B,
+                                              int64_t ldb, int nb, int d, double sigma, int order,
+                                              double *K, int64_t ldk, int flags, double diag_shift,
+                                              void *workspace, size_t ws_bytes, void *stream)
+{
+    const bool sym = (flags & QMLG_KERNEL_SYMMETRIC) != 0;
+    if (na < 0 || nb < 0 || d < 0 || !(sigma > 0.0) || !std::isfinite(sigma)) return QMLG_E_ARG;
+    if (order < 0 || order > 2) return QMLG_E_ARG;
+    if ((na > 0 && (A == nullptr || lda < d)) || (nb > 0 && (B == nullptr || ldb < d)))
+        return QMLG_E_ARG;
+    if (K == nullptr || ldk < na) return QMLG_E_ARG;
+    if (sym && (na != nb || A != B || lda != ldb)) return QMLG_E_ARG;
+    if (na == 0 || nb == 0) return QMLG_OK;
+    if (order == 0)
+        return qmlg_matern_kernel_l2(A, lda, na, B, ldb, nb, d, sigma, order, K, ldk, flags,
+                                     diag_shift, stream);
+    if (ws_bytes < qmlg_matern_kernel_l2_emulated_workspace_size(na, nb, d, flags))
+        return QMLG_E_WORKSPACE;
+    cudaStream_t s = qmlg::as_stream(stream);
+    qmlg::Workspace ws(workspace, ws_bytes);
+    GaussBufs b;
+    if (!take_gauss(ws, na, nb, d, sym, false, b)) return QMLG_E_WORKSPACE;
+    int S = 0;
+    int st = prepare_gauss(A, lda, na, B, ldb, nb, d, sigma, sym, b, S, s, 3.0);
+    if (st != QMLG_OK) return st;
+    if (S == 0)
+        return qmlg_matern_kernel_l2(A, lda, na, B, ldb, nb, d, sigma, order, K, ldk, flags,
+                                     diag_shift, stream);
+    return launch_gauss(kMatern, b, na, nb, d, S, sigma, K, ldk, sym, diag_shift, nullptr, nullptr,
+                        s, order);
 }
 
 extern "C" size_t qmlg_predict_emulated_workspace_size(int ntrain, int ntest, int d)

@@ -410,3 +410,36 @@ def test_linear_kernel_emulated_non_finite_and_reference(cuda, oracle):
     Ke = core.kernel_matrix("linear", Xb, Xst, 1.0, emulated=True).cpu().numpy()
     Kf = core.kernel_matrix("linear", Xb, Xst, 1.0).cpu().numpy()
     assert np.array_equal(Ke, Kf, equal_nan=True)
+
+
+@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("na,nb", [(1, 1), (63, 65), (300, 173)])
+def test_matern_kernel_emulated(cuda, oracle, cm_features, order, na, nb):
+    # Matern L2 orders 1 and 2 on the tensor cores: within 1e-12 relative per entry,
+    # exactly symmetric, the shifted diagonal, and rows a hair apart (d near 0)
+    A, B = cm_features[:na], cm_features[300:300 + nb]
+    near = A + np.random.default_rng(na).standard_normal(A.shape) * 1e-7
+    At, Bt, Nt = (torch.from_numpy(x).to(cuda) for x in (A, B, near))
+    for sigma in (1000.0, 250.0):
+        K = core.kernel_matrix("matern_l2", At, Bt, sigma, order=order, emulated=True)
+        assert relerr(K.cpu().numpy(), oracle.matern_kernel_l2(A, B, sigma, order)) <= RTOL
+        Kn = core.kernel_matrix("matern_l2", At, Nt, sigma, order=order, emulated=True)
+        assert relerr(Kn.cpu().numpy(), oracle.matern_kernel_l2(A, near, sigma, order)) <= RTOL
+        Ks = core.kernel_matrix("matern_l2", At, At, sigma, order=order, symmetric=True,
+                                diag_shift=0.5, emulated=True).cpu().numpy()
+        assert np.array_equal(Ks, Ks.T)
+        assert relerr(Ks, oracle.matern_kernel_l2(A, A, sigma, order) + 0.5 * np.eye(na)) <= RTOL
+
+
+def test_matern_kernel_emulated_falls_back(cuda, cm_features):
+    # order 0, a sigma too small for the digit bound, and non-finite input take the
+    # FP64 kernel: the same bits as emulated=False
+    A = cm_features[:70].copy()
+    At = torch.from_numpy(A).to(cuda)
+    bad = A.copy()
+    bad[4, 7] = np.nan
+    Bt = torch.from_numpy(bad).to(cuda)
+    for X, Y, sigma, order in ((At, At, 1000.0, 0), (At, At, 1.0, 2), (At, Bt, 1000.0, 1)):
+        Ke = core.kernel_matrix("matern_l2", X, Y, sigma, order=order, emulated=True)
+        Kf = core.kernel_matrix("matern_l2", X, Y, sigma, order=order)
+        assert np.array_equal(Ke.cpu().numpy(), Kf.cpu().numpy(), equal_nan=True)
