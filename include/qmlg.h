@@ -196,6 +196,25 @@ int qmlg_local_kernels(int kind, const double *A, int64_t lda, const int64_t *of
                        const double *sigmas, int nsigmas, double *K, int flags, void *stream);
 
 /*
+ * The same local kernels from atom-pair kernel matrices: for each sigma and each
+ * chunk of A's molecules (about 2 GiB of atom pairs), qmlg_gaussian_kernel_emulated
+ * (tensor cores) or qmlg_laplacian_kernel_fixed (fixed-point L1 sums) gives the
+ * chunk's atoms against all of B's, then two reductions sum them per molecule pair.
+ * Every term is positive, so each entry keeps the atom-pair kernel's relative bound
+ * (1e-12; those calls take their FP64 kernels where the bound cannot be met).
+ * Arguments as qmlg_local_kernels.  Reads the offsets and sigmas back to the host
+ * first (a synchronisation).  QMLG_E_TOO_LARGE when one molecule holds more atoms
+ * than a chunk's rows.  ws: qmlg_local_kernels_emulated_workspace_size(kind,
+ * atoms of A, atoms of B, nm2, d).
+ */
+size_t qmlg_local_kernels_emulated_workspace_size(int kind, int64_t natoms_a, int64_t natoms_b,
+                                                  int nm2, int d);
+int qmlg_local_kernels_emulated(int kind, const double *A, int64_t lda, const int64_t *offsets_a,
+                                int nm1, const double *B, int64_t ldb, const int64_t *offsets_b,
+                                int nm2, int d, const double *sigmas, int nsigmas, double *K,
+                                int flags, void *workspace, size_t ws_bytes, void *stream);
+
+/*
  * Gaussian kernel with the contraction a.b emulated to FP64 accuracy on the bf16
  * tensor cores (tcgen05): rows are scaled by powers of two and cut into base-128
  * digit planes; the digit products are summed exactly in tensor memory and

@@ -91,6 +91,9 @@ SIGNATURES = {
     "qmlg_atomic_coulomb_matrix": (_I, [_P, _P, _P, _I, _P, _P, _I, _I, _I, _D, _D, _D, _D, _P, _P,
                                         _P]),
     "qmlg_local_kernels": (_I, [_I, _P, _I64, _P, _I, _P, _I64, _P, _I, _I, _P, _I, _P, _I, _P]),
+    "qmlg_local_kernels_emulated_workspace_size": (_SZ, [_I, _I64, _I64, _I, _I]),
+    "qmlg_local_kernels_emulated": (_I, [_I, _P, _I64, _P, _I, _P, _I64, _P, _I, _I, _P, _I, _P,
+                                         _I, _P, _SZ, _P]),
     "qmlg_cho_invert_workspace_size": (_SZ, [_I, _I]),
     "qmlg_cho_invert": (_I, [_P, _I, _I64, _P, _I64, _I, _P, _SZ, _P]),
     "qmlg_bkf_solve_workspace_size": (_SZ, [_I]),

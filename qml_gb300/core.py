@@ -141,9 +141,12 @@ def atomic_coulomb_matrix_batch(charges: torch.Tensor, coordinates: torch.Tensor
 
 
 def local_kernels(kind: str, A: torch.Tensor, B: torch.Tensor, offsets_a: torch.Tensor,
-                  offsets_b: torch.Tensor, sigmas, symmetric: bool = False) -> torch.Tensor:
+                  offsets_b: torch.Tensor, sigmas, symmetric: bool = False,
+                  emulated: bool = False) -> torch.Tensor:
     """Local kernels (nsigmas, nm1, nm2) float64 on the GPU (a Fortran-ordered view)
-    for atom rows A, B grouped by molecule offsets.  kind "gaussian" or "laplacian"."""
+    for atom rows A, B grouped by molecule offsets.  kind "gaussian" or "laplacian".
+    emulated=True sums atom-pair kernel matrices from the tensor-core Gaussian or the
+    fixed-point Laplacian (qmlg_local_kernels_emulated, within 1e-12 per entry)."""
     if kind not in ("gaussian", "laplacian"):
         raise ValueError("unknown local kernel %r" % (kind,))
     _require_cuda(A, B)
@@ -159,6 +162,19 @@ def local_kernels(kind: str, A: torch.Tensor, B: torch.Tensor, offsets_a: torch.
     sg = torch.as_tensor(sigmas, dtype=torch.float64).reshape(-1).to(A.device).contiguous()
     nm1, nm2, ns = offsets_a.shape[0] - 1, offsets_b.shape[0] - 1, sg.shape[0]
     buf = torch.zeros((nm2, nm1, ns), dtype=torch.float64, device=A.device)
+    if emulated:
+        kc = 0 if kind == "gaussian" else 1
+        # the atom counts the library sizes its chunks by (it reads the offsets too)
+        nat_a, nat_b = int(offsets_a[-1]), int(offsets_b[-1])
+        ws = workspaces.get(lib().qmlg_local_kernels_emulated_workspace_size(kc, nat_a, nat_b, nm2,
+                                                                             A.shape[1]), A.device)
+        check(lib().qmlg_local_kernels_emulated(kc, A.data_ptr(), lda, offsets_a.data_ptr(), nm1,
+                                                B.data_ptr(), ldb, offsets_b.data_ptr(), nm2,
+                                                A.shape[1], sg.data_ptr(), ns, buf.data_ptr(),
+                                                _lib.QMLG_KERNEL_SYMMETRIC if symmetric else 0,
+                                                ws.data_ptr(), ws.numel(), _stream(A.device)),
+              "qmlg_local_kernels_emulated")
+        return buf.permute(2, 1, 0)
     check(lib().qmlg_local_kernels(0 if kind == "gaussian" else 1, A.data_ptr(), lda,
                                    offsets_a.data_ptr(), nm1, B.data_ptr(), ldb,
                                    offsets_b.data_ptr(), nm2, A.shape[1], sg.data_ptr(), ns,

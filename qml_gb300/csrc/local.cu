@@ -13,6 +13,7 @@
 // same atoms on both sides) computes b >= a and writes the mirror as well, so K is
 // exactly symmetric.
 #include <cmath>
+#include <vector>
 
 #include "common.cuh"
 
@@ -125,4 +126,182 @@ extern "C" int qmlg_local_kernels(int kind, const double *A, int64_t lda, const 
                                                     sigmas, nsigmas, K, symmetric ? 1 : 0);
     qmlg::count_launches(1);
     return qmlg::check_launch();
+}
+
+// ---- local kernels from atom-pair kernel matrices (tensor cores / fixed point) --
+//
+// For each sigma and each chunk of A's molecules, the atom-pair matrix
+// Ka[j, i] = k(A_j, B_i) of the chunk's atoms against all of B's comes from the
+// Gaussian tensor-core kernel (qmlg_gaussian_kernel_emulated) or the fixed-point
+// Laplacian (qmlg_laplacian_kernel_fixed), column-major in the workspace.  Two
+// reductions then give the molecule pairs: R[j, b] = sum over B-molecule b's atoms
+// (one thread per row j, so a warp reads 32 consecutive doubles of a column), and
+// K[s, a, b] = sum over A-molecule a's rows of R.  Every term is positive, so each
+// K entry keeps the per-entry relative bound of the atom-pair kernel.
+
+namespace {
+
+constexpr int64_t kLocalPairBytes = 2ll << 30;  // atom-pair matrix per chunk
+constexpr int64_t kLocalMinRows = 4096;         // rows a chunk may always hold
+
+int64_t local_chunk_rows(int64_t natoms_a, int64_t natoms_b)
+{
+    int64_t r = kLocalPairBytes / (8 * (natoms_b < 1 ? 1 : natoms_b));
+    if (r < kLocalMinRows) r = kLocalMinRows;
+    if (r > 65535ll * 256) r = 65535ll * 256;  // the row-sum grid's y extent
+    return r < natoms_a ? r : (natoms_a < 1 ? 1 : natoms_a);
+}
+
+__global__ void local_rowsum_kernel(const double *__restrict__ Ka, int64_t ldka, int rows,
+                                    const int64_t *__restrict__ offb, double *__restrict__ R,
+                                    int64_t ldr)
+{
+    const int mb = blockIdx.x;
+    const int j = blockIdx.y * blockDim.x + threadIdx.x;
+    if (j >= rows) return;
+    const int64_t i0 = offb[mb], i1 = offb[mb + 1];
+    double acc = 0.0;
+    for (int64_t i = i0; i < i1; ++i) acc += Ka[j + ldka * i];
+    R[j + ldr * mb] = acc;
+}
+
+__global__ void local_segsum_kernel(const double *__restrict__ R, int64_t ldr,
+                                    const int64_t *__restrict__ offa, int ma0, int cnt, int nm1,
+                                    int nm2, int ns, int si, double *__restrict__ K)
+{
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)cnt * nm2) return;
+    const int ma = ma0 + (int)(t % cnt);
+    const int mb = (int)(t / cnt);
+    const int64_t base = offa[ma0];
+    const int64_t j0 = offa[ma] - base, j1 = offa[ma + 1] - base;
+    double acc = 0.0;
+    for (int64_t j = j0; j < j1; ++j) acc += R[j + ldr * mb];
+    K[si + (int64_t)ns * (ma + (int64_t)nm1 * mb)] = acc;
+}
+
+// Symmetric mode: K[s, b, a] = K[s, a, b] for b > a.  The two sums run over the
+// same terms in a different order, so the copy makes K exactly symmetric.
+__global__ void local_mirror_kernel(double *__restrict__ K, int nm, int ns)
+{
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t per = (int64_t)nm * nm;
+    if (t >= per * ns) return;
+    const int si = (int)(t % ns);
+    const int64_t ab = t / ns;
+    const int a = (int)(ab % nm), b = (int)(ab / nm);
+    if (b > a) K[si + (int64_t)ns * (b + (int64_t)nm * a)] = K[si + (int64_t)ns * (a + (int64_t)nm * b)];
+}
+
+size_t local_inner_ws(int kind, int64_t rows, int64_t natoms_b, int d)
+{
+    return kind == 0 ? qmlg_gaussian_kernel_emulated_workspace_size((int)rows, (int)natoms_b, d, 0)
+                     : qmlg_laplacian_kernel_fixed_workspace_size((int)rows, (int)natoms_b, d, 0);
+}
+
+}  // namespace
+
+extern "C" size_t qmlg_local_kernels_emulated_workspace_size(int kind, int64_t natoms_a,
+                                                             int64_t natoms_b, int nm2, int d)
+{
+    const int64_t rows = local_chunk_rows(natoms_a, natoms_b);
+    qmlg::WorkspacePlan p;
+    p.add<double>((size_t)rows * (size_t)(natoms_b < 1 ? 1 : natoms_b));
+    p.add<double>((size_t)rows * (size_t)(nm2 < 1 ? 1 : nm2));
+    p.add<char>(local_inner_ws(kind, rows, natoms_b, d));
+    return p.total();
+}
+
+extern "C" int qmlg_local_kernels_emulated(int kind, const double *A, int64_t lda,
+                                           const int64_t *offsets_a, int nm1, const double *B,
+                                           int64_t ldb, const int64_t *offsets_b, int nm2, int d,
+                                           const double *sigmas, int nsigmas, double *K, int flags,
+                                           void *workspace, size_t ws_bytes, void *stream)
+{
+    if ((kind != 0 && kind != 1) || nm1 < 0 || nm2 < 0 || d < 0 || nsigmas < 0) return QMLG_E_ARG;
+    if (nm1 == 0 || nm2 == 0 || nsigmas == 0) return QMLG_OK;
+    if (A == nullptr || B == nullptr || offsets_a == nullptr || offsets_b == nullptr ||
+        sigmas == nullptr || K == nullptr || lda < d || ldb < d)
+        return QMLG_E_ARG;
+    const bool symmetric = (flags & QMLG_KERNEL_SYMMETRIC) != 0;
+    if (symmetric && (nm1 != nm2 || A != B || lda != ldb || offsets_a != offsets_b)) return QMLG_E_ARG;
+    cudaStream_t s = qmlg::as_stream(stream);
+    // the offsets and sigmas steer the host loop
+    std::vector<int64_t> oa(nm1 + 1), ob(nm2 + 1);
+    std::vector<double> sg(nsigmas);
+    cudaError_t e = cudaMemcpyAsync(oa.data(), offsets_a, sizeof(int64_t) * (nm1 + 1),
+                                    cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ob.data(), offsets_b, sizeof(int64_t) * (nm2 + 1), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(sg.data(), sigmas, sizeof(double) * nsigmas, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return qmlg::set_cuda_error(e);
+    if (oa[0] != 0 || ob[0] != 0) return QMLG_E_ARG;
+    for (int m = 0; m < nm1; ++m)
+        if (oa[m + 1] < oa[m]) return QMLG_E_ARG;
+    for (int m = 0; m < nm2; ++m)
+        if (ob[m + 1] < ob[m]) return QMLG_E_ARG;
+    const int64_t nat_a = oa[nm1], nat_b = ob[nm2];
+    if (nat_a > 0x7fffffffll || nat_b > 0x7fffffffll) return QMLG_E_TOO_LARGE;
+    if (ws_bytes < qmlg_local_kernels_emulated_workspace_size(kind, nat_a, nat_b, nm2, d))
+        return QMLG_E_WORKSPACE;
+    const int64_t rows_max = local_chunk_rows(nat_a, nat_b);
+    if (nat_a == 0 || nat_b == 0) {
+        // molecules without atoms: every sum is empty
+        e = cudaMemsetAsync(K, 0, sizeof(double) * (size_t)nsigmas * nm1 * nm2, s);
+        return e == cudaSuccess ? QMLG_OK : qmlg::set_cuda_error(e);
+    }
+    qmlg::Workspace ws(workspace, ws_bytes);
+    double *Ka = ws.take<double>((size_t)rows_max * (size_t)nat_b);
+    double *R = ws.take<double>((size_t)rows_max * (size_t)nm2);
+    const size_t inner_bytes = local_inner_ws(kind, rows_max, nat_b, d);
+    char *inner = ws.take<char>(inner_bytes);
+    if (!Ka || !R || !inner) return QMLG_E_WORKSPACE;
+    // one chunk covering every atom of a symmetric problem takes the symmetric kernel
+    const bool sym_chunk = symmetric && rows_max >= nat_a;
+    for (int si = 0; si < nsigmas; ++si) {
+        if (!(sg[si] > 0.0) || !std::isfinite(sg[si])) return QMLG_E_ARG;
+        int ma0 = 0;
+        while (ma0 < nm1) {
+            int ma1 = ma0;
+            while (ma1 < nm1 && oa[ma1 + 1] - oa[ma0] <= rows_max) ++ma1;
+            if (ma1 == ma0) return QMLG_E_TOO_LARGE;  // one molecule above the chunk rows
+            const int64_t r0 = oa[ma0];
+            const int rows = (int)(oa[ma1] - r0);
+            int st = QMLG_OK;
+            if (rows > 0) {
+                const double *Ac = A + r0 * lda;
+                const int fl = sym_chunk ? QMLG_KERNEL_SYMMETRIC : 0;
+                st = kind == 0
+                         ? qmlg_gaussian_kernel_emulated(Ac, lda, rows, sym_chunk ? Ac : B,
+                                                         sym_chunk ? lda : ldb, (int)nat_b, d, sg[si],
+                                                         Ka, rows, fl, 0.0, inner, inner_bytes, stream)
+                         : qmlg_laplacian_kernel_fixed(Ac, lda, rows, sym_chunk ? Ac : B,
+                                                       sym_chunk ? lda : ldb, (int)nat_b, d, sg[si], Ka,
+                                                       rows, fl, 0.0, inner, inner_bytes, stream);
+                if (st != QMLG_OK) return st;
+                local_rowsum_kernel<<<dim3((unsigned)nm2, (unsigned)qmlg::ceil_div(rows, 256)), 256,
+                                      0, s>>>(Ka, rows, rows, offsets_b, R, rows);
+                qmlg::count_launches(1);
+                st = qmlg::check_launch();
+                if (st != QMLG_OK) return st;
+            }
+            const int cnt = ma1 - ma0;
+            const int64_t pairs = (int64_t)cnt * nm2;
+            local_segsum_kernel<<<(unsigned)qmlg::ceil_div(pairs, 256), 256, 0, s>>>(
+                R, rows > 0 ? rows : 1, offsets_a, ma0, cnt, nm1, nm2, nsigmas, si, K);
+            qmlg::count_launches(1);
+            st = qmlg::check_launch();
+            if (st != QMLG_OK) return st;
+            ma0 = ma1;
+        }
+    }
+    if (symmetric && nm1 > 1) {
+        const int64_t total = (int64_t)nm1 * nm1 * nsigmas;
+        local_mirror_kernel<<<(unsigned)qmlg::ceil_div(total, 256), 256, 0, s>>>(K, nm1, nsigmas);
+        qmlg::count_launches(1);
+        return qmlg::check_launch();
+    }
+    return QMLG_OK;
 }

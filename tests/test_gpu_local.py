@@ -130,3 +130,50 @@ def test_local_krr_reference_end_to_end(cuda):
         alpha = cho_solve(K, Y)
         mae = np.mean(np.abs(Ys - Ks @ alpha))
         assert abs(mae_ref - mae) < 1.0, (kind, mae)
+
+
+def test_local_kernels_emulated_vs_oracle(cuda, oracle):
+    # atom-pair matrices from the tensor-core Gaussian / fixed-point Laplacian, summed
+    # per molecule pair: within 1e-12 per entry, exactly symmetric in symmetric mode
+    L = load_golden("local_krr_qm7.npz")
+    X, Xs, N, Ns = local_krr_features(oracle, L)
+    sigmas = [200.0, 724.0, 10 ** 3.6]
+    Xt, Xst = torch.from_numpy(X).to(cuda), torch.from_numpy(Xs).to(cuda)
+    off = torch.from_numpy(np.concatenate([[0], np.cumsum(N)])).to(cuda)
+    offs = torch.from_numpy(np.concatenate([[0], np.cumsum(Ns)])).to(cuda)
+    for kind in ("gaussian", "laplacian"):
+        K = core.local_kernels(kind, Xt, Xt, off, off, sigmas, symmetric=True,
+                               emulated=True).cpu().numpy()
+        assert relerr(K, oracle.local_kernels(kind, X, X, N, N, sigmas)) <= RTOL
+        for s in range(3):
+            assert np.array_equal(K[s], K[s].T)
+        Ks = core.local_kernels(kind, Xst, Xt, offs, off, sigmas, emulated=True).cpu().numpy()
+        assert relerr(Ks, oracle.local_kernels(kind, Xs, X, Ns, N, sigmas)) <= RTOL
+
+
+def test_local_kernels_emulated_chunks_and_empty_molecules(cuda):
+    # 70000 B atoms hold a chunk to 4096 A rows, so 600 A molecules take three chunks;
+    # molecules without atoms give zeros.  Held to the FP64 local kernel (itself
+    # pinned to the oracle above)
+    ba = generate_molecules(600, seed=11)
+    bb = generate_molecules(5000, seed=12)
+    za, ra, oa = (torch.from_numpy(x).to(cuda) for x in (ba.charges, ba.coordinates, ba.offsets))
+    zb, rb, ob = (torch.from_numpy(x).to(cuda) for x in (bb.charges, bb.coordinates, bb.offsets))
+    A = core.atomic_coulomb_matrix_batch(za, ra, oa, 23, "row-norm")
+    B = core.atomic_coulomb_matrix_batch(zb, rb, ob, 23, "row-norm")
+    assert A.shape[0] > 8192 and B.shape[0] > 65536
+    for kind, sig in (("gaussian", [724.0]), ("laplacian", [10 ** 3.6])):
+        Ke = core.local_kernels(kind, A, B, oa, ob, sig, emulated=True).cpu().numpy()
+        Kf = core.local_kernels(kind, A, B, oa, ob, sig).cpu().numpy()
+        assert relerr(Ke, Kf) <= RTOL
+    # empty molecules at the ends and in the middle
+    n = np.array([0, 5, 0, 7, 3, 0])
+    rows = torch.from_numpy(np.random.default_rng(5).uniform(0, 50, (int(n.sum()), 40))).to(cuda)
+    o = torch.from_numpy(np.concatenate([[0], np.cumsum(n)])).to(cuda)
+    Ke = core.local_kernels("gaussian", rows, rows, o, o, [30.0], symmetric=True,
+                            emulated=True).cpu().numpy()
+    Kf = core.local_kernels("gaussian", rows, rows, o, o, [30.0], symmetric=True).cpu().numpy()
+    empty = n == 0
+    assert np.all(Ke[0][empty, :] == 0) and np.all(Ke[0][:, empty] == 0)
+    full = ~empty
+    assert relerr(Ke[0][np.ix_(full, full)], Kf[0][np.ix_(full, full)]) <= RTOL
