@@ -11,7 +11,7 @@ from __future__ import annotations
 
 import ctypes
 import os
-from typing import Iterable, List, Sequence
+from typing import Iterable, Sequence
 
 import numpy as np
 import torch

@@ -112,6 +112,10 @@ def test_read_xyz_batch_errors_are_the_reference_ones(tmp_path):
             read_xyz_batch([str(good)] * 100 + [str(p)])
     with pytest.raises(FileNotFoundError):
         read_xyz_batch([str(good), str(tmp_path / "missing.xyz")])
+    # not a regular file: the native reader gives it no bytes, read_xyz raises
+    (tmp_path / "adir.xyz").mkdir()
+    with pytest.raises(IsADirectoryError):
+        read_xyz_batch([str(good), str(tmp_path / "adir.xyz")])
 
 
 def test_native_parser_flags_instead_of_guessing():
