@@ -152,31 +152,33 @@ int64_t local_chunk_rows(int64_t natoms_a, int64_t natoms_b)
     return r < natoms_a ? r : (natoms_a < 1 ? 1 : natoms_a);
 }
 
+// B molecules mb0, mb0 + 1, ...; the atom-pair matrix starts at B atom col0.
 __global__ void local_rowsum_kernel(const double *__restrict__ Ka, int64_t ldka, int rows,
-                                    const int64_t *__restrict__ offb, double *__restrict__ R,
-                                    int64_t ldr)
+                                    const int64_t *__restrict__ offb, int mb0, int64_t col0,
+                                    double *__restrict__ R, int64_t ldr)
 {
-    const int mb = blockIdx.x;
+    const int mb = mb0 + blockIdx.x;
     const int j = blockIdx.y * blockDim.x + threadIdx.x;
     if (j >= rows) return;
-    const int64_t i0 = offb[mb], i1 = offb[mb + 1];
+    const int64_t i0 = offb[mb] - col0, i1 = offb[mb + 1] - col0;
     double acc = 0.0;
     for (int64_t i = i0; i < i1; ++i) acc += Ka[j + ldka * i];
-    R[j + ldr * mb] = acc;
+    R[j + ldr * (mb - mb0)] = acc;
 }
 
+// A molecules ma0 .. ma0 + cnt - 1 against B molecules mb0 .. nm2 - 1.
 __global__ void local_segsum_kernel(const double *__restrict__ R, int64_t ldr,
                                     const int64_t *__restrict__ offa, int ma0, int cnt, int nm1,
-                                    int nm2, int ns, int si, double *__restrict__ K)
+                                    int mb0, int nm2, int ns, int si, double *__restrict__ K)
 {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (int64_t)cnt * nm2) return;
+    if (t >= (int64_t)cnt * (nm2 - mb0)) return;
     const int ma = ma0 + (int)(t % cnt);
-    const int mb = (int)(t / cnt);
+    const int mb = mb0 + (int)(t / cnt);
     const int64_t base = offa[ma0];
     const int64_t j0 = offa[ma] - base, j1 = offa[ma + 1] - base;
     double acc = 0.0;
-    for (int64_t j = j0; j < j1; ++j) acc += R[j + ldr * mb];
+    for (int64_t j = j0; j < j1; ++j) acc += R[j + ldr * (mb - mb0)];
     K[si + (int64_t)ns * (ma + (int64_t)nm1 * mb)] = acc;
 }
 
@@ -258,7 +260,9 @@ extern "C" int qmlg_local_kernels_emulated(int kind, const double *A, int64_t ld
     const size_t inner_bytes = local_inner_ws(kind, rows_max, nat_b, d);
     char *inner = ws.take<char>(inner_bytes);
     if (!Ka || !R || !inner) return QMLG_E_WORKSPACE;
-    // one chunk covering every atom of a symmetric problem takes the symmetric kernel
+    // one chunk covering every atom of a symmetric problem takes the symmetric kernel;
+    // with several, a chunk of a symmetric problem starts at its own first atom and
+    // molecule on the B side (the pairs before them come from the mirror)
     const bool sym_chunk = symmetric && rows_max >= nat_a;
     for (int si = 0; si < nsigmas; ++si) {
         if (!(sg[si] > 0.0) || !std::isfinite(sg[si])) return QMLG_E_ARG;
@@ -269,28 +273,32 @@ extern "C" int qmlg_local_kernels_emulated(int kind, const double *A, int64_t ld
             if (ma1 == ma0) return QMLG_E_TOO_LARGE;  // one molecule above the chunk rows
             const int64_t r0 = oa[ma0];
             const int rows = (int)(oa[ma1] - r0);
+            const int mb0 = symmetric ? ma0 : 0;      // first B molecule of this chunk
+            const int64_t c0 = symmetric ? r0 : 0;    // its first atom
+            const int cols = (int)(nat_b - c0);
             int st = QMLG_OK;
             if (rows > 0) {
                 const double *Ac = A + r0 * lda;
+                const double *Bc = symmetric ? Ac : B;
                 const int fl = sym_chunk ? QMLG_KERNEL_SYMMETRIC : 0;
                 st = kind == 0
-                         ? qmlg_gaussian_kernel_emulated(Ac, lda, rows, sym_chunk ? Ac : B,
-                                                         sym_chunk ? lda : ldb, (int)nat_b, d, sg[si],
-                                                         Ka, rows, fl, 0.0, inner, inner_bytes, stream)
-                         : qmlg_laplacian_kernel_fixed(Ac, lda, rows, sym_chunk ? Ac : B,
-                                                       sym_chunk ? lda : ldb, (int)nat_b, d, sg[si], Ka,
-                                                       rows, fl, 0.0, inner, inner_bytes, stream);
+                         ? qmlg_gaussian_kernel_emulated(Ac, lda, rows, Bc, symmetric ? lda : ldb, cols,
+                                                         d, sg[si], Ka, rows, fl, 0.0, inner,
+                                                         inner_bytes, stream)
+                         : qmlg_laplacian_kernel_fixed(Ac, lda, rows, Bc, symmetric ? lda : ldb, cols,
+                                                       d, sg[si], Ka, rows, fl, 0.0, inner, inner_bytes,
+                                                       stream);
                 if (st != QMLG_OK) return st;
-                local_rowsum_kernel<<<dim3((unsigned)nm2, (unsigned)qmlg::ceil_div(rows, 256)), 256,
-                                      0, s>>>(Ka, rows, rows, offsets_b, R, rows);
+                local_rowsum_kernel<<<dim3((unsigned)(nm2 - mb0), (unsigned)qmlg::ceil_div(rows, 256)),
+                                      256, 0, s>>>(Ka, rows, rows, offsets_b, mb0, c0, R, rows);
                 qmlg::count_launches(1);
                 st = qmlg::check_launch();
                 if (st != QMLG_OK) return st;
             }
             const int cnt = ma1 - ma0;
-            const int64_t pairs = (int64_t)cnt * nm2;
+            const int64_t pairs = (int64_t)cnt * (nm2 - mb0);
             local_segsum_kernel<<<(unsigned)qmlg::ceil_div(pairs, 256), 256, 0, s>>>(
-                R, rows > 0 ? rows : 1, offsets_a, ma0, cnt, nm1, nm2, nsigmas, si, K);
+                R, rows > 0 ? rows : 1, offsets_a, ma0, cnt, nm1, mb0, nm2, nsigmas, si, K);
             qmlg::count_launches(1);
             st = qmlg::check_launch();
             if (st != QMLG_OK) return st;

@@ -166,6 +166,18 @@ def test_local_kernels_emulated_chunks_and_empty_molecules(cuda):
         Ke = core.local_kernels(kind, A, B, oa, ob, sig, emulated=True).cpu().numpy()
         Kf = core.local_kernels(kind, A, B, oa, ob, sig).cpu().numpy()
         assert relerr(Ke, Kf) <= RTOL
+    # a symmetric problem past one chunk (about 21000 atoms, chunks of 2 GiB hold
+    # 12800): each chunk starts at its own first atom, the mirror fills the rest
+    bs = generate_molecules(1500, seed=13)
+    zs, rs, os_ = (torch.from_numpy(x).to(cuda) for x in (bs.charges, bs.coordinates, bs.offsets))
+    S = core.atomic_coulomb_matrix_batch(zs, rs, os_, 23, "row-norm")
+    assert S.shape[0] > 2 ** 31 // (8 * S.shape[0])
+    for kind, sig in (("gaussian", [724.0, 2000.0]), ("laplacian", [10 ** 3.6])):
+        Ke = core.local_kernels(kind, S, S, os_, os_, sig, symmetric=True, emulated=True).cpu().numpy()
+        Kf = core.local_kernels(kind, S, S, os_, os_, sig, symmetric=True).cpu().numpy()
+        assert relerr(Ke, Kf) <= RTOL
+        for k in range(len(sig)):
+            assert np.array_equal(Ke[k], Ke[k].T)
     # empty molecules at the ends and in the middle
     n = np.array([0, 5, 0, 7, 3, 0])
     rows = torch.from_numpy(np.random.default_rng(5).uniform(0, 50, (int(n.sum()), 40))).to(cuda)
