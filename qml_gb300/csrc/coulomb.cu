@@ -13,6 +13,7 @@
 //   output: packed lower triangle cm[m(m+1)/2 + n] = M[s_m][s_n], zero-filled.
 // Lane i owns atom i, so molecules have at most 32 atoms (QM7 has at most 23).
 #include <cfloat>
+#include <climits>
 #include <cmath>
 #include <mutex>
 
@@ -163,29 +164,19 @@ __device__ __forceinline__ double acm_pref(double dik, const AcmParams &q)
     return dik > q.cc - q.cd ? __dmul_rn(0.5, acm_cos1(dik, q.cc, q.cd)) : 1.0;
 }
 
-__global__ void __launch_bounds__(kAcmWarps * 32)
-atomic_cm_kernel(const double *__restrict__ charges, const double *__restrict__ coords,
-                 const int64_t *__restrict__ offsets, int n_mol,
-                 const int64_t *__restrict__ central_offsets, const int *__restrict__ central,
-                 int n_central, AcmParams q, double *__restrict__ out, int *__restrict__ status)
+typedef double AcmRow[kMaxAtoms + 1];
+
+// One central atom (task) of molecule mol by the reference's per-centre steps, on
+// one warp with its shared arrays D (distances), P (pair values) and ord.
+__device__ void acm_task(const double *__restrict__ charges, const double *__restrict__ coords,
+                         const int64_t *__restrict__ offsets, const int64_t *__restrict__ coff,
+                         const int *__restrict__ central, int task, int mol, const AcmParams &q,
+                         double *__restrict__ out, int *__restrict__ status, AcmRow *D, AcmRow *P,
+                         int *ord)
 {
-    __shared__ double sD[kAcmWarps][kMaxAtoms][kMaxAtoms + 1];
-    __shared__ double sP[kAcmWarps][kMaxAtoms][kMaxAtoms + 1];
-    __shared__ int sOrd[kAcmWarps][kMaxAtoms];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int task = blockIdx.x * kAcmWarps + warp;
-    if (task >= n_central) return;
+    const int lane = threadIdx.x & 31;
     const int64_t len = (int64_t)q.size * (q.size + 1) / 2;
     double *dst = out + (int64_t)task * len;
-    // molecule of this central atom: last m with coff[m] <= task
-    const int64_t *coff = central_offsets != nullptr ? central_offsets : offsets;
-    int lo = 0, hi = n_mol - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (coff[mid] <= task) lo = mid;
-        else hi = mid - 1;
-    }
-    const int mol = lo;
     const int64_t first = offsets[mol];
     const int natoms = (int)(offsets[mol + 1] - first);
     const int k = central != nullptr ? central[task] : (int)(task - coff[mol]);
@@ -222,7 +213,7 @@ atomic_cm_kernel(const double *__restrict__ charges, const double *__restrict__ 
             dd = __dsqrt_rn(s2);
             if (dd < q.cc) ++cnt;
         }
-        sD[warp][lane][j] = dd;
+        D[lane][j] = dd;
     }
     __syncwarp();
     const int cntk = __shfl_sync(0xffffffffu, cnt, k);
@@ -230,13 +221,13 @@ atomic_cm_kernel(const double *__restrict__ charges, const double *__restrict__ 
         if (lane == 0 && status != nullptr) atomicMin(status, QMLG_E_TOO_MANY_ATOMS);
         return;
     }
-    const double dk = live ? sD[warp][lane][k] : 0.0;  // this atom's distance to the centre
+    const double dk = live ? D[lane][k] : 0.0;  // this atom's distance to the centre
     if (q.sorting == 1) {
         // pair value P(a, b), a < b, as the reference's loop forms it (0 when skipped)
         auto pair = [&](int a, int b, double za, double zb) -> double {
-            const double dak = sD[warp][a][k], dbk = sD[warp][b][k], dab = sD[warp][a][b];
+            const double dak = D[a][k], dbk = D[b][k], dab = D[a][b];
             if (dak > q.cc || dbk > q.cc || dab > q.ic) return 0.0;
-            double pn = __ddiv_rn(__dmul_rn(__dmul_rn(acm_pref(dak, q), za), zb), sD[warp][b][a]);
+            double pn = __ddiv_rn(__dmul_rn(__dmul_rn(acm_pref(dak, q), za), zb), D[b][a]);
             if (dab > q.ic - q.id) pn = __dmul_rn(__dmul_rn(pn, 0.5), acm_cos1(dab, q.ic, q.id));
             if (dbk > q.cc - q.cd) pn = __dmul_rn(__dmul_rn(pn, 0.5), acm_cos1(dbk, q.cc, q.cd));
             return pn;
@@ -248,7 +239,7 @@ atomic_cm_kernel(const double *__restrict__ charges, const double *__restrict__ 
             double p;
             if (i < lane) {
                 p = pair(i, lane, zo, z);
-                if (sD[warp][i][k] <= q.cc && dk <= q.cc && sD[warp][i][lane] <= q.ic)
+                if (D[i][k] <= q.cc && dk <= q.cc && D[i][lane] <= q.ic)
                     rn = __dadd_rn(rn, __dmul_rn(p, p));
             } else if (i == lane) {
                 p = 0.0;
@@ -259,10 +250,10 @@ atomic_cm_kernel(const double *__restrict__ charges, const double *__restrict__ 
                 }
             } else {
                 p = pair(lane, i, z, zo);
-                if (dk <= q.cc && sD[warp][i][k] <= q.cc && sD[warp][lane][i] <= q.ic)
+                if (dk <= q.cc && D[i][k] <= q.cc && D[lane][i] <= q.ic)
                     rn = __dadd_rn(rn, __dmul_rn(p, p));
             }
-            sP[warp][lane][i] = p;
+            P[lane][i] = p;
         }
         double key = live ? (lane == k ? DBL_MAX : rn) : -INFINITY;
         for (int m = 0; m < cntk; ++m) {
@@ -276,13 +267,13 @@ atomic_cm_kernel(const double *__restrict__ charges, const double *__restrict__ 
                     bi = oi;
                 }
             }
-            if (lane == 0) sOrd[warp][m] = bi;
+            if (lane == 0) ord[m] = bi;
             if (lane == bi) key = 0.0;
         }
         __syncwarp();
         for (int m = 0; m < cntk; ++m) {
-            const int idx = (m * m + m) / 2, a = sOrd[warp][m];
-            for (int n = lane; n <= m; n += 32) dst[idx + n] = sP[warp][a][sOrd[warp][n]];
+            const int idx = (m * m + m) / 2, a = ord[m];
+            for (int n = lane; n <= m; n += 32) dst[idx + n] = P[a][ord[n]];
         }
     } else {
         // centre-independent pair matrix
@@ -293,7 +284,7 @@ atomic_cm_kernel(const double *__restrict__ charges, const double *__restrict__ 
             if (j == lane) {
                 p = __dmul_rn(0.5, zp);
             } else {
-                const double dij = sD[warp][lane][j];
+                const double dij = D[lane][j];
                 p = 0.0;
                 if (!(dij > q.ic)) {
                     const double za = j < lane ? zo : z, zb = j < lane ? z : zo;
@@ -301,7 +292,7 @@ atomic_cm_kernel(const double *__restrict__ charges, const double *__restrict__ 
                     if (dij > q.ic - q.id) p = __dmul_rn(__dmul_rn(p, 0.5), acm_cos1(dij, q.ic, q.id));
                 }
             }
-            sP[warp][lane][j] = p;
+            P[lane][j] = p;
         }
         double key = live ? dk : INFINITY;
         for (int m = 0; m < cntk; ++m) {
@@ -315,23 +306,190 @@ atomic_cm_kernel(const double *__restrict__ charges, const double *__restrict__ 
                     bi = oi;
                 }
             }
-            if (lane == 0) sOrd[warp][m] = bi;
+            if (lane == 0) ord[m] = bi;
             if (lane == bi) key = DBL_MAX;
         }
         __syncwarp();
         for (int m = 0; m < cntk; ++m) {
-            const int i = sOrd[warp][m];
-            const double dik = sD[warp][i][k];
+            const int i = ord[m];
+            const double dik = D[i][k];
             if (dik > q.cc) continue;
             const double pr = acm_pref(dik, q);
             const int idx = (m * m + m) / 2;
             for (int n = lane; n <= m; n += 32) {
-                const int j = sOrd[warp][n];
-                double pn = __dmul_rn(pr, sP[warp][i][j]);
-                const double djk = sD[warp][j][k];
+                const int j = ord[n];
+                double pn = __dmul_rn(pr, P[i][j]);
+                const double djk = D[j][k];
                 if (djk > q.cc - q.cd) pn = __dmul_rn(__dmul_rn(pn, 0.5), acm_cos1(djk, q.cc, q.cd));
                 dst[idx + n] = pn;
             }
+        }
+    }
+}
+
+
+// Order-preserving integer key of a double >= 0.
+__device__ __forceinline__ long long acm_key(double v) { return __double_as_longlong(v); }
+
+// One warp per molecule.  Where no cutoff or decay mask touches the molecule (every
+// distance positive, inside the central cutoff and below both decay bands: the
+// default cutoffs), the prefactors are all 1.0, so the pair values, and for row-norm
+// sorting the row norms, are the same for every central atom: the warp forms them
+// once and writes every centre's row from them, with the arithmetic acm_task uses
+// (multiplying by a prefactor of 1.0 is exact), so the rows are the same bits.
+// Row-norm order for centre k is k, then the molecule's one descending order
+// without k; distance order is selected per centre on integer keys.  Any other
+// molecule runs acm_task for each of its central atoms.
+__global__ void __launch_bounds__(kAcmWarps * 32)
+atomic_cm_kernel(const double *__restrict__ charges, const double *__restrict__ coords,
+                 const int64_t *__restrict__ offsets, int n_mol,
+                 const int64_t *__restrict__ central_offsets, const int *__restrict__ central,
+                 int n_central, AcmParams q, double *__restrict__ out, int *__restrict__ status)
+{
+    __shared__ double sD[kAcmWarps][kMaxAtoms][kMaxAtoms + 1];
+    __shared__ double sP[kAcmWarps][kMaxAtoms][kMaxAtoms + 1];
+    __shared__ int sOrd[kAcmWarps][kMaxAtoms];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int mol = blockIdx.x * kAcmWarps + warp;
+    if (mol >= n_mol) return;
+    const int64_t *coff = central_offsets != nullptr ? central_offsets : offsets;
+    const int64_t t0 = coff[mol], t1 = coff[mol + 1];
+    if (t0 >= t1 || t0 >= n_central) return;
+    const int64_t first = offsets[mol];
+    const int natoms = (int)(offsets[mol + 1] - first);
+    const int64_t len = (int64_t)q.size * (q.size + 1) / 2;
+    bool fast = natoms >= 1 && natoms <= kMaxAtoms && natoms <= q.size && t1 <= n_central;
+    if (fast) {
+        bool kok = true;
+        for (int64_t t = t0 + lane; t < t1; t += 32) {
+            const int k = central != nullptr ? central[t] : (int)(t - t0);
+            kok = kok && k >= 0 && k < natoms;
+        }
+        fast = __all_sync(0xffffffffu, kok);
+    }
+    const bool live = lane < natoms;
+    double z = 0.0, zp = 0.0, rn = 0.0;
+    if (fast) {
+        double x = 0.0, y = 0.0, w = 0.0;
+        if (live) {
+            z = charges[first + lane];
+            x = coords[3 * (first + lane) + 0];
+            y = coords[3 * (first + lane) + 1];
+            w = coords[3 * (first + lane) + 2];
+        }
+        const int zi = (int)z;
+        if ((double)zi == z && zi >= 0 && zi < kZTable) zp = c_zpow[zi];
+        else zp = pow(z, 2.4);
+        bool ok = true;
+        for (int j = 0; j < natoms; ++j) {
+            const double xj = __shfl_sync(0xffffffffu, x, j);
+            const double yj = __shfl_sync(0xffffffffu, y, j);
+            const double wj = __shfl_sync(0xffffffffu, w, j);
+            if (!live) continue;
+            double dd = 0.0;
+            if (j != lane) {
+                const double dx = __dsub_rn(xj, x), dy = __dsub_rn(yj, y), dz = __dsub_rn(wj, w);
+                double s2 = __dmul_rn(dx, dx);
+                s2 = __dadd_rn(s2, __dmul_rn(dy, dy));
+                s2 = __dadd_rn(s2, __dmul_rn(dz, dz));
+                dd = __dsqrt_rn(s2);
+                ok = ok && dd > 0.0 && dd < q.cc && dd <= q.cc - q.cd && dd <= q.ic - q.id &&
+                     dd <= q.ic;
+            }
+            sD[warp][lane][j] = dd;
+        }
+        fast = __all_sync(0xffffffffu, ok);
+    }
+    if (fast) {
+        __syncwarp();
+        // pair values: 0.5 Z^2.4 on the diagonal, Z_a Z_b / D_ab (a the smaller index)
+        for (int j = 0; j < natoms; ++j) {
+            const double zo = __shfl_sync(0xffffffffu, z, j);
+            if (!live) continue;
+            double p;
+            if (j == lane) {
+                p = __dmul_rn(0.5, zp);
+            } else {
+                const double za = j < lane ? zo : z, zb = j < lane ? z : zo;
+                p = __ddiv_rn(__dmul_rn(za, zb), sD[warp][lane][j]);
+            }
+            sP[warp][lane][j] = p;
+            rn = __dadd_rn(rn, __dmul_rn(p, p));
+        }
+        __syncwarp();
+        // the selections below need every row norm positive and below DBL_MAX
+        if (q.sorting == 1) fast = __all_sync(0xffffffffu, !live || (rn > 0.0 && rn < DBL_MAX));
+    }
+    if (!fast) {
+        for (int64_t t = t0; t < t1 && t < n_central; ++t) {
+            __syncwarp();
+            acm_task(charges, coords, offsets, coff, central, (int)t, mol, q, out, status,
+                     sD[warp], sP[warp], sOrd[warp]);
+        }
+        return;
+    }
+    int posk_base = 0;
+    if (q.sorting == 1) {
+        // the molecule's order: row norm descending, the first index among equals
+        long long key = live ? acm_key(rn) : -1ll;
+        for (int m = 0; m < natoms; ++m) {
+            long long bv = key;
+            int bi = lane;
+            for (int off = 16; off > 0; off >>= 1) {
+                const long long ov = __shfl_xor_sync(0xffffffffu, bv, off);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+                if (ov > bv || (ov == bv && oi < bi)) {
+                    bv = ov;
+                    bi = oi;
+                }
+            }
+            if (lane == 0) sOrd[warp][m] = bi;
+            if (lane == bi) {
+                key = -2ll;
+                posk_base = m;  // this lane's place in the order
+            }
+        }
+        __syncwarp();
+    }
+    const int tri = natoms * (natoms + 1) / 2;
+    for (int64_t t = t0; t < t1; ++t) {
+        const int k = central != nullptr ? central[t] : (int)(t - t0);
+        double *dst = out + t * len;
+        for (int64_t e = tri + lane; e < len; e += 32) dst[e] = 0.0;
+        int ordl = 0;  // lane m < natoms: the atom in place m for this centre
+        if (q.sorting == 1) {
+            const int pk = __shfl_sync(0xffffffffu, posk_base, k);
+            if (live) ordl = lane == 0 ? k : sOrd[warp][lane - 1 < pk ? lane - 1 : lane];
+        } else {
+            // distance to the centre ascending, the first index among equals
+            long long key = live ? acm_key(sD[warp][lane][k]) : LLONG_MAX;
+            for (int m = 0; m < natoms; ++m) {
+                long long bv = key;
+                int bi = lane;
+                for (int off = 16; off > 0; off >>= 1) {
+                    const long long ov = __shfl_xor_sync(0xffffffffu, bv, off);
+                    const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+                    if (ov < bv || (ov == bv && oi < bi)) {
+                        bv = ov;
+                        bi = oi;
+                    }
+                }
+                if (lane == m) ordl = bi;
+                if (lane == bi) key = LLONG_MAX - 1;
+            }
+        }
+        // entry e of the packed lower triangle: row m, column n <= m (every lane runs
+        // every trip, so the shuffles see the whole warp)
+        int m = 0;
+        for (int e0 = 0; e0 < tri; e0 += 32) {
+            const int e = e0 + lane;
+            const bool in = e < tri;
+            if (in)
+                while ((m + 1) * (m + 2) / 2 <= e) ++m;
+            const int n = in ? e - m * (m + 1) / 2 : 0;
+            const int a = __shfl_sync(0xffffffffu, ordl, in ? m : 0);
+            const int b2 = __shfl_sync(0xffffffffu, ordl, n);
+            if (in) dst[e] = sP[warp][a][b2];
         }
     }
 }
@@ -391,7 +549,7 @@ extern "C" int qmlg_atomic_coulomb_matrix(const double *charges, const double *c
     q.id = interaction_decay < 0 ? 0.0 : (interaction_decay > q.ic ? q.ic : interaction_decay);
     q.size = size;
     q.sorting = sorting;
-    const int blocks = (int)qmlg::ceil_div(n_central, kAcmWarps);
+    const int blocks = (int)qmlg::ceil_div(n_mol, kAcmWarps);
     {
         atomic_cm_kernel<<<blocks, kAcmWarps * 32, 0, qmlg::as_stream(stream)>>>(
             charges, coordinates, atom_offsets, n_mol, central_offsets, central_atoms, n_central, q,
