@@ -71,6 +71,40 @@ def test_atomic_cm_indices(cuda, oracle):
 
 
 @pytest.mark.parametrize("sorting", ["distance", "row-norm"])
+def test_atomic_cm_batch_mixed_paths(cuda, oracle, sorting):
+    # a cutoff that only some molecules reach: in one launch, the molecules it does
+    # not touch take the one-pass path (bit-exact), the others the per-centre steps
+    # (within 1e-13: the device cos); with central-atom subsets as well
+    b = generate_molecules(400, seed=21)
+    kw = dict(central_cutoff=6.0, central_decay=1.0, interaction_cutoff=9.0, interaction_decay=1.0)
+    span = np.array([np.max(np.linalg.norm(r[:, None] - r[None], axis=-1))
+                     for r in (b.molecule(m)[1] for m in range(400))])
+    inside = span <= 5.0
+    assert 20 < inside.sum() < 380
+    X = generate_atomic_coulomb_matrix_batch(b.charges, b.coordinates, b.offsets, size=23,
+                                             sorting=sorting, **kw).cpu().numpy()
+    rows = [oracle.atomic_cm(*b.molecule(m), None, 23, sorting, **kw) for m in range(400)]
+    Xo = np.concatenate(rows)
+    start = np.concatenate([[0], np.cumsum([r.shape[0] for r in rows])])
+    for m in range(400):
+        got, want = X[start[m]:start[m + 1]], Xo[start[m]:start[m + 1]]
+        if inside[m]:
+            assert np.array_equal(got, want), m
+        else:
+            assert np.max(np.abs(got - want)) <= 1e-13 * max(1.0, np.max(np.abs(want))), m
+    # every second atom as centre, through the C ABI's central subsets
+    z, r, o = (torch.from_numpy(x).to(cuda) for x in (b.charges, b.coordinates, b.offsets))
+    cen = [np.arange(0, b.offsets[m + 1] - b.offsets[m], 2) for m in range(400)]
+    coff = torch.from_numpy(np.concatenate([[0], np.cumsum([c.shape[0] for c in cen])])).to(cuda)
+    cat = torch.from_numpy(np.concatenate(cen).astype(np.int32)).to(cuda)
+    Xs = core.atomic_coulomb_matrix_batch(z, r, o, 23, sorting, central_offsets=coff,
+                                          central_atoms=cat, **kw).cpu().numpy()
+    want = np.concatenate([oracle.atomic_cm(*b.molecule(m), cen[m], 23, sorting, **kw)
+                           for m in range(400)])
+    assert np.max(np.abs(Xs - want)) <= 1e-13 * np.max(np.abs(want))
+
+
+@pytest.mark.parametrize("sorting", ["distance", "row-norm"])
 def test_atomic_cm_batch_bit_exact(cuda, oracle, sorting):
     # one launch over a synthetic batch against the per-molecule oracle
     b = generate_molecules(300, seed=11)
