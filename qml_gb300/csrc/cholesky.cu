@@ -23,6 +23,7 @@
 
 #include "common.cuh"
 #include "emulated_gemm.cuh"
+#include "rsqrt.cuh"
 #include "exact_acc.cuh"
 
 namespace cg = cooperative_groups;
@@ -35,33 +36,6 @@ constexpr int NB = 64;
 
 // 1/sqrt(p) for a positive finite double, with as few FP64 instructions as possible
 // (on this GPU each costs ~64 cycles of the FP64 pipe; sqrt and division ~650): an
-// FP32 rsqrtf of p's leading bits gives ~23 bits, and one Halley step (cubic
-// convergence for f(y) = 1/y^2 - p) brings it to full FP64 precision:
-//   e = 1 - p y^2,  y <- y + y e (1/2 + 3/8 e).
-// The FP32 <-> FP64 moves are done on the bits.  Outside [2^-120, 2^120] p is first
-// scaled by an even power of two into [1, 4).
-__device__ __forceinline__ double rsqrt_halley(double p)
-{
-    double q = p;
-    int h = 0;
-    const int ed = (int)((unsigned long long)__double_as_longlong(p) >> 52);
-    if (ed < 1023 - 120 || ed > 1023 + 120) {
-        const int ex = ilogb(p) & ~1;
-        q = scalbn(p, -ex);
-        h = -ex / 2;
-    }
-    const unsigned long long qb = (unsigned long long)__double_as_longlong(q);
-    // q truncated to FP32: exponent rebiased from 1023 to 127, top 23 mantissa bits
-    const uint32_t fb = (uint32_t)(((qb >> 52) - 896ull) << 23) | (uint32_t)((qb >> 29) & 0x7fffffull);
-    const uint32_t yb = __float_as_uint(rsqrtf(__uint_as_float(fb)));
-    // the FP32 estimate (a normal positive float) as an exact double
-    double y = __longlong_as_double((long long)((((unsigned long long)(yb >> 23) + 896ull) << 52) |
-                                                ((unsigned long long)(yb & 0x7fffffu) << 29)));
-    const double e = fma(-q * y, y, 1.0);
-    y = fma(y * e, fma(0.375, e, 0.5), y);
-    return h != 0 ? scalbn(y, h) : y;
-}
-
 // Number of lower-triangle elements (r, s) with c < s <= r < NB.
 __host__ __device__ constexpr int tri_prefix(int c) { return (NB - 1 - c) * (NB - c) / 2; }
 

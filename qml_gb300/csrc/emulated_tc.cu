@@ -32,6 +32,7 @@
 #include <mutex>
 #include <vector>
 
+#include "rsqrt.cuh"
 #include "common.cuh"
 #include "emulated_gemm.cuh"
 #include "tc_ptx.cuh"
@@ -610,8 +611,12 @@ __device__ __forceinline__ void emu_tc_body(const CUtensorMap &mapA, const CUten
                                                      : m2s * pow2i(ew);
                                 const double x = fma((double)v64[col], w, aj + sb);
                                 if constexpr (MODE == kMatern) {
-                                    // d^2 rounds below 0 only for (near) equal rows
-                                    const double d2 = fmax(x, 0.0), dd = sqrt(d2);
+                                    // d^2 rounds below 0 only for (near) equal rows; the
+                                    // sign and zero tests are on the bits, and d = d^2 /
+                                    // sqrt(d^2) comes from rsqrt_halley (within 2 ulp)
+                                    const bool pos = __double_as_longlong(x) > 0;
+                                    const double d2 = pos ? x : 0.0;
+                                    const double dd = pos ? d2 * rsqrt_halley(d2) : 0.0;
                                     double poly = 1.0 - p.s1 * dd;
                                     if (p.order == 2) poly += p.s2 * d2;
                                     kv = exp_nonpos(p.s1 * dd) * poly;
