@@ -68,32 +68,72 @@ coulomb_kernel(const double *__restrict__ charges, const double *__restrict__ co
     }
     const double diag = __dmul_rn(0.5, zp);
 
-    // Row i of M into shared memory, row norm in the reference's order.
-    double norm = __dmul_rn(diag, diag);
-    for (int j = 0; j < natoms; ++j) {
-        const double zj = __shfl_sync(0xffffffffu, z, j);
-        const double xj = __shfl_sync(0xffffffffu, x, j);
-        const double yj = __shfl_sync(0xffffffffu, y, j);
-        const double wj = __shfl_sync(0xffffffffu, w, j);
-        if (!live) continue;
-        double p;
-        if (j == lane) {
-            p = diag;
-        } else {
-            const double dx = __dsub_rn(xj, x);
-            const double dy = __dsub_rn(yj, y);
-            const double dz = __dsub_rn(wj, w);
+    // M's pairs into shared memory, dealt out one per lane.  An FP64 instruction holds
+    // its scheduler's FP64 pipe for the same time whatever its active lanes, so the
+    // n(n-1)/2 pairs (i < j) go through the sqrt and division in n(n-1)/64 trips
+    // instead of one trip per atom.  Pair (i, j) is what lane i formed before,
+    // (z_i z_j) / sqrt(dx^2 + dy^2 + dz^2) with dx = x_j - x_i; lane j got the same
+    // bits ((-dx)^2 = dx^2, z_j z_i = z_i z_j), so it is stored at (i, j) and (j, i).
+    const int npairs = natoms * (natoms - 1) / 2;
+    for (int t0 = 0; t0 < npairs; t0 += 32) {
+        const int t = t0 + lane;
+        const bool in = t < npairs;
+        int i = 0, j = 1;
+        if (in) {
+            // t = j (j - 1) / 2 + i, 0 <= i < j
+            j = (int)((1.0f + sqrtf(8.0f * (float)t + 1.0f)) * 0.5f);
+            while (j * (j - 1) / 2 > t) --j;
+            while ((j + 1) * j / 2 <= t) ++j;
+            i = t - j * (j - 1) / 2;
+        }
+        const double zi_ = __shfl_sync(0xffffffffu, z, i), zj = __shfl_sync(0xffffffffu, z, j);
+        const double xi = __shfl_sync(0xffffffffu, x, i), xj = __shfl_sync(0xffffffffu, x, j);
+        const double yi = __shfl_sync(0xffffffffu, y, i), yj = __shfl_sync(0xffffffffu, y, j);
+        const double wi = __shfl_sync(0xffffffffu, w, i), wj = __shfl_sync(0xffffffffu, w, j);
+        if (in) {
+            const double dx = __dsub_rn(xj, xi);
+            const double dy = __dsub_rn(yj, yi);
+            const double dz = __dsub_rn(wj, wi);
             double s = __dmul_rn(dx, dx);
             s = __dadd_rn(s, __dmul_rn(dy, dy));
             s = __dadd_rn(s, __dmul_rn(dz, dz));
-            p = __ddiv_rn(__dmul_rn(z, zj), __dsqrt_rn(s));
-            norm = __dadd_rn(norm, __dmul_rn(p, p));
+            const double p = __ddiv_rn(__dmul_rn(zi_, zj), __dsqrt_rn(s));
+            s_m[warp][i][j] = p;
+            s_m[warp][j][i] = p;
         }
-        s_m[warp][lane][j] = p;
+    }
+    if (live) s_m[warp][lane][lane] = diag;
+    __syncwarp();
+    // row norm in the reference's order: the diagonal, then j ascending
+    double norm = __dmul_rn(diag, diag);
+    for (int j = 0; j < natoms; ++j) {
+        if (!live || j == lane) continue;
+        const double p = s_m[warp][lane][j];
+        norm = __dadd_rn(norm, __dmul_rn(p, p));
     }
 
     // Selection order.
-    if (sorting) {
+    if (sorting && __all_sync(0xffffffffu, !live || !(norm != norm))) {
+        // no NaN norm: the norms (>= 0), DBL_MAX and +inf order as their bits do,
+        // so the selection runs on integer keys (the same picks, ties included)
+        long long key = live ? __double_as_longlong(norm) : __double_as_longlong(INFINITY);
+        const long long picked = __double_as_longlong(DBL_MAX);
+        for (int k = 0; k < natoms; ++k) {
+            long long bv = key;
+            int bi = lane;
+            for (int off = 16; off > 0; off >>= 1) {
+                const long long ov = __shfl_xor_sync(0xffffffffu, bv, off);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+                if (ov < bv || (ov == bv && oi < bi)) {
+                    bv = ov;
+                    bi = oi;
+                }
+            }
+            if (bi >= natoms) bi = 0;
+            if (lane == 0) s_order[warp][natoms - 1 - k] = bi;
+            if (lane == bi) key = picked;
+        }
+    } else if (sorting) {
         double key = live ? norm : INFINITY;
         for (int k = 0; k < natoms; ++k) {
             double bv = key;
