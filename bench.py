@@ -351,7 +351,8 @@ def run_extra(a, dev, batch, X, stream):
         "linear_tensor": gpu_time(kernel("linear", True), reps=3),
         "matern_l2_order2_fp64": gpu_time(kernel("matern_l2", False, order=2)),
         "matern_l2_order2_tensor": gpu_time(kernel("matern_l2", True, order=2), reps=3),
-        "sargan_2gammas_fp64": gpu_time(kernel("sargan", False, gammas=[1.0, 1.0 / 3.0]))}
+        "sargan_2gammas_fp64": gpu_time(kernel("sargan", False, gammas=[1.0, 1.0 / 3.0])),
+        "sargan_2gammas_fixed": gpu_time(kernel("sargan", True, gammas=[1.0, 1.0 / 3.0]), reps=3)}
     torch.cuda.empty_cache()
 
     sub = batch.slice(0, 25000)
@@ -443,6 +444,7 @@ def run_extra(a, dev, batch, X, stream):
                       "cpu_oracle_s_scaled": (time.perf_counter() - c0) * ntr / rows}
     other["linear"]["gpu_tensor_s"] = out["train_kernel_matrix_s"]["linear_tensor"]
     other["matern_l2_order2"]["gpu_tensor_s"] = out["train_kernel_matrix_s"]["matern_l2_order2_tensor"]
+    other["sargan_2gammas"]["gpu_fixed_s"] = out["train_kernel_matrix_s"]["sargan_2gammas_fixed"]
     out["other_global_kernels"] = other
     del Xg
 

@@ -232,6 +232,21 @@ int qmlg_gaussian_kernel_emulated(const double *A, int64_t lda, int na, const do
                                   size_t ws_bytes, void *stream);
 
 /*
+ * The Sargan kernel (qml/fkernels.f90:487-531) from exact fixed-point L1 sums: the
+ * qmlg_laplacian_kernel_fixed grid and kernel with the Sargan polynomial in the
+ * epilogue.  For gammas >= 0 the grid's bound on t = d / sigma is tightened by
+ * 1 + ng max(1, sum gamma), which keeps every entry within 0.5e-12 relative; a
+ * negative or non-finite gamma, input that is not finite and a bound the grid
+ * cannot meet take qmlg_sargan_kernel.  gammas: device array (read back once).
+ * Arguments as qmlg_sargan_kernel.  ws: qmlg_sargan_kernel_fixed_workspace_size.
+ */
+size_t qmlg_sargan_kernel_fixed_workspace_size(int na, int nb, int d, int flags);
+int qmlg_sargan_kernel_fixed(const double *A, int64_t lda, int na, const double *B, int64_t ldb,
+                             int nb, int d, double sigma, const double *gammas, int ng, double *K,
+                             int64_t ldk, int flags, double diag_shift, void *workspace,
+                             size_t ws_bytes, void *stream);
+
+/*
  * The Matern L2 kernel (qml/fkernels.f90:426-484) of order 1 or 2 on the tensor
  * cores: the Gaussian tile kernel's d^2 = |a|^2 + |b|^2 - 2 a.b with the Matern
  * epilogue.  Both orders are flat at d = 0, so |K - K_exact| / K stays below

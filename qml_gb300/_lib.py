@@ -111,6 +111,9 @@ SIGNATURES = {
     "qmlg_predict_emulated": (_I, [_P, _I64, _I, _P, _I64, _I, _I, _D, _P, _P, _P, _SZ, _P]),
     "qmlg_predict_emulated_async": (_I, [_P, _I64, _I, _P, _I64, _I, _I, _D, _P, _P, _P, _P,
                                          _SZ, _P]),
+    "qmlg_sargan_kernel_fixed_workspace_size": (_SZ, [_I, _I, _I, _I]),
+    "qmlg_sargan_kernel_fixed": (_I, [_P, _I64, _I, _P, _I64, _I, _I, _D, _P, _I, _P, _I64, _I, _D,
+                                      _P, _SZ, _P]),
     "qmlg_matern_kernel_l2_emulated_workspace_size": (_SZ, [_I, _I, _I, _I]),
     "qmlg_matern_kernel_l2_emulated": (_I, [_P, _I64, _I, _P, _I64, _I, _I, _D, _I, _P, _I64, _I,
                                             _D, _P, _SZ, _P]),

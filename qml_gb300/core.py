@@ -226,8 +226,9 @@ def kernel_matrix(kind: str, A: torch.Tensor, B: torch.Tensor, sigma: float,
     on the tensor cores (qmlg_gaussian_kernel_emulated), the Laplacian L1 sums in
     fixed-point integers (qmlg_laplacian_kernel_fixed), the linear kernel's dot
     products and the Matern L2 orders 1 and 2 on the tensor cores
-    (qmlg_linear_kernel_emulated, qmlg_matern_kernel_l2_emulated); Matern order 0
-    and Sargan take their FP64 kernels."""
+    (qmlg_linear_kernel_emulated, qmlg_matern_kernel_l2_emulated), the Sargan kernel
+    from fixed-point L1 sums (qmlg_sargan_kernel_fixed); Matern order 0 takes its FP64
+    kernel."""
     _require_cuda(A, B)
     A, lda = _rows(A)
     if symmetric:
@@ -293,6 +294,15 @@ def kernel_matrix(kind: str, A: torch.Tensor, B: torch.Tensor, sigma: float,
     if kind == "sargan":
         g = torch.as_tensor(gammas if gammas is not None else [], dtype=torch.float64)
         g = g.reshape(-1).to(A.device).contiguous()
+        if emulated:
+            ws = workspaces.get(lib().qmlg_sargan_kernel_fixed_workspace_size(na, nb, d, flags),
+                                A.device)
+            check(lib().qmlg_sargan_kernel_fixed(A.data_ptr(), lda, na, B.data_ptr(), ldb, nb, d,
+                                                 float(sigma), g.data_ptr() if g.numel() else None,
+                                                 int(g.numel()), buf.data_ptr(), na, flags,
+                                                 float(diag_shift), ws.data_ptr(), ws.numel(), st),
+                  "qmlg_sargan_kernel_fixed")
+            return buf.T
         check(lib().qmlg_sargan_kernel(A.data_ptr(), lda, na, B.data_ptr(), ldb, nb, d,
                                        float(sigma), g.data_ptr() if g.numel() else None,
                                        int(g.numel()), buf.data_ptr(), na, flags,

@@ -20,6 +20,7 @@
 #include <cmath>
 #include <cstring>
 #include <mutex>
+#include <vector>
 
 #include "common.cuh"
 
@@ -576,8 +577,11 @@ struct FixedPlan {
 __global__ void fixed_plan_kernel(const unsigned long long *__restrict__ maxbits, int nmax, int d,
                                   double sigma, FixedPlan *__restrict__ plan, int *__restrict__ flag)
 {
-    double m = 0.0;
-    for (int k = 0; k < nmax; ++k) m = fmax(m, __longlong_as_double((long long)maxbits[k]));
+    // the largest |x| bit pattern: NaN sorts above +inf, so any NaN makes m non-finite
+    // (an fmax would drop it)
+    unsigned long long mbits = 0;
+    for (int k = 0; k < nmax; ++k) mbits = maxbits[k] > mbits ? maxbits[k] : mbits;
+    const double m = __longlong_as_double((long long)mbits);
     bool ok = isfinite(m);
     int F = 0;
     if (ok) {
@@ -613,11 +617,13 @@ __global__ void to_fixed_kernel(const double *__restrict__ X, int64_t ldx, int r
 
 __device__ __forceinline__ long long iabs64(long long v) { return v < 0 ? -v : v; }
 
+// EPI 0: Laplacian exp(-d / sigma); 1: Sargan exp(-d / sigma) (1 + sum_m gamma_m t^m).
+template <int EPI>
 __global__ void __launch_bounds__(NT)
 laplace_fixed_kernel(const long long *__restrict__ A, int na, const long long *__restrict__ B,
                      int nb, int d, double inv_scale, double neg_inv_sigma,
                      double *__restrict__ K, int64_t ldk, int symmetric, double diag_shift,
-                     const FixedPlan *__restrict__ plan)
+                     const FixedPlan *__restrict__ plan, const double *__restrict__ gammas, int ng)
 {
     if (plan != nullptr) {  // the device-side grid: nothing to do when it failed
         if (!plan->ok) return;
@@ -670,7 +676,18 @@ laplace_fixed_kernel(const long long *__restrict__ A, int na, const long long *_
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
             const int j = j0 + tx + 16 * a, i = i0 + ty + 16 * b;
-            double v = exp(neg_inv_sigma * ((double)acc[a][b] * inv_scale));
+            const double dist = (double)acc[a][b] * inv_scale;
+            double v = exp(neg_inv_sigma * dist);
+            if (EPI == 1) {
+                // Sargan, as kernel_matrix_kernel forms it: t = d / sigma
+                const double t = -neg_inv_sigma * dist;
+                double pw = 1.0, sum = 0.0;
+                for (int m = 0; m < ng; ++m) {
+                    pw *= t;
+                    sum += gammas[m] * pw;
+                }
+                v *= 1.0 + sum;
+            }
             if (symmetric && i == j) v = 1.0 + diag_shift;
             if (j < na && i < nb) K[(int64_t)i * ldk + j] = v;
             T[ty + 16 * b][tx + 16 * a] = v;
@@ -768,10 +785,27 @@ extern "C" size_t qmlg_laplacian_kernel_fixed_workspace_size(int na, int nb, int
     return p.total();
 }
 
-extern "C" int qmlg_laplacian_kernel_fixed(const double *A, int64_t lda, int na, const double *B,
-                                           int64_t ldb, int nb, int d, double sigma, double *K,
-                                           int64_t ldk, int flags, double diag_shift,
-                                           void *workspace, size_t ws_bytes, void *stream)
+namespace {
+
+// The FP64 kernel behind a fixed-point call that cannot meet its bound.
+int l1_fp64(const double *A, int64_t lda, int na, const double *B, int64_t ldb, int nb, int d,
+            double sigma, const double *gammas, int ng, double *K, int64_t ldk, int flags,
+            double diag_shift, void *stream)
+{
+    return gammas == nullptr
+               ? qmlg_laplacian_kernel(A, lda, na, B, ldb, nb, d, sigma, K, ldk, flags, diag_shift,
+                                       stream)
+               : qmlg_sargan_kernel(A, lda, na, B, ldb, nb, d, sigma, gammas, ng, K, ldk, flags,
+                                    diag_shift, stream);
+}
+
+// L1 kernel matrices from exact fixed-point sums: the Laplacian (gammas == nullptr)
+// or the Sargan kernel.  gain multiplies the grid's bound on t = d / sigma, for an
+// epilogue that passes an error in t into K amplified.
+int fixed_l1_matrix(const double *A, int64_t lda, int na, const double *B, int64_t ldb, int nb,
+                    int d, double sigma, const double *gammas, int ng, double gain, double *K,
+                    int64_t ldk, int flags, double diag_shift, void *workspace, size_t ws_bytes,
+                    void *stream)
 {
     int st = check_common(A, lda, na, B, ldb, nb, d, sigma);
     if (st != QMLG_OK) return st;
@@ -799,31 +833,85 @@ extern "C" int qmlg_laplacian_kernel_fixed(const double *A, int64_t lda, int na,
     unsigned long long h[2] = {0, 0};
     st = qmlg::read_back(h, mx, sizeof(h), s);
     if (st != QMLG_OK) return st;
-    double ma, mb;
-    std::memcpy(&ma, &h[0], sizeof(double));
-    std::memcpy(&mb, &h[1], sizeof(double));
-    const double m = std::fmax(ma, symmetric ? ma : mb);
+    // the larger |x| bit pattern: a NaN in either operand makes m non-finite
+    const unsigned long long hb = symmetric ? h[0] : std::max(h[0], h[1]);
+    double m;
+    std::memcpy(&m, &hb, sizeof(double));
     if (!std::isfinite(m))
-        return qmlg_laplacian_kernel(A, lda, na, B, ldb, nb, d, sigma, K, ldk, flags, diag_shift,
-                                     stream);
+        return l1_fp64(A, lda, na, B, ldb, nb, d, sigma, gammas, ng, K, ldk, flags, diag_shift,
+                       stream);
     int em = 0;
     if (m > 0.0) std::frexp(m, &em);  // m < 2^em
     int ed = 0;
     std::frexp((double)(2 * (int64_t)(d < 1 ? 1 : d)), &ed);  // 2d <= 2^ed
     const int F = std::min(62 - ed - em, 1000);
     const double bound = std::ldexp((double)d, -F) / sigma;
-    if (bound > 0.5e-12)  // not representable finely enough: the FP64 kernel
-        return qmlg_laplacian_kernel(A, lda, na, B, ldb, nb, d, sigma, K, ldk, flags, diag_shift,
-                                     stream);
+    if (gain * bound > 0.5e-12)  // not representable finely enough: the FP64 kernel
+        return l1_fp64(A, lda, na, B, ldb, nb, d, sigma, gammas, ng, K, ldk, flags, diag_shift,
+                       stream);
     const double scale = std::ldexp(1.0, F), inv_scale = std::ldexp(1.0, -F);
     to_fixed_kernel<<<blocks((int64_t)na * d), 256, 0, s>>>(A, lda, na, d, scale, qa, nullptr);
     if (!symmetric)
         to_fixed_kernel<<<blocks((int64_t)nb * d), 256, 0, s>>>(B, ldb, nb, d, scale, qb, nullptr);
     qmlg::count_launches(symmetric ? 1 : 2);
-    laplace_fixed_kernel<<<grid, NT, 0, s>>>(qa, na, qb, nb, d, inv_scale, -1.0 / sigma, K, ldk,
-                                             symmetric ? 1 : 0, diag_shift, nullptr);
+    if (gammas == nullptr)
+        laplace_fixed_kernel<0><<<grid, NT, 0, s>>>(qa, na, qb, nb, d, inv_scale, -1.0 / sigma, K,
+                                                    ldk, symmetric ? 1 : 0, diag_shift, nullptr,
+                                                    nullptr, 0);
+    else
+        laplace_fixed_kernel<1><<<grid, NT, 0, s>>>(qa, na, qb, nb, d, inv_scale, -1.0 / sigma, K,
+                                                    ldk, symmetric ? 1 : 0, diag_shift, nullptr,
+                                                    gammas, ng);
     qmlg::count_launches(1);
     return qmlg::check_launch();
+}
+
+}  // namespace
+
+extern "C" int qmlg_laplacian_kernel_fixed(const double *A, int64_t lda, int na, const double *B,
+                                           int64_t ldb, int nb, int d, double sigma, double *K,
+                                           int64_t ldk, int flags, double diag_shift,
+                                           void *workspace, size_t ws_bytes, void *stream)
+{
+    return fixed_l1_matrix(A, lda, na, B, ldb, nb, d, sigma, nullptr, 0, 1.0, K, ldk, flags,
+                           diag_shift, workspace, ws_bytes, stream);
+}
+
+extern "C" size_t qmlg_sargan_kernel_fixed_workspace_size(int na, int nb, int d, int flags)
+{
+    return qmlg_laplacian_kernel_fixed_workspace_size(na, nb, d, flags);
+}
+
+// With t = d / sigma, ln K = -t + ln(1 + sum_m gamma_m t^m).  For gamma_m >= 0 the
+// polynomial is >= 1 and its log-derivative is at most ng max(1, sum gamma), so an
+// error in t reaches K relative at most (1 + ng max(1, sum gamma)) times; that factor
+// tightens the grid's bound.  A negative gamma takes the FP64 kernel.
+extern "C" int qmlg_sargan_kernel_fixed(const double *A, int64_t lda, int na, const double *B,
+                                        int64_t ldb, int nb, int d, double sigma,
+                                        const double *gammas, int ng, double *K, int64_t ldk,
+                                        int flags, double diag_shift, void *workspace,
+                                        size_t ws_bytes, void *stream)
+{
+    if (ng < 0 || (ng > 0 && gammas == nullptr)) return QMLG_E_ARG;
+    if (ng == 0)
+        return fixed_l1_matrix(A, lda, na, B, ldb, nb, d, sigma, nullptr, 0, 1.0, K, ldk, flags,
+                               diag_shift, workspace, ws_bytes, stream);
+    std::vector<double> g(ng);
+    cudaStream_t s = qmlg::as_stream(stream);
+    int st = qmlg::read_back(g.data(), gammas, sizeof(double) * ng, s);
+    if (st != QMLG_OK) return st;
+    double sum = 0.0;
+    bool nonneg = true;
+    for (double v : g) {
+        nonneg = nonneg && v >= 0.0 && std::isfinite(v);
+        sum += v;
+    }
+    if (!nonneg)
+        return qmlg_sargan_kernel(A, lda, na, B, ldb, nb, d, sigma, gammas, ng, K, ldk, flags,
+                                  diag_shift, stream);
+    const double gain = 1.0 + ng * std::fmax(1.0, sum);
+    return fixed_l1_matrix(A, lda, na, B, ldb, nb, d, sigma, gammas, ng, gain, K, ldk, flags,
+                           diag_shift, workspace, ws_bytes, stream);
 }
 
 extern "C" size_t qmlg_predict_laplacian_fixed_workspace_size(int ntrain, int ntest, int d)
@@ -871,10 +959,10 @@ extern "C" int qmlg_predict_laplacian_fixed(const double *Xtrain, int64_t ldtrai
     qmlg::count_launches(2);
     unsigned long long h[2] = {0, 0};
     if ((st = qmlg::read_back(h, mx, sizeof(h), s)) != QMLG_OK) return st;
-    double ma, mb;
-    std::memcpy(&ma, &h[0], sizeof(double));
-    std::memcpy(&mb, &h[1], sizeof(double));
-    const double m = std::fmax(ma, mb);
+    // the larger |x| bit pattern: a NaN in either operand makes m non-finite
+    const unsigned long long hb = std::max(h[0], h[1]);
+    double m;
+    std::memcpy(&m, &hb, sizeof(double));
     // the same fixed-point grid and 1e-12 bound as qmlg_laplacian_kernel_fixed
     int F = 0;
     bool fixed = std::isfinite(m);
@@ -949,8 +1037,8 @@ extern "C" int qmlg_laplacian_kernel_fixed_async(const double *A, int64_t lda, i
     to_fixed_kernel<<<blocks((int64_t)na * d), 256, 0, s>>>(A, lda, na, d, 0.0, qa, plan);
     if (!symmetric)
         to_fixed_kernel<<<blocks((int64_t)nb * d), 256, 0, s>>>(B, ldb, nb, d, 0.0, qb, plan);
-    laplace_fixed_kernel<<<grid, NT, 0, s>>>(qa, na, qb, nb, d, 0.0, -1.0 / sigma, K, ldk,
-                                             symmetric ? 1 : 0, diag_shift, plan);
+    laplace_fixed_kernel<0><<<grid, NT, 0, s>>>(qa, na, qb, nb, d, 0.0, -1.0 / sigma, K, ldk,
+                                             symmetric ? 1 : 0, diag_shift, plan, nullptr, 0);
     EpiParams ep;
     ep.s1 = -1.0 / sigma;
     kernel_matrix_kernel<kLaplace><<<grid, NT, 0, s>>>(A, lda, na, B, ldb, nb, d, ep, K, ldk,

@@ -443,3 +443,38 @@ def test_matern_kernel_emulated_falls_back(cuda, cm_features):
         Ke = core.kernel_matrix("matern_l2", X, Y, sigma, order=order, emulated=True)
         Kf = core.kernel_matrix("matern_l2", X, Y, sigma, order=order)
         assert np.array_equal(Ke.cpu().numpy(), Kf.cpu().numpy(), equal_nan=True)
+
+
+@pytest.mark.parametrize("na,nb", [(1, 1), (63, 65), (300, 173)])
+def test_sargan_kernel_fixed(cuda, oracle, cm_features, na, nb):
+    # the Sargan kernel from exact fixed-point L1 sums: within 1e-12 relative per entry
+    # for gammas >= 0, exactly symmetric with a shifted diagonal
+    A, B = cm_features[:na], cm_features[300:300 + nb]
+    At, Bt = torch.from_numpy(A).to(cuda), torch.from_numpy(B).to(cuda)
+    for gam in ([], [0.7], [0.7, 0.2, 0.05]):
+        for sigma in (1000.0, 500.0):
+            K = core.kernel_matrix("sargan", At, Bt, sigma, gammas=gam, emulated=True)
+            assert relerr(K.cpu().numpy(), oracle.sargan_kernel(A, B, sigma, gam)) <= RTOL
+            Ks = core.kernel_matrix("sargan", At, At, sigma, gammas=gam, symmetric=True,
+                                    diag_shift=0.5, emulated=True).cpu().numpy()
+            assert np.array_equal(Ks, Ks.T)
+            Ko = oracle.sargan_kernel(A, A, sigma, gam) + 0.5 * np.eye(na)
+            assert relerr(Ks, Ko) <= RTOL
+
+
+def test_sargan_kernel_fixed_falls_back(cuda, cm_features):
+    # a negative gamma, a sigma too small for the grid's bound and NaN input take the
+    # FP64 kernel: the same bits as emulated=False
+    A = cm_features[:70].copy()
+    At = torch.from_numpy(A).to(cuda)
+    bad = A.copy()
+    bad[4, 7] = np.nan
+    Bt = torch.from_numpy(bad).to(cuda)
+    for Y, sigma, gam in ((At, 1000.0, [0.7, -0.2]), (At, 1e-3, [0.5]), (Bt, 1000.0, [0.5])):
+        Ke = core.kernel_matrix("sargan", At, Y, sigma, gammas=gam, emulated=True).cpu().numpy()
+        Kf = core.kernel_matrix("sargan", At, Y, sigma, gammas=gam).cpu().numpy()
+        assert np.array_equal(Ke, Kf, equal_nan=True)
+    # a NaN in B alone reaches the fixed-point Laplacian's FP64 fallback too
+    Ke = core.kernel_matrix("laplacian", At, Bt, 1000.0, emulated=True).cpu().numpy()
+    Kf = core.kernel_matrix("laplacian", At, Bt, 1000.0).cpu().numpy()
+    assert np.array_equal(Ke, Kf, equal_nan=True)
