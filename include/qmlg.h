@@ -202,8 +202,9 @@ int qmlg_local_kernels(int kind, const double *A, int64_t lda, const int64_t *of
  * chunk's atoms against all of B's, then two reductions sum them per molecule pair.
  * Every term is positive, so each entry keeps the atom-pair kernel's relative bound
  * (1e-12; those calls take their FP64 kernels where the bound cannot be met).
- * Arguments as qmlg_local_kernels.  Reads the offsets and sigmas back to the host
- * first (a synchronisation).  QMLG_E_TOO_LARGE when one molecule holds more atoms
+ * Arguments as qmlg_local_kernels, with both offset arrays starting at 0
+ * (QMLG_E_ARG otherwise).  Reads the offsets and sigmas back to the host first (a
+ * synchronisation).  QMLG_E_TOO_LARGE when one molecule holds more atoms
  * than a chunk's rows.  ws: qmlg_local_kernels_emulated_workspace_size(kind,
  * atoms of A, atoms of B, nm2, d).
  */
