@@ -478,3 +478,15 @@ def test_sargan_kernel_fixed_falls_back(cuda, cm_features):
     Ke = core.kernel_matrix("laplacian", At, Bt, 1000.0, emulated=True).cpu().numpy()
     Kf = core.kernel_matrix("laplacian", At, Bt, 1000.0).cpu().numpy()
     assert np.array_equal(Ke, Kf, equal_nan=True)
+
+
+def test_laplacian_fixed_predict_nan_falls_back(cuda, cm_features):
+    # a NaN in the test rows alone takes the fused FP64 prediction: the same bits
+    Xtr = torch.from_numpy(cm_features[:200].copy()).to(cuda)
+    bad = cm_features[200:260].copy()
+    bad[3, 11] = np.nan
+    Xte = torch.from_numpy(bad).to(cuda)
+    alpha = torch.linspace(-1.0, 1.0, 200, dtype=torch.float64, device=cuda)
+    ye = core.predict("laplacian", Xtr, Xte, 1000.0, alpha, emulated=True).cpu().numpy()
+    yf = core.predict("laplacian", Xtr, Xte, 1000.0, alpha).cpu().numpy()
+    assert np.isnan(ye[3]) and np.array_equal(ye, yf, equal_nan=True)
